@@ -1,0 +1,427 @@
+"""Throughput of the GB300 terrain tile producer (elevation + normal tiles/s).
+
+Workload (one step): a frame of 4096 independent tile requests, levels uniform in
+1..12, 25% of them 197-wide and the rest 101-wide; every request has its own
+materialised fBm parent tile (zf, zm planes), an iid N(0, (2000 * 0.5^l)^2)
+residual tile and per-level noise 300 * 0.55^l m with the DEM noise table.
+Each step produces the elevation (zf, zc, zm) and normal (nx, ny) tiles of all
+requests.  The inputs of one step (about 1.8 GB) exceed the 129 MB L2, so no
+flush is needed between steps.
+
+  value  device-resident throughput: inputs already in HBM, job arrays already
+         on the device, CUDA events around K steps on the launch stream.
+  e2e    the same frame through the C ABI with host buffers: host->device copy
+         of parents and residuals from pinned memory, the batch call (which
+         also uploads its job array), device->host copy of all output tiles.
+
+--impl reference times the reference's CPU path for this hot path (the C
+restatement of CPUElevationProducer::doCreateTile plus the shader's noise, zc,
+zm and normal arithmetic) on all host cores, on a bounded sample per step.
+"""
+import argparse
+import ctypes as C
+import json
+import os
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "proland-4.0_gb300")
+for _p in (ROOT, PKG):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "elev+normal tiles/s (101² and 197²), plain vs learned; max err vs FP64"
+UNIT = "tiles/s"
+ROOT_QUAD = 100000.0          # meters: terrainNode size 50000 -> root quad 2 * size
+BYTES_PER_TILE = {101: 260960, 197: 1000544}   # algorithmic bytes (parent window, residual, elevation, normals)
+FALLBACK_HBM_GBS = 6800.0
+
+
+def hbm_peak():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+# ------------------------------------------------------------------ workload
+class FrameClass:
+    """All requests of one tile width, laid out in slots: outputs [0, n), parents [n, 2n)."""
+
+    def __init__(self, W, levels, tx, ty, seed, n_unique_parents=48):
+        from proland_gb300 import workloads
+        import proland_gb300 as tp
+        self.W, self.n = W, len(levels)
+        self.levels, self.tx, self.ty = levels, tx, ty
+        uz, um = workloads.fbm_parent_tiles(min(n_unique_parents, self.n), W, seed)
+        pick = np.arange(self.n) % uz.shape[0]
+        self.parent_zf = uz[pick]
+        self.parent_zm = um[pick]
+        self.residual = workloads.residual_tiles(levels, W, seed + 1)
+        self.jobs = []
+        for k in range(self.n):
+            l = int(levels[k])
+            rot, layer = tp.noise_select(1, l, int(tx[k]), int(ty[k]))
+            self.jobs.append(tp.make_job(l, int(tx[k]), int(ty[k]), out_slot=k, parent_slot=self.n + k,
+                                         residual_slot=k, normal_slot=k, noise_rot=rot, noise_layer=layer,
+                                         noise_amp=float(workloads.noise_amplitude(l)),
+                                         tile_meters=ROOT_QUAD / (1 << l)))
+
+    def allocate(self, tp):
+        self.elev = tp.TileStorage(self.W, 3, 2 * self.n)
+        self.res = tp.TileStorage(self.W, 1, self.n)
+        self.nrm = tp.TileStorage(self.W - 4, 2, self.n)
+
+    def upload_inputs(self, tp, stream=None):
+        self.elev.upload(self.n, tp.ZF, self.h_parent_zf, stream)
+        self.elev.upload(self.n, tp.ZM, self.h_parent_zm, stream)
+        self.res.upload(0, 0, self.h_residual, stream)
+
+    def download_outputs(self, tp, stream=None):
+        for c, buf in ((tp.ZF, self.h_zf), (tp.ZC, self.h_zc), (tp.ZM, self.h_zm)):
+            self.elev.download(0, self.n, c, buf, stream)
+        self.nrm.download(0, self.n, tp.NX, self.h_nx, stream)
+        self.nrm.download(0, self.n, tp.NY, self.h_ny, stream)
+
+    def pin(self, torch):
+        W, n = self.W, self.n
+
+        def pinned(shape):
+            return torch.empty(shape, dtype=torch.float32, pin_memory=True).numpy()
+        self.h_parent_zf = pinned((n, W, W)); self.h_parent_zf[:] = self.parent_zf
+        self.h_parent_zm = pinned((n, W, W)); self.h_parent_zm[:] = self.parent_zm
+        self.h_residual = pinned((n, W, W)); self.h_residual[:] = self.residual
+        self.h_zf, self.h_zc, self.h_zm = (pinned((n, W, W)) for _ in range(3))
+        self.h_nx, self.h_ny = (pinned((n, W - 4, W - 4)) for _ in range(2))
+        self.h2d_bytes = 3 * n * W * W * 4 + n * C.sizeof(self.jobs[0])
+        self.d2h_bytes = n * (3 * W * W + 2 * (W - 4) ** 2) * 4
+
+
+def make_frame(nreq, seed):
+    from proland_gb300 import workloads
+    levels, tx, ty, wide = workloads.frame_requests(nreq, seed)
+    classes = []
+    for W, sel in ((101, ~wide), (197, wide)):
+        idx = np.nonzero(sel)[0]
+        if len(idx):
+            classes.append(FrameClass(W, levels[idx], tx[idx], ty[idx], seed + W))
+    return classes
+
+
+# ------------------------------------------------------------------ clocks
+class ClockSampler:
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index=0):
+        self.proc = None
+        self.path = None
+        self.dev = device_index
+
+    def start(self):
+        try:
+            os.makedirs(os.path.join(ROOT, "gpurun_out"), exist_ok=True)
+            self.path = os.path.join(ROOT, "gpurun_out", "bench_clocks_%d.csv" % os.getpid())
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.dev), "--query-gpu=" + self.QUERY,
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return None
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.close()
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ------------------------------------------------------------------ CPU path
+def cpu_jobs(classes, limit_per_class, outs_keepalive):
+    """or_job descriptors for the first `limit_per_class` requests of each class."""
+    import oracle
+    jobs = []
+    for fc in classes:
+        W = fc.W
+        table = oracle.dem_noise(W)
+        outs_keepalive.append(table)
+        m = min(limit_per_class[W], fc.n)
+        zf = np.empty((m, W, W), np.float32); zc = np.empty_like(zf); zm = np.empty_like(zf)
+        nx = np.empty((m, W - 4, W - 4), np.float32); ny = np.empty_like(nx)
+        outs_keepalive += [zf, zc, zm, nx, ny]
+        fp = oracle._f32p
+        for k in range(m):
+            j = fc.jobs[k]
+            b = oracle.Job()
+            b.W, b.level, b.tx, b.ty = W, j.level, j.tx, j.ty
+            b.parent_zf = fc.parent_zf[k].ctypes.data_as(fp)
+            b.parent_zm = fc.parent_zm[k].ctypes.data_as(fp)
+            b.parent_pitch = W
+            b.residual = fc.residual[k].ctypes.data_as(fp)
+            b.res_pitch, b.rx, b.ry, b.rscale = W, 0, 0, 1.0
+            b.noise = table[j.noise_layer].ctypes.data_as(fp)
+            b.noise_rot, b.noise_amp = j.noise_rot, j.noise_amp
+            b.tile_meters = j.tile_meters
+            b.out_zf, b.out_zc, b.out_zm = (a[k].ctypes.data_as(fp) for a in (zf, zc, zm))
+            b.out_pitch = W
+            b.out_nx, b.out_ny = nx[k].ctypes.data_as(fp), ny[k].ctypes.data_as(fp)
+            b.nrm_pitch = W - 4
+            jobs.append(b)
+    return jobs
+
+
+def time_cpu(classes, min_seconds=4.0):
+    """Tiles/s of the CPU path on all host threads over a bounded sample."""
+    import oracle
+    from oracle import build as obuild
+    obuild.build()
+    threads = os.cpu_count() or 1
+    keep = []
+    # keep the 101/197 mix of the frame: 3 : 1
+    jobs = cpu_jobs(classes, {101: 12 * threads, 197: 4 * threads}, keep)
+    oracle.run_jobs(jobs[:threads], threads)          # warm-up
+    t0 = time.perf_counter()
+    reps = 0
+    while True:
+        oracle.run_jobs(jobs, threads)
+        reps += 1
+        el = time.perf_counter() - t0
+        if el >= min_seconds:
+            break
+    return {"value": reps * len(jobs) / el, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": "%d tiles (%d x 101, %d x 197) of the frame, %d repetitions, %.1f s" % (
+                len(jobs), sum(1 for j in jobs if j.W == 101), sum(1 for j in jobs if j.W == 197), reps, el)}
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    classes = make_frame(args.requests, args.seed)
+    import oracle
+    from oracle import build as obuild
+    obuild.build()
+    threads = os.cpu_count() or 1
+    keep = []
+    jobs = cpu_jobs(classes, {101: 24 * threads, 197: 8 * threads}, keep)
+    for _ in range(max(args.warmup, 1)):
+        oracle.run_jobs(jobs, threads)
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        oracle.run_jobs(jobs, threads)
+        times.append(time.perf_counter() - t0)
+    total = sum(times)
+    value = args.steps * len(jobs) / total
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * total / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic",
+            "config": {"workload": "frame: %d requests, levels 1-12, 25%% 197-wide; CPU sample of %d tiles per step"
+                       % (args.requests, len(jobs)), "form": "plain"},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": "%d tiles of the frame per step (3:1 101/197 mix)" % len(jobs)},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+# ------------------------------------------------------------------ GPU path
+def fp64_errors(tp, classes):
+    """Max error of a few produced tiles against the FP64 evaluation of the same
+    definition (and of the normals computed from FP64 elevations)."""
+    import oracle
+    out = {"zf_abs": 0.0, "zf_rel": 0.0, "normal_abs": 0.0, "tiles": 0}
+    for fc in classes:
+        table = oracle.dem_noise(fc.W)
+        for k in range(min(4, fc.n)):
+            j = fc.jobs[k]
+            zf = fc.elev.download(k, 1, tp.ZF)[0]
+            nx = fc.nrm.download(k, 1, tp.NX)[0]
+            d_zf, d_zc, d_zm = oracle.elevation_tile(
+                fc.W, j.level, j.tx, j.ty, fc.parent_zf[k], fc.parent_zm[k], fc.residual[k],
+                noise=table[j.noise_layer], noise_rot=j.noise_rot, noise_amp=j.noise_amp, f64=True)
+            dnx, _ = oracle.normals_flat_f64(fc.W, d_zm, j.tile_meters)
+            e = np.abs(zf.astype(np.float64) - d_zf)
+            out["zf_abs"] = max(out["zf_abs"], float(e.max()))
+            out["zf_rel"] = max(out["zf_rel"], float((e / np.maximum(np.abs(d_zf), 1.0)).max()))
+            out["normal_abs"] = max(out["normal_abs"], float(np.abs(nx - dnx).max()))
+            out["tiles"] += 1
+    return out
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=10)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--requests", type=int, default=4096)
+    ap.add_argument("--seed", type=int, default=2024)
+    ap.add_argument("--e2e-steps", type=int, default=5)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+    import proland_gb300 as tp
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    warmup = max(args.warmup, 3)
+
+    classes = make_frame(args.requests, args.seed + rank)
+    stream = torch.cuda.Stream()
+    sh = C.c_void_p(stream.cuda_stream)
+    params = tp.make_params()
+    for fc in classes:
+        fc.allocate(tp)
+        fc.pin(torch)
+        fc.upload_inputs(tp, sh)
+        arr = (tp.TileJob * fc.n)(*fc.jobs)
+        fc.dev_jobs = torch.empty(C.sizeof(arr), dtype=torch.uint8, device="cuda")
+        fc.dev_jobs.copy_(torch.frombuffer(bytearray(bytes(arr)), dtype=torch.uint8))
+    torch.cuda.synchronize()
+
+    def step(events=None):
+        for i, fc in enumerate(classes):
+            if events is not None:
+                events[i][0].record(stream)
+            tp.elevation_batch_device(fc.elev, fc.res, fc.nrm, params, C.c_void_p(fc.dev_jobs.data_ptr()),
+                                      fc.n, sh)
+            if events is not None:
+                events[i][1].record(stream)
+
+    with torch.cuda.stream(stream):
+        for _ in range(warmup):
+            step()
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    clocks = ClockSampler(local)
+    clocks.start()
+    kernel_ev = [[(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+                  for _ in classes] for _ in range(args.steps)]
+    t_start = torch.cuda.Event(enable_timing=True)
+    t_end = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    t_start.record(stream)
+    for s in range(args.steps):
+        step(kernel_ev[s])
+    t_end.record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    ms_total = t_start.elapsed_time(t_end)
+    kernel_ms = [sum(kernel_ev[s][i][0].elapsed_time(kernel_ev[s][i][1]) for s in range(args.steps)) / args.steps
+                 for i in range(len(classes))]
+    if world > 1:
+        t = torch.tensor([ms_total], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_total = float(t.item())
+    ms_step = ms_total / args.steps
+    tiles = sum(fc.n for fc in classes)
+    value = world * tiles / (ms_step / 1000.0)
+
+    # end to end through the C ABI with host buffers
+    e2e_ms = []
+    for s in range(args.e2e_steps + 2):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for fc in classes:
+            fc.upload_inputs(tp, sh)
+            tp.elevation_batch(fc.elev, fc.res, fc.nrm, params, fc.jobs, sh)
+            fc.download_outputs(tp, sh)
+        stream.synchronize()
+        if s >= 2:
+            e2e_ms.append(1000.0 * (time.perf_counter() - t0))
+    e2e_step = float(np.mean(e2e_ms))
+    if world > 1:
+        t = torch.tensor([e2e_step], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_step = float(t.item())
+
+    if rank != 0:
+        dist.barrier()
+        dist.destroy_process_group()
+        return
+
+    peak, peak_src = hbm_peak()
+    alg = {fc.W: fc.n * BYTES_PER_TILE[fc.W] for fc in classes}
+    per_kernel = {}
+    for fc, kms in zip(classes, kernel_ms):
+        gbs = alg[fc.W] / (kms / 1000.0) / 1e9
+        per_kernel["W%d" % fc.W] = {"tiles": fc.n, "ms": kms, "achieved_gbs": gbs, "frac": gbs / peak}
+    tot_kernel_ms = sum(kernel_ms)
+    achieved = sum(alg.values()) / (tot_kernel_ms / 1000.0) / 1e9
+    traffic = None
+    prof = os.path.join(ROOT, "profiles", "elevation_kernel_traffic.json")
+    if os.path.exists(prof):
+        try:
+            traffic = json.load(open(prof)).get("bytes_per_step")
+        except Exception:
+            traffic = None
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "frame: %d independent requests per GPU, levels 1-12, %d x 101 + %d x 197 tiles, "
+                               "materialised fBm parents, residual sigma 2000*0.5^l, noise 300*0.55^l"
+                               % (tiles, sum(fc.n for fc in classes if fc.W == 101),
+                                  sum(fc.n for fc in classes if fc.W == 197)),
+                   "form": "plain", "l2": "inputs larger than L2 (%.2f GB per step)" % (sum(alg.values()) / 1e9),
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": traffic, "peak_source": peak_src, "per_kernel": per_kernel,
+                     "algorithmic_bytes_per_step": sum(alg.values())},
+        "e2e": {"value": world * tiles / (e2e_step / 1000.0), "unit": UNIT, "ms_per_step": e2e_step,
+                "h2d_bytes_per_step": sum(fc.h2d_bytes for fc in classes),
+                "d2h_bytes_per_step": sum(fc.d2h_bytes for fc in classes)},
+        "gpu_launches": args.steps * len(classes),
+        "clocks": clk,
+        "max_err_vs_fp64": fp64_errors(tp, classes),
+    }
+    if not args.no_cpu:
+        line["cpu_baseline"] = time_cpu(classes)
+    print(json.dumps(line))
+    if world > 1:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

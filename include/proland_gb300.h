@@ -1,0 +1,126 @@
+/*
+ * proland_gb300 -- GB300-native terrain tile production (elevation upsample +
+ * residual + noise + normals) behind Proland's TileStorage / TileCache /
+ * TileProducer protocol.
+ *
+ * C ABI only: plain pointers, ints and floats; cudaStream_t is passed as void*.
+ * Every function returns TP_OK (0) or a negative TP_E_* code and never aborts;
+ * tp_last_error() gives a message for the last failure on the calling thread.
+ *
+ * Reference interfaces each entry point replaces are cited as file:line,
+ * relative to the Proland 4.0 source root (src/...).
+ *
+ * Tile layout.  A tile of width W (W = n + 5 for elevation/residual tiles with a
+ * 2-sample border, n + 1 for normal tiles) is stored as `channels` planes of W
+ * rows x `pitch` floats (pitch = W rounded up to 8), row-major, x fastest, row 0
+ * the bottom (GL) row.  A slot is channels * W * pitch floats; the slots of a
+ * storage are one contiguous device allocation.  Elevation slots have three
+ * planes (zf, zc, zm) -- the reference's RGB32F texel split into planes;
+ * normal slots (format 2) have two (nx, ny).
+ */
+#ifndef PROLAND_GB300_H
+#define PROLAND_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define TP_OK 0
+#define TP_E_BAD_ARG (-1)        /* invalid argument, size or state */
+#define TP_E_CACHE_FULL (-2)     /* no free and no evictable slot (TileCache.cpp:198-199) */
+#define TP_E_MISSING_PARENT (-3) /* a child tile's parent is neither resident nor in the batch */
+#define TP_E_TIMEOUT (-4)        /* a device-side dependency wait gave up; status word set */
+#define TP_E_CUDA (-5)           /* a CUDA runtime call failed */
+#define TP_E_IO (-6)             /* residual file missing, truncated or corrupt */
+#define TP_E_NO_DEVICE (-7)      /* no CUDA device (the library has no CPU fallback) */
+
+const char *tp_last_error(void);
+/* Library version, and whether the CUDA kernels can run here (1) or not (0). */
+int tp_version(void);
+int tp_device_available(void);
+
+/* ------------------------------------------------------------------------
+ * Storage: a pool of equally sized tile slots.
+ * Replaces TileStorage (core/.../producer/TileStorage.h:140-182),
+ * GPUTileStorage::init (core/.../producer/GPUTileStorage.cpp:151-205) and
+ * CPUTileStorage<float> (core/.../producer/CPUTileStorage.h:43-151).
+ * on_device = 1 allocates device memory, 0 pinned host memory. */
+typedef struct tp_storage tp_storage;
+int tp_storage_create(int tile_width, int channels, int capacity, int on_device, tp_storage **out);
+int tp_storage_destroy(tp_storage *s);
+int tp_storage_tile_size(const tp_storage *s);   /* getTileSize */
+int tp_storage_capacity(const tp_storage *s);    /* getCapacity */
+int tp_storage_free_slots(const tp_storage *s);  /* getFreeSlots */
+int tp_storage_channels(const tp_storage *s);
+int tp_storage_pitch(const tp_storage *s);       /* floats per row */
+/* newSlot / deleteSlot (TileStorage.cpp:90-100): slot index or -1 when full */
+int tp_storage_new_slot(tp_storage *s);
+int tp_storage_delete_slot(tp_storage *s, int slot);
+/* Address of plane `channel` of `slot` (device or pinned host memory). */
+float *tp_storage_plane(tp_storage *s, int slot, int channel);
+/* Copies `count` consecutive slots' plane `channel` from/to a dense host array
+ * [count][W][W] (pitch W), asynchronously on `stream`; host memory should be
+ * pinned for the copy to overlap. */
+int tp_storage_upload(tp_storage *s, int first_slot, int count, int channel,
+                      const float *host, void *stream);
+int tp_storage_download(tp_storage *s, int first_slot, int count, int channel,
+                        float *host, void *stream);
+
+/* ------------------------------------------------------------------------
+ * Kernel-level batch: produce elevation (+ normal) tiles whose inputs are
+ * named by slot.  This is what ElevationProducer::doCreateTile
+ * (terrain/.../dem/ElevationProducer.cpp:280-405) plus
+ * NormalProducer::doCreateTile (terrain/.../dem/NormalProducer.cpp:164-289)
+ * compute for one tile, for a whole frame of tiles in one launch. */
+typedef struct {
+    int32_t level, tx, ty;
+    int32_t out_slot;       /* elevation slot written */
+    int32_t parent_slot;    /* elevation slot of (level-1, tx/2, ty/2); -1 at level 0 */
+    int32_t residual_slot;  /* residual slot, -1 when ResidualProducer::hasTile is false */
+    int32_t rx, ry;         /* residual window: (tx % mod) * n, (ty % mod) * n */
+    int32_t normal_slot;    /* normal slot written, -1: elevation only */
+    int32_t noise_rot;      /* 0..3, from the tile's edge noise signs */
+    int32_t noise_layer;    /* 0..5 */
+    float noise_amp;        /* noiseAmp[level] (0 when level >= size) */
+    float rscale;           /* residual value scale (residualOSH.w) */
+    float tile_meters;      /* rootQuadSize / 2^level */
+    int32_t parent_job;     /* index of the job in this batch writing the parent, -1 if resident */
+    int32_t reserved;
+} tp_tile_job;
+
+/* Per-producer constants of a batch (one tile width). */
+typedef struct {
+    int32_t grid_size;      /* gridMeshSize (default 24): zc uses g = n / grid_size */
+    int32_t flip;           /* flipDiagonals */
+    int32_t no_clamp;       /* NO_CLAMP: zm = zf instead of max(zf, 0) */
+    int32_t noise_mode;     /* 0: zf += |amp| N (terrain1 shader); 1: slope/curvature modulated (demo shader) */
+    int32_t normal_format;  /* 2: two signed fp32 planes (the only one supported by the batch kernel) */
+    int32_t reserved[3];
+} tp_elev_params;
+
+/* Produces n jobs on `stream`.  `jobs` is host memory; it is copied into a
+ * device buffer owned by the storage `elev`.  All jobs must be independent
+ * (parent_job == -1) unless ordered_waves != 0, in which case the batch is run
+ * in dependency waves.  `residuals`/`normals` may be NULL when unused. */
+int tp_elevation_batch(tp_storage *elev, tp_storage *residuals, tp_storage *normals,
+                       const tp_elev_params *params, const tp_tile_job *jobs, int n,
+                       void *stream);
+/* Same with the job array already in device memory (no host->device copy). */
+int tp_elevation_batch_device(tp_storage *elev, tp_storage *residuals, tp_storage *normals,
+                              const tp_elev_params *params, const tp_tile_job *jobs_dev, int n,
+                              void *stream);
+
+/* ------------------------------------------------------------------------
+ * Noise helpers (host).  createDemNoise (ElevationProducer.cpp:50-133) and the
+ * per-tile layer choice (ElevationProducer.cpp:345-376). */
+int tp_dem_noise(int tile_width, float *out /* 6 * W * W, fp16-rounded */);
+float tp_cnoise(float x, float y);               /* noise.cpp:118-165, period 0 */
+int tp_noise_select(int face, int level, int tx, int ty, int *rot, int *layer);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,291 @@
+"""CPU oracle for the terrain tile-production path -- TEST INFRASTRUCTURE ONLY.
+
+ctypes bindings over oracle/_build/liboracle.so (the C restatement in
+oracle.c) plus a pure-Python reader of the reference's ``.dat`` residual
+pyramids.  Only tests/, ``__graft_entry__.smoke()`` and bench.py's CPU-baseline
+leg use this package, always as the checker; the product does not import it.
+"""
+import ctypes as C
+import os
+import struct
+import zlib
+
+import numpy as np
+
+from . import build as _build
+
+_LIB = None
+_f32p = C.POINTER(C.c_float)
+_f64p = C.POINTER(C.c_double)
+
+
+class ElevTile(C.Structure):
+    _fields_ = [
+        ("W", C.c_int), ("level", C.c_int), ("tx", C.c_int), ("ty", C.c_int),
+        ("parent_zf", _f32p), ("parent_zm", _f32p), ("parent_pitch", C.c_int),
+        ("residual", _f32p), ("res_pitch", C.c_int), ("rx", C.c_int), ("ry", C.c_int),
+        ("rscale", C.c_float),
+        ("noise", _f32p), ("noise_rot", C.c_int), ("noise_amp", C.c_float),
+        ("noise_mode", C.c_int), ("meters_per_sample", C.c_float),
+        ("grid_g", C.c_int), ("flip", C.c_int), ("no_clamp", C.c_int),
+        ("out_zf", _f32p), ("out_zc", _f32p), ("out_zm", _f32p), ("out_pitch", C.c_int),
+    ]
+
+
+class SphereFrame(C.Structure):
+    _fields_ = [("C", C.c_float * 16), ("N", C.c_float * 16), ("L", C.c_float * 4),
+                ("W2T", C.c_float * 9), ("R", C.c_float), ("size", C.c_float)]
+
+
+class Job(C.Structure):
+    _fields_ = [
+        ("W", C.c_int), ("level", C.c_int), ("tx", C.c_int), ("ty", C.c_int),
+        ("parent_zf", _f32p), ("parent_zm", _f32p), ("parent_pitch", C.c_int),
+        ("residual", _f32p), ("res_pitch", C.c_int), ("rx", C.c_int), ("ry", C.c_int),
+        ("rscale", C.c_float),
+        ("noise", _f32p), ("noise_rot", C.c_int), ("noise_amp", C.c_float),
+        ("tile_meters", C.c_float),
+        ("out_zf", _f32p), ("out_zc", _f32p), ("out_zm", _f32p), ("out_pitch", C.c_int),
+        ("out_nx", _f32p), ("out_ny", _f32p), ("nrm_pitch", C.c_int),
+    ]
+
+
+def lib():
+    global _LIB
+    if _LIB is None:
+        path = _build.LIB
+        if not os.path.exists(path):
+            path = _build.build()
+        L = C.CDLL(path)
+        L.or_lrandom.argtypes = [C.POINTER(C.c_long)]
+        L.or_lrandom.restype = C.c_long
+        L.or_frandom.argtypes = [C.POINTER(C.c_long)]
+        L.or_frandom.restype = C.c_float
+        L.or_half_round.argtypes = [C.c_float]
+        L.or_half_round.restype = C.c_float
+        L.or_dem_noise.argtypes = [C.c_int, _f32p]
+        L.or_cnoise2.argtypes = [C.c_float, C.c_float]
+        L.or_cnoise2.restype = C.c_float
+        L.or_noise_select.argtypes = [C.c_int] * 4 + [C.POINTER(C.c_int)] * 2
+        L.or_elevation_tile.argtypes = [C.POINTER(ElevTile)]
+        L.or_elevation_tile_f64.argtypes = [C.POINTER(ElevTile), _f64p, _f64p, _f64p]
+        L.or_cpu_elevation_tile.argtypes = [C.c_int] * 4 + [_f32p, C.c_int, _f32p, C.c_int,
+                                                            C.c_int, C.c_int, _f32p, C.c_int]
+        L.or_normals_flat.argtypes = [C.c_int, _f32p, C.c_int, C.c_float, C.c_int, _f32p, _f32p, C.c_int]
+        L.or_normals_flat_f64.argtypes = [C.c_int, _f64p, C.c_int, C.c_double, _f64p, _f64p, C.c_int]
+        L.or_sphere_frame_make.argtypes = [C.c_double, C.c_int, C.c_int, C.c_int, C.POINTER(SphereFrame)]
+        L.or_normals_sphere.argtypes = [C.c_int, _f32p, C.c_int, C.POINTER(SphereFrame), _f32p, _f32p, C.c_int]
+        L.or_run_jobs.argtypes = [C.POINTER(Job), C.c_int, C.c_int]
+        L.or_compute_residual.argtypes = [C.c_int, C.c_int, C.c_int, _f32p, _f32p, _f32p,
+                                          C.POINTER(C.c_int16), _f32p]
+        _LIB = L
+    return _LIB
+
+
+def _p(a, t=_f32p):
+    return None if a is None else a.ctypes.data_as(t)
+
+
+def _f32(a):
+    return None if a is None else np.ascontiguousarray(a, dtype=np.float32)
+
+
+# ---------------------------------------------------------------- noise
+def lrandom_seq(seed, n):
+    s = C.c_long(seed)
+    return [lib().or_lrandom(C.byref(s)) for _ in range(n)]
+
+
+def half_round(x):
+    return lib().or_half_round(float(x))
+
+
+def dem_noise(W):
+    out = np.empty((6, W, W), np.float32)
+    lib().or_dem_noise(W, _p(out))
+    return out
+
+
+def cnoise(x, y):
+    return lib().or_cnoise2(float(x), float(y))
+
+
+def noise_select(face, level, tx, ty):
+    r, l = C.c_int(), C.c_int()
+    lib().or_noise_select(face, level, tx, ty, C.byref(r), C.byref(l))
+    return r.value, l.value
+
+
+# ---------------------------------------------------------------- elevation
+def _elev_struct(W, level, tx, ty, parent_zf, parent_zm, residual, rx, ry, rscale,
+                 noise, noise_rot, noise_amp, noise_mode, meters_per_sample,
+                 grid_g, flip, no_clamp, outs):
+    t = ElevTile()
+    t.W, t.level, t.tx, t.ty = W, level, tx, ty
+    if level > 0:
+        t.parent_zf, t.parent_zm = _p(parent_zf), _p(parent_zm)
+        t.parent_pitch = parent_zf.shape[1]
+    t.residual = _p(residual)
+    t.res_pitch = 0 if residual is None else residual.shape[1]
+    t.rx, t.ry, t.rscale = rx, ry, rscale
+    t.noise = _p(noise)
+    t.noise_rot, t.noise_amp, t.noise_mode = noise_rot, noise_amp, noise_mode
+    t.meters_per_sample = meters_per_sample
+    t.grid_g = grid_g if grid_g else (W - 5) // 24
+    t.flip, t.no_clamp = int(flip), int(no_clamp)
+    t.out_zf, t.out_zc, t.out_zm = [_p(o) for o in outs]
+    t.out_pitch = W
+    return t
+
+
+def elevation_tile(W, level, tx, ty, parent_zf=None, parent_zm=None, residual=None,
+                   rx=0, ry=0, rscale=1.0, noise=None, noise_rot=0, noise_amp=0.0,
+                   noise_mode=0, meters_per_sample=1.0, grid_g=0, flip=False,
+                   no_clamp=False, f64=False):
+    """One elevation tile; returns (zf, zc, zm) W x W arrays (float32, or float64 if f64)."""
+    parent_zf, parent_zm, residual, noise = map(_f32, (parent_zf, parent_zm, residual, noise))
+    if level > 0 and parent_zm is None:
+        parent_zm = np.maximum(parent_zf, 0).astype(np.float32)
+    outs32 = [np.empty((W, W), np.float32) for _ in range(3)]
+    t = _elev_struct(W, level, tx, ty, parent_zf, parent_zm, residual, rx, ry, rscale,
+                     noise, noise_rot, noise_amp, noise_mode, meters_per_sample,
+                     grid_g, flip, no_clamp, outs32)
+    if f64:
+        o = [np.empty((W, W), np.float64) for _ in range(3)]
+        lib().or_elevation_tile_f64(C.byref(t), _p(o[0], _f64p), _p(o[1], _f64p), _p(o[2], _f64p))
+        return tuple(o)
+    lib().or_elevation_tile(C.byref(t))
+    return tuple(outs32)
+
+
+def cpu_elevation_tile(W, level, tx, ty, parent=None, residual=None, rx=0, ry=0):
+    parent, residual = _f32(parent), _f32(residual)
+    out = np.empty((W, W), np.float32)
+    lib().or_cpu_elevation_tile(W, level, tx, ty, _p(parent), 0 if parent is None else parent.shape[1],
+                                _p(residual), 0 if residual is None else residual.shape[1], rx, ry,
+                                _p(out), W)
+    return out
+
+
+def normals_flat(W, zm, tile_meters, fmt=2):
+    zm = _f32(zm)
+    n1 = W - 4
+    nx = np.empty((n1, n1), np.float32)
+    ny = np.empty((n1, n1), np.float32)
+    lib().or_normals_flat(W, _p(zm), zm.shape[1], float(tile_meters), fmt, _p(nx), _p(ny), n1)
+    return nx, ny
+
+
+def normals_flat_f64(W, zm, tile_meters):
+    zm = np.ascontiguousarray(zm, np.float64)
+    n1 = W - 4
+    nx = np.empty((n1, n1), np.float64)
+    ny = np.empty((n1, n1), np.float64)
+    lib().or_normals_flat_f64(W, _p(zm, _f64p), zm.shape[1], float(tile_meters),
+                              _p(nx, _f64p), _p(ny, _f64p), n1)
+    return nx, ny
+
+
+def sphere_frame(root_quad_size, level, tx, ty):
+    f = SphereFrame()
+    lib().or_sphere_frame_make(float(root_quad_size), level, tx, ty, C.byref(f))
+    return f
+
+
+def normals_sphere(W, zm, frame):
+    zm = _f32(zm)
+    n1 = W - 4
+    nx = np.empty((n1, n1), np.float32)
+    ny = np.empty((n1, n1), np.float32)
+    lib().or_normals_sphere(W, _p(zm), zm.shape[1], C.byref(frame), _p(nx), _p(ny), n1)
+    return nx, ny
+
+
+def compute_residual(W, tx, ty, parent_approx, fine):
+    parent_approx, fine = _f32(parent_approx), _f32(fine)
+    rq = np.empty((W, W), np.float32)
+    enc = np.empty((W, W), np.int16)
+    approx = np.empty((W, W), np.float32)
+    lib().or_compute_residual(W, tx, ty, _p(parent_approx), _p(fine), _p(rq),
+                              enc.ctypes.data_as(C.POINTER(C.c_int16)), _p(approx))
+    return rq, enc, approx
+
+
+def run_jobs(jobs, nthreads):
+    arr = (Job * len(jobs))(*jobs)
+    lib().or_run_jobs(arr, len(jobs), int(nthreads))
+
+
+# ---------------------------------------------------------------- .dat pyramid
+class DatFile:
+    """Reader of ResidualProducer's .dat pyramid (ResidualProducer.cpp:93-107,
+    253-340): a 7-word header {minLevel, maxLevel, tileSize, rootLevel, rootTx,
+    rootTy: int32, scale: float32}, then 2 * ntiles uint32 [start, end) offsets
+    relative to the end of the header, then one single-strip deflate TIFF per tile.
+    Pure Python (struct + zlib), independent of the product's C++ reader."""
+
+    def __init__(self, data: bytes):
+        self.data = data
+        (self.min_level, self.max_level, self.tile_size, self.root_level,
+         self.root_tx, self.root_ty) = struct.unpack_from("<6i", data, 0)
+        (self.scale,) = struct.unpack_from("<f", data, 24)
+        l = max(self.max_level - self.min_level, 0)
+        self.ntiles = self.min_level + ((1 << (l * 2 + 2)) - 1) // 3
+        self.header = 4 + 4 * (6 + self.ntiles * 2)
+        self.offsets = np.frombuffer(data, "<u4", self.ntiles * 2, 28)
+
+    @classmethod
+    def open(cls, path):
+        with open(path, "rb") as f:
+            return cls(f.read())
+
+    def tile_width(self, level):
+        ts = self.tile_size >> (self.min_level - level) if level < self.min_level else self.tile_size
+        return ts + 5
+
+    def tile_id(self, level, tx, ty):
+        if level < self.min_level:
+            return level
+        l = level - self.min_level
+        return self.min_level + tx + ty * (1 << l) + ((1 << (2 * l)) - 1) // 3
+
+    def strip(self, level, tx, ty):
+        tid = self.tile_id(level, tx, ty)
+        a, b = int(self.offsets[2 * tid]), int(self.offsets[2 * tid + 1])
+        return self.data[self.header + a:self.header + b]
+
+    def tile_int16(self, level, tx, ty):
+        """Decoded int16 samples of one tile, shape (w, w)."""
+        w = self.tile_width(level)
+        raw = decode_tiff_strip(self.strip(level, tx, ty))
+        return np.frombuffer(raw[:2 * w * w], "<i2").reshape(w, w)
+
+
+def decode_tiff_strip(blob: bytes) -> bytes:
+    """Decodes strip 0 of a little- or big-endian TIFF with deflate (8 or 32946)
+    or no compression; returns the raw strip bytes."""
+    bo = "<" if blob[:2] == b"II" else ">"
+    (ifd,) = struct.unpack_from(bo + "I", blob, 4)
+    (count,) = struct.unpack_from(bo + "H", blob, ifd)
+    tags = {}
+    sizes = {1: 1, 2: 1, 3: 2, 4: 4, 5: 8}
+    for k in range(count):
+        tag, typ, n, val = struct.unpack_from(bo + "HHI4s", blob, ifd + 2 + 12 * k)
+        fmt = {3: "H", 4: "I"}.get(typ)
+        if fmt is None:
+            continue
+        if sizes[typ] * n <= 4:
+            vals = struct.unpack_from(bo + fmt * n, val, 0)
+        else:
+            (off,) = struct.unpack_from(bo + "I", val, 0)
+            vals = struct.unpack_from(bo + fmt * n, blob, off)
+        tags[tag] = vals
+    comp = tags.get(259, (1,))[0]
+    off = tags[273][0]
+    cnt = tags[279][0]
+    data = blob[off:off + cnt]
+    if comp in (8, 32946):
+        return zlib.decompress(data)
+    if comp == 1:
+        return data
+    raise ValueError("unsupported TIFF compression %d" % comp)

@@ -1,0 +1,33 @@
+"""Builds the CPU oracle (test infrastructure) into oracle/_build/liboracle.so.
+
+The oracle is compiled with -ffp-contract=off so that each float operation is
+rounded on its own, in the order the C source writes it; the CUDA product
+follows the same order with explicitly rounded intrinsics.  No -march flag: the
+same source must give the same bits on x86-64 and aarch64 hosts.
+"""
+import os
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+OUT_DIR = os.path.join(HERE, "_build")
+LIB = os.path.join(OUT_DIR, "liboracle.so")
+
+
+def build(force: bool = False) -> str:
+    src = os.path.join(HERE, "oracle.c")
+    hdr = os.path.join(HERE, "oracle.h")
+    if (not force and os.path.exists(LIB)
+            and os.path.getmtime(LIB) >= max(os.path.getmtime(src), os.path.getmtime(hdr))):
+        return LIB
+    os.makedirs(OUT_DIR, exist_ok=True)
+    tmp = LIB + ".tmp%d" % os.getpid()
+    cmd = ["gcc", "-O2", "-std=c11", "-D_GNU_SOURCE", "-ffp-contract=off", "-fno-fast-math",
+           "-fPIC", "-shared", "-pthread", "-Wall", "-o", tmp, src, "-lm"]
+    subprocess.check_call(cmd)
+    os.replace(tmp, LIB)
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(force="--force" in sys.argv))

@@ -1,0 +1,119 @@
+/*
+ * CPU oracle for the terrain tile-production path -- TEST INFRASTRUCTURE ONLY.
+ *
+ * This is a plain-C restatement of the arithmetic of Proland 4.0's elevation,
+ * residual and normal producers.  It is the checker the CUDA product is compared
+ * against; the product never links, loads or calls it.  Only the test-suite,
+ * the smoke check and the CPU-baseline leg of the benchmark use it.
+ *
+ * Each function cites the reference file:line it follows (paths relative to the
+ * reference project root).  Compile with -ffp-contract=off so that every float
+ * operation is rounded on its own, exactly as written: the CUDA kernels follow
+ * the same operation order with explicitly rounded intrinsics, which makes the
+ * elevation outputs bit-identical on both sides.
+ *
+ * Parity pins: the stencil, residual addressing, int16 residual decode and tile
+ * ids are pinned by the reference's DEM.dat fixtures and by mathematical known
+ * answers (tests/test_oracle_*.py).  Noise-layer selection, zc/flip and normals
+ * have no reference fixture: for those the oracle is a restatement only.
+ */
+#ifndef PROLAND_ORACLE_H
+#define PROLAND_ORACLE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- LCG, noise table, Perlin noise sign (math/noise.h:50-68, noise.cpp:68-165) ---- */
+long  or_lrandom(long *seed);
+float or_frandom(long *seed);
+float or_half_round(float x);                 /* float -> IEEE half (RNE) -> float */
+void  or_dem_noise(int W, float *out);        /* 6*W*W fp16-rounded values (ElevationProducer.cpp:50-133) */
+float or_cnoise2(float x, float y);           /* noise.cpp:118-165 with period 0 */
+void  or_noise_select(int face, int level, int tx, int ty, int *rot, int *layer); /* ElevationProducer.cpp:347-374 */
+
+/* ---- per-tile parameters of one elevation tile ---- */
+typedef struct {
+    int W;               /* tile width incl. 2-sample borders on each side: n + 5 */
+    int level;           /* 0: no parent */
+    int tx, ty;          /* quadtree coordinates */
+    const float *parent_zf;  /* parent zf plane (W x W, pitch parent_pitch); unused at level 0 */
+    const float *parent_zm;  /* parent zm plane */
+    int parent_pitch;
+    const float *residual;   /* residual tile (Wr x Wr, pitch res_pitch) or NULL */
+    int res_pitch;
+    int rx, ry;              /* residual sub-window origin: (tx % mod) * n, (ty % mod) * n */
+    float rscale;            /* residualOSH.w */
+    const float *noise;      /* one noise layer (W x W, fp16-rounded) or NULL */
+    int noise_rot;           /* 0..3 */
+    float noise_amp;         /* noiseAmp[level] */
+    int noise_mode;          /* 0: |amp| N (terrain1 shader), 1: slope/curvature modulated (demo shader) */
+    float meters_per_sample; /* tileWSDF.y, demo noise mode only */
+    int grid_g;              /* tileWSDF.z = n / gridSize */
+    int flip;                /* tileWSDF.w */
+    int no_clamp;            /* NO_CLAMP: zm = zf */
+    float *out_zf, *out_zc, *out_zm;
+    int out_pitch;
+} or_elev_tile;
+
+/* Full elevation tile (zf, zc, zm): upsampleShader.glsl main() semantics with the
+ * stencil evaluated in CPUElevationProducer.cpp:202-245 order. */
+void or_elevation_tile(const or_elev_tile *t);
+/* FP64 evaluation of the same definition (outputs as double, pitch out_pitch). */
+void or_elevation_tile_f64(const or_elev_tile *t, double *zf, double *zc, double *zm);
+/* CPUElevationProducer::doCreateTile (CPUElevationProducer.cpp:156-248): zf = z + r only. */
+void or_cpu_elevation_tile(int W, int level, int tx, int ty,
+                           const float *parent, int parent_pitch,
+                           const float *residual, int res_pitch, int rx, int ry,
+                           float *out, int out_pitch);
+
+/* ---- normals ---- */
+/* Flat normals, (W-4)^2 samples from the zm plane (terrain1/normalShader.glsl:52-74,
+ * NormalProducer.cpp:274-283).  tile_meters = rootQuadSize / 2^level.
+ * format 2: two signed fp32 planes; format 3: RG8 unsigned (values written as floats 0..255). */
+void or_normals_flat(int W, const float *zm, int zm_pitch, float tile_meters,
+                     int format, float *nx, float *ny, int out_pitch);
+void or_normals_flat_f64(int W, const double *zm, int zm_pitch, double tile_meters,
+                         double *nx, double *ny, int out_pitch);
+
+/* Spherical-deformation frames of one tile (NormalProducer.cpp:215-273), FP64 on the
+ * host and cast to float as the reference uploads them.  Layout of the 44 floats:
+ * C[16] (row-major 4x4), N[16] (row-major), L[4], W2T[9] (row-major 3x3), R, tileMeters... */
+typedef struct {
+    float C[16];
+    float N[16];
+    float L[4];
+    float W2T[9];
+    float R;          /* deform.w */
+    float size;       /* deform.z = D / 2^level */
+} or_sphere_frame;
+void or_sphere_frame_make(double rootQuadSize, int level, int tx, int ty, or_sphere_frame *f);
+/* Sphere normals (terrain2/normalShader.glsl:56-89). */
+void or_normals_sphere(int W, const float *zm, int zm_pitch, const or_sphere_frame *f,
+                       float *nx, float *ny, int out_pitch);
+
+/* ---- batch helpers for the timed CPU baseline ---- */
+typedef struct {
+    int W, level, tx, ty;
+    const float *parent_zf, *parent_zm; int parent_pitch;
+    const float *residual; int res_pitch; int rx, ry; float rscale;
+    const float *noise; int noise_rot; float noise_amp;
+    float tile_meters;
+    float *out_zf, *out_zc, *out_zm; int out_pitch;
+    float *out_nx, *out_ny; int nrm_pitch;
+} or_job;
+/* Elevation + flat normals for n jobs on nthreads host threads (grid g = n/24). */
+void or_run_jobs(const or_job *jobs, int n, int nthreads);
+
+/* ---- preprocess (HeightMipmap.cpp:449-559) ---- */
+/* residual = fine - upsample(parentApprox); encoded = short(roundf(residual));
+ * approx = upsample + encoded.  Tile is W x W with pitch W. */
+void or_compute_residual(int W, int tx, int ty, const float *parent_approx,
+                         const float *fine, float *residual_q, int16_t *encoded, float *approx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

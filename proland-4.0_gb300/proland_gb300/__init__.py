@@ -1,0 +1,129 @@
+"""proland_gb300: Python view of the GB300 terrain tile producer.
+
+Thin wrappers over the C ABI (include/proland_gb300.h) that mirror Proland's
+TileStorage / TileCache / TileProducer classes; every computation runs in the
+CUDA library, which must be built (there is no CPU fallback).
+"""
+import ctypes as C
+
+import numpy as np
+
+from ._lib import (ElevParams, TileJob, TPError, check, lib, LIB_PATH,  # noqa: F401
+                   TP_OK, TP_E_BAD_ARG, TP_E_CACHE_FULL, TP_E_MISSING_PARENT,
+                   TP_E_TIMEOUT, TP_E_CUDA, TP_E_IO, TP_E_NO_DEVICE)
+
+ZF, ZC, ZM = 0, 1, 2      # planes of an elevation slot (the reference's RGB32F texel)
+NX, NY = 0, 1             # planes of a normal slot (format 2)
+
+
+def device_available():
+    return bool(lib().tp_device_available())
+
+
+class TileStorage:
+    """A pool of tile slots (GPUTileStorage / CPUTileStorage,
+    core/.../producer/TileStorage.h:140-182)."""
+
+    def __init__(self, tile_size, channels, capacity, on_device=True):
+        h = C.c_void_p()
+        check(lib().tp_storage_create(tile_size, channels, capacity, int(on_device), C.byref(h)))
+        self.handle = h
+        self.tile_size = tile_size
+        self.channels = channels
+        self.capacity = capacity
+        self.pitch = lib().tp_storage_pitch(h)
+
+    def close(self):
+        if self.handle:
+            lib().tp_storage_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def get_tile_size(self):
+        return lib().tp_storage_tile_size(self.handle)
+
+    def get_capacity(self):
+        return lib().tp_storage_capacity(self.handle)
+
+    def get_free_slots(self):
+        return lib().tp_storage_free_slots(self.handle)
+
+    def new_slot(self):
+        return lib().tp_storage_new_slot(self.handle)
+
+    def delete_slot(self, slot):
+        check(lib().tp_storage_delete_slot(self.handle, slot))
+
+    def plane_ptr(self, slot, channel):
+        return lib().tp_storage_plane(self.handle, slot, channel)
+
+    def upload(self, first_slot, channel, host, stream=None):
+        """host: float32 array [count, W, W] (pinned memory for asynchronous copies)."""
+        a = np.ascontiguousarray(host, dtype=np.float32)
+        W = self.tile_size
+        a = a.reshape(-1, W, W)
+        check(lib().tp_storage_upload(self.handle, first_slot, a.shape[0], channel,
+                                      a.ctypes.data, stream))
+        return a
+
+    def download(self, first_slot, count, channel, out=None, stream=None):
+        W = self.tile_size
+        if out is None:
+            out = np.empty((count, W, W), np.float32)
+        check(lib().tp_storage_download(self.handle, first_slot, count, channel,
+                                        out.ctypes.data, stream))
+        return out
+
+
+def make_params(grid_size=24, flip=False, no_clamp=False, noise_mode=0, normal_format=2):
+    p = ElevParams()
+    p.grid_size, p.flip, p.no_clamp = grid_size, int(flip), int(no_clamp)
+    p.noise_mode, p.normal_format = noise_mode, normal_format
+    return p
+
+
+def make_job(level, tx, ty, out_slot, parent_slot=-1, residual_slot=-1, rx=0, ry=0,
+             normal_slot=-1, noise_rot=0, noise_layer=0, noise_amp=0.0, rscale=1.0,
+             tile_meters=1000.0, parent_job=-1):
+    j = TileJob()
+    j.level, j.tx, j.ty = level, tx, ty
+    j.out_slot, j.parent_slot, j.residual_slot = out_slot, parent_slot, residual_slot
+    j.rx, j.ry, j.normal_slot = rx, ry, normal_slot
+    j.noise_rot, j.noise_layer, j.noise_amp = noise_rot, noise_layer, noise_amp
+    j.rscale, j.tile_meters, j.parent_job = rscale, tile_meters, parent_job
+    return j
+
+
+def elevation_batch(elev, residuals, normals, params, jobs, stream=None):
+    """Produces the jobs (a list of TileJob) in one batch (tp_elevation_batch)."""
+    arr = (TileJob * len(jobs))(*jobs)
+    check(lib().tp_elevation_batch(elev.handle, residuals.handle if residuals else None,
+                                   normals.handle if normals else None, C.byref(params),
+                                   arr, len(jobs), stream))
+
+
+def elevation_batch_device(elev, residuals, normals, params, jobs_dev_ptr, n, stream=None):
+    check(lib().tp_elevation_batch_device(elev.handle, residuals.handle if residuals else None,
+                                          normals.handle if normals else None, C.byref(params),
+                                          jobs_dev_ptr, n, stream))
+
+
+def dem_noise(tile_width):
+    out = np.empty((6, tile_width, tile_width), np.float32)
+    check(lib().tp_dem_noise(tile_width, out.ctypes.data_as(C.POINTER(C.c_float))))
+    return out
+
+
+def cnoise(x, y):
+    return lib().tp_cnoise(float(x), float(y))
+
+
+def noise_select(face, level, tx, ty):
+    r, l = C.c_int(), C.c_int()
+    check(lib().tp_noise_select(face, level, tx, ty, C.byref(r), C.byref(l)))
+    return r.value, l.value

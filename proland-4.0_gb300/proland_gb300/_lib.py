@@ -1,0 +1,102 @@
+"""ctypes binding of libproland_gb300.so (the C ABI declared in include/proland_gb300.h).
+
+The shared library is the product: every compute call goes through it and there
+is no CPU fallback.  Loading fails loudly when the library has not been built.
+"""
+import ctypes as C
+import os
+
+PKG_ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+LIB_PATH = os.path.join(PKG_ROOT, "lib", "libproland_gb300.so")
+
+TP_OK = 0
+TP_E_BAD_ARG = -1
+TP_E_CACHE_FULL = -2
+TP_E_MISSING_PARENT = -3
+TP_E_TIMEOUT = -4
+TP_E_CUDA = -5
+TP_E_IO = -6
+TP_E_NO_DEVICE = -7
+
+ERROR_NAMES = {
+    TP_E_BAD_ARG: "TP_E_BAD_ARG", TP_E_CACHE_FULL: "TP_E_CACHE_FULL",
+    TP_E_MISSING_PARENT: "TP_E_MISSING_PARENT", TP_E_TIMEOUT: "TP_E_TIMEOUT",
+    TP_E_CUDA: "TP_E_CUDA", TP_E_IO: "TP_E_IO", TP_E_NO_DEVICE: "TP_E_NO_DEVICE",
+}
+
+
+class TPError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("%s (%d): %s" % (ERROR_NAMES.get(code, "TP_E_?"), code, msg))
+        self.code = code
+
+
+class TileJob(C.Structure):
+    """tp_tile_job"""
+    _fields_ = [
+        ("level", C.c_int32), ("tx", C.c_int32), ("ty", C.c_int32),
+        ("out_slot", C.c_int32), ("parent_slot", C.c_int32), ("residual_slot", C.c_int32),
+        ("rx", C.c_int32), ("ry", C.c_int32), ("normal_slot", C.c_int32),
+        ("noise_rot", C.c_int32), ("noise_layer", C.c_int32),
+        ("noise_amp", C.c_float), ("rscale", C.c_float), ("tile_meters", C.c_float),
+        ("parent_job", C.c_int32), ("reserved", C.c_int32),
+    ]
+
+
+class ElevParams(C.Structure):
+    """tp_elev_params"""
+    _fields_ = [
+        ("grid_size", C.c_int32), ("flip", C.c_int32), ("no_clamp", C.c_int32),
+        ("noise_mode", C.c_int32), ("normal_format", C.c_int32), ("reserved", C.c_int32 * 3),
+    ]
+
+
+_LIB = None
+_vp = C.c_void_p
+_i = C.c_int
+_f32p = C.POINTER(C.c_float)
+
+
+def lib():
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    if not os.path.exists(LIB_PATH):
+        raise ImportError("libproland_gb300.so is not built (%s): run "
+                          "`python -c \"import __graft_entry__ as g; g.build()\"`" % LIB_PATH)
+    L = C.CDLL(LIB_PATH)
+    sig = {
+        "tp_last_error": ([], C.c_char_p),
+        "tp_version": ([], _i),
+        "tp_device_available": ([], _i),
+        "tp_storage_create": ([_i, _i, _i, _i, C.POINTER(_vp)], _i),
+        "tp_storage_destroy": ([_vp], _i),
+        "tp_storage_tile_size": ([_vp], _i),
+        "tp_storage_capacity": ([_vp], _i),
+        "tp_storage_free_slots": ([_vp], _i),
+        "tp_storage_channels": ([_vp], _i),
+        "tp_storage_pitch": ([_vp], _i),
+        "tp_storage_new_slot": ([_vp], _i),
+        "tp_storage_delete_slot": ([_vp, _i], _i),
+        "tp_storage_plane": ([_vp, _i, _i], _vp),
+        "tp_storage_upload": ([_vp, _i, _i, _i, _vp, _vp], _i),
+        "tp_storage_download": ([_vp, _i, _i, _i, _vp, _vp], _i),
+        "tp_elevation_batch": ([_vp, _vp, _vp, C.POINTER(ElevParams), C.POINTER(TileJob), _i, _vp], _i),
+        "tp_elevation_batch_device": ([_vp, _vp, _vp, C.POINTER(ElevParams), _vp, _i, _vp], _i),
+        "tp_dem_noise": ([_i, _f32p], _i),
+        "tp_cnoise": ([C.c_float, C.c_float], C.c_float),
+        "tp_noise_select": ([_i, _i, _i, _i, C.POINTER(_i), C.POINTER(_i)], _i),
+    }
+    for name, (args, res) in sig.items():
+        f = getattr(L, name)
+        f.argtypes = args
+        f.restype = res
+    _LIB = L
+    return L
+
+
+def check(rc):
+    """Raises TPError for a negative return code, else returns it."""
+    if rc < 0:
+        raise TPError(rc, lib().tp_last_error().decode(errors="replace"))
+    return rc
