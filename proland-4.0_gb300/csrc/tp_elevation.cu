@@ -155,6 +155,9 @@ elevation_kernel(const tp::ElevLaunch a)
     const int r0 = (warp * W) / kWarps, r1 = ((warp + 1) * W) / kWarps;
     const int i0 = lane * SPL;
     const bool store_lane = i0 < a.pitch;
+    // lanes past the last sample column compute on the last in-tile quad so that
+    // every load of theirs stays inside the tile (their results are not stored)
+    const int i0c = min(i0, ((W - 1) / SPL) * SPL);
 
     float *ozf = a.elev + (long long)J.out_slot * a.slot_stride;
     float *ozc = ozf + a.plane_stride;
@@ -179,7 +182,7 @@ elevation_kernel(const tp::ElevLaunch a)
         // residual: one or two aligned 16-byte loads per lane
         float res[SPL];
         if (R) {
-            const float4 *rp = reinterpret_cast<const float4 *>(R + (long long)(j + J.ry) * a.res_pitch + i0 + J.rx);
+            const float4 *rp = reinterpret_cast<const float4 *>(R + (long long)(j + J.ry) * a.res_pitch + i0c + J.rx);
 #pragma unroll
             for (int q = 0; q < SPL / 4; ++q) {
                 float4 t = __ldg(rp + q);

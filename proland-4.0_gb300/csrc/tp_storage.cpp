@@ -228,8 +228,12 @@ static int check_params(tp_storage *elev, tp_storage *res, tp_storage *nrm, cons
     // parent window: the stencil reads parent samples [d, d + n/2 + 4], the modulated
     // noise up to d + n/2 + 5, the coarse-mesh lookups down to d + 2 - g
     L->wlo = g > 2 ? -tp::round_up(g - 2, 4) : 0;
-    L->wh = n / 2 + 6 - L->wlo;
+    const int kmax = (n + 2 + g) / (2 * g);             // largest coarse-mesh index of a sample
+    const int hi = std::max(n / 2 + 5, 2 + g * kmax);   // last window sample, relative to d
+    L->wh = hi + 1 - L->wlo;
     L->ww = tp::round_up(L->wh, 4);
+    if (sizeof(float) * 2 * (size_t)L->ww * L->wh > 200 * 1024)
+        return tp::fail(TP_E_BAD_ARG, "batch: grid_size too small for the batch kernel's parent window");
     return TP_OK;
 }
 
