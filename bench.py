@@ -346,6 +346,7 @@ def main():
     t_end.record(stream)
     torch.cuda.synchronize()
     clk = clocks.stop()
+    tp.stream_check(sh)
     ms_total = t_start.elapsed_time(t_end)
     kernel_ms = [sum(kernel_ev[s][i][0].elapsed_time(kernel_ev[s][i][1]) for s in range(args.steps)) / args.steps
                  for i in range(len(classes))]

@@ -98,13 +98,15 @@ typedef struct {
     int32_t no_clamp;       /* NO_CLAMP: zm = zf instead of max(zf, 0) */
     int32_t noise_mode;     /* 0: zf += |amp| N (terrain1 shader); 1: slope/curvature modulated (demo shader) */
     int32_t normal_format;  /* 2: two signed fp32 planes (the only one supported by the batch kernel) */
-    int32_t reserved[3];
+    int32_t band_rows;      /* rows per kernel work unit; 0 picks the tuned default */
+    int32_t reserved[2];
 } tp_elev_params;
 
 /* Produces n jobs on `stream`.  `jobs` is host memory; it is copied into a
- * device buffer owned by the storage `elev`.  All jobs must be independent
- * (parent_job == -1) unless ordered_waves != 0, in which case the batch is run
- * in dependency waves.  `residuals`/`normals` may be NULL when unused. */
+ * device buffer owned by the storage `elev`.  A job whose parent is produced by
+ * an earlier job of the same batch names it in parent_job; such a batch runs in
+ * dependency waves (parents before children).  `residuals`/`normals` may be NULL
+ * when unused.  One batch per storage and stream at a time. */
 int tp_elevation_batch(tp_storage *elev, tp_storage *residuals, tp_storage *normals,
                        const tp_elev_params *params, const tp_tile_job *jobs, int n,
                        void *stream);
@@ -112,6 +114,12 @@ int tp_elevation_batch(tp_storage *elev, tp_storage *residuals, tp_storage *norm
 int tp_elevation_batch_device(tp_storage *elev, tp_storage *residuals, tp_storage *normals,
                               const tp_elev_params *params, const tp_tile_job *jobs_dev, int n,
                               void *stream);
+
+/* Device status word: TP_OK, or the first TP_E_* code a kernel reported (a
+ * dependency or copy wait that gave up).  tp_status reads it (and clears it when
+ * `clear`); tp_stream_check synchronises `stream`, then reads and clears it. */
+int tp_status(int *status, int clear);
+int tp_stream_check(void *stream);
 
 /* ------------------------------------------------------------------------
  * Noise helpers (host).  createDemNoise (ElevationProducer.cpp:50-133) and the

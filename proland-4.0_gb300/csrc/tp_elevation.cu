@@ -1,37 +1,112 @@
 // Fused elevation + normal tile kernel for sm_103a.
 //
-// One CTA produces one tile.  The parent's zf and zm planes over the window the
-// child reads are staged in shared memory; each warp then sweeps a band of rows
-// of the child tile, every lane owning SPL consecutive columns (SPL = 4 for
-// 101-wide tiles, 8 for 197-wide: one lane row covers the padded pitch).  Per
-// row a lane computes zf / zc / zm, writes them with 16-byte stores, and keeps
-// the last three zm rows in registers; the normal of the row before the current
-// one is then formed from those registers, the horizontal neighbours crossing
-// lane boundaries by warp shuffles.
+// Work unit: one band of rows [j0, j1) of one child tile (a whole 101-wide tile,
+// or a quarter of a 197-wide one; the band height is a launch parameter).  Per
+// unit, one thread issues two TMA copies into shared memory, completing on one
+// mbarrier:
+//   * the residual rows [j0 - 1, j1 + 1) of the tile's residual window
+//     (cp.async.bulk.tensor.3d over the residual slot pool), and
+//   * the parent zf window the stencil of those rows reads (over the elevation
+//     slot pool, plane zf of the parent slot);
+// while the copies fly, the other threads fetch the parent zm at the coarse-mesh
+// vertices zc interpolates (a 14 x 14 lattice for the default grid).
+// Phase A then computes zf, zc, zm of rows [j0 - 1, j1] (the band plus one halo
+// row each side), writing the band rows to HBM with 16-byte stores and every
+// row's zm back over its residual in shared memory.  Phase B forms the normals
+// of the band rows from that zm: vertical neighbours from the rows above and
+// below, horizontal neighbours across quad boundaries by warp shuffles.
 //
 // Arithmetic follows the reference exactly:
 //  * stencil: CPUElevationProducer.cpp:202-238 (the same loops as
 //    ResidualProducer.cpp:342-384 and HeightMipmap.cpp:449-497), in that
-//    operation order, each operation rounded on its own (__f*_rn) so the result
+//    operation order, each operation rounded on its own (__f*_rn), so the result
 //    is bit-identical to a CPU build without floating-point contraction;
 //  * residual, noise, zc, zm: upsampleShader.glsl main()
 //    (terrain/examples/terrain1/upsampleShader.glsl:81-125; flip variant
 //    terrain/examples/terrain4/upsampleShader.glsl:112-127; modulated noise
 //    demo/shaders/elevation/upsampleShader.glsl:140-203);
-//  * normals: terrain/examples/terrain1/normalShader.glsl:57-74 with point
-//    sampling of the zm channel.
+//  * normals: terrain/examples/terrain1/normalShader.glsl:57-74, point sampling
+//    of the zm channel.
+#include <cuda.h>
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 #include "tp_internal.h"
 
+__device__ int g_tp_status = 0;  // TP_OK, or the first TP_E_* a kernel reported
+
 namespace {
 
 constexpr int kThreads = 256;
+constexpr int kWarps = kThreads / 32;
+constexpr unsigned kWaitLimit = 1u << 22;  // mbarrier polls before a wait is declared failed
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p)
+{
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity)
+{
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// Waits for phase `parity` of the barrier with a bounded number of polls.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity)
+{
+    for (unsigned k = 0; k < kWaitLimit; ++k)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
+
+__device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *map, uint64_t *bar, int x, int y, int z)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];"
+        ::"r"(smem_u32(dst)), "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
+        : "memory");
+}
 
 __device__ __forceinline__ int floordiv(int a, int b) { return a >= 0 ? a / b : -((-a + b - 1) / b); }
 __device__ __forceinline__ int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
 
-// Stencil of one child sample.  `c` points at the parent sample (i/2 + px, j/2 + py)
+// floor(a / (2g)) for a grid step g known at compile time (power of two) or not (G == 0)
+template <int G>
+__device__ __forceinline__ int fdiv2g(int a, int g)
+{
+    if constexpr (G == 4) return a >> 3;
+    else if constexpr (G == 8) return a >> 4;
+    else return floordiv(a, 2 * g);
+}
+template <int G>
+__device__ __forceinline__ int fmod2g(int a, int g)
+{
+    if constexpr (G == 4) return a & 7;
+    else if constexpr (G == 8) return a & 15;
+    else return a - 2 * g * floordiv(a, 2 * g);
+}
+
+// Stencil of one child sample; `c` points at the parent sample (i/2 + px, j/2 + py)
 // in the staged window, `ww` is the window row pitch.
 __device__ __forceinline__ float upsample_at(const float *c, int ww, int i, int j)
 {
@@ -85,7 +160,7 @@ __device__ __forceinline__ float mdot16(const float *cz, const float *M)
     return s;
 }
 
-__device__ float demo_modulation(const float *cz, int mi, float mps)
+__device__ __noinline__ float demo_modulation(const float *cz, int mi, float mps)
 {
     float sx = mdot16(cz, c_slopex[mi]);
     float sy = mdot16(cz, c_slopey[mi]);
@@ -99,142 +174,130 @@ __device__ float demo_modulation(const float *cz, int mi, float mps)
     return a > b ? a : b;
 }
 
-// Noise texel of sample (i, j) under rotation `rot` (the shader reads
-// (uvs[rot], uvs[(rot+1)%4]) with uvs = (u, v, 1-u, 1-v), u = (i+0.5)/W).
-__device__ __forceinline__ int noise_index(int W, int rot, int i, int j)
+__device__ __forceinline__ void report(int code) { atomicCAS(&g_tp_status, 0, code); }
+
+template <int G>
+__global__ void __launch_bounds__(kThreads, 3)
+elevation_kernel(const __grid_constant__ CUtensorMap parent_map, const __grid_constant__ CUtensorMap res_map,
+                 const tp::ElevLaunch a)
 {
-    switch (rot & 3) {
-    case 0: return i + j * W;
-    case 1: return j + (W - 1 - i) * W;
-    case 2: return (W - 1 - i) + (W - 1 - j) * W;
-    default: return (W - 1 - j) + i * W;
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    __shared__ uint64_t bar;
+    // TMA destinations on 128-byte boundaries (the launch adds 128 bytes of slack)
+    const uint32_t raw = smem_u32(smem_raw);
+    float *sbuf = reinterpret_cast<float *>(smem_raw + (((raw + 127u) & ~127u) - raw));  // residual rows, then zm rows
+    float *spar = sbuf + a.buf_floats;                      // parent zf window
+    float *scoarse = spar + a.par_floats;                   // parent zm at the coarse-mesh vertices
+
+    const int unit = a.first + blockIdx.x;
+    const int jslot = unit / a.bands;
+    const int band = unit - jslot * a.bands;
+    const int jidx = a.order ? a.order[jslot] : jslot;
+    const tp_tile_job &J = a.jobs[jidx];
+    const int W = a.W, n = W - 5, PE = a.pitch, g = G ? G : a.g;
+    const int level = J.level, tx = J.tx, ty = J.ty;
+    const int dx = (tx & 1) * (n / 2), dy = (ty & 1) * (n / 2);
+    const bool has_parent = level > 0, has_res = J.residual_slot >= 0;
+    const int j0 = (band * W) / a.bands, j1 = ((band + 1) * W) / a.bands;
+    const int ja = max(j0 - 1, 0), jb = min(j1, W - 1);
+    const int pr0 = ja / 2 + dy;  // first parent row of the window
+
+    // ---- issue the copies
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        uint32_t bytes = 0;
+        if (has_res) bytes += a.res_box_bytes;
+        if (has_parent) bytes += a.par_box_bytes;
+        mbar_expect_tx(&bar, bytes);
+        if (has_res) tma_load_3d(sbuf, &res_map, &bar, J.rx, J.ry + j0 - 1, J.residual_slot);
+        if (has_parent) tma_load_3d(spar, &parent_map, &bar, dx, pr0, J.parent_slot * 3 + 0);
     }
-}
-
-template <int SPL>
-__device__ __forceinline__ void store_row(float *dst, const float (&v)[SPL])
-{
-#pragma unroll
-    for (int q = 0; q < SPL / 4; ++q)
-        reinterpret_cast<float4 *>(dst)[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
-}
-
-template <int SPL>
-__global__ void __launch_bounds__(kThreads)
-elevation_kernel(const tp::ElevLaunch a)
-{
-    extern __shared__ float4 smem4[];
-    float *szf = reinterpret_cast<float *>(smem4);
-    float *szm = szf + a.ww * a.wh;
-
-    const int jidx = a.order ? a.order[a.first + blockIdx.x] : a.first + blockIdx.x;
-    const tp_tile_job J = a.jobs[jidx];
-    const int W = a.W, n = W - 5;
-    const int dx = (J.tx & 1) * (n / 2), dy = (J.ty & 1) * (n / 2);
-    const bool has_parent = J.level > 0;
-
-    // ---- stage the parent window: parent samples [d + wlo, d + wlo + ww) on both axes,
-    // clamped to the tile (CLAMP_TO_EDGE for the coarse-mesh lookups of zc)
+    // coarse-mesh vertices (parent zm, CLAMP_TO_EDGE) with plain loads meanwhile
     if (has_parent) {
-        const float *pzf = a.elev + (long long)J.parent_slot * a.slot_stride;
-        const float *pzm = pzf + 2 * a.plane_stride;
-        const int wx0 = dx + a.wlo, wy0 = dy + a.wlo;
-        const int total = a.ww * a.wh;
-        for (int e = threadIdx.x; e < total; e += kThreads) {
-            int r = e / a.ww, c = e - r * a.ww;
-            int gx = clampi(wx0 + c, 0, W - 1), gy = clampi(wy0 + r, 0, W - 1);
-            long long o = (long long)gy * a.pitch + gx;
-            szf[e] = __ldg(pzf + o);
-            szm[e] = __ldg(pzm + o);
+        const float *pzm = a.elev + (long long)J.parent_slot * a.slot_stride + 2 * a.plane_stride;
+        for (int t = threadIdx.x; t < a.ck * a.ck; t += kThreads) {
+            const int ky = t / a.ck - 1, kx = t - (ky + 1) * a.ck - 1;
+            const int X = clampi(2 + dx + g * kx, 0, W - 1), Y = clampi(2 + dy + g * ky, 0, W - 1);
+            scoarse[t] = __ldg(pzm + (long long)Y * PE + X);
         }
     }
-    __syncthreads();
+    __syncthreads();  // barrier initialised, coarse lattice written
+    if (has_res || has_parent) {
+        if (!mbar_wait_bounded(&bar, 0)) {
+            report(TP_E_TIMEOUT);
+            mbar_wait_bounded(&bar, 0);  // give the copies a second chance to land before leaving
+            return;
+        }
+    }
+    if (!has_res) {
+        for (int t = threadIdx.x; t < a.buf_floats; t += kThreads) sbuf[t] = 0.0f;
+        __syncthreads();
+    }
 
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    constexpr int kWarps = kThreads / 32;
-    const int r0 = (warp * W) / kWarps, r1 = ((warp + 1) * W) / kWarps;
-    const int i0 = lane * SPL;
-    const bool store_lane = i0 < a.pitch;
-    // lanes past the last sample column compute on the last in-tile quad so that
-    // every load of theirs stays inside the tile (their results are not stored)
-    const int i0c = min(i0, ((W - 1) / SPL) * SPL);
-
+    // ---- phase A: elevation of rows [ja, jb], quads of 4 samples
+    const int NQ = PE / 4;
     float *ozf = a.elev + (long long)J.out_slot * a.slot_stride;
     float *ozc = ozf + a.plane_stride;
     float *ozm = ozf + 2 * a.plane_stride;
-    const float *R = J.residual_slot >= 0 ? a.res + (long long)J.residual_slot * a.res_slot_stride : nullptr;
-    const float *NZ = J.noise_amp != 0.0f ? a.noise + (long long)J.noise_layer * W * W : nullptr;
-    const bool want_normals = a.nrm != nullptr && J.normal_slot >= 0;
-    float *onx = want_normals ? a.nrm + (long long)J.normal_slot * a.nrm_slot_stride : nullptr;
-    float *ony = want_normals ? onx + a.nrm_plane_stride : nullptr;
-    const int Wn = W - 4;
-    const float h2 = __fmul_rn(2.0f, __fdiv_rn(J.tile_meters, (float)n));
+    const bool noisy = J.noise_amp != 0.0f;
+    const __half *nz_base = a.noise + (long long)(J.noise_rot * 6 + J.noise_layer) * W * PE;
     const float abs_amp = fabsf(J.noise_amp);
-    const int g = a.g;
-
-    float zmA[SPL], zmB[SPL], zmC[SPL];
-#pragma unroll
-    for (int k = 0; k < SPL; ++k) zmA[k] = zmB[k] = zmC[k] = 0.0f;
-
-    const int ja = max(r0 - 1, 0), jb = min(r1, W - 1);
-    for (int j = ja; j <= jb; ++j) {
-        float vf[SPL], vc[SPL], vm[SPL];
-        // residual: one or two aligned 16-byte loads per lane
-        float res[SPL];
-        if (R) {
-            const float4 *rp = reinterpret_cast<const float4 *>(R + (long long)(j + J.ry) * a.res_pitch + i0c + J.rx);
-#pragma unroll
-            for (int q = 0; q < SPL / 4; ++q) {
-                float4 t = __ldg(rp + q);
-                res[4 * q] = t.x; res[4 * q + 1] = t.y; res[4 * q + 2] = t.z; res[4 * q + 3] = t.w;
-            }
+    const int nitems = (jb - ja + 1) * NQ;
+    for (int it = threadIdx.x; it < nitems; it += kThreads) {
+        const int rr = it / NQ, q = it - rr * NQ;
+        const int j = ja + rr, i0 = 4 * q;
+        float *brow = sbuf + (j - j0 + 1) * PE;
+        const float4 r4 = *reinterpret_cast<const float4 *>(brow + i0);
+        const float rv[4] = {r4.x, r4.y, r4.z, r4.w};
+        float nv[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+        if (noisy) {
+            const uint2 h = __ldg(reinterpret_cast<const uint2 *>(nz_base + (long long)j * PE + i0));
+            const float2 n01 = __half22float2(*reinterpret_cast<const __half2 *>(&h.x));
+            const float2 n23 = __half22float2(*reinterpret_cast<const __half2 *>(&h.y));
+            nv[0] = n01.x; nv[1] = n01.y; nv[2] = n23.x; nv[3] = n23.y;
         }
-        const float *crow = szf + (j / 2 + 1 - a.wlo) * a.ww;
+        const float *prow = spar + (j / 2 + 1 + dy - pr0) * a.par_pitch;
+        const int cy = j - 2;
+        const int kyr = fdiv2g<G>(cy + g, g) + 1, kyf = fdiv2g<G>(cy, g) + 1;
+        const bool flip_row = a.flip && fmod2g<G>(cy, g) == g;
+        float vf[4], vc[4], vm[4];
 #pragma unroll
-        for (int k = 0; k < SPL; ++k) {
+        for (int k = 0; k < 4; ++k) {
             const int i = min(i0 + k, W - 1);
-            float zf = R ? __fmul_rn(J.rscale, res[k]) : 0.0f;
-            if (NZ) {
-                float N = __ldg(NZ + noise_index(W, J.noise_rot, i, j));
+            float zf = has_res ? __fmul_rn(J.rscale, rv[k]) : 0.0f;
+            if (noisy) {
                 if (a.noise_mode == 0) {
-                    zf = __fadd_rn(zf, __fmul_rn(abs_amp, N));
+                    zf = __fadd_rn(zf, __fmul_rn(abs_amp, nv[k]));
                 } else if (J.noise_amp < 0.0f) {
-                    zf = __fsub_rn(zf, __fmul_rn(J.noise_amp, N));
+                    zf = __fsub_rn(zf, __fmul_rn(J.noise_amp, nv[k]));
                 } else {
                     float cz[16];
 #pragma unroll
-                    for (int q = 0; q < 16; ++q)
-                        cz[q] = has_parent ? szf[(j / 2 - a.wlo + q / 4) * a.ww + (i / 2 - a.wlo + q % 4)] : 0.0f;
-                    float mps = __fdiv_rn(J.tile_meters, (float)n);
-                    float m = demo_modulation(cz, (i & 1) + 2 * (j & 1), mps);
-                    zf = __fadd_rn(zf, __fmul_rn(__fmul_rn(m, J.noise_amp), N));
+                    for (int t = 0; t < 16; ++t) {
+                        const int X = clampi(i / 2 + dx + t % 4, 0, W - 1) - dx;
+                        const int Y = clampi(j / 2 + dy + t / 4, 0, W - 1) - pr0;
+                        cz[t] = has_parent ? spar[Y * a.par_pitch + X] : 0.0f;
+                    }
+                    const float mps = __fdiv_rn(J.tile_meters, (float)n);
+                    const float m = demo_modulation(cz, (i & 1) + 2 * (j & 1), mps);
+                    zf = __fadd_rn(zf, __fmul_rn(__fmul_rn(m, J.noise_amp), nv[k]));
                 }
             }
             float zc = zf;
             if (has_parent) {
-                zf = __fadd_rn(zf, upsample_at(crow + (i / 2 + 1 - a.wlo), a.ww, i, j));
-                // coarse-mesh elevation (zc) from the parent zm plane
-                const int cx = i - 2, cy = j - 2;
-                const int kxr = floordiv(cx + g, 2 * g), kxf = floordiv(cx, 2 * g);
-                const int kyr = floordiv(cy + g, 2 * g), kyf = floordiv(cy, 2 * g);
-                const int Xr = clampi(2 + dx + g * kxr, 0, W - 1) - dx - a.wlo;
-                const int Xf = clampi(2 + dx + g * kxf, 0, W - 1) - dx - a.wlo;
-                const int Yr = clampi(2 + dy + g * kyr, 0, W - 1) - dy - a.wlo;
-                const int Yf = clampi(2 + dy + g * kyf, 0, W - 1) - dy - a.wlo;
-                const float zc1 = szm[Yf * a.ww + Xr];
-                const float zc3 = szm[Yr * a.ww + Xf];
-                bool flipped = false;
-                if (a.flip) {
-                    const int mx = ((cx % (2 * g)) + 2 * g) % (2 * g), my = ((cy % (2 * g)) + 2 * g) % (2 * g);
-                    if (mx == g && my == g) {
-                        const float zc0 = szm[Yf * a.ww + Xf];
-                        const float zc2 = szm[Yr * a.ww + Xr];
-                        const float s13 = __fadd_rn(zc3, zc1), s02 = __fadd_rn(zc0, zc2);
-                        zc = __fmul_rn(s13 >= s02 ? __fadd_rn(zc1, zc3) : s02, 0.5f);
-                        flipped = true;
-                    }
+                zf = __fadd_rn(zf, upsample_at(prow + (i / 2 + 1), a.par_pitch, i, j));
+                const int cx = i - 2;
+                const int kxr = fdiv2g<G>(cx + g, g) + 1, kxf = fdiv2g<G>(cx, g) + 1;
+                const float zc1 = scoarse[kyf * a.ck + kxr];
+                const float zc3 = scoarse[kyr * a.ck + kxf];
+                if (flip_row && fmod2g<G>(cx, g) == g) {
+                    const float zc0 = scoarse[kyf * a.ck + kxf];
+                    const float zc2 = scoarse[kyr * a.ck + kxr];
+                    const float s13 = __fadd_rn(zc3, zc1), s02 = __fadd_rn(zc0, zc2);
+                    zc = __fmul_rn(s13 >= s02 ? __fadd_rn(zc1, zc3) : s02, 0.5f);
+                } else {
+                    zc = __fmul_rn(__fadd_rn(zc1, zc3), 0.5f);
                 }
-                if (!flipped) zc = __fmul_rn(__fadd_rn(zc1, zc3), 0.5f);
             }
             const float zm = a.no_clamp ? zf : (zf > 0.0f ? zf : 0.0f);
             const bool pad = i0 + k >= W;
@@ -242,56 +305,74 @@ elevation_kernel(const tp::ElevLaunch a)
             vc[k] = pad ? 0.0f : zc;
             vm[k] = pad ? 0.0f : zm;
         }
-        if (j >= r0 && j < r1 && store_lane) {
-            const long long o = (long long)j * a.pitch + i0;
-            store_row<SPL>(ozf + o, vf);
-            store_row<SPL>(ozc + o, vc);
-            store_row<SPL>(ozm + o, vm);
+        if (j >= j0 && j < j1) {
+            const long long o = (long long)j * PE + i0;
+            *reinterpret_cast<float4 *>(ozf + o) = make_float4(vf[0], vf[1], vf[2], vf[3]);
+            *reinterpret_cast<float4 *>(ozc + o) = make_float4(vc[0], vc[1], vc[2], vc[3]);
+            *reinterpret_cast<float4 *>(ozm + o) = make_float4(vm[0], vm[1], vm[2], vm[3]);
         }
+        *reinterpret_cast<float4 *>(brow + i0) = make_float4(vm[0], vm[1], vm[2], vm[3]);
+    }
+    if (a.nrm == nullptr || J.normal_slot < 0) return;
+    __syncthreads();
+
+    // ---- phase B: normals of rows jn in [max(j0, 2), min(j1, W - 2)), one warp per row
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int Wn = W - 4, NQn = a.nrm_pitch / 4;
+    float *onx = a.nrm + (long long)J.normal_slot * a.nrm_slot_stride;
+    float *ony = onx + a.nrm_plane_stride;
+    const float h2 = __fmul_rn(2.0f, __fdiv_rn(J.tile_meters, (float)n));
+    const float hh = h2 * h2;
+    for (int jn = max(j0, 2) + warp; jn < min(j1, W - 2); jn += kWarps) {
+        const float *c = sbuf + (jn - j0 + 1) * PE;
+        const float *up = c + PE, *dn = c - PE;
+        for (int base = 0; base < NQn; base += 32) {
+            const int m = base + lane;
+            const bool act = m < NQn;
+            const int e = act ? 4 * m + 2 : 2;  // elevation column of this quad's first normal
+            const float2 c01 = *reinterpret_cast<const float2 *>(c + e);
+            const float2 c23 = *reinterpret_cast<const float2 *>(c + e + 2);
+            const float2 u01 = *reinterpret_cast<const float2 *>(up + e);
+            const float2 u23 = *reinterpret_cast<const float2 *>(up + e + 2);
+            const float2 d01 = *reinterpret_cast<const float2 *>(dn + e);
+            const float2 d23 = *reinterpret_cast<const float2 *>(dn + e + 2);
+            // horizontal neighbours e - 1 and e + 4 live in the adjacent lanes' quads
+            float left = __shfl_up_sync(0xffffffffu, c23.y, 1);
+            float right = __shfl_down_sync(0xffffffffu, c01.x, 1);
+            if (lane == 0) left = c[e - 1];
+            if (lane == 31 || m == NQn - 1) right = c[min(e + 4, PE - 1)];
+            const float zc_[6] = {left, c01.x, c01.y, c23.x, c23.y, right};
+            const float zu[4] = {u01.x, u01.y, u23.x, u23.y};
+            const float zd[4] = {d01.x, d01.y, d23.x, d23.y};
+            float nx[4], ny[4];
 #pragma unroll
-        for (int k = 0; k < SPL; ++k) {
-            zmA[k] = zmB[k];
-            zmB[k] = zmC[k];
-            zmC[k] = vm[k];
-        }
-        // ---- normals of row jn = j - 1 from zm rows j-2, j-1, j
-        const int jn = j - 1;
-        if (want_normals && jn >= max(r0, 2) && jn < min(r1, W - 2)) {
-            const float left = __shfl_up_sync(0xffffffffu, zmB[SPL - 1], 1);
-            const float right = __shfl_down_sync(0xffffffffu, zmB[0], 1);
-            float nx[SPL], ny[SPL];
-#pragma unroll
-            for (int k = 0; k < SPL; ++k) {
-                const float zl = k == 0 ? left : zmB[k - 1];
-                const float zr = k == SPL - 1 ? right : zmB[k + 1];
-                const float ax = -__fsub_rn(zr, zl);
-                const float ay = -__fsub_rn(zmC[k], zmA[k]);
-                const float inv = rsqrtf(ax * ax + ay * ay + h2 * h2);
-                nx[k] = ax * inv;
-                ny[k] = ay * inv;
+            for (int k = 0; k < 4; ++k) {
+                const float ax = -__fsub_rn(zc_[k + 2], zc_[k]);
+                const float ay = -__fsub_rn(zu[k], zd[k]);
+                const float inv = rsqrtf(ax * ax + ay * ay + hh);
+                const bool pad = 4 * m + k >= Wn;
+                nx[k] = pad ? 0.0f : ax * inv;
+                ny[k] = pad ? 0.0f : ay * inv;
             }
-            // normal column p sits at elevation column p + 2: lane m stores normal
-            // columns [SPL m, SPL m + SPL) = its own k = 2.. and lane m+1's k = 0, 1
-            const float nx0 = __shfl_down_sync(0xffffffffu, nx[0], 1);
-            const float nx1 = __shfl_down_sync(0xffffffffu, nx[1], 1);
-            const float ny0 = __shfl_down_sync(0xffffffffu, ny[0], 1);
-            const float ny1 = __shfl_down_sync(0xffffffffu, ny[1], 1);
-            float sx[SPL], sy[SPL];
-#pragma unroll
-            for (int k = 0; k < SPL; ++k) {
-                float vx = k < SPL - 2 ? nx[k + 2] : (k == SPL - 2 ? nx0 : nx1);
-                float vy = k < SPL - 2 ? ny[k + 2] : (k == SPL - 2 ? ny0 : ny1);
-                const bool pad = i0 + k >= Wn;
-                sx[k] = pad ? 0.0f : vx;
-                sy[k] = pad ? 0.0f : vy;
-            }
-            if (i0 < a.nrm_pitch) {
-                const long long o = (long long)(jn - 2) * a.nrm_pitch + i0;
-                store_row<SPL>(onx + o, sx);
-                store_row<SPL>(ony + o, sy);
+            if (act) {
+                const long long o = (long long)(jn - 2) * a.nrm_pitch + 4 * m;
+                *reinterpret_cast<float4 *>(onx + o) = make_float4(nx[0], nx[1], nx[2], nx[3]);
+                *reinterpret_cast<float4 *>(ony + o) = make_float4(ny[0], ny[1], ny[2], ny[3]);
             }
         }
     }
+}
+
+template <int G>
+int launch_g(const tp::ElevLaunch &a, cudaStream_t s)
+{
+    const size_t smem = a.smem_bytes + 128;
+    cudaError_t e = cudaFuncSetAttribute(elevation_kernel<G>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return tp::cuda_fail("cudaFuncSetAttribute", e);
+    elevation_kernel<G><<<a.count, kThreads, smem, s>>>(*a.parent_map, *a.res_map, a);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return tp::cuda_fail("elevation kernel launch", e);
+    return TP_OK;
 }
 
 }  // namespace
@@ -301,22 +382,23 @@ namespace tp {
 int launch_elevation(const ElevLaunch &a, void *stream)
 {
     if (a.count <= 0) return TP_OK;
-    const size_t smem = sizeof(float) * 2 * (size_t)a.ww * a.wh;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
-    cudaError_t e;
-    if (a.pitch <= 32 * 4) {
-        e = cudaFuncSetAttribute(elevation_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return cuda_fail("cudaFuncSetAttribute", e);
-        elevation_kernel<4><<<a.count, kThreads, smem, s>>>(a);
-    } else if (a.pitch <= 32 * 8) {
-        e = cudaFuncSetAttribute(elevation_kernel<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return cuda_fail("cudaFuncSetAttribute", e);
-        elevation_kernel<8><<<a.count, kThreads, smem, s>>>(a);
-    } else {
-        return fail(TP_E_BAD_ARG, "tile width above 256 is not supported by the batch kernel");
+    if (a.g == 4) return launch_g<4>(a, s);
+    if (a.g == 8) return launch_g<8>(a, s);
+    return launch_g<0>(a, s);
+}
+
+int read_status(int *status, bool clear)
+{
+    int v = 0;
+    cudaError_t e = cudaMemcpyFromSymbol(&v, g_tp_status, sizeof(int));
+    if (e != cudaSuccess) return cuda_fail("cudaMemcpyFromSymbol (status)", e);
+    if (clear && v != 0) {
+        int z = 0;
+        e = cudaMemcpyToSymbol(g_tp_status, &z, sizeof(int));
+        if (e != cudaSuccess) return cuda_fail("cudaMemcpyToSymbol (status)", e);
     }
-    e = cudaGetLastError();
-    if (e != cudaSuccess) return cuda_fail("elevation kernel launch", e);
+    *status = v;
     return TP_OK;
 }
 

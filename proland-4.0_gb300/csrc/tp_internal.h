@@ -1,9 +1,14 @@
 // Internal declarations shared by the host C++ and the CUDA translation units.
 #pragma once
 
+#include <cuda.h>
+#include <cuda_fp16.h>
+
 #include <cstdint>
+#include <map>
 #include <mutex>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "../../include/proland_gb300.h"
@@ -37,35 +42,49 @@ struct tp_storage {
     size_t job_buf_bytes = 0;
     void *order_buf = nullptr;
     size_t order_buf_bytes = 0;
+    // TMA descriptors over this pool, by box (width, height)
+    std::map<std::pair<int, int>, CUtensorMap> maps;
 };
 
 namespace tp {
 
-// Device noise table (6 layers of W x W fp16-rounded floats) for tile width W,
-// created on first use and kept for the life of the process.
-const float *device_noise_table(int W, int *err);
+// Device noise table for tile width W: the six DEM noise layers (fp16, as the
+// reference's R16F texture), pre-rotated for the four rotations, laid out
+// [rotation][layer][row][pitch] with pitch = W rounded up to 8.
+const __half *device_noise_table(int W, int *err);
 
-// Host noise table (the product's own restatement of createDemNoise).
+// Host noise table (the product's own restatement of createDemNoise): 6 * W * W floats.
 void build_dem_noise(int W, float *out);
+
+// TMA descriptor of a float pool seen as a 3D tensor (x: W samples, y: W rows,
+// z: slot * channels + channel), cached on the storage.
+int tensor_map(tp_storage *s, int box_x, int box_y, const CUtensorMap **out);
 
 struct ElevLaunch {
     const tp_tile_job *jobs;  // device
     const int *order;         // device, or nullptr for identity
-    int first, count;
+    int first, count;         // units (job slot * bands + band)
+    int bands;                // row bands per tile
     float *elev;
     int W, pitch;
     long long plane_stride, slot_stride;
     const float *res;
-    int res_pitch;
-    long long res_slot_stride;
     float *nrm;
     int nrm_pitch;
     long long nrm_plane_stride, nrm_slot_stride;
-    const float *noise;
+    const __half *noise;
     int g, flip, no_clamp, noise_mode;
-    int wlo, ww, wh;  // parent window: origin offset (<= 0), smem row pitch, rows
+    // shared-memory layout of a unit
+    int buf_floats;           // (band rows + 2) * pitch, rounded to 128 bytes
+    int par_pitch, par_rows;  // parent zf window
+    int par_floats;
+    int ck;                   // coarse-mesh lattice side
+    uint32_t res_box_bytes, par_box_bytes;
+    int smem_bytes;
+    const CUtensorMap *parent_map, *res_map;
 };
 
 int launch_elevation(const ElevLaunch &a, void *stream);
+int read_status(int *status, bool clear);
 
 }  // namespace tp

@@ -100,7 +100,7 @@ const GradientNoise2 &gradient_noise()
 }
 
 std::mutex g_noise_mu;
-std::map<std::pair<int, int>, float *> g_noise_tables;  // (device, W) -> device table
+std::map<std::pair<int, int>, __half *> g_noise_tables;  // (device, W) -> device table
 
 }  // namespace
 
@@ -153,7 +153,7 @@ void build_dem_noise(int W, float *out)
     }
 }
 
-const float *device_noise_table(int W, int *err)
+const __half *device_noise_table(int W, int *err)
 {
     int dev = 0;
     cudaGetDevice(&dev);
@@ -161,11 +161,29 @@ const float *device_noise_table(int W, int *err)
     auto key = std::make_pair(dev, W);
     auto it = g_noise_tables.find(key);
     if (it != g_noise_tables.end()) return it->second;
-    std::vector<float> host((size_t)6 * W * W);
-    build_dem_noise(W, host.data());
-    float *d = nullptr;
-    cudaError_t e = cudaMalloc(&d, sizeof(float) * host.size());
-    if (e == cudaSuccess) e = cudaMemcpy(d, host.data(), sizeof(float) * host.size(), cudaMemcpyHostToDevice);
+    std::vector<float> base((size_t)6 * W * W);
+    build_dem_noise(W, base.data());
+    // pre-rotate: entry (rot, layer, j, i) is the texel the shader reads for sample
+    // (i, j) under rotation rot, i.e. (uvs[rot], uvs[(rot+1)%4]) with
+    // uvs = (u, v, 1-u, 1-v), u = (i+0.5)/W, at NEAREST filtering
+    const int P = round_up(W, 8);
+    std::vector<__half> rot((size_t)4 * 6 * W * P, __float2half_rn(0.0f));
+    for (int r = 0; r < 4; ++r)
+        for (int l = 0; l < 6; ++l)
+            for (int j = 0; j < W; ++j)
+                for (int i = 0; i < W; ++i) {
+                    int x, y;
+                    switch (r) {
+                    case 0: x = i; y = j; break;
+                    case 1: x = j; y = W - 1 - i; break;
+                    case 2: x = W - 1 - i; y = W - 1 - j; break;
+                    default: x = W - 1 - j; y = i; break;
+                    }
+                    rot[(((size_t)r * 6 + l) * W + j) * P + i] = __float2half_rn(base[(size_t)l * W * W + x + (size_t)y * W]);
+                }
+    __half *d = nullptr;
+    cudaError_t e = cudaMalloc(&d, sizeof(__half) * rot.size());
+    if (e == cudaSuccess) e = cudaMemcpy(d, rot.data(), sizeof(__half) * rot.size(), cudaMemcpyHostToDevice);
     if (e != cudaSuccess) {
         if (d) cudaFree(d);
         *err = cuda_fail("noise table upload", e);

@@ -187,8 +187,8 @@ static int check_params(tp_storage *elev, tp_storage *res, tp_storage *nrm, cons
         return tp::fail(TP_E_BAD_ARG, "batch: elevation storage must be a device storage with 3 channels");
     const int W = elev->W, n = W - 5;
     if (n < 8 || n % 8 != 0) return tp::fail(TP_E_BAD_ARG, "batch: tile width must be 8k + 5");
-    if (W > 256) return tp::fail(TP_E_BAD_ARG, "batch: tile width above 256 is not supported");
-    if (p->grid_size < 1 || n % p->grid_size != 0 || n / p->grid_size < 1)
+    if (W > 253) return tp::fail(TP_E_BAD_ARG, "batch: tile width above 253 is not supported");
+    if (p->grid_size < 1 || n % p->grid_size != 0)
         return tp::fail(TP_E_BAD_ARG, "batch: grid_size must divide the tile size");
     if (p->noise_mode != 0 && p->noise_mode != 1) return tp::fail(TP_E_BAD_ARG, "batch: bad noise_mode");
     if (res) {
@@ -207,11 +207,7 @@ static int check_params(tp_storage *elev, tp_storage *res, tp_storage *nrm, cons
     L->pitch = elev->pitch;
     L->plane_stride = elev->plane_stride;
     L->slot_stride = elev->slot_stride;
-    if (res) {
-        L->res = res->base;
-        L->res_pitch = res->pitch;
-        L->res_slot_stride = res->slot_stride;
-    }
+    if (res) L->res = res->base;
     if (nrm) {
         L->nrm = nrm->base;
         L->nrm_pitch = nrm->pitch;
@@ -225,15 +221,34 @@ static int check_params(tp_storage *elev, tp_storage *res, tp_storage *nrm, cons
     L->flip = p->flip ? 1 : 0;
     L->no_clamp = p->no_clamp ? 1 : 0;
     L->noise_mode = p->noise_mode;
-    // parent window: the stencil reads parent samples [d, d + n/2 + 4], the modulated
-    // noise up to d + n/2 + 5, the coarse-mesh lookups down to d + 2 - g
-    L->wlo = g > 2 ? -tp::round_up(g - 2, 4) : 0;
-    const int kmax = (n + 2 + g) / (2 * g);             // largest coarse-mesh index of a sample
-    const int hi = std::max(n / 2 + 5, 2 + g * kmax);   // last window sample, relative to d
-    L->wh = hi + 1 - L->wlo;
-    L->ww = tp::round_up(L->wh, 4);
-    if (sizeof(float) * 2 * (size_t)L->ww * L->wh > 200 * 1024)
-        return tp::fail(TP_E_BAD_ARG, "batch: grid_size too small for the batch kernel's parent window");
+    // band height: whole 101-wide tiles, quarters of 197-wide ones, unless asked
+    int br = p->band_rows > 0 ? p->band_rows : (W <= 128 ? W : (W + 3) / 4);
+    br = std::min(std::max(br, 8), W);
+    L->bands = (W + br - 1) / br;
+    br = (W + L->bands - 1) / L->bands;          // the tallest band actually launched
+    if (br + 2 > 256) return tp::fail(TP_E_BAD_ARG, "batch: band taller than a TMA box");
+    const int PE = elev->pitch;
+    L->buf_floats = tp::round_up((br + 2) * PE, 32);
+    // parent zf window: columns [d, d + n/2 + 5] (stencil and modulated-noise taps),
+    // rows from the first computed row's parent row, (br + 1)/2 + 5 of them
+    L->par_pitch = tp::round_up(n / 2 + 6, 4);
+    L->par_rows = (br + 1) / 2 + 5;
+    if (L->par_pitch > 256 || L->par_rows > 256) return tp::fail(TP_E_BAD_ARG, "batch: parent window above a TMA box");
+    L->par_floats = tp::round_up(L->par_pitch * L->par_rows, 32);
+    const int kmax = (n + 2 + g) / (2 * g);     // largest coarse-mesh index of a sample
+    L->ck = kmax + 2;
+    L->res_box_bytes = (uint32_t)(sizeof(float) * PE * (br + 2));
+    L->par_box_bytes = (uint32_t)(sizeof(float) * L->par_pitch * L->par_rows);
+    L->smem_bytes = (int)(sizeof(float) * ((size_t)L->buf_floats + L->par_floats + tp::round_up(L->ck * L->ck, 32)));
+    if (L->smem_bytes > 200 * 1024) return tp::fail(TP_E_BAD_ARG, "batch: band too tall for shared memory");
+    int rc = tp::tensor_map(elev, L->par_pitch, L->par_rows, &L->parent_map);
+    if (rc) return rc;
+    if (res) {
+        rc = tp::tensor_map(res, PE, br + 2, &L->res_map);
+        if (rc) return rc;
+    } else {
+        L->res_map = L->parent_map;  // never dereferenced by the kernel without residuals
+    }
     return TP_OK;
 }
 
@@ -300,7 +315,7 @@ extern "C" int tp_elevation_batch(tp_storage *elev, tp_storage *res, tp_storage 
     if (max_depth == 0) {
         L.order = nullptr;
         L.first = 0;
-        L.count = n;
+        L.count = n * L.bands;
         return tp::launch_elevation(L, stream);
     }
     // dependency waves: all jobs of depth d run in one launch, after depth d - 1
@@ -317,8 +332,8 @@ extern "C" int tp_elevation_batch(tp_storage *elev, tp_storage *res, tp_storage 
     // cudaMemcpyAsync from pageable memory has staged it before returning
     L.order = static_cast<const int *>(elev->order_buf);
     for (int d = 0; d <= max_depth; ++d) {
-        L.first = start[d];
-        L.count = start[d + 1] - start[d];
+        L.first = start[d] * L.bands;
+        L.count = (start[d + 1] - start[d]) * L.bands;
         rc = tp::launch_elevation(L, stream);
         if (rc) return rc;
     }
@@ -336,6 +351,24 @@ extern "C" int tp_elevation_batch_device(tp_storage *elev, tp_storage *res, tp_s
     L.jobs = jobs_dev;
     L.order = nullptr;
     L.first = 0;
-    L.count = n;
+    L.count = n * L.bands;
     return tp::launch_elevation(L, stream);
+}
+
+extern "C" int tp_status(int *status, int clear)
+{
+    if (!status) return tp::fail(TP_E_BAD_ARG, "tp_status: status is NULL");
+    return tp::read_status(status, clear != 0);
+}
+
+extern "C" int tp_stream_check(void *stream)
+{
+    cudaError_t e = cudaStreamSynchronize(static_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess) return tp::cuda_fail("cudaStreamSynchronize", e);
+    int st = 0;
+    int rc = tp::read_status(&st, true);
+    if (rc) return rc;
+    if (st == TP_E_TIMEOUT) return tp::fail(TP_E_TIMEOUT, "a device-side wait gave up (status word set)");
+    if (st != 0) return tp::fail(st, "device status word set");
+    return TP_OK;
 }

@@ -1,0 +1,64 @@
+// TMA tensor-map descriptors over tile pools.  The driver entry point is looked
+// up at run time through the CUDA runtime, so the library does not link libcuda.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+#include <cuda_runtime.h>
+
+#include <cstring>
+
+#include "tp_internal.h"
+
+namespace {
+
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn(int *err)
+{
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    static std::once_flag once;
+    static cudaError_t status = cudaSuccess;
+    std::call_once(once, [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        status = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q);
+        if (status == cudaSuccess && q == cudaDriverEntryPointSuccess) fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    });
+    if (!fn) *err = tp::fail(TP_E_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
+    return fn;
+}
+
+}  // namespace
+
+namespace tp {
+
+int tensor_map(tp_storage *s, int box_x, int box_y, const CUtensorMap **out)
+{
+    auto key = std::make_pair(box_x, box_y);
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        auto it = s->maps.find(key);
+        if (it != s->maps.end()) {
+            *out = &it->second;
+            return TP_OK;
+        }
+    }
+    if (box_x < 1 || box_x > 256 || box_y < 1 || box_y > 256 || (box_x * 4) % 16 != 0)
+        return fail(TP_E_BAD_ARG, "tensor map: box outside TMA limits");
+    int err = TP_OK;
+    auto fn = encode_fn(&err);
+    if (!fn) return err;
+    CUtensorMap m;
+    std::memset(&m, 0, sizeof m);
+    cuuint64_t dims[3] = {(cuuint64_t)s->W, (cuuint64_t)s->W, (cuuint64_t)s->capacity * s->channels};
+    cuuint64_t strides[2] = {(cuuint64_t)s->pitch * sizeof(float), (cuuint64_t)s->plane_stride * sizeof(float)};
+    cuuint32_t box[3] = {(cuuint32_t)box_x, (cuuint32_t)box_y, 1};
+    cuuint32_t estr[3] = {1, 1, 1};
+    CUresult r = fn(&m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, s->base, dims, strides, box, estr,
+                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return fail(TP_E_CUDA, "cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")");
+    std::lock_guard<std::mutex> lk(s->mu);
+    auto ins = s->maps.emplace(key, m);
+    *out = &ins.first->second;
+    return TP_OK;
+}
+
+}  // namespace tp

@@ -80,11 +80,16 @@ class TileStorage:
         return out
 
 
-def make_params(grid_size=24, flip=False, no_clamp=False, noise_mode=0, normal_format=2):
+def make_params(grid_size=24, flip=False, no_clamp=False, noise_mode=0, normal_format=2, band_rows=0):
     p = ElevParams()
     p.grid_size, p.flip, p.no_clamp = grid_size, int(flip), int(no_clamp)
-    p.noise_mode, p.normal_format = noise_mode, normal_format
+    p.noise_mode, p.normal_format, p.band_rows = noise_mode, normal_format, band_rows
     return p
+
+
+def stream_check(stream=None):
+    """Synchronises `stream` and raises if a kernel reported a failure."""
+    check(lib().tp_stream_check(stream))
 
 
 def make_job(level, tx, ty, out_slot, parent_slot=-1, residual_slot=-1, rx=0, ry=0,

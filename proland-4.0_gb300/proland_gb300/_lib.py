@@ -47,7 +47,8 @@ class ElevParams(C.Structure):
     """tp_elev_params"""
     _fields_ = [
         ("grid_size", C.c_int32), ("flip", C.c_int32), ("no_clamp", C.c_int32),
-        ("noise_mode", C.c_int32), ("normal_format", C.c_int32), ("reserved", C.c_int32 * 3),
+        ("noise_mode", C.c_int32), ("normal_format", C.c_int32), ("band_rows", C.c_int32),
+        ("reserved", C.c_int32 * 2),
     ]
 
 
@@ -83,6 +84,8 @@ def lib():
         "tp_storage_download": ([_vp, _i, _i, _i, _vp, _vp], _i),
         "tp_elevation_batch": ([_vp, _vp, _vp, C.POINTER(ElevParams), C.POINTER(TileJob), _i, _vp], _i),
         "tp_elevation_batch_device": ([_vp, _vp, _vp, C.POINTER(ElevParams), _vp, _i, _vp], _i),
+        "tp_status": ([C.POINTER(_i), _i], _i),
+        "tp_stream_check": ([_vp], _i),
         "tp_dem_noise": ([_i, _f32p], _i),
         "tp_cnoise": ([C.c_float, C.c_float], C.c_float),
         "tp_noise_select": ([_i, _i, _i, _i, C.POINTER(_i), C.POINTER(_i)], _i),

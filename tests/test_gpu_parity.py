@@ -40,6 +40,7 @@ def run_cases(tp, oracle, cases, params, exact=True, residual_width=None, with_n
                                 rscale=c.rscale, tile_meters=float(c.tile_meters)))
         expect.append(c.oracle(oracle, table, params_dict(params), rot, layer))
     tp.elevation_batch(elev, res, nrm, params, jobs)
+    tp.stream_check()
     zf = elev.download(0, n, tp.ZF)
     zc = elev.download(0, n, tp.ZC)
     zm = elev.download(0, n, tp.ZM)
@@ -69,6 +70,13 @@ def test_stencil_residual_normals(gpu, oracle_lib, W):
     cases = [Case(W, lvl, tx, ty, seed=10 * lvl + tx + 3 * ty)
              for lvl, tx, ty in [(1, 0, 0), (1, 1, 0), (1, 0, 1), (1, 1, 1), (5, 17, 9), (7, 100, 127)]]
     run_cases(gpu, oracle_lib, cases, gpu.make_params())
+
+
+@pytest.mark.parametrize("W,band_rows", [(101, 26), (101, 51), (197, 99), (197, 140), (197, 33)])
+def test_band_heights(gpu, oracle_lib, W, band_rows):
+    """Every band split of a tile produces the same bits (halo rows, window origins)."""
+    cases = [Case(W, lvl, tx, ty, seed=lvl + 5 * tx, noise_amp=-20.0) for lvl, tx, ty in [(1, 1, 0), (4, 7, 12), (0, 0, 0)]]
+    run_cases(gpu, oracle_lib, cases, gpu.make_params(band_rows=band_rows, flip=True))
 
 
 def test_residual_window_mod2(gpu, oracle_lib):
@@ -129,6 +137,7 @@ def test_quadtree_waves(gpu, oracle_lib):
         jobs.append(tp.make_job(l, x, y, out_slot=k, parent_slot=pj, residual_slot=k, normal_slot=k,
                                 tile_meters=50000.0 / (1 << l), parent_job=pj))
     tp.elevation_batch(elev, res, nrm, tp.make_params(), jobs)
+    tp.stream_check()
     zf = elev.download(0, n, tp.ZF)
     zm = elev.download(0, n, tp.ZM)
     nx = nrm.download(0, n, tp.NX)
