@@ -360,7 +360,7 @@ def main():
 
     # end to end through the C ABI with host buffers
     e2e_ms = []
-    for s in range(args.e2e_steps + 2):
+    for s in range(args.e2e_steps + 2 if args.e2e_steps > 0 else 0):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         for fc in classes:
@@ -370,7 +370,7 @@ def main():
         stream.synchronize()
         if s >= 2:
             e2e_ms.append(1000.0 * (time.perf_counter() - t0))
-    e2e_step = float(np.mean(e2e_ms))
+    e2e_step = float(np.mean(e2e_ms)) if e2e_ms else float("nan")
     if world > 1:
         t = torch.tensor([e2e_step], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
