@@ -62,8 +62,10 @@ int tp_storage_delete_slot(tp_storage *s, int slot);
 /* Address of plane `channel` of `slot` (device or pinned host memory). */
 float *tp_storage_plane(tp_storage *s, int slot, int channel);
 /* Copies `count` consecutive slots' plane `channel` from/to a dense host array
- * [count][W][W] (pitch W), asynchronously on `stream`; host memory should be
- * pinned for the copy to overlap. */
+ * [count][W][W] (pitch W), asynchronously on `stream` (one linear host<->device
+ * copy through a staging buffer owned by the storage, repacked on the device);
+ * host memory should be pinned.  Copies of one storage must be issued on one
+ * stream (they share the staging buffer).  Host storages copy synchronously. */
 int tp_storage_upload(tp_storage *s, int first_slot, int count, int channel,
                       const float *host, void *stream);
 int tp_storage_download(tp_storage *s, int first_slot, int count, int channel,
@@ -102,11 +104,12 @@ typedef struct {
     int32_t reserved[2];
 } tp_elev_params;
 
-/* Produces n jobs on `stream`.  `jobs` is host memory; it is copied into a
- * device buffer owned by the storage `elev`.  A job whose parent is produced by
- * an earlier job of the same batch names it in parent_job; such a batch runs in
- * dependency waves (parents before children).  `residuals`/`normals` may be NULL
- * when unused.  One batch per storage and stream at a time. */
+/* Produces n jobs on `stream` in one persistent launch (a one-class frame).
+ * `jobs` is host memory; it is copied into a device buffer owned by the storage
+ * `elev`.  A job whose parent is produced by an earlier job of the same batch
+ * names it in parent_job: the launch orders it after its parent.
+ * `residuals`/`normals` may be NULL when unused.  One batch per storage and
+ * stream at a time. */
 int tp_elevation_batch(tp_storage *elev, tp_storage *residuals, tp_storage *normals,
                        const tp_elev_params *params, const tp_tile_job *jobs, int n,
                        void *stream);
@@ -114,6 +117,32 @@ int tp_elevation_batch(tp_storage *elev, tp_storage *residuals, tp_storage *norm
 int tp_elevation_batch_device(tp_storage *elev, tp_storage *residuals, tp_storage *normals,
                               const tp_elev_params *params, const tp_tile_job *jobs_dev, int n,
                               void *stream);
+
+/* ------------------------------------------------------------------------
+ * Frames: all tile requests of a frame -- for up to two tile widths (e.g. 101
+ * and 197) -- produced by one persistent launch per tile width.  The CTAs take
+ * work units (bands of tiles) from a device counter in list order; a job naming
+ * its parent's job (parent_job, which must come earlier in the same class) waits
+ * on that job's completion counter, so parents are produced before children
+ * inside the launch.  This is the batched form of TileProducer's task graph
+ * (core/.../producer/TileProducer.cpp:749-771, CreateTile::run :199-217).
+ * tp_frame_graph_launch captures the frame (counter reset + launch) into a CUDA
+ * graph on its first call and replays it afterwards; the job arrays are
+ * uploaded once, before the capture.  One frame per stream at a time. */
+typedef struct tp_frame tp_frame;
+int tp_frame_create(tp_frame **out);
+int tp_frame_destroy(tp_frame *f);
+int tp_frame_clear(tp_frame *f);
+int tp_frame_add(tp_frame *f, tp_storage *elev, tp_storage *residuals, tp_storage *normals,
+                 const tp_elev_params *params, const tp_tile_job *jobs, int n);
+/* Same with a job array in device memory, owned by the caller (not validated);
+ * has_dependencies = 0 promises that no job names a parent_job. */
+int tp_frame_add_device(tp_frame *f, tp_storage *elev, tp_storage *residuals, tp_storage *normals,
+                        const tp_elev_params *params, const tp_tile_job *jobs_dev, int n,
+                        int has_dependencies);
+int tp_frame_launch(tp_frame *f, void *stream);
+int tp_frame_graph_launch(tp_frame *f, void *stream);
+int tp_frame_units(const tp_frame *f);   /* work units of one launch */
 
 /* Device status word: TP_OK, or the first TP_E_* code a kernel reported (a
  * dependency or copy wait that gave up).  tp_status reads it (and clears it when

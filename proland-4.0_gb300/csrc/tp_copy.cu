@@ -1,0 +1,75 @@
+// Host <-> slot copies.  A host tile array is dense ([count][W][W], rows of W
+// floats) while slots have a padded pitch; a strided DMA of 400-byte rows runs
+// far below the host link's rate, so one linear copy moves the whole array into
+// a device staging buffer and a kernel (re)packs rows between the staging buffer
+// and the slot planes at HBM speed.
+#include <cuda_runtime.h>
+
+#include "tp_internal.h"
+
+namespace {
+
+// One warp per row: dense row (count * W rows in all) <-> slot plane row.
+__global__ void __launch_bounds__(256) repack_rows(const float *__restrict__ src, float *__restrict__ dst, int W,
+                                                   int pitch, long long slot_stride, long long rows, bool to_slots)
+{
+    const long long row = (long long)blockIdx.x * 8 + (threadIdx.x >> 5);
+    if (row >= rows) return;
+    const int lane = threadIdx.x & 31;
+    const long long tile = row / W;
+    const int r = (int)(row - tile * W);
+    const long long dense = row * W;
+    const long long slot = tile * slot_stride + (long long)r * pitch;
+    if (to_slots) {
+        for (int i = lane; i < W; i += 32) dst[slot + i] = __ldg(src + dense + i);
+    } else {
+        for (int i = lane; i < W; i += 32) dst[dense + i] = __ldg(src + slot + i);
+    }
+}
+
+int ensure_staging(tp_storage *s, size_t bytes)
+{
+    if (s->staging_bytes >= bytes) return TP_OK;
+    if (s->staging) cudaFree(s->staging);
+    s->staging = nullptr;
+    s->staging_bytes = 0;
+    cudaError_t e = cudaMalloc(&s->staging, bytes);
+    if (e != cudaSuccess) return tp::cuda_fail("cudaMalloc (staging)", e);
+    s->staging_bytes = bytes;
+    return TP_OK;
+}
+
+}  // namespace
+
+namespace tp {
+
+int staged_copy(tp_storage *s, int first, int count, int channel, float *host, bool up, void *stream)
+{
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const size_t bytes = sizeof(float) * (size_t)count * s->W * s->W;
+    std::lock_guard<std::mutex> lk(s->copy_mu);
+    int rc = ensure_staging(s, bytes);
+    if (rc) return rc;
+    float *plane = s->base + (long long)first * s->slot_stride + (long long)channel * s->plane_stride;
+    const long long rows = (long long)count * s->W;
+    const unsigned blocks = (unsigned)((rows + 7) / 8);
+    cudaError_t e;
+    if (up) {
+        e = cudaMemcpyAsync(s->staging, host, bytes, cudaMemcpyHostToDevice, st);
+        if (e != cudaSuccess) return cuda_fail("cudaMemcpyAsync (upload)", e);
+        repack_rows<<<blocks, 256, 0, st>>>(static_cast<const float *>(s->staging), plane, s->W, s->pitch,
+                                            s->slot_stride, rows, true);
+    } else {
+        repack_rows<<<blocks, 256, 0, st>>>(plane, static_cast<float *>(s->staging), s->W, s->pitch, s->slot_stride,
+                                            rows, false);
+    }
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail("repack kernel launch", e);
+    if (!up) {
+        e = cudaMemcpyAsync(host, s->staging, bytes, cudaMemcpyDeviceToHost, st);
+        if (e != cudaSuccess) return cuda_fail("cudaMemcpyAsync (download)", e);
+    }
+    return TP_OK;
+}
+
+}  // namespace tp

@@ -1,20 +1,27 @@
-// Fused elevation + normal tile kernel for sm_103a.
+// Persistent, double-buffered elevation + normal tile kernel for sm_103a.
 //
-// Work unit: one band of rows [j0, j1) of one child tile (a whole 101-wide tile,
-// or a quarter of a 197-wide one; the band height is a launch parameter).  Per
-// unit, one thread issues two TMA copies into shared memory, completing on one
-// mbarrier:
-//   * the residual rows [j0 - 1, j1 + 1) of the tile's residual window
-//     (cp.async.bulk.tensor.3d over the residual slot pool), and
-//   * the parent zf window the stencil of those rows reads (over the elevation
-//     slot pool, plane zf of the parent slot);
-// while the copies fly, the other threads fetch the parent zm at the coarse-mesh
-// vertices zc interpolates (a 14 x 14 lattice for the default grid).
-// Phase A then computes zf, zc, zm of rows [j0 - 1, j1] (the band plus one halo
-// row each side), writing the band rows to HBM with 16-byte stores and every
-// row's zm back over its residual in shared memory.  Phase B forms the normals
-// of the band rows from that zm: vertical neighbours from the rows above and
-// below, horizontal neighbours across quad boundaries by warp shuffles.
+// A frame is a list of work units: one band of rows [j0, j1) of one child tile
+// (a whole 101-wide tile, or a quarter of a 197-wide one), for up to two tile
+// widths.  A grid of resident CTAs pulls units from a device counter in frame
+// order; because the host lists parents before children, a unit's parent tile
+// has always been taken by a running CTA, and a per-job completion counter
+// (release on the producer side, acquire + bounded wait on the consumer side)
+// orders a child after its parent inside the single launch.
+//
+// Per unit, one thread issues two TMA copies into a shared-memory stage,
+// completing on that stage's mbarrier:
+//   * the residual rows [j0 - 1, j1 + 1) of the tile's residual window, and
+//   * the parent zf window those rows' stencil reads;
+// every thread adds cp.async copies of the parent zm at the coarse-mesh
+// vertices zc interpolates.  Two stages alternate: the copies of the next unit
+// are in flight while the current one is computed.
+//
+// Phase A computes zf, zc, zm of rows [j0 - 1, j1] (the band plus one halo row
+// each side), writing the band rows to HBM with 16-byte stores and each row's zm
+// over its residual in shared memory; every thread sweeps one column quad down a
+// strip of rows holding the four parent rows its stencil reads in registers.
+// Phase B forms the normals of the band rows from that zm: vertical neighbours
+// from the rows above and below, horizontal ones across quads by warp shuffles.
 //
 // Arithmetic follows the reference exactly:
 //  * stencil: CPUElevationProducer.cpp:202-238 (the same loops as
@@ -31,15 +38,19 @@
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
+#include <mutex>
+#include <type_traits>
+
 #include "tp_internal.h"
 
 __device__ int g_tp_status = 0;  // TP_OK, or the first TP_E_* a kernel reported
 
 namespace {
 
-constexpr int kThreads = 256;
+constexpr int kThreads = tp::kFrameThreads;
 constexpr int kWarps = kThreads / 32;
-constexpr unsigned kWaitLimit = 1u << 22;  // mbarrier polls before a wait is declared failed
+constexpr unsigned kWaitLimit = 1u << 22;   // mbarrier polls before a copy wait is declared failed
+constexpr unsigned kDepLimit = 1u << 22;    // dependency polls (64 ns back-off) before giving up
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p)
 {
@@ -58,6 +69,11 @@ __device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes)
                  : "memory");
 }
 
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar)
+{
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
 __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity)
 {
     uint32_t ok;
@@ -71,7 +87,6 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity)
     return ok != 0;
 }
 
-// Waits for phase `parity` of the barrier with a bounded number of polls.
 __device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity)
 {
     for (unsigned k = 0; k < kWaitLimit; ++k)
@@ -87,44 +102,35 @@ __device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *map, u
         : "memory");
 }
 
+__device__ __forceinline__ void cp_async4(void *dst, const void *src)
+{
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all_but_one() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+
+__device__ __forceinline__ void fence_proxy_async_global()
+{
+    asm volatile("fence.proxy.async.global;" ::: "memory");
+}
+
+__device__ __forceinline__ int ld_acquire(const int *p)
+{
+    int v;
+    asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
 __device__ __forceinline__ int floordiv(int a, int b) { return a >= 0 ? a / b : -((-a + b - 1) / b); }
 __device__ __forceinline__ int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
 
-// floor(a / (2g)) for a grid step g known at compile time (power of two) or not (G == 0)
-template <int G>
-__device__ __forceinline__ int fdiv2g(int a, int g)
+// floor(a / (2g)) and a mod 2g: a shift and a mask when g is a power of two
+// (gshift = log2(2g)), a division otherwise (gshift < 0).
+__device__ __forceinline__ int fdiv2g(int a, int g, int gshift) { return gshift >= 0 ? a >> gshift : floordiv(a, 2 * g); }
+__device__ __forceinline__ int fmod2g(int a, int g, int gshift)
 {
-    if constexpr (G == 4) return a >> 3;
-    else if constexpr (G == 8) return a >> 4;
-    else return floordiv(a, 2 * g);
-}
-template <int G>
-__device__ __forceinline__ int fmod2g(int a, int g)
-{
-    if constexpr (G == 4) return a & 7;
-    else if constexpr (G == 8) return a & 15;
-    else return a - 2 * g * floordiv(a, 2 * g);
-}
-
-// Stencil of one child sample; `c` points at the parent sample (i/2 + px, j/2 + py)
-// in the staged window, `ww` is the window row pitch.
-__device__ __forceinline__ float upsample_at(const float *c, int ww, int i, int j)
-{
-    if ((j & 1) == 0) {
-        if ((i & 1) == 0) return c[0];
-        return __fmul_rn(__fsub_rn(__fmul_rn(__fadd_rn(c[0], c[1]), 9.0f), __fadd_rn(c[-1], c[2])), 0.0625f);
-    }
-    if ((i & 1) == 0)
-        return __fmul_rn(__fsub_rn(__fmul_rn(__fadd_rn(c[0], c[ww]), 9.0f), __fadd_rn(c[-ww], c[2 * ww])), 0.0625f);
-    // odd/odd: the reference sums the 16 products f*g*z one by one, rows outer
-    constexpr float w[4] = {-1.0f / 16.0f, 9.0f / 16.0f, 9.0f / 16.0f, -1.0f / 16.0f};
-    float z = 0.0f;
-#pragma unroll
-    for (int dj = 0; dj < 4; ++dj)
-#pragma unroll
-        for (int di = 0; di < 4; ++di)
-            z = __fadd_rn(z, __fmul_rn(w[dj] * w[di], c[(di - 1) + (dj - 1) * ww]));
-    return z;
+    return gshift >= 0 ? a & ((1 << gshift) - 1) : a - 2 * g * floordiv(a, 2 * g);
 }
 
 // 4x4 operators of the modulated-noise shader, entry k weighing parent sample
@@ -160,7 +166,7 @@ __device__ __forceinline__ float mdot16(const float *cz, const float *M)
     return s;
 }
 
-__device__ __noinline__ float demo_modulation(const float *cz, int mi, float mps)
+__device__ __forceinline__ float demo_modulation(const float *cz, int mi, float mps)
 {
     float sx = mdot16(cz, c_slopex[mi]);
     float sy = mdot16(cz, c_slopey[mi]);
@@ -176,216 +182,427 @@ __device__ __noinline__ float demo_modulation(const float *cz, int mi, float mps
 
 __device__ __forceinline__ void report(int code) { atomicCAS(&g_tp_status, 0, code); }
 
-template <int G>
-__global__ void __launch_bounds__(kThreads, 3)
-elevation_kernel(const __grid_constant__ CUtensorMap parent_map, const __grid_constant__ CUtensorMap res_map,
-                 const tp::ElevLaunch a)
-{
-    extern __shared__ __align__(128) unsigned char smem_raw[];
-    __shared__ uint64_t bar;
-    // TMA destinations on 128-byte boundaries (the launch adds 128 bytes of slack)
-    const uint32_t raw = smem_u32(smem_raw);
-    float *sbuf = reinterpret_cast<float *>(smem_raw + (((raw + 127u) & ~127u) - raw));  // residual rows, then zm rows
-    float *spar = sbuf + a.buf_floats;                      // parent zf window
-    float *scoarse = spar + a.par_floats;                   // parent zm at the coarse-mesh vertices
+// A unit as decoded by thread 0 and shared with the CTA.
+struct UnitInfo {
+    int valid;    // 0: past the end of the frame
+    int job;      // job index
+    int band;
+};
 
-    const int unit = a.first + blockIdx.x;
-    const int jslot = unit / a.bands;
-    const int band = unit - jslot * a.bands;
-    const int jidx = a.order ? a.order[jslot] : jslot;
-    const tp_tile_job &J = a.jobs[jidx];
-    const int W = a.W, n = W - 5, PE = a.pitch, g = G ? G : a.g;
-    const int level = J.level, tx = J.tx, ty = J.ty;
-    const int dx = (tx & 1) * (n / 2), dy = (ty & 1) * (n / 2);
-    const bool has_parent = level > 0, has_res = J.residual_slot >= 0;
-    const int j0 = (band * W) / a.bands, j1 = ((band + 1) * W) / a.bands;
+// Thread 0: wait (bounded) until the parent job's bands are complete, then issue
+// the TMA copies of unit (job, band) into `stage`, completing on `bar`.
+__device__ void issue_copies(const tp::ClassLaunch &c, const CUtensorMap *pmap, const CUtensorMap *rmap, int job,
+                             int band, float *stage, uint64_t *bar)
+{
+    const tp_tile_job &J = c.jobs[job];
+    if (J.parent_job >= 0) {
+        unsigned k = 0;
+        while (ld_acquire(c.done + J.parent_job) < c.bands) {
+            if (++k > kDepLimit) {
+                report(TP_E_TIMEOUT);
+                break;
+            }
+            __nanosleep(64);
+        }
+        fence_proxy_async_global();  // the parent's generic-proxy writes before our async-proxy reads
+    }
+    const int n = c.W - 5;
+    const int dx = (J.tx & 1) * (n / 2), dy = (J.ty & 1) * (n / 2);
+    const int j0 = (band * c.W) / c.bands;
+    const int ja = max(j0 - 1, 0);
+    const bool has_parent = J.level > 0, has_res = J.residual_slot >= 0;
+    uint32_t bytes = 0;
+    if (has_res) bytes += c.res_box_bytes;
+    if (has_parent) bytes += c.par_box_bytes;
+    if (bytes == 0) {
+        mbar_arrive(bar);
+        return;
+    }
+    mbar_expect_tx(bar, bytes);
+    if (has_res) tma_load_3d(stage, rmap, bar, J.rx, J.ry + j0 - 1, J.residual_slot);
+    if (has_parent) tma_load_3d(stage + c.buf_floats, pmap, bar, dx, ja / 2 + dy, J.parent_slot * 3 + 0);
+}
+
+// All threads: cp.async copies of the coarse-mesh lattice (parent zm) of a job.
+__device__ __forceinline__ void issue_lattice(const tp::ClassLaunch &c, int job, float *stage)
+{
+    const tp_tile_job &J = c.jobs[job];
+    if (J.level <= 0) return;
+    const int W = c.W, n = W - 5;
+    const int dx = (J.tx & 1) * (n / 2), dy = (J.ty & 1) * (n / 2);
+    const float *pzm = c.elev + (long long)J.parent_slot * c.slot_stride + 2 * c.plane_stride;
+    float *lat = stage + c.buf_floats + c.par_floats;
+    for (int t = threadIdx.x; t < c.ck * c.ck; t += kThreads) {
+        const int ky = t / c.ck - 1, kx = t - (ky + 1) * c.ck - 1;
+        const int X = clampi(2 + dx + c.g * kx, 0, W - 1), Y = clampi(2 + dy + c.g * ky, 0, W - 1);
+        cp_async4(lat + t, pzm + (long long)Y * c.pitch + X);
+    }
+}
+
+// All threads: produce unit (job, band) from `stage` (its copies complete).
+// MOD: the class uses the slope/curvature-modulated noise (a separate kernel
+// instantiation keeps its 4x4 neighbourhood out of the common path's registers).
+template <bool MOD>
+__device__ __forceinline__ void compute_unit(const tp::ClassLaunch &c, int job, int band, float *stage)
+{
+    const tp_tile_job J = c.jobs[job];
+    const int W = c.W, n = W - 5, PE = c.pitch, g = c.g, gs = c.gshift;
+    const int dx = (J.tx & 1) * (n / 2), dy = (J.ty & 1) * (n / 2);
+    const bool has_parent = J.level > 0, has_res = J.residual_slot >= 0;
+    const int j0 = (band * W) / c.bands, j1 = ((band + 1) * W) / c.bands;
     const int ja = max(j0 - 1, 0), jb = min(j1, W - 1);
     const int pr0 = ja / 2 + dy;  // first parent row of the window
+    float *sbuf = stage;                        // residual rows, then zm rows
+    const float *spar = stage + c.buf_floats;   // parent zf window
+    const float *slat = spar + c.par_floats;    // parent zm at the coarse-mesh vertices
 
-    // ---- issue the copies
-    if (threadIdx.x == 0) {
-        mbar_init(&bar, 1);
-        uint32_t bytes = 0;
-        if (has_res) bytes += a.res_box_bytes;
-        if (has_parent) bytes += a.par_box_bytes;
-        mbar_expect_tx(&bar, bytes);
-        if (has_res) tma_load_3d(sbuf, &res_map, &bar, J.rx, J.ry + j0 - 1, J.residual_slot);
-        if (has_parent) tma_load_3d(spar, &parent_map, &bar, dx, pr0, J.parent_slot * 3 + 0);
-    }
-    // coarse-mesh vertices (parent zm, CLAMP_TO_EDGE) with plain loads meanwhile
-    if (has_parent) {
-        const float *pzm = a.elev + (long long)J.parent_slot * a.slot_stride + 2 * a.plane_stride;
-        for (int t = threadIdx.x; t < a.ck * a.ck; t += kThreads) {
-            const int ky = t / a.ck - 1, kx = t - (ky + 1) * a.ck - 1;
-            const int X = clampi(2 + dx + g * kx, 0, W - 1), Y = clampi(2 + dy + g * ky, 0, W - 1);
-            scoarse[t] = __ldg(pzm + (long long)Y * PE + X);
-        }
-    }
-    __syncthreads();  // barrier initialised, coarse lattice written
-    if (has_res || has_parent) {
-        if (!mbar_wait_bounded(&bar, 0)) {
-            report(TP_E_TIMEOUT);
-            mbar_wait_bounded(&bar, 0);  // give the copies a second chance to land before leaving
-            return;
-        }
-    }
-    if (!has_res) {
-        for (int t = threadIdx.x; t < a.buf_floats; t += kThreads) sbuf[t] = 0.0f;
-        __syncthreads();
-    }
-
-    // ---- phase A: elevation of rows [ja, jb], quads of 4 samples
+    // ---- phase A: elevation of rows [ja, jb].  Thread t sweeps one column quad
+    // (4 samples) down a strip of S rows (S even, so every lane of a warp sees the
+    // same row parity), keeping the four parent rows its stencil reads in
+    // registers: one new parent row (5 samples) per two child rows.
     const int NQ = PE / 4;
-    float *ozf = a.elev + (long long)J.out_slot * a.slot_stride;
-    float *ozc = ozf + a.plane_stride;
-    float *ozm = ozf + 2 * a.plane_stride;
-    const bool noisy = J.noise_amp != 0.0f;
-    const __half *nz_base = a.noise + (long long)(J.noise_rot * 6 + J.noise_layer) * W * PE;
-    const float abs_amp = fabsf(J.noise_amp);
-    const int nitems = (jb - ja + 1) * NQ;
-    for (int it = threadIdx.x; it < nitems; it += kThreads) {
-        const int rr = it / NQ, q = it - rr * NQ;
-        const int j = ja + rr, i0 = 4 * q;
-        float *brow = sbuf + (j - j0 + 1) * PE;
-        const float4 r4 = *reinterpret_cast<const float4 *>(brow + i0);
-        const float rv[4] = {r4.x, r4.y, r4.z, r4.w};
-        float nv[4] = {0.0f, 0.0f, 0.0f, 0.0f};
-        if (noisy) {
-            const uint2 h = __ldg(reinterpret_cast<const uint2 *>(nz_base + (long long)j * PE + i0));
-            const float2 n01 = __half22float2(*reinterpret_cast<const __half2 *>(&h.x));
-            const float2 n23 = __half22float2(*reinterpret_cast<const __half2 *>(&h.y));
-            nv[0] = n01.x; nv[1] = n01.y; nv[2] = n23.x; nv[3] = n23.y;
-        }
-        const float *prow = spar + (j / 2 + 1 + dy - pr0) * a.par_pitch;
-        const int cy = j - 2;
-        const int kyr = fdiv2g<G>(cy + g, g) + 1, kyf = fdiv2g<G>(cy, g) + 1;
-        const bool flip_row = a.flip && fmod2g<G>(cy, g) == g;
-        float vf[4], vc[4], vm[4];
+    const int nseg = max(1, kThreads / NQ);
+    const int nrows = jb - ja + 1;
+    const int S = ((nrows + nseg - 1) / nseg + 1) & ~1;
+    if (threadIdx.x < NQ * nseg) {
+        const int q = threadIdx.x % NQ, seg = threadIdx.x / NQ;
+        const int i0 = 4 * q;
+        const int rbeg = ja + seg * S, rend = min(rbeg + S, jb + 1);
+        float *ozf = c.elev + (long long)J.out_slot * c.slot_stride + i0;
+        const long long pstride = c.plane_stride;
+        const bool noisy = J.noise_amp != 0.0f;
+        const bool modulated = MOD && J.noise_amp > 0.0f;
+        const __half *nz = c.noise + (long long)(J.noise_rot * 6 + J.noise_layer) * W * PE + i0;
+        // zf + |amp| N (terrain1), or zf - amp N (modulated shader, amp < 0): -(amp N) == (-amp) N exactly
+        const float namp = c.noise_mode == 0 ? fabsf(J.noise_amp) : -J.noise_amp;
+        const float rscale = J.rscale;
+        // coarse-mesh lattice columns of the quad's samples: for g >= 2 four
+        // consecutive columns span at most two lattice cells, (A, B) with a selector
+        // (g == 1 falls back to per-sample lattice reads)
+        const int xr0 = fdiv2g(min(i0, W - 1) - 2 + g, g, gs) + 1, xr3 = fdiv2g(min(i0 + 3, W - 1) - 2 + g, g, gs) + 1;
+        const int xf0 = fdiv2g(min(i0, W - 1) - 2, g, gs) + 1, xf3 = fdiv2g(min(i0 + 3, W - 1) - 2, g, gs) + 1;
+        unsigned selr = 0, self_ = 0, fmask = 0;  // bit k: sample k uses cell B / is a flip column
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
-            const int i = min(i0 + k, W - 1);
-            float zf = has_res ? __fmul_rn(J.rscale, rv[k]) : 0.0f;
-            if (noisy) {
-                if (a.noise_mode == 0) {
-                    zf = __fadd_rn(zf, __fmul_rn(abs_amp, nv[k]));
-                } else if (J.noise_amp < 0.0f) {
-                    zf = __fsub_rn(zf, __fmul_rn(J.noise_amp, nv[k]));
-                } else {
-                    float cz[16];
+            const int cx = min(i0 + k, W - 1) - 2;
+            if (fdiv2g(cx + g, g, gs) + 1 != xr0) selr |= 1u << k;
+            if (fdiv2g(cx, g, gs) + 1 != xf0) self_ |= 1u << k;
+            if (c.flip && fmod2g(cx, g, gs) == g) fmask |= 1u << k;
+        }
+        const bool two_cells = g >= 2;
+        float P[4][5];
+        int wr0 = -1000;
+        const float *pcol = spar + 2 * q;
+        auto load_row = [&](float(&dst)[5], int r) {
+            const float *src = pcol + r * c.par_pitch;
+            const float2 a01 = *reinterpret_cast<const float2 *>(src);
+            const float2 a23 = *reinterpret_cast<const float2 *>(src + 2);
+            dst[0] = a01.x; dst[1] = a01.y; dst[2] = a23.x; dst[3] = a23.y; dst[4] = src[4];
+        };
+        auto advance = [&](int pc) {
+            if (wr0 == pc - 1) return;
+            if (wr0 + 1 == pc - 1) {
 #pragma unroll
-                    for (int t = 0; t < 16; ++t) {
-                        const int X = clampi(i / 2 + dx + t % 4, 0, W - 1) - dx;
-                        const int Y = clampi(j / 2 + dy + t / 4, 0, W - 1) - pr0;
-                        cz[t] = has_parent ? spar[Y * a.par_pitch + X] : 0.0f;
-                    }
+                for (int cc = 0; cc < 5; ++cc) { P[0][cc] = P[1][cc]; P[1][cc] = P[2][cc]; P[2][cc] = P[3][cc]; }
+                load_row(P[3], pc + 2);
+            } else {
+                load_row(P[0], pc - 1);
+                load_row(P[1], pc);
+                load_row(P[2], pc + 1);
+                load_row(P[3], pc + 2);
+            }
+            wr0 = pc - 1;
+        };
+        auto row = [&](int j, auto odd_tag) {
+            constexpr bool ODD = decltype(odd_tag)::value;
+            float *brow = sbuf + (j - j0 + 1) * PE + i0;
+            const float4 r4 = *reinterpret_cast<const float4 *>(brow);
+            float zf[4];
+            zf[0] = has_res ? __fmul_rn(rscale, r4.x) : 0.0f;
+            zf[1] = has_res ? __fmul_rn(rscale, r4.y) : 0.0f;
+            zf[2] = has_res ? __fmul_rn(rscale, r4.z) : 0.0f;
+            zf[3] = has_res ? __fmul_rn(rscale, r4.w) : 0.0f;
+            if (noisy) {
+                const uint2 h = __ldg(reinterpret_cast<const uint2 *>(nz + j * PE));
+                const float2 n01 = __half22float2(*reinterpret_cast<const __half2 *>(&h.x));
+                const float2 n23 = __half22float2(*reinterpret_cast<const __half2 *>(&h.y));
+                const float nv[4] = {n01.x, n01.y, n23.x, n23.y};
+                if (!MOD || !modulated) {
+#pragma unroll
+                    for (int k = 0; k < 4; ++k) zf[k] = __fadd_rn(zf[k], __fmul_rn(namp, nv[k]));
+                } else if constexpr (MOD) {
                     const float mps = __fdiv_rn(J.tile_meters, (float)n);
-                    const float m = demo_modulation(cz, (i & 1) + 2 * (j & 1), mps);
-                    zf = __fadd_rn(zf, __fmul_rn(__fmul_rn(m, J.noise_amp), nv[k]));
+#pragma unroll 1
+                    for (int k = 0; k < 4; ++k) {
+                        const int i = i0 + k;
+                        float cz[16];
+#pragma unroll
+                        for (int t = 0; t < 16; ++t) {
+                            const int X = clampi(i / 2 + dx + t % 4, 0, W - 1) - dx;
+                            const int Y = clampi(j / 2 + dy + t / 4, 0, W - 1) - pr0;
+                            cz[t] = has_parent ? spar[Y * c.par_pitch + X] : 0.0f;
+                        }
+                        const float m = demo_modulation(cz, (i & 1) + 2 * (j & 1), mps);
+                        zf[k] = __fadd_rn(zf[k], __fmul_rn(__fmul_rn(m, J.noise_amp), nv[k]));
+                    }
                 }
             }
-            float zc = zf;
+            float zc[4] = {zf[0], zf[1], zf[2], zf[3]};
             if (has_parent) {
-                zf = __fadd_rn(zf, upsample_at(prow + (i / 2 + 1), a.par_pitch, i, j));
-                const int cx = i - 2;
-                const int kxr = fdiv2g<G>(cx + g, g) + 1, kxf = fdiv2g<G>(cx, g) + 1;
-                const float zc1 = scoarse[kyf * a.ck + kxr];
-                const float zc3 = scoarse[kyr * a.ck + kxf];
-                if (flip_row && fmod2g<G>(cx, g) == g) {
-                    const float zc0 = scoarse[kyf * a.ck + kxf];
-                    const float zc2 = scoarse[kyr * a.ck + kxr];
-                    const float s13 = __fadd_rn(zc3, zc1), s02 = __fadd_rn(zc0, zc2);
-                    zc = __fmul_rn(s13 >= s02 ? __fadd_rn(zc1, zc3) : s02, 0.5f);
+                float up[4];
+                if constexpr (!ODD) {
+                    up[0] = P[1][1];
+                    up[1] = __fmul_rn(__fsub_rn(__fmul_rn(__fadd_rn(P[1][1], P[1][2]), 9.0f), __fadd_rn(P[1][0], P[1][3])), 0.0625f);
+                    up[2] = P[1][2];
+                    up[3] = __fmul_rn(__fsub_rn(__fmul_rn(__fadd_rn(P[1][2], P[1][3]), 9.0f), __fadd_rn(P[1][1], P[1][4])), 0.0625f);
                 } else {
-                    zc = __fmul_rn(__fadd_rn(zc1, zc3), 0.5f);
+                    up[0] = __fmul_rn(__fsub_rn(__fmul_rn(__fadd_rn(P[1][1], P[2][1]), 9.0f), __fadd_rn(P[0][1], P[3][1])), 0.0625f);
+                    up[2] = __fmul_rn(__fsub_rn(__fmul_rn(__fadd_rn(P[1][2], P[2][2]), 9.0f), __fadd_rn(P[0][2], P[3][2])), 0.0625f);
+                    // odd/odd: the reference sums the 16 products f*g*z one by one, rows outer
+                    constexpr float w[4] = {-1.0f / 16.0f, 9.0f / 16.0f, 9.0f / 16.0f, -1.0f / 16.0f};
+                    float z1 = 0.0f, z3 = 0.0f;
+#pragma unroll
+                    for (int dj = 0; dj < 4; ++dj)
+#pragma unroll
+                        for (int di = 0; di < 4; ++di) {
+                            z1 = __fadd_rn(z1, __fmul_rn(w[dj] * w[di], P[dj][di]));
+                            z3 = __fadd_rn(z3, __fmul_rn(w[dj] * w[di], P[dj][di + 1]));
+                        }
+                    up[1] = z1;
+                    up[3] = z3;
+                }
+                const int cy = j - 2;
+                const int yr = (fdiv2g(cy + g, g, gs) + 1) * c.ck, yf = (fdiv2g(cy, g, gs) + 1) * c.ck;
+                const bool frow = c.flip && fmod2g(cy, g, gs) == g;
+                float r1[4], r3[4];
+                if (two_cells) {
+                    const float a1 = slat[yf + xr0], b1 = slat[yf + xr3];
+                    const float a3 = slat[yr + xf0], b3 = slat[yr + xf3];
+#pragma unroll
+                    for (int k = 0; k < 4; ++k) {
+                        r1[k] = (selr >> k) & 1u ? b1 : a1;
+                        r3[k] = (self_ >> k) & 1u ? b3 : a3;
+                    }
+                } else {
+#pragma unroll
+                    for (int k = 0; k < 4; ++k) {
+                        const int cx = min(i0 + k, W - 1) - 2;
+                        r1[k] = slat[yf + fdiv2g(cx + g, g, gs) + 1];
+                        r3[k] = slat[yr + fdiv2g(cx, g, gs) + 1];
+                    }
+                }
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    zf[k] = __fadd_rn(zf[k], up[k]);
+                    if (frow && ((fmask >> k) & 1u)) {
+                        const int cx = min(i0 + k, W - 1) - 2;
+                        const int xr = fdiv2g(cx + g, g, gs) + 1, xf = fdiv2g(cx, g, gs) + 1;
+                        const float zc0 = slat[yf + xf];
+                        const float zc2 = slat[yr + xr];
+                        const float s13 = __fadd_rn(r3[k], r1[k]), s02 = __fadd_rn(zc0, zc2);
+                        zc[k] = __fmul_rn(s13 >= s02 ? __fadd_rn(r1[k], r3[k]) : s02, 0.5f);
+                    } else {
+                        zc[k] = __fmul_rn(__fadd_rn(r1[k], r3[k]), 0.5f);
+                    }
                 }
             }
-            const float zm = a.no_clamp ? zf : (zf > 0.0f ? zf : 0.0f);
-            const bool pad = i0 + k >= W;
-            vf[k] = pad ? 0.0f : zf;
-            vc[k] = pad ? 0.0f : zc;
-            vm[k] = pad ? 0.0f : zm;
+            float vf[4], vc[4], vm[4];
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const bool pad = i0 + k >= W;
+                const float zm = c.no_clamp ? zf[k] : (zf[k] > 0.0f ? zf[k] : 0.0f);
+                vf[k] = pad ? 0.0f : zf[k];
+                vc[k] = pad ? 0.0f : zc[k];
+                vm[k] = pad ? 0.0f : zm;
+            }
+            if (j >= j0 && j < j1) {
+                float *o = ozf + j * PE;
+                *reinterpret_cast<float4 *>(o) = make_float4(vf[0], vf[1], vf[2], vf[3]);
+                *reinterpret_cast<float4 *>(o + pstride) = make_float4(vc[0], vc[1], vc[2], vc[3]);
+                *reinterpret_cast<float4 *>(o + 2 * pstride) = make_float4(vm[0], vm[1], vm[2], vm[3]);
+            }
+            *reinterpret_cast<float4 *>(brow) = make_float4(vm[0], vm[1], vm[2], vm[3]);
+        };
+        using Even = std::integral_constant<bool, false>;
+        using Odd = std::integral_constant<bool, true>;
+#pragma unroll 1
+        for (int j = rbeg; j < rend; ++j) {
+            if (has_parent) advance(j / 2 + 1 + dy - pr0);  // (even, odd) rows share the stencil centre row
+            if (j & 1) row(j, Odd{});
+            else row(j, Even{});
         }
-        if (j >= j0 && j < j1) {
-            const long long o = (long long)j * PE + i0;
-            *reinterpret_cast<float4 *>(ozf + o) = make_float4(vf[0], vf[1], vf[2], vf[3]);
-            *reinterpret_cast<float4 *>(ozc + o) = make_float4(vc[0], vc[1], vc[2], vc[3]);
-            *reinterpret_cast<float4 *>(ozm + o) = make_float4(vm[0], vm[1], vm[2], vm[3]);
-        }
-        *reinterpret_cast<float4 *>(brow + i0) = make_float4(vm[0], vm[1], vm[2], vm[3]);
     }
-    if (a.nrm == nullptr || J.normal_slot < 0) return;
     __syncthreads();
 
     // ---- phase B: normals of rows jn in [max(j0, 2), min(j1, W - 2)), one warp per row
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int Wn = W - 4, NQn = a.nrm_pitch / 4;
-    float *onx = a.nrm + (long long)J.normal_slot * a.nrm_slot_stride;
-    float *ony = onx + a.nrm_plane_stride;
-    const float h2 = __fmul_rn(2.0f, __fdiv_rn(J.tile_meters, (float)n));
-    const float hh = h2 * h2;
-    for (int jn = max(j0, 2) + warp; jn < min(j1, W - 2); jn += kWarps) {
-        const float *c = sbuf + (jn - j0 + 1) * PE;
-        const float *up = c + PE, *dn = c - PE;
-        for (int base = 0; base < NQn; base += 32) {
-            const int m = base + lane;
-            const bool act = m < NQn;
-            const int e = act ? 4 * m + 2 : 2;  // elevation column of this quad's first normal
-            const float2 c01 = *reinterpret_cast<const float2 *>(c + e);
-            const float2 c23 = *reinterpret_cast<const float2 *>(c + e + 2);
-            const float2 u01 = *reinterpret_cast<const float2 *>(up + e);
-            const float2 u23 = *reinterpret_cast<const float2 *>(up + e + 2);
-            const float2 d01 = *reinterpret_cast<const float2 *>(dn + e);
-            const float2 d23 = *reinterpret_cast<const float2 *>(dn + e + 2);
-            // horizontal neighbours e - 1 and e + 4 live in the adjacent lanes' quads
-            float left = __shfl_up_sync(0xffffffffu, c23.y, 1);
-            float right = __shfl_down_sync(0xffffffffu, c01.x, 1);
-            if (lane == 0) left = c[e - 1];
-            if (lane == 31 || m == NQn - 1) right = c[min(e + 4, PE - 1)];
-            const float zc_[6] = {left, c01.x, c01.y, c23.x, c23.y, right};
-            const float zu[4] = {u01.x, u01.y, u23.x, u23.y};
-            const float zd[4] = {d01.x, d01.y, d23.x, d23.y};
-            float nx[4], ny[4];
+    if (c.nrm != nullptr && J.normal_slot >= 0) {
+        const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+        const int Wn = W - 4, NQn = c.nrm_pitch / 4;
+        float *onx = c.nrm + (long long)J.normal_slot * c.nrm_slot_stride;
+        float *ony = onx + c.nrm_plane_stride;
+        const float h2 = __fmul_rn(2.0f, __fdiv_rn(J.tile_meters, (float)n));
+        const float hh = h2 * h2;
+        for (int jn = max(j0, 2) + warp; jn < min(j1, W - 2); jn += kWarps) {
+            const float *cr = sbuf + (jn - j0 + 1) * PE;
+            const float *up = cr + PE, *dn = cr - PE;
+            for (int base = 0; base < NQn; base += 32) {
+                const int m = base + lane;
+                const bool act = m < NQn;
+                const int e = act ? 4 * m + 2 : 2;  // elevation column of this quad's first normal
+                const float2 c01 = *reinterpret_cast<const float2 *>(cr + e);
+                const float2 c23 = *reinterpret_cast<const float2 *>(cr + e + 2);
+                const float2 u01 = *reinterpret_cast<const float2 *>(up + e);
+                const float2 u23 = *reinterpret_cast<const float2 *>(up + e + 2);
+                const float2 d01 = *reinterpret_cast<const float2 *>(dn + e);
+                const float2 d23 = *reinterpret_cast<const float2 *>(dn + e + 2);
+                // horizontal neighbours e - 1 and e + 4 live in the adjacent lanes' quads
+                float left = __shfl_up_sync(0xffffffffu, c23.y, 1);
+                float right = __shfl_down_sync(0xffffffffu, c01.x, 1);
+                if (lane == 0) left = cr[e - 1];
+                if (lane == 31 || m == NQn - 1) right = cr[min(e + 4, PE - 1)];
+                const float zr[6] = {left, c01.x, c01.y, c23.x, c23.y, right};
+                const float zu[4] = {u01.x, u01.y, u23.x, u23.y};
+                const float zd[4] = {d01.x, d01.y, d23.x, d23.y};
+                float nx[4], ny[4];
 #pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                const float ax = -__fsub_rn(zc_[k + 2], zc_[k]);
-                const float ay = -__fsub_rn(zu[k], zd[k]);
-                const float inv = rsqrtf(ax * ax + ay * ay + hh);
-                const bool pad = 4 * m + k >= Wn;
-                nx[k] = pad ? 0.0f : ax * inv;
-                ny[k] = pad ? 0.0f : ay * inv;
-            }
-            if (act) {
-                const long long o = (long long)(jn - 2) * a.nrm_pitch + 4 * m;
-                *reinterpret_cast<float4 *>(onx + o) = make_float4(nx[0], nx[1], nx[2], nx[3]);
-                *reinterpret_cast<float4 *>(ony + o) = make_float4(ny[0], ny[1], ny[2], ny[3]);
+                for (int k = 0; k < 4; ++k) {
+                    const float ax = -__fsub_rn(zr[k + 2], zr[k]);
+                    const float ay = -__fsub_rn(zu[k], zd[k]);
+                    const float inv = rsqrtf(ax * ax + ay * ay + hh);
+                    const bool pad = 4 * m + k >= Wn;
+                    nx[k] = pad ? 0.0f : ax * inv;
+                    ny[k] = pad ? 0.0f : ay * inv;
+                }
+                if (act) {
+                    const int o = (jn - 2) * c.nrm_pitch + 4 * m;
+                    *reinterpret_cast<float4 *>(onx + o) = make_float4(nx[0], nx[1], nx[2], nx[3]);
+                    *reinterpret_cast<float4 *>(ony + o) = make_float4(ny[0], ny[1], ny[2], ny[3]);
+                }
             }
         }
     }
 }
 
-template <int G>
-int launch_g(const tp::ElevLaunch &a, cudaStream_t s)
+template <int MINB, bool MOD>
+__global__ void __launch_bounds__(kThreads, MINB)
+frame_kernel(const __grid_constant__ CUtensorMap pmap, const __grid_constant__ CUtensorMap rmap,
+             const tp::FrameLaunch f)
 {
-    const size_t smem = a.smem_bytes + 128;
-    cudaError_t e = cudaFuncSetAttribute(elevation_kernel<G>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return tp::cuda_fail("cudaFuncSetAttribute", e);
-    elevation_kernel<G><<<a.count, kThreads, smem, s>>>(*a.parent_map, *a.res_map, a);
-    e = cudaGetLastError();
-    if (e != cudaSuccess) return tp::cuda_fail("elevation kernel launch", e);
-    return TP_OK;
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    __shared__ uint64_t bar;
+    __shared__ UnitInfo info;
+    __shared__ int timed_out;
+    const uint32_t raw = smem_u32(smem_raw);
+    float *const stage = reinterpret_cast<float *>(smem_raw + (((raw + 127u) & ~127u) - raw));
+    const tp::ClassLaunch &c = f.c;
+    const int units = c.njobs * c.bands;
+
+    if (threadIdx.x == 0) {
+        timed_out = 0;
+        mbar_init(&bar, 1);
+    }
+    for (uint32_t phase = 0;; phase ^= 1u) {
+        // take the next unit; its parent was taken earlier by a running CTA, so
+        // waiting for it (bounded) cannot deadlock
+        if (threadIdx.x == 0) {
+            UnitInfo x{0, 0, 0};
+            const int u = atomicAdd(f.counter, 1);
+            if (u < units) {
+                x.valid = 1;
+                x.job = u / c.bands;
+                x.band = u - x.job * c.bands;
+                issue_copies(c, &pmap, &rmap, x.job, x.band, stage, &bar);
+            }
+            info = x;
+        }
+        __syncthreads();
+        const UnitInfo x = info;
+        if (!x.valid) break;
+        issue_lattice(c, x.job, stage);
+        cp_async_commit();
+        // warp 0 polls the mbarrier; the other warps wait at the CTA barrier below
+        if (threadIdx.x < 32) {
+            if (!mbar_wait_bounded(&bar, phase)) {
+                report(TP_E_TIMEOUT);
+                mbar_wait_bounded(&bar, phase);  // the copies get a second chance to land
+                timed_out = 1;
+            }
+        }
+        cp_async_wait_all();
+        const bool no_res = c.jobs[x.job].residual_slot < 0;
+        __syncthreads();
+        if (timed_out) break;
+        if (no_res) {
+            for (int t = threadIdx.x; t < c.buf_floats; t += kThreads) stage[t] = 0.0f;
+            __syncthreads();
+        }
+        compute_unit<MOD>(c, x.job, x.band, stage);
+        if (f.any_deps) fence_proxy_async_global();
+        __syncthreads();  // the stage is free again; all of this unit's stores are issued
+        if (f.any_deps && threadIdx.x == 0) {
+            __threadfence();
+            atomicAdd(c.done + x.job, 1);  // release: this band of the tile is complete
+        }
+    }
+    cp_async_wait_all();
 }
 
 }  // namespace
 
 namespace tp {
 
-int launch_elevation(const ElevLaunch &a, void *stream)
+static size_t frame_smem(int stage_floats) { return sizeof(float) * (size_t)stage_floats + 128; }
+
+template <int MINB, bool MOD>
+static int ensure_smem_attr(size_t smem)
 {
-    if (a.count <= 0) return TP_OK;
+    static std::mutex mu;
+    static size_t have = 0;
+    std::lock_guard<std::mutex> lk(mu);
+    if (smem <= have) return TP_OK;
+    cudaError_t e = cudaFuncSetAttribute(frame_kernel<MINB, MOD>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return cuda_fail("cudaFuncSetAttribute", e);
+    have = smem;
+    return TP_OK;
+}
+
+template <int MINB, bool MOD>
+static int launch_variant(const FrameLaunch &f, const CUtensorMap *pmap, const CUtensorMap *rmap, int grid,
+                          cudaStream_t s)
+{
+    const size_t smem = frame_smem(f.stage_floats);
+    int rc = ensure_smem_attr<MINB, MOD>(smem);
+    if (rc) return rc;
+    frame_kernel<MINB, MOD><<<grid, kThreads, smem, s>>>(*pmap, *rmap, f);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail("frame kernel launch", e);
+    return TP_OK;
+}
+
+int launch_frame(const FrameLaunch &f, const CUtensorMap *pmap, const CUtensorMap *rmap, int grid, void *stream)
+{
+    if (f.c.njobs <= 0) return TP_OK;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
-    if (a.g == 4) return launch_g<4>(a, s);
-    if (a.g == 8) return launch_g<8>(a, s);
-    return launch_g<0>(a, s);
+    const bool mod = f.c.noise_mode == 1;
+    if (f.minb >= 3) return mod ? launch_variant<3, true>(f, pmap, rmap, grid, s) : launch_variant<3, false>(f, pmap, rmap, grid, s);
+    return mod ? launch_variant<2, true>(f, pmap, rmap, grid, s) : launch_variant<2, false>(f, pmap, rmap, grid, s);
+}
+
+template <int MINB, bool MOD>
+static int occupancy_variant(int stage_floats, int *blocks_per_sm)
+{
+    const size_t smem = frame_smem(stage_floats);
+    int rc = ensure_smem_attr<MINB, MOD>(smem);
+    if (rc) return rc;
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, frame_kernel<MINB, MOD>, kThreads, smem);
+    if (e != cudaSuccess) return cuda_fail("cudaOccupancyMaxActiveBlocksPerMultiprocessor", e);
+    return TP_OK;
+}
+
+int frame_occupancy(int stage_floats, int minb, bool mod, int *blocks_per_sm)
+{
+    if (minb >= 3) return mod ? occupancy_variant<3, true>(stage_floats, blocks_per_sm) : occupancy_variant<3, false>(stage_floats, blocks_per_sm);
+    return mod ? occupancy_variant<2, true>(stage_floats, blocks_per_sm) : occupancy_variant<2, false>(stage_floats, blocks_per_sm);
 }
 
 int read_status(int *status, bool clear)

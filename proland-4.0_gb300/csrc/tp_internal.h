@@ -37,13 +37,14 @@ struct tp_storage {
     std::vector<int> free_list;  // stack of free slot indices
     std::vector<uint8_t> in_use;
     std::mutex mu;
-    // device scratch for job arrays of batches produced into this storage
-    void *job_buf = nullptr;
-    size_t job_buf_bytes = 0;
-    void *order_buf = nullptr;
-    size_t order_buf_bytes = 0;
+    // frame reused by the batch calls that produce into this storage
+    struct tp_frame *batch_frame = nullptr;
     // TMA descriptors over this pool, by box (width, height)
     std::map<std::pair<int, int>, CUtensorMap> maps;
+    // device staging buffer of host <-> slot copies
+    void *staging = nullptr;
+    size_t staging_bytes = 0;
+    std::mutex copy_mu;
 };
 
 namespace tp {
@@ -60,31 +61,45 @@ void build_dem_noise(int W, float *out);
 // z: slot * channels + channel), cached on the storage.
 int tensor_map(tp_storage *s, int box_x, int box_y, const CUtensorMap **out);
 
-struct ElevLaunch {
+constexpr int kFrameThreads = 256;
+
+// One tile width of a frame, as the persistent kernel sees it.
+struct ClassLaunch {
     const tp_tile_job *jobs;  // device
-    const int *order;         // device, or nullptr for identity
-    int first, count;         // units (job slot * bands + band)
+    int njobs;
     int bands;                // row bands per tile
+    int *done;                // per-job count of completed bands (device)
     float *elev;
     int W, pitch;
     long long plane_stride, slot_stride;
-    const float *res;
     float *nrm;
     int nrm_pitch;
     long long nrm_plane_stride, nrm_slot_stride;
     const __half *noise;
-    int g, flip, no_clamp, noise_mode;
-    // shared-memory layout of a unit
+    int g, gshift, flip, no_clamp, noise_mode;
+    // shared-memory layout of a unit within a stage
     int buf_floats;           // (band rows + 2) * pitch, rounded to 128 bytes
     int par_pitch, par_rows;  // parent zf window
     int par_floats;
     int ck;                   // coarse-mesh lattice side
     uint32_t res_box_bytes, par_box_bytes;
-    int smem_bytes;
-    const CUtensorMap *parent_map, *res_map;
 };
 
-int launch_elevation(const ElevLaunch &a, void *stream);
+// One persistent launch: the jobs of one tile width.
+struct FrameLaunch {
+    ClassLaunch c;
+    int *counter;             // next unit to take (device)
+    int stage_floats;         // shared-memory stage of one unit
+    int any_deps;             // some job waits on a parent produced in this launch
+    int minb;                 // kernel variant: CTAs per SM the register budget targets (2 or 3)
+};
+
+int launch_frame(const FrameLaunch &f, const CUtensorMap *pmap, const CUtensorMap *rmap, int grid, void *stream);
+int frame_occupancy(int stage_floats, int minb, bool mod, int *blocks_per_sm);
+
+// Copies `count` slots' plane `channel` between a dense host array and the slots
+// through the storage's staging buffer (one linear copy + a repack kernel).
+int staged_copy(tp_storage *s, int first, int count, int channel, float *host, bool up, void *stream);
 int read_status(int *status, bool clear);
 
 }  // namespace tp

@@ -85,8 +85,8 @@ extern "C" int tp_storage_destroy(tp_storage *s)
         if (s->on_device) cudaFree(s->base);
         else cudaFreeHost(s->base);
     }
-    if (s->job_buf) cudaFree(s->job_buf);
-    if (s->order_buf) cudaFree(s->order_buf);
+    if (s->batch_frame) tp_frame_destroy(s->batch_frame);
+    if (s->staging) cudaFree(s->staging);
     delete s;
     return TP_OK;
 }
@@ -135,23 +135,16 @@ static int storage_copy(tp_storage *s, int first, int count, int channel, float 
 {
     if (!s || !host || first < 0 || count < 1 || first + count > s->capacity || channel < 0 || channel >= s->channels)
         return tp::fail(TP_E_BAD_ARG, "tp_storage copy: bad range");
-    if (count == 0) return TP_OK;
-    float *dev = s->base + (long long)first * s->slot_stride + (long long)channel * s->plane_stride;
-    cudaMemcpy3DParms p;
-    std::memset(&p, 0, sizeof p);
-    cudaPitchedPtr hp = make_cudaPitchedPtr(host, sizeof(float) * s->W, s->W, s->W);
-    cudaPitchedPtr dp = make_cudaPitchedPtr(dev, sizeof(float) * s->pitch, s->W, (size_t)s->W * s->channels);
-    if (up) {
-        p.srcPtr = hp;
-        p.dstPtr = dp;
-    } else {
-        p.srcPtr = dp;
-        p.dstPtr = hp;
+    if (s->on_device) return tp::staged_copy(s, first, count, channel, host, up, stream);
+    // host storage: plain pitched copy on the calling thread
+    for (int t = 0; t < count; ++t) {
+        float *plane = s->base + (long long)(first + t) * s->slot_stride + (long long)channel * s->plane_stride;
+        for (int r = 0; r < s->W; ++r) {
+            float *dense = host + ((size_t)t * s->W + r) * s->W;
+            if (up) std::memcpy(plane + (size_t)r * s->pitch, dense, sizeof(float) * s->W);
+            else std::memcpy(dense, plane + (size_t)r * s->pitch, sizeof(float) * s->W);
+        }
     }
-    p.extent = make_cudaExtent(sizeof(float) * s->W, s->W, count);
-    p.kind = cudaMemcpyDefault;
-    cudaError_t e = cudaMemcpy3DAsync(&p, static_cast<cudaStream_t>(stream));
-    if (e != cudaSuccess) return tp::cuda_fail("cudaMemcpy3DAsync", e);
     return TP_OK;
 }
 
@@ -163,196 +156,6 @@ extern "C" int tp_storage_upload(tp_storage *s, int first_slot, int count, int c
 extern "C" int tp_storage_download(tp_storage *s, int first_slot, int count, int channel, float *host, void *stream)
 {
     return storage_copy(s, first_slot, count, channel, host, false, stream);
-}
-
-// ---------------------------------------------------------------- batch
-static int ensure_buffer(void **buf, size_t *have, size_t need)
-{
-    if (*have >= need) return TP_OK;
-    if (*buf) cudaFree(*buf);
-    *buf = nullptr;
-    *have = 0;
-    size_t sz = std::max(need, (size_t)4096);
-    cudaError_t e = cudaMalloc(buf, sz);
-    if (e != cudaSuccess) return tp::cuda_fail("cudaMalloc (job buffer)", e);
-    *have = sz;
-    return TP_OK;
-}
-
-static int check_params(tp_storage *elev, tp_storage *res, tp_storage *nrm, const tp_elev_params *p,
-                        tp::ElevLaunch *L)
-{
-    if (!elev || !p) return tp::fail(TP_E_BAD_ARG, "batch: elevation storage and params are required");
-    if (!elev->on_device || elev->channels != 3)
-        return tp::fail(TP_E_BAD_ARG, "batch: elevation storage must be a device storage with 3 channels");
-    const int W = elev->W, n = W - 5;
-    if (n < 8 || n % 8 != 0) return tp::fail(TP_E_BAD_ARG, "batch: tile width must be 8k + 5");
-    if (W > 253) return tp::fail(TP_E_BAD_ARG, "batch: tile width above 253 is not supported");
-    if (p->grid_size < 1 || n % p->grid_size != 0)
-        return tp::fail(TP_E_BAD_ARG, "batch: grid_size must divide the tile size");
-    if (p->noise_mode != 0 && p->noise_mode != 1) return tp::fail(TP_E_BAD_ARG, "batch: bad noise_mode");
-    if (res) {
-        if (!res->on_device || res->channels != 1) return tp::fail(TP_E_BAD_ARG, "batch: residual storage must be 1-channel device storage");
-        if ((res->W - 5) % n != 0) return tp::fail(TP_E_BAD_ARG, "batch: residual tile size must be a multiple of the tile size");
-    }
-    if (nrm) {
-        if (!nrm->on_device || nrm->channels != 2 || nrm->W != W - 4)
-            return tp::fail(TP_E_BAD_ARG, "batch: normal storage must be 2-channel device storage of width W - 4");
-        if (p->normal_format != 2) return tp::fail(TP_E_BAD_ARG, "batch: only normal format 2 (signed fp32) is supported");
-    }
-    const int g = n / p->grid_size;
-    std::memset(L, 0, sizeof *L);
-    L->elev = elev->base;
-    L->W = W;
-    L->pitch = elev->pitch;
-    L->plane_stride = elev->plane_stride;
-    L->slot_stride = elev->slot_stride;
-    if (res) L->res = res->base;
-    if (nrm) {
-        L->nrm = nrm->base;
-        L->nrm_pitch = nrm->pitch;
-        L->nrm_plane_stride = nrm->plane_stride;
-        L->nrm_slot_stride = nrm->slot_stride;
-    }
-    int err = TP_OK;
-    L->noise = tp::device_noise_table(W, &err);
-    if (!L->noise) return err;
-    L->g = g;
-    L->flip = p->flip ? 1 : 0;
-    L->no_clamp = p->no_clamp ? 1 : 0;
-    L->noise_mode = p->noise_mode;
-    // band height: whole 101-wide tiles, quarters of 197-wide ones, unless asked
-    int br = p->band_rows > 0 ? p->band_rows : (W <= 128 ? W : (W + 3) / 4);
-    br = std::min(std::max(br, 8), W);
-    L->bands = (W + br - 1) / br;
-    br = (W + L->bands - 1) / L->bands;          // the tallest band actually launched
-    if (br + 2 > 256) return tp::fail(TP_E_BAD_ARG, "batch: band taller than a TMA box");
-    const int PE = elev->pitch;
-    L->buf_floats = tp::round_up((br + 2) * PE, 32);
-    // parent zf window: columns [d, d + n/2 + 5] (stencil and modulated-noise taps),
-    // rows from the first computed row's parent row, (br + 1)/2 + 5 of them
-    L->par_pitch = tp::round_up(n / 2 + 6, 4);
-    L->par_rows = (br + 1) / 2 + 5;
-    if (L->par_pitch > 256 || L->par_rows > 256) return tp::fail(TP_E_BAD_ARG, "batch: parent window above a TMA box");
-    L->par_floats = tp::round_up(L->par_pitch * L->par_rows, 32);
-    const int kmax = (n + 2 + g) / (2 * g);     // largest coarse-mesh index of a sample
-    L->ck = kmax + 2;
-    L->res_box_bytes = (uint32_t)(sizeof(float) * PE * (br + 2));
-    L->par_box_bytes = (uint32_t)(sizeof(float) * L->par_pitch * L->par_rows);
-    L->smem_bytes = (int)(sizeof(float) * ((size_t)L->buf_floats + L->par_floats + tp::round_up(L->ck * L->ck, 32)));
-    if (L->smem_bytes > 200 * 1024) return tp::fail(TP_E_BAD_ARG, "batch: band too tall for shared memory");
-    int rc = tp::tensor_map(elev, L->par_pitch, L->par_rows, &L->parent_map);
-    if (rc) return rc;
-    if (res) {
-        rc = tp::tensor_map(res, PE, br + 2, &L->res_map);
-        if (rc) return rc;
-    } else {
-        L->res_map = L->parent_map;  // never dereferenced by the kernel without residuals
-    }
-    return TP_OK;
-}
-
-static int check_job(const tp_storage *elev, const tp_storage *res, const tp_storage *nrm, const tp_tile_job &j,
-                     int index, int n)
-{
-    const int W = elev->W, ts = W - 5;
-    char buf[160];
-    auto bad = [&](const char *what) {
-        snprintf(buf, sizeof buf, "batch: job %d (level %d, %d, %d): %s", index, j.level, j.tx, j.ty, what);
-        return tp::fail(TP_E_BAD_ARG, buf);
-    };
-    if (j.level < 0 || j.level > 30 || j.tx < 0 || j.ty < 0 || (j.tx >> j.level) != 0 || (j.ty >> j.level) != 0)
-        return bad("bad quadtree coordinates");
-    if (j.out_slot < 0 || j.out_slot >= elev->capacity) return bad("bad out_slot");
-    if (j.level > 0) {
-        if (j.parent_slot < 0 || j.parent_slot >= elev->capacity) {
-            snprintf(buf, sizeof buf, "batch: job %d (level %d, %d, %d): parent tile missing", index, j.level, j.tx, j.ty);
-            return tp::fail(TP_E_MISSING_PARENT, buf);
-        }
-        if (j.parent_slot == j.out_slot) return bad("parent_slot == out_slot");
-    }
-    if (j.parent_job >= index || j.parent_job < -1 || j.parent_job >= n) return bad("parent_job must precede the job");
-    if (j.residual_slot >= 0) {
-        if (!res || j.residual_slot >= res->capacity) return bad("bad residual_slot");
-        if (j.rx < 0 || j.ry < 0 || j.rx % ts != 0 || j.ry % ts != 0 || j.rx + W > res->W || j.ry + W > res->W)
-            return bad("residual window outside the residual tile");
-    }
-    if (j.normal_slot >= 0 && (!nrm || j.normal_slot >= nrm->capacity)) return bad("bad normal_slot");
-    if (j.noise_layer < 0 || j.noise_layer > 5 || j.noise_rot < 0 || j.noise_rot > 3) return bad("bad noise layer / rotation");
-    if (!(j.tile_meters > 0.0f)) return bad("tile_meters must be positive");
-    return TP_OK;
-}
-
-extern "C" int tp_elevation_batch(tp_storage *elev, tp_storage *res, tp_storage *nrm, const tp_elev_params *params,
-                                  const tp_tile_job *jobs, int n, void *stream)
-{
-    tp::ElevLaunch L;
-    int rc = check_params(elev, res, nrm, params, &L);
-    if (rc) return rc;
-    if (n < 0 || (n > 0 && !jobs)) return tp::fail(TP_E_BAD_ARG, "batch: bad job array");
-    if (n == 0) return TP_OK;
-    std::vector<int> depth(n, 0);
-    int max_depth = 0;
-    for (int k = 0; k < n; ++k) {
-        rc = check_job(elev, res, nrm, jobs[k], k, n);
-        if (rc) return rc;
-        if (jobs[k].parent_job >= 0) {
-            const tp_tile_job &pj = jobs[jobs[k].parent_job];
-            if (pj.out_slot != jobs[k].parent_slot || pj.level != jobs[k].level - 1 || pj.tx != jobs[k].tx / 2 ||
-                pj.ty != jobs[k].ty / 2)
-                return tp::fail(TP_E_BAD_ARG, "batch: parent_job does not produce the parent tile");
-            depth[k] = depth[jobs[k].parent_job] + 1;
-            max_depth = std::max(max_depth, depth[k]);
-        }
-    }
-    cudaStream_t s = static_cast<cudaStream_t>(stream);
-    std::lock_guard<std::mutex> lk(elev->mu);
-    rc = ensure_buffer(&elev->job_buf, &elev->job_buf_bytes, sizeof(tp_tile_job) * n);
-    if (rc) return rc;
-    cudaError_t e = cudaMemcpyAsync(elev->job_buf, jobs, sizeof(tp_tile_job) * n, cudaMemcpyHostToDevice, s);
-    if (e != cudaSuccess) return tp::cuda_fail("cudaMemcpyAsync (jobs)", e);
-    L.jobs = static_cast<const tp_tile_job *>(elev->job_buf);
-    if (max_depth == 0) {
-        L.order = nullptr;
-        L.first = 0;
-        L.count = n * L.bands;
-        return tp::launch_elevation(L, stream);
-    }
-    // dependency waves: all jobs of depth d run in one launch, after depth d - 1
-    std::vector<int> order(n), start(max_depth + 2, 0);
-    for (int k = 0; k < n; ++k) start[depth[k] + 1]++;
-    for (int d = 0; d <= max_depth; ++d) start[d + 1] += start[d];
-    std::vector<int> fill(start.begin(), start.end() - 1);
-    for (int k = 0; k < n; ++k) order[fill[depth[k]]++] = k;
-    rc = ensure_buffer(&elev->order_buf, &elev->order_buf_bytes, sizeof(int) * n);
-    if (rc) return rc;
-    e = cudaMemcpyAsync(elev->order_buf, order.data(), sizeof(int) * n, cudaMemcpyHostToDevice, s);
-    if (e != cudaSuccess) return tp::cuda_fail("cudaMemcpyAsync (order)", e);
-    // the host vector must outlive the asynchronous copy from pageable memory:
-    // cudaMemcpyAsync from pageable memory has staged it before returning
-    L.order = static_cast<const int *>(elev->order_buf);
-    for (int d = 0; d <= max_depth; ++d) {
-        L.first = start[d] * L.bands;
-        L.count = (start[d + 1] - start[d]) * L.bands;
-        rc = tp::launch_elevation(L, stream);
-        if (rc) return rc;
-    }
-    return TP_OK;
-}
-
-extern "C" int tp_elevation_batch_device(tp_storage *elev, tp_storage *res, tp_storage *nrm,
-                                         const tp_elev_params *params, const tp_tile_job *jobs_dev, int n,
-                                         void *stream)
-{
-    tp::ElevLaunch L;
-    int rc = check_params(elev, res, nrm, params, &L);
-    if (rc) return rc;
-    if (n < 0 || (n > 0 && !jobs_dev)) return tp::fail(TP_E_BAD_ARG, "batch: bad job array");
-    L.jobs = jobs_dev;
-    L.order = nullptr;
-    L.first = 0;
-    L.count = n * L.bands;
-    return tp::launch_elevation(L, stream);
 }
 
 extern "C" int tp_status(int *status, int clear)

@@ -118,6 +118,47 @@ def elevation_batch_device(elev, residuals, normals, params, jobs_dev_ptr, n, st
                                           jobs_dev_ptr, n, stream))
 
 
+class Frame:
+    """All requests of a frame (up to two tile widths) produced by one persistent
+    launch, optionally replayed from a CUDA graph (tp_frame_*)."""
+
+    def __init__(self):
+        h = C.c_void_p()
+        check(lib().tp_frame_create(C.byref(h)))
+        self.handle = h
+        self._keep = []
+
+    def close(self):
+        if self.handle:
+            lib().tp_frame_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def add(self, elev, residuals, normals, params, jobs):
+        arr = (TileJob * len(jobs))(*jobs)
+        check(lib().tp_frame_add(self.handle, elev.handle, residuals.handle if residuals else None,
+                                 normals.handle if normals else None, C.byref(params), arr, len(jobs)))
+
+    def add_device(self, elev, residuals, normals, params, jobs_dev_ptr, n, has_dependencies=True):
+        check(lib().tp_frame_add_device(self.handle, elev.handle, residuals.handle if residuals else None,
+                                        normals.handle if normals else None, C.byref(params), jobs_dev_ptr, n,
+                                        int(has_dependencies)))
+
+    def launch(self, stream=None):
+        check(lib().tp_frame_launch(self.handle, stream))
+
+    def graph_launch(self, stream=None):
+        check(lib().tp_frame_graph_launch(self.handle, stream))
+
+    def units(self):
+        return check(lib().tp_frame_units(self.handle))
+
+
 def dem_noise(tile_width):
     out = np.empty((6, tile_width, tile_width), np.float32)
     check(lib().tp_dem_noise(tile_width, out.ctypes.data_as(C.POINTER(C.c_float))))

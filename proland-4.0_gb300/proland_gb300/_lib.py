@@ -84,6 +84,14 @@ def lib():
         "tp_storage_download": ([_vp, _i, _i, _i, _vp, _vp], _i),
         "tp_elevation_batch": ([_vp, _vp, _vp, C.POINTER(ElevParams), C.POINTER(TileJob), _i, _vp], _i),
         "tp_elevation_batch_device": ([_vp, _vp, _vp, C.POINTER(ElevParams), _vp, _i, _vp], _i),
+        "tp_frame_create": ([C.POINTER(_vp)], _i),
+        "tp_frame_destroy": ([_vp], _i),
+        "tp_frame_clear": ([_vp], _i),
+        "tp_frame_add": ([_vp, _vp, _vp, _vp, C.POINTER(ElevParams), C.POINTER(TileJob), _i], _i),
+        "tp_frame_add_device": ([_vp, _vp, _vp, _vp, C.POINTER(ElevParams), _vp, _i, _i], _i),
+        "tp_frame_launch": ([_vp, _vp], _i),
+        "tp_frame_graph_launch": ([_vp, _vp], _i),
+        "tp_frame_units": ([_vp], _i),
         "tp_status": ([C.POINTER(_i), _i], _i),
         "tp_stream_check": ([_vp], _i),
         "tp_dem_noise": ([_i, _f32p], _i),

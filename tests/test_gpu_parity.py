@@ -176,3 +176,64 @@ def test_errors(gpu):
     with pytest.raises(tp.TPError) as e:
         tp.elevation_batch(elev, None, None, tp.make_params(grid_size=7), [tp.make_job(0, 0, 0, out_slot=0)])
     assert e.value.code == tp.TP_E_BAD_ARG
+
+
+def _class_setup(tp, orc, W, specs, seed):
+    """Storages, jobs and oracle outputs of one tile width for a frame."""
+    cases = [Case(W, lvl, tx, ty, seed=seed + 7 * k, noise_amp=a) for k, (lvl, tx, ty, a) in enumerate(specs)]
+    n = len(cases)
+    elev = tp.TileStorage(W, 3, 2 * n)
+    res = tp.TileStorage(W, 1, n)
+    nrm = tp.TileStorage(W - 4, 2, n)
+    table = orc.dem_noise(W)
+    jobs, expect = [], []
+    params = tp.make_params(flip=True)
+    for k, c in enumerate(cases):
+        ps = -1
+        if c.level > 0:
+            ps = n + k
+            elev.upload(ps, tp.ZF, c.parent_zf[None])
+            elev.upload(ps, tp.ZM, c.parent_zm[None])
+        res.upload(k, 0, c.residual[None])
+        rot, layer = tp.noise_select(1, c.level, c.tx, c.ty)
+        jobs.append(tp.make_job(c.level, c.tx, c.ty, out_slot=k, parent_slot=ps, residual_slot=k, normal_slot=k,
+                                noise_rot=rot, noise_layer=layer, noise_amp=c.noise_amp,
+                                tile_meters=float(c.tile_meters)))
+        expect.append(c.oracle(orc, table, params_dict(params), rot, layer))
+    return dict(elev=elev, res=res, nrm=nrm, jobs=jobs, expect=expect, params=params, n=n)
+
+
+def _check_class(tp, k):
+    n = k["n"]
+    zf = k["elev"].download(0, n, tp.ZF)
+    zc = k["elev"].download(0, n, tp.ZC)
+    nx = k["nrm"].download(0, n, tp.NX)
+    for i, (ezf, ezc, ezm, enx, eny) in enumerate(k["expect"]):
+        assert np.array_equal(zf[i], ezf), "zf of job %d" % i
+        assert np.array_equal(zc[i], ezc), "zc of job %d" % i
+        assert_normals_close(nx[i], enx, "nx of job %d" % i)
+
+
+def test_frame_two_widths_one_launch_and_graph(gpu, oracle_lib):
+    """101- and 197-wide tiles in one persistent launch, then the same frame
+    replayed from its CUDA graph (outputs cleared in between)."""
+    tp, orc = gpu, oracle_lib
+    a = _class_setup(tp, orc, 101, [(1, 0, 1, -140.0), (3, 5, 2, 5.0), (6, 40, 33, 0.0), (2, 3, 3, -15.0)], 100)
+    b = _class_setup(tp, orc, 197, [(2, 1, 2, -100.0), (5, 17, 30, 1.5), (1, 1, 1, 0.0)], 200)
+    f = tp.Frame()
+    for k in (a, b):
+        f.add(k["elev"], k["res"], k["nrm"], k["params"], k["jobs"])
+    assert f.units() == 4 * 1 + 3 * 4
+    f.launch()
+    tp.stream_check()
+    _check_class(tp, a)
+    _check_class(tp, b)
+    for k in (a, b):
+        W, n = k["elev"].tile_size, k["n"]
+        for c in (tp.ZF, tp.ZC, tp.ZM):
+            k["elev"].upload(0, c, np.zeros((n, W, W), np.float32))
+    for _ in range(3):
+        f.graph_launch()
+    tp.stream_check()
+    _check_class(tp, a)
+    _check_class(tp, b)
