@@ -324,6 +324,9 @@ def main():
         frame.add_device(fc.elev, fc.res, fc.nrm, params, C.c_void_p(fc.dev_jobs.data_ptr()), fc.n,
                          has_dependencies=False)
 
+    frame.autotune(sh, repeats=5)
+    tuned = {"W%d" % fc.W: frame.config(i) for i, fc in enumerate(classes)}
+
     def step(events=None):
         if events is not None:
             events[0][0].record(stream)
@@ -403,7 +406,7 @@ def main():
                                % (tiles, sum(fc.n for fc in classes if fc.W == 101),
                                   sum(fc.n for fc in classes if fc.W == 197)),
                    "form": "plain", "l2": "inputs larger than L2 (%.2f GB per step)" % (sum(alg.values()) / 1e9),
-                   "parallelism": "replicas" if world > 1 else "single GPU"},
+                   "parallelism": "replicas" if world > 1 else "single GPU", "autotuned": tuned},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": traffic, "peak_source": peak_src, "kernel": "frame_kernel (one persistent launch per tile width, replayed from a CUDA graph)",
                      "kernel_ms": kernel_ms, "units_per_launch": frame.units(),

@@ -101,7 +101,8 @@ typedef struct {
     int32_t noise_mode;     /* 0: zf += |amp| N (terrain1 shader); 1: slope/curvature modulated (demo shader) */
     int32_t normal_format;  /* 2: two signed fp32 planes (the only one supported by the batch kernel) */
     int32_t band_rows;      /* rows per kernel work unit; 0 picks the tuned default */
-    int32_t reserved[2];
+    int32_t stages;         /* shared-memory stages per CTA: 1, or 2 to prefetch the next unit (0: 1) */
+    int32_t reserved;
 } tp_elev_params;
 
 /* Produces n jobs on `stream` in one persistent launch (a one-class frame).
@@ -143,6 +144,12 @@ int tp_frame_add_device(tp_frame *f, tp_storage *elev, tp_storage *residuals, tp
 int tp_frame_launch(tp_frame *f, void *stream);
 int tp_frame_graph_launch(tp_frame *f, void *stream);
 int tp_frame_units(const tp_frame *f);   /* work units of one launch */
+/* Autotuner: times each tile width's launch under every candidate work-unit
+ * shape -- band height (whole tile vs 2..6 bands), one or two shared-memory
+ * stages per CTA, two or three CTAs per SM -- `repeats` times each, on the
+ * frame's own inputs (its outputs are rewritten), and keeps the fastest. */
+int tp_frame_autotune(tp_frame *f, void *stream, int repeats);
+int tp_frame_config(const tp_frame *f, int klass, int *band_rows, int *stages, int *ctas_per_sm);
 
 /* Device status word: TP_OK, or the first TP_E_* code a kernel reported (a
  * dependency or copy wait that gave up).  tp_status reads it (and clears it when

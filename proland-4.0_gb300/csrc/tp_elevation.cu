@@ -38,6 +38,7 @@
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
+#include <map>
 #include <mutex>
 #include <type_traits>
 
@@ -279,15 +280,19 @@ __device__ __forceinline__ void compute_unit(const tp::ClassLaunch &c, int job, 
         // coarse-mesh lattice columns of the quad's samples: for g >= 2 four
         // consecutive columns span at most two lattice cells, (A, B) with a selector
         // (g == 1 falls back to per-sample lattice reads)
-        const int xr0 = fdiv2g(min(i0, W - 1) - 2 + g, g, gs) + 1, xr3 = fdiv2g(min(i0 + 3, W - 1) - 2 + g, g, gs) + 1;
-        const int xf0 = fdiv2g(min(i0, W - 1) - 2, g, gs) + 1, xf3 = fdiv2g(min(i0 + 3, W - 1) - 2, g, gs) + 1;
-        unsigned selr = 0, self_ = 0, fmask = 0;  // bit k: sample k uses cell B / is a flip column
+        // packed in one register: xr0 | xr3 << 8 | xf0 << 16 | xf3 << 24 (lattice sides <= 255)
+        uint32_t xcells;
+        unsigned selr = 0, self_ = 0;  // bit k: sample k uses cell B
+        {
+            const int xr0 = fdiv2g(min(i0, W - 1) - 2 + g, g, gs) + 1, xr3 = fdiv2g(min(i0 + 3, W - 1) - 2 + g, g, gs) + 1;
+            const int xf0 = fdiv2g(min(i0, W - 1) - 2, g, gs) + 1, xf3 = fdiv2g(min(i0 + 3, W - 1) - 2, g, gs) + 1;
+            xcells = (uint32_t)xr0 | ((uint32_t)xr3 << 8) | ((uint32_t)xf0 << 16) | ((uint32_t)xf3 << 24);
 #pragma unroll
-        for (int k = 0; k < 4; ++k) {
-            const int cx = min(i0 + k, W - 1) - 2;
-            if (fdiv2g(cx + g, g, gs) + 1 != xr0) selr |= 1u << k;
-            if (fdiv2g(cx, g, gs) + 1 != xf0) self_ |= 1u << k;
-            if (c.flip && fmod2g(cx, g, gs) == g) fmask |= 1u << k;
+            for (int k = 0; k < 4; ++k) {
+                const int cx = min(i0 + k, W - 1) - 2;
+                if (fdiv2g(cx + g, g, gs) + 1 != xr0) selr |= 1u << k;
+                if (fdiv2g(cx, g, gs) + 1 != xf0) self_ |= 1u << k;
+            }
         }
         const bool two_cells = g >= 2;
         float P[4][5];
@@ -313,17 +318,18 @@ __device__ __forceinline__ void compute_unit(const tp::ClassLaunch &c, int job, 
             }
             wr0 = pc - 1;
         };
-        auto row = [&](int j, auto odd_tag) {
+        const bool edge = i0 + 3 >= W;  // the quad holding the last sample column and the padding
+        auto row = [&](int j, const uint2 h, auto odd_tag) {
             constexpr bool ODD = decltype(odd_tag)::value;
             float *brow = sbuf + (j - j0 + 1) * PE + i0;
             const float4 r4 = *reinterpret_cast<const float4 *>(brow);
+            // (a tile without residual has a zeroed buffer: rscale * 0 == 0)
             float zf[4];
-            zf[0] = has_res ? __fmul_rn(rscale, r4.x) : 0.0f;
-            zf[1] = has_res ? __fmul_rn(rscale, r4.y) : 0.0f;
-            zf[2] = has_res ? __fmul_rn(rscale, r4.z) : 0.0f;
-            zf[3] = has_res ? __fmul_rn(rscale, r4.w) : 0.0f;
+            zf[0] = __fmul_rn(rscale, r4.x);
+            zf[1] = __fmul_rn(rscale, r4.y);
+            zf[2] = __fmul_rn(rscale, r4.z);
+            zf[3] = __fmul_rn(rscale, r4.w);
             if (noisy) {
-                const uint2 h = __ldg(reinterpret_cast<const uint2 *>(nz + j * PE));
                 const float2 n01 = __half22float2(*reinterpret_cast<const __half2 *>(&h.x));
                 const float2 n23 = __half22float2(*reinterpret_cast<const __half2 *>(&h.y));
                 const float nv[4] = {n01.x, n01.y, n23.x, n23.y};
@@ -376,8 +382,8 @@ __device__ __forceinline__ void compute_unit(const tp::ClassLaunch &c, int job, 
                 const bool frow = c.flip && fmod2g(cy, g, gs) == g;
                 float r1[4], r3[4];
                 if (two_cells) {
-                    const float a1 = slat[yf + xr0], b1 = slat[yf + xr3];
-                    const float a3 = slat[yr + xf0], b3 = slat[yr + xf3];
+                    const float a1 = slat[yf + (int)(xcells & 255u)], b1 = slat[yf + (int)((xcells >> 8) & 255u)];
+                    const float a3 = slat[yr + (int)((xcells >> 16) & 255u)], b3 = slat[yr + (int)(xcells >> 24)];
 #pragma unroll
                     for (int k = 0; k < 4; ++k) {
                         r1[k] = (selr >> k) & 1u ? b1 : a1;
@@ -394,8 +400,9 @@ __device__ __forceinline__ void compute_unit(const tp::ClassLaunch &c, int job, 
 #pragma unroll
                 for (int k = 0; k < 4; ++k) {
                     zf[k] = __fadd_rn(zf[k], up[k]);
-                    if (frow && ((fmask >> k) & 1u)) {
-                        const int cx = min(i0 + k, W - 1) - 2;
+                    const int cxk = min(i0 + k, W - 1) - 2;
+                    if (frow && fmod2g(cxk, g, gs) == g) {
+                        const int cx = cxk;
                         const int xr = fdiv2g(cx + g, g, gs) + 1, xf = fdiv2g(cx, g, gs) + 1;
                         const float zc0 = slat[yf + xf];
                         const float zc2 = slat[yr + xr];
@@ -409,11 +416,14 @@ __device__ __forceinline__ void compute_unit(const tp::ClassLaunch &c, int job, 
             float vf[4], vc[4], vm[4];
 #pragma unroll
             for (int k = 0; k < 4; ++k) {
-                const bool pad = i0 + k >= W;
-                const float zm = c.no_clamp ? zf[k] : (zf[k] > 0.0f ? zf[k] : 0.0f);
-                vf[k] = pad ? 0.0f : zf[k];
-                vc[k] = pad ? 0.0f : zc[k];
-                vm[k] = pad ? 0.0f : zm;
+                vf[k] = zf[k];
+                vc[k] = zc[k];
+                vm[k] = c.no_clamp ? zf[k] : (zf[k] > 0.0f ? zf[k] : 0.0f);
+            }
+            if (edge) {
+#pragma unroll
+                for (int k = 1; k < 4; ++k)
+                    if (i0 + k >= W) vf[k] = vc[k] = vm[k] = 0.0f;
             }
             if (j >= j0 && j < j1) {
                 float *o = ozf + j * PE;
@@ -425,11 +435,16 @@ __device__ __forceinline__ void compute_unit(const tp::ClassLaunch &c, int job, 
         };
         using Even = std::integral_constant<bool, false>;
         using Odd = std::integral_constant<bool, true>;
+        // noise rows come from L2: the next row's quad is fetched one row ahead
+        uint2 nzh = make_uint2(0u, 0u);
+        if (noisy && rbeg < rend) nzh = __ldg(reinterpret_cast<const uint2 *>(nz + rbeg * PE));
 #pragma unroll 1
         for (int j = rbeg; j < rend; ++j) {
+            const uint2 h = nzh;
+            if (noisy && j + 1 < rend) nzh = __ldg(reinterpret_cast<const uint2 *>(nz + (j + 1) * PE));
             if (has_parent) advance(j / 2 + 1 + dy - pr0);  // (even, odd) rows share the stencil centre row
-            if (j & 1) row(j, Odd{});
-            else row(j, Even{});
+            if (j & 1) row(j, h, Odd{});
+            else row(j, h, Even{});
         }
     }
     __syncthreads();
@@ -455,11 +470,13 @@ __device__ __forceinline__ void compute_unit(const tp::ClassLaunch &c, int job, 
                 const float2 u23 = *reinterpret_cast<const float2 *>(up + e + 2);
                 const float2 d01 = *reinterpret_cast<const float2 *>(dn + e);
                 const float2 d23 = *reinterpret_cast<const float2 *>(dn + e + 2);
-                // horizontal neighbours e - 1 and e + 4 live in the adjacent lanes' quads
+                // horizontal neighbours e - 1 and e + 4 live in the adjacent lanes' quads;
+                // the warp's first and last lanes read theirs from shared memory
+                const float lpatch = cr[e - 1], rpatch = cr[min(e + 4, PE - 1)];
                 float left = __shfl_up_sync(0xffffffffu, c23.y, 1);
                 float right = __shfl_down_sync(0xffffffffu, c01.x, 1);
-                if (lane == 0) left = cr[e - 1];
-                if (lane == 31 || m == NQn - 1) right = cr[min(e + 4, PE - 1)];
+                left = lane == 0 ? lpatch : left;
+                right = (lane == 31 || m == NQn - 1) ? rpatch : right;
                 const float zr[6] = {left, c01.x, c01.y, c23.x, c23.y, right};
                 const float zu[4] = {u01.x, u01.y, u23.x, u23.y};
                 const float zd[4] = {d01.x, d01.y, d23.x, d23.y};
@@ -469,9 +486,13 @@ __device__ __forceinline__ void compute_unit(const tp::ClassLaunch &c, int job, 
                     const float ax = -__fsub_rn(zr[k + 2], zr[k]);
                     const float ay = -__fsub_rn(zu[k], zd[k]);
                     const float inv = rsqrtf(ax * ax + ay * ay + hh);
-                    const bool pad = 4 * m + k >= Wn;
-                    nx[k] = pad ? 0.0f : ax * inv;
-                    ny[k] = pad ? 0.0f : ay * inv;
+                    nx[k] = ax * inv;
+                    ny[k] = ay * inv;
+                }
+                if (4 * m + 3 >= Wn) {
+#pragma unroll
+                    for (int k = 0; k < 4; ++k)
+                        if (4 * m + k >= Wn) nx[k] = ny[k] = 0.0f;
                 }
                 if (act) {
                     const int o = (jn - 2) * c.nrm_pitch + 4 * m;
@@ -497,16 +518,18 @@ frame_kernel(const __grid_constant__ CUtensorMap pmap, const __grid_constant__ C
     const tp::ClassLaunch &c = f.c;
     const int units = c.njobs * c.bands;
 
+    __shared__ int reserved;  // unit index taken ahead, while the current unit is computed
     if (threadIdx.x == 0) {
         timed_out = 0;
         mbar_init(&bar, 1);
+        reserved = atomicAdd(f.counter, 1);
     }
     for (uint32_t phase = 0;; phase ^= 1u) {
-        // take the next unit; its parent was taken earlier by a running CTA, so
-        // waiting for it (bounded) cannot deadlock
+        // start the reserved unit; its parent has a smaller index, taken earlier by a
+        // running CTA, so waiting for it (bounded) cannot deadlock
         if (threadIdx.x == 0) {
             UnitInfo x{0, 0, 0};
-            const int u = atomicAdd(f.counter, 1);
+            const int u = reserved;
             if (u < units) {
                 x.valid = 1;
                 x.job = u / c.bands;
@@ -518,6 +541,7 @@ frame_kernel(const __grid_constant__ CUtensorMap pmap, const __grid_constant__ C
         __syncthreads();
         const UnitInfo x = info;
         if (!x.valid) break;
+        if (threadIdx.x == 0) reserved = atomicAdd(f.counter, 1);
         issue_lattice(c, x.job, stage);
         cp_async_commit();
         // warp 0 polls the mbarrier; the other warps wait at the CTA barrier below
@@ -547,62 +571,169 @@ frame_kernel(const __grid_constant__ CUtensorMap pmap, const __grid_constant__ C
     cp_async_wait_all();
 }
 
+// Double-buffered variant: two stages per CTA; the copies of the next unit are
+// issued before the current one is computed (unless the next unit's parent is
+// still in production, possibly by this CTA: then they are issued after it).
+__device__ __forceinline__ bool parent_ready(const tp::ClassLaunch &c, int job)
+{
+    const int pj = c.jobs[job].parent_job;
+    return pj < 0 || ld_acquire(c.done + pj) >= c.bands;
+}
+
+template <int MINB, bool MOD>
+__global__ void __launch_bounds__(kThreads, MINB)
+frame_kernel2(const __grid_constant__ CUtensorMap pmap, const __grid_constant__ CUtensorMap rmap,
+              const tp::FrameLaunch f)
+{
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    __shared__ uint64_t bars[2];
+    __shared__ UnitInfo info[2];
+    __shared__ int issued[2];
+    __shared__ int timed_out;
+    const uint32_t raw = smem_u32(smem_raw);
+    float *const stage0 = reinterpret_cast<float *>(smem_raw + (((raw + 127u) & ~127u) - raw));
+    float *const stage1 = stage0 + f.stage_floats;
+    const tp::ClassLaunch &c = f.c;
+    const int units = c.njobs * c.bands;
+    auto take = [&]() {
+        UnitInfo x{0, 0, 0};
+        const int u = atomicAdd(f.counter, 1);
+        if (u < units) {
+            x.valid = 1;
+            x.job = u / c.bands;
+            x.band = u - x.job * c.bands;
+        }
+        return x;
+    };
+
+    if (threadIdx.x == 0) {
+        timed_out = 0;
+        mbar_init(&bars[0], 1);
+        mbar_init(&bars[1], 1);
+        const UnitInfo x = take();
+        // the first unit's parent was taken earlier by a running CTA: waiting is safe
+        if (x.valid) issue_copies(c, &pmap, &rmap, x.job, x.band, stage0, &bars[0]);
+        info[0] = x;
+        issued[0] = 1;
+    }
+    __syncthreads();
+    if (info[0].valid) issue_lattice(c, info[0].job, stage0);
+    cp_async_commit();
+
+    uint32_t phases = 0u;  // bit s: parity of stage s's next completion
+    for (int cur = 0;; cur ^= 1) {
+        const int nxt = cur ^ 1;
+        float *const scur = cur ? stage1 : stage0;
+        float *const snxt = cur ? stage0 : stage1;
+        const UnitInfo x = info[cur];
+        if (!x.valid) break;
+        if (threadIdx.x == 0) {
+            const UnitInfo y = take();
+            int iss = 0;
+            if (y.valid && parent_ready(c, y.job)) {
+                issue_copies(c, &pmap, &rmap, y.job, y.band, snxt, &bars[nxt]);
+                iss = 1;
+            }
+            info[nxt] = y;
+            issued[nxt] = iss;
+        }
+        __syncthreads();
+        const bool y_valid = info[nxt].valid != 0, y_issued = issued[nxt] != 0;
+        if (y_valid && y_issued) issue_lattice(c, info[nxt].job, snxt);
+        cp_async_commit();
+        if (threadIdx.x < 32) {
+            if (!mbar_wait_bounded(&bars[cur], (phases >> cur) & 1u)) {
+                report(TP_E_TIMEOUT);
+                mbar_wait_bounded(&bars[cur], (phases >> cur) & 1u);
+                timed_out = 1;
+            }
+        }
+        phases ^= 1u << cur;
+        cp_async_wait_all_but_one();
+        const bool no_res = c.jobs[x.job].residual_slot < 0;
+        __syncthreads();
+        if (timed_out) break;
+        if (no_res) {
+            for (int t = threadIdx.x; t < c.buf_floats; t += kThreads) scur[t] = 0.0f;
+            __syncthreads();
+        }
+        compute_unit<MOD>(c, x.job, x.band, scur);
+        if (f.any_deps) fence_proxy_async_global();
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            if (f.any_deps) {
+                __threadfence();
+                atomicAdd(c.done + x.job, 1);  // release: this band of the tile is complete
+            }
+            if (y_valid && !y_issued) {
+                issue_copies(c, &pmap, &rmap, info[nxt].job, info[nxt].band, snxt, &bars[nxt]);
+                issued[nxt] = 1;
+            }
+        }
+        if (y_valid && !y_issued) {
+            __syncthreads();  // thread 0 has seen the parent complete
+            issue_lattice(c, info[nxt].job, snxt);
+            cp_async_commit();
+        }
+    }
+    cp_async_wait_all();
+}
+
 }  // namespace
 
 namespace tp {
 
-static size_t frame_smem(int stage_floats) { return sizeof(float) * (size_t)stage_floats + 128; }
+static size_t frame_smem(int stage_floats, int stages) { return sizeof(float) * (size_t)stage_floats * stages + 128; }
 
-template <int MINB, bool MOD>
-static int ensure_smem_attr(size_t smem)
+using KernelFn = void (*)(const CUtensorMap, const CUtensorMap, const FrameLaunch);
+
+// The kernel instance of a (stages, CTAs-per-SM target, modulated-noise) choice.
+static KernelFn pick(int stages, int minb, bool mod)
 {
-    static std::mutex mu;
-    static size_t have = 0;
-    std::lock_guard<std::mutex> lk(mu);
-    if (smem <= have) return TP_OK;
-    cudaError_t e = cudaFuncSetAttribute(frame_kernel<MINB, MOD>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return cuda_fail("cudaFuncSetAttribute", e);
-    have = smem;
-    return TP_OK;
+    if (stages >= 2) {
+        if (minb >= 3) return mod ? frame_kernel2<3, true> : frame_kernel2<3, false>;
+        return mod ? frame_kernel2<2, true> : frame_kernel2<2, false>;
+    }
+    if (minb >= 3) return mod ? frame_kernel<3, true> : frame_kernel<3, false>;
+    return mod ? frame_kernel<2, true> : frame_kernel<2, false>;
 }
 
-template <int MINB, bool MOD>
-static int launch_variant(const FrameLaunch &f, const CUtensorMap *pmap, const CUtensorMap *rmap, int grid,
-                          cudaStream_t s)
+// Raises a kernel's dynamic shared-memory limit (a host-side attribute, set
+// before any stream capture that launches the kernel).
+static int ensure_smem_attr(KernelFn fn, size_t smem)
 {
-    const size_t smem = frame_smem(f.stage_floats);
-    int rc = ensure_smem_attr<MINB, MOD>(smem);
-    if (rc) return rc;
-    frame_kernel<MINB, MOD><<<grid, kThreads, smem, s>>>(*pmap, *rmap, f);
-    cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess) return cuda_fail("frame kernel launch", e);
+    static std::mutex mu;
+    static std::map<KernelFn, size_t> have;
+    std::lock_guard<std::mutex> lk(mu);
+    if (smem <= have[fn]) return TP_OK;
+    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return cuda_fail("cudaFuncSetAttribute", e);
+    have[fn] = smem;
     return TP_OK;
 }
 
 int launch_frame(const FrameLaunch &f, const CUtensorMap *pmap, const CUtensorMap *rmap, int grid, void *stream)
 {
     if (f.c.njobs <= 0) return TP_OK;
-    cudaStream_t s = static_cast<cudaStream_t>(stream);
-    const bool mod = f.c.noise_mode == 1;
-    if (f.minb >= 3) return mod ? launch_variant<3, true>(f, pmap, rmap, grid, s) : launch_variant<3, false>(f, pmap, rmap, grid, s);
-    return mod ? launch_variant<2, true>(f, pmap, rmap, grid, s) : launch_variant<2, false>(f, pmap, rmap, grid, s);
-}
-
-template <int MINB, bool MOD>
-static int occupancy_variant(int stage_floats, int *blocks_per_sm)
-{
-    const size_t smem = frame_smem(stage_floats);
-    int rc = ensure_smem_attr<MINB, MOD>(smem);
+    const KernelFn fn = pick(f.stages, f.minb, f.c.noise_mode == 1);
+    const size_t smem = frame_smem(f.stage_floats, f.stages);
+    int rc = ensure_smem_attr(fn, smem);
     if (rc) return rc;
-    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, frame_kernel<MINB, MOD>, kThreads, smem);
-    if (e != cudaSuccess) return cuda_fail("cudaOccupancyMaxActiveBlocksPerMultiprocessor", e);
+    fn<<<grid, kThreads, smem, static_cast<cudaStream_t>(stream)>>>(*pmap, *rmap, f);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail("frame kernel launch", e);
     return TP_OK;
 }
 
-int frame_occupancy(int stage_floats, int minb, bool mod, int *blocks_per_sm)
+int frame_occupancy(int stage_floats, int stages, int minb, bool mod, int *blocks_per_sm)
 {
-    if (minb >= 3) return mod ? occupancy_variant<3, true>(stage_floats, blocks_per_sm) : occupancy_variant<3, false>(stage_floats, blocks_per_sm);
-    return mod ? occupancy_variant<2, true>(stage_floats, blocks_per_sm) : occupancy_variant<2, false>(stage_floats, blocks_per_sm);
+    const KernelFn fn = pick(stages, minb, mod);
+    const size_t smem = frame_smem(stage_floats, stages);
+    int rc = ensure_smem_attr(fn, smem);
+    if (rc) return rc;
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, fn, kThreads, smem);
+    if (e != cudaSuccess) return cuda_fail("cudaOccupancyMaxActiveBlocksPerMultiprocessor", e);
+    return TP_OK;
 }
 
 int read_status(int *status, bool clear)

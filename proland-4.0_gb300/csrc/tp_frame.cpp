@@ -20,6 +20,7 @@ struct tp_frame {
         tp::ClassLaunch L{};
         const CUtensorMap *pmap = nullptr, *rmap = nullptr;
         bool device_deps = false;  // a device job list that names parent jobs
+        int minb_override = 0;     // CTAs per SM the kernel variant targets (0: automatic)
     };
     Class cls[2];
     int nclasses = 0;
@@ -29,7 +30,6 @@ struct tp_frame {
     tp_tile_job *jobs_buf = nullptr;
     size_t jobs_buf_count = 0;
     bool uploaded = false;
-    int minb_override = 0;
     // CUDA graph of (reset + launch), built on first tp_frame_graph_launch
     cudaGraphExec_t graph = nullptr;
     cudaStream_t graph_stream = nullptr;
@@ -247,9 +247,11 @@ int prepare(tp_frame *f, tp::FrameLaunch *F, void *stream)
         if (k.jobs.empty() && k.njobs > 0 && k.device_deps) L.any_deps = 1;  // as declared by the caller
         for (const auto &j : k.jobs)
             if (j.parent_job >= 0) L.any_deps = 1;
-        // three CTAs per SM when three stages fit in shared memory
-        const size_t per_cta = sizeof(float) * (size_t)L.stage_floats + 128 + 1024;
-        L.minb = f->minb_override ? f->minb_override : (3 * per_cta <= 227 * 1024 ? 3 : 2);
+        // double-buffer when the class asks for it; three CTAs per SM when three
+        // CTAs' stages fit in shared memory
+        L.stages = k.params.stages == 2 ? 2 : 1;
+        const size_t per_cta = sizeof(float) * (size_t)L.stage_floats * L.stages + 128 + 1024;
+        L.minb = k.minb_override ? k.minb_override : (3 * per_cta <= 227 * 1024 ? 3 : 2);
     }
     return TP_OK;
 }
@@ -264,7 +266,7 @@ int enqueue(tp_frame *f, const tp::FrameLaunch *F, void *stream)
         const int units = L.c.njobs * L.c.bands;
         if (units == 0) continue;
         int per_sm = 0;
-        int rc = tp::frame_occupancy(L.stage_floats, L.minb, L.c.noise_mode == 1, &per_sm);
+        int rc = tp::frame_occupancy(L.stage_floats, L.stages, L.minb, L.c.noise_mode == 1, &per_sm);
         if (rc) return rc;
         if (per_sm < 1) return tp::fail(TP_E_BAD_ARG, "frame: the kernel's stage does not fit in shared memory");
         const int grid = std::min(units, per_sm * sm_count());
@@ -369,7 +371,7 @@ extern "C" int tp_frame_graph_launch(tp_frame *f, void *stream)
         // set the kernels' attributes outside the capture
         for (int c = 0; c < f->nclasses; ++c) {
             int per_sm = 0;
-            rc = tp::frame_occupancy(F[c].stage_floats, F[c].minb, F[c].c.noise_mode == 1, &per_sm);
+            rc = tp::frame_occupancy(F[c].stage_floats, F[c].stages, F[c].minb, F[c].c.noise_mode == 1, &per_sm);
             if (rc) {
                 cudaStreamDestroy(cap);
                 return rc;
@@ -408,6 +410,110 @@ extern "C" int tp_frame_units(const tp_frame *f)
     int u = 0;
     for (int c = 0; c < f->nclasses; ++c) u += f->cls[c].njobs * f->cls[c].L.bands;
     return u;
+}
+
+// ---------------------------------------------------------------- autotuner
+namespace {
+
+// Launch time (ms, mean of `repeats`) of class c alone under its current shape.
+int time_class(tp_frame *f, int c, cudaStream_t s, int repeats, float *ms)
+{
+    tp::FrameLaunch F[2];
+    int rc = prepare(f, F, s);
+    if (rc) return rc;
+    const tp::FrameLaunch &L = F[c];
+    const int units = L.c.njobs * L.c.bands;
+    int per_sm = 0;
+    rc = tp::frame_occupancy(L.stage_floats, L.stages, L.minb, L.c.noise_mode == 1, &per_sm);
+    if (rc) return rc;
+    if (per_sm < 1) return tp::fail(TP_E_BAD_ARG, "autotune: shape does not fit");
+    const int grid = std::min(units, per_sm * sm_count());
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    float total = 0.0f;
+    for (int r = -1; r < repeats; ++r) {  // r = -1: warm-up
+        cudaMemsetAsync(f->flags, 0, sizeof(int) * f->flags_count, s);
+        cudaEventRecord(e0, s);
+        rc = tp::launch_frame(L, f->cls[c].pmap, f->cls[c].rmap, grid, s);
+        cudaEventRecord(e1, s);
+        if (rc) break;
+        cudaError_t e = cudaEventSynchronize(e1);
+        if (e != cudaSuccess) {
+            rc = tp::cuda_fail("autotune", e);
+            break;
+        }
+        float t = 0.0f;
+        cudaEventElapsedTime(&t, e0, e1);
+        if (r >= 0) total += t;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc) return rc;
+    *ms = total / repeats;
+    return TP_OK;
+}
+
+}  // namespace
+
+extern "C" int tp_frame_autotune(tp_frame *f, void *stream, int repeats)
+{
+    if (!f || f->nclasses == 0) return tp::fail(TP_E_BAD_ARG, "tp_frame_autotune: empty frame");
+    if (repeats < 1) repeats = 3;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    for (int c = 0; c < f->nclasses; ++c) {
+        auto &k = f->cls[c];
+        if (k.njobs == 0) continue;
+        const int W = k.elev->W;
+        std::vector<int> bands = W <= 128 ? std::vector<int>{W, (W + 1) / 2, (W + 2) / 3, (W + 3) / 4}
+                                          : std::vector<int>{(W + 1) / 2, (W + 2) / 3, (W + 3) / 4, (W + 4) / 5, (W + 5) / 6};
+        const tp_elev_params orig = k.params;
+        const int orig_minb = k.minb_override;
+        float best = 1e30f;
+        tp_elev_params best_p = orig;
+        int best_minb = orig_minb;
+        for (int br : bands)
+            for (int stages = 1; stages <= 2; ++stages)
+                for (int minb = 2; minb <= 3; ++minb) {
+                    k.params = orig;
+                    k.params.band_rows = br;
+                    k.params.stages = stages;
+                    k.minb_override = minb;
+                    if (setup_class(k)) continue;
+                    const size_t per_cta = sizeof(float) * (size_t)stage_floats_of(k.L) * stages + 128 + 1024;
+                    if (per_cta * minb > 227 * 1024) continue;
+                    f->uploaded = f->uploaded;  // job lists are unchanged
+                    float ms = 0.0f;
+                    if (time_class(f, c, s, repeats, &ms)) continue;
+                    if (ms < best) {
+                        best = ms;
+                        best_p = k.params;
+                        best_minb = minb;
+                    }
+                }
+        k.params = best_p;
+        k.minb_override = best_minb;
+        int rc = setup_class(k);
+        if (rc) return rc;
+    }
+    drop_graph(f);
+    int st = 0;
+    tp::read_status(&st, true);
+    if (st != 0) return tp::fail(st, "autotune: a kernel reported a failure");
+    return TP_OK;
+}
+
+extern "C" int tp_frame_config(const tp_frame *f, int klass, int *band_rows, int *stages, int *ctas_per_sm)
+{
+    if (!f || klass < 0 || klass >= f->nclasses) return tp::fail(TP_E_BAD_ARG, "tp_frame_config: bad class");
+    const auto &k = f->cls[klass];
+    if (band_rows) *band_rows = (k.elev->W + k.L.bands - 1) / k.L.bands;
+    if (stages) *stages = k.params.stages == 2 ? 2 : 1;
+    if (ctas_per_sm) {
+        const size_t per_cta = sizeof(float) * (size_t)stage_floats_of(k.L) * (k.params.stages == 2 ? 2 : 1) + 128 + 1024;
+        *ctas_per_sm = k.minb_override ? k.minb_override : (3 * per_cta <= 227 * 1024 ? 3 : 2);
+    }
+    return TP_OK;
 }
 
 // ---------------------------------------------------------------- batch calls

@@ -92,10 +92,11 @@ struct FrameLaunch {
     int stage_floats;         // shared-memory stage of one unit
     int any_deps;             // some job waits on a parent produced in this launch
     int minb;                 // kernel variant: CTAs per SM the register budget targets (2 or 3)
+    int stages;               // 1: one stage per CTA; 2: double-buffered (next unit's copies in flight)
 };
 
 int launch_frame(const FrameLaunch &f, const CUtensorMap *pmap, const CUtensorMap *rmap, int grid, void *stream);
-int frame_occupancy(int stage_floats, int minb, bool mod, int *blocks_per_sm);
+int frame_occupancy(int stage_floats, int stages, int minb, bool mod, int *blocks_per_sm);
 
 // Copies `count` slots' plane `channel` between a dense host array and the slots
 // through the storage's staging buffer (one linear copy + a repack kernel).

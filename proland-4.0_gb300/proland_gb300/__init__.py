@@ -80,10 +80,11 @@ class TileStorage:
         return out
 
 
-def make_params(grid_size=24, flip=False, no_clamp=False, noise_mode=0, normal_format=2, band_rows=0):
+def make_params(grid_size=24, flip=False, no_clamp=False, noise_mode=0, normal_format=2, band_rows=0,
+                stages=0):
     p = ElevParams()
     p.grid_size, p.flip, p.no_clamp = grid_size, int(flip), int(no_clamp)
-    p.noise_mode, p.normal_format, p.band_rows = noise_mode, normal_format, band_rows
+    p.noise_mode, p.normal_format, p.band_rows, p.stages = noise_mode, normal_format, band_rows, stages
     return p
 
 
@@ -157,6 +158,14 @@ class Frame:
 
     def units(self):
         return check(lib().tp_frame_units(self.handle))
+
+    def autotune(self, stream=None, repeats=3):
+        check(lib().tp_frame_autotune(self.handle, stream, repeats))
+
+    def config(self, klass):
+        b, s, m = C.c_int(), C.c_int(), C.c_int()
+        check(lib().tp_frame_config(self.handle, klass, C.byref(b), C.byref(s), C.byref(m)))
+        return {"band_rows": b.value, "stages": s.value, "ctas_per_sm": m.value}
 
 
 def dem_noise(tile_width):

@@ -48,7 +48,7 @@ class ElevParams(C.Structure):
     _fields_ = [
         ("grid_size", C.c_int32), ("flip", C.c_int32), ("no_clamp", C.c_int32),
         ("noise_mode", C.c_int32), ("normal_format", C.c_int32), ("band_rows", C.c_int32),
-        ("reserved", C.c_int32 * 2),
+        ("stages", C.c_int32), ("reserved", C.c_int32),
     ]
 
 
@@ -92,6 +92,8 @@ def lib():
         "tp_frame_launch": ([_vp, _vp], _i),
         "tp_frame_graph_launch": ([_vp, _vp], _i),
         "tp_frame_units": ([_vp], _i),
+        "tp_frame_autotune": ([_vp, _vp, _i], _i),
+        "tp_frame_config": ([_vp, _i, C.POINTER(_i), C.POINTER(_i), C.POINTER(_i)], _i),
         "tp_status": ([C.POINTER(_i), _i], _i),
         "tp_stream_check": ([_vp], _i),
         "tp_dem_noise": ([_i, _f32p], _i),

@@ -72,11 +72,12 @@ def test_stencil_residual_normals(gpu, oracle_lib, W):
     run_cases(gpu, oracle_lib, cases, gpu.make_params())
 
 
-@pytest.mark.parametrize("W,band_rows", [(101, 26), (101, 51), (197, 99), (197, 140), (197, 33)])
-def test_band_heights(gpu, oracle_lib, W, band_rows):
-    """Every band split of a tile produces the same bits (halo rows, window origins)."""
+@pytest.mark.parametrize("W,band_rows,stages", [(101, 26, 1), (101, 51, 2), (197, 99, 1), (197, 140, 1),
+                                                 (197, 33, 2), (101, 101, 2)])
+def test_band_heights(gpu, oracle_lib, W, band_rows, stages):
+    """Every band split of a tile, single- or double-buffered, produces the same bits."""
     cases = [Case(W, lvl, tx, ty, seed=lvl + 5 * tx, noise_amp=-20.0) for lvl, tx, ty in [(1, 1, 0), (4, 7, 12), (0, 0, 0)]]
-    run_cases(gpu, oracle_lib, cases, gpu.make_params(band_rows=band_rows, flip=True))
+    run_cases(gpu, oracle_lib, cases, gpu.make_params(band_rows=band_rows, flip=True, stages=stages))
 
 
 def test_residual_window_mod2(gpu, oracle_lib):
@@ -237,3 +238,49 @@ def test_frame_two_widths_one_launch_and_graph(gpu, oracle_lib):
     tp.stream_check()
     _check_class(tp, a)
     _check_class(tp, b)
+
+
+def test_autotuned_frame_keeps_results(gpu, oracle_lib):
+    """The autotuner changes only the work-unit shape, never the produced bits."""
+    tp, orc = gpu, oracle_lib
+    a = _class_setup(tp, orc, 101, [(1, 0, 1, -140.0), (3, 5, 2, 5.0), (2, 3, 3, -15.0)], 300)
+    b = _class_setup(tp, orc, 197, [(2, 1, 2, -100.0), (5, 17, 30, 1.5)], 400)
+    f = tp.Frame()
+    for k in (a, b):
+        f.add(k["elev"], k["res"], k["nrm"], k["params"], k["jobs"])
+    f.autotune(repeats=1)
+    for i in range(2):
+        cfg = f.config(i)
+        assert cfg["stages"] in (1, 2) and cfg["ctas_per_sm"] in (2, 3) and cfg["band_rows"] >= 8
+    f.graph_launch()
+    tp.stream_check()
+    _check_class(tp, a)
+    _check_class(tp, b)
+
+
+def test_quadtree_double_buffered(gpu, oracle_lib):
+    """Parent/child ordering inside one launch with the next unit prefetched."""
+    tp, orc = gpu, oracle_lib
+    W = 101
+    rng = np.random.default_rng(9)
+    tiles = [(l, x, y) for l in range(4) for y in range(1 << l) for x in range(1 << l)]
+    index = {t: k for k, t in enumerate(tiles)}
+    n = len(tiles)
+    elev = tp.TileStorage(W, 3, n)
+    res = tp.TileStorage(W, 1, n)
+    resid = (rng.standard_normal((n, W, W)) * 50.0).astype(np.float32)
+    res.upload(0, 0, resid)
+    jobs = []
+    for k, (l, x, y) in enumerate(tiles):
+        pj = index[(l - 1, x // 2, y // 2)] if l > 0 else -1
+        jobs.append(tp.make_job(l, x, y, out_slot=k, parent_slot=pj, residual_slot=k,
+                                tile_meters=50000.0 / (1 << l), parent_job=pj))
+    tp.elevation_batch(elev, res, None, tp.make_params(band_rows=34, stages=2), jobs)
+    tp.stream_check()
+    zf = elev.download(0, n, tp.ZF)
+    want = {}
+    for k, (l, x, y) in enumerate(tiles):
+        p = want.get((l - 1, x // 2, y // 2))
+        ezf, ezc, ezm = orc.elevation_tile(W, l, x, y, p[0] if p else None, p[2] if p else None, resid[k])
+        want[(l, x, y)] = (ezf, ezc, ezm)
+        assert np.array_equal(zf[k], ezf), "zf of tile %s" % (tiles[k],)
