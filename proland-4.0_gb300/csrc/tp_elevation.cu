@@ -269,11 +269,10 @@ __device__ __forceinline__ void compute_unit(const tp::ClassLaunch &c, int job, 
         const int q = threadIdx.x % NQ, seg = threadIdx.x / NQ;
         const int i0 = 4 * q;
         const int rbeg = ja + seg * S, rend = min(rbeg + S, jb + 1);
-        float *ozf = c.elev + (long long)J.out_slot * c.slot_stride + i0;
-        const long long pstride = c.plane_stride;
+        const int out_slot = J.out_slot;
         const bool noisy = J.noise_amp != 0.0f;
         const bool modulated = MOD && J.noise_amp > 0.0f;
-        const __half *nz = c.noise + (long long)(J.noise_rot * 6 + J.noise_layer) * W * PE + i0;
+        const int nzo = (J.noise_rot * 6 + J.noise_layer) * W * PE + i0;  // offset of the quad in the noise table
         // zf + |amp| N (terrain1), or zf - amp N (modulated shader, amp < 0): -(amp N) == (-amp) N exactly
         const float namp = c.noise_mode == 0 ? fabsf(J.noise_amp) : -J.noise_amp;
         const float rscale = J.rscale;
@@ -297,6 +296,8 @@ __device__ __forceinline__ void compute_unit(const tp::ClassLaunch &c, int job, 
         const bool two_cells = g >= 2;
         float P[4][5];
         int wr0 = -1000;
+        float zcv[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+        int zkey = -1;
         const float *pcol = spar + 2 * q;
         auto load_row = [&](float(&dst)[5], int r) {
             const float *src = pcol + r * c.par_pitch;
@@ -377,39 +378,51 @@ __device__ __forceinline__ void compute_unit(const tp::ClassLaunch &c, int job, 
                     up[1] = z1;
                     up[3] = z3;
                 }
+                // zc from the parent zm lattice: constant between lattice rows, so the
+                // four values are cached and recomputed only when the row's cells change
                 const int cy = j - 2;
-                const int yr = (fdiv2g(cy + g, g, gs) + 1) * c.ck, yf = (fdiv2g(cy, g, gs) + 1) * c.ck;
-                const bool frow = c.flip && fmod2g(cy, g, gs) == g;
-                float r1[4], r3[4];
-                if (two_cells) {
-                    const float a1 = slat[yf + (int)(xcells & 255u)], b1 = slat[yf + (int)((xcells >> 8) & 255u)];
-                    const float a3 = slat[yr + (int)((xcells >> 16) & 255u)], b3 = slat[yr + (int)(xcells >> 24)];
+                const int kyr = fdiv2g(cy + g, g, gs) + 1, kyf = fdiv2g(cy, g, gs) + 1;
+                const int key = (kyr << 16) | kyf;
+                if (key != zkey) {
+                    zkey = key;
+                    const int yr = kyr * c.ck, yf = kyf * c.ck;
+                    float r1[4], r3[4];
+                    if (two_cells) {
+                        const float a1 = slat[yf + (int)(xcells & 255u)], b1 = slat[yf + (int)((xcells >> 8) & 255u)];
+                        const float a3 = slat[yr + (int)((xcells >> 16) & 255u)], b3 = slat[yr + (int)(xcells >> 24)];
 #pragma unroll
-                    for (int k = 0; k < 4; ++k) {
-                        r1[k] = (selr >> k) & 1u ? b1 : a1;
-                        r3[k] = (self_ >> k) & 1u ? b3 : a3;
-                    }
-                } else {
+                        for (int k = 0; k < 4; ++k) {
+                            r1[k] = (selr >> k) & 1u ? b1 : a1;
+                            r3[k] = (self_ >> k) & 1u ? b3 : a3;
+                        }
+                    } else {
 #pragma unroll
-                    for (int k = 0; k < 4; ++k) {
-                        const int cx = min(i0 + k, W - 1) - 2;
-                        r1[k] = slat[yf + fdiv2g(cx + g, g, gs) + 1];
-                        r3[k] = slat[yr + fdiv2g(cx, g, gs) + 1];
+                        for (int k = 0; k < 4; ++k) {
+                            const int cx = min(i0 + k, W - 1) - 2;
+                            r1[k] = slat[yf + fdiv2g(cx + g, g, gs) + 1];
+                            r3[k] = slat[yr + fdiv2g(cx, g, gs) + 1];
+                        }
                     }
+#pragma unroll
+                    for (int k = 0; k < 4; ++k) zcv[k] = __fmul_rn(__fadd_rn(r1[k], r3[k]), 0.5f);
                 }
 #pragma unroll
                 for (int k = 0; k < 4; ++k) {
                     zf[k] = __fadd_rn(zf[k], up[k]);
-                    const int cxk = min(i0 + k, W - 1) - 2;
-                    if (frow && fmod2g(cxk, g, gs) == g) {
-                        const int cx = cxk;
-                        const int xr = fdiv2g(cx + g, g, gs) + 1, xf = fdiv2g(cx, g, gs) + 1;
-                        const float zc0 = slat[yf + xf];
-                        const float zc2 = slat[yr + xr];
-                        const float s13 = __fadd_rn(r3[k], r1[k]), s02 = __fadd_rn(zc0, zc2);
-                        zc[k] = __fmul_rn(s13 >= s02 ? __fadd_rn(r1[k], r3[k]) : s02, 0.5f);
-                    } else {
-                        zc[k] = __fmul_rn(__fadd_rn(r1[k], r3[k]), 0.5f);
+                    zc[k] = zcv[k];
+                }
+                if (c.flip && fmod2g(cy, g, gs) == g) {  // cell-centre rows of a flipped mesh
+                    const int yr = kyr * c.ck, yf = kyf * c.ck;
+#pragma unroll
+                    for (int k = 0; k < 4; ++k) {
+                        const int cx = min(i0 + k, W - 1) - 2;
+                        if (fmod2g(cx, g, gs) == g) {
+                            const int xr = fdiv2g(cx + g, g, gs) + 1, xf = fdiv2g(cx, g, gs) + 1;
+                            const float zc1 = slat[yf + xr], zc3 = slat[yr + xf];
+                            const float zc0 = slat[yf + xf], zc2 = slat[yr + xr];
+                            const float s13 = __fadd_rn(zc3, zc1), s02 = __fadd_rn(zc0, zc2);
+                            zc[k] = __fmul_rn(s13 >= s02 ? __fadd_rn(zc1, zc3) : s02, 0.5f);
+                        }
                     }
                 }
             }
@@ -426,10 +439,10 @@ __device__ __forceinline__ void compute_unit(const tp::ClassLaunch &c, int job, 
                     if (i0 + k >= W) vf[k] = vc[k] = vm[k] = 0.0f;
             }
             if (j >= j0 && j < j1) {
-                float *o = ozf + j * PE;
+                float *o = c.elev + (long long)out_slot * c.slot_stride + (j * PE + i0);
                 *reinterpret_cast<float4 *>(o) = make_float4(vf[0], vf[1], vf[2], vf[3]);
-                *reinterpret_cast<float4 *>(o + pstride) = make_float4(vc[0], vc[1], vc[2], vc[3]);
-                *reinterpret_cast<float4 *>(o + 2 * pstride) = make_float4(vm[0], vm[1], vm[2], vm[3]);
+                *reinterpret_cast<float4 *>(o + c.plane_stride) = make_float4(vc[0], vc[1], vc[2], vc[3]);
+                *reinterpret_cast<float4 *>(o + 2 * c.plane_stride) = make_float4(vm[0], vm[1], vm[2], vm[3]);
             }
             *reinterpret_cast<float4 *>(brow) = make_float4(vm[0], vm[1], vm[2], vm[3]);
         };
@@ -437,11 +450,11 @@ __device__ __forceinline__ void compute_unit(const tp::ClassLaunch &c, int job, 
         using Odd = std::integral_constant<bool, true>;
         // noise rows come from L2: the next row's quad is fetched one row ahead
         uint2 nzh = make_uint2(0u, 0u);
-        if (noisy && rbeg < rend) nzh = __ldg(reinterpret_cast<const uint2 *>(nz + rbeg * PE));
+        if (noisy && rbeg < rend) nzh = __ldg(reinterpret_cast<const uint2 *>(c.noise + nzo + rbeg * PE));
 #pragma unroll 1
         for (int j = rbeg; j < rend; ++j) {
             const uint2 h = nzh;
-            if (noisy && j + 1 < rend) nzh = __ldg(reinterpret_cast<const uint2 *>(nz + (j + 1) * PE));
+            if (noisy && j + 1 < rend) nzh = __ldg(reinterpret_cast<const uint2 *>(c.noise + nzo + (j + 1) * PE));
             if (has_parent) advance(j / 2 + 1 + dy - pr0);  // (even, odd) rows share the stencil centre row
             if (j & 1) row(j, h, Odd{});
             else row(j, h, Even{});
