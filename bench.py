@@ -289,6 +289,8 @@ def main():
     ap.add_argument("--seed", type=int, default=2024)
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true", help="keep the default work-unit shapes")
+    ap.add_argument("--no-per-width", action="store_true", help="skip the per-width timings")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -324,7 +326,8 @@ def main():
         frame.add_device(fc.elev, fc.res, fc.nrm, params, C.c_void_p(fc.dev_jobs.data_ptr()), fc.n,
                          has_dependencies=False)
 
-    frame.autotune(sh, repeats=5)
+    if not args.no_autotune:
+        frame.autotune(sh, repeats=5)
     tuned = {"W%d" % fc.W: frame.config(i) for i, fc in enumerate(classes)}
 
     def step(events=None):
@@ -363,6 +366,31 @@ def main():
     ms_step = ms_total / args.steps
     tiles = sum(fc.n for fc in classes)
     value = world * tiles / (ms_step / 1000.0)
+
+    # per tile width: each width alone in its own frame, same tuned shape
+    per_width = {}
+    for fc in ([] if args.no_per_width else classes):
+        fw = tp.Frame()
+        fw.add_device(fc.elev, fc.res, fc.nrm, params, C.c_void_p(fc.dev_jobs.data_ptr()), fc.n,
+                      has_dependencies=False)
+        if not args.no_autotune:
+            fw.autotune(sh, repeats=3)
+        with torch.cuda.stream(stream):
+            for _ in range(warmup):
+                fw.graph_launch(sh)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(args.steps):
+            fw.graph_launch(sh)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / args.steps
+        gbs = fc.n * BYTES_PER_TILE[fc.W] / (ms / 1000.0) / 1e9
+        per_width["W%d" % fc.W] = {"tiles": fc.n, "ms": ms, "tiles_per_s": fc.n / (ms / 1000.0),
+                                   "achieved_gbs": gbs, "frac": gbs / hbm_peak()[0], "shape": fw.config(0)}
+        fw.close()
+    tp.stream_check(sh)
 
     # end to end through the C ABI with host buffers
     e2e_ms = []
@@ -409,7 +437,7 @@ def main():
                    "parallelism": "replicas" if world > 1 else "single GPU", "autotuned": tuned},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": traffic, "peak_source": peak_src, "kernel": "frame_kernel (one persistent launch per tile width, replayed from a CUDA graph)",
-                     "kernel_ms": kernel_ms, "units_per_launch": frame.units(),
+                     "kernel_ms": kernel_ms, "units_per_launch": frame.units(), "per_width": per_width,
                      "algorithmic_bytes_per_step": sum(alg.values())},
         "e2e": {"value": world * tiles / (e2e_step / 1000.0), "unit": UNIT, "ms_per_step": e2e_step,
                 "h2d_bytes_per_step": sum(fc.h2d_bytes for fc in classes),
