@@ -47,7 +47,8 @@ int tp_device_available(void);
  * Replaces TileStorage (core/.../producer/TileStorage.h:140-182),
  * GPUTileStorage::init (core/.../producer/GPUTileStorage.cpp:151-205) and
  * CPUTileStorage<float> (core/.../producer/CPUTileStorage.h:43-151).
- * on_device = 1 allocates device memory, 0 pinned host memory. */
+ * on_device = 1 allocates device memory, 0 pinned host memory, 2 no memory at
+ * all (slot bookkeeping only, usable without a GPU). */
 typedef struct tp_storage tp_storage;
 int tp_storage_create(int tile_width, int channels, int capacity, int on_device, tp_storage **out);
 int tp_storage_destroy(tp_storage *s);
@@ -156,6 +157,74 @@ int tp_frame_config(const tp_frame *f, int klass, int *band_rows, int *stages, i
  * `clear`); tp_stream_check synchronises `stream`, then reads and clears it. */
 int tp_status(int *status, int clear);
 int tp_stream_check(void *stream);
+
+/* ------------------------------------------------------------------------
+ * Tile cache and producers: the TileCache / TileProducer protocol.
+ *
+ * tp_cache replaces TileCache (core/.../producer/TileCache.h:201-309,
+ * TileCache.cpp:150-377): tiles keyed by (producer, level, tx, ty) with a users
+ * count; tiles without users stay cached in an LRU list and their slots are
+ * recycled oldest first; getTile returns NULL (TP_E_CACHE_FULL in
+ * tp_last_error) when no slot is free or recyclable.
+ * tp_producer replaces TileProducer (core/.../producer/TileProducer.h:147-378)
+ * for the three producers of this path:
+ *   residuals  ResidualProducer (terrain/.../dem/ResidualProducer.cpp:70-438):
+ *              a .dat pyramid (file, delta, zscale), a host callback, or zero
+ *              residuals for an empty file name;
+ *   elevations ElevationProducer (ElevationProducer.cpp:178-579);
+ *   normals    NormalProducer (NormalProducer.cpp:71-385), flat deformation.
+ * getTile acquires the tile; a tile not produced yet is queued together with
+ * the tiles it is made from (startCreateTile), which it holds until it is
+ * produced.  tp_scheduler_run produces every queued tile of the producers
+ * given (and of those they use) on `stream`: the batched doCreateTile of a
+ * frame, parents before children, normals fused into the elevation launch.
+ * The caches' storages must be used from one stream. */
+typedef struct tp_cache tp_cache;
+typedef struct tp_producer tp_producer;
+typedef struct tp_tile tp_tile;
+typedef struct tp_dat tp_dat;
+/* Host residual source: fills `out` (width x width floats, row-major) with the
+ * residual tile (level, tx, ty); returns 0 on success. */
+typedef int (*tp_residual_source)(void *user, int level, int tx, int ty, float *out, int width);
+
+int tp_cache_create(tp_storage *storage, const char *name, tp_cache **out);
+int tp_cache_destroy(tp_cache *c);
+int tp_cache_used_tiles(tp_cache *c);     /* getUsedTiles */
+int tp_cache_unused_tiles(tp_cache *c);   /* getUnusedTiles */
+int tp_cache_stats(tp_cache *c, long long *queries, long long *misses);
+
+int tp_residual_producer_create(tp_cache *cache, const char *file, int delta, float zscale, tp_producer **out);
+int tp_residual_producer_set_source(tp_producer *p, tp_residual_source fn, void *user);
+/* noise_amp: per-level amplitudes (ElevationProducer.cpp:488-499); face as in
+ * ElevationProducer.cpp:509-515 (0 flat, 1..6 cube faces). */
+int tp_elevation_producer_create(tp_cache *cache, tp_producer *residuals, const float *noise_amp, int n_noise,
+                                 const tp_elev_params *params, int face, tp_producer **out);
+int tp_normal_producer_create(tp_cache *cache, tp_producer *elevations, int deform, tp_producer **out);
+int tp_producer_destroy(tp_producer *p);
+int tp_producer_id(const tp_producer *p);
+int tp_producer_border(const tp_producer *p);                                  /* getBorder */
+int tp_producer_set_root_quad_size(tp_producer *p, float size);              /* setRootQuadSize */
+int tp_producer_has_tile(const tp_producer *p, int level, int tx, int ty);    /* hasTile */
+tp_tile *tp_producer_get_tile(tp_producer *p, int level, int tx, int ty);    /* getTile */
+tp_tile *tp_producer_find_tile(tp_producer *p, int level, int tx, int ty, int include_cache, int done); /* findTile */
+int tp_producer_put_tile(tp_producer *p, tp_tile *t);                          /* putTile: users left */
+int tp_producer_prefetch_tile(tp_producer *p, int level, int tx, int ty);    /* prefetchTile */
+int tp_producer_invalidate_tiles(tp_producer *p);                             /* invalidateTiles */
+int tp_producer_queued(const tp_producer *p);                                  /* tiles waiting for production */
+int tp_tile_info(const tp_tile *t, int *level, int *tx, int *ty, int *slot, int *users, int *done);
+int tp_scheduler_run(tp_producer *const *producers, int n, void *stream);
+/* A residual producer's tile computed on the host (the reference keeps residual
+ * tiles in CPU storage): `out` is width x width, width the cache's tile width. */
+int tp_residual_tile(tp_producer *p, int level, int tx, int ty, float *out, int width);
+
+/* Residual pyramid files (ResidualProducer.cpp:93-107, 253-340): header
+ * {minLevel, maxLevel, tileSize, rootLevel, rootTx, rootTy, ntiles} and int16
+ * tiles decoded from their deflate TIFF strips. */
+int tp_dat_open(const char *path, tp_dat **out);
+int tp_dat_close(tp_dat *d);
+int tp_dat_info(const tp_dat *d, int *info7, float *scale);
+int tp_dat_read_tile(const tp_dat *d, int level, int tx, int ty, int16_t *out, int capacity, int *width);
+int tp_inflate_zlib(const uint8_t *data, size_t n, uint8_t *out, size_t capacity, size_t *written);
 
 /* ------------------------------------------------------------------------
  * Noise helpers (host).  createDemNoise (ElevationProducer.cpp:50-133) and the

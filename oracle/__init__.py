@@ -76,6 +76,7 @@ def lib():
         L.or_sphere_frame_make.argtypes = [C.c_double, C.c_int, C.c_int, C.c_int, C.POINTER(SphereFrame)]
         L.or_normals_sphere.argtypes = [C.c_int, _f32p, C.c_int, C.POINTER(SphereFrame), _f32p, _f32p, C.c_int]
         L.or_run_jobs.argtypes = [C.POINTER(Job), C.c_int, C.c_int]
+        L.or_residual_upsample.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, _f32p, _f32p]
         L.or_compute_residual.argtypes = [C.c_int, C.c_int, C.c_int, _f32p, _f32p, _f32p,
                                           C.POINTER(C.c_int16), _f32p]
         _LIB = L
@@ -289,3 +290,24 @@ def decode_tiff_strip(blob: bytes) -> bytes:
     if comp == 1:
         return data
     raise ValueError("unsupported TIFF compression %d" % comp)
+
+
+def residual_chain_root(dat, delta, zscale=1.0):
+    """The root residual tile of a producer started `delta` levels below the
+    pyramid's first level: readTile(0), then for i = 1..delta upsample and add
+    readTile(i) (ResidualProducer.cpp:218-225, 268-384)."""
+    W = dat.tile_size + 5
+    scale = np.float32(np.float32(dat.scale) * np.float32(zscale))
+    out = np.zeros((W, W), np.float32)
+    t0 = dat.tile_int16(0, 0, 0)
+    w = t0.shape[0]
+    out[:w, :w] = (t0.astype(np.float32) * scale).astype(np.float32)
+    tmp = np.zeros((W, W), np.float32)
+    for i in range(1, delta + 1):
+        ts = dat.tile_size >> (dat.min_level - i) if i < dat.min_level else dat.tile_size
+        lib().or_residual_upsample(W, ts, 0, 0, _p(out), _p(tmp))
+        ti = dat.tile_int16(i, 0, 0)
+        w = ti.shape[0]
+        out = tmp.copy()
+        out[:w, :w] = (tmp[:w, :w] + (ti.astype(np.float32) * scale)).astype(np.float32)
+    return out

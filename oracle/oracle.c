@@ -667,3 +667,13 @@ void or_compute_residual(int W, int tx, int ty, const float *parent_approx,
             if (approx) approx[o] = z + (float)q;
         }
 }
+
+/* ResidualProducer::upsample (ResidualProducer.cpp:342-384): child of a tile of
+ * `tilesize` intervals at quadrant (tx % 2, ty % 2); both arrays have pitch n. */
+void or_residual_upsample(int n, int tilesize, int tx, int ty, const float *parent, float *out)
+{
+    int px = 1 + (tx % 2) * tilesize / 2, py = 1 + (ty % 2) * tilesize / 2;
+    for (int j = 0; j <= tilesize + 4; ++j)
+        for (int i = 0; i <= tilesize + 4; ++i)
+            out[i + (size_t)j * n] = upsample_sample(parent, n, i, j, px, py);
+}

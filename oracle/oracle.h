@@ -113,6 +113,9 @@ void or_run_jobs(const or_job *jobs, int n, int nthreads);
 void or_compute_residual(int W, int tx, int ty, const float *parent_approx,
                          const float *fine, float *residual_q, int16_t *encoded, float *approx);
 
+/* ResidualProducer::upsample for the small tiles below the pyramid's minLevel. */
+void or_residual_upsample(int n, int tilesize, int tx, int ty, const float *parent, float *out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -38,7 +38,9 @@ def _compile(src, verbose_ptxas=False):
         if verbose_ptxas:
             cmd += ["-Xptxas", "-v"]
     else:
-        cmd = ["g++", "-c", src, "-o", obj, "-O2", "-std=c++17", "-fPIC", "-Wall",
+        # -ffp-contract=off: host arithmetic (residual pyramids) rounds each operation
+        # as written on x86-64 and aarch64 alike
+        cmd = ["g++", "-c", src, "-o", obj, "-O2", "-std=c++17", "-fPIC", "-Wall", "-ffp-contract=off",
                "-I", INCLUDE, "-I", os.path.join(CUDA_HOME, "include")]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:

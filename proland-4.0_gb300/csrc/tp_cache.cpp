@@ -1,0 +1,768 @@
+// TileCache and TileProducer over device slot pools.
+//
+// The cache follows TileCache.cpp:150-377: tiles are keyed by
+// (producer id, level, tx, ty); a tile with users is "used", a tile without is
+// kept in an LRU list of "unused" tiles whose slots are recycled, oldest first,
+// when the storage has no free slot; getTile returns NULL when nothing can be
+// recycled (a full cache).  A tile whose content is not produced yet is queued
+// on its producer together with the tiles it is made from (TileProducer's
+// startCreateTile, e.g. ElevationProducer.cpp:246-271, NormalProducer.cpp:139-156),
+// which are acquired with getTile and released with putTile once it is produced
+// (stopCreateTile).  tp_scheduler_run produces every queued tile of a set of
+// producers: residual tiles on the host (file decode) and one upload, then each
+// elevation producer's queue as one frame launch ordered parents-first, with
+// the normal tiles of the same (level, tx, ty) produced by the same launch.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <list>
+#include <map>
+#include <mutex>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "tp_internal.h"
+
+namespace {
+
+enum Kind { kResidual = 0, kElevation = 1, kNormal = 2 };
+using TKey = std::tuple<int, int, int, int>;  // producer id, level, tx, ty
+
+int next_producer_id()
+{
+    static std::mutex mu;
+    static int next = 1;
+    std::lock_guard<std::mutex> lk(mu);
+    return next++;
+}
+
+}  // namespace
+
+struct tp_tile {
+    int producer_id = 0, level = 0, tx = 0, ty = 0;
+    int slot = -1;
+    int users = 0;
+    bool done = false;    // content produced
+    bool queued = false;  // waiting in its producer's queue
+    // tiles acquired to produce this one, released once it is produced
+    tp_tile *dep_parent = nullptr;
+    tp_producer *dep_parent_owner = nullptr;
+    tp_tile *dep_input = nullptr;  // residual tile (elevation) or elevation tile (normal)
+    tp_producer *dep_input_owner = nullptr;
+};
+
+struct tp_cache {
+    tp_storage *storage = nullptr;
+    std::string name;
+    std::recursive_mutex mu;
+    std::map<TKey, tp_tile *> used;
+    std::list<tp_tile *> lru;  // unused tiles, least recently used first
+    std::map<TKey, std::list<tp_tile *>::iterator> unused;
+    long long queries = 0, misses = 0;
+};
+
+struct tp_producer {
+    Kind kind = kElevation;
+    int id = 0;
+    tp_cache *cache = nullptr;
+    float root_quad_size = 0.0f;
+    std::vector<tp_tile *> queue;
+    // residual producer
+    tp_dat *dat = nullptr;
+    bool own_dat = false;
+    int delta = 0;
+    float zscale = 1.0f;
+    tp_residual_source source = nullptr;
+    void *source_user = nullptr;
+    // elevation producer
+    tp_producer *residuals = nullptr;
+    std::vector<float> noise_amp;
+    tp_elev_params params{};
+    int face = 0;
+    tp_frame *frame = nullptr;
+    // normal producer
+    tp_producer *elevations = nullptr;
+    int deform = 0;
+};
+
+namespace {
+
+TKey key_of(const tp_producer *p, int level, int tx, int ty) { return TKey(p->id, level, tx, ty); }
+
+void release_deps(tp_tile *t);
+
+// Drops a tile that is being recycled: its queued production is cancelled.
+void forget_tile(tp_tile *t, tp_producer *owner)
+{
+    if (t->queued && owner) {
+        auto &q = owner->queue;
+        q.erase(std::remove(q.begin(), q.end(), t), q.end());
+        t->queued = false;
+        release_deps(t);
+    }
+    delete t;
+}
+
+}  // namespace
+
+namespace tp {
+
+// Registry of producers by id, to find a recycled tile's owner.
+static std::mutex g_prod_mu;
+static std::map<int, tp_producer *> g_producers;
+
+static tp_producer *producer_by_id(int id)
+{
+    std::lock_guard<std::mutex> lk(g_prod_mu);
+    auto it = g_producers.find(id);
+    return it == g_producers.end() ? nullptr : it->second;
+}
+
+}  // namespace tp
+
+namespace {
+
+int schedule(tp_producer *p, tp_tile *t);
+int put_tile(tp_producer *p, tp_tile *t);
+
+// TileCache::getTile (TileCache.cpp:174-252).
+tp_tile *get_tile(tp_producer *p, int level, int tx, int ty, int *users_before, int *err)
+{
+    tp_cache *c = p->cache;
+    std::lock_guard<std::recursive_mutex> lk(c->mu);
+    const TKey k = key_of(p, level, tx, ty);
+    tp_tile *t = nullptr;
+    auto u = c->used.find(k);
+    if (u != c->used.end()) {
+        t = u->second;
+    } else {
+        ++c->queries;
+        auto it = c->unused.find(k);
+        if (it != c->unused.end()) {
+            t = *it->second;
+            c->lru.erase(it->second);
+            c->unused.erase(it);
+        } else {
+            int slot = tp_storage_new_slot(c->storage);
+            if (slot < 0 && !c->lru.empty()) {
+                // recycle the least recently used unused tile's slot
+                tp_tile *old = c->lru.front();
+                c->lru.pop_front();
+                c->unused.erase(TKey(old->producer_id, old->level, old->tx, old->ty));
+                slot = old->slot;
+                forget_tile(old, tp::producer_by_id(old->producer_id));
+            }
+            if (slot < 0) {
+                if (err) *err = tp::fail(TP_E_CACHE_FULL, "Insufficient tile cache size (" + c->name + ")");
+                return nullptr;
+            }
+            ++c->misses;
+            t = new tp_tile;
+            t->producer_id = p->id;
+            t->level = level;
+            t->tx = tx;
+            t->ty = ty;
+            t->slot = slot;
+        }
+        c->used[k] = t;
+    }
+    if (users_before) *users_before = t->users;
+    t->users += 1;
+    if (!t->done && !t->queued) {
+        int rc = schedule(p, t);
+        if (rc) {
+            // the tiles it is made from cannot be had: hand it back, unproduced
+            if (err) *err = rc;
+            put_tile(p, t);
+            return nullptr;
+        }
+    }
+    return t;
+}
+
+// TileCache::putTile (TileCache.cpp:312-336).
+int put_tile(tp_producer *p, tp_tile *t)
+{
+    tp_cache *c = p->cache;
+    std::lock_guard<std::recursive_mutex> lk(c->mu);
+    t->users -= 1;
+    if (t->users == 0) {
+        const TKey k = key_of(p, t->level, t->tx, t->ty);
+        c->used.erase(k);
+        c->lru.push_back(t);
+        c->unused[k] = std::prev(c->lru.end());
+    }
+    return t->users;
+}
+
+void release_deps(tp_tile *t)
+{
+    if (t->dep_parent) put_tile(t->dep_parent_owner, t->dep_parent);
+    if (t->dep_input) put_tile(t->dep_input_owner, t->dep_input);
+    t->dep_parent = t->dep_input = nullptr;
+    t->dep_parent_owner = t->dep_input_owner = nullptr;
+}
+
+bool residual_has_tile(const tp_producer *r, int level, int tx, int ty);
+
+// startCreateTile: acquire the tiles this tile is made from, then queue it.
+int schedule(tp_producer *p, tp_tile *t)
+{
+    int err = TP_OK;
+    if (p->kind == kElevation) {
+        if (t->level > 0) {
+            t->dep_parent = get_tile(p, t->level - 1, t->tx / 2, t->ty / 2, nullptr, &err);
+            if (!t->dep_parent) return err ? err : tp::fail(TP_E_CACHE_FULL, "cache full (parent)");
+            t->dep_parent_owner = p;
+        }
+        if (p->residuals) {
+            const int n = p->cache->storage->W - 5;
+            const int mod = (p->residuals->cache->storage->W - 5) / n;
+            if (residual_has_tile(p->residuals, t->level, t->tx / mod, t->ty / mod)) {
+                t->dep_input = get_tile(p->residuals, t->level, t->tx / mod, t->ty / mod, nullptr, &err);
+                if (!t->dep_input) {
+                    release_deps(t);
+                    return err ? err : tp::fail(TP_E_CACHE_FULL, "cache full (residual)");
+                }
+                t->dep_input_owner = p->residuals;
+            }
+        }
+    } else if (p->kind == kNormal) {
+        t->dep_input = get_tile(p->elevations, t->level, t->tx, t->ty, nullptr, &err);
+        if (!t->dep_input) return err ? err : tp::fail(TP_E_CACHE_FULL, "cache full (elevation)");
+        t->dep_input_owner = p->elevations;
+        if (t->level > 0) {
+            t->dep_parent = get_tile(p, t->level - 1, t->tx / 2, t->ty / 2, nullptr, &err);
+            if (!t->dep_parent) {
+                release_deps(t);
+                return err ? err : tp::fail(TP_E_CACHE_FULL, "cache full (parent normals)");
+            }
+            t->dep_parent_owner = p;
+        }
+    }
+    t->queued = true;
+    p->queue.push_back(t);
+    return TP_OK;
+}
+
+// ResidualProducer::hasTile (ResidualProducer.cpp:161-175).
+bool residual_has_tile(const tp_producer *r, int level, int tx, int ty)
+{
+    if (!r->dat) return true;  // synthetic source or zero residuals: every tile exists
+    const int l = level + r->delta - r->dat->root_level;
+    return l >= 0 && (tx >> l) == r->dat->root_tx && (ty >> l) == r->dat->root_ty && l <= r->dat->max_level;
+}
+
+// ResidualProducer::upsample (ResidualProducer.cpp:342-384): 2x interpolation of
+// a tile of `tilesize` intervals into its child at (tx % 2, ty % 2); n is the
+// pitch of both arrays.  Used only to chain the pyramid's levels up to the
+// root when the producer starts `delta` levels below the file's first level.
+void upsample_small(int level_tilesize, int tx, int ty, const float *parent, float *out, int pitch)
+{
+    const int ts = level_tilesize;
+    const int px = 1 + (tx % 2) * ts / 2, py = 1 + (ty % 2) * ts / 2;
+    for (int j = 0; j <= ts + 4; ++j)
+        for (int i = 0; i <= ts + 4; ++i) {
+            const float *cc = parent + (i / 2 + px) + (size_t)(j / 2 + py) * pitch;
+            float z;
+            if ((j & 1) == 0) {
+                z = (i & 1) == 0 ? cc[0] : ((cc[0] + cc[1]) * 9 - (cc[-1] + cc[2])) / 16;
+            } else if ((i & 1) == 0) {
+                z = ((cc[0] + cc[pitch]) * 9 - (cc[-pitch] + cc[2 * pitch])) / 16;
+            } else {
+                z = 0;
+                for (int dj = -1; dj <= 2; ++dj) {
+                    const float f = (dj == -1 || dj == 2) ? -1 / 16.0f : 9 / 16.0f;
+                    for (int di = -1; di <= 2; ++di) {
+                        const float g = (di == -1 || di == 2) ? -1 / 16.0f : 9 / 16.0f;
+                        z += f * g * cc[di + (ptrdiff_t)dj * pitch];
+                    }
+                }
+            }
+            out[i + (size_t)j * pitch] = z;
+        }
+}
+
+// ResidualProducer::doCreateTile + readTile (ResidualProducer.cpp:177-232,
+// 268-340) into a dense Wr x Wr host tile.
+int produce_residual(tp_producer *r, const tp_tile *t, float *out)
+{
+    const int Wr = r->cache->storage->W;
+    std::fill(out, out + (size_t)Wr * Wr, 0.0f);
+    if (r->source) {
+        int rc = r->source(r->source_user, t->level, t->tx, t->ty, out, Wr);
+        return rc ? tp::fail(TP_E_IO, "residual source callback failed") : TP_OK;
+    }
+    if (!r->dat) return TP_OK;  // zero residuals
+    const tp_dat *d = r->dat;
+    int level = t->level + r->delta - d->root_level;
+    if (level < 0 || (t->tx >> level) != d->root_tx || (t->ty >> level) != d->root_ty) return TP_OK;
+    const int tx = t->tx - (d->root_tx << level), ty = t->ty - (d->root_ty << level);
+    const float scale = d->scale * r->zscale;
+    if (d->tile_size + 5 != Wr) return tp::fail(TP_E_BAD_ARG, "residual storage width does not match the file");
+    auto read = [&](int lv, int x, int y, const float *base) -> int {
+        std::vector<int16_t> v;
+        int w = 0;
+        int rc = tp::dat_tile_int16(d, lv, x, y, v, &w);
+        if (rc) return rc;
+        for (int j = 0; j < w; ++j)
+            for (int i = 0; i < w; ++i) {
+                const size_t o = i + (size_t)j * Wr;
+                out[o] = base ? base[o] + v[i + (size_t)j * w] * scale : v[i + (size_t)j * w] * scale;
+            }
+        return TP_OK;
+    };
+    if (r->delta > 0 && level == r->delta) {
+        // the root of a producer started delta levels down: chain levels 0..delta
+        std::vector<float> tmp((size_t)Wr * Wr);
+        int rc = read(0, 0, 0, nullptr);
+        for (int i = 1; i <= r->delta && !rc; ++i) {
+            const int ts = (i < d->min_level ? d->tile_size >> (d->min_level - i) : d->tile_size);
+            upsample_small(ts, 0, 0, out, tmp.data(), Wr);
+            rc = read(i, 0, 0, tmp.data());
+        }
+        return rc;
+    }
+    return read(level, tx, ty, nullptr);
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------- C ABI: cache
+extern "C" int tp_cache_create(tp_storage *storage, const char *name, tp_cache **out)
+{
+    if (!storage || !out) return tp::fail(TP_E_BAD_ARG, "tp_cache_create: bad arguments");
+    auto *c = new tp_cache;
+    c->storage = storage;
+    c->name = name ? name : "";
+    *out = c;
+    return TP_OK;
+}
+
+extern "C" int tp_cache_destroy(tp_cache *c)
+{
+    if (!c) return TP_OK;
+    for (auto &kv : c->used) delete kv.second;
+    for (tp_tile *t : c->lru) delete t;
+    delete c;
+    return TP_OK;
+}
+
+extern "C" int tp_cache_used_tiles(tp_cache *c)
+{
+    if (!c) return TP_E_BAD_ARG;
+    std::lock_guard<std::recursive_mutex> lk(c->mu);
+    return (int)c->used.size();
+}
+
+extern "C" int tp_cache_unused_tiles(tp_cache *c)
+{
+    if (!c) return TP_E_BAD_ARG;
+    std::lock_guard<std::recursive_mutex> lk(c->mu);
+    return (int)c->lru.size();
+}
+
+extern "C" int tp_cache_stats(tp_cache *c, long long *queries, long long *misses)
+{
+    if (!c) return TP_E_BAD_ARG;
+    std::lock_guard<std::recursive_mutex> lk(c->mu);
+    if (queries) *queries = c->queries;
+    if (misses) *misses = c->misses;
+    return TP_OK;
+}
+
+// ---------------------------------------------------------------- C ABI: producers
+static tp_producer *new_producer(Kind kind, tp_cache *cache)
+{
+    auto *p = new tp_producer;
+    p->kind = kind;
+    p->id = next_producer_id();
+    p->cache = cache;
+    std::lock_guard<std::mutex> lk(tp::g_prod_mu);
+    tp::g_producers[p->id] = p;
+    return p;
+}
+
+extern "C" int tp_residual_producer_create(tp_cache *cache, const char *file, int delta, float zscale,
+                                           tp_producer **out)
+{
+    if (!cache || !out) return tp::fail(TP_E_BAD_ARG, "tp_residual_producer_create: bad arguments");
+    *out = nullptr;
+    tp_dat *d = nullptr;
+    if (file && file[0]) {
+        int rc = tp_dat_open(file, &d);
+        if (rc) return rc;
+        if (delta < 0 || delta > d->min_level) {
+            tp_dat_close(d);
+            return tp::fail(TP_E_BAD_ARG, "tp_residual_producer_create: delta must be in [0, minLevel]");
+        }
+        if (d->tile_size + 5 != cache->storage->W) {
+            tp_dat_close(d);
+            return tp::fail(TP_E_BAD_ARG, "residual cache tile width does not match the file's tileSize + 5");
+        }
+    }
+    tp_producer *p = new_producer(kResidual, cache);
+    p->dat = d;
+    p->own_dat = d != nullptr;
+    p->delta = d && d->root_level == 0 ? delta : 0;
+    p->zscale = zscale;
+    *out = p;
+    return TP_OK;
+}
+
+extern "C" int tp_residual_producer_set_source(tp_producer *p, tp_residual_source fn, void *user)
+{
+    if (!p || p->kind != kResidual) return tp::fail(TP_E_BAD_ARG, "tp_residual_producer_set_source: not a residual producer");
+    p->source = fn;
+    p->source_user = user;
+    return TP_OK;
+}
+
+extern "C" int tp_elevation_producer_create(tp_cache *cache, tp_producer *residuals, const float *noise_amp, int n_noise,
+                                            const tp_elev_params *params, int face, tp_producer **out)
+{
+    if (!cache || !params || !out || n_noise < 0 || (n_noise > 0 && !noise_amp))
+        return tp::fail(TP_E_BAD_ARG, "tp_elevation_producer_create: bad arguments");
+    if (cache->storage->channels != 3) return tp::fail(TP_E_BAD_ARG, "elevation cache must have 3-channel slots");
+    if (residuals && residuals->kind != kResidual) return tp::fail(TP_E_BAD_ARG, "residuals must be a residual producer");
+    tp_producer *p = new_producer(kElevation, cache);
+    p->residuals = residuals;
+    p->noise_amp.assign(noise_amp, noise_amp + n_noise);
+    p->params = *params;
+    p->face = face;
+    *out = p;
+    return TP_OK;
+}
+
+extern "C" int tp_normal_producer_create(tp_cache *cache, tp_producer *elevations, int deform, tp_producer **out)
+{
+    if (!cache || !elevations || !out || elevations->kind != kElevation)
+        return tp::fail(TP_E_BAD_ARG, "tp_normal_producer_create: bad arguments");
+    if (cache->storage->channels != 2 || cache->storage->W != elevations->cache->storage->W - 4)
+        return tp::fail(TP_E_BAD_ARG, "normal cache must have 2-channel slots of width W - 4");
+    if (deform) return tp::fail(TP_E_BAD_ARG, "spherical deformation is produced by tp_normals_sphere");
+    tp_producer *p = new_producer(kNormal, cache);
+    p->elevations = elevations;
+    p->deform = deform;
+    *out = p;
+    return TP_OK;
+}
+
+extern "C" int tp_producer_destroy(tp_producer *p)
+{
+    if (!p) return TP_OK;
+    {
+        std::lock_guard<std::mutex> lk(tp::g_prod_mu);
+        tp::g_producers.erase(p->id);
+    }
+    if (p->frame) tp_frame_destroy(p->frame);
+    if (p->own_dat) tp_dat_close(p->dat);
+    delete p;
+    return TP_OK;
+}
+
+extern "C" int tp_producer_id(const tp_producer *p) { return p ? p->id : TP_E_BAD_ARG; }
+
+extern "C" int tp_producer_border(const tp_producer *p)
+{
+    if (!p) return TP_E_BAD_ARG;
+    return p->kind == kNormal ? 0 : 2;  // ElevationProducer.cpp:235-239, NormalProducer.cpp:124-127
+}
+
+extern "C" int tp_producer_set_root_quad_size(tp_producer *p, float size)
+{
+    if (!p || !(size > 0.0f)) return tp::fail(TP_E_BAD_ARG, "tp_producer_set_root_quad_size: bad arguments");
+    p->root_quad_size = size;
+    if (p->kind == kElevation && p->residuals) p->residuals->root_quad_size = size;
+    if (p->kind == kNormal) tp_producer_set_root_quad_size(p->elevations, size);
+    return TP_OK;
+}
+
+extern "C" int tp_producer_has_tile(const tp_producer *p, int level, int tx, int ty)
+{
+    if (!p) return TP_E_BAD_ARG;
+    if (p->kind == kResidual) return residual_has_tile(p, level, tx, ty) ? 1 : 0;
+    if (p->kind == kNormal) return tp_producer_has_tile(p->elevations, level, tx, ty);
+    return level >= 0 && tx >= 0 && ty >= 0 && (tx >> level) == 0 && (ty >> level) == 0 ? 1 : 0;
+}
+
+extern "C" tp_tile *tp_producer_get_tile(tp_producer *p, int level, int tx, int ty)
+{
+    if (!p || level < 0 || level > 30 || tx < 0 || ty < 0 || (tx >> level) != 0 || (ty >> level) != 0) {
+        tp::fail(TP_E_BAD_ARG, "tp_producer_get_tile: bad arguments");
+        return nullptr;
+    }
+    int err = TP_OK;
+    return get_tile(p, level, tx, ty, nullptr, &err);
+}
+
+extern "C" tp_tile *tp_producer_find_tile(tp_producer *p, int level, int tx, int ty, int include_cache, int done)
+{
+    if (!p) return nullptr;
+    tp_cache *c = p->cache;
+    std::lock_guard<std::recursive_mutex> lk(c->mu);
+    const TKey k = key_of(p, level, tx, ty);
+    tp_tile *t = nullptr;
+    auto u = c->used.find(k);
+    if (u != c->used.end()) t = u->second;
+    if (!t && include_cache) {
+        auto it = c->unused.find(k);
+        if (it != c->unused.end()) t = *it->second;
+    }
+    if (t && done && !t->done) t = nullptr;
+    return t;
+}
+
+extern "C" int tp_producer_put_tile(tp_producer *p, tp_tile *t)
+{
+    if (!p || !t || t->producer_id != p->id || t->users <= 0)
+        return tp::fail(TP_E_BAD_ARG, "tp_producer_put_tile: tile not held");
+    return put_tile(p, t);
+}
+
+// TileCache::prefetchTile (TileCache.cpp:254-310): create the tile (queued for
+// production) among the unused tiles; 1 if a tile was created, 0 if it exists
+// or the cache is full.
+extern "C" int tp_producer_prefetch_tile(tp_producer *p, int level, int tx, int ty)
+{
+    if (!p || level < 0 || level > 30 || tx < 0 || ty < 0 || (tx >> level) != 0 || (ty >> level) != 0)
+        return tp::fail(TP_E_BAD_ARG, "tp_producer_prefetch_tile: bad arguments");
+    tp_cache *c = p->cache;
+    std::lock_guard<std::recursive_mutex> lk(c->mu);
+    const TKey k = key_of(p, level, tx, ty);
+    if (c->used.count(k) || c->unused.count(k)) return 0;
+    int err = TP_OK;
+    tp_tile *t = get_tile(p, level, tx, ty, nullptr, &err);
+    if (!t) return err == TP_E_CACHE_FULL ? 0 : err;
+    put_tile(p, t);  // keep it, unused, at the back of the LRU list
+    return 1;
+}
+
+// TileCache::invalidateTiles (TileCache.cpp:338-377): every tile of the
+// producer is produced again before its next use.
+extern "C" int tp_producer_invalidate_tiles(tp_producer *p)
+{
+    if (!p) return tp::fail(TP_E_BAD_ARG, "tp_producer_invalidate_tiles: bad arguments");
+    tp_cache *c = p->cache;
+    std::lock_guard<std::recursive_mutex> lk(c->mu);
+    for (auto &kv : c->used)
+        if (kv.second->producer_id == p->id) {
+            kv.second->done = false;
+            if (!kv.second->queued) {
+                int rc = schedule(p, kv.second);
+                if (rc) return rc;
+            }
+        }
+    for (tp_tile *t : c->lru)
+        if (t->producer_id == p->id) t->done = false;
+    return TP_OK;
+}
+
+extern "C" int tp_producer_queued(const tp_producer *p) { return p ? (int)p->queue.size() : TP_E_BAD_ARG; }
+
+// ResidualProducer::doCreateTile on a host tile: the residual tile (level, tx, ty)
+// as the producer would upload it (width = the residual cache's tile width).
+extern "C" int tp_residual_tile(tp_producer *p, int level, int tx, int ty, float *out, int width)
+{
+    if (!p || p->kind != kResidual || !out || width != p->cache->storage->W || level < 0 || level > 30 || tx < 0 ||
+        ty < 0 || (tx >> level) != 0 || (ty >> level) != 0)
+        return tp::fail(TP_E_BAD_ARG, "tp_residual_tile: bad arguments");
+    tp_tile t;
+    t.level = level;
+    t.tx = tx;
+    t.ty = ty;
+    return produce_residual(p, &t, out);
+}
+
+extern "C" int tp_tile_info(const tp_tile *t, int *level, int *tx, int *ty, int *slot, int *users, int *done)
+{
+    if (!t) return tp::fail(TP_E_BAD_ARG, "tp_tile_info: tile is NULL");
+    if (level) *level = t->level;
+    if (tx) *tx = t->tx;
+    if (ty) *ty = t->ty;
+    if (slot) *slot = t->slot;
+    if (users) *users = t->users;
+    if (done) *done = t->done ? 1 : 0;
+    return TP_OK;
+}
+
+// ---------------------------------------------------------------- scheduler
+namespace {
+
+int run_residuals(tp_producer *r, void *stream)
+{
+    if (r->queue.empty()) return TP_OK;
+    tp_storage *s = r->cache->storage;
+    const int Wr = s->W;
+    const size_t per = (size_t)Wr * Wr;
+    std::vector<float> host(per * r->queue.size());
+    std::vector<int> slots;
+    for (size_t k = 0; k < r->queue.size(); ++k) {
+        int rc = produce_residual(r, r->queue[k], host.data() + k * per);
+        if (rc) return rc;
+        slots.push_back(r->queue[k]->slot);
+    }
+    if (s->on_device == 1) {
+        int rc = tp::staged_copy_slots(s, slots.data(), (int)slots.size(), 0, host.data(), stream);
+        if (rc) return rc;
+        // the host buffer must live until the copy has read it
+        cudaError_t e = cudaStreamSynchronize(static_cast<cudaStream_t>(stream));
+        if (e != cudaSuccess) return tp::cuda_fail("cudaStreamSynchronize (residual upload)", e);
+    }
+    for (tp_tile *t : r->queue) {
+        t->done = true;
+        t->queued = false;
+    }
+    r->queue.clear();
+    return TP_OK;
+}
+
+int run_elevations(tp_producer *e, tp_producer *normals, void *stream)
+{
+    // normal tiles whose elevation tile is produced by this same launch are fused in
+    std::map<const tp_tile *, tp_tile *> fused;  // elevation tile -> normal tile
+    if (normals)
+        for (tp_tile *nt : normals->queue)
+            if (nt->dep_input && nt->dep_input->queued) fused[nt->dep_input] = nt;
+    if (e->queue.empty()) return TP_OK;
+    if (!(e->root_quad_size > 0.0f)) return tp::fail(TP_E_BAD_ARG, "elevation producer: root quad size not set");
+    std::vector<tp_tile *> q = e->queue;
+    std::stable_sort(q.begin(), q.end(), [](const tp_tile *a, const tp_tile *b) { return a->level < b->level; });
+    std::map<const tp_tile *, int> index;
+    for (size_t k = 0; k < q.size(); ++k) index[q[k]] = (int)k;
+    const int n = e->cache->storage->W - 5;
+    const int mod = e->residuals ? (e->residuals->cache->storage->W - 5) / n : 1;
+    std::vector<tp_tile_job> jobs(q.size());
+    for (size_t k = 0; k < q.size(); ++k) {
+        const tp_tile *t = q[k];
+        tp_tile_job &j = jobs[k];
+        std::memset(&j, 0, sizeof j);
+        j.level = t->level;
+        j.tx = t->tx;
+        j.ty = t->ty;
+        j.out_slot = t->slot;
+        j.parent_slot = t->dep_parent ? t->dep_parent->slot : -1;
+        j.parent_job = -1;
+        if (t->dep_parent) {
+            auto it = index.find(t->dep_parent);
+            if (it != index.end()) j.parent_job = it->second;
+            else if (!t->dep_parent->done) return tp::fail(TP_E_MISSING_PARENT, "elevation parent tile is not produced");
+        }
+        j.residual_slot = t->dep_input ? t->dep_input->slot : -1;
+        j.rx = (t->tx % mod) * n;
+        j.ry = (t->ty % mod) * n;
+        j.rscale = 1.0f;
+        auto f = fused.find(t);
+        j.normal_slot = f != fused.end() ? f->second->slot : -1;
+        int rot = 0, layer = 0;
+        tp_noise_select(e->face, t->level, t->tx, t->ty, &rot, &layer);
+        j.noise_rot = rot;
+        j.noise_layer = layer;
+        j.noise_amp = t->level < (int)e->noise_amp.size() ? e->noise_amp[t->level] : 0.0f;
+        j.tile_meters = e->root_quad_size / (float)(1u << t->level);
+    }
+    if (!e->frame) tp_frame_create(&e->frame);
+    tp_frame_clear(e->frame);
+    int rc = tp_frame_add(e->frame, e->cache->storage, e->residuals ? e->residuals->cache->storage : nullptr,
+                          normals && !fused.empty() ? normals->cache->storage : nullptr, &e->params, jobs.data(),
+                          (int)jobs.size());
+    if (rc) return rc;
+    rc = tp_frame_launch(e->frame, stream);
+    if (rc) return rc;
+    for (tp_tile *t : q) {
+        t->done = true;
+        t->queued = false;
+        release_deps(t);
+    }
+    e->queue.clear();
+    if (normals) {
+        std::vector<tp_tile *> rest;
+        for (tp_tile *nt : normals->queue) {
+            bool was_fused = false;
+            for (auto &kv : fused)
+                if (kv.second == nt) was_fused = true;
+            if (was_fused) {
+                nt->done = true;
+                nt->queued = false;
+                release_deps(nt);
+            } else {
+                rest.push_back(nt);
+            }
+        }
+        normals->queue.swap(rest);
+    }
+    return TP_OK;
+}
+
+int run_normals(tp_producer *np, void *stream)
+{
+    if (np->queue.empty()) return TP_OK;
+    tp_producer *e = np->elevations;
+    if (!(e->root_quad_size > 0.0f)) return tp::fail(TP_E_BAD_ARG, "normal producer: root quad size not set");
+    std::vector<int> eslot, nslot;
+    std::vector<float> meters;
+    for (tp_tile *t : np->queue) {
+        if (!t->dep_input || !t->dep_input->done) return tp::fail(TP_E_MISSING_PARENT, "normal tile's elevation is not produced");
+        eslot.push_back(t->dep_input->slot);
+        nslot.push_back(t->slot);
+        meters.push_back(e->root_quad_size / (float)(1u << t->level));
+    }
+    int rc = tp::launch_normals(e->cache->storage, np->cache->storage, eslot.data(), nslot.data(), meters.data(),
+                                (int)eslot.size(), stream);
+    if (rc) return rc;
+    for (tp_tile *t : np->queue) {
+        t->done = true;
+        t->queued = false;
+        release_deps(t);
+    }
+    np->queue.clear();
+    return TP_OK;
+}
+
+}  // namespace
+
+// Produces every queued tile of the given producers (and of the producers they
+// use): residuals, then elevations (with fused normals), then other normals.
+extern "C" int tp_scheduler_run(tp_producer *const *producers, int n, void *stream)
+{
+    if (n < 0 || (n > 0 && !producers)) return tp::fail(TP_E_BAD_ARG, "tp_scheduler_run: bad arguments");
+    std::vector<tp_producer *> res, elev, nrm;
+    auto add = [](std::vector<tp_producer *> &v, tp_producer *p) {
+        if (p && std::find(v.begin(), v.end(), p) == v.end()) v.push_back(p);
+    };
+    for (int k = 0; k < n; ++k) {
+        tp_producer *p = producers[k];
+        if (!p) continue;
+        if (p->kind == kNormal) {
+            add(nrm, p);
+            p = p->elevations;
+        }
+        if (p->kind == kElevation) {
+            add(elev, p);
+            p = p->residuals;
+        }
+        if (p && p->kind == kResidual) add(res, p);
+    }
+    for (tp_producer *r : res) {
+        int rc = run_residuals(r, stream);
+        if (rc) return rc;
+    }
+    for (tp_producer *e : elev) {
+        tp_producer *fuse = nullptr;
+        for (tp_producer *np : nrm)
+            if (np->elevations == e) {
+                fuse = np;
+                break;
+            }
+        int rc = run_elevations(e, fuse, stream);
+        if (rc) return rc;
+    }
+    for (tp_producer *np : nrm) {
+        int rc = run_normals(np, stream);
+        if (rc) return rc;
+    }
+    return TP_OK;
+}

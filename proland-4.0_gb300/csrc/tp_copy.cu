@@ -10,8 +10,10 @@
 namespace {
 
 // One warp per row: dense row (count * W rows in all) <-> slot plane row.
+// slot_map (device, optional): slot of each dense tile; consecutive slots otherwise.
 __global__ void __launch_bounds__(256) repack_rows(const float *__restrict__ src, float *__restrict__ dst, int W,
-                                                   int pitch, long long slot_stride, long long rows, bool to_slots)
+                                                   int pitch, long long slot_stride, long long rows, bool to_slots,
+                                                   const int *__restrict__ slot_map)
 {
     const long long row = (long long)blockIdx.x * 8 + (threadIdx.x >> 5);
     if (row >= rows) return;
@@ -19,7 +21,7 @@ __global__ void __launch_bounds__(256) repack_rows(const float *__restrict__ src
     const long long tile = row / W;
     const int r = (int)(row - tile * W);
     const long long dense = row * W;
-    const long long slot = tile * slot_stride + (long long)r * pitch;
+    const long long slot = (slot_map ? (long long)slot_map[tile] : tile) * slot_stride + (long long)r * pitch;
     if (to_slots) {
         for (int i = lane; i < W; i += 32) dst[slot + i] = __ldg(src + dense + i);
     } else {
@@ -58,10 +60,10 @@ int staged_copy(tp_storage *s, int first, int count, int channel, float *host, b
         e = cudaMemcpyAsync(s->staging, host, bytes, cudaMemcpyHostToDevice, st);
         if (e != cudaSuccess) return cuda_fail("cudaMemcpyAsync (upload)", e);
         repack_rows<<<blocks, 256, 0, st>>>(static_cast<const float *>(s->staging), plane, s->W, s->pitch,
-                                            s->slot_stride, rows, true);
+                                            s->slot_stride, rows, true, nullptr);
     } else {
         repack_rows<<<blocks, 256, 0, st>>>(plane, static_cast<float *>(s->staging), s->W, s->pitch, s->slot_stride,
-                                            rows, false);
+                                            rows, false, nullptr);
     }
     e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_fail("repack kernel launch", e);
@@ -69,6 +71,29 @@ int staged_copy(tp_storage *s, int first, int count, int channel, float *host, b
         e = cudaMemcpyAsync(host, s->staging, bytes, cudaMemcpyDeviceToHost, st);
         if (e != cudaSuccess) return cuda_fail("cudaMemcpyAsync (download)", e);
     }
+    return TP_OK;
+}
+
+int staged_copy_slots(tp_storage *s, const int *slots, int count, int channel, const float *host, void *stream)
+{
+    if (count <= 0) return TP_OK;
+    for (int k = 0; k < count; ++k)
+        if (slots[k] < 0 || slots[k] >= s->capacity) return fail(TP_E_BAD_ARG, "upload: slot out of range");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const size_t bytes = sizeof(float) * (size_t)count * s->W * s->W;
+    std::lock_guard<std::mutex> lk(s->copy_mu);
+    int rc = ensure_staging(s, bytes + sizeof(int) * (size_t)count + 256);
+    if (rc) return rc;
+    int *dmap = reinterpret_cast<int *>(static_cast<char *>(s->staging) + ((bytes + 255) & ~(size_t)255));
+    cudaError_t e = cudaMemcpyAsync(s->staging, host, bytes, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dmap, slots, sizeof(int) * count, cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) return cuda_fail("cudaMemcpyAsync (slot upload)", e);
+    float *plane = s->base + (long long)channel * s->plane_stride;
+    const long long rows = (long long)count * s->W;
+    repack_rows<<<(unsigned)((rows + 7) / 8), 256, 0, st>>>(static_cast<const float *>(s->staging), plane, s->W,
+                                                            s->pitch, s->slot_stride, rows, true, dmap);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail("repack kernel launch", e);
     return TP_OK;
 }
 

@@ -55,7 +55,7 @@ int setup_class(tp_frame::Class &k)
     tp_storage *elev = k.elev, *res = k.res, *nrm = k.nrm;
     const tp_elev_params *p = &k.params;
     if (!elev) return tp::fail(TP_E_BAD_ARG, "frame: an elevation storage is required");
-    if (!elev->on_device || elev->channels != 3)
+    if (elev->on_device != 1 || elev->channels != 3)
         return tp::fail(TP_E_BAD_ARG, "frame: elevation storage must be a device storage with 3 channels");
     const int W = elev->W, n = W - 5;
     if (n < 8 || n % 8 != 0) return tp::fail(TP_E_BAD_ARG, "frame: tile width must be 8k + 5");
@@ -64,13 +64,13 @@ int setup_class(tp_frame::Class &k)
         return tp::fail(TP_E_BAD_ARG, "frame: grid_size must divide the tile size");
     if (p->noise_mode != 0 && p->noise_mode != 1) return tp::fail(TP_E_BAD_ARG, "frame: bad noise_mode");
     if (res) {
-        if (!res->on_device || res->channels != 1)
+        if (res->on_device != 1 || res->channels != 1)
             return tp::fail(TP_E_BAD_ARG, "frame: residual storage must be 1-channel device storage");
         if ((res->W - 5) % n != 0)
             return tp::fail(TP_E_BAD_ARG, "frame: residual tile size must be a multiple of the tile size");
     }
     if (nrm) {
-        if (!nrm->on_device || nrm->channels != 2 || nrm->W != W - 4)
+        if (nrm->on_device != 1 || nrm->channels != 2 || nrm->W != W - 4)
             return tp::fail(TP_E_BAD_ARG, "frame: normal storage must be 2-channel device storage of width W - 4");
         if (p->normal_format != 2)
             return tp::fail(TP_E_BAD_ARG, "frame: only normal format 2 (signed fp32) is supported");

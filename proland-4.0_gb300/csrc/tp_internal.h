@@ -32,7 +32,7 @@ struct tp_storage {
     int pitch = 0;        // floats per row (W rounded up to 8: rows start on 32-byte sectors)
     long long plane_stride = 0;  // W * pitch floats
     long long slot_stride = 0;   // channels * plane_stride floats
-    bool on_device = true;
+    int on_device = 1;            // 1 device memory, 0 pinned host memory, 2 none (bookkeeping only)
     float *base = nullptr;
     std::vector<int> free_list;  // stack of free slot indices
     std::vector<uint8_t> in_use;
@@ -45,6 +45,15 @@ struct tp_storage {
     void *staging = nullptr;
     size_t staging_bytes = 0;
     std::mutex copy_mu;
+};
+
+// A residual pyramid file held in memory (header fields and all its bytes).
+struct tp_dat {
+    int min_level = 0, max_level = -1, tile_size = 0, root_level = 0, root_tx = 0, root_ty = 0;
+    float scale = 1.0f;
+    int ntiles = 0;
+    std::vector<uint8_t> bytes;  // whole file
+    size_t header = 0;
 };
 
 namespace tp {
@@ -102,5 +111,14 @@ int frame_occupancy(int stage_floats, int stages, int minb, bool mod, int *block
 // through the storage's staging buffer (one linear copy + a repack kernel).
 int staged_copy(tp_storage *s, int first, int count, int channel, float *host, bool up, void *stream);
 int read_status(int *status, bool clear);
+// Uploads `count` dense host tiles into the given (not necessarily consecutive) slots.
+int staged_copy_slots(tp_storage *s, const int *slots, int count, int channel, const float *host, void *stream);
+// Normal tiles from produced elevation tiles (flat deformation).
+int launch_normals(tp_storage *elev, tp_storage *nrm, const int *eslots, const int *nslots, const float *meters,
+                   int count, void *stream);
+// Residual pyramid files.
+int dat_tile_width(const tp_dat *d, int level);
+int dat_tile_id(const tp_dat *d, int level, int tx, int ty);
+int dat_tile_int16(const tp_dat *d, int level, int tx, int ty, std::vector<int16_t> &out, int *width);
 
 }  // namespace tp

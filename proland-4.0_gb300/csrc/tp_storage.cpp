@@ -48,9 +48,10 @@ extern "C" int tp_storage_create(int tile_width, int channels, int capacity, int
 {
     if (!out) return tp::fail(TP_E_BAD_ARG, "tp_storage_create: out is NULL");
     *out = nullptr;
-    if (tile_width < 5 || tile_width > 4096 || channels < 1 || channels > 8 || capacity < 1)
-        return tp::fail(TP_E_BAD_ARG, "tp_storage_create: bad tile_width / channels / capacity");
-    if (on_device && !tp_device_available()) return tp::fail(TP_E_NO_DEVICE, "no CUDA device");
+    if (tile_width < 5 || tile_width > 4096 || channels < 1 || channels > 8 || capacity < 1 || on_device < 0 ||
+        on_device > 2)
+        return tp::fail(TP_E_BAD_ARG, "tp_storage_create: bad tile_width / channels / capacity / memory kind");
+    if (on_device != 2 && !tp_device_available()) return tp::fail(TP_E_NO_DEVICE, "no CUDA device");
     auto *s = new tp_storage;
     s->W = tile_width;
     s->channels = channels;
@@ -58,18 +59,21 @@ extern "C" int tp_storage_create(int tile_width, int channels, int capacity, int
     s->pitch = tp::round_up(tile_width, 8);
     s->plane_stride = (long long)tile_width * s->pitch;
     s->slot_stride = s->plane_stride * channels;
-    s->on_device = on_device != 0;
+    s->on_device = on_device;
     size_t bytes = sizeof(float) * (size_t)s->slot_stride * capacity;
-    cudaError_t e = s->on_device ? cudaMalloc(&s->base, bytes) : cudaMallocHost(&s->base, bytes);
-    if (e != cudaSuccess) {
-        delete s;
-        return tp::cuda_fail("tp_storage_create: allocation", e);
-    }
-    e = s->on_device ? cudaMemset(s->base, 0, bytes) : (std::memset(s->base, 0, bytes), cudaSuccess);
-    if (e != cudaSuccess) {
-        cudaFree(s->base);
-        delete s;
-        return tp::cuda_fail("tp_storage_create: memset", e);
+    if (on_device != 2) {
+        cudaError_t e = on_device == 1 ? cudaMalloc(&s->base, bytes) : cudaMallocHost(&s->base, bytes);
+        if (e != cudaSuccess) {
+            delete s;
+            return tp::cuda_fail("tp_storage_create: allocation", e);
+        }
+        e = on_device == 1 ? cudaMemset(s->base, 0, bytes) : (std::memset(s->base, 0, bytes), cudaSuccess);
+        if (e != cudaSuccess) {
+            if (on_device == 1) cudaFree(s->base);
+            else cudaFreeHost(s->base);
+            delete s;
+            return tp::cuda_fail("tp_storage_create: memset", e);
+        }
     }
     s->in_use.assign(capacity, 0);
     s->free_list.reserve(capacity);
@@ -82,8 +86,8 @@ extern "C" int tp_storage_destroy(tp_storage *s)
 {
     if (!s) return TP_OK;
     if (s->base) {
-        if (s->on_device) cudaFree(s->base);
-        else cudaFreeHost(s->base);
+        if (s->on_device == 1) cudaFree(s->base);
+        else if (s->on_device == 0) cudaFreeHost(s->base);
     }
     if (s->batch_frame) tp_frame_destroy(s->batch_frame);
     if (s->staging) cudaFree(s->staging);
@@ -135,7 +139,8 @@ static int storage_copy(tp_storage *s, int first, int count, int channel, float 
 {
     if (!s || !host || first < 0 || count < 1 || first + count > s->capacity || channel < 0 || channel >= s->channels)
         return tp::fail(TP_E_BAD_ARG, "tp_storage copy: bad range");
-    if (s->on_device) return tp::staged_copy(s, first, count, channel, host, up, stream);
+    if (s->on_device == 2) return tp::fail(TP_E_BAD_ARG, "tp_storage copy: storage has no memory");
+    if (s->on_device == 1) return tp::staged_copy(s, first, count, channel, host, up, stream);
     // host storage: plain pitched copy on the calling thread
     for (int t = 0; t < count; ++t) {
         float *plane = s->base + (long long)(first + t) * s->slot_stride + (long long)channel * s->plane_stride;

@@ -8,7 +8,7 @@ import ctypes as C
 
 import numpy as np
 
-from ._lib import (ElevParams, TileJob, TPError, check, lib, LIB_PATH,  # noqa: F401
+from ._lib import (ElevParams, TileJob, TPError, check, lib, LIB_PATH, RESIDUAL_SOURCE,  # noqa: F401
                    TP_OK, TP_E_BAD_ARG, TP_E_CACHE_FULL, TP_E_MISSING_PARENT,
                    TP_E_TIMEOUT, TP_E_CUDA, TP_E_IO, TP_E_NO_DEVICE)
 
@@ -24,9 +24,12 @@ class TileStorage:
     """A pool of tile slots (GPUTileStorage / CPUTileStorage,
     core/.../producer/TileStorage.h:140-182)."""
 
+    DEVICE, PINNED_HOST, BOOKKEEPING = 1, 0, 2
+
     def __init__(self, tile_size, channels, capacity, on_device=True):
         h = C.c_void_p()
-        check(lib().tp_storage_create(tile_size, channels, capacity, int(on_device), C.byref(h)))
+        kind = on_device if isinstance(on_device, int) and not isinstance(on_device, bool) else int(bool(on_device))
+        check(lib().tp_storage_create(tile_size, channels, capacity, kind, C.byref(h)))
         self.handle = h
         self.tile_size = tile_size
         self.channels = channels
@@ -182,3 +185,181 @@ def noise_select(face, level, tx, ty):
     r, l = C.c_int(), C.c_int()
     check(lib().tp_noise_select(face, level, tx, ty, C.byref(r), C.byref(l)))
     return r.value, l.value
+
+
+# ------------------------------------------------------------------ cache and producers
+class TileCache:
+    """TileCache (core/.../producer/TileCache.h:201-309) over a TileStorage."""
+
+    def __init__(self, storage, name=""):
+        h = C.c_void_p()
+        check(lib().tp_cache_create(storage.handle, name.encode(), C.byref(h)))
+        self.handle, self.storage = h, storage
+
+    def close(self):
+        if self.handle:
+            lib().tp_cache_destroy(self.handle)
+            self.handle = None
+
+    def get_used_tiles(self):
+        return check(lib().tp_cache_used_tiles(self.handle))
+
+    def get_unused_tiles(self):
+        return check(lib().tp_cache_unused_tiles(self.handle))
+
+    def stats(self):
+        q, m = C.c_longlong(), C.c_longlong()
+        check(lib().tp_cache_stats(self.handle, C.byref(q), C.byref(m)))
+        return q.value, m.value
+
+
+class Tile:
+    """A tile handle (TileCache::Tile)."""
+
+    def __init__(self, handle):
+        self.handle = handle
+
+    def info(self):
+        v = [C.c_int() for _ in range(6)]
+        check(lib().tp_tile_info(self.handle, *[C.byref(x) for x in v]))
+        return dict(zip(("level", "tx", "ty", "slot", "users", "done"), (x.value for x in v)))
+
+    @property
+    def slot(self):
+        return self.info()["slot"]
+
+
+class TileProducer:
+    """Common TileProducer calls (core/.../producer/TileProducer.h:68-378)."""
+
+    def __init__(self, handle, cache):
+        self.handle, self.cache = handle, cache
+
+    def close(self):
+        if self.handle:
+            lib().tp_producer_destroy(self.handle)
+            self.handle = None
+
+    def get_id(self):
+        return lib().tp_producer_id(self.handle)
+
+    def get_border(self):
+        return lib().tp_producer_border(self.handle)
+
+    def set_root_quad_size(self, size):
+        check(lib().tp_producer_set_root_quad_size(self.handle, float(size)))
+
+    def has_tile(self, level, tx, ty):
+        return bool(check(lib().tp_producer_has_tile(self.handle, level, tx, ty)))
+
+    def get_tile(self, level, tx, ty):
+        h = lib().tp_producer_get_tile(self.handle, level, tx, ty)
+        return Tile(h) if h else None
+
+    def find_tile(self, level, tx, ty, include_cache=False, done=False):
+        h = lib().tp_producer_find_tile(self.handle, level, tx, ty, int(include_cache), int(done))
+        return Tile(h) if h else None
+
+    def put_tile(self, tile):
+        return check(lib().tp_producer_put_tile(self.handle, tile.handle))
+
+    def prefetch_tile(self, level, tx, ty):
+        return check(lib().tp_producer_prefetch_tile(self.handle, level, tx, ty))
+
+    def invalidate_tiles(self):
+        check(lib().tp_producer_invalidate_tiles(self.handle))
+
+    def queued(self):
+        return check(lib().tp_producer_queued(self.handle))
+
+
+class ResidualProducer(TileProducer):
+    """ResidualProducer: a .dat pyramid, a host callback or zero residuals."""
+
+    def __init__(self, cache, file="", delta=0, zscale=1.0, source=None):
+        h = C.c_void_p()
+        check(lib().tp_residual_producer_create(cache.handle, (file or "").encode(), delta, zscale, C.byref(h)))
+        super().__init__(h, cache)
+        self._source = None
+        if source is not None:
+            self.set_source(source)
+
+    def tile(self, level, tx, ty):
+        """The residual tile as computed on the host (tp_residual_tile)."""
+        W = self.cache.storage.tile_size
+        out = np.empty((W, W), np.float32)
+        check(lib().tp_residual_tile(self.handle, level, tx, ty, out.ctypes.data_as(C.POINTER(C.c_float)), W))
+        return out
+
+    def set_source(self, fn):
+        """fn(level, tx, ty, width) -> float32 array [width, width]."""
+        def cb(user, level, tx, ty, out, width):
+            try:
+                a = np.ascontiguousarray(fn(level, tx, ty, width), dtype=np.float32).reshape(width, width)
+                C.memmove(out, a.ctypes.data, a.nbytes)
+                return 0
+            except Exception:
+                return 1
+        self._source = RESIDUAL_SOURCE(cb)
+        check(lib().tp_residual_producer_set_source(self.handle, self._source, None))
+
+
+class ElevationProducer(TileProducer):
+    def __init__(self, cache, residuals=None, noise_amp=(), params=None, face=0):
+        h = C.c_void_p()
+        amps = (C.c_float * max(1, len(noise_amp)))(*noise_amp)
+        check(lib().tp_elevation_producer_create(cache.handle, residuals.handle if residuals else None, amps,
+                                                 len(noise_amp), C.byref(params or make_params()), face, C.byref(h)))
+        super().__init__(h, cache)
+        self.residuals = residuals
+
+
+class NormalProducer(TileProducer):
+    def __init__(self, cache, elevations, deform=False):
+        h = C.c_void_p()
+        check(lib().tp_normal_producer_create(cache.handle, elevations.handle, int(deform), C.byref(h)))
+        super().__init__(h, cache)
+        self.elevations = elevations
+
+
+def scheduler_run(producers, stream=None):
+    """Produces every queued tile of the producers (tp_scheduler_run)."""
+    arr = (C.c_void_p * len(producers))(*[p.handle for p in producers])
+    check(lib().tp_scheduler_run(arr, len(producers), stream))
+
+
+# ------------------------------------------------------------------ residual files
+class DatPyramid:
+    """A residual pyramid file (tp_dat_*)."""
+
+    def __init__(self, path):
+        h = C.c_void_p()
+        check(lib().tp_dat_open(path.encode(), C.byref(h)))
+        self.handle = h
+        info = (C.c_int * 7)()
+        sc = C.c_float()
+        check(lib().tp_dat_info(h, info, C.byref(sc)))
+        (self.min_level, self.max_level, self.tile_size, self.root_level, self.root_tx, self.root_ty,
+         self.ntiles) = list(info)
+        self.scale = sc.value
+
+    def close(self):
+        if self.handle:
+            lib().tp_dat_close(self.handle)
+            self.handle = None
+
+    def tile_int16(self, level, tx, ty):
+        cap = (self.tile_size + 5) ** 2
+        out = np.empty(cap, np.int16)
+        w = C.c_int()
+        check(lib().tp_dat_read_tile(self.handle, level, tx, ty, out.ctypes.data_as(C.POINTER(C.c_int16)), cap,
+                                     C.byref(w)))
+        return out[:w.value * w.value].reshape(w.value, w.value)
+
+
+def inflate_zlib(data, capacity):
+    out = np.empty(capacity, np.uint8)
+    n = C.c_size_t()
+    src = np.frombuffer(data, np.uint8)
+    check(lib().tp_inflate_zlib(src.ctypes.data, len(data), out.ctypes.data, capacity, C.byref(n)))
+    return out[:n.value].tobytes()

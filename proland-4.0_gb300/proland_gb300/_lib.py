@@ -52,6 +52,8 @@ class ElevParams(C.Structure):
     ]
 
 
+RESIDUAL_SOURCE = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_float), C.c_int)
+
 _LIB = None
 _vp = C.c_void_p
 _i = C.c_int
@@ -96,6 +98,34 @@ def lib():
         "tp_frame_config": ([_vp, _i, C.POINTER(_i), C.POINTER(_i), C.POINTER(_i)], _i),
         "tp_status": ([C.POINTER(_i), _i], _i),
         "tp_stream_check": ([_vp], _i),
+        "tp_cache_create": ([_vp, C.c_char_p, C.POINTER(_vp)], _i),
+        "tp_cache_destroy": ([_vp], _i),
+        "tp_cache_used_tiles": ([_vp], _i),
+        "tp_cache_unused_tiles": ([_vp], _i),
+        "tp_cache_stats": ([_vp, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)], _i),
+        "tp_residual_producer_create": ([_vp, C.c_char_p, _i, C.c_float, C.POINTER(_vp)], _i),
+        "tp_residual_producer_set_source": ([_vp, RESIDUAL_SOURCE, _vp], _i),
+        "tp_elevation_producer_create": ([_vp, _vp, _f32p, _i, C.POINTER(ElevParams), _i, C.POINTER(_vp)], _i),
+        "tp_normal_producer_create": ([_vp, _vp, _i, C.POINTER(_vp)], _i),
+        "tp_producer_destroy": ([_vp], _i),
+        "tp_producer_id": ([_vp], _i),
+        "tp_producer_border": ([_vp], _i),
+        "tp_producer_set_root_quad_size": ([_vp, C.c_float], _i),
+        "tp_producer_has_tile": ([_vp, _i, _i, _i], _i),
+        "tp_producer_get_tile": ([_vp, _i, _i, _i], _vp),
+        "tp_producer_find_tile": ([_vp, _i, _i, _i, _i, _i], _vp),
+        "tp_producer_put_tile": ([_vp, _vp], _i),
+        "tp_producer_prefetch_tile": ([_vp, _i, _i, _i], _i),
+        "tp_producer_invalidate_tiles": ([_vp], _i),
+        "tp_producer_queued": ([_vp], _i),
+        "tp_tile_info": ([_vp] + [C.POINTER(_i)] * 6, _i),
+        "tp_scheduler_run": ([C.POINTER(_vp), _i, _vp], _i),
+        "tp_residual_tile": ([_vp, _i, _i, _i, _f32p, _i], _i),
+        "tp_dat_open": ([C.c_char_p, C.POINTER(_vp)], _i),
+        "tp_dat_close": ([_vp], _i),
+        "tp_dat_info": ([_vp, C.POINTER(_i), C.POINTER(C.c_float)], _i),
+        "tp_dat_read_tile": ([_vp, _i, _i, _i, C.POINTER(C.c_int16), _i, C.POINTER(_i)], _i),
+        "tp_inflate_zlib": ([_vp, C.c_size_t, _vp, C.c_size_t, C.POINTER(C.c_size_t)], _i),
         "tp_dem_noise": ([_i, _f32p], _i),
         "tp_cnoise": ([C.c_float, C.c_float], C.c_float),
         "tp_noise_select": ([_i, _i, _i, _i, C.POINTER(_i), C.POINTER(_i)], _i),
