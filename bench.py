@@ -308,7 +308,8 @@ def main():
         dist.init_process_group("nccl")
     warmup = max(args.warmup, 3)
 
-    classes = make_frame(args.requests, args.seed + rank)
+    from proland_gb300 import replicas
+    classes = make_frame(args.requests, replicas.rank_seed(args.seed, rank))
     stream = torch.cuda.Stream()
     sh = C.c_void_p(stream.cuda_stream)
     params = tp.make_params()
@@ -360,13 +361,10 @@ def main():
     tp.stream_check(sh)
     ms_total = t_start.elapsed_time(t_end)
     kernel_ms = sum(kernel_ev[s][0][0].elapsed_time(kernel_ev[s][0][1]) for s in range(args.steps)) / args.steps
-    if world > 1:
-        t = torch.tensor([ms_total], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms_total = float(t.item())
+    ms_total = replicas.max_over_ranks(ms_total, dist if world > 1 else None, "cuda")
     ms_step = ms_total / args.steps
     tiles = sum(fc.n for fc in classes)
-    value = world * tiles / (ms_step / 1000.0)
+    value = replicas.whole_job_rate(tiles, ms_step, world)
 
     # per tile width: each width alone in its own frame, same tuned shape
     per_width = {}
@@ -406,10 +404,7 @@ def main():
         if s >= 2:
             e2e_ms.append(1000.0 * (time.perf_counter() - t0))
     e2e_step = float(np.mean(e2e_ms)) if e2e_ms else float("nan")
-    if world > 1:
-        t = torch.tensor([e2e_step], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_step = float(t.item())
+    e2e_step = replicas.max_over_ranks(e2e_step, dist if world > 1 else None, "cuda")
 
     if rank != 0:
         dist.barrier()

@@ -216,6 +216,9 @@ int tp_scheduler_run(tp_producer *const *producers, int n, void *stream);
 /* A residual producer's tile computed on the host (the reference keeps residual
  * tiles in CPU storage): `out` is width x width, width the cache's tile width. */
 int tp_residual_tile(tp_producer *p, int level, int tx, int ty, float *out, int width);
+/* Spherical-deformation frame of a tile (NormalProducer.cpp:215-273), 47 floats:
+ * C[16], N[16], L[4], W2T[9], R, size (normal producers with deform = 1 use it). */
+int tp_sphere_frame(double root_quad_size, int level, int tx, int ty, float *out47);
 
 /* Residual pyramid files (ResidualProducer.cpp:93-107, 253-340): header
  * {minLevel, maxLevel, tileSize, rootLevel, rootTx, rootTy, ntiles} and int16

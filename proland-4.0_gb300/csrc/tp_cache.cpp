@@ -443,7 +443,6 @@ extern "C" int tp_normal_producer_create(tp_cache *cache, tp_producer *elevation
         return tp::fail(TP_E_BAD_ARG, "tp_normal_producer_create: bad arguments");
     if (cache->storage->channels != 2 || cache->storage->W != elevations->cache->storage->W - 4)
         return tp::fail(TP_E_BAD_ARG, "normal cache must have 2-channel slots of width W - 4");
-    if (deform) return tp::fail(TP_E_BAD_ARG, "spherical deformation is produced by tp_normals_sphere");
     tp_producer *p = new_producer(kNormal, cache);
     p->elevations = elevations;
     p->deform = deform;
@@ -623,8 +622,9 @@ int run_residuals(tp_producer *r, void *stream)
 int run_elevations(tp_producer *e, tp_producer *normals, void *stream)
 {
     // normal tiles whose elevation tile is produced by this same launch are fused in
+    // (flat deformation; spherical normals run in their own kernel afterwards)
     std::map<const tp_tile *, tp_tile *> fused;  // elevation tile -> normal tile
-    if (normals)
+    if (normals && !normals->deform)
         for (tp_tile *nt : normals->queue)
             if (nt->dep_input && nt->dep_input->queued) fused[nt->dep_input] = nt;
     if (e->queue.empty()) return TP_OK;
@@ -704,14 +704,19 @@ int run_normals(tp_producer *np, void *stream)
     if (!(e->root_quad_size > 0.0f)) return tp::fail(TP_E_BAD_ARG, "normal producer: root quad size not set");
     std::vector<int> eslot, nslot;
     std::vector<float> meters;
+    std::vector<tp::SphereFrame> frames;
     for (tp_tile *t : np->queue) {
         if (!t->dep_input || !t->dep_input->done) return tp::fail(TP_E_MISSING_PARENT, "normal tile's elevation is not produced");
         eslot.push_back(t->dep_input->slot);
         nslot.push_back(t->slot);
         meters.push_back(e->root_quad_size / (float)(1u << t->level));
+        if (np->deform) {
+            frames.emplace_back();
+            tp::sphere_frame(e->root_quad_size, t->level, t->tx, t->ty, &frames.back());
+        }
     }
     int rc = tp::launch_normals(e->cache->storage, np->cache->storage, eslot.data(), nslot.data(), meters.data(),
-                                (int)eslot.size(), stream);
+                                (int)eslot.size(), stream, np->deform ? frames.data() : nullptr);
     if (rc) return rc;
     for (tp_tile *t : np->queue) {
         t->done = true;
@@ -764,5 +769,63 @@ extern "C" int tp_scheduler_run(tp_producer *const *producers, int n, void *stre
         int rc = run_normals(np, stream);
         if (rc) return rc;
     }
+    return TP_OK;
+}
+
+namespace tp {
+
+// NormalProducer.cpp:215-273: the tile's corners on the sphere of radius
+// R = D / 2 (D the root quad size) centred below the face, their unit verticals and
+// distances, and the rotation into the tangent frame at the tile centre.
+void sphere_frame(double D, int level, int tx, int ty, SphereFrame *f)
+{
+    const double R = D / 2.0, s = (double)(1u << level);
+    const double x0 = (double)tx / s * D - R, x1 = (double)(tx + 1) / s * D - R;
+    const double y0 = (double)ty / s * D - R, y1 = (double)(ty + 1) / s * D - R;
+    const double P[4][3] = {{x0, y0, R}, {x1, y0, R}, {x0, y1, R}, {x1, y1, R}};
+    double v[4][3], l[4], vc[3] = {0, 0, 0};
+    for (int k = 0; k < 4; ++k) {
+        l[k] = std::sqrt(P[k][0] * P[k][0] + P[k][1] * P[k][1] + P[k][2] * P[k][2]);
+        for (int c = 0; c < 3; ++c) {
+            v[k][c] = P[k][c] / l[k];
+            vc[c] += v[k][c];
+        }
+    }
+    for (int c = 0; c < 3; ++c) vc[c] *= 0.25;
+    for (int r = 0; r < 3; ++r)
+        for (int k = 0; k < 4; ++k) {
+            f->C[r * 4 + k] = (float)(v[k][r] * R - vc[r] * R);
+            f->N[r * 4 + k] = (float)v[k][r];
+        }
+    for (int k = 0; k < 4; ++k) {
+        f->C[12 + k] = 1.0f;
+        f->N[12 + k] = 0.0f;
+        f->L[k] = (float)l[k];
+    }
+    const double pc[3] = {(x0 + x1) * 0.5, (y0 + y1) * 0.5, R};
+    const double lc = std::sqrt(pc[0] * pc[0] + pc[1] * pc[1] + pc[2] * pc[2]);
+    const double uz[3] = {pc[0] / lc, pc[1] / lc, pc[2] / lc};
+    const double t[3] = {uz[2], 0.0, -uz[0]};  // (0, 1, 0) x uz
+    const double lt = std::sqrt(t[0] * t[0] + t[1] * t[1] + t[2] * t[2]);
+    const double ux[3] = {t[0] / lt, t[1] / lt, t[2] / lt};
+    const double uy[3] = {uz[1] * ux[2] - uz[2] * ux[1], uz[2] * ux[0] - uz[0] * ux[2], uz[0] * ux[1] - uz[1] * ux[0]};
+    for (int c = 0; c < 3; ++c) {
+        f->W2T[c] = (float)ux[c];
+        f->W2T[3 + c] = (float)uy[c];
+        f->W2T[6 + c] = (float)uz[c];
+    }
+    f->R = (float)R;
+    f->size = (float)(D / s);
+}
+
+}  // namespace tp
+
+extern "C" int tp_sphere_frame(double root_quad_size, int level, int tx, int ty, float *out47)
+{
+    if (!out47 || !(root_quad_size > 0.0) || level < 0 || level > 30) return tp::fail(TP_E_BAD_ARG, "tp_sphere_frame: bad arguments");
+    tp::SphereFrame f;
+    tp::sphere_frame(root_quad_size, level, tx, ty, &f);
+    static_assert(sizeof(f) == 47 * sizeof(float), "frame layout");
+    std::memcpy(out47, &f, sizeof f);
     return TP_OK;
 }

@@ -113,9 +113,23 @@ int staged_copy(tp_storage *s, int first, int count, int channel, float *host, b
 int read_status(int *status, bool clear);
 // Uploads `count` dense host tiles into the given (not necessarily consecutive) slots.
 int staged_copy_slots(tp_storage *s, const int *slots, int count, int channel, const float *host, void *stream);
-// Normal tiles from produced elevation tiles (flat deformation).
+// Spherical-deformation frame of one tile (NormalProducer.cpp:215-273), computed in
+// FP64 on the host and cast to float: patch corners relative to their mean (C,
+// row-major 4x4 with a row of ones), corner verticals (N), corner distances (L),
+// world-to-tangent rotation (W2T, row-major 3x3), radius and tile size.
+struct SphereFrame {
+    float C[16];
+    float N[16];
+    float L[4];
+    float W2T[9];
+    float R;
+    float size;
+};
+void sphere_frame(double root_quad_size, int level, int tx, int ty, SphereFrame *f);
+
+// Normal tiles from produced elevation tiles (flat, or spherical with one frame per tile).
 int launch_normals(tp_storage *elev, tp_storage *nrm, const int *eslots, const int *nslots, const float *meters,
-                   int count, void *stream);
+                   int count, void *stream, const SphereFrame *frames = nullptr);
 // Residual pyramid files.
 int dat_tile_width(const tp_dat *d, int level);
 int dat_tile_id(const tp_dat *d, int level, int tx, int ty);

@@ -363,3 +363,10 @@ def inflate_zlib(data, capacity):
     src = np.frombuffer(data, np.uint8)
     check(lib().tp_inflate_zlib(src.ctypes.data, len(data), out.ctypes.data, capacity, C.byref(n)))
     return out[:n.value].tobytes()
+
+
+def sphere_frame(root_quad_size, level, tx, ty):
+    """The 47 floats of a tile's spherical frame (tp_sphere_frame)."""
+    out = np.empty(47, np.float32)
+    check(lib().tp_sphere_frame(float(root_quad_size), level, tx, ty, out.ctypes.data_as(C.POINTER(C.c_float))))
+    return out

@@ -121,6 +121,7 @@ def lib():
         "tp_tile_info": ([_vp] + [C.POINTER(_i)] * 6, _i),
         "tp_scheduler_run": ([C.POINTER(_vp), _i, _vp], _i),
         "tp_residual_tile": ([_vp, _i, _i, _i, _f32p, _i], _i),
+        "tp_sphere_frame": ([C.c_double, _i, _i, _i, _f32p], _i),
         "tp_dat_open": ([C.c_char_p, C.POINTER(_vp)], _i),
         "tp_dat_close": ([_vp], _i),
         "tp_dat_info": ([_vp, C.POINTER(_i), C.POINTER(C.c_float)], _i),

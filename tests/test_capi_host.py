@@ -80,3 +80,11 @@ def test_bad_arguments_return_codes(product):
     assert lib.tp_storage_create(3, 1, 1, 1, None) == product.TP_E_BAD_ARG
     assert lib.tp_dem_noise(5, None) == product.TP_E_BAD_ARG
     assert lib.tp_last_error()
+
+
+@pytest.mark.parametrize("D,level,tx,ty", [(12.72e6, 0, 0, 0), (12.72e6, 3, 5, 2), (12.72e6, 12, 1000, 3000), (100000.0, 2, 1, 3)])
+def test_sphere_frame_matches_oracle(product, oracle_lib, D, level, tx, ty):
+    a = product.sphere_frame(D, level, tx, ty)
+    f = oracle_lib.sphere_frame(D, level, tx, ty)
+    b = np.concatenate([np.array(f.C), np.array(f.N), np.array(f.L), np.array(f.W2T), [f.R, f.size]]).astype(np.float32)
+    assert np.array_equal(a, b)

@@ -135,3 +135,32 @@ def test_dem_dat_residuals_terrain4_layout(gpu, oracle_lib):
     want = oracle_tree(orc, {(0, 0, 0)} | set(tiles), 101, [], 0, lambda l, x, y: res[(l, x, y)], mod=2)
     for h, t in zip(held, tiles):
         assert np.array_equal(download(es, h.slot, tp.ZF), want[t][0]), t
+
+
+@pytest.mark.parametrize("face", [1, 3])
+def test_planet_face_sphere_normals(gpu, oracle_lib, face):
+    """Normals of a spherically deformed face (NormalProducer deform, terrain2
+    normal shader) against the oracle's sphere normals, from the same elevations."""
+    tp, orc = gpu, oracle_lib
+    W = 197
+    D = 2.0 * 6360000.0
+    es = tp.TileStorage(W, 3, 64)
+    rs = tp.TileStorage(W, 1, 64)
+    ns = tp.TileStorage(W - 4, 2, 64)
+    ec, rc, nc = tp.TileCache(es, "e"), tp.TileCache(rs, "r"), tp.TileCache(ns, "n")
+    r = tp.ResidualProducer(rc, source=synthetic_residual)
+    amps = [300.0 * 0.55 ** l for l in range(12)]
+    e = tp.ElevationProducer(ec, r, noise_amp=amps, params=tp.make_params(), face=face)
+    n = tp.NormalProducer(nc, e, deform=True)
+    n.set_root_quad_size(D)
+    wanted = [(0, 0, 0), (3, 5, 2), (6, 40, 17)]
+    held = [n.get_tile(*t) for t in wanted]
+    tp.scheduler_run([n])
+    tp.stream_check()
+    for h, t in zip(held, wanted):
+        et = e.find_tile(*t, include_cache=True, done=True)
+        zm = download(es, et.slot, tp.ZM)
+        f = orc.sphere_frame(D, *t)
+        enx, eny = orc.normals_sphere(W, zm, f)
+        assert_normals_close(download(ns, h.slot, tp.NX), enx, "sphere nx %s" % (t,))
+        assert_normals_close(download(ns, h.slot, tp.NY), eny, "sphere ny %s" % (t,))
