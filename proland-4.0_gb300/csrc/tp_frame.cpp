@@ -306,6 +306,15 @@ int add_class(tp_frame *f, tp_storage *elev, tp_storage *res, tp_storage *nrm, c
 
 }  // namespace
 
+int tp::check_batch_jobs(tp_storage *elev, tp_storage *res, tp_storage *nrm, const tp_tile_job *jobs, int n)
+{
+    tp_frame::Class k;
+    k.elev = elev;
+    k.res = res;
+    k.nrm = nrm;
+    return check_jobs(k, jobs, n);
+}
+
 extern "C" int tp_frame_create(tp_frame **out)
 {
     if (!out) return tp::fail(TP_E_BAD_ARG, "tp_frame_create: out is NULL");

@@ -69,6 +69,10 @@ void build_dem_noise(int W, float *out);
 // TMA descriptor of a float pool seen as a 3D tensor (x: W samples, y: W rows,
 // z: slot * channels + channel), cached on the storage.
 int tensor_map(tp_storage *s, int box_x, int box_y, const CUtensorMap **out);
+// The same descriptor written into `out` (no cache).
+int encode_tensor_map(const tp_storage *s, int box_x, int box_y, CUtensorMap *out);
+// Validates a host job array against the storages as a one-class frame does.
+int check_batch_jobs(tp_storage *elev, tp_storage *res, tp_storage *nrm, const tp_tile_job *jobs, int n);
 
 constexpr int kFrameThreads = 256;
 

@@ -61,4 +61,23 @@ int tensor_map(tp_storage *s, int box_x, int box_y, const CUtensorMap **out)
     return TP_OK;
 }
 
+int encode_tensor_map(const tp_storage *s, int box_x, int box_y, CUtensorMap *out)
+{
+    if (box_x < 1 || box_x > 256 || box_y < 1 || box_y > 256 || (box_x * 4) % 16 != 0)
+        return fail(TP_E_BAD_ARG, "tensor map: box outside TMA limits");
+    int err = TP_OK;
+    auto fn = encode_fn(&err);
+    if (!fn) return err;
+    std::memset(out, 0, sizeof *out);
+    cuuint64_t dims[3] = {(cuuint64_t)s->W, (cuuint64_t)s->W, (cuuint64_t)s->capacity * s->channels};
+    cuuint64_t strides[2] = {(cuuint64_t)s->pitch * sizeof(float), (cuuint64_t)s->plane_stride * sizeof(float)};
+    cuuint32_t box[3] = {(cuuint32_t)box_x, (cuuint32_t)box_y, 1};
+    cuuint32_t estr[3] = {1, 1, 1};
+    CUresult r = fn(out, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, s->base, dims, strides, box, estr,
+                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return fail(TP_E_CUDA, "cuTensorMapEncodeTiled failed");
+    return TP_OK;
+}
+
 }  // namespace tp
