@@ -249,6 +249,60 @@ int tp_dem_noise(int tile_width, float *out /* 6 * W * W, fp16-rounded */);
 float tp_cnoise(float x, float y);               /* noise.cpp:118-165, period 0 */
 int tp_noise_select(int face, int level, int tx, int ty, int *rot, int *layer);
 
+/* ------------------------------------------------------------------------
+ * Preprocess on the device (HeightMipmap.cpp:199-323, 399-559): residual
+ * pyramids from a height field, as the reference's preprocess tool builds them.
+ * tp_fbm_heights: a procedural value-noise fBm (octaves of base_cells * 2^o
+ * cells, gain 1/2, the octave sum normalised to `amplitude` metres) sampled on a
+ * size x size grid spanning [0, 1]^2, in int16 units of `quantum` metres.
+ * tp_preprocess_level: all 4^level tiles (width tile_size + 5, row-major by
+ * (ty, tx)) of one level of the pyramid over a base grid of
+ * tile_size * 2^max_level + 1 samples: the approximate tiles (input of the
+ * next level), and for level >= 1 the upsampled parents, the residuals (as
+ * floats) and their int16 encoding; any of the last three may be NULL. */
+int tp_fbm_heights(int size, int octaves, int base_cells, float amplitude, float quantum, uint32_t seed,
+                   int16_t *out_dev, void *stream);
+int tp_preprocess_level(const int16_t *base_dev, int tile_size, int max_level, int level, float scale,
+                        const float *parent_approx_dev, float *approx_dev, float *upsampled_dev,
+                        float *residual_dev, int16_t *encoded_dev, void *stream);
+
+/* ------------------------------------------------------------------------
+ * Learned residual predictor (no counterpart in the reference: it stands in for
+ * stored residuals below a terrain's finest stored level).  A 5-layer 3x3
+ * convolutional net, 32 features, GELU, bf16 weights and activations with fp32
+ * accumulation on the tensor cores.  Input: the upsampled parent tile (minus its
+ * mean, over the level's input sigma), the sample parities and a constant
+ * channel, plus a learned per-level embedding; output: the residual tile over
+ * the level's output sigma.  Parameters are one flat fp32 array (per layer
+ * W[cout][9][cin] then b[cout]; then the embedding [24][32]).  Device arrays are
+ * dense n x W x W fp32 tiles; `levels` are host arrays of n ints in [0, 24). */
+typedef struct tp_learned tp_learned;
+int tp_learned_create(int tile_width, int max_batch, tp_learned **out);
+int tp_learned_destroy(tp_learned *net);
+int tp_learned_param_count(const tp_learned *net);
+int tp_learned_init(tp_learned *net, uint32_t seed);
+int tp_learned_get_params(tp_learned *net, float *host, int count);
+int tp_learned_set_params(tp_learned *net, const float *host, int count);
+int tp_learned_get_grads(tp_learned *net, float *host, int count);
+int tp_learned_set_sigmas(tp_learned *net, const float *sigma_in, const float *sigma_out, int nlevels);
+/* Predicted residuals (metres) into out_dev (may be NULL); training = 1 keeps
+ * what tp_learned_backward needs. */
+int tp_learned_forward(tp_learned *net, const float *up_dev, const int *levels, int n, int training,
+                       float *out_dev, void *stream);
+/* Gradients of the mean squared error (in units of the level sigmas) against
+ * target residuals (metres) of the last training forward pass; *loss = that error. */
+int tp_learned_backward(tp_learned *net, const float *target_dev, float *loss, void *stream);
+int tp_learned_adam(tp_learned *net, float lr, void *stream);
+/* Training batch: tile src[k] (< n_src) of (up_src, res_src) under symmetry
+ * dihedral[k] (bit 2 transposes, bit 0 mirrors x, bit 1 mirrors y). */
+int tp_learned_gather(tp_learned *net, const float *up_src, const float *res_src, int n_src, const int *src,
+                      const int *dihedral, int n, float *up_out, float *res_out, void *stream);
+/* Learned residual tiles of n jobs (level >= 1, resident parent_slot, residual_slot
+ * in `residuals`, a storage of the net's width): the jobs can then be produced by
+ * tp_elevation_batch with those residual slots. */
+int tp_learned_predict_residuals(tp_learned *net, tp_storage *elev, const tp_tile_job *jobs, int n,
+                                 tp_storage *residuals, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

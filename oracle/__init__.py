@@ -79,6 +79,13 @@ def lib():
         L.or_residual_upsample.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, _f32p, _f32p]
         L.or_compute_residual.argtypes = [C.c_int, C.c_int, C.c_int, _f32p, _f32p, _f32p,
                                           C.POINTER(C.c_int16), _f32p]
+        _i16p = C.POINTER(C.c_int16)
+        L.or_fbm_heights.argtypes = [C.c_int, C.c_int, C.c_int, C.c_float, C.c_float, C.c_uint32, _i16p]
+        L.or_level_tile.argtypes = [_i16p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_float, _f32p]
+        L.or_learned_param_count.restype = C.c_int
+        L.or_learned_loss_grad.argtypes = [C.c_int, C.c_int, _f32p, _f32p, _f32p, C.POINTER(C.c_int), _f32p, _f32p,
+                                           C.c_int, _f32p, _f64p]
+        L.or_learned_loss_grad.restype = C.c_double
         _LIB = L
     return _LIB
 
@@ -311,3 +318,38 @@ def residual_chain_root(dat, delta, zscale=1.0):
         out = tmp.copy()
         out[:w, :w] = (tmp[:w, :w] + (ti.astype(np.float32) * scale)).astype(np.float32)
     return out
+
+
+# ---------------------------------------------------------------- preprocess and learned net
+def fbm_heights(size, octaves=12, base_cells=4, amplitude=4000.0, quantum=0.25, seed=1):
+    """The device preprocess's procedural fBm height field as int16 (size x size)."""
+    out = np.empty((size, size), np.int16)
+    lib().or_fbm_heights(size, octaves, base_cells, amplitude, quantum, seed,
+                         out.ctypes.data_as(C.POINTER(C.c_int16)))
+    return out
+
+
+def level_tile(base, ts, max_level, level, tx, ty, scale=1.0):
+    """HeightMipmap::getTile of a decimated level of `base` (int16, ts * 2^max_level + 1 square)."""
+    base = np.ascontiguousarray(base, np.int16)
+    out = np.empty((ts + 5, ts + 5), np.float32)
+    lib().or_level_tile(base.ctypes.data_as(C.POINTER(C.c_int16)), ts, max_level, level, tx, ty, scale, _p(out))
+    return out
+
+
+def learned_param_count():
+    return lib().or_learned_param_count()
+
+
+def learned_loss_grad(params, up, target, levels, sigma_in, sigma_out, emulate=True, want_grad=True):
+    """Loss (mean squared error in sigma units), normalised predictions [n, W, W] and
+    the gradient (float64, flat like the parameters) of the learned net."""
+    params, up, target = _f32(params), _f32(up), _f32(target)
+    n, W = up.shape[0], up.shape[1]
+    lv = np.ascontiguousarray(levels, np.int32)
+    si, so = _f32(sigma_in), _f32(sigma_out)
+    pred = np.empty((n, W, W), np.float32)
+    grad = np.empty(learned_param_count(), np.float64) if want_grad else None
+    loss = lib().or_learned_loss_grad(W, n, _p(params), _p(up), _p(target), lv.ctypes.data_as(C.POINTER(C.c_int)),
+                                      _p(si), _p(so), int(emulate), _p(pred), _p(grad, _f64p))
+    return loss, pred, grad

@@ -15,15 +15,15 @@ LIB = os.path.join(OUT_DIR, "liboracle.so")
 
 
 def build(force: bool = False) -> str:
-    src = os.path.join(HERE, "oracle.c")
+    srcs = [os.path.join(HERE, "oracle.c"), os.path.join(HERE, "learned.c")]
     hdr = os.path.join(HERE, "oracle.h")
     if (not force and os.path.exists(LIB)
-            and os.path.getmtime(LIB) >= max(os.path.getmtime(src), os.path.getmtime(hdr))):
+            and os.path.getmtime(LIB) >= max([os.path.getmtime(p) for p in srcs] + [os.path.getmtime(hdr)])):
         return LIB
     os.makedirs(OUT_DIR, exist_ok=True)
     tmp = LIB + ".tmp%d" % os.getpid()
     cmd = ["gcc", "-O2", "-std=c11", "-D_GNU_SOURCE", "-ffp-contract=off", "-fno-fast-math",
-           "-fPIC", "-shared", "-pthread", "-Wall", "-o", tmp, src, "-lm"]
+           "-fPIC", "-shared", "-pthread", "-Wall", "-o", tmp, *srcs, "-lm"]
     subprocess.check_call(cmd)
     os.replace(tmp, LIB)
     return LIB

@@ -116,6 +116,13 @@ void or_compute_residual(int W, int tx, int ty, const float *parent_approx,
 /* ResidualProducer::upsample for the small tiles below the pyramid's minLevel. */
 void or_residual_upsample(int n, int tilesize, int tx, int ty, const float *parent, float *out);
 
+/* ---- learned.c: device preprocess height field, level tiles, learned net ---- */
+void or_fbm_heights(int size, int octaves, int base_cells, float amplitude, float quantum, uint32_t seed, int16_t *out);
+void or_level_tile(const int16_t *base, int ts, int max_level, int level, int tx, int ty, float scale, float *out);
+int or_learned_param_count(void);
+double or_learned_loss_grad(int W, int n, const float *params, const float *up, const float *target, const int *levels,
+                            const float *sigma_in, const float *sigma_out, int emulate, float *pred_out, double *grad);
+
 #ifdef __cplusplus
 }
 #endif

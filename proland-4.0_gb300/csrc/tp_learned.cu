@@ -1,0 +1,559 @@
+// Kernels of the learned residual predictor (sm_103a).
+//
+// Convolutions are implicit GEMMs on the 5th-generation tensor cores: a CTA owns a
+// block of 8 x 16 output pixels (M = 128 rows of one tcgen05.mma), TMA stages the
+// block's input halo (10 x 18 pixels, zero-filled outside the image) into shared
+// memory as one plane of 8-channel rows per channel group, and each of the nine
+// taps is a descriptor offset into that halo -- no im2col copy.  K runs over
+// (tap, 16-channel step); the weights are the B operand, packed once per update in
+// the canonical no-swizzle K-major layout.  Accumulators live in tensor memory and
+// are read back with tcgen05.ld for a fused epilogue (bias, level embedding, GELU,
+// or the GELU derivative of the backward pass).
+//
+// The weight gradient is a GEMM over pixels: D[(tap, ci)][co] += X[p + tap][ci] *
+// dZ[p][co] with both operands MN-major (pixels along K), each 8-pixel row of an
+// operand tile brought in by TMA at the tap's offset; a CTA accumulates its blocks
+// in tensor memory and adds its sums to the gradient once at the end.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <mutex>
+
+#include "tp_internal.h"
+#include "tp_learned.h"
+#include "tp_sm100.h"
+#include "tp_stencil.h"
+
+namespace tp {
+namespace learned {
+namespace {
+
+using namespace tp::sm100;
+
+constexpr int kThreads = 128;
+constexpr int kHaloX = kBlockX + 2, kHaloY = kBlockY + 2;
+constexpr int kRowStride = kHaloX * 16;                     // bytes per halo row of one channel group
+constexpr int kHaloBytes = kRowStride * kHaloY;             // one channel group: 2880
+constexpr int kGroupStride = (kHaloBytes + 127) / 128 * 128;  // 2944: TMA destinations 128-byte aligned
+constexpr int kBoxBytes = 8 * kBlockX * kBlockY * 2;        // one 8-channel group of a block: 2048
+
+__device__ __forceinline__ float gelu(float z) { return 0.5f * z * (1.0f + erff(z * 0.70710678118654752f)); }
+__device__ __forceinline__ float gelu_grad(float z)
+{
+    return 0.5f * (1.0f + erff(z * 0.70710678118654752f)) + z * 0.39894228040143268f * expf(-0.5f * z * z);
+}
+
+__device__ __forceinline__ uint32_t pack2(float a, float b)
+{
+    __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+    return *reinterpret_cast<uint32_t *>(&h);
+}
+
+template <int C>
+__device__ __forceinline__ void store_bf16(__nv_bfloat16 *dst, const float *v)
+{
+#pragma unroll
+    for (int q = 0; q < C / 8; ++q) {
+        uint4 u;
+        u.x = pack2(v[8 * q + 0], v[8 * q + 1]);
+        u.y = pack2(v[8 * q + 2], v[8 * q + 3]);
+        u.z = pack2(v[8 * q + 4], v[8 * q + 5]);
+        u.w = pack2(v[8 * q + 6], v[8 * q + 7]);
+        reinterpret_cast<uint4 *>(dst)[q] = u;
+    }
+}
+
+template <int C>
+__device__ __forceinline__ void load_bf16(const __nv_bfloat16 *src, float *v)
+{
+#pragma unroll
+    for (int q = 0; q < C / 8; ++q) {
+        uint4 u = reinterpret_cast<const uint4 *>(src)[q];
+        const __nv_bfloat162 *h = reinterpret_cast<const __nv_bfloat162 *>(&u);
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+            float2 f = __bfloat1622float2(h[e]);
+            v[8 * q + 2 * e] = f.x;
+            v[8 * q + 2 * e + 1] = f.y;
+        }
+    }
+}
+
+template <int CIN, int COUT>
+constexpr int conv_smem_bytes()
+{
+    return (CIN / 8) * kGroupStride + 9 * CIN * COUT * 2 + 32;
+}
+
+template <int CIN, int COUT, int MODE>
+__global__ void __launch_bounds__(kThreads) conv_kernel(const __grid_constant__ CUtensorMap xmap, const ConvLaunch a)
+{
+    extern __shared__ __align__(1024) uint8_t smem[];
+    constexpr int NCG = CIN / 8, KSTEPS = CIN / 16, NMMA = 9 * KSTEPS;
+    constexpr int BBYTES = NMMA * COUT * 32;
+    uint8_t *halo = smem;
+    uint8_t *bsm = smem + NCG * kGroupStride;
+    uint64_t *bars = reinterpret_cast<uint64_t *>(bsm + BBYTES);
+    uint32_t *tslot = reinterpret_cast<uint32_t *>(bars + 2);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+
+    for (int i = tid; i < BBYTES / 16; i += kThreads)
+        reinterpret_cast<uint4 *>(bsm)[i] = reinterpret_cast<const uint4 *>(a.wpack)[i];
+    if (tid == 0) {
+        mbar_init(&bars[0], 1);
+        mbar_init(&bars[1], 1);
+    }
+    if (warp == 0) tmem_alloc(tslot, 32);
+    fence_proxy_async_smem();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tslot;
+    const int per_img = a.tiles_x * a.tiles_y, total = a.nimg * per_img;
+    const int Wp = a.W + 2;
+    constexpr uint32_t idesc = idesc_bf16(128, COUT, 0, 0);
+    const uint32_t halo_a = smem_u32(halo), b_a = smem_u32(bsm);
+    bool ok = true;
+    uint32_t it = 0;
+    for (int t = blockIdx.x; t < total; t += gridDim.x, ++it) {
+        const int img = t / per_img, rem = t - img * per_img;
+        const int by = rem / a.tiles_x, bx = rem - by * a.tiles_x;
+        const int x0 = bx * kBlockX, y0 = by * kBlockY;
+        if (tid == 0) {
+            mbar_expect_tx(&bars[0], NCG * kHaloBytes);
+#pragma unroll
+            for (int cg = 0; cg < NCG; ++cg) tma_load_4d(halo + cg * kGroupStride, &xmap, cg * 8, x0, y0, img, &bars[0]);
+        }
+        if (!__syncthreads_and(mbar_wait(&bars[0], it & 1))) {
+            ok = false;
+            break;
+        }
+        if (tid == 0) {
+            tc_fence_after();
+#pragma unroll
+            for (int q = 0; q < NMMA; ++q) {
+                const int tap = q / KSTEPS, s = q - tap * KSTEPS;
+                const int dy = tap / 3, dx = tap - dy * 3;
+                const uint64_t ad = sdesc(halo_a + 2 * s * kGroupStride + dy * kRowStride + dx * 16, kGroupStride,
+                                          kRowStride);
+                const uint64_t bd = sdesc(b_a + q * COUT * 32, 128, 256);
+                mma_bf16(tmem, ad, bd, idesc, q > 0 ? 1u : 0u);
+            }
+            mma_commit(&bars[1]);
+        }
+        if (!__syncthreads_and(mbar_wait(&bars[1], it & 1))) {
+            ok = false;
+            break;
+        }
+        tc_fence_after();
+        float acc[COUT];
+        const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16);
+        if (COUT == 32)
+            tmem_ld32(taddr, acc);
+        else
+            tmem_ld16(taddr, acc);
+        const int m = warp * 32 + lane, r = m >> 3, c = m & 7;
+        const int px = x0 + c, py = y0 + r;
+        if (px < a.W && py < a.W) {
+            const size_t pix = ((size_t)img * Wp + (py + 1)) * Wp + (px + 1);
+            if (MODE == kHidden) {
+                const float *e = a.emb ? a.emb + (size_t)min(max(a.level[img], 0), kLevels - 1) * COUT : nullptr;
+#pragma unroll
+                for (int j = 0; j < COUT; ++j) acc[j] += a.bias[j] + (e ? e[j] : 0.0f);
+                if (a.zsave) store_bf16<COUT>(a.zsave + pix * COUT, acc);
+#pragma unroll
+                for (int j = 0; j < COUT; ++j) acc[j] = gelu(acc[j]);
+                store_bf16<COUT>(a.out + pix * COUT, acc);
+            } else if (MODE == kLast) {
+                a.out_f32[((size_t)img * a.W + py) * a.W + px] = acc[0] + a.bias[0];
+            } else {
+                float z[COUT];
+                load_bf16<COUT>(a.zprev + pix * COUT, z);
+#pragma unroll
+                for (int j = 0; j < COUT; ++j) acc[j] *= gelu_grad(z[j]);
+                store_bf16<COUT>(a.out + pix * COUT, acc);
+            }
+        }
+        tc_fence_before();
+        __syncthreads();
+    }
+    if (!ok && tid == 0) atomicExch(a.status, TP_E_TIMEOUT);
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (warp == 0) tmem_dealloc(tmem, 32);
+}
+
+template <int CIN, int COUT>
+constexpr int wgrad_tiles()
+{
+    return (9 * CIN / 8 + 15) / 16;
+}
+template <int CIN, int COUT>
+constexpr int wgrad_smem_bytes()
+{
+    return wgrad_tiles<CIN, COUT>() * 16 * kBoxBytes + (COUT / 8) * kBoxBytes + 32;
+}
+
+template <int CIN, int COUT>
+__global__ void __launch_bounds__(kThreads) wgrad_kernel(const __grid_constant__ CUtensorMap xmap,
+                                                         const __grid_constant__ CUtensorMap zmap, const WgradLaunch a)
+{
+    extern __shared__ __align__(1024) uint8_t smem[];
+    constexpr int NCG = CIN / 8, NGO = COUT / 8, NG = 9 * NCG;
+    constexpr int NMT = wgrad_tiles<CIN, COUT>();
+    constexpr int ABYTES = NMT * 16 * kBoxBytes;
+    constexpr uint32_t TCOLS = NMT * 32 <= 32 ? 32 : (NMT * 32 <= 64 ? 64 : 128);
+    uint8_t *asm_ = smem;
+    uint8_t *bsm = smem + ABYTES;
+    uint64_t *bars = reinterpret_cast<uint64_t *>(bsm + NGO * kBoxBytes);
+    uint32_t *tslot = reinterpret_cast<uint32_t *>(bars + 2);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+
+    // rows of the last M tile past the real (tap, channel) groups are never loaded
+    for (int i = NG * kBoxBytes / 16 + tid; i < ABYTES / 16; i += kThreads) reinterpret_cast<uint4 *>(asm_)[i] = make_uint4(0, 0, 0, 0);
+    if (tid == 0) {
+        mbar_init(&bars[0], 1);
+        mbar_init(&bars[1], 1);
+    }
+    if (warp == 0) tmem_alloc(tslot, TCOLS);
+    fence_proxy_async_smem();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tslot;
+    const int per_img = a.tiles_x * a.tiles_y, total = a.nimg * per_img;
+    constexpr uint32_t idesc = idesc_bf16(128, COUT, 1, 1);
+    const uint32_t a_a = smem_u32(asm_), b_a = smem_u32(bsm);
+    bool ok = true;
+    uint32_t it = 0;
+    const int bn = tid % COUT;
+    for (int t = blockIdx.x; t < total; t += gridDim.x, ++it) {
+        const int img = t / per_img, rem = t - img * per_img;
+        const int by = rem / a.tiles_x, bx = rem - by * a.tiles_x;
+        const int x0 = bx * kBlockX, y0 = by * kBlockY;
+        if (tid == 0) {
+            mbar_expect_tx(&bars[0], (NG + NGO) * kBoxBytes);
+            for (int g = 0; g < NG; ++g) {
+                const int tap = g / NCG, cg = g - tap * NCG;
+                const int dy = tap / 3, dx = tap - dy * 3;
+                tma_load_4d(asm_ + g * kBoxBytes, &xmap, cg * 8, x0 + dx, y0 + dy, img, &bars[0]);
+            }
+#pragma unroll
+            for (int go = 0; go < NGO; ++go) tma_load_4d(bsm + go * kBoxBytes, &zmap, go * 8, x0 + 1, y0 + 1, img, &bars[0]);
+        }
+        if (!__syncthreads_and(mbar_wait(&bars[0], it & 1))) {
+            ok = false;
+            break;
+        }
+        if (tid == 0) {
+            tc_fence_after();
+#pragma unroll
+            for (int mt = 0; mt < NMT; ++mt)
+#pragma unroll
+                for (int s = 0; s < kBlockY / 2; ++s) {
+                    const uint64_t ad = sdesc(a_a + mt * 16 * kBoxBytes + s * 256, 128, kBoxBytes);
+                    const uint64_t bd = sdesc(b_a + s * 256, 128, kBoxBytes);
+                    mma_bf16(tmem + mt * 32, ad, bd, idesc, (it > 0 || s > 0) ? 1u : 0u);
+                }
+            mma_commit(&bars[1]);
+        }
+        // bias (and level-embedding) gradient of this block from the staged dZ tile
+        {
+            float sum = 0.0f;
+            const __nv_bfloat16 *bz = reinterpret_cast<const __nv_bfloat16 *>(bsm);
+            for (int k = tid / COUT; k < kBlockX * kBlockY; k += kThreads / COUT)
+                sum += __bfloat162float(bz[((bn >> 3) * kBoxBytes + (k >> 3) * 128 + (k & 7) * 16) / 2 + (bn & 7)]);
+            atomicAdd(a.gb + bn, sum);
+            if (a.gemb) atomicAdd(a.gemb + (size_t)min(max(a.level[img], 0), kLevels - 1) * COUT + bn, sum);
+        }
+        if (!__syncthreads_and(mbar_wait(&bars[1], it & 1))) {
+            ok = false;
+            break;
+        }
+    }
+    if (!ok && tid == 0) atomicExch(a.status, TP_E_TIMEOUT);
+    tc_fence_after();
+    if (ok && it > 0) {
+#pragma unroll
+        for (int mt = 0; mt < NMT; ++mt) {
+            float v[COUT];
+            const uint32_t taddr = tmem + mt * 32 + ((uint32_t)(warp * 32) << 16);
+            if (COUT == 32)
+                tmem_ld32(taddr, v);
+            else
+                tmem_ld16(taddr, v);
+            const int m = mt * 128 + warp * 32 + lane;
+            if (m < 9 * CIN)
+#pragma unroll
+                for (int n = 0; n < COUT; ++n) atomicAdd(a.gw + (size_t)n * 9 * CIN + m, v[n]);
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (warp == 0) tmem_dealloc(tmem, TCOLS);
+}
+
+// ---------------------------------------------------------------- launch helpers
+int sm_count()
+{
+    static int n = 0;
+    if (!n) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+        if (n <= 0) n = 1;
+    }
+    return n;
+}
+
+template <typename K>
+int grid_for(K kernel, int smem, int units, int *grid)
+{
+    static std::mutex mu;
+    std::lock_guard<std::mutex> lk(mu);
+    cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e != cudaSuccess) return tp::cuda_fail("cudaFuncSetAttribute (learned)", e);
+    int per_sm = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kThreads, smem);
+    if (e != cudaSuccess) return tp::cuda_fail("occupancy (learned)", e);
+    if (per_sm < 1) return tp::fail(TP_E_BAD_ARG, "learned: kernel does not fit on an SM");
+    *grid = std::max(1, std::min(units, per_sm * sm_count()));
+    return TP_OK;
+}
+
+template <int CIN, int COUT, int MODE>
+int conv_instance(const ConvLaunch &a, const CUtensorMap *halo, cudaStream_t s)
+{
+    const int units = a.nimg * a.tiles_x * a.tiles_y;
+    if (units <= 0) return TP_OK;
+    constexpr int smem = conv_smem_bytes<CIN, COUT>();
+    int grid = 0;
+    int rc = grid_for(conv_kernel<CIN, COUT, MODE>, smem, units, &grid);
+    if (rc) return rc;
+    conv_kernel<CIN, COUT, MODE><<<grid, kThreads, smem, s>>>(*halo, a);
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? TP_OK : tp::cuda_fail("conv kernel launch", e);
+}
+
+template <int CIN, int COUT>
+int wgrad_instance(const WgradLaunch &a, const CUtensorMap *xb, const CUtensorMap *zb, cudaStream_t s)
+{
+    const int units = a.nimg * a.tiles_x * a.tiles_y;
+    if (units <= 0) return TP_OK;
+    constexpr int smem = wgrad_smem_bytes<CIN, COUT>();
+    int grid = 0;
+    int rc = grid_for(wgrad_kernel<CIN, COUT>, smem, units, &grid);
+    if (rc) return rc;
+    wgrad_kernel<CIN, COUT><<<grid, kThreads, smem, s>>>(*xb, *zb, a);
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? TP_OK : tp::cuda_fail("weight-gradient kernel launch", e);
+}
+
+// ---------------------------------------------------------------- small kernels
+__global__ void pack_kernel(const float *w, int cin, int cout, uint8_t *fwd, uint8_t *bwd)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= cout * 9 * cin) return;
+    const int co = i / (9 * cin), rem = i - co * 9 * cin, tap = rem / cin, ci = rem - tap * cin;
+    const __nv_bfloat16 v = __float2bfloat16_rn(w[i]);
+    {  // forward: B[n = co][k = (tap, ci)], 16-channel K steps
+        const int q = tap * (cin / 16) + ci / 16, kk = ci % 16;
+        const size_t off = (size_t)q * cout * 32 + (co / 8) * 256 + (kk / 8) * 128 + (co % 8) * 16 + (kk % 8) * 2;
+        *reinterpret_cast<__nv_bfloat16 *>(fwd + off) = v;
+    }
+    {  // data gradient: a convolution of dZ with B'[n = ci][k = (8 - tap, co)]
+        const int tp_ = 8 - tap;
+        const int q = tp_ * (cout / 16) + co / 16, kk = co % 16;
+        const size_t off = (size_t)q * cin * 32 + (ci / 8) * 256 + (kk / 8) * 128 + (ci % 8) * 16 + (kk % 8) * 2;
+        *reinterpret_cast<__nv_bfloat16 *>(bwd + off) = v;
+    }
+}
+
+__global__ void prep_kernel(const float *up, const int *level, const float *sigma_in, int W, __nv_bfloat16 *x0)
+{
+    const int img = blockIdx.x, n = W * W;
+    const float *u = up + (size_t)img * n;
+    __shared__ double part[256];
+    double s = 0.0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) s += u[i];
+    part[threadIdx.x] = s;
+    __syncthreads();
+    for (int k = blockDim.x / 2; k > 0; k >>= 1) {
+        if (threadIdx.x < k) part[threadIdx.x] += part[threadIdx.x + k];
+        __syncthreads();
+    }
+    const float mean = (float)(part[0] / n);
+    const float inv = 1.0f / sigma_in[min(max(level[img], 0), kLevels - 1)];
+    const int Wp = W + 2;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const int y = i / W, x = i - y * W;
+        float v[16] = {(u[i] - mean) * inv, (float)(x & 1), (float)(y & 1), 1.0f};
+        store_bf16<16>(x0 + (((size_t)img * Wp + y + 1) * Wp + x + 1) * 16, v);
+    }
+}
+
+__global__ void loss_kernel(const float *pred, const float *target, const int *level, const float *sigma_out, int W,
+                            int nimg, float scale, __nv_bfloat16 *dz, float *loss)
+{
+    const size_t n = (size_t)W * W;
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    float d2 = 0.0f;
+    if (i < n * nimg) {
+        const int img = (int)(i / n), p = (int)(i - (size_t)img * n), y = p / W, x = p - y * W;
+        const float t = target[i] / sigma_out[min(max(level[img], 0), kLevels - 1)];
+        const float d = pred[i] - t;
+        d2 = d * d;
+        float v[16] = {2.0f * d * scale};
+        const int Wp = W + 2;
+        store_bf16<16>(dz + (((size_t)img * Wp + y + 1) * Wp + x + 1) * 16, v);
+    }
+    for (int o = 16; o > 0; o >>= 1) d2 += __shfl_xor_sync(0xffffffffu, d2, o);
+    if ((threadIdx.x & 31) == 0) atomicAdd(loss, d2);
+}
+
+__global__ void adam_kernel(float *p, const float *g, float *m, float *v, const float *mask, int n, float lr, float b1,
+                            float b2, float eps, float c1, float c2)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float gi = g[i] * mask[i];
+    const float mi = b1 * m[i] + (1.0f - b1) * gi;
+    const float vi = b2 * v[i] + (1.0f - b2) * gi * gi;
+    m[i] = mi;
+    v[i] = vi;
+    p[i] = mask[i] * (p[i] - lr * (mi / c1) / (sqrtf(vi / c2) + eps));
+}
+
+__global__ void scale_kernel(const float *pred, const int *level, const float *sigma_out, int W, int nimg, float *out)
+{
+    const size_t n = (size_t)W * W;
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n * nimg) return;
+    out[i] = pred[i] * sigma_out[min(max(level[i / n], 0), kLevels - 1)];
+}
+
+// the eight symmetries of the square: bit 2 transposes, bit 0 mirrors x, bit 1 mirrors y
+__global__ void gather_kernel(const float *up, const float *res, const int *src, const int *dihedral, int W, int n,
+                              float *up_out, float *res_out)
+{
+    const size_t np = (size_t)W * W;
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= np * n) return;
+    const int s = (int)(i / np), p = (int)(i - (size_t)s * np), y = p / W, x = p - y * W;
+    const int d = dihedral[s];
+    int u = x, v = y;
+    if (d & 4) {
+        u = y;
+        v = x;
+    }
+    if (d & 1) u = W - 1 - u;
+    if (d & 2) v = W - 1 - v;
+    const size_t o = (size_t)src[s] * np + (size_t)v * W + u;
+    up_out[i] = up[o];
+    res_out[i] = res[o];
+}
+
+__global__ void upsample_kernel(const float *elev, int pitch, long long plane_stride, long long slot_stride,
+                                const int *parent_slot, const int *tx, const int *ty, int W, int n, float *up)
+{
+    const size_t np = (size_t)W * W;
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= np * n) return;
+    const int s = (int)(i / np), p = (int)(i - (size_t)s * np), j = p / W, c = p - j * W;
+    const int ts = W - 5;
+    const float *P = elev + (long long)parent_slot[s] * slot_stride;  // plane 0: zf
+    up[i] = tp::upsample_cpu_order(P, pitch, c, j, 1 + (tx[s] & 1) * ts / 2, 1 + (ty[s] & 1) * ts / 2);
+    (void)plane_stride;
+}
+
+__global__ void store_residuals_kernel(const float *pred, const int *level, const float *sigma_out, int W, int n,
+                                       float *res, int pitch, long long slot_stride, const int *slots)
+{
+    const size_t np = (size_t)W * W;
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= np * n) return;
+    const int s = (int)(i / np), p = (int)(i - (size_t)s * np), y = p / W, x = p - y * W;
+    res[(long long)slots[s] * slot_stride + (long long)y * pitch + x] =
+        pred[i] * sigma_out[min(max(level[s], 0), kLevels - 1)];
+}
+
+inline unsigned blocks_for(size_t n, int t) { return (unsigned)((n + t - 1) / t); }
+
+}  // namespace
+
+int launch_conv(int cin, int cout, int mode, const ConvLaunch &a, const CUtensorMap *halo, cudaStream_t s)
+{
+    if (cin == 16 && cout == 32 && mode == kHidden) return conv_instance<16, 32, kHidden>(a, halo, s);
+    if (cin == 32 && cout == 32 && mode == kHidden) return conv_instance<32, 32, kHidden>(a, halo, s);
+    if (cin == 32 && cout == 16 && mode == kLast) return conv_instance<32, 16, kLast>(a, halo, s);
+    if (cin == 16 && cout == 32 && mode == kBackData) return conv_instance<16, 32, kBackData>(a, halo, s);
+    if (cin == 32 && cout == 32 && mode == kBackData) return conv_instance<32, 32, kBackData>(a, halo, s);
+    return tp::fail(TP_E_BAD_ARG, "learned: no convolution instance for this shape");
+}
+
+int launch_wgrad(int cin, int cout, const WgradLaunch &a, const CUtensorMap *xb, const CUtensorMap *zb, cudaStream_t s)
+{
+    if (cin == 16 && cout == 32) return wgrad_instance<16, 32>(a, xb, zb, s);
+    if (cin == 32 && cout == 32) return wgrad_instance<32, 32>(a, xb, zb, s);
+    if (cin == 32 && cout == 16) return wgrad_instance<32, 16>(a, xb, zb, s);
+    return tp::fail(TP_E_BAD_ARG, "learned: no weight-gradient instance for this shape");
+}
+
+void launch_pack(const float *w, int cin, int cout, uint8_t *fwd, uint8_t *bwd, cudaStream_t s)
+{
+    const int n = cout * 9 * cin;
+    pack_kernel<<<blocks_for(n, 256), 256, 0, s>>>(w, cin, cout, fwd, bwd);
+}
+
+void launch_prep(const float *up, const int *level, const float *sigma_in, int W, int nimg, __nv_bfloat16 *x0,
+                 cudaStream_t s)
+{
+    if (nimg > 0) prep_kernel<<<nimg, 256, 0, s>>>(up, level, sigma_in, W, x0);
+}
+
+void launch_loss(const float *pred, const float *target, const int *level, const float *sigma_out, int W, int nimg,
+                 __nv_bfloat16 *dz, float *loss, cudaStream_t s)
+{
+    const size_t n = (size_t)W * W * nimg;
+    if (n) loss_kernel<<<blocks_for(n, 256), 256, 0, s>>>(pred, target, level, sigma_out, W, nimg, 1.0f / (float)n, dz, loss);
+}
+
+void launch_adam(float *p, const float *g, float *m, float *v, const float *mask, int n, float lr, float b1, float b2,
+                 float eps, int step, cudaStream_t s)
+{
+    const float c1 = 1.0f - powf(b1, (float)step), c2 = 1.0f - powf(b2, (float)step);
+    adam_kernel<<<blocks_for(n, 256), 256, 0, s>>>(p, g, m, v, mask, n, lr, b1, b2, eps, c1, c2);
+}
+
+void launch_scale_out(const float *pred, const int *level, const float *sigma_out, int W, int nimg, float *out,
+                      cudaStream_t s)
+{
+    const size_t n = (size_t)W * W * nimg;
+    if (n) scale_kernel<<<blocks_for(n, 256), 256, 0, s>>>(pred, level, sigma_out, W, nimg, out);
+}
+
+void launch_gather(const float *up, const float *res, const int *src, const int *dihedral, int W, int n, float *up_out,
+                   float *res_out, cudaStream_t s)
+{
+    const size_t t = (size_t)W * W * n;
+    if (t) gather_kernel<<<blocks_for(t, 256), 256, 0, s>>>(up, res, src, dihedral, W, n, up_out, res_out);
+}
+
+void launch_upsample(const float *elev, int pitch, long long plane_stride, long long slot_stride, const int *parent_slot,
+                     const int *tx, const int *ty, int W, int n, float *up, cudaStream_t s)
+{
+    const size_t t = (size_t)W * W * n;
+    if (t) upsample_kernel<<<blocks_for(t, 256), 256, 0, s>>>(elev, pitch, plane_stride, slot_stride, parent_slot, tx, ty, W, n, up);
+}
+
+void launch_store_residuals(const float *pred, const int *level, const float *sigma_out, int W, int n, float *res,
+                            int pitch, long long slot_stride, const int *slots, cudaStream_t s)
+{
+    const size_t t = (size_t)W * W * n;
+    if (t) store_residuals_kernel<<<blocks_for(t, 256), 256, 0, s>>>(pred, level, sigma_out, W, n, res, pitch, slot_stride, slots);
+}
+
+}  // namespace learned
+}  // namespace tp

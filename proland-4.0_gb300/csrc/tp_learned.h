@@ -1,0 +1,74 @@
+// Learned residual predictor: a 5-layer 3x3 convolutional net (32 features, GELU)
+// that maps an upsampled parent tile (plus a per-level embedding) to the residual
+// tile the stencil leaves out.  BF16 activations and weights, FP32 accumulation in
+// tensor memory, trained by the library's own forward/backward kernels.
+#pragma once
+
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace tp {
+namespace learned {
+
+constexpr int kLayers = 5;
+constexpr int kCin[kLayers] = {16, 32, 32, 32, 32};    // layer 0 input: 4 used channels, padded to 16
+constexpr int kCout[kLayers] = {32, 32, 32, 32, 16};   // last layer: 1 used channel, padded to 16
+constexpr int kLevels = 24;                            // rows of the level embedding / sigma tables
+constexpr int kInputChannels = 4;                      // height, x parity, y parity, ones
+
+// Pixel blocks of the convolutions: 8 columns x 16 rows = one 128-row MMA tile.
+constexpr int kBlockX = 8, kBlockY = 16;
+
+// One convolution launch.  Activations are NHWC bf16 images of (W+2)^2 pixels with
+// a zero border of one pixel, read through a TMA tensor map.
+struct ConvLaunch {
+    int W, nimg, tiles_x, tiles_y;
+    const uint8_t *wpack;        // packed B operand (weights), 9 * Cin * Cout bf16
+    const float *bias;           // [Cout]
+    const float *emb;            // [kLevels][Cout] level embedding (layer 0) or null
+    const int *level;            // [nimg] level of each image (device)
+    __nv_bfloat16 *out;          // mode 0: activation; mode 2: gradient of the previous pre-activation
+    __nv_bfloat16 *zsave;        // mode 0: pre-activation (for the backward pass) or null
+    const __nv_bfloat16 *zprev;  // mode 2: the previous layer's saved pre-activation
+    float *out_f32;              // mode 1: [nimg][W][W] output channel 0
+    int *status;
+};
+
+// Weight gradient of one layer over a batch: dW[co][tap][ci] += sum_p dZ[p][co] X[p + tap][ci].
+struct WgradLaunch {
+    int W, nimg, tiles_x, tiles_y;
+    float *gw;        // [Cout][9][Cin]
+    float *gb;        // [Cout]
+    float *gemb;      // [kLevels][Cout] or null
+    const int *level; // [nimg]
+    int *status;
+};
+
+enum ConvMode { kHidden = 0, kLast = 1, kBackData = 2 };
+
+int launch_conv(int cin, int cout, int mode, const ConvLaunch &a, const CUtensorMap *halo, cudaStream_t s);
+int launch_wgrad(int cin, int cout, const WgradLaunch &a, const CUtensorMap *xbox, const CUtensorMap *zbox,
+                 cudaStream_t s);
+int encode_act_map(void *base, int W, int channels, int nimg, int box_x, int box_y, CUtensorMap *out);
+
+// small kernels
+void launch_pack(const float *w, int cin, int cout, uint8_t *fwd, uint8_t *bwd, cudaStream_t s);
+void launch_prep(const float *up, const int *level, const float *sigma_in, int W, int nimg, __nv_bfloat16 *x0,
+                 cudaStream_t s);
+void launch_loss(const float *pred, const float *target, const int *level, const float *sigma_out, int W, int nimg,
+                 __nv_bfloat16 *dz, float *loss, cudaStream_t s);
+void launch_adam(float *p, const float *g, float *m, float *v, const float *mask, int n, float lr, float b1, float b2,
+                 float eps, int step, cudaStream_t s);
+void launch_scale_out(const float *pred, const int *level, const float *sigma_out, int W, int nimg, float *out,
+                      cudaStream_t s);
+void launch_gather(const float *up, const float *res, const int *src, const int *dihedral, int W, int n, float *up_out,
+                   float *res_out, cudaStream_t s);
+void launch_upsample(const float *elev, int pitch, long long plane_stride, long long slot_stride, const int *parent_slot,
+                     const int *tx, const int *ty, int W, int n, float *up, cudaStream_t s);
+void launch_store_residuals(const float *pred, const int *level, const float *sigma_out, int W, int n, float *res,
+                            int pitch, long long slot_stride, const int *slots, cudaStream_t s);
+
+}  // namespace learned
+}  // namespace tp

@@ -131,6 +131,21 @@ def lib():
         "tp_dem_noise": ([_i, _f32p], _i),
         "tp_cnoise": ([C.c_float, C.c_float], C.c_float),
         "tp_noise_select": ([_i, _i, _i, _i, C.POINTER(_i), C.POINTER(_i)], _i),
+        "tp_fbm_heights": ([_i, _i, _i, C.c_float, C.c_float, C.c_uint32, _vp, _vp], _i),
+        "tp_preprocess_level": ([_vp, _i, _i, _i, C.c_float, _vp, _vp, _vp, _vp, _vp, _vp], _i),
+        "tp_learned_create": ([_i, _i, C.POINTER(_vp)], _i),
+        "tp_learned_destroy": ([_vp], _i),
+        "tp_learned_param_count": ([_vp], _i),
+        "tp_learned_init": ([_vp, C.c_uint32], _i),
+        "tp_learned_get_params": ([_vp, _f32p, _i], _i),
+        "tp_learned_set_params": ([_vp, _f32p, _i], _i),
+        "tp_learned_get_grads": ([_vp, _f32p, _i], _i),
+        "tp_learned_set_sigmas": ([_vp, _f32p, _f32p, _i], _i),
+        "tp_learned_forward": ([_vp, _vp, C.POINTER(_i), _i, _i, _vp, _vp], _i),
+        "tp_learned_backward": ([_vp, _vp, _f32p, _vp], _i),
+        "tp_learned_adam": ([_vp, C.c_float, _vp], _i),
+        "tp_learned_gather": ([_vp, _vp, _vp, _i, C.POINTER(_i), C.POINTER(_i), _i, _vp, _vp, _vp], _i),
+        "tp_learned_predict_residuals": ([_vp, _vp, C.POINTER(TileJob), _i, _vp, _vp], _i),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)

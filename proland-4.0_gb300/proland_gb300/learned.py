@@ -1,0 +1,251 @@
+"""Learned residual predictor and the device preprocess that makes its training data.
+
+* `fbm_heights`, `preprocess_level`, `build_pyramid`: residual pyramids built on the
+  device the way the reference's preprocess tool builds them (decimated mipmap,
+  residual = sample - upsample(parent approximation), rounded to int16), from a
+  procedural fBm height field;
+* `LearnedPredictor`: the 5-layer BF16 convolutional net of the C ABI
+  (tp_learned_*), trained by the library's own forward/backward/Adam kernels;
+* `train`: the training loop over (upsampled parent, residual) pairs of a pyramid,
+  with the eight symmetries of the square as augmentation;
+* `evaluate`: RMS / max height error and normal-angle error per level of the
+  learned residuals against the stored ones, beside the plain method (stencil +
+  noise, no residual).
+
+Device buffers are torch CUDA tensors (plumbing); every computation runs in the
+library's kernels.
+"""
+import ctypes as C
+
+import numpy as np
+
+from ._lib import TileJob, check, lib
+
+try:
+    import torch
+except ImportError:  # pragma: no cover - the GPU paths need torch for device buffers
+    torch = None
+
+_f32p = C.POINTER(C.c_float)
+
+
+def _ptr(t):
+    return C.c_void_p(t.data_ptr()) if t is not None else None
+
+
+def _stream():
+    return C.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+# ---------------------------------------------------------------- preprocess
+def fbm_heights(size, octaves=12, base_cells=4, amplitude=4000.0, quantum=0.25, seed=1):
+    """int16 heights (units of `quantum` metres) of the procedural fBm on a size x size grid."""
+    out = torch.empty((size, size), dtype=torch.int16, device="cuda")
+    check(lib().tp_fbm_heights(size, octaves, base_cells, amplitude, quantum, seed, _ptr(out), _stream()))
+    return out
+
+
+def preprocess_level(base, tile_size, max_level, level, parent=None, scale=1.0, want=("up", "res", "enc")):
+    """One pyramid level on the device: (approx, up, res, enc) tensors of
+    [4^level, W, W] (up/res/enc None at level 0 or when not wanted)."""
+    W = tile_size + 5
+    n = 1 << (2 * level)
+    approx = torch.empty((n, W, W), dtype=torch.float32, device="cuda")
+    up = res = enc = None
+    if level > 0:
+        up = torch.empty_like(approx) if "up" in want else None
+        res = torch.empty_like(approx) if "res" in want else None
+        enc = torch.empty((n, W, W), dtype=torch.int16, device="cuda") if "enc" in want else None
+    check(lib().tp_preprocess_level(_ptr(base), tile_size, max_level, level, scale, _ptr(parent), _ptr(approx),
+                                    _ptr(up), _ptr(res), _ptr(enc), _stream()))
+    return approx, up, res, enc
+
+
+def build_pyramid(max_level, tile_size=96, octaves=12, base_cells=4, amplitude=4000.0, quantum=0.25, seed=1,
+                  first_level=1):
+    """Training pairs of a residual pyramid: dict with 'up' [N, W, W] (upsampled parent
+    approximations, metres), 'res' [N, W, W] (residuals, metres), 'level' [N] and
+    'tile' [N, 3] (level, tx, ty), for levels first_level..max_level."""
+    base = fbm_heights((tile_size << max_level) + 1, octaves, base_cells, amplitude, quantum, seed)
+    approx, _, _, _ = preprocess_level(base, tile_size, max_level, 0)
+    ups, ress, levels, tiles = [], [], [], []
+    for l in range(1, max_level + 1):
+        approx, up, res, _ = preprocess_level(base, tile_size, max_level, l, approx, want=("up", "res"))
+        if l >= first_level:
+            ups.append(up * quantum)
+            ress.append(res * quantum)
+            side = 1 << l
+            levels.append(np.full(side * side, l, np.int32))
+            tiles.append(np.stack([np.full(side * side, l), np.arange(side * side) % side,
+                                   np.arange(side * side) // side], 1))
+    return {"up": torch.cat(ups), "res": torch.cat(ress), "level": np.concatenate(levels),
+            "tile": np.concatenate(tiles), "quantum": quantum, "tile_size": tile_size}
+
+
+def level_sigmas(data, nlevels=24, extrapolate=0.5):
+    """Per-level input sigma (RMS of the mean-removed upsampled tile) and output sigma
+    (RMS of the residual); levels without data continue the last level by the
+    factor `extrapolate` per level (fBm of gain 1/2)."""
+    si = np.zeros(nlevels, np.float32)
+    so = np.zeros(nlevels, np.float32)
+    lv = data["level"]
+    for l in np.unique(lv):
+        idx = torch.from_numpy(np.nonzero(lv == l)[0]).cuda()
+        u = data["up"].index_select(0, idx)
+        u = u - u.mean(dim=(1, 2), keepdim=True)
+        si[l] = float(u.pow(2).mean().sqrt())
+        so[l] = float(data["res"].index_select(0, idx).pow(2).mean().sqrt())
+    known = [l for l in range(nlevels) if so[l] > 0]
+    lo, hi = min(known), max(known)
+    for l in range(nlevels):
+        if l < lo:
+            si[l], so[l] = si[lo], so[lo]
+        elif l > hi:
+            si[l] = si[hi] * extrapolate ** (l - hi)
+            so[l] = so[hi] * extrapolate ** (l - hi)
+    return np.maximum(si, 1e-6), np.maximum(so, 1e-6)
+
+
+# ---------------------------------------------------------------- the net
+class LearnedPredictor:
+    """tp_learned: 5 x (3x3 conv, 32 features), GELU, BF16 weights and activations,
+    FP32 accumulation on the tensor cores."""
+
+    def __init__(self, tile_width=101, max_batch=256, seed=1):
+        h = C.c_void_p()
+        check(lib().tp_learned_create(tile_width, max_batch, C.byref(h)))
+        self.handle = h
+        self.W = tile_width
+        self.max_batch = max_batch
+        if seed != 1:
+            check(lib().tp_learned_init(h, seed))
+
+    def close(self):
+        if self.handle:
+            lib().tp_learned_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def param_count(self):
+        return lib().tp_learned_param_count(self.handle)
+
+    def get_params(self):
+        out = np.empty(self.param_count, np.float32)
+        check(lib().tp_learned_get_params(self.handle, out.ctypes.data_as(_f32p), out.size))
+        return out
+
+    def set_params(self, p):
+        p = np.ascontiguousarray(p, np.float32)
+        check(lib().tp_learned_set_params(self.handle, p.ctypes.data_as(_f32p), p.size))
+
+    def get_grads(self):
+        out = np.empty(self.param_count, np.float32)
+        check(lib().tp_learned_get_grads(self.handle, out.ctypes.data_as(_f32p), out.size))
+        return out
+
+    def set_sigmas(self, sigma_in, sigma_out):
+        si = np.ascontiguousarray(sigma_in, np.float32)
+        so = np.ascontiguousarray(sigma_out, np.float32)
+        check(lib().tp_learned_set_sigmas(self.handle, si.ctypes.data_as(_f32p), so.ctypes.data_as(_f32p), si.size))
+
+    def forward(self, up, levels, training=False, out=None):
+        """Residuals (metres) predicted for the upsampled tiles `up` [n, W, W]."""
+        n = up.shape[0]
+        lv = (C.c_int * n)(*[int(v) for v in levels])
+        if out is None:
+            out = torch.empty_like(up)
+        check(lib().tp_learned_forward(self.handle, _ptr(up), lv, n, int(training), _ptr(out), _stream()))
+        return out
+
+    def backward(self, target):
+        loss = C.c_float()
+        check(lib().tp_learned_backward(self.handle, _ptr(target), C.byref(loss), _stream()))
+        return loss.value
+
+    def adam(self, lr):
+        check(lib().tp_learned_adam(self.handle, lr, _stream()))
+
+    def gather(self, up_src, res_src, src, dihedral, up_out, res_out):
+        n = len(src)
+        s = (C.c_int * n)(*[int(v) for v in src])
+        d = (C.c_int * n)(*[int(v) for v in dihedral])
+        check(lib().tp_learned_gather(self.handle, _ptr(up_src), _ptr(res_src), up_src.shape[0], s, d, n, _ptr(up_out),
+                                      _ptr(res_out),
+                                      _stream()))
+
+    def predict_residuals(self, elev, jobs, residuals, stream=None):
+        arr = (TileJob * len(jobs))(*jobs)
+        check(lib().tp_learned_predict_residuals(self.handle, elev.handle, arr, len(jobs), residuals.handle, stream))
+
+
+def train(net, data, steps, batch=256, lr=3e-4, seed=0, log_every=0, lr_final=None):
+    """Adam on random (tile, symmetry) pairs of `data`; returns the loss history.
+    With lr_final the rate decays geometrically to it over the run."""
+    rng = np.random.default_rng(seed)
+    N = data["up"].shape[0]
+    W = net.W
+    up_b = torch.empty((batch, W, W), dtype=torch.float32, device="cuda")
+    res_b = torch.empty_like(up_b)
+    losses = []
+    for s in range(steps):
+        src = rng.integers(0, N, batch)
+        dih = rng.integers(0, 8, batch)
+        net.gather(data["up"], data["res"], src, dih, up_b, res_b)
+        net.forward(up_b, data["level"][src], training=True)
+        losses.append(net.backward(res_b))
+        rate = lr if lr_final is None else lr * (lr_final / lr) ** (s / max(1, steps - 1))
+        net.adam(rate)
+        if log_every and (s + 1) % log_every == 0:
+            print("step %d loss %.4f" % (s + 1, float(np.mean(losses[-log_every:]))))
+    return losses
+
+
+def evaluate(net, data, sigma_out, batch=None):
+    """Per level: RMS and max height error of the learned residuals, of the plain
+    method without residual (error = the residual itself), and the RMS of the
+    normal-angle error of both (finite differences over the interior)."""
+    lv = data["level"]
+    batch = min(batch or net.max_batch, net.max_batch)
+    out = {}
+    for l in np.unique(lv):
+        idx = np.nonzero(lv == l)[0]
+        se_l = se_p = 0.0
+        mx_l = mx_p = 0.0
+        ang_l = ang_p = 0.0
+        count = 0
+        h = 2.0 * (50000.0 / (1 << int(l))) / (net.W - 5)
+        for k in range(0, len(idx), batch):
+            sel = torch.from_numpy(idx[k:k + batch]).cuda()
+            up = data["up"].index_select(0, sel)
+            res = data["res"].index_select(0, sel)
+            pred = net.forward(up, lv[idx[k:k + batch]])
+            e_l = pred - res
+            se_l += float(e_l.pow(2).sum())
+            se_p += float(res.pow(2).sum())
+            mx_l = max(mx_l, float(e_l.abs().max()))
+            mx_p = max(mx_p, float(res.abs().max()))
+            ang_l += float(_angle_sq(up + pred, up + res, h).sum())
+            ang_p += float(_angle_sq(up, up + res, h).sum())
+            count += res.numel()
+        ni = count * ((net.W - 2) / net.W) ** 2
+        out[int(l)] = {"rms_learned": (se_l / count) ** 0.5, "rms_plain": (se_p / count) ** 0.5,
+                       "max_learned": mx_l, "max_plain": mx_p, "sigma": float(sigma_out[l]),
+                       "angle_rms_learned": (ang_l / ni) ** 0.5, "angle_rms_plain": (ang_p / ni) ** 0.5}
+    return out
+
+
+def _angle_sq(za, zb, h):
+    """Squared angle between central-difference normals of za and zb (interior samples)."""
+    def nrm(z):
+        dx = z[:, 1:-1, 2:] - z[:, 1:-1, :-2]
+        dy = z[:, 2:, 1:-1] - z[:, :-2, 1:-1]
+        v = torch.stack([-dx, -dy, torch.full_like(dx, h)], 0)
+        return v / v.norm(dim=0, keepdim=True)
+    c = (nrm(za) * nrm(zb)).sum(0).clamp(-1.0, 1.0)
+    return torch.acos(c) ** 2
