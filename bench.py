@@ -280,6 +280,96 @@ def fp64_errors(tp, classes):
     return out
 
 
+# forward FLOPs of the learned net per W x W tile: 2 x samples x 9 taps x sum(cin x cout)
+# over the used channels (4 -> 32, 3 x 32 -> 32, 32 -> 1), and as executed on the tensor
+# cores (padded channels 16 -> 32, 32 -> 16; 8 x 16 pixel blocks covering the tile)
+def learned_flops(W):
+    used = 2 * W * W * 9 * (4 * 32 + 3 * 32 * 32 + 32 * 1)
+    rows = ((W + 7) // 8) * ((W + 15) // 16) * 128
+    executed = 2 * rows * 9 * (16 * 32 + 3 * 32 * 32 + 32 * 16)
+    return used, executed
+
+
+def learned_section(tp, torch, stream, sh, args, plain_w101):
+    """The learned-residual form beside the plain one: a net trained briefly on a
+    5-level residual pyramid (device preprocess of a procedural fBm), its per-level
+    error against stored residuals, the net's inference rate (tiles/s, tensor
+    FLOP/s) and the rate of learned-form tiles (net + elevation kernel)."""
+    from proland_gb300 import learned as L
+    W, B = 101, 256
+    with torch.cuda.stream(stream):
+        data = L.build_pyramid(5, seed=args.seed)
+        si, so = L.level_sigmas(data)
+        net = L.LearnedPredictor(W, B, seed=1)
+        net.set_sigmas(si, so)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        losses = L.train(net, data, args.learned_steps, batch=64, lr=2e-3, lr_final=2e-4)
+        torch.cuda.synchronize()
+        train_ms = 1000.0 * (time.perf_counter() - t0) / max(1, args.learned_steps)
+        ev = L.evaluate(net, data, so)
+        # inference: B tiles of level 6 per call, inputs resident
+        idx = torch.arange(B, device="cuda") % data["up"].shape[0]
+        up = data["up"].index_select(0, idx).contiguous()
+        lv = [6] * B
+        out = torch.empty_like(up)
+        for _ in range(3):
+            net.forward(up, lv, out=out)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        reps = 20
+        e0.record(stream)
+        for _ in range(reps):
+            net.forward(up, lv, out=out)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        fwd_ms = e0.elapsed_time(e1) / reps
+        # learned-form tiles: residuals predicted into slots, then the elevation kernel
+        elev = tp.TileStorage(W, 3, B + 1)
+        res = tp.TileStorage(W, 1, B)
+        nrm = tp.TileStorage(W - 4, 2, B + 1)
+        par = data["up"][0].cpu().numpy()[None]
+        elev.upload(0, tp.ZF, par)
+        elev.upload(0, tp.ZM, np.maximum(par, 0))
+        jobs = [tp.make_job(6, 10 + (k % 2), 20 + (k // 2) % 2, out_slot=1 + k, parent_slot=0, residual_slot=k,
+                            normal_slot=1 + k, tile_meters=50000.0 / 64) for k in range(B)]
+        params = tp.make_params()
+        for _ in range(3):
+            net.predict_residuals(elev, jobs, res, sh)
+            tp.elevation_batch(elev, res, nrm, params, jobs, sh)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            net.predict_residuals(elev, jobs, res, sh)
+            tp.elevation_batch(elev, res, nrm, params, jobs, sh)
+        stream.synchronize()
+        form_ms = 1000.0 * (time.perf_counter() - t0) / reps
+        tp.stream_check(sh)
+    used, executed = learned_flops(W)
+    peak = None
+    try:
+        with open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "MEASURED_PEAKS.json")) as f:
+            peak = float(json.load(f)["bf16_tflops"])
+    except (OSError, ValueError, KeyError):
+        peak = 1900.0
+    tflops = B * used / (fwd_ms / 1000.0) / 1e12
+    net.close()
+    return {
+        "tile_width": W, "batch": B,
+        "net_tiles_per_s": B / (fwd_ms / 1000.0), "net_ms_per_batch": fwd_ms,
+        "form_tiles_per_s": B / (form_ms / 1000.0), "form_ms_per_batch": form_ms,
+        "plain_tiles_per_s_w101": plain_w101["tiles_per_s"] if plain_w101 else None,
+        "tensor": {"achieved_tflops": tflops, "executed_tflops": B * executed / (fwd_ms / 1000.0) / 1e12,
+                   "peak_tflops": peak, "frac": tflops / peak,
+                   "flops_per_tile": used, "executed_flops_per_tile": executed},
+        "train": {"steps": args.learned_steps, "batch": 64, "ms_per_step": train_ms,
+                  "loss_first": float(np.mean(losses[:20])), "loss_last": float(np.mean(losses[-20:])),
+                  "pairs": int(data["up"].shape[0]), "data": "5-level residual pyramid of a 12-octave fBm "
+                                                             "(device preprocess), 8 symmetries"},
+        "levels": {str(l): {k: round(v, 5) for k, v in e.items()} for l, e in ev.items()},
+    }
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -292,6 +382,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default work-unit shapes")
     ap.add_argument("--no-per-width", action="store_true", help="skip the per-width timings")
+    ap.add_argument("--no-learned", action="store_true", help="skip the learned-residual form")
+    ap.add_argument("--learned-steps", type=int, default=400, help="training steps before the learned timings")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -438,6 +530,8 @@ def main():
         "clocks": clk,
         "max_err_vs_fp64": fp64_errors(tp, classes),
     }
+    if not args.no_learned:
+        line["learned"] = learned_section(tp, torch, stream, sh, args, per_width.get("W101"))
     if not args.no_cpu:
         line["cpu_baseline"] = time_cpu(classes)
     print(json.dumps(line))

@@ -184,17 +184,24 @@ class LearnedPredictor:
         check(lib().tp_learned_predict_residuals(self.handle, elev.handle, arr, len(jobs), residuals.handle, stream))
 
 
-def train(net, data, steps, batch=256, lr=3e-4, seed=0, log_every=0, lr_final=None):
+def train(net, data, steps, batch=256, lr=3e-4, seed=0, log_every=0, lr_final=None, balance_levels=True):
     """Adam on random (tile, symmetry) pairs of `data`; returns the loss history.
-    With lr_final the rate decays geometrically to it over the run."""
+    With lr_final the rate decays geometrically to it over the run; with
+    balance_levels each sample first draws a level uniformly (a pyramid holds 4x
+    more tiles per level), then a tile of that level."""
     rng = np.random.default_rng(seed)
     N = data["up"].shape[0]
     W = net.W
+    by_level = [np.nonzero(data["level"] == l)[0] for l in np.unique(data["level"])]
     up_b = torch.empty((batch, W, W), dtype=torch.float32, device="cuda")
     res_b = torch.empty_like(up_b)
     losses = []
     for s in range(steps):
-        src = rng.integers(0, N, batch)
+        if balance_levels:
+            pick = rng.integers(0, len(by_level), batch)
+            src = np.array([by_level[k][rng.integers(0, len(by_level[k]))] for k in pick])
+        else:
+            src = rng.integers(0, N, batch)
         dih = rng.integers(0, 8, batch)
         net.gather(data["up"], data["res"], src, dih, up_b, res_b)
         net.forward(up_b, data["level"][src], training=True)
