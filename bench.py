@@ -219,9 +219,47 @@ def time_cpu(classes, min_seconds=4.0):
         el = time.perf_counter() - t0
         if el >= min_seconds:
             break
-    return {"value": reps * len(jobs) / el, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": "%d tiles (%d x 101, %d x 197) of the frame, %d repetitions, %.1f s" % (
-                len(jobs), sum(1 for j in jobs if j.W == 101), sum(1 for j in jobs if j.W == 197), reps, el)}
+    out = {"value": reps * len(jobs) / el, "unit": UNIT, "cores": threads, "kind": "port",
+           "sample": "%d tiles (%d x 101, %d x 197) of the frame, %d repetitions, %.1f s" % (
+               len(jobs), sum(1 for j in jobs if j.W == 101), sum(1 for j in jobs if j.W == 197), reps, el)}
+    # one thread, same mix
+    one = jobs[:12] + [j for j in jobs if j.W == 197][:4]
+    t0 = time.perf_counter()
+    reps = 0
+    while time.perf_counter() - t0 < min_seconds / 2:
+        oracle.run_jobs(one, 1)
+        reps += 1
+    out["single_thread"] = {"value": reps * len(one) / (time.perf_counter() - t0), "unit": UNIT, "cores": 1}
+    out["residual_decode"] = residual_decode_rate()
+    return out
+
+
+def residual_decode_rate(min_seconds=1.0):
+    """Host decode of residual tiles from the reference's DEM.dat pyramid (deflate
+    TIFF strips, int16 x scale), the work ResidualProducer does per tile: the
+    oracle's zlib-based decoder and the library's own inflate, tiles/s on one thread."""
+    import oracle
+    import proland_gb300 as tp
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "tests", "golden", "dem_terrain4_mini.dat")
+    if not os.path.exists(path):
+        return None
+    d = oracle.DatFile.open(path)
+    tiles = [(l, x, y) for l in range(0, d.max_level + 1) for x in range(1 << l) for y in range(1 << l)
+             if (l >= d.min_level or (x == 0 and y == 0)) and d.tile_id(l, x, y) < d.ntiles
+             and len(d.strip(l, x, y)) > 0]
+    def rate(fn):
+        t0 = time.perf_counter()
+        k = 0
+        while time.perf_counter() - t0 < min_seconds:
+            for t in tiles:
+                fn(*t)
+                k += 1
+        return k / (time.perf_counter() - t0)
+    lib = tp.DatPyramid(path)
+    res = {"oracle_zlib_tiles_per_s": rate(d.tile_int16), "library_inflate_tiles_per_s": rate(lib.tile_int16),
+           "tiles": len(tiles), "tile_width": d.tile_size + 5, "file": "tests/golden/dem_terrain4_mini.dat"}
+    lib.close()
+    return res
 
 
 def run_reference(args):

@@ -226,6 +226,23 @@ int tp_producer_invalidate_tiles(tp_producer *p);                             /*
 int tp_producer_queued(const tp_producer *p);                                  /* tiles waiting for production */
 int tp_tile_info(const tp_tile *t, int *level, int *tx, int *ty, int *slot, int *users, int *done);
 int tp_scheduler_run(tp_producer *const *producers, int n, void *stream);
+/* Batched doCreateTile (TileProducer.h:331-378 in the frame form): acquires each
+ * requested tile as tp_producer_get_tile does, then produces every queued tile of
+ * `p` and its inputs in one scheduler run on `stream`.  tiles_out[i] holds one user
+ * (release with tp_producer_put_tile).  On failure (e.g. TP_E_CACHE_FULL) no tile
+ * of the call stays acquired. */
+typedef struct {
+    int32_t level, tx, ty;
+} tp_tile_req;
+int tp_create_tiles(tp_producer *p, const tp_tile_req *reqs, int n, tp_tile **tiles_out, void *stream);
+int tp_create_tile(tp_producer *p, int level, int tx, int ty, tp_tile **tile_out, void *stream);
+/* The tiles of a terrain quadtree for one camera position (the TileSampler's
+ * requests): TerrainQuad::update's split rule (TerrainQuad.cpp:80-105) with
+ * TerrainNode::getCameraDist (TerrainNode.cpp:92-97), root quad [-size/2, size/2]^2,
+ * every quad visible; parents first.  *count receives the number of quads even
+ * when it exceeds `capacity` (then TP_E_BAD_ARG). */
+int tp_quadtree_requests(double root_size, int max_level, float split_dist, float dist_factor, double cam_x,
+                         double cam_y, double cam_z, double ground, tp_tile_req *out, int capacity, int *count);
 /* A residual producer's tile computed on the host (the reference keeps residual
  * tiles in CPU storage): `out` is width x width, width the cache's tile width. */
 int tp_residual_tile(tp_producer *p, int level, int tx, int ty, float *out, int width);

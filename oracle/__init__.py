@@ -353,3 +353,27 @@ def learned_loss_grad(params, up, target, levels, sigma_in, sigma_out, emulate=T
     loss = lib().or_learned_loss_grad(W, n, _p(params), _p(up), _p(target), lv.ctypes.data_as(C.POINTER(C.c_int)),
                                       _p(si), _p(so), int(emulate), _p(pred), _p(grad, _f64p))
     return loss, pred, grad
+
+
+def quadtree_requests(cam, root, max_level, split, dist_factor=1.0, ground=0.0):
+    """TerrainQuad::update's split rule (TerrainQuad.cpp:80-138) with
+    TerrainNode::getCameraDist (TerrainNode.cpp:92-97): the quads of the tree,
+    parents first, children near to far; every quad visible."""
+    cx, cy, cz = (float(v) for v in cam)
+    zmin, zmax = min(0.0, ground), max(0.0, ground)
+    order = {(0, 0): (0, 1, 2, 3), (0, 1): (1, 0, 3, 2), (1, 0): (2, 0, 3, 1), (1, 1): (3, 1, 2, 0)}
+    out = []
+
+    def visit(level, tx, ty, ox, oy, l):
+        out.append((level, tx, ty))
+        d = max(abs(cz - zmax) / dist_factor, max(min(abs(cx - ox), abs(cx - (ox + l))),
+                                                   min(abs(cy - oy), abs(cy - (oy + l)))))
+        dist = float(np.float32(d))
+        if not (dist < l * float(np.float32(split)) and level < max_level):
+            return
+        for c in order[(0 if cy < oy + l / 2.0 else 1, 0 if cx < ox + l / 2.0 else 1)]:
+            i, j = c & 1, c >> 1
+            visit(level + 1, 2 * tx + i, 2 * ty + j, ox + i * l / 2.0, oy + j * l / 2.0, l / 2.0)
+
+    visit(0, 0, 0, -root / 2.0, -root / 2.0, root)
+    return out

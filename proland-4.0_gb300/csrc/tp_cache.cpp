@@ -820,6 +820,62 @@ void sphere_frame(double D, int level, int tx, int ty, SphereFrame *f)
 
 }  // namespace tp
 
+// A queued, unproduced tile that nobody uses any more: its task is dropped and the
+// tiles it was to be made from are released (and dropped in turn when orphaned).
+static void cancel_orphan(tp_producer *p, tp_tile *t)
+{
+    if (!p || !t || t->users != 0 || t->done || !t->queued) return;
+    auto &q = p->queue;
+    q.erase(std::remove(q.begin(), q.end(), t), q.end());
+    t->queued = false;
+    tp_tile *deps[2] = {t->dep_parent, t->dep_input};
+    tp_producer *owners[2] = {t->dep_parent_owner, t->dep_input_owner};
+    release_deps(t);
+    for (int k = 0; k < 2; ++k) cancel_orphan(owners[k], deps[k]);
+}
+
+// The frame form of TileProducer's per-tile protocol (TileProducer.h:331-378: one
+// CreateTile task per getTile, each running doCreateTile): every requested tile is
+// acquired as getTile does, then all queued tiles of the producer (with their
+// inputs) are produced in one scheduler run.  Each returned tile holds one user,
+// released with tp_producer_put_tile.  On failure the tiles acquired by this call
+// are released and none is returned.
+extern "C" int tp_create_tiles(tp_producer *p, const tp_tile_req *reqs, int n, tp_tile **tiles_out, void *stream)
+{
+    if (!p || n < 0 || (n > 0 && (!reqs || !tiles_out))) return tp::fail(TP_E_BAD_ARG, "tp_create_tiles: bad arguments");
+    for (int i = 0; i < n; ++i) {
+        const tp_tile_req &r = reqs[i];
+        if (r.level < 0 || r.level > 30 || r.tx < 0 || r.ty < 0 || (r.tx >> r.level) != 0 || (r.ty >> r.level) != 0)
+            return tp::fail(TP_E_BAD_ARG, "tp_create_tiles: bad quadtree coordinates");
+    }
+    int rc = TP_OK;
+    int got = 0;
+    for (; got < n; ++got) {
+        tiles_out[got] = get_tile(p, reqs[got].level, reqs[got].tx, reqs[got].ty, nullptr, &rc);
+        if (!tiles_out[got]) break;
+    }
+    if (got == n) {
+        tp_producer *all[1] = {p};
+        rc = tp_scheduler_run(all, 1, stream);
+        if (rc == TP_OK) return TP_OK;
+    }
+    if (rc == TP_OK) rc = TP_E_CACHE_FULL;
+    const std::string msg = tp_last_error();
+    for (int i = 0; i < got; ++i) {
+        put_tile(p, tiles_out[i]);
+        cancel_orphan(p, tiles_out[i]);
+        tiles_out[i] = nullptr;
+    }
+    return tp::fail(rc, msg);
+}
+
+// doCreateTile of one tile (level, tx, ty): tp_create_tiles with one request.
+extern "C" int tp_create_tile(tp_producer *p, int level, int tx, int ty, tp_tile **tile_out, void *stream)
+{
+    const tp_tile_req r = {level, tx, ty};
+    return tp_create_tiles(p, &r, 1, tile_out, stream);
+}
+
 extern "C" int tp_sphere_frame(double root_quad_size, int level, int tx, int ty, float *out47)
 {
     if (!out47 || !(root_quad_size > 0.0) || level < 0 || level > 30) return tp::fail(TP_E_BAD_ARG, "tp_sphere_frame: bad arguments");

@@ -272,6 +272,20 @@ class TileProducer:
     def queued(self):
         return check(lib().tp_producer_queued(self.handle))
 
+    def create_tiles(self, requests, stream=None):
+        """Batched doCreateTile (tp_create_tiles): [(level, tx, ty), ...] -> produced
+        tiles, each holding one user."""
+        n = len(requests)
+        flat = (C.c_int32 * (3 * n))(*[int(v) for r in requests for v in r])
+        out = (C.c_void_p * n)()
+        check(lib().tp_create_tiles(self.handle, flat, n, out, stream))
+        return [Tile(out[i]) for i in range(n)]
+
+    def create_tile(self, level, tx, ty, stream=None):
+        h = C.c_void_p()
+        check(lib().tp_create_tile(self.handle, level, tx, ty, C.byref(h), stream))
+        return Tile(h.value)
+
 
 class ResidualProducer(TileProducer):
     """ResidualProducer: a .dat pyramid, a host callback or zero residuals."""

@@ -121,6 +121,10 @@ def lib():
         "tp_producer_queued": ([_vp], _i),
         "tp_tile_info": ([_vp] + [C.POINTER(_i)] * 6, _i),
         "tp_scheduler_run": ([C.POINTER(_vp), _i, _vp], _i),
+        "tp_create_tiles": ([_vp, C.POINTER(C.c_int32), _i, C.POINTER(_vp), _vp], _i),
+        "tp_create_tile": ([_vp, _i, _i, _i, C.POINTER(_vp), _vp], _i),
+        "tp_quadtree_requests": ([C.c_double, _i, C.c_float, C.c_float, C.c_double, C.c_double, C.c_double,
+                                  C.c_double, C.POINTER(C.c_int32), _i, C.POINTER(_i)], _i),
         "tp_residual_tile": ([_vp, _i, _i, _i, _f32p, _i], _i),
         "tp_sphere_frame": ([C.c_double, _i, _i, _i, _f32p], _i),
         "tp_dat_open": ([C.c_char_p, C.POINTER(_vp)], _i),

@@ -164,3 +164,41 @@ def test_planet_face_sphere_normals(gpu, oracle_lib, face):
         enx, eny = orc.normals_sphere(W, zm, f)
         assert_normals_close(download(ns, h.slot, tp.NX), enx, "sphere nx %s" % (t,))
         assert_normals_close(download(ns, h.slot, tp.NY), eny, "sphere ny %s" % (t,))
+
+
+def test_create_tiles_frame_form_and_cache_full(gpu, oracle_lib):
+    """tp_create_tiles / tp_create_tile (the batched doCreateTile): produced tiles
+    equal the oracle's; a request that overflows the cache fails with
+    TP_E_CACHE_FULL and leaves none of its tiles acquired."""
+    tp, orc = gpu, oracle_lib
+    W = 101
+    es, rs = tp.TileStorage(W, 3, 64), tp.TileStorage(W, 1, 64)
+    ec, rc = tp.TileCache(es, "e"), tp.TileCache(rs, "r")
+    r = tp.ResidualProducer(rc, source=synthetic_residual)
+    amps = [-140.0, -100.0, -15.0]
+    e = tp.ElevationProducer(ec, r, noise_amp=amps, params=tp.make_params(), face=0)
+    e.set_root_quad_size(ROOT)
+    reqs = [(2, 1, 3), (2, 2, 3), (1, 0, 1)]
+    tiles = e.create_tiles(reqs)
+    one = e.create_tile(2, 3, 0)
+    tree = set()
+    for (l, x, y) in reqs + [(2, 3, 0)]:
+        while l >= 0:
+            tree.add((l, x, y))
+            l, x, y = l - 1, x // 2, y // 2
+    want = oracle_tree(orc, tree, W, amps, 0, lambda l, x, y: synthetic_residual(l, x, y, W))
+    for t, h in zip(reqs + [(2, 3, 0)], tiles + [one]):
+        info = h.info()
+        assert info["done"] == 1 and info["users"] >= 1 and (info["level"], info["tx"], info["ty"]) == t
+        assert np.array_equal(download(es, h.slot, tp.ZF), want[t][0]), t
+    for h in tiles + [one]:
+        e.put_tile(h)
+    # a 4-slot cache cannot hold six level-2 tiles and their parents
+    small = tp.TileStorage(W, 3, 4)
+    sc = tp.TileCache(small, "small")
+    e2 = tp.ElevationProducer(sc, r, noise_amp=amps, params=tp.make_params(), face=0)
+    e2.set_root_quad_size(ROOT)
+    with pytest.raises(tp.TPError) as err:
+        e2.create_tiles([(2, x, y) for x in range(3) for y in range(2)])
+    assert err.value.code == tp.TP_E_CACHE_FULL
+    assert sc.get_used_tiles() == 0
