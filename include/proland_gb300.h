@@ -119,6 +119,13 @@ int tp_elevation_batch(tp_storage *elev, tp_storage *residuals, tp_storage *norm
 int tp_elevation_batch_device(tp_storage *elev, tp_storage *residuals, tp_storage *normals,
                               const tp_elev_params *params, const tp_tile_job *jobs_dev, int n,
                               void *stream);
+/* Normal tiles of already produced elevation tiles: job k reads elevation slot
+ * jobs[k].out_slot and writes normal slot jobs[k].normal_slot (format 2), sample
+ * spacing tile_meters / (W - 5).  root_quad_size > 0: the tiles lie on the sphere
+ * of a cube-face planet of that root quad size (NormalProducer with deformation,
+ * NormalProducer.cpp:215-273; terrain2/normalShader.glsl); 0: flat. */
+int tp_normal_batch(tp_storage *elev, tp_storage *normals, const tp_tile_job *jobs, int n, double root_quad_size,
+                    void *stream);
 /* Same as tp_elevation_batch, allocating nothing.  (No counterpart in the
  * reference: its producers draw on GL textures created up front.)  For callers
  * that may not allocate while producing tiles: the kernel's scratch (work

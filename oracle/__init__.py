@@ -79,6 +79,8 @@ def lib():
         L.or_residual_upsample.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, _f32p, _f32p]
         L.or_compute_residual.argtypes = [C.c_int, C.c_int, C.c_int, _f32p, _f32p, _f32p,
                                           C.POINTER(C.c_int16), _f32p]
+        L.or_normals_sphere_f64.argtypes = [C.c_int, _f64p, C.c_int, C.c_double, C.c_int, C.c_int, C.c_int,
+                                            _f64p, _f64p, C.c_int]
         _i16p = C.POINTER(C.c_int16)
         L.or_fbm_heights.argtypes = [C.c_int, C.c_int, C.c_int, C.c_float, C.c_float, C.c_uint32, _i16p]
         L.or_level_tile.argtypes = [_i16p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_float, _f32p]
@@ -206,6 +208,16 @@ def normals_sphere(W, zm, frame):
     nx = np.empty((n1, n1), np.float32)
     ny = np.empty((n1, n1), np.float32)
     lib().or_normals_sphere(W, _p(zm), zm.shape[1], C.byref(frame), _p(nx), _p(ny), n1)
+    return nx, ny
+
+
+def normals_sphere_f64(W, zm, root_quad_size, level, tx, ty):
+    zm = np.ascontiguousarray(zm, np.float64)
+    n1 = W - 4
+    nx = np.empty((n1, n1), np.float64)
+    ny = np.empty((n1, n1), np.float64)
+    lib().or_normals_sphere_f64(W, _p(zm, _f64p), zm.shape[1], float(root_quad_size), level, tx, ty,
+                                _p(nx, _f64p), _p(ny, _f64p), n1)
     return nx, ny
 
 

@@ -601,6 +601,77 @@ void or_normals_sphere(int W, const float *zm, int zm_pitch, const or_sphere_fra
         }
 }
 
+/* FP64 twin of or_sphere_frame_make + or_normals_sphere: the frame and the
+ * positions in double, from double heights (the FP64 evaluation the errors of
+ * the float path are stated against). */
+void or_normals_sphere_f64(int W, const double *zm, int zm_pitch, double D, int level, int tx, int ty,
+                           double *nx, double *ny, int out_pitch)
+{
+    double R = D / 2.0, sc = (double)(1 << level);
+    double x0 = (double)tx / sc * D - R, x1 = (double)(tx + 1) / sc * D - R;
+    double y0 = (double)ty / sc * D - R, y1 = (double)(ty + 1) / sc * D - R;
+    double p[4][3] = {{x0, y0, R}, {x1, y0, R}, {x0, y1, R}, {x1, y1, R}};
+    double v[4][3], L[4], vc[3] = {0, 0, 0}, C[3][4], N[3][4];
+    for (int k = 0; k < 4; ++k) {
+        v3_norm(p[k], v[k], &L[k]);
+        for (int c = 0; c < 3; ++c) vc[c] += v[k][c];
+    }
+    for (int c = 0; c < 3; ++c) vc[c] *= 0.25;
+    for (int r = 0; r < 3; ++r)
+        for (int k = 0; k < 4; ++k) {
+            C[r][k] = v[k][r] * R - vc[r] * R;
+            N[r][k] = v[k][r];
+        }
+    double pc[3] = {(x0 + x1) * 0.5, (y0 + y1) * 0.5, R}, uz[3], ux[3], uy[3];
+    v3_norm(pc, uz, NULL);
+    double t[3] = {uz[2], 0.0, -uz[0]};
+    v3_norm(t, ux, NULL);
+    uy[0] = uz[1] * ux[2] - uz[2] * ux[1];
+    uy[1] = uz[2] * ux[0] - uz[0] * ux[2];
+    uy[2] = uz[0] * ux[1] - uz[1] * ux[0];
+    double size = D / sc, e0 = R / 32.0, e1 = R / 64.0;
+    double sm = (size - e0) / (e1 - e0);
+    sm = sm < 0.0 ? 0.0 : (sm > 1.0 ? 1.0 : sm);
+    sm = sm * sm * (3.0 - 2.0 * sm);
+    int n = W - 5;
+    for (int q = 0; q <= n; ++q)
+        for (int pp = 0; pp <= n; ++pp) {
+            double P[4][3];
+            const int du[4] = {-1, 1, 0, 0}, dv[4] = {0, 0, -1, 1};
+            for (int m = 0; m < 4; ++m) {
+                double u = (double)(pp + du[m]) / n, vv = (double)(q + dv[m]) / n;
+                double al[4] = {(1 - u) * (1 - vv), u * (1 - vv), (1 - u) * vv, u * vv};
+                double d = 0.0, ap[4], up[3], cp[3];
+                for (int k = 0; k < 4; ++k) d += al[k] * L[k];
+                for (int k = 0; k < 4; ++k) ap[k] = al[k] * L[k] / d;
+                for (int r = 0; r < 3; ++r) {
+                    up[r] = cp[r] = 0.0;
+                    for (int k = 0; k < 4; ++k) {
+                        up[r] += N[r][k] * ap[k];
+                        cp[r] += C[r][k] * ap[k];
+                    }
+                }
+                double len = sqrt(up[0] * up[0] + up[1] * up[1] + up[2] * up[2]);
+                double kk = len * (1.0 - sm) + sm;
+                double h = zm[(pp + 2 + du[m]) + (size_t)(q + 2 + dv[m]) * zm_pitch];
+                double hp = (h + R * (1.0 - kk)) / kk;
+                for (int r = 0; r < 3; ++r) P[m][r] = cp[r] + hp * up[r];
+            }
+            double a[3], b[3], cr[3];
+            for (int r = 0; r < 3; ++r) {
+                a[r] = P[1][r] - P[0][r];
+                b[r] = P[3][r] - P[2][r];
+            }
+            cr[0] = a[1] * b[2] - a[2] * b[1];
+            cr[1] = a[2] * b[0] - a[0] * b[2];
+            cr[2] = a[0] * b[1] - a[1] * b[0];
+            double inv = 1.0 / sqrt(cr[0] * cr[0] + cr[1] * cr[1] + cr[2] * cr[2]);
+            size_t o = pp + (size_t)q * out_pitch;
+            nx[o] = (ux[0] * cr[0] + ux[1] * cr[1] + ux[2] * cr[2]) * inv;
+            ny[o] = (uy[0] * cr[0] + uy[1] * cr[1] + uy[2] * cr[2]) * inv;
+        }
+}
+
 /* ---- batch runner for the timed CPU baseline ------------------------------ */
 typedef struct {
     const or_job *jobs;

@@ -116,6 +116,9 @@ void or_compute_residual(int W, int tx, int ty, const float *parent_approx,
 /* ResidualProducer::upsample for the small tiles below the pyramid's minLevel. */
 void or_residual_upsample(int n, int tilesize, int tx, int ty, const float *parent, float *out);
 
+void or_normals_sphere_f64(int W, const double *zm, int zm_pitch, double D, int level, int tx, int ty,
+                           double *nx, double *ny, int out_pitch);
+
 /* ---- learned.c: device preprocess height field, level tiles, learned net ---- */
 void or_fbm_heights(int size, int octaves, int base_cells, float amplitude, float quantum, uint32_t seed, int16_t *out);
 void or_level_tile(const int16_t *base, int ts, int max_level, int level, int tx, int ty, float scale, float *out);

@@ -185,3 +185,31 @@ int launch_normals(tp_storage *elev, tp_storage *nrm, const int *eslots, const i
 }
 
 }  // namespace tp
+
+// Kernel-level entry of the normal pass: job k reads elevation slot out_slot and
+// writes normal slot normal_slot; with root_quad_size > 0 the tiles lie on the
+// sphere of a cube-face terrain (NormalProducer's deform path), else on a plane.
+extern "C" int tp_normal_batch(tp_storage *elev, tp_storage *normals, const tp_tile_job *jobs, int n,
+                               double root_quad_size, void *stream)
+{
+    if (!elev || !normals || n < 0 || (n > 0 && !jobs)) return tp::fail(TP_E_BAD_ARG, "tp_normal_batch: bad arguments");
+    if (elev->on_device != 1 || elev->channels != 3 || normals->on_device != 1 || normals->channels != 2 ||
+        normals->W != elev->W - 4)
+        return tp::fail(TP_E_BAD_ARG, "tp_normal_batch: device storages of W (3 channels) and W - 4 (2 channels) needed");
+    if (n == 0) return TP_OK;
+    std::vector<int> es(n), ns(n);
+    std::vector<float> meters(n);
+    std::vector<tp::SphereFrame> frames(root_quad_size > 0.0 ? n : 0);
+    for (int k = 0; k < n; ++k) {
+        const tp_tile_job &j = jobs[k];
+        if (j.level < 0 || j.level > 30 || (j.tx >> j.level) != 0 || (j.ty >> j.level) != 0 || j.tx < 0 || j.ty < 0)
+            return tp::fail(TP_E_BAD_ARG, "tp_normal_batch: bad quadtree coordinates");
+        es[k] = j.out_slot;
+        ns[k] = j.normal_slot;
+        meters[k] = j.tile_meters;
+        if (!(j.tile_meters > 0.0f)) return tp::fail(TP_E_BAD_ARG, "tp_normal_batch: tile_meters must be positive");
+        if (root_quad_size > 0.0) tp::sphere_frame(root_quad_size, j.level, j.tx, j.ty, &frames[k]);
+    }
+    return tp::launch_normals(elev, normals, es.data(), ns.data(), meters.data(), n, stream,
+                              root_quad_size > 0.0 ? frames.data() : nullptr);
+}

@@ -116,6 +116,13 @@ def elevation_batch(elev, residuals, normals, params, jobs, stream=None):
                                    arr, len(jobs), stream))
 
 
+def normal_batch(elev, normals, jobs, root_quad_size=0.0, stream=None):
+    """Normal tiles of produced elevation tiles (tp_normal_batch); sphere normals
+    when root_quad_size > 0."""
+    arr = (TileJob * len(jobs))(*jobs)
+    check(lib().tp_normal_batch(elev.handle, normals.handle, arr, len(jobs), float(root_quad_size), stream))
+
+
 def elevation_batch_device(elev, residuals, normals, params, jobs_dev_ptr, n, stream=None):
     check(lib().tp_elevation_batch_device(elev.handle, residuals.handle if residuals else None,
                                           normals.handle if normals else None, C.byref(params),

@@ -86,6 +86,7 @@ def lib():
         "tp_storage_download": ([_vp, _i, _i, _i, _vp, _vp], _i),
         "tp_elevation_batch": ([_vp, _vp, _vp, C.POINTER(ElevParams), C.POINTER(TileJob), _i, _vp], _i),
         "tp_elevation_batch_device": ([_vp, _vp, _vp, C.POINTER(ElevParams), _vp, _i, _vp], _i),
+        "tp_normal_batch": ([_vp, _vp, C.POINTER(TileJob), _i, C.c_double, _vp], _i),
         "tp_elevation_batch_noalloc": ([_vp, _vp, _vp, C.POINTER(ElevParams), C.POINTER(TileJob), _i, _vp], _i),
         "tp_frame_create": ([C.POINTER(_vp)], _i),
         "tp_frame_destroy": ([_vp], _i),
