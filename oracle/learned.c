@@ -110,10 +110,26 @@ static float bf16r(float x)
     return x;
 }
 
-static double gelu_d(double z) { return 0.5 * z * (1.0 + erf(z * 0.70710678118654752)); }
-static double gelu_grad_d(double z) { return 0.5 * (1.0 + erf(z * 0.70710678118654752)) + z * 0.39894228040143268 * exp(-0.5 * z * z); }
-static float gelu_f(float z) { return 0.5f * z * (1.0f + erff(z * 0.70710678118654752f)); }
-static float gelu_grad_f(float z) { return 0.5f * (1.0f + erff(z * 0.70710678118654752f)) + z * 0.39894228040143268f * expf(-0.5f * z * z); }
+/* GELU in its tanh form: 0.5 z (1 + tanh(sqrt(2/pi) (z + 0.044715 z^3))) */
+static double gelu_d(double z)
+{
+    return 0.5 * z * (1.0 + tanh(0.7978845608028654 * (z + 0.044715 * z * z * z)));
+}
+static double gelu_grad_d(double z)
+{
+    const double t = tanh(0.7978845608028654 * (z + 0.044715 * z * z * z));
+    return 0.5 * (1.0 + t) + 0.5 * z * (1.0 - t * t) * 0.7978845608028654 * (1.0 + 0.134145 * z * z);
+}
+static float gelu_f(float z)
+{
+    const float t = tanhf(0.7978845608028654f * (z + 0.044715f * z * z * z));
+    return 0.5f * z * (1.0f + t);
+}
+static float gelu_grad_f(float z)
+{
+    const float t = tanhf(0.7978845608028654f * (z + 0.044715f * z * z * z));
+    return 0.5f * (1.0f + t) + 0.5f * z * (1.0f - t * t) * 0.7978845608028654f * (1.0f + 0.134145f * z * z);
+}
 
 /* Z[img][p][co] = sum_{tap, ci} X[img][p + tap][ci] w[co][tap][ci], zero outside the image */
 static void conv_fwd(int W, int n, const double *X, int cin, const double *w, int cout, double *Z)

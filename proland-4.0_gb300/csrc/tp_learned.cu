@@ -30,17 +30,28 @@ namespace {
 
 using namespace tp::sm100;
 
-constexpr int kThreads = 128;
 constexpr int kHaloX = kBlockX + 2, kHaloY = kBlockY + 2;
 constexpr int kRowStride = kHaloX * 16;                     // bytes per halo row of one channel group
 constexpr int kHaloBytes = kRowStride * kHaloY;             // one channel group: 2880
 constexpr int kGroupStride = (kHaloBytes + 127) / 128 * 128;  // 2944: TMA destinations 128-byte aligned
 constexpr int kBoxBytes = 8 * kBlockX * kBlockY * 2;        // one 8-channel group of a block: 2048
 
-__device__ __forceinline__ float gelu(float z) { return 0.5f * z * (1.0f + erff(z * 0.70710678118654752f)); }
+// GELU in its tanh form, 0.5 z (1 + tanh(sqrt(2/pi) (z + 0.044715 z^3))), on the SFU's tanh.
+__device__ __forceinline__ float tanh_sfu(float x)
+{
+    float y;
+    asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ float gelu(float z)
+{
+    const float t = tanh_sfu(0.7978845608028654f * (z + 0.044715f * z * z * z));
+    return 0.5f * z * (1.0f + t);
+}
 __device__ __forceinline__ float gelu_grad(float z)
 {
-    return 0.5f * (1.0f + erff(z * 0.70710678118654752f)) + z * 0.39894228040143268f * expf(-0.5f * z * z);
+    const float t = tanh_sfu(0.7978845608028654f * (z + 0.044715f * z * z * z));
+    return 0.5f * (1.0f + t) + 0.5f * z * (1.0f - t * t) * 0.7978845608028654f * (1.0f + 0.134145f * z * z);
 }
 
 __device__ __forceinline__ uint32_t pack2(float a, float b)
@@ -79,109 +90,149 @@ __device__ __forceinline__ void load_bf16(const __nv_bfloat16 *src, float *v)
     }
 }
 
+// Roles of a CTA: warp 0 issues the TMA copies, warp 1 the tensor-core MMAs (and owns
+// the tensor memory), warps 2-5 (one per tensor-memory lane quadrant) run the epilogue.
+constexpr int kRoleThreads = 192;
+constexpr int kConvStages = 4;
+
 template <int CIN, int COUT>
 constexpr int conv_smem_bytes()
 {
-    return (CIN / 8) * kGroupStride + 9 * CIN * COUT * 2 + 32;
+    return kConvStages * (CIN / 8) * kGroupStride + 9 * CIN * COUT * 2 + 128;
 }
 
+// Tiles this CTA takes from a persistent loop over `total` tiles.
+__device__ __forceinline__ int my_tiles(int total) { return (total - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x; }
+
 template <int CIN, int COUT, int MODE>
-__global__ void __launch_bounds__(kThreads) conv_kernel(const __grid_constant__ CUtensorMap xmap, const ConvLaunch a)
+__global__ void __launch_bounds__(kRoleThreads) conv_kernel(const __grid_constant__ CUtensorMap xmap, const ConvLaunch a)
 {
     extern __shared__ __align__(1024) uint8_t smem[];
     constexpr int NCG = CIN / 8, KSTEPS = CIN / 16, NMMA = 9 * KSTEPS;
+    constexpr int STAGE = NCG * kGroupStride;
     constexpr int BBYTES = NMMA * COUT * 32;
     uint8_t *halo = smem;
-    uint8_t *bsm = smem + NCG * kGroupStride;
-    uint64_t *bars = reinterpret_cast<uint64_t *>(bsm + BBYTES);
-    uint32_t *tslot = reinterpret_cast<uint32_t *>(bars + 2);
+    uint8_t *bsm = smem + kConvStages * STAGE;
+    uint64_t *full = reinterpret_cast<uint64_t *>(bsm + BBYTES);
+    uint64_t *empty = full + kConvStages;
+    uint64_t *acc_full = empty + kConvStages;
+    uint64_t *acc_empty = acc_full + 2;
+    uint32_t *tslot = reinterpret_cast<uint32_t *>(acc_empty + 2);
+    volatile int *abort = reinterpret_cast<volatile int *>(tslot + 1);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 
-    for (int i = tid; i < BBYTES / 16; i += kThreads)
+    for (int i = tid; i < BBYTES / 16; i += kRoleThreads)
         reinterpret_cast<uint4 *>(bsm)[i] = reinterpret_cast<const uint4 *>(a.wpack)[i];
     if (tid == 0) {
-        mbar_init(&bars[0], 1);
-        mbar_init(&bars[1], 1);
+        for (int s = 0; s < kConvStages; ++s) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], 1);
+        }
+        for (int b = 0; b < 2; ++b) {
+            mbar_init(&acc_full[b], 1);
+            mbar_init(&acc_empty[b], 128);
+        }
+        *abort = 0;
     }
-    if (warp == 0) tmem_alloc(tslot, 32);
+    if (warp == 1) tmem_alloc(tslot, 64);
     fence_proxy_async_smem();
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = *tslot;
     const int per_img = a.tiles_x * a.tiles_y, total = a.nimg * per_img;
-    const int Wp = a.W + 2;
-    constexpr uint32_t idesc = idesc_bf16(128, COUT, 0, 0);
-    const uint32_t halo_a = smem_u32(halo), b_a = smem_u32(bsm);
-    bool ok = true;
-    uint32_t it = 0;
-    for (int t = blockIdx.x; t < total; t += gridDim.x, ++it) {
-        const int img = t / per_img, rem = t - img * per_img;
-        const int by = rem / a.tiles_x, bx = rem - by * a.tiles_x;
-        const int x0 = bx * kBlockX, y0 = by * kBlockY;
-        if (tid == 0) {
-            mbar_expect_tx(&bars[0], NCG * kHaloBytes);
+    const int mine = my_tiles(total);
+
+    if (warp == 0) {
+        if (lane == 0) {  // producer: halo of tile i into stage i % kConvStages
+            int i = 0;
+            for (; i < mine; ++i) {
+                const int s = i % kConvStages;
+                if (i >= kConvStages && !mbar_wait_abortable(&empty[s], ((i / kConvStages) - 1) & 1, abort)) break;
+                const int t = blockIdx.x + i * gridDim.x;
+                const int img = t / per_img, rem = t - img * per_img;
+                const int by = rem / a.tiles_x, bx = rem - by * a.tiles_x;
+                mbar_expect_tx(&full[s], NCG * kHaloBytes);
 #pragma unroll
-            for (int cg = 0; cg < NCG; ++cg) tma_load_4d(halo + cg * kGroupStride, &xmap, cg * 8, x0, y0, img, &bars[0]);
+                for (int cg = 0; cg < NCG; ++cg)
+                    tma_load_4d(halo + s * STAGE + cg * kGroupStride, &xmap, cg * 8, bx * kBlockX, by * kBlockY, img,
+                                &full[s]);
+            }
+            if (*abort)  // copies in flight land before the CTA leaves
+                for (int k = i > kConvStages ? i - kConvStages : 0; k < i; ++k)
+                    mbar_wait(&full[k % kConvStages], (k / kConvStages) & 1);
         }
-        if (!__syncthreads_and(mbar_wait(&bars[0], it & 1))) {
-            ok = false;
-            break;
+    } else if (warp == 1) {
+        if (lane == 0) {  // MMA issuer: tile i into accumulator i % 2
+            constexpr uint32_t idesc = idesc_bf16(128, COUT, 0, 0);
+            const uint32_t b_a = smem_u32(bsm);
+            int i = 0;
+            for (; i < mine; ++i) {
+                const int s = i % kConvStages, b = i & 1;
+                if (!mbar_wait_abortable(&full[s], (i / kConvStages) & 1, abort)) break;
+                if (i >= 2 && !mbar_wait_abortable(&acc_empty[b], ((i >> 1) - 1) & 1, abort)) break;
+                tc_fence_after();
+                const uint32_t h_a = smem_u32(halo + s * STAGE);
+#pragma unroll
+                for (int q = 0; q < NMMA; ++q) {
+                    const int tap = q / KSTEPS, st = q - tap * KSTEPS;
+                    const int dy = tap / 3, dx = tap - dy * 3;
+                    const uint64_t ad = sdesc(h_a + 2 * st * kGroupStride + dy * kRowStride + dx * 16, kGroupStride,
+                                              kRowStride);
+                    const uint64_t bd = sdesc(b_a + q * COUT * 32, 128, 256);
+                    mma_bf16(tmem + b * 32, ad, bd, idesc, q > 0 ? 1u : 0u);
+                }
+                mma_commit(&empty[s]);
+                mma_commit(&acc_full[b]);
+            }
+            if (*abort && i > 0) mbar_wait(&empty[(i - 1) % kConvStages], ((i - 1) / kConvStages) & 1);
         }
-        if (tid == 0) {
+    } else {  // epilogue: rows 32 q .. 32 q + 31 of the accumulator
+        const int q = warp & 3;
+        const int Wp = a.W + 2;
+        for (int i = 0; i < mine; ++i) {
+            const int b = i & 1;
+            if (!__all_sync(0xffffffffu, mbar_wait_abortable(&acc_full[b], (i >> 1) & 1, abort))) break;
             tc_fence_after();
+            float acc[COUT];
+            const uint32_t taddr = tmem + b * 32 + ((uint32_t)(q * 32) << 16);
+            if (COUT == 32)
+                tmem_ld32(taddr, acc);
+            else
+                tmem_ld16(taddr, acc);
+            tc_fence_before();
+            mbar_arrive(&acc_empty[b]);
+            const int t = blockIdx.x + i * gridDim.x;
+            const int img = t / per_img, rem = t - img * per_img;
+            const int by = rem / a.tiles_x, bx = rem - by * a.tiles_x;
+            const int m = q * 32 + lane;
+            const int px = bx * kBlockX + (m & 7), py = by * kBlockY + (m >> 3);
+            if (px < a.W && py < a.W) {
+                const size_t pix = ((size_t)img * Wp + (py + 1)) * Wp + (px + 1);
+                if (MODE == kHidden) {
+                    const float *e = a.emb ? a.emb + (size_t)min(max(a.level[img], 0), kLevels - 1) * COUT : nullptr;
 #pragma unroll
-            for (int q = 0; q < NMMA; ++q) {
-                const int tap = q / KSTEPS, s = q - tap * KSTEPS;
-                const int dy = tap / 3, dx = tap - dy * 3;
-                const uint64_t ad = sdesc(halo_a + 2 * s * kGroupStride + dy * kRowStride + dx * 16, kGroupStride,
-                                          kRowStride);
-                const uint64_t bd = sdesc(b_a + q * COUT * 32, 128, 256);
-                mma_bf16(tmem, ad, bd, idesc, q > 0 ? 1u : 0u);
-            }
-            mma_commit(&bars[1]);
-        }
-        if (!__syncthreads_and(mbar_wait(&bars[1], it & 1))) {
-            ok = false;
-            break;
-        }
-        tc_fence_after();
-        float acc[COUT];
-        const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16);
-        if (COUT == 32)
-            tmem_ld32(taddr, acc);
-        else
-            tmem_ld16(taddr, acc);
-        const int m = warp * 32 + lane, r = m >> 3, c = m & 7;
-        const int px = x0 + c, py = y0 + r;
-        if (px < a.W && py < a.W) {
-            const size_t pix = ((size_t)img * Wp + (py + 1)) * Wp + (px + 1);
-            if (MODE == kHidden) {
-                const float *e = a.emb ? a.emb + (size_t)min(max(a.level[img], 0), kLevels - 1) * COUT : nullptr;
+                    for (int j = 0; j < COUT; ++j) acc[j] += a.bias[j] + (e ? e[j] : 0.0f);
+                    if (a.zsave) store_bf16<COUT>(a.zsave + pix * COUT, acc);
 #pragma unroll
-                for (int j = 0; j < COUT; ++j) acc[j] += a.bias[j] + (e ? e[j] : 0.0f);
-                if (a.zsave) store_bf16<COUT>(a.zsave + pix * COUT, acc);
+                    for (int j = 0; j < COUT; ++j) acc[j] = gelu(acc[j]);
+                    store_bf16<COUT>(a.out + pix * COUT, acc);
+                } else if (MODE == kLast) {
+                    a.out_f32[((size_t)img * a.W + py) * a.W + px] = acc[0] + a.bias[0];
+                } else {
+                    float z[COUT];
+                    load_bf16<COUT>(a.zprev + pix * COUT, z);
 #pragma unroll
-                for (int j = 0; j < COUT; ++j) acc[j] = gelu(acc[j]);
-                store_bf16<COUT>(a.out + pix * COUT, acc);
-            } else if (MODE == kLast) {
-                a.out_f32[((size_t)img * a.W + py) * a.W + px] = acc[0] + a.bias[0];
-            } else {
-                float z[COUT];
-                load_bf16<COUT>(a.zprev + pix * COUT, z);
-#pragma unroll
-                for (int j = 0; j < COUT; ++j) acc[j] *= gelu_grad(z[j]);
-                store_bf16<COUT>(a.out + pix * COUT, acc);
+                    for (int j = 0; j < COUT; ++j) acc[j] *= gelu_grad(z[j]);
+                    store_bf16<COUT>(a.out + pix * COUT, acc);
+                }
             }
         }
-        tc_fence_before();
-        __syncthreads();
     }
-    if (!ok && tid == 0) atomicExch(a.status, TP_E_TIMEOUT);
-    tc_fence_before();
     __syncthreads();
+    if (tid == 0 && *abort) atomicExch(a.status, TP_E_TIMEOUT);
     tc_fence_after();
-    if (warp == 0) tmem_dealloc(tmem, 32);
+    if (warp == 1) tmem_dealloc(tmem, 64);
 }
 
 template <int CIN, int COUT>
@@ -190,109 +241,139 @@ constexpr int wgrad_tiles()
     return (9 * CIN / 8 + 15) / 16;
 }
 template <int CIN, int COUT>
+constexpr int wgrad_stage_bytes()
+{
+    return wgrad_tiles<CIN, COUT>() * 16 * kBoxBytes + (COUT / 8) * kBoxBytes;
+}
+template <int CIN, int COUT>
 constexpr int wgrad_smem_bytes()
 {
-    return wgrad_tiles<CIN, COUT>() * 16 * kBoxBytes + (COUT / 8) * kBoxBytes + 32;
+    return 2 * wgrad_stage_bytes<CIN, COUT>() + 128;
 }
 
 template <int CIN, int COUT>
-__global__ void __launch_bounds__(kThreads) wgrad_kernel(const __grid_constant__ CUtensorMap xmap,
-                                                         const __grid_constant__ CUtensorMap zmap, const WgradLaunch a)
+__global__ void __launch_bounds__(kRoleThreads) wgrad_kernel(const __grid_constant__ CUtensorMap xmap,
+                                                             const __grid_constant__ CUtensorMap zmap, const WgradLaunch a)
 {
     extern __shared__ __align__(1024) uint8_t smem[];
     constexpr int NCG = CIN / 8, NGO = COUT / 8, NG = 9 * NCG;
     constexpr int NMT = wgrad_tiles<CIN, COUT>();
     constexpr int ABYTES = NMT * 16 * kBoxBytes;
+    constexpr int STAGE = wgrad_stage_bytes<CIN, COUT>();
     constexpr uint32_t TCOLS = NMT * 32 <= 32 ? 32 : (NMT * 32 <= 64 ? 64 : 128);
-    uint8_t *asm_ = smem;
-    uint8_t *bsm = smem + ABYTES;
-    uint64_t *bars = reinterpret_cast<uint64_t *>(bsm + NGO * kBoxBytes);
-    uint32_t *tslot = reinterpret_cast<uint32_t *>(bars + 2);
+    uint64_t *full = reinterpret_cast<uint64_t *>(smem + 2 * STAGE);
+    uint64_t *empty = full + 2;
+    uint64_t *done = empty + 2;
+    uint32_t *tslot = reinterpret_cast<uint32_t *>(done + 1);
+    volatile int *abort = reinterpret_cast<volatile int *>(tslot + 1);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 
     // rows of the last M tile past the real (tap, channel) groups are never loaded
-    for (int i = NG * kBoxBytes / 16 + tid; i < ABYTES / 16; i += kThreads) reinterpret_cast<uint4 *>(asm_)[i] = make_uint4(0, 0, 0, 0);
+    for (int s = 0; s < 2; ++s)
+        for (int i = NG * kBoxBytes / 16 + tid; i < ABYTES / 16; i += kRoleThreads)
+            reinterpret_cast<uint4 *>(smem + s * STAGE)[i] = make_uint4(0, 0, 0, 0);
     if (tid == 0) {
-        mbar_init(&bars[0], 1);
-        mbar_init(&bars[1], 1);
+        for (int s = 0; s < 2; ++s) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], 1 + 128);  // the MMAs' commit and the 128 bias threads
+        }
+        mbar_init(done, 1);
+        *abort = 0;
     }
-    if (warp == 0) tmem_alloc(tslot, TCOLS);
+    if (warp == 1) tmem_alloc(tslot, TCOLS);
     fence_proxy_async_smem();
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = *tslot;
     const int per_img = a.tiles_x * a.tiles_y, total = a.nimg * per_img;
-    constexpr uint32_t idesc = idesc_bf16(128, COUT, 1, 1);
-    const uint32_t a_a = smem_u32(asm_), b_a = smem_u32(bsm);
-    bool ok = true;
-    uint32_t it = 0;
-    const int bn = tid % COUT;
-    for (int t = blockIdx.x; t < total; t += gridDim.x, ++it) {
-        const int img = t / per_img, rem = t - img * per_img;
-        const int by = rem / a.tiles_x, bx = rem - by * a.tiles_x;
-        const int x0 = bx * kBlockX, y0 = by * kBlockY;
-        if (tid == 0) {
-            mbar_expect_tx(&bars[0], (NG + NGO) * kBoxBytes);
-            for (int g = 0; g < NG; ++g) {
-                const int tap = g / NCG, cg = g - tap * NCG;
-                const int dy = tap / 3, dx = tap - dy * 3;
-                tma_load_4d(asm_ + g * kBoxBytes, &xmap, cg * 8, x0 + dx, y0 + dy, img, &bars[0]);
-            }
-#pragma unroll
-            for (int go = 0; go < NGO; ++go) tma_load_4d(bsm + go * kBoxBytes, &zmap, go * 8, x0 + 1, y0 + 1, img, &bars[0]);
-        }
-        if (!__syncthreads_and(mbar_wait(&bars[0], it & 1))) {
-            ok = false;
-            break;
-        }
-        if (tid == 0) {
-            tc_fence_after();
-#pragma unroll
-            for (int mt = 0; mt < NMT; ++mt)
-#pragma unroll
-                for (int s = 0; s < kBlockY / 2; ++s) {
-                    const uint64_t ad = sdesc(a_a + mt * 16 * kBoxBytes + s * 256, 128, kBoxBytes);
-                    const uint64_t bd = sdesc(b_a + s * 256, 128, kBoxBytes);
-                    mma_bf16(tmem + mt * 32, ad, bd, idesc, (it > 0 || s > 0) ? 1u : 0u);
+    const int mine = my_tiles(total);
+
+    if (warp == 0) {
+        if (lane == 0) {
+            int i = 0;
+            for (; i < mine; ++i) {
+                const int s = i & 1;
+                if (i >= 2 && !mbar_wait_abortable(&empty[s], ((i >> 1) - 1) & 1, abort)) break;
+                const int t = blockIdx.x + i * gridDim.x;
+                const int img = t / per_img, rem = t - img * per_img;
+                const int by = rem / a.tiles_x, bx = rem - by * a.tiles_x;
+                const int x0 = bx * kBlockX, y0 = by * kBlockY;
+                uint8_t *st = smem + s * STAGE;
+                mbar_expect_tx(&full[s], (NG + NGO) * kBoxBytes);
+                for (int g = 0; g < NG; ++g) {
+                    const int tap = g / NCG, cg = g - tap * NCG;
+                    const int dy = tap / 3, dx = tap - dy * 3;
+                    tma_load_4d(st + g * kBoxBytes, &xmap, cg * 8, x0 + dx, y0 + dy, img, &full[s]);
                 }
-            mma_commit(&bars[1]);
+#pragma unroll
+                for (int go = 0; go < NGO; ++go)
+                    tma_load_4d(st + ABYTES + go * kBoxBytes, &zmap, go * 8, x0 + 1, y0 + 1, img, &full[s]);
+            }
+            if (*abort)
+                for (int k = i > 2 ? i - 2 : 0; k < i; ++k) mbar_wait(&full[k & 1], (k >> 1) & 1);
         }
-        // bias (and level-embedding) gradient of this block from the staged dZ tile
-        {
+    } else if (warp == 1) {
+        if (lane == 0) {
+            constexpr uint32_t idesc = idesc_bf16(128, COUT, 1, 1);
+            int i = 0;
+            for (; i < mine; ++i) {
+                const int s = i & 1;
+                if (!mbar_wait_abortable(&full[s], (i >> 1) & 1, abort)) break;
+                tc_fence_after();
+                const uint32_t a_a = smem_u32(smem + s * STAGE), b_a = a_a + ABYTES;
+#pragma unroll
+                for (int mt = 0; mt < NMT; ++mt)
+#pragma unroll
+                    for (int k = 0; k < kBlockY / 2; ++k) {
+                        const uint64_t ad = sdesc(a_a + mt * 16 * kBoxBytes + k * 256, 128, kBoxBytes);
+                        const uint64_t bd = sdesc(b_a + k * 256, 128, kBoxBytes);
+                        mma_bf16(tmem + mt * 32, ad, bd, idesc, (i > 0 || k > 0) ? 1u : 0u);
+                    }
+                mma_commit(&empty[s]);
+            }
+            mma_commit(done);  // every MMA of this CTA
+            if (*abort && i > 0) mbar_wait(&empty[(i - 1) & 1], ((i - 1) >> 1) & 1);
+        }
+    } else {
+        const int bt = tid - 64, bn = bt % COUT;
+        const int q = warp & 3;
+        int i = 0;
+        for (; i < mine; ++i) {
+            const int s = i & 1;
+            if (!__all_sync(0xffffffffu, mbar_wait_abortable(&full[s], (i >> 1) & 1, abort))) break;
+            // bias (and level-embedding) gradient of this block from the staged dZ tile
+            const __nv_bfloat16 *bz = reinterpret_cast<const __nv_bfloat16 *>(smem + s * STAGE + ABYTES);
             float sum = 0.0f;
-            const __nv_bfloat16 *bz = reinterpret_cast<const __nv_bfloat16 *>(bsm);
-            for (int k = tid / COUT; k < kBlockX * kBlockY; k += kThreads / COUT)
+            for (int k = bt / COUT; k < kBlockX * kBlockY; k += 128 / COUT)
                 sum += __bfloat162float(bz[((bn >> 3) * kBoxBytes + (k >> 3) * 128 + (k & 7) * 16) / 2 + (bn & 7)]);
+            const int t = blockIdx.x + i * gridDim.x;
+            const int img = t / per_img;
             atomicAdd(a.gb + bn, sum);
             if (a.gemb) atomicAdd(a.gemb + (size_t)min(max(a.level[img], 0), kLevels - 1) * COUT + bn, sum);
+            mbar_arrive(&empty[s]);
         }
-        if (!__syncthreads_and(mbar_wait(&bars[1], it & 1))) {
-            ok = false;
-            break;
+        if (i == mine && mine > 0 && __all_sync(0xffffffffu, mbar_wait_abortable(done, 0, abort))) {
+            tc_fence_after();
+#pragma unroll
+            for (int mt = 0; mt < NMT; ++mt) {
+                float v[COUT];
+                const uint32_t taddr = tmem + mt * 32 + ((uint32_t)(q * 32) << 16);
+                if (COUT == 32)
+                    tmem_ld32(taddr, v);
+                else
+                    tmem_ld16(taddr, v);
+                const int m = mt * 128 + q * 32 + lane;
+                if (m < 9 * CIN)
+#pragma unroll
+                    for (int n = 0; n < COUT; ++n) atomicAdd(a.gw + (size_t)n * 9 * CIN + m, v[n]);
+            }
         }
     }
-    if (!ok && tid == 0) atomicExch(a.status, TP_E_TIMEOUT);
-    tc_fence_after();
-    if (ok && it > 0) {
-#pragma unroll
-        for (int mt = 0; mt < NMT; ++mt) {
-            float v[COUT];
-            const uint32_t taddr = tmem + mt * 32 + ((uint32_t)(warp * 32) << 16);
-            if (COUT == 32)
-                tmem_ld32(taddr, v);
-            else
-                tmem_ld16(taddr, v);
-            const int m = mt * 128 + warp * 32 + lane;
-            if (m < 9 * CIN)
-#pragma unroll
-                for (int n = 0; n < COUT; ++n) atomicAdd(a.gw + (size_t)n * 9 * CIN + m, v[n]);
-        }
-    }
-    tc_fence_before();
     __syncthreads();
+    if (tid == 0 && *abort) atomicExch(a.status, TP_E_TIMEOUT);
     tc_fence_after();
-    if (warp == 0) tmem_dealloc(tmem, TCOLS);
+    if (warp == 1) tmem_dealloc(tmem, TCOLS);
 }
 
 // ---------------------------------------------------------------- launch helpers
@@ -316,7 +397,7 @@ int grid_for(K kernel, int smem, int units, int *grid)
     cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (e != cudaSuccess) return tp::cuda_fail("cudaFuncSetAttribute (learned)", e);
     int per_sm = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kThreads, smem);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kRoleThreads, smem);
     if (e != cudaSuccess) return tp::cuda_fail("occupancy (learned)", e);
     if (per_sm < 1) return tp::fail(TP_E_BAD_ARG, "learned: kernel does not fit on an SM");
     *grid = std::max(1, std::min(units, per_sm * sm_count()));
@@ -332,7 +413,7 @@ int conv_instance(const ConvLaunch &a, const CUtensorMap *halo, cudaStream_t s)
     int grid = 0;
     int rc = grid_for(conv_kernel<CIN, COUT, MODE>, smem, units, &grid);
     if (rc) return rc;
-    conv_kernel<CIN, COUT, MODE><<<grid, kThreads, smem, s>>>(*halo, a);
+    conv_kernel<CIN, COUT, MODE><<<grid, kRoleThreads, smem, s>>>(*halo, a);
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? TP_OK : tp::cuda_fail("conv kernel launch", e);
 }
@@ -346,7 +427,7 @@ int wgrad_instance(const WgradLaunch &a, const CUtensorMap *xb, const CUtensorMa
     int grid = 0;
     int rc = grid_for(wgrad_kernel<CIN, COUT>, smem, units, &grid);
     if (rc) return rc;
-    wgrad_kernel<CIN, COUT><<<grid, kThreads, smem, s>>>(*xb, *zb, a);
+    wgrad_kernel<CIN, COUT><<<grid, kRoleThreads, smem, s>>>(*xb, *zb, a);
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? TP_OK : tp::cuda_fail("weight-gradient kernel launch", e);
 }
