@@ -17,6 +17,7 @@
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
+#include <map>
 #include <mutex>
 
 #include "tp_internal.h"
@@ -60,8 +61,12 @@ __device__ __forceinline__ uint32_t pack2(float a, float b)
     return *reinterpret_cast<uint32_t *>(&h);
 }
 
+// Activations are stored per 8-channel group: image `img` of C channels is C / 8
+// planes of (W + 2)^2 pixels of 16 bytes (one pixel's 8 channels), so that a TMA box
+// of one channel group reads whole 16-byte pixels of contiguous rows.  `plane` is
+// (W + 2)^2 and `pix` the pixel's index in its plane.
 template <int C>
-__device__ __forceinline__ void store_bf16(__nv_bfloat16 *dst, const float *v)
+__device__ __forceinline__ void store_bf16(__nv_bfloat16 *base, int img, size_t plane, size_t pix, const float *v)
 {
 #pragma unroll
     for (int q = 0; q < C / 8; ++q) {
@@ -70,16 +75,16 @@ __device__ __forceinline__ void store_bf16(__nv_bfloat16 *dst, const float *v)
         u.y = pack2(v[8 * q + 2], v[8 * q + 3]);
         u.z = pack2(v[8 * q + 4], v[8 * q + 5]);
         u.w = pack2(v[8 * q + 6], v[8 * q + 7]);
-        reinterpret_cast<uint4 *>(dst)[q] = u;
+        *reinterpret_cast<uint4 *>(base + (((size_t)img * (C / 8) + q) * plane + pix) * 8) = u;
     }
 }
 
 template <int C>
-__device__ __forceinline__ void load_bf16(const __nv_bfloat16 *src, float *v)
+__device__ __forceinline__ void load_bf16(const __nv_bfloat16 *base, int img, size_t plane, size_t pix, float *v)
 {
 #pragma unroll
     for (int q = 0; q < C / 8; ++q) {
-        uint4 u = reinterpret_cast<const uint4 *>(src)[q];
+        uint4 u = *reinterpret_cast<const uint4 *>(base + (((size_t)img * (C / 8) + q) * plane + pix) * 8);
         const __nv_bfloat162 *h = reinterpret_cast<const __nv_bfloat162 *>(&u);
 #pragma unroll
         for (int e = 0; e < 4; ++e) {
@@ -98,7 +103,7 @@ constexpr int kConvStages = 4;
 template <int CIN, int COUT>
 constexpr int conv_smem_bytes()
 {
-    return kConvStages * (CIN / 8) * kGroupStride + 9 * CIN * COUT * 2 + 128;
+    return kConvStages * (CIN / 8) * kGroupStride + 9 * CIN * COUT * 2 + 128 + COUT * 4;
 }
 
 // Tiles this CTA takes from a persistent loop over `total` tiles.
@@ -119,10 +124,12 @@ __global__ void __launch_bounds__(kRoleThreads) conv_kernel(const __grid_constan
     uint64_t *acc_empty = acc_full + 2;
     uint32_t *tslot = reinterpret_cast<uint32_t *>(acc_empty + 2);
     volatile int *abort = reinterpret_cast<volatile int *>(tslot + 1);
+    float *bias_s = reinterpret_cast<float *>(tslot + 4);  // 16-byte aligned, COUT floats
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 
     for (int i = tid; i < BBYTES / 16; i += kRoleThreads)
         reinterpret_cast<uint4 *>(bsm)[i] = reinterpret_cast<const uint4 *>(a.wpack)[i];
+    if (tid < COUT) bias_s[tid] = a.bias ? a.bias[tid] : 0.0f;
     if (tid == 0) {
         for (int s = 0; s < kConvStages; ++s) {
             mbar_init(&full[s], 1);
@@ -155,8 +162,8 @@ __global__ void __launch_bounds__(kRoleThreads) conv_kernel(const __grid_constan
                 mbar_expect_tx(&full[s], NCG * kHaloBytes);
 #pragma unroll
                 for (int cg = 0; cg < NCG; ++cg)
-                    tma_load_4d(halo + s * STAGE + cg * kGroupStride, &xmap, cg * 8, bx * kBlockX, by * kBlockY, img,
-                                &full[s]);
+                    tma_load_3d(halo + s * STAGE + cg * kGroupStride, &xmap, bx * kBlockX * 8, by * kBlockY,
+                                img * NCG + cg, &full[s]);
             }
             if (*abort)  // copies in flight land before the CTA leaves
                 for (int k = i > kConvStages ? i - kConvStages : 0; k < i; ++k)
@@ -208,23 +215,42 @@ __global__ void __launch_bounds__(kRoleThreads) conv_kernel(const __grid_constan
             const int m = q * 32 + lane;
             const int px = bx * kBlockX + (m & 7), py = by * kBlockY + (m >> 3);
             if (px < a.W && py < a.W) {
-                const size_t pix = ((size_t)img * Wp + (py + 1)) * Wp + (px + 1);
+                const size_t plane = (size_t)Wp * Wp, pix = (size_t)(py + 1) * Wp + (px + 1);
                 if (MODE == kHidden) {
-                    const float *e = a.emb ? a.emb + (size_t)min(max(a.level[img], 0), kLevels - 1) * COUT : nullptr;
+                    const float4 *b4 = reinterpret_cast<const float4 *>(bias_s);
+                    if (a.emb) {
+                        const float4 *e4 = reinterpret_cast<const float4 *>(
+                            a.emb + (size_t)min(max(a.level[img], 0), kLevels - 1) * COUT);
 #pragma unroll
-                    for (int j = 0; j < COUT; ++j) acc[j] += a.bias[j] + (e ? e[j] : 0.0f);
-                    if (a.zsave) store_bf16<COUT>(a.zsave + pix * COUT, acc);
+                        for (int j = 0; j < COUT / 4; ++j) {
+                            const float4 bb = b4[j], ee = __ldg(e4 + j);
+                            acc[4 * j] += bb.x + ee.x;
+                            acc[4 * j + 1] += bb.y + ee.y;
+                            acc[4 * j + 2] += bb.z + ee.z;
+                            acc[4 * j + 3] += bb.w + ee.w;
+                        }
+                    } else {
+#pragma unroll
+                        for (int j = 0; j < COUT / 4; ++j) {
+                            const float4 bb = b4[j];
+                            acc[4 * j] += bb.x;
+                            acc[4 * j + 1] += bb.y;
+                            acc[4 * j + 2] += bb.z;
+                            acc[4 * j + 3] += bb.w;
+                        }
+                    }
+                    if (a.zsave) store_bf16<COUT>(a.zsave, img, plane, pix, acc);
 #pragma unroll
                     for (int j = 0; j < COUT; ++j) acc[j] = gelu(acc[j]);
-                    store_bf16<COUT>(a.out + pix * COUT, acc);
+                    store_bf16<COUT>(a.out, img, plane, pix, acc);
                 } else if (MODE == kLast) {
-                    a.out_f32[((size_t)img * a.W + py) * a.W + px] = acc[0] + a.bias[0];
+                    a.out_f32[((size_t)img * a.W + py) * a.W + px] = acc[0] + bias_s[0];
                 } else {
                     float z[COUT];
-                    load_bf16<COUT>(a.zprev + pix * COUT, z);
+                    load_bf16<COUT>(a.zprev, img, plane, pix, z);
 #pragma unroll
                     for (int j = 0; j < COUT; ++j) acc[j] *= gelu_grad(z[j]);
-                    store_bf16<COUT>(a.out + pix * COUT, acc);
+                    store_bf16<COUT>(a.out, img, plane, pix, acc);
                 }
             }
         }
@@ -304,11 +330,11 @@ __global__ void __launch_bounds__(kRoleThreads) wgrad_kernel(const __grid_consta
                 for (int g = 0; g < NG; ++g) {
                     const int tap = g / NCG, cg = g - tap * NCG;
                     const int dy = tap / 3, dx = tap - dy * 3;
-                    tma_load_4d(st + g * kBoxBytes, &xmap, cg * 8, x0 + dx, y0 + dy, img, &full[s]);
+                    tma_load_3d(st + g * kBoxBytes, &xmap, (x0 + dx) * 8, y0 + dy, img * NCG + cg, &full[s]);
                 }
 #pragma unroll
                 for (int go = 0; go < NGO; ++go)
-                    tma_load_4d(st + ABYTES + go * kBoxBytes, &zmap, go * 8, x0 + 1, y0 + 1, img, &full[s]);
+                    tma_load_3d(st + ABYTES + go * kBoxBytes, &zmap, (x0 + 1) * 8, y0 + 1, img * NGO + go, &full[s]);
             }
             if (*abort)
                 for (int k = i > 2 ? i - 2 : 0; k < i; ++k) mbar_wait(&full[k & 1], (k >> 1) & 1);
@@ -389,17 +415,41 @@ int sm_count()
     return n;
 }
 
+// CTAs of `kernel` resident on one SM, from its shared memory, registers, threads
+// and tensor-memory columns.  The runtime's occupancy query assumes one CTA per SM
+// for kernels that allocate tensor memory; on GB300 several run together as long
+// as their columns fit in the SM's 512.  An overestimate only queues CTAs (they
+// never wait on one another).
 template <typename K>
-int grid_for(K kernel, int smem, int units, int *grid)
+int grid_for(K kernel, int smem, int tmem_cols, int units, int *grid)
 {
     static std::mutex mu;
+    static std::map<const void *, int> cache;  // per kernel instance
     std::lock_guard<std::mutex> lk(mu);
-    cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    if (e != cudaSuccess) return tp::cuda_fail("cudaFuncSetAttribute (learned)", e);
-    int per_sm = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kRoleThreads, smem);
-    if (e != cudaSuccess) return tp::cuda_fail("occupancy (learned)", e);
-    if (per_sm < 1) return tp::fail(TP_E_BAD_ARG, "learned: kernel does not fit on an SM");
+    int &per_sm = cache[reinterpret_cast<const void *>(kernel)];
+    if (!per_sm) {
+        cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
+        if (e != cudaSuccess) return tp::cuda_fail("cudaFuncSetAttribute (learned)", e);
+        cudaFuncAttributes fa;
+        e = cudaFuncGetAttributes(&fa, kernel);
+        if (e != cudaSuccess) return tp::cuda_fail("cudaFuncGetAttributes (learned)", e);
+        int dev = 0, smem_sm = 0, regs_sm = 0, reserved = 0, threads_sm = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+        cudaDeviceGetAttribute(&regs_sm, cudaDevAttrMaxRegistersPerMultiprocessor, dev);
+        cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev);
+        cudaDeviceGetAttribute(&threads_sm, cudaDevAttrMaxThreadsPerMultiProcessor, dev);
+        const int warps = (kRoleThreads + 31) / 32;
+        const int regs_warp = (fa.numRegs * 32 + 255) / 256 * 256;
+        int n = smem_sm / (smem + (int)fa.sharedSizeBytes + reserved);
+        n = std::min(n, regs_sm / std::max(1, regs_warp * warps));
+        n = std::min(n, threads_sm / kRoleThreads);
+        n = std::min(n, 512 / tmem_cols);
+        if (n < 1) return tp::fail(TP_E_BAD_ARG, "learned: kernel does not fit on an SM");
+        per_sm = n;
+    }
     *grid = std::max(1, std::min(units, per_sm * sm_count()));
     return TP_OK;
 }
@@ -411,7 +461,7 @@ int conv_instance(const ConvLaunch &a, const CUtensorMap *halo, cudaStream_t s)
     if (units <= 0) return TP_OK;
     constexpr int smem = conv_smem_bytes<CIN, COUT>();
     int grid = 0;
-    int rc = grid_for(conv_kernel<CIN, COUT, MODE>, smem, units, &grid);
+    int rc = grid_for(conv_kernel<CIN, COUT, MODE>, smem, 64, units, &grid);
     if (rc) return rc;
     conv_kernel<CIN, COUT, MODE><<<grid, kRoleThreads, smem, s>>>(*halo, a);
     cudaError_t e = cudaGetLastError();
@@ -425,7 +475,8 @@ int wgrad_instance(const WgradLaunch &a, const CUtensorMap *xb, const CUtensorMa
     if (units <= 0) return TP_OK;
     constexpr int smem = wgrad_smem_bytes<CIN, COUT>();
     int grid = 0;
-    int rc = grid_for(wgrad_kernel<CIN, COUT>, smem, units, &grid);
+    constexpr int NMT = wgrad_tiles<CIN, COUT>();
+    int rc = grid_for(wgrad_kernel<CIN, COUT>, smem, NMT * 32 <= 32 ? 32 : (NMT * 32 <= 64 ? 64 : 128), units, &grid);
     if (rc) return rc;
     wgrad_kernel<CIN, COUT><<<grid, kRoleThreads, smem, s>>>(*xb, *zb, a);
     cudaError_t e = cudaGetLastError();
@@ -471,7 +522,7 @@ __global__ void prep_kernel(const float *up, const int *level, const float *sigm
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
         const int y = i / W, x = i - y * W;
         float v[16] = {(u[i] - mean) * inv, (float)(x & 1), (float)(y & 1), 1.0f};
-        store_bf16<16>(x0 + (((size_t)img * Wp + y + 1) * Wp + x + 1) * 16, v);
+        store_bf16<16>(x0, img, (size_t)Wp * Wp, (size_t)(y + 1) * Wp + x + 1, v);
     }
 }
 
@@ -488,7 +539,7 @@ __global__ void loss_kernel(const float *pred, const float *target, const int *l
         d2 = d * d;
         float v[16] = {2.0f * d * scale};
         const int Wp = W + 2;
-        store_bf16<16>(dz + (((size_t)img * Wp + y + 1) * Wp + x + 1) * 16, v);
+        store_bf16<16>(dz, img, (size_t)Wp * Wp, (size_t)(y + 1) * Wp + x + 1, v);
     }
     for (int o = 16; o > 0; o >>= 1) d2 += __shfl_xor_sync(0xffffffffu, d2, o);
     if ((threadIdx.x & 31) == 0) atomicAdd(loss, d2);

@@ -86,23 +86,25 @@ int encode_tensor_map(const tp_storage *s, int box_x, int box_y, CUtensorMap *ou
 namespace tp {
 namespace learned {
 
-// NHWC bf16 activations of `nimg` images of (W+2)^2 pixels seen as a 4D tensor
-// (channel, x, y, image); boxes of 8 channels x box_x x box_y pixels; reads
+// bf16 activations of `nimg` images of (W+2)^2 pixels, stored as channels / 8
+// planes per image of 16-byte pixels (8 channels), seen as a 3D tensor (x and
+// channel merged: (W+2) x 8 elements per row, y, image x group); boxes of box_x
+// whole pixels (box_x x 16 contiguous bytes) x box_y rows of one plane; reads
 // outside the tensor return zeros.
 int encode_act_map(void *base, int W, int channels, int nimg, int box_x, int box_y, CUtensorMap *out)
 {
-    if (channels % 8 != 0 || box_x < 1 || box_x > 256 || box_y < 1 || box_y > 256 || nimg < 1)
+    if (channels % 8 != 0 || box_x < 1 || box_x > 32 || box_y < 1 || box_y > 256 || nimg < 1)
         return fail(TP_E_BAD_ARG, "activation tensor map: bad shape");
     int err = TP_OK;
     auto fn = encode_fn(&err);
     if (!fn) return err;
     std::memset(out, 0, sizeof *out);
     const cuuint64_t Wp = (cuuint64_t)W + 2;
-    cuuint64_t dims[4] = {(cuuint64_t)channels, Wp, Wp, (cuuint64_t)nimg};
-    cuuint64_t strides[3] = {(cuuint64_t)channels * 2, Wp * channels * 2, Wp * Wp * channels * 2};
-    cuuint32_t box[4] = {8, (cuuint32_t)box_x, (cuuint32_t)box_y, 1};
-    cuuint32_t estr[4] = {1, 1, 1, 1};
-    CUresult r = fn(out, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, base, dims, strides, box, estr,
+    cuuint64_t dims[3] = {Wp * 8, Wp, (cuuint64_t)nimg * (channels / 8)};
+    cuuint64_t strides[2] = {Wp * 16, Wp * Wp * 16};
+    cuuint32_t box[3] = {(cuuint32_t)box_x * 8, (cuuint32_t)box_y, 1};
+    cuuint32_t estr[3] = {1, 1, 1};
+    CUresult r = fn(out, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, base, dims, strides, box, estr,
                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) return fail(TP_E_CUDA, "cuTensorMapEncodeTiled failed (activations)");
