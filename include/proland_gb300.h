@@ -126,6 +126,16 @@ int tp_elevation_batch_device(tp_storage *elev, tp_storage *residuals, tp_storag
  * NormalProducer.cpp:215-273; terrain2/normalShader.glsl); 0: flat. */
 int tp_normal_batch(tp_storage *elev, tp_storage *normals, const tp_tile_job *jobs, int n, double root_quad_size,
                     void *stream);
+/* The same in any of the reference's normal formats (NormalProducer.cpp:195;
+ * demo normalShader.glsl:93-124): 0 = (nf, nc) signed, 1 = (nf, nc) as 8-bit
+ * unsigned (stored as k / 255), 2 = nf signed, 3 = nf as 8-bit unsigned; formats
+ * 0 and 1 need 4-channel normal slots, their coarse normals nc average the parent
+ * normal tile (parent_normal_slots[k], or nc = nf when NULL or -1) at the
+ * coarse-mesh vertices of grid_mesh (gridMeshSize, 24 in the examples).  Jobs are
+ * produced level by level, parents first. */
+int tp_normal_batch_format(tp_storage *elev, tp_storage *normals, const tp_tile_job *jobs, int n,
+                           double root_quad_size, int format, const int *parent_normal_slots, int grid_mesh,
+                           void *stream);
 /* Same as tp_elevation_batch, allocating nothing.  (No counterpart in the
  * reference: its producers draw on GL textures created up front.)  For callers
  * that may not allocate while producing tiles: the kernel's scratch (work
@@ -220,6 +230,9 @@ int tp_residual_producer_set_source(tp_producer *p, tp_residual_source fn, void 
 int tp_elevation_producer_create(tp_cache *cache, tp_producer *residuals, const float *noise_amp, int n_noise,
                                  const tp_elev_params *params, int face, tp_producer **out);
 int tp_normal_producer_create(tp_cache *cache, tp_producer *elevations, int deform, tp_producer **out);
+/* A normal producer's output format (0-3 as tp_normal_batch_format; a 4-channel
+ * storage starts at 0, a 2-channel one at 2) and the coarse mesh size. */
+int tp_normal_producer_set_format(tp_producer *p, int format, int grid_mesh);
 int tp_producer_destroy(tp_producer *p);
 int tp_producer_id(const tp_producer *p);
 int tp_producer_border(const tp_producer *p);                                  /* getBorder */

@@ -81,6 +81,10 @@ def lib():
                                           C.POINTER(C.c_int16), _f32p]
         L.or_normals_sphere_f64.argtypes = [C.c_int, _f64p, C.c_int, C.c_double, C.c_int, C.c_int, C.c_int,
                                             _f64p, _f64p, C.c_int]
+        L.or_parent_to_tangent.argtypes = [C.c_double, C.c_int, C.c_int, C.c_int, _f32p]
+        L.or_normals_full.argtypes = [C.c_int, _f32p, C.c_int, C.c_float, C.POINTER(SphereFrame), _f32p, C.c_int,
+                                      C.c_int, C.c_int, C.c_int, _f32p, _f32p, C.c_int, _f32p, _f32p, _f32p, _f32p,
+                                      C.c_int]
         _i16p = C.POINTER(C.c_int16)
         L.or_fbm_heights.argtypes = [C.c_int, C.c_int, C.c_int, C.c_float, C.c_float, C.c_uint32, _i16p]
         L.or_level_tile.argtypes = [_i16p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_float, _f32p]
@@ -219,6 +223,27 @@ def normals_sphere_f64(W, zm, root_quad_size, level, tx, ty):
     lib().or_normals_sphere_f64(W, _p(zm, _f64p), zm.shape[1], float(root_quad_size), level, tx, ty,
                                 _p(nx, _f64p), _p(ny, _f64p), n1)
     return nx, ny
+
+
+def parent_to_tangent(root_quad_size, level, tx, ty):
+    out = np.empty(9, np.float32)
+    lib().or_parent_to_tangent(float(root_quad_size), level, tx, ty, _p(out))
+    return out
+
+
+def normals_full(W, zm, tile_meters, fmt, tx, ty, parent=None, root_quad_size=0.0, level=0, grid_mesh=24):
+    """Normal tile planes of format `fmt` (4 planes for 0/1, 2 for 2/3); `parent`:
+    the parent normal tile's first two planes (nx, ny) or None."""
+    zm = _f32(zm)
+    Wn = W - 4
+    outs = [np.zeros((Wn, Wn), np.float32) for _ in range(4)]
+    frame = sphere_frame(root_quad_size, level, tx, ty) if root_quad_size > 0 else None
+    p2t = parent_to_tangent(root_quad_size, level, tx, ty) if (root_quad_size > 0 and level > 0) else None
+    pnx = _f32(parent[0]) if parent is not None else None
+    pny = _f32(parent[1]) if parent is not None else None
+    lib().or_normals_full(W, _p(zm), zm.shape[1], float(tile_meters), C.byref(frame) if frame else None, _p(p2t),
+                          fmt, grid_mesh, tx, ty, _p(pnx), _p(pny), Wn, *[_p(o) for o in outs], Wn)
+    return outs[:4] if fmt in (0, 1) else outs[:2]
 
 
 def compute_residual(W, tx, ty, parent_approx, fine):

@@ -601,6 +601,102 @@ void or_normals_sphere(int W, const float *zm, int zm_pitch, const or_sphere_fra
         }
 }
 
+/* parentToTangentFrame (NormalProducer.cpp:256-270): the child's world-to-tangent
+ * frame times the parent tile centre's tangent-to-world frame, row-major. */
+void or_parent_to_tangent(double D, int level, int tx, int ty, float *p2t)
+{
+    double R = D / 2.0, sc = (double)(1 << level);
+    double x0 = (double)tx / sc * D - R, x1 = (double)(tx + 1) / sc * D - R;
+    double y0 = (double)ty / sc * D - R, y1 = (double)(ty + 1) / sc * D - R;
+    double pc[3] = {(x0 + x1) * 0.5, (y0 + y1) * 0.5, R}, w[3][3], t[3][3];
+    double uz[3], ux[3], uy[3];
+    for (int pass = 0; pass < 2; ++pass) {
+        if (pass == 1) {
+            double ps = (double)(1 << (level - 1));
+            pc[0] = ((double)(tx / 2) + 0.5) / ps * D - R;
+            pc[1] = ((double)(ty / 2) + 0.5) / ps * D - R;
+            pc[2] = R;
+        }
+        v3_norm(pc, uz, NULL);
+        double a[3] = {uz[2], 0.0, -uz[0]};
+        v3_norm(a, ux, NULL);
+        uy[0] = uz[1] * ux[2] - uz[2] * ux[1];
+        uy[1] = uz[2] * ux[0] - uz[0] * ux[2];
+        uy[2] = uz[0] * ux[1] - uz[1] * ux[0];
+        for (int c = 0; c < 3; ++c) {
+            if (pass == 0) { w[0][c] = ux[c]; w[1][c] = uy[c]; w[2][c] = uz[c]; }
+            else { t[c][0] = ux[c]; t[c][1] = uy[c]; t[c][2] = uz[c]; }
+        }
+    }
+    for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 3; ++c) p2t[r * 3 + c] = (float)(w[r][0] * t[0][c] + w[r][1] * t[1][c] + w[r][2] * t[2][c]);
+}
+
+static float unorm8(float v)
+{
+    v = v < 0.0f ? 0.0f : (v > 1.0f ? 1.0f : v);
+    return floorf(v * 255.0f + 0.5f) / 255.0f;
+}
+
+/* NormalProducer::doCreateTile in its four output formats (demo
+ * normalShader.glsl:93-124): nf from the finite differences of zm (flat, or on the
+ * sphere frame f); nc, for formats 0 and 1 above level 0, the mean of the parent
+ * normal tile's nf at the two nearest coarse-mesh vertices
+ * g floor(ij / 2g + (1/2, 0)) and g floor(ij / 2g + (0, 1/2)), g = (Wn - 1) / gridMeshSize,
+ * in the parent's quadrant (tx % 2, ty % 2) x (Wn - 1) / 2 (point sampled),
+ * decoded from unsigned for format 1 and rotated by parentToTangentFrame (p2t)
+ * on a sphere; otherwise nc = nf.  Formats 1 and 3 are 8-bit unsigned textures:
+ * their values are stored as k / 255.  pnx/pny: the parent's first two planes. */
+void or_normals_full(int W, const float *zm, int zm_pitch, float tile_meters, const or_sphere_frame *f,
+                     const float *p2t, int format, int grid_mesh, int tx, int ty, const float *pnx, const float *pny,
+                     int ppitch, float *o0, float *o1, float *o2, float *o3, int out_pitch)
+{
+    const int Wn = W - 4, n = W - 5;
+    float *nfx = (float *)malloc(sizeof(float) * Wn * Wn), *nfy = (float *)malloc(sizeof(float) * Wn * Wn);
+    if (f)
+        or_normals_sphere(W, zm, zm_pitch, f, nfx, nfy, Wn);
+    else
+        or_normals_flat(W, zm, zm_pitch, tile_meters, 2, nfx, nfy, Wn);
+    const int g = (Wn - 1) / grid_mesh;
+    const int dxi = (tx % 2) * ((Wn - 1) / 2), dyi = (ty % 2) * ((Wn - 1) / 2);
+    const int coarse = (format == 0 || format == 1) && pnx && pny;
+    for (int q = 0; q <= n; ++q)
+        for (int p = 0; p <= n; ++p) {
+            const size_t k = p + (size_t)q * Wn, o = p + (size_t)q * out_pitch;
+            float vx = nfx[k], vy = nfy[k], cx = vx, cy = vy;
+            if (coarse) {
+                const int ax = g * ((p + g) / (2 * g)) + dxi, ay = g * (q / (2 * g)) + dyi;
+                const int bx = g * (p / (2 * g)) + dxi, by = g * ((q + g) / (2 * g)) + dyi;
+                cx = (pnx[ax + (size_t)ay * ppitch] + pnx[bx + (size_t)by * ppitch]) * 0.5f;
+                cy = (pny[ax + (size_t)ay * ppitch] + pny[bx + (size_t)by * ppitch]) * 0.5f;
+                if (format == 1) {
+                    cx = cx * 2.0f - 1.0f;
+                    cy = cy * 2.0f - 1.0f;
+                }
+                if (f && p2t) {
+                    float cz2 = 1.0f - (cx * cx + cy * cy);
+                    const float cz = sqrtf(cz2 > 0.0f ? cz2 : 0.0f);
+                    const float rx = p2t[0] * cx + p2t[1] * cy + p2t[2] * cz;
+                    const float ry = p2t[3] * cx + p2t[4] * cy + p2t[5] * cz;
+                    cx = rx;
+                    cy = ry;
+                }
+            }
+            if (format == 0) {
+                o0[o] = vx; o1[o] = vy; o2[o] = cx; o3[o] = cy;
+            } else if (format == 1) {
+                o0[o] = unorm8(vx * 0.5f + 0.5f); o1[o] = unorm8(vy * 0.5f + 0.5f);
+                o2[o] = unorm8(cx * 0.5f + 0.5f); o3[o] = unorm8(cy * 0.5f + 0.5f);
+            } else if (format == 2) {
+                o0[o] = vx; o1[o] = vy;
+            } else {
+                o0[o] = unorm8(vx * 0.5f + 0.5f); o1[o] = unorm8(vy * 0.5f + 0.5f);
+            }
+        }
+    free(nfx);
+    free(nfy);
+}
+
 /* FP64 twin of or_sphere_frame_make + or_normals_sphere: the frame and the
  * positions in double, from double heights (the FP64 evaluation the errors of
  * the float path are stated against). */

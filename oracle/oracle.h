@@ -119,6 +119,11 @@ void or_residual_upsample(int n, int tilesize, int tx, int ty, const float *pare
 void or_normals_sphere_f64(int W, const double *zm, int zm_pitch, double D, int level, int tx, int ty,
                            double *nx, double *ny, int out_pitch);
 
+void or_parent_to_tangent(double D, int level, int tx, int ty, float *p2t);
+void or_normals_full(int W, const float *zm, int zm_pitch, float tile_meters, const or_sphere_frame *f,
+                     const float *p2t, int format, int grid_mesh, int tx, int ty, const float *pnx, const float *pny,
+                     int ppitch, float *o0, float *o1, float *o2, float *o3, int out_pitch);
+
 /* ---- learned.c: device preprocess height field, level tiles, learned net ---- */
 void or_fbm_heights(int size, int octaves, int base_cells, float amplitude, float quantum, uint32_t seed, int16_t *out);
 void or_level_tile(const int16_t *base, int ts, int max_level, int level, int tx, int ty, float scale, float *out);

@@ -86,6 +86,8 @@ struct tp_producer {
     // normal producer
     tp_producer *elevations = nullptr;
     int deform = 0;
+    int normal_format = 2;  // 0..3 (NormalProducer.cpp:195); 0/1 add coarse normals
+    int grid_mesh = 24;
 };
 
 namespace {
@@ -441,12 +443,27 @@ extern "C" int tp_normal_producer_create(tp_cache *cache, tp_producer *elevation
 {
     if (!cache || !elevations || !out || elevations->kind != kElevation)
         return tp::fail(TP_E_BAD_ARG, "tp_normal_producer_create: bad arguments");
-    if (cache->storage->channels != 2 || cache->storage->W != elevations->cache->storage->W - 4)
-        return tp::fail(TP_E_BAD_ARG, "normal cache must have 2-channel slots of width W - 4");
+    if ((cache->storage->channels != 2 && cache->storage->channels != 4) ||
+        cache->storage->W != elevations->cache->storage->W - 4)
+        return tp::fail(TP_E_BAD_ARG, "normal cache must have 2- or 4-channel slots of width W - 4");
     tp_producer *p = new_producer(kNormal, cache);
     p->elevations = elevations;
     p->deform = deform;
+    // as the reference picks the format from the storage (NormalProducer.cpp:195): 4 signed
+    // components carry the coarse normals too
+    p->normal_format = cache->storage->channels == 4 ? 0 : 2;
     *out = p;
+    return TP_OK;
+}
+
+extern "C" int tp_normal_producer_set_format(tp_producer *p, int format, int grid_mesh)
+{
+    if (!p || p->kind != kNormal || format < 0 || format > 3 || grid_mesh < 1)
+        return tp::fail(TP_E_BAD_ARG, "tp_normal_producer_set_format: bad arguments");
+    if (p->cache->storage->channels < (format <= 1 ? 4 : 2))
+        return tp::fail(TP_E_BAD_ARG, "tp_normal_producer_set_format: formats 0 and 1 need a 4-channel storage");
+    p->normal_format = format;
+    p->grid_mesh = grid_mesh;
     return TP_OK;
 }
 
@@ -624,7 +641,7 @@ int run_elevations(tp_producer *e, tp_producer *normals, void *stream)
     // normal tiles whose elevation tile is produced by this same launch are fused in
     // (flat deformation; spherical normals run in their own kernel afterwards)
     std::map<const tp_tile *, tp_tile *> fused;  // elevation tile -> normal tile
-    if (normals && !normals->deform)
+    if (normals && !normals->deform && normals->normal_format == 2)
         for (tp_tile *nt : normals->queue)
             if (nt->dep_input && nt->dep_input->queued) fused[nt->dep_input] = nt;
     if (e->queue.empty()) return TP_OK;
@@ -697,11 +714,57 @@ int run_elevations(tp_producer *e, tp_producer *normals, void *stream)
     return TP_OK;
 }
 
+// Normal tiles in a format other than 2 (coarse normals from the parent normal
+// tile): one launch per level, parents first.
+int run_normals_format(tp_producer *np, void *stream)
+{
+    tp_producer *e = np->elevations;
+    std::vector<tp_tile *> q = np->queue;
+    std::stable_sort(q.begin(), q.end(), [](const tp_tile *a, const tp_tile *b) { return a->level < b->level; });
+    size_t k = 0;
+    while (k < q.size()) {
+        const int level = q[k]->level;
+        std::vector<int> eslot, nslot, pslot, txs, tys;
+        std::vector<float> meters, p2t;
+        std::vector<tp::SphereFrame> frames;
+        for (; k < q.size() && q[k]->level == level; ++k) {
+            tp_tile *t = q[k];
+            if (!t->dep_input || !t->dep_input->done)
+                return tp::fail(TP_E_MISSING_PARENT, "normal tile's elevation is not produced");
+            eslot.push_back(t->dep_input->slot);
+            nslot.push_back(t->slot);
+            pslot.push_back(t->dep_parent ? t->dep_parent->slot : -1);
+            txs.push_back(t->tx);
+            tys.push_back(t->ty);
+            meters.push_back(e->root_quad_size / (float)(1u << t->level));
+            if (np->deform) {
+                frames.emplace_back();
+                tp::sphere_frame(e->root_quad_size, t->level, t->tx, t->ty, &frames.back());
+                p2t.resize(p2t.size() + 9, 0.0f);
+                if (t->level > 0) tp::parent_to_tangent(e->root_quad_size, t->level, t->tx, t->ty, &p2t[p2t.size() - 9]);
+            }
+        }
+        int rc = tp::launch_normals_format(e->cache->storage, np->cache->storage, eslot.data(), nslot.data(),
+                                           meters.data(), pslot.data(), txs.data(), tys.data(), (int)eslot.size(),
+                                           np->normal_format, np->grid_mesh, stream,
+                                           np->deform ? frames.data() : nullptr, np->deform ? p2t.data() : nullptr);
+        if (rc) return rc;
+    }
+    for (tp_tile *t : np->queue) {
+        t->done = true;
+        t->queued = false;
+        release_deps(t);
+    }
+    np->queue.clear();
+    return TP_OK;
+}
+
 int run_normals(tp_producer *np, void *stream)
 {
     if (np->queue.empty()) return TP_OK;
     tp_producer *e = np->elevations;
     if (!(e->root_quad_size > 0.0f)) return tp::fail(TP_E_BAD_ARG, "normal producer: root quad size not set");
+    if (np->normal_format != 2) return run_normals_format(np, stream);
     std::vector<int> eslot, nslot;
     std::vector<float> meters;
     std::vector<tp::SphereFrame> frames;
@@ -773,6 +836,33 @@ extern "C" int tp_scheduler_run(tp_producer *const *producers, int n, void *stre
 }
 
 namespace tp {
+
+// parentToTangentFrame (NormalProducer.cpp:256-270): the tile's world-to-tangent frame
+// times the tangent-to-world frame at its parent's centre, in FP64, row-major floats.
+void parent_to_tangent(double D, int level, int tx, int ty, float *p2t)
+{
+    auto frame = [&](double cx, double cy, double m[3][3]) {
+        const double R = D / 2.0;
+        const double l = std::sqrt(cx * cx + cy * cy + R * R);
+        const double uz[3] = {cx / l, cy / l, R / l};
+        const double a[3] = {uz[2], 0.0, -uz[0]};  // (0, 1, 0) x uz
+        const double la = std::sqrt(a[0] * a[0] + a[1] * a[1] + a[2] * a[2]);
+        const double ux[3] = {a[0] / la, a[1] / la, a[2] / la};
+        const double uy[3] = {uz[1] * ux[2] - uz[2] * ux[1], uz[2] * ux[0] - uz[0] * ux[2], uz[0] * ux[1] - uz[1] * ux[0]};
+        for (int c = 0; c < 3; ++c) {
+            m[0][c] = ux[c];
+            m[1][c] = uy[c];
+            m[2][c] = uz[c];
+        }
+    };
+    const double R = D / 2.0, s = (double)(1u << level), ps = (double)(1u << (level > 0 ? level - 1 : 0));
+    double w[3][3], t[3][3];
+    frame(((double)tx + 0.5) / s * D - R, ((double)ty + 0.5) / s * D - R, w);
+    frame(((double)(tx / 2) + 0.5) / ps * D - R, ((double)(ty / 2) + 0.5) / ps * D - R, t);
+    for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 3; ++c)  // w * t^T: t's rows are the parent's tangent axes
+            p2t[r * 3 + c] = (float)(w[r][0] * t[c][0] + w[r][1] * t[c][1] + w[r][2] * t[c][2]);
+}
 
 // NormalProducer.cpp:215-273: the tile's corners on the sphere of radius
 // R = D / 2 (D the root quad size) centred below the face, their unit verticals and

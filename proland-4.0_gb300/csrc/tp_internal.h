@@ -134,6 +134,13 @@ void sphere_frame(double root_quad_size, int level, int tx, int ty, SphereFrame 
 // Normal tiles from produced elevation tiles (flat, or spherical with one frame per tile).
 int launch_normals(tp_storage *elev, tp_storage *nrm, const int *eslots, const int *nslots, const float *meters,
                    int count, void *stream, const SphereFrame *frames = nullptr);
+// Normal tiles in format 0-3 (4 channels for 0/1), coarse normals from parent normal
+// slots (pslots, -1 for none), spherical frames and parent-to-tangent rotations (9
+// floats per job, row-major) when given.  No job may be another's parent.
+int launch_normals_format(tp_storage *elev, tp_storage *nrm, const int *eslots, const int *nslots, const float *meters,
+                          const int *pslots, const int *txs, const int *tys, int count, int format, int grid_mesh,
+                          void *stream, const SphereFrame *frames, const float *p2t);
+void parent_to_tangent(double root_quad_size, int level, int tx, int ty, float *p2t);
 // Residual pyramid files.
 int dat_tile_width(const tp_dat *d, int level);
 int dat_tile_id(const tp_dat *d, int level, int tx, int ty);

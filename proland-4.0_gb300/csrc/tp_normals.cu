@@ -5,6 +5,7 @@
 // tiles of a spherically deformed terrain (terrain/examples/terrain2/normalShader.glsl).
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <mutex>
 #include <vector>
 
@@ -15,8 +16,20 @@ namespace {
 struct NormalJob {
     int eslot, nslot;
     float tile_meters;
-    int frame;  // index of the job's spherical frame, -1 for flat deformation
+    int frame;   // index of the job's spherical frame, -1 for flat deformation
+    int pslot;   // parent normal slot for the coarse normals (formats 0/1), -1 for none
+    int tx, ty;
+    int pad;
 };
+
+// Normals in the reference's four formats (demo normalShader.glsl:116-124): 0 = nf, nc
+// signed; 1 = the same as 8-bit unsigned (stored as k / 255); 2 = nf signed; 3 = nf
+// as 8-bit unsigned.
+__device__ __forceinline__ float unorm8(float v)
+{
+    v = fminf(fmaxf(v, 0.0f), 1.0f);
+    return floorf(__fadd_rn(__fmul_rn(v, 255.0f), 0.5f)) / 255.0f;
+}
 
 // Each operation of the spherical path is rounded on its own (no fused
 // multiply-add), in the order the shader writes it: the positions are ~R = 6.4e6
@@ -136,9 +149,157 @@ __global__ void __launch_bounds__(256) normals_kernel(const float *__restrict__ 
     }
 }
 
+// All formats: nf as in the kernel above (flat finite differences or the sphere),
+// then nc from the parent normal tile (formats 0/1 above level 0) and the format's
+// encoding.  One CTA per tile.
+__global__ void __launch_bounds__(256) normals_format_kernel(
+    const float *__restrict__ elev, int pitch, long long eplane, long long eslot_stride, float *__restrict__ nrm,
+    int npitch, long long nplane, long long nslot_stride, const NormalJob *__restrict__ jobs,
+    const tp::SphereFrame *__restrict__ frames, const float *__restrict__ p2t, int W, int format, int g)
+{
+    const NormalJob J = jobs[blockIdx.x];
+    __shared__ tp::SphereFrame F;
+    __shared__ float R[9];
+    if (threadIdx.x == 0 && J.frame >= 0) F = frames[J.frame];
+    if (threadIdx.x < 9) R[threadIdx.x] = (J.frame >= 0 && p2t) ? p2t[9 * blockIdx.x + threadIdx.x] : 0.0f;
+    __syncthreads();
+    const float *zm = elev + (long long)J.eslot * eslot_stride + 2 * eplane;
+    float *o = nrm + (long long)J.nslot * nslot_stride;
+    const float *par = J.pslot >= 0 ? nrm + (long long)J.pslot * nslot_stride : nullptr;
+    const int Wn = W - 4, n = W - 5;
+    const int dxi = (J.tx & 1) * ((Wn - 1) / 2), dyi = (J.ty & 1) * ((Wn - 1) / 2);
+    const bool coarse = (format == 0 || format == 1) && par;
+    const float h2 = __fmul_rn(2.0f, __fdiv_rn(J.tile_meters, (float)n));
+    const float hh = h2 * h2;
+    const float nn = (float)n;
+    for (int idx = threadIdx.x; idx < Wn * Wn; idx += blockDim.x) {
+        const int q = idx / Wn, p = idx - q * Wn;
+        const float *c = zm + (long long)(q + 2) * pitch + (p + 2);
+        float vx, vy;
+        if (J.frame >= 0) {
+            float p0[3], p1[3], p2[3], p3[3];
+            sphere_pos(F, nn, (float)(p - 1), (float)q, __ldg(c - 1), p0);
+            sphere_pos(F, nn, (float)(p + 1), (float)q, __ldg(c + 1), p1);
+            sphere_pos(F, nn, (float)p, (float)(q - 1), __ldg(c - pitch), p2);
+            sphere_pos(F, nn, (float)p, (float)(q + 1), __ldg(c + pitch), p3);
+            const float a[3] = {s_(p1[0], p0[0]), s_(p1[1], p0[1]), s_(p1[2], p0[2])};
+            const float b[3] = {s_(p3[0], p2[0]), s_(p3[1], p2[1]), s_(p3[2], p2[2])};
+            float cr[3] = {s_(m_(a[1], b[2]), m_(a[2], b[1])), s_(m_(a[2], b[0]), m_(a[0], b[2])),
+                           s_(m_(a[0], b[1]), m_(a[1], b[0]))};
+            const float inv = __fdiv_rn(1.0f, __fsqrt_rn(dot3(cr, cr)));
+            cr[0] = m_(cr[0], inv);
+            cr[1] = m_(cr[1], inv);
+            cr[2] = m_(cr[2], inv);
+            vx = dot3(F.W2T, cr);
+            vy = dot3(F.W2T + 3, cr);
+        } else {
+            const float ax = -__fsub_rn(__ldg(c + 1), __ldg(c - 1));
+            const float ay = -__fsub_rn(__ldg(c + pitch), __ldg(c - pitch));
+            const float inv = rsqrtf(ax * ax + ay * ay + hh);
+            vx = ax * inv;
+            vy = ay * inv;
+        }
+        float cx = vx, cy = vy;
+        if (coarse) {
+            // the two coarse-mesh vertices g floor(ij / 2g + (1/2, 0)), g floor(ij / 2g + (0, 1/2))
+            const int ax = g * ((p + g) / (2 * g)) + dxi, ay = g * (q / (2 * g)) + dyi;
+            const int bx = g * (p / (2 * g)) + dxi, by = g * ((q + g) / (2 * g)) + dyi;
+            cx = (__ldg(par + (long long)ay * npitch + ax) + __ldg(par + (long long)by * npitch + bx)) * 0.5f;
+            cy = (__ldg(par + nplane + (long long)ay * npitch + ax) + __ldg(par + nplane + (long long)by * npitch + bx)) *
+                 0.5f;
+            if (format == 1) {
+                cx = cx * 2.0f - 1.0f;
+                cy = cy * 2.0f - 1.0f;
+            }
+            if (J.frame >= 0 && p2t) {
+                const float cz = sqrtf(fmaxf(1.0f - (cx * cx + cy * cy), 0.0f));
+                const float rx = R[0] * cx + R[1] * cy + R[2] * cz;
+                const float ry = R[3] * cx + R[4] * cy + R[5] * cz;
+                cx = rx;
+                cy = ry;
+            }
+        }
+        const long long k = (long long)q * npitch + p;
+        if (format == 0) {
+            o[k] = vx;
+            o[nplane + k] = vy;
+            o[2 * nplane + k] = cx;
+            o[3 * nplane + k] = cy;
+        } else if (format == 1) {
+            o[k] = unorm8(vx * 0.5f + 0.5f);
+            o[nplane + k] = unorm8(vy * 0.5f + 0.5f);
+            o[2 * nplane + k] = unorm8(cx * 0.5f + 0.5f);
+            o[3 * nplane + k] = unorm8(cy * 0.5f + 0.5f);
+        } else if (format == 2) {
+            o[k] = vx;
+            o[nplane + k] = vy;
+        } else {
+            o[k] = unorm8(vx * 0.5f + 0.5f);
+            o[nplane + k] = unorm8(vy * 0.5f + 0.5f);
+        }
+    }
+}
+
 }  // namespace
 
 namespace tp {
+
+// Normal tiles in any format, with coarse normals from parent normal slots
+// (pslots[k] >= 0) and spherical frames / parent-to-tangent rotations when given.
+// Jobs of one call must not be each other's parents (launch level by level).
+int launch_normals_format(tp_storage *elev, tp_storage *nrm, const int *eslots, const int *nslots, const float *meters,
+                          const int *pslots, const int *txs, const int *tys, int count, int format, int grid_mesh,
+                          void *stream, const SphereFrame *frames, const float *p2t)
+{
+    if (count <= 0) return TP_OK;
+    if (format < 0 || format > 3 || nrm->channels < ((format <= 1) ? 4 : 2))
+        return fail(TP_E_BAD_ARG, "normals: format needs a normal storage of 4 (formats 0, 1) or 2 channels");
+    const int Wn = elev->W - 4;
+    if (grid_mesh < 1 || (Wn - 1) / grid_mesh < 1) return fail(TP_E_BAD_ARG, "normals: bad grid mesh size");
+    static std::mutex mu;
+    static char *dbuf = nullptr;
+    static size_t dcap = 0;
+    std::lock_guard<std::mutex> lk(mu);
+    std::vector<NormalJob> h(count);
+    for (int k = 0; k < count; ++k) {
+        if (eslots[k] < 0 || eslots[k] >= elev->capacity || nslots[k] < 0 || nslots[k] >= nrm->capacity ||
+            (pslots && (pslots[k] >= nrm->capacity || pslots[k] == nslots[k])))
+            return fail(TP_E_BAD_ARG, "normals: slot out of range");
+        h[k] = NormalJob{eslots[k], nslots[k], meters[k], frames ? k : -1, pslots ? pslots[k] : -1, txs[k], tys[k], 0};
+    }
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const size_t jobs_bytes = (sizeof(NormalJob) * count + 255) & ~(size_t)255;
+    const size_t frames_bytes = frames ? ((sizeof(SphereFrame) * count + 255) & ~(size_t)255) : 0;
+    const size_t need = jobs_bytes + frames_bytes + (p2t ? sizeof(float) * 9 * count : 0);
+    if (dcap < need) {
+        if (dbuf) {
+            cudaStreamSynchronize(s);
+            cudaFree(dbuf);
+        }
+        dbuf = nullptr;
+        dcap = 0;
+        cudaError_t e = cudaMalloc(&dbuf, need);
+        if (e != cudaSuccess) return cuda_fail("cudaMalloc (normal jobs)", e);
+        dcap = need;
+    }
+    cudaError_t e = cudaMemcpyAsync(dbuf, h.data(), sizeof(NormalJob) * count, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess && frames)
+        e = cudaMemcpyAsync(dbuf + jobs_bytes, frames, sizeof(SphereFrame) * count, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess && p2t)
+        e = cudaMemcpyAsync(dbuf + jobs_bytes + frames_bytes, p2t, sizeof(float) * 9 * count, cudaMemcpyHostToDevice, s);
+    if (e != cudaSuccess) return cuda_fail("cudaMemcpyAsync (normal jobs)", e);
+    normals_format_kernel<<<count, 256, 0, s>>>(
+        elev->base, elev->pitch, elev->plane_stride, elev->slot_stride, nrm->base, nrm->pitch, nrm->plane_stride,
+        nrm->slot_stride, reinterpret_cast<const NormalJob *>(dbuf),
+        reinterpret_cast<const SphereFrame *>(dbuf + jobs_bytes),
+        p2t ? reinterpret_cast<const float *>(dbuf + jobs_bytes + frames_bytes) : nullptr, elev->W, format,
+        (Wn - 1) / grid_mesh);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail("normals kernel launch", e);
+    e = cudaStreamSynchronize(s);  // the job buffer is reused by the next call
+    if (e != cudaSuccess) return cuda_fail("cudaStreamSynchronize (normals)", e);
+    return TP_OK;
+}
 
 int launch_normals(tp_storage *elev, tp_storage *nrm, const int *eslots, const int *nslots, const float *meters,
                    int count, void *stream, const SphereFrame *frames)
@@ -152,7 +313,7 @@ int launch_normals(tp_storage *elev, tp_storage *nrm, const int *eslots, const i
     for (int k = 0; k < count; ++k) {
         if (eslots[k] < 0 || eslots[k] >= elev->capacity || nslots[k] < 0 || nslots[k] >= nrm->capacity)
             return fail(TP_E_BAD_ARG, "normals: slot out of range");
-        h[k] = NormalJob{eslots[k], nslots[k], meters[k], frames ? k : -1};
+        h[k] = NormalJob{eslots[k], nslots[k], meters[k], frames ? k : -1, -1, 0, 0, 0};
     }
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     const size_t jobs_bytes = (sizeof(NormalJob) * count + 255) & ~(size_t)255;
@@ -212,4 +373,54 @@ extern "C" int tp_normal_batch(tp_storage *elev, tp_storage *normals, const tp_t
     }
     return tp::launch_normals(elev, normals, es.data(), ns.data(), meters.data(), n, stream,
                               root_quad_size > 0.0 ? frames.data() : nullptr);
+}
+
+// Kernel-level normals in any format: jobs as tp_normal_batch; parent_normal_slots[k]
+// (or NULL) names the slot holding the parent normal tile for the coarse normals of
+// formats 0 and 1.  Jobs run level by level, so a batch may hold parents and children.
+extern "C" int tp_normal_batch_format(tp_storage *elev, tp_storage *normals, const tp_tile_job *jobs, int n,
+                                      double root_quad_size, int format, const int *parent_normal_slots,
+                                      int grid_mesh, void *stream)
+{
+    if (!elev || !normals || n < 0 || (n > 0 && !jobs) || format < 0 || format > 3)
+        return tp::fail(TP_E_BAD_ARG, "tp_normal_batch_format: bad arguments");
+    if (elev->on_device != 1 || elev->channels != 3 || normals->on_device != 1 || normals->W != elev->W - 4)
+        return tp::fail(TP_E_BAD_ARG, "tp_normal_batch_format: device storages of widths W and W - 4 needed");
+    std::vector<int> order(n);
+    for (int k = 0; k < n; ++k) {
+        const tp_tile_job &j = jobs[k];
+        if (j.level < 0 || j.level > 30 || j.tx < 0 || j.ty < 0 || (j.tx >> j.level) != 0 || (j.ty >> j.level) != 0 ||
+            !(j.tile_meters > 0.0f))
+            return tp::fail(TP_E_BAD_ARG, "tp_normal_batch_format: bad job");
+        order[k] = k;
+    }
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return jobs[a].level < jobs[b].level; });
+    size_t k = 0;
+    while (k < order.size()) {
+        const int level = jobs[order[k]].level;
+        std::vector<int> es, ns, ps, txs, tys;
+        std::vector<float> meters, p2t;
+        std::vector<tp::SphereFrame> frames;
+        for (; k < order.size() && jobs[order[k]].level == level; ++k) {
+            const tp_tile_job &j = jobs[order[k]];
+            es.push_back(j.out_slot);
+            ns.push_back(j.normal_slot);
+            ps.push_back(parent_normal_slots && j.level > 0 ? parent_normal_slots[order[k]] : -1);
+            txs.push_back(j.tx);
+            tys.push_back(j.ty);
+            meters.push_back(j.tile_meters);
+            if (root_quad_size > 0.0) {
+                frames.emplace_back();
+                tp::sphere_frame(root_quad_size, j.level, j.tx, j.ty, &frames.back());
+                p2t.resize(p2t.size() + 9, 0.0f);
+                if (j.level > 0) tp::parent_to_tangent(root_quad_size, j.level, j.tx, j.ty, &p2t[p2t.size() - 9]);
+            }
+        }
+        int rc = tp::launch_normals_format(elev, normals, es.data(), ns.data(), meters.data(), ps.data(), txs.data(),
+                                           tys.data(), (int)es.size(), format, grid_mesh, stream,
+                                           root_quad_size > 0.0 ? frames.data() : nullptr,
+                                           root_quad_size > 0.0 ? p2t.data() : nullptr);
+        if (rc) return rc;
+    }
+    return TP_OK;
 }

@@ -123,6 +123,15 @@ def normal_batch(elev, normals, jobs, root_quad_size=0.0, stream=None):
     check(lib().tp_normal_batch(elev.handle, normals.handle, arr, len(jobs), float(root_quad_size), stream))
 
 
+def normal_batch_format(elev, normals, jobs, fmt, parent_slots=None, root_quad_size=0.0, grid_mesh=24, stream=None):
+    """Normal tiles in format 0-3 with coarse normals from parent normal slots
+    (tp_normal_batch_format)."""
+    arr = (TileJob * len(jobs))(*jobs)
+    ps = (C.c_int * len(jobs))(*parent_slots) if parent_slots is not None else None
+    check(lib().tp_normal_batch_format(elev.handle, normals.handle, arr, len(jobs), float(root_quad_size), fmt, ps,
+                                       grid_mesh, stream))
+
+
 def elevation_batch_device(elev, residuals, normals, params, jobs_dev_ptr, n, stream=None):
     check(lib().tp_elevation_batch_device(elev.handle, residuals.handle if residuals else None,
                                           normals.handle if normals else None, C.byref(params),
@@ -341,6 +350,10 @@ class NormalProducer(TileProducer):
         check(lib().tp_normal_producer_create(cache.handle, elevations.handle, int(deform), C.byref(h)))
         super().__init__(h, cache)
         self.elevations = elevations
+
+    def set_format(self, fmt, grid_mesh=24):
+        """Output format 0-3 (NormalProducer.cpp:195): 0/1 carry the coarse normals."""
+        check(lib().tp_normal_producer_set_format(self.handle, fmt, grid_mesh))
 
 
 def scheduler_run(producers, stream=None):

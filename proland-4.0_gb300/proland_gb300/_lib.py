@@ -87,6 +87,8 @@ def lib():
         "tp_elevation_batch": ([_vp, _vp, _vp, C.POINTER(ElevParams), C.POINTER(TileJob), _i, _vp], _i),
         "tp_elevation_batch_device": ([_vp, _vp, _vp, C.POINTER(ElevParams), _vp, _i, _vp], _i),
         "tp_normal_batch": ([_vp, _vp, C.POINTER(TileJob), _i, C.c_double, _vp], _i),
+        "tp_normal_batch_format": ([_vp, _vp, C.POINTER(TileJob), _i, C.c_double, _i, C.POINTER(_i), _i, _vp], _i),
+        "tp_normal_producer_set_format": ([_vp, _i, _i], _i),
         "tp_elevation_batch_noalloc": ([_vp, _vp, _vp, C.POINTER(ElevParams), C.POINTER(TileJob), _i, _vp], _i),
         "tp_frame_create": ([C.POINTER(_vp)], _i),
         "tp_frame_destroy": ([_vp], _i),
