@@ -383,6 +383,7 @@ def learned_section(tp, torch, stream, sh, args, plain_w101):
         stream.synchronize()
         form_ms = 1000.0 * (time.perf_counter() - t0) / reps
         tp.stream_check(sh)
+    trained = (net.get_params(), si, so)
     used, executed = learned_flops(W)
     peak = None
     try:
@@ -392,7 +393,7 @@ def learned_section(tp, torch, stream, sh, args, plain_w101):
         peak = 1900.0
     tflops = B * used / (fwd_ms / 1000.0) / 1e12
     net.close()
-    return {
+    return trained, {
         "tile_width": W, "batch": B,
         "net_tiles_per_s": B / (fwd_ms / 1000.0), "net_ms_per_batch": fwd_ms,
         "form_tiles_per_s": B / (form_ms / 1000.0), "form_ms_per_batch": form_ms,
@@ -406,6 +407,60 @@ def learned_section(tp, torch, stream, sh, args, plain_w101):
                                                              "(device preprocess), 8 symmetries"},
         "levels": {str(l): {k: round(v, 5) for k, v in e.items()} for l, e in ev.items()},
     }
+
+
+def planet_section(tp, torch, stream, sh, args, trained):
+    """Planet-scale mixed frames: requests on six cube faces, 197-wide tiles at levels
+    0-16, stored residuals through level 10, residuals of the learned net (trained on
+    101-wide tiles; the net is fully convolutional) at 11-16, sphere normals.  A step
+    = learned residuals in chunks + one persistent elevation launch (CUDA graph) +
+    the normal pass.  Errors per level against FP64 on sampled tiles."""
+    import oracle
+    from proland_gb300 import learned as L, planet
+    params, si, so = trained
+    pf = planet.PlanetFrame(n=args.planet_requests, seed=args.seed + 7)
+    pf.allocate()
+    net = L.LearnedPredictor(197, 512, seed=1)
+    net.set_params(params)
+    net.set_sigmas(si, so)
+    with torch.cuda.stream(stream):
+        pf.build(net, chunk=512)
+        pf.frame.autotune(sh, repeats=3)
+        for _ in range(2):
+            pf.produce(sh)
+        torch.cuda.synchronize()
+        steps = 5
+        parts = {"learned": 0.0, "elevation": 0.0, "normals": 0.0}
+        t_all = time.perf_counter()
+        for _ in range(steps):
+            t0 = time.perf_counter()
+            for s0 in range(0, len(pf.learned_jobs), pf.chunk):
+                net.predict_residuals(pf.elev, pf.learned_jobs[s0:s0 + pf.chunk], pf.res, sh)
+            stream.synchronize()
+            t1 = time.perf_counter()
+            pf.frame.graph_launch(sh)
+            stream.synchronize()
+            t2 = time.perf_counter()
+            tp.normal_batch(pf.elev, pf.nrm, pf.all_jobs, pf.root, sh)
+            stream.synchronize()
+            t3 = time.perf_counter()
+            parts["learned"] += t1 - t0
+            parts["elevation"] += t2 - t1
+            parts["normals"] += t3 - t2
+        ms = 1000.0 * (time.perf_counter() - t_all) / steps
+        tp.stream_check(sh)
+    errs = pf.fp64_errors(oracle, per_level=2)
+    out = {"requests": pf.n, "tile_width": 197, "levels": "0-16", "faces": 6,
+           "learned_tiles": int(len(pf.learned_idx)), "stored_max_level": pf.stored_max,
+           "tiles_per_s": pf.n / (ms / 1000.0), "ms_per_step": ms,
+           "ms_learned": 1000.0 * parts["learned"] / steps, "ms_elevation": 1000.0 * parts["elevation"] / steps,
+           "ms_normals": 1000.0 * parts["normals"] / steps, "elevation_shape": pf.frame.config(0),
+           "timing": "host clock around each synchronised part, %d steps" % steps,
+           "fp64_errors_per_level": {str(l): {k: (round(v, 8) if isinstance(v, float) else v) for k, v in e.items()}
+                                     for l, e in errs.items()}}
+    pf.close()
+    net.close()
+    return out
 
 
 def main():
@@ -422,6 +477,8 @@ def main():
     ap.add_argument("--no-per-width", action="store_true", help="skip the per-width timings")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-residual form")
     ap.add_argument("--learned-steps", type=int, default=400, help="training steps before the learned timings")
+    ap.add_argument("--no-planet", action="store_true", help="skip the planet-scale mixed frame")
+    ap.add_argument("--planet-requests", type=int, default=16384)
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -569,7 +626,9 @@ def main():
         "max_err_vs_fp64": fp64_errors(tp, classes),
     }
     if not args.no_learned:
-        line["learned"] = learned_section(tp, torch, stream, sh, args, per_width.get("W101"))
+        trained, line["learned"] = learned_section(tp, torch, stream, sh, args, per_width.get("W101"))
+        if not args.no_planet:
+            line["planet"] = planet_section(tp, torch, stream, sh, args, trained)
     if not args.no_cpu:
         line["cpu_baseline"] = time_cpu(classes)
     print(json.dumps(line))

@@ -18,7 +18,8 @@ EARTH_ROOT = 2.0 * 6360000.0   # root quad size of a face: twice the radius (ter
 
 
 class PlanetFrame:
-    def __init__(self, n=16384, seed=11, W=197, max_level=16, stored_max=10, root=EARTH_ROOT, n_unique_parents=48):
+    def __init__(self, n=16384, seed=11, W=197, max_level=16, stored_max=10, root=EARTH_ROOT, n_unique_parents=48,
+                 n_residual_pool=64):
         rng = np.random.default_rng(seed)
         self.W, self.n, self.root = W, n, root
         self.stored_max = stored_max
@@ -29,9 +30,10 @@ class PlanetFrame:
         uz, um = workloads.fbm_parent_tiles(min(n_unique_parents, n), W, seed)
         pick = np.arange(n) % uz.shape[0]
         self.parent_zf, self.parent_zm = uz[pick], um[pick]
-        lv = np.minimum(self.levels, stored_max)
-        self.residual = workloads.residual_tiles(lv, W, seed + 1)
-        self.residual[self.levels > stored_max] = 0.0
+        # stored residuals: a pool of unit N(0, 1) tiles scaled by the level's sigma
+        pool = np.random.default_rng(seed + 1).standard_normal((min(n_residual_pool, n), W, W), dtype=np.float32)
+        sig = np.where(self.levels > stored_max, 0.0, 2000.0 * 0.5 ** np.minimum(self.levels, stored_max))
+        self.residual = pool[np.arange(n) % pool.shape[0]] * sig.astype(np.float32)[:, None, None]
         self.learned_idx = np.nonzero(self.levels > stored_max)[0]
 
     def jobs(self, learned):
