@@ -225,6 +225,9 @@ int tp_cache_stats(tp_cache *c, long long *queries, long long *misses);
 
 int tp_residual_producer_create(tp_cache *cache, const char *file, int delta, float zscale, tp_producer **out);
 int tp_residual_producer_set_source(tp_producer *p, tp_residual_source fn, void *user);
+/* A residual producer over a .dat file decodes its tiles on the device (1) or on
+ * the host (0, the default). */
+int tp_residual_producer_set_device_decode(tp_producer *p, int on);
 /* noise_amp: per-level amplitudes (ElevationProducer.cpp:488-499); face as in
  * ElevationProducer.cpp:509-515 (0 flat, 1..6 cube faces). */
 int tp_elevation_producer_create(tp_cache *cache, tp_producer *residuals, const float *noise_amp, int n_noise,
@@ -278,6 +281,13 @@ int tp_dat_close(tp_dat *d);
 int tp_dat_info(const tp_dat *d, int *info7, float *scale);
 int tp_dat_read_tile(const tp_dat *d, int level, int tx, int ty, int16_t *out, int capacity, int *width);
 int tp_inflate_zlib(const uint8_t *data, size_t n, uint8_t *out, size_t capacity, size_t *written);
+/* Tiles of the pyramid decoded on the device (the file's bytes are copied to the
+ * device once): tile k = (levels[k], txs[k], tys[k]) in the file's pyramid, or a zero
+ * tile when levels[k] < 0, written as int16 x scale into slots[k] of `residuals` (a
+ * 1-channel device storage of width tileSize + 5; smaller tiles below minLevel fill
+ * the slot's lower-left corner, the rest is zero).  TP_E_IO for a corrupt strip. */
+int tp_dat_decode_device(tp_dat *d, const int *levels, const int *txs, const int *tys, int n, float scale,
+                         tp_storage *residuals, const int *slots, void *stream);
 
 /* ------------------------------------------------------------------------
  * Noise helpers (host).  createDemNoise (ElevationProducer.cpp:50-133) and the

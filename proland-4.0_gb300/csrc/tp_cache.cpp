@@ -87,6 +87,7 @@ struct tp_producer {
     tp_producer *elevations = nullptr;
     int deform = 0;
     int normal_format = 2;  // 0..3 (NormalProducer.cpp:195); 0/1 add coarse normals
+    int device_decode = 0;  // residual producer over a .dat file: decode tiles on the device
     int grid_mesh = 24;
 };
 
@@ -456,6 +457,13 @@ extern "C" int tp_normal_producer_create(tp_cache *cache, tp_producer *elevation
     return TP_OK;
 }
 
+extern "C" int tp_residual_producer_set_device_decode(tp_producer *p, int on)
+{
+    if (!p || p->kind != kResidual) return tp::fail(TP_E_BAD_ARG, "tp_residual_producer_set_device_decode: not a residual producer");
+    p->device_decode = on ? 1 : 0;
+    return TP_OK;
+}
+
 extern "C" int tp_normal_producer_set_format(tp_producer *p, int format, int grid_mesh)
 {
     if (!p || p->kind != kNormal || format < 0 || format > 3 || grid_mesh < 1)
@@ -608,9 +616,56 @@ extern "C" int tp_tile_info(const tp_tile *t, int *level, int *tx, int *ty, int 
 // ---------------------------------------------------------------- scheduler
 namespace {
 
+// Residual tiles of a .dat file decoded on the device; the root of a delta chain
+// (upsampled through the levels above the file's root) stays on the host.
+int run_residuals_device(tp_producer *r, void *stream)
+{
+    tp_dat *d = r->dat;
+    std::vector<int> lv, txs, tys, slots;
+    std::vector<tp_tile *> host;
+    for (tp_tile *t : r->queue) {
+        const int level = t->level + r->delta - d->root_level;
+        if (r->delta > 0 && level == r->delta) {
+            host.push_back(t);
+            continue;
+        }
+        const bool inside = level >= 0 && (t->tx >> level) == d->root_tx && (t->ty >> level) == d->root_ty &&
+                            level <= d->max_level;
+        lv.push_back(inside ? level : -1);
+        txs.push_back(inside ? t->tx - (d->root_tx << level) : 0);
+        tys.push_back(inside ? t->ty - (d->root_ty << level) : 0);
+        slots.push_back(t->slot);
+    }
+    int rc = tp_dat_decode_device(d, lv.data(), txs.data(), tys.data(), (int)lv.size(), d->scale * r->zscale,
+                                  r->cache->storage, slots.data(), stream);
+    if (rc) return rc;
+    if (!host.empty()) {
+        tp_storage *s = r->cache->storage;
+        const size_t per = (size_t)s->W * s->W;
+        std::vector<float> buf(per * host.size());
+        std::vector<int> hs;
+        for (size_t k = 0; k < host.size(); ++k) {
+            rc = produce_residual(r, host[k], buf.data() + k * per);
+            if (rc) return rc;
+            hs.push_back(host[k]->slot);
+        }
+        rc = tp::staged_copy_slots(s, hs.data(), (int)hs.size(), 0, buf.data(), stream);
+        if (rc) return rc;
+        cudaError_t e = cudaStreamSynchronize(static_cast<cudaStream_t>(stream));
+        if (e != cudaSuccess) return tp::cuda_fail("cudaStreamSynchronize (residual upload)", e);
+    }
+    for (tp_tile *t : r->queue) {
+        t->done = true;
+        t->queued = false;
+    }
+    r->queue.clear();
+    return TP_OK;
+}
+
 int run_residuals(tp_producer *r, void *stream)
 {
     if (r->queue.empty()) return TP_OK;
+    if (r->dat && r->device_decode && r->cache->storage->on_device == 1) return run_residuals_device(r, stream);
     tp_storage *s = r->cache->storage;
     const int Wr = s->W;
     const size_t per = (size_t)Wr * Wr;

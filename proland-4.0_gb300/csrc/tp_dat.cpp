@@ -3,6 +3,8 @@
 // HeightMipmap.cpp:561-655).  The TIFF strip parser and the inflate decoder
 // (RFC 1950/1951) are this library's own, so the host side needs no zlib or
 // libtiff.
+#include <cuda_runtime.h>
+
 #include <cstdint>
 #include <cstdio>
 #include <cstring>
@@ -354,6 +356,7 @@ extern "C" int tp_dat_open(const char *path, tp_dat **out)
 
 extern "C" int tp_dat_close(tp_dat *d)
 {
+    if (d && d->dev_bytes) cudaFree(d->dev_bytes);
     delete d;
     return TP_OK;
 }

@@ -54,6 +54,8 @@ struct tp_dat {
     int ntiles = 0;
     std::vector<uint8_t> bytes;  // whole file
     size_t header = 0;
+    uint8_t *dev_bytes = nullptr;  // device copy, made on the first device decode
+    std::mutex dev_mu;
 };
 
 namespace tp {
@@ -145,5 +147,6 @@ void parent_to_tangent(double root_quad_size, int level, int tx, int ty, float *
 int dat_tile_width(const tp_dat *d, int level);
 int dat_tile_id(const tp_dat *d, int level, int tx, int ty);
 int dat_tile_int16(const tp_dat *d, int level, int tx, int ty, std::vector<int16_t> &out, int *width);
+int dat_device_bytes(tp_dat *d, const uint8_t **out);
 
 }  // namespace tp

@@ -306,13 +306,15 @@ class TileProducer:
 class ResidualProducer(TileProducer):
     """ResidualProducer: a .dat pyramid, a host callback or zero residuals."""
 
-    def __init__(self, cache, file="", delta=0, zscale=1.0, source=None):
+    def __init__(self, cache, file="", delta=0, zscale=1.0, source=None, device_decode=False):
         h = C.c_void_p()
         check(lib().tp_residual_producer_create(cache.handle, (file or "").encode(), delta, zscale, C.byref(h)))
         super().__init__(h, cache)
         self._source = None
         if source is not None:
             self.set_source(source)
+        if device_decode:
+            check(lib().tp_residual_producer_set_device_decode(h, 1))
 
     def tile(self, level, tx, ty):
         """The residual tile as computed on the host (tp_residual_tile)."""
@@ -381,6 +383,15 @@ class DatPyramid:
         if self.handle:
             lib().tp_dat_close(self.handle)
             self.handle = None
+
+    def decode_device(self, tiles, scale, residuals, slots, stream=None):
+        """Decodes [(level, tx, ty), ...] on the device into residual slots (tp_dat_decode_device)."""
+        n = len(tiles)
+        lv = (C.c_int * n)(*[t[0] for t in tiles])
+        xs = (C.c_int * n)(*[t[1] for t in tiles])
+        ys = (C.c_int * n)(*[t[2] for t in tiles])
+        sl = (C.c_int * n)(*slots)
+        check(lib().tp_dat_decode_device(self.handle, lv, xs, ys, n, scale, residuals.handle, sl, stream))
 
     def tile_int16(self, level, tx, ty):
         cap = (self.tile_size + 5) ** 2

@@ -134,6 +134,9 @@ def lib():
         "tp_dat_close": ([_vp], _i),
         "tp_dat_info": ([_vp, C.POINTER(_i), C.POINTER(C.c_float)], _i),
         "tp_dat_read_tile": ([_vp, _i, _i, _i, C.POINTER(C.c_int16), _i, C.POINTER(_i)], _i),
+        "tp_dat_decode_device": ([_vp, C.POINTER(_i), C.POINTER(_i), C.POINTER(_i), _i, C.c_float, _vp,
+                                  C.POINTER(_i), _vp], _i),
+        "tp_residual_producer_set_device_decode": ([_vp, _i], _i),
         "tp_inflate_zlib": ([_vp, C.c_size_t, _vp, C.c_size_t, C.POINTER(C.c_size_t)], _i),
         "tp_dem_noise": ([_i, _f32p], _i),
         "tp_cnoise": ([C.c_float, C.c_float], C.c_float),

@@ -111,15 +111,17 @@ def test_eviction_and_reproduction(gpu, oracle_lib):
     assert np.array_equal(zf0, want[(2, 0, 0)][0])
 
 
-def test_dem_dat_residuals_terrain4_layout(gpu, oracle_lib):
+@pytest.mark.parametrize("device_decode", [False, True])
+def test_dem_dat_residuals_terrain4_layout(gpu, oracle_lib, device_decode):
     """101-wide elevations over the reference's 197-wide residual pyramid with
-    delta 2 (terrain/examples/terrain4/helloworld.xml): mod 2 residual windows."""
+    delta 2 (terrain/examples/terrain4/helloworld.xml): mod 2 residual windows;
+    residual tiles decoded on the host or on the device."""
     tp, orc = gpu, oracle_lib
     path = os.path.join(GOLDEN, "dem_edit3_mini.dat")
     es = tp.TileStorage(101, 3, 32)
     rs = tp.TileStorage(197, 1, 8)
     ec, rc = tp.TileCache(es, "e"), tp.TileCache(rs, "r")
-    r = tp.ResidualProducer(rc, path, delta=2, zscale=0.1)
+    r = tp.ResidualProducer(rc, path, delta=2, zscale=0.1, device_decode=device_decode)
     e = tp.ElevationProducer(ec, r, params=tp.make_params(), face=0)
     e.set_root_quad_size(ROOT)
     assert r.has_tile(0, 0, 0) and r.has_tile(1, 0, 0) and r.has_tile(2, 1, 1)
