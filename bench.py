@@ -39,6 +39,7 @@ UNIT = "tiles/s"
 ROOT_QUAD = 100000.0          # meters: terrainNode size 50000 -> root quad 2 * size
 BYTES_PER_TILE = {101: 260960, 197: 1000544}   # algorithmic bytes (parent window, residual, elevation, normals)
 FALLBACK_HBM_GBS = 6800.0
+E2E_CHUNK = {101: 256, 197: 64}   # tiles per chunk of the host-buffer pipeline
 TRAFFIC_BYTES_PER_STEP = (207.4 + 574.2 + 238.1 + 741.3) * 1e6   # ncu dram__bytes_read/write of the two launches
 
 
@@ -84,6 +85,13 @@ class FrameClass:
         self.elev.upload(self.n, tp.ZM, self.h_parent_zm, stream)
         self.res.upload(0, 0, self.h_residual, stream)
 
+    def run_host(self, tp, pipe, params, stream):
+        """The whole frame of this width from host tiles to host tiles; parent zm is
+        derived on the device from parent zf (max(zf, 0)), as the parent's own
+        production wrote it."""
+        pipe.run(params, self.jobs, self.h_parent_zf, None, self.h_residual, self.h_zf, self.h_zc, self.h_zm,
+                 self.h_nx, self.h_ny, stream)
+
     def download_outputs(self, tp, stream=None):
         for c, buf in ((tp.ZF, self.h_zf), (tp.ZC, self.h_zc), (tp.ZM, self.h_zm)):
             self.elev.download(0, self.n, c, buf, stream)
@@ -100,7 +108,7 @@ class FrameClass:
         self.h_residual = pinned((n, W, W)); self.h_residual[:] = self.residual
         self.h_zf, self.h_zc, self.h_zm = (pinned((n, W, W)) for _ in range(3))
         self.h_nx, self.h_ny = (pinned((n, W - 4, W - 4)) for _ in range(2))
-        self.h2d_bytes = 3 * n * W * W * 4 + n * C.sizeof(self.jobs[0])
+        self.h2d_bytes = 2 * n * W * W * 4 + n * C.sizeof(self.jobs[0])   # parent zf, residual, jobs
         self.d2h_bytes = n * (3 * W * W + 2 * (W - 4) ** 2) * 4
 
 
@@ -295,6 +303,21 @@ def run_reference(args):
 
 
 # ------------------------------------------------------------------ GPU path
+def check_host_outputs(classes, sample=16):
+    """The host-buffer run's outputs against the device run's slots (same jobs and
+    inputs): True when the sampled tiles are bit-identical in all five planes."""
+    import proland_gb300 as tp
+    for fc in classes:
+        m = min(sample, fc.n)
+        dev = [fc.elev.download(0, m, c) for c in (tp.ZF, tp.ZC, tp.ZM)] + \
+              [fc.nrm.download(0, m, c) for c in (tp.NX, tp.NY)]
+        host = (fc.h_zf, fc.h_zc, fc.h_zm, fc.h_nx, fc.h_ny)
+        for d, h in zip(dev, host):
+            if not np.array_equal(d, h[:m]):
+                return False
+    return True
+
+
 def fp64_errors(tp, classes):
     """Max error of a few produced tiles against the FP64 evaluation of the same
     definition (and of the normals computed from FP64 elevations)."""
@@ -578,18 +601,26 @@ def main():
         fw.close()
     tp.stream_check(sh)
 
-    # end to end through the C ABI with host buffers
+    # end to end through the C ABI with host buffers: tp_elevation_batch_host per
+    # tile width (chunked host->device copies, launches and device->host copies
+    # overlapping), each width on its own caller stream
     e2e_ms = []
+    pipes = [tp.HostPipeline(fc.W, chunk=E2E_CHUNK[fc.W]) for fc in classes] if args.e2e_steps > 0 else []
+    e2e_streams = [torch.cuda.Stream() for _ in classes]
     for s in range(args.e2e_steps + 2 if args.e2e_steps > 0 else 0):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        for fc in classes:
-            fc.upload_inputs(tp, sh)
-            tp.elevation_batch(fc.elev, fc.res, fc.nrm, params, fc.jobs, sh)
-            fc.download_outputs(tp, sh)
-        stream.synchronize()
+        for fc, pipe, st in zip(classes, pipes, e2e_streams):
+            fc.run_host(tp, pipe, params, C.c_void_p(st.cuda_stream))
+        for st in e2e_streams:
+            st.synchronize()
         if s >= 2:
             e2e_ms.append(1000.0 * (time.perf_counter() - t0))
+    for st in e2e_streams:
+        tp.stream_check(C.c_void_p(st.cuda_stream))
+    e2e_check = check_host_outputs(classes) if pipes else None
+    for pipe in pipes:
+        pipe.close()
     e2e_step = float(np.mean(e2e_ms)) if e2e_ms else float("nan")
     e2e_step = replicas.max_over_ranks(e2e_step, dist if world > 1 else None, "cuda")
 
@@ -620,7 +651,10 @@ def main():
                      "algorithmic_bytes_per_step": sum(alg.values())},
         "e2e": {"value": world * tiles / (e2e_step / 1000.0), "unit": UNIT, "ms_per_step": e2e_step,
                 "h2d_bytes_per_step": sum(fc.h2d_bytes for fc in classes),
-                "d2h_bytes_per_step": sum(fc.d2h_bytes for fc in classes)},
+                "d2h_bytes_per_step": sum(fc.d2h_bytes for fc in classes),
+                "path": "tp_elevation_batch_host per tile width (chunks of %s tiles, copies overlapping launches)"
+                        % "/".join(str(E2E_CHUNK[fc.W]) for fc in classes),
+                "identical_to_device_run": e2e_check},
         "gpu_launches": args.steps * len(classes),
         "clocks": clk,
         "max_err_vs_fp64": fp64_errors(tp, classes),

@@ -151,6 +151,39 @@ int tp_elevation_batch_noalloc(tp_storage *elev, tp_storage *residuals, tp_stora
                                void *stream);
 
 /* ------------------------------------------------------------------------
+ * Host-buffer batches: the tiles of a frame whose inputs and outputs live in host
+ * memory, as CPUElevationProducer::doCreateTile's slots do
+ * (terrain/.../dem/CPUElevationProducer.cpp:156-248: parent tile in, W x W
+ * floats out), with the GPU path's zc, zm, noise and normals
+ * (ElevationProducer.cpp:280-405, NormalProducer.cpp:164-289).  The pipeline
+ * owns device slots for `nbuf` chunks of `chunk` tiles and three internal
+ * streams; a call splits its jobs into chunks and overlaps, chunk by chunk, the
+ * host->device copy of the next chunk, the persistent elevation launch of the
+ * current one and the device->host copy of the previous one.  Host memory
+ * should be pinned for the copies to be asynchronous. */
+typedef struct tp_pipeline tp_pipeline;
+int tp_pipeline_create(int tile_width, int chunk, int nbuf, tp_pipeline **out);
+int tp_pipeline_destroy(tp_pipeline *p);
+/* Dense host tile arrays of a call; tile k of each array belongs to job k. */
+typedef struct {
+    const float *parent_zf;  /* [n][W][W] parent zf planes (ignored for level-0 jobs) */
+    const float *parent_zm;  /* [n][W][W] parent zm planes; NULL: derived from parent_zf
+                                (max(zf, 0), or zf under no_clamp), as the parent's
+                                own production wrote it */
+    const float *residual;   /* [n][W][W] residual tiles; NULL when no job has one */
+    float *zf, *zc, *zm;     /* [n][W][W] outputs */
+    float *nx, *ny;          /* [n][W-4][W-4] normal outputs (format 2); NULL: none */
+} tp_host_tiles;
+/* Produces n independent jobs (parent_job must be -1) from host tiles into host
+ * tiles.  The slot fields of the jobs are replaced by the pipeline's own; a job
+ * with residual_slot < 0 adds no residual; residual windows must be (0, 0) (host
+ * residual tiles are W x W).  Work is ordered after what `stream` holds at the
+ * call, and `stream` waits for the last copy: synchronise `stream` before
+ * reading the outputs.  Calls on one pipeline are ordered among themselves. */
+int tp_elevation_batch_host(tp_pipeline *p, const tp_elev_params *params, const tp_tile_job *jobs, int n,
+                            const tp_host_tiles *io, void *stream);
+
+/* ------------------------------------------------------------------------
  * Frames: all tile requests of a frame -- for up to two tile widths (e.g. 101
  * and 197) -- produced by one persistent launch per tile width.  The CTAs take
  * work units (bands of tiles) from a device counter in list order; a job naming

@@ -5,6 +5,8 @@
 // and the slot planes at HBM speed.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "tp_internal.h"
 
 namespace {
@@ -26,6 +28,26 @@ __global__ void __launch_bounds__(256) repack_rows(const float *__restrict__ src
         for (int i = lane; i < W; i += 32) dst[slot + i] = __ldg(src + dense + i);
     } else {
         for (int i = lane; i < W; i += 32) dst[dense + i] = __ldg(src + slot + i);
+    }
+}
+
+// Several plane copies in one launch (blockIdx.y picks the copy), one warp per
+// row; rows of a copy are [count][rows] with independent tile and row strides on
+// each side, so dense arrays and pitched slot planes can be either end.
+__global__ void __launch_bounds__(256) repack_planes(tp::PlaneXfers x)
+{
+    const tp::PlaneXfer &p = x.p[blockIdx.y];
+    const long long row = (long long)blockIdx.x * 8 + (threadIdx.x >> 5);
+    if (row >= (long long)p.count * p.rows) return;
+    const int lane = threadIdx.x & 31;
+    const long long tile = row / p.rows;
+    const int r = (int)(row - tile * p.rows);
+    const float *src = p.src + tile * p.src_tile + (long long)r * p.src_pitch;
+    float *dst = p.dst + tile * p.dst_tile + (long long)r * p.dst_pitch;
+    if (p.clamp0) {
+        for (int i = lane; i < p.width; i += 32) dst[i] = fmaxf(__ldg(src + i), 0.0f);
+    } else {
+        for (int i = lane; i < p.width; i += 32) dst[i] = __ldg(src + i);
     }
 }
 
@@ -93,6 +115,19 @@ int staged_copy_slots(tp_storage *s, const int *slots, int count, int channel, c
     repack_rows<<<(unsigned)((rows + 7) / 8), 256, 0, st>>>(static_cast<const float *>(s->staging), plane, s->W,
                                                             s->pitch, s->slot_stride, rows, true, dmap);
     e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail("repack kernel launch", e);
+    return TP_OK;
+}
+
+int launch_repack_planes(const PlaneXfers &x, void *stream)
+{
+    if (x.n < 1 || x.n > kMaxPlaneXfers) return fail(TP_E_BAD_ARG, "repack: bad plane count");
+    long long rows = 0;
+    for (int i = 0; i < x.n; ++i) rows = std::max(rows, (long long)x.p[i].count * x.p[i].rows);
+    if (rows == 0) return TP_OK;
+    const dim3 grid((unsigned)((rows + 7) / 8), (unsigned)x.n);
+    repack_planes<<<grid, 256, 0, static_cast<cudaStream_t>(stream)>>>(x);
+    cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_fail("repack kernel launch", e);
     return TP_OK;
 }

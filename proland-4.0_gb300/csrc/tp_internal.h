@@ -117,6 +117,23 @@ int frame_occupancy(int stage_floats, int stages, int minb, bool mod, int *block
 // through the storage's staging buffer (one linear copy + a repack kernel).
 int staged_copy(tp_storage *s, int first, int count, int channel, float *host, bool up, void *stream);
 int read_status(int *status, bool clear);
+// One plane copy of repack_planes: `count` tiles of `rows` rows of `width` floats.
+struct PlaneXfer {
+    const float *src;
+    float *dst;
+    long long src_tile, dst_tile;  // floats between tiles
+    int src_pitch, dst_pitch;      // floats between rows
+    int rows, width, count;
+    int clamp0;                    // 1: dst = max(src, 0)
+};
+constexpr int kMaxPlaneXfers = 8;
+struct PlaneXfers {
+    PlaneXfer p[kMaxPlaneXfers];
+    int n;
+};
+// Runs the x.n plane copies in one launch on `stream`.
+int launch_repack_planes(const PlaneXfers &x, void *stream);
+
 // Uploads `count` dense host tiles into the given (not necessarily consecutive) slots.
 int staged_copy_slots(tp_storage *s, const int *slots, int count, int channel, const float *host, void *stream);
 // Spherical-deformation frame of one tile (NormalProducer.cpp:215-273), computed in

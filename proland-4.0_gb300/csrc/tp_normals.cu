@@ -47,9 +47,21 @@ __device__ __forceinline__ float dot3(const float *r, const float *x)
     return a_(a_(m_(r[0], x[0]), m_(r[1], x[1])), m_(r[2], x[2]));
 }
 
+// smoothstep(R/32, R/64, size) of getWorldPosition: one value per tile.
+__device__ __forceinline__ float sphere_blend(const tp::SphereFrame &f)
+{
+    const float R = f.R;
+    const float e0 = R / 32.0f, e1 = R / 64.0f;  // exact: powers of two
+    float s = __fdiv_rn(s_(f.size, e0), s_(e1, e0));
+    s = s < 0.0f ? 0.0f : (s > 1.0f ? 1.0f : s);
+    return m_(m_(s, s), s_(3.0f, m_(2.0f, s)));
+}
+
 // getWorldPosition of terrain2/normalShader.glsl:56-73 (the patch's projective
-// mapping onto the sphere), for grid position (u, v) in samples and height h.
-__device__ __forceinline__ void sphere_pos(const tp::SphereFrame &f, float n, float u, float v, float h, float *out)
+// mapping onto the sphere), for grid position (u, v) in samples and height h;
+// s = sphere_blend(f).
+__device__ __forceinline__ void sphere_pos(const tp::SphereFrame &f, float s, float n, float u, float v, float h,
+                                           float *out)
 {
     u = __fdiv_rn(u, n);
     v = __fdiv_rn(v, n);
@@ -66,15 +78,85 @@ __device__ __forceinline__ void sphere_pos(const tp::SphereFrame &f, float n, fl
         cp[r] = dot4(f.C + r * 4, ap);
     }
     const float R = f.R;
-    const float e0 = R / 32.0f, e1 = R / 64.0f;  // exact: powers of two
-    float s = __fdiv_rn(s_(f.size, e0), s_(e1, e0));  // smoothstep(R/32, R/64, size)
-    s = s < 0.0f ? 0.0f : (s > 1.0f ? 1.0f : s);
-    s = m_(m_(s, s), s_(3.0f, m_(2.0f, s)));
     const float len = __fsqrt_rn(dot3(up, up));
     const float k = a_(m_(len, s_(1.0f, s)), s);
     const float hp = __fdiv_rn(a_(h, m_(R, s_(1.0f, k))), k);
 #pragma unroll
     for (int r = 0; r < 3; ++r) out[r] = a_(cp[r], m_(hp, up[r]));
+}
+
+// Rows of world positions per band of normal rows (kSphereBand rows), kept in a
+// shared-memory ring of kSphereBand + 2 rows: each grid position is evaluated once
+// and read by the four normals around it.
+constexpr int kSphereBand = 16;
+constexpr int kSphereRing = kSphereBand + 2;
+
+__host__ __device__ constexpr int sphere_smem_floats(int W) { return 3 * kSphereRing * (W - 2); }
+
+// Positions of grid rows v in [v0, v1) (v in [-1, W - 4]), columns u in [-1, W - 4],
+// heights from the zm plane (texel (u + 2, v + 2)), into the ring.
+__device__ __forceinline__ void sphere_rows(const tp::SphereFrame &F, float s, float nn, const float *__restrict__ zm,
+                                            int pitch, int W, int v0, int v1, float *ring)
+{
+    const int PW = W - 2;
+    float *X = ring, *Y = ring + kSphereRing * PW, *Z = ring + 2 * kSphereRing * PW;
+    const int cnt = (v1 - v0) * PW;
+    for (int i = threadIdx.x; i < cnt; i += blockDim.x) {
+        const int r = i / PW;
+        const int u = i - r * PW - 1, v = v0 + r;
+        float o[3];
+        sphere_pos(F, s, nn, (float)u, (float)v, __ldg(zm + (long long)(v + 2) * pitch + (u + 2)), o);
+        const int k = ((v + 1) % kSphereRing) * PW + (u + 1);
+        X[k] = o[0];
+        Y[k] = o[1];
+        Z[k] = o[2];
+    }
+}
+
+// The normal at (p, q) from the ring (terrain2/normalShader.glsl:75-88): the cross
+// product of the neighbour differences, normalised, rotated into the tangent frame.
+__device__ __forceinline__ void sphere_normal(const tp::SphereFrame &F, const float *ring, int W, int p, int q,
+                                              float &vx, float &vy)
+{
+    const int PW = W - 2;
+    const float *X = ring, *Y = ring + kSphereRing * PW, *Z = ring + 2 * kSphereRing * PW;
+    const int rq = ((q + 1) % kSphereRing) * PW, rm = (q % kSphereRing) * PW, rp = ((q + 2) % kSphereRing) * PW;
+    const int i0 = rq + p, i1 = rq + p + 2, i2 = rm + p + 1, i3 = rp + p + 1;
+    const float a[3] = {s_(X[i1], X[i0]), s_(Y[i1], Y[i0]), s_(Z[i1], Z[i0])};
+    const float b[3] = {s_(X[i3], X[i2]), s_(Y[i3], Y[i2]), s_(Z[i3], Z[i2])};
+    float cr[3] = {s_(m_(a[1], b[2]), m_(a[2], b[1])), s_(m_(a[2], b[0]), m_(a[0], b[2])),
+                   s_(m_(a[0], b[1]), m_(a[1], b[0]))};
+    const float inv = __fdiv_rn(1.0f, __fsqrt_rn(dot3(cr, cr)));
+    cr[0] = m_(cr[0], inv);
+    cr[1] = m_(cr[1], inv);
+    cr[2] = m_(cr[2], inv);
+    vx = dot3(F.W2T, cr);
+    vy = dot3(F.W2T + 3, cr);
+}
+
+// Runs the bands of one spherical tile: fills the ring, then calls
+// epi(p, q, vx, vy) for every normal sample of the band.
+template <class Epi>
+__device__ __forceinline__ void sphere_tile(const tp::SphereFrame &F, const float *__restrict__ zm, int pitch, int W,
+                                            float *ring, Epi epi)
+{
+    const int Wn = W - 4;
+    const float nn = (float)(W - 5);
+    const float s = sphere_blend(F);
+    sphere_rows(F, s, nn, zm, pitch, W, -1, min(kSphereBand, Wn) + 1, ring);
+    for (int q0 = 0; q0 < Wn; q0 += kSphereBand) {
+        const int q1 = min(q0 + kSphereBand, Wn);
+        if (q0 > 0) sphere_rows(F, s, nn, zm, pitch, W, q0 + 1, q1 + 1, ring);
+        __syncthreads();
+        const int cnt = (q1 - q0) * Wn;
+        for (int i = threadIdx.x; i < cnt; i += blockDim.x) {
+            const int q = q0 + i / Wn, p = i % Wn;
+            float vx, vy;
+            sphere_normal(F, ring, W, p, q, vx, vy);
+            epi(p, q, vx, vy);
+        }
+        __syncthreads();
+    }
 }
 
 __global__ void __launch_bounds__(256) normals_kernel(const float *__restrict__ elev, int pitch, long long eplane,
@@ -87,6 +169,7 @@ __global__ void __launch_bounds__(256) normals_kernel(const float *__restrict__ 
     if (J.frame >= 0) {
         // spherical deformation (terrain2/normalShader.glsl:75-88): world positions of
         // the four neighbours, their cross product rotated into the tile's tangent frame
+        extern __shared__ float ring[];
         __shared__ tp::SphereFrame F;
         if (threadIdx.x == 0) F = frames[J.frame];
         __syncthreads();
@@ -94,30 +177,15 @@ __global__ void __launch_bounds__(256) normals_kernel(const float *__restrict__ 
         float *nx = nrm + (long long)J.nslot * nslot_stride;
         float *ny = nx + nplane;
         const int Wn = W - 4;
-        const float n = (float)(W - 5);
-        for (int idx = threadIdx.x; idx < Wn * npitch; idx += blockDim.x) {
-            const int q = idx / npitch, p = idx - q * npitch;
-            float vx = 0.0f, vy = 0.0f;
-            if (p < Wn) {
-                const float *c = zm + (long long)(q + 2) * pitch + (p + 2);
-                float p0[3], p1[3], p2[3], p3[3];
-                sphere_pos(F, n, (float)(p - 1), (float)q, __ldg(c - 1), p0);
-                sphere_pos(F, n, (float)(p + 1), (float)q, __ldg(c + 1), p1);
-                sphere_pos(F, n, (float)p, (float)(q - 1), __ldg(c - pitch), p2);
-                sphere_pos(F, n, (float)p, (float)(q + 1), __ldg(c + pitch), p3);
-                const float a[3] = {s_(p1[0], p0[0]), s_(p1[1], p0[1]), s_(p1[2], p0[2])};
-                const float b[3] = {s_(p3[0], p2[0]), s_(p3[1], p2[1]), s_(p3[2], p2[2])};
-                float cr[3] = {s_(m_(a[1], b[2]), m_(a[2], b[1])), s_(m_(a[2], b[0]), m_(a[0], b[2])),
-                               s_(m_(a[0], b[1]), m_(a[1], b[0]))};
-                const float inv = __fdiv_rn(1.0f, __fsqrt_rn(dot3(cr, cr)));
-                cr[0] = m_(cr[0], inv);
-                cr[1] = m_(cr[1], inv);
-                cr[2] = m_(cr[2], inv);
-                vx = dot3(F.W2T, cr);
-                vy = dot3(F.W2T + 3, cr);
-            }
+        sphere_tile(F, zm, pitch, W, ring, [&](int p, int q, float vx, float vy) {
             nx[(long long)q * npitch + p] = vx;
             ny[(long long)q * npitch + p] = vy;
+        });
+        // the pitch padding of each row
+        for (int idx = threadIdx.x; idx < Wn * (npitch - Wn); idx += blockDim.x) {
+            const int q = idx / (npitch - Wn), p = Wn + idx % (npitch - Wn);
+            nx[(long long)q * npitch + p] = 0.0f;
+            ny[(long long)q * npitch + p] = 0.0f;
         }
         return;
     }
@@ -171,34 +239,7 @@ __global__ void __launch_bounds__(256) normals_format_kernel(
     const bool coarse = (format == 0 || format == 1) && par;
     const float h2 = __fmul_rn(2.0f, __fdiv_rn(J.tile_meters, (float)n));
     const float hh = h2 * h2;
-    const float nn = (float)n;
-    for (int idx = threadIdx.x; idx < Wn * Wn; idx += blockDim.x) {
-        const int q = idx / Wn, p = idx - q * Wn;
-        const float *c = zm + (long long)(q + 2) * pitch + (p + 2);
-        float vx, vy;
-        if (J.frame >= 0) {
-            float p0[3], p1[3], p2[3], p3[3];
-            sphere_pos(F, nn, (float)(p - 1), (float)q, __ldg(c - 1), p0);
-            sphere_pos(F, nn, (float)(p + 1), (float)q, __ldg(c + 1), p1);
-            sphere_pos(F, nn, (float)p, (float)(q - 1), __ldg(c - pitch), p2);
-            sphere_pos(F, nn, (float)p, (float)(q + 1), __ldg(c + pitch), p3);
-            const float a[3] = {s_(p1[0], p0[0]), s_(p1[1], p0[1]), s_(p1[2], p0[2])};
-            const float b[3] = {s_(p3[0], p2[0]), s_(p3[1], p2[1]), s_(p3[2], p2[2])};
-            float cr[3] = {s_(m_(a[1], b[2]), m_(a[2], b[1])), s_(m_(a[2], b[0]), m_(a[0], b[2])),
-                           s_(m_(a[0], b[1]), m_(a[1], b[0]))};
-            const float inv = __fdiv_rn(1.0f, __fsqrt_rn(dot3(cr, cr)));
-            cr[0] = m_(cr[0], inv);
-            cr[1] = m_(cr[1], inv);
-            cr[2] = m_(cr[2], inv);
-            vx = dot3(F.W2T, cr);
-            vy = dot3(F.W2T + 3, cr);
-        } else {
-            const float ax = -__fsub_rn(__ldg(c + 1), __ldg(c - 1));
-            const float ay = -__fsub_rn(__ldg(c + pitch), __ldg(c - pitch));
-            const float inv = rsqrtf(ax * ax + ay * ay + hh);
-            vx = ax * inv;
-            vy = ay * inv;
-        }
+    auto emit = [&](int p, int q, float vx, float vy) {
         float cx = vx, cy = vy;
         if (coarse) {
             // the two coarse-mesh vertices g floor(ij / 2g + (1/2, 0)), g floor(ij / 2g + (0, 1/2))
@@ -237,7 +278,32 @@ __global__ void __launch_bounds__(256) normals_format_kernel(
             o[k] = unorm8(vx * 0.5f + 0.5f);
             o[nplane + k] = unorm8(vy * 0.5f + 0.5f);
         }
+    };
+    if (J.frame >= 0) {
+        extern __shared__ float ring[];
+        sphere_tile(F, zm, pitch, W, ring, emit);
+        return;
     }
+    for (int idx = threadIdx.x; idx < Wn * Wn; idx += blockDim.x) {
+        const int q = idx / Wn, p = idx - q * Wn;
+        const float *c = zm + (long long)(q + 2) * pitch + (p + 2);
+        const float ax = -__fsub_rn(__ldg(c + 1), __ldg(c - 1));
+        const float ay = -__fsub_rn(__ldg(c + pitch), __ldg(c - pitch));
+        const float inv = rsqrtf(ax * ax + ay * ay + hh);
+        emit(p, q, ax * inv, ay * inv);
+    }
+}
+
+// Dynamic shared memory of a spherical launch (the position ring), with the
+// kernel's limit raised when it exceeds the default 48 KB.
+int sphere_smem_attr(const void *kernel, int W, size_t *bytes)
+{
+    *bytes = sizeof(float) * (size_t)sphere_smem_floats(W);
+    if (*bytes > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)*bytes);
+        if (e != cudaSuccess) return tp::cuda_fail("cudaFuncSetAttribute (normals)", e);
+    }
+    return TP_OK;
 }
 
 }  // namespace
@@ -288,7 +354,12 @@ int launch_normals_format(tp_storage *elev, tp_storage *nrm, const int *eslots, 
     if (e == cudaSuccess && p2t)
         e = cudaMemcpyAsync(dbuf + jobs_bytes + frames_bytes, p2t, sizeof(float) * 9 * count, cudaMemcpyHostToDevice, s);
     if (e != cudaSuccess) return cuda_fail("cudaMemcpyAsync (normal jobs)", e);
-    normals_format_kernel<<<count, 256, 0, s>>>(
+    size_t smem = 0;
+    if (frames) {
+        int rc = sphere_smem_attr(reinterpret_cast<const void *>(normals_format_kernel), elev->W, &smem);
+        if (rc) return rc;
+    }
+    normals_format_kernel<<<count, 256, smem, s>>>(
         elev->base, elev->pitch, elev->plane_stride, elev->slot_stride, nrm->base, nrm->pitch, nrm->plane_stride,
         nrm->slot_stride, reinterpret_cast<const NormalJob *>(dbuf),
         reinterpret_cast<const SphereFrame *>(dbuf + jobs_bytes),
@@ -333,7 +404,12 @@ int launch_normals(tp_storage *elev, tp_storage *nrm, const int *eslots, const i
     if (e == cudaSuccess && frames)
         e = cudaMemcpyAsync(dbuf + jobs_bytes, frames, sizeof(SphereFrame) * count, cudaMemcpyHostToDevice, s);
     if (e != cudaSuccess) return cuda_fail("cudaMemcpyAsync (normal jobs)", e);
-    normals_kernel<<<count, 256, 0, s>>>(elev->base, elev->pitch, elev->plane_stride, elev->slot_stride, nrm->base,
+    size_t smem = 0;
+    if (frames) {
+        int rc = sphere_smem_attr(reinterpret_cast<const void *>(normals_kernel), elev->W, &smem);
+        if (rc) return rc;
+    }
+    normals_kernel<<<count, 256, smem, s>>>(elev->base, elev->pitch, elev->plane_stride, elev->slot_stride, nrm->base,
                                          nrm->pitch, nrm->plane_stride, nrm->slot_stride,
                                          reinterpret_cast<const NormalJob *>(dbuf),
                                          reinterpret_cast<const SphereFrame *>(dbuf + jobs_bytes), elev->W);

@@ -8,7 +8,7 @@ import ctypes as C
 
 import numpy as np
 
-from ._lib import (ElevParams, TileJob, TPError, check, lib, LIB_PATH, RESIDUAL_SOURCE,  # noqa: F401
+from ._lib import (ElevParams, HostTiles, TileJob, TPError, check, lib, LIB_PATH, RESIDUAL_SOURCE,  # noqa: F401
                    TP_OK, TP_E_BAD_ARG, TP_E_CACHE_FULL, TP_E_MISSING_PARENT,
                    TP_E_TIMEOUT, TP_E_CUDA, TP_E_IO, TP_E_NO_DEVICE)
 
@@ -136,6 +136,51 @@ def elevation_batch_device(elev, residuals, normals, params, jobs_dev_ptr, n, st
     check(lib().tp_elevation_batch_device(elev.handle, residuals.handle if residuals else None,
                                           normals.handle if normals else None, C.byref(params),
                                           jobs_dev_ptr, n, stream))
+
+
+class HostPipeline:
+    """Host-buffer batches (tp_pipeline_*, tp_elevation_batch_host): dense host
+    tile arrays in, dense host tile arrays out, the copies of neighbouring chunks
+    overlapping the elevation launches.  Arrays should be pinned (e.g. from
+    torch.empty(..., pin_memory=True).numpy()) for the copies to overlap."""
+
+    def __init__(self, tile_width, chunk=256, nbuf=3):
+        h = C.c_void_p()
+        check(lib().tp_pipeline_create(tile_width, chunk, nbuf, C.byref(h)))
+        self.handle = h
+        self.tile_width = tile_width
+
+    def close(self):
+        if self.handle:
+            lib().tp_pipeline_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def run(self, params, jobs, parent_zf, parent_zm, residual, zf, zc, zm, nx=None, ny=None, stream=None):
+        """Enqueues the batch; synchronise `stream` (or call stream_check) before
+        reading the outputs.  Arrays must be C-contiguous float32 [n, W, W]
+        ([n, W-4, W-4] for nx, ny); parent_zm and residual may be None."""
+        n = len(jobs)
+        W = self.tile_width
+        io = HostTiles()
+
+        def ptr(a, side):
+            if a is None:
+                return None
+            if a.dtype != np.float32 or not a.flags["C_CONTIGUOUS"] or a.shape[0] < n or a.shape[1:] != (side, side):
+                raise ValueError("host tiles must be contiguous float32 [n, %d, %d]" % (side, side))
+            return a.ctypes.data
+        io.parent_zf, io.parent_zm, io.residual = ptr(parent_zf, W), ptr(parent_zm, W), ptr(residual, W)
+        io.zf, io.zc, io.zm = ptr(zf, W), ptr(zc, W), ptr(zm, W)
+        io.nx, io.ny = ptr(nx, W - 4), ptr(ny, W - 4)
+        self._arr = (TileJob * n)(*jobs)
+        self._io = io
+        check(lib().tp_elevation_batch_host(self.handle, C.byref(params), self._arr, n, C.byref(io), stream))
 
 
 class Frame:

@@ -52,6 +52,11 @@ class ElevParams(C.Structure):
     ]
 
 
+class HostTiles(C.Structure):
+    """tp_host_tiles"""
+    _fields_ = [(n, C.c_void_p) for n in ("parent_zf", "parent_zm", "residual", "zf", "zc", "zm", "nx", "ny")]
+
+
 RESIDUAL_SOURCE = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_float), C.c_int)
 
 _LIB = None
@@ -90,6 +95,10 @@ def lib():
         "tp_normal_batch_format": ([_vp, _vp, C.POINTER(TileJob), _i, C.c_double, _i, C.POINTER(_i), _i, _vp], _i),
         "tp_normal_producer_set_format": ([_vp, _i, _i], _i),
         "tp_elevation_batch_noalloc": ([_vp, _vp, _vp, C.POINTER(ElevParams), C.POINTER(TileJob), _i, _vp], _i),
+        "tp_pipeline_create": ([_i, _i, _i, C.POINTER(_vp)], _i),
+        "tp_pipeline_destroy": ([_vp], _i),
+        "tp_elevation_batch_host": ([_vp, C.POINTER(ElevParams), C.POINTER(TileJob), _i, C.POINTER(HostTiles), _vp],
+                                    _i),
         "tp_frame_create": ([C.POINTER(_vp)], _i),
         "tp_frame_destroy": ([_vp], _i),
         "tp_frame_clear": ([_vp], _i),
