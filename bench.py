@@ -351,6 +351,81 @@ def learned_flops(W):
     return used, executed
 
 
+ORTHO_W = 196
+ORTHO_BYTES_PER_TILE = 4 * ((ORTHO_W // 2 + 2) ** 2 + 2 * ORTHO_W * ORTHO_W)   # parent window, residual, output
+
+
+def ortho_section(tp, torch, stream, sh, args):
+    """Ortho (colour) tiles: a frame of 4096 independent 196-wide RGBA8 requests,
+    levels 1-12, each with its own parent tile (48 distinct random parents cycled)
+    and a stored residual (bytes around 128), HSV noise as terrain3 configures it
+    (rnoise 60,150,20, cnoise 70,80,100, amplitude 255 at every level).  One
+    persistent launch per step; CUDA events on the launch stream."""
+    import oracle
+    W, n = ORTHO_W, 4096
+    rng = np.random.default_rng(args.seed + 3)
+    levels = rng.integers(1, 13, n)
+    tx = np.array([rng.integers(0, 1 << int(l)) for l in levels])
+    ty = np.array([rng.integers(0, 1 << int(l)) for l in levels])
+    pool = rng.integers(0, 256, (48, W, W, 4), dtype=np.uint8)
+    rpool = np.clip(rng.normal(128.0, 20.0, (64, W, W, 4)), 0, 255).astype(np.uint8)
+    orth = tp.TileStorage(W, 1, 2 * n)
+    res = tp.TileStorage(W, 1, n)
+    idx = np.arange(n)
+    orth.upload(n, 0, tp.rgba_to_texels(pool[idx % 48]), sh)
+    res.upload(0, 0, tp.rgba_to_texels(rpool[idx % 64]), sh)
+    params = tp.make_ortho_params(root_color=(60 / 255, 150 / 255, 20 / 255, 1.0),
+                                  noise_color=(70 / 255, 80 / 255, 100 / 255, 1.0), scale=2.0, hsv=True)
+    jobs = []
+    for k in range(n):
+        l = int(levels[k])
+        rot, layer = tp.noise_select(1, l, int(tx[k]), int(ty[k]))
+        jobs.append(tp.make_ortho_job(l, int(tx[k]), int(ty[k]), out_slot=k, parent_slot=n + k, residual_slot=k,
+                                      noise_rot=rot, noise_layer=layer, noise_amp=255.0))
+    arr = (tp.OrthoJob * n)(*jobs)
+    dev_jobs = torch.empty(C.sizeof(arr), dtype=torch.uint8, device="cuda")
+    dev_jobs.copy_(torch.frombuffer(bytearray(bytes(arr)), dtype=torch.uint8))
+    torch.cuda.synchronize()
+    jp = C.c_void_p(dev_jobs.data_ptr())
+    for _ in range(max(args.warmup, 3)):
+        tp.ortho_batch_device(orth, res, params, jp, n, sh)
+    steps = max(args.steps // 4, 10)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(steps):
+        tp.ortho_batch_device(orth, res, params, jp, n, sh)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    tp.stream_check(sh)
+    ms = e0.elapsed_time(e1) / steps
+    gbs = n * ORTHO_BYTES_PER_TILE / (ms / 1000.0) / 1e9
+    peak, src = hbm_peak()
+    # parity on sampled tiles against the oracle, and the oracle's single-thread rate
+    table = oracle.ortho_noise(W)
+    ok = True
+    t0 = time.perf_counter()
+    sample = [0, 1, n // 2, n - 1]
+    for k in sample:
+        j = jobs[k]
+        want = oracle.ortho_tile(W, j.level, j.tx, j.ty, pool[k % 48], rpool[k % 64], table[j.noise_layer],
+                                 j.noise_rot, j.noise_amp, root_color=list(params.root_color),
+                                 noise_color=list(params.noise_color), scale=params.scale, hsv=True)
+        got = tp.texels_to_rgba(orth.download(k, 1, 0)[0])
+        ok = ok and bool(np.array_equal(got, want))
+    cpu_rate = len(sample) / (time.perf_counter() - t0)
+    out = {"workload": "%d independent 196x196 RGBA8 ortho requests, levels 1-12, stored residuals, HSV noise" % n,
+           "tiles_per_s": n / (ms / 1000.0), "ms_per_step": ms, "steps": steps,
+           "algorithmic_bytes_per_tile": ORTHO_BYTES_PER_TILE,
+           "roofline": {"bound": "hbm", "achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak,
+                        "peak_source": src, "kernel": "ortho_kernel (one persistent launch)"},
+           "identical_to_oracle_on_sample": ok,
+           "cpu_single_thread_oracle_tiles_per_s": cpu_rate}
+    orth.close()
+    res.close()
+    return out
+
+
 def learned_section(tp, torch, stream, sh, args, plain_w101):
     """The learned-residual form beside the plain one: a net trained briefly on a
     5-level residual pyramid (device preprocess of a procedural fBm), its per-level
@@ -501,6 +576,7 @@ def main():
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-residual form")
     ap.add_argument("--learned-steps", type=int, default=400, help="training steps before the learned timings")
     ap.add_argument("--no-planet", action="store_true", help="skip the planet-scale mixed frame")
+    ap.add_argument("--no-ortho", action="store_true", help="skip the ortho (colour) tile frame")
     ap.add_argument("--planet-requests", type=int, default=16384)
     args = ap.parse_args()
     if args.impl == "reference":
@@ -659,6 +735,8 @@ def main():
         "clocks": clk,
         "max_err_vs_fp64": fp64_errors(tp, classes),
     }
+    if not args.no_ortho:
+        line["ortho"] = ortho_section(tp, torch, stream, sh, args)
     if not args.no_learned:
         trained, line["learned"] = learned_section(tp, torch, stream, sh, args, per_width.get("W101"))
         if not args.no_planet:

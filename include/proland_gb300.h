@@ -330,6 +330,65 @@ float tp_cnoise(float x, float y);               /* noise.cpp:118-165, period 0 
 int tp_noise_select(int face, int level, int tx, int ty, int *rot, int *layer);
 
 /* ------------------------------------------------------------------------
+ * Ortho (colour) tiles: OrthoProducer::doCreateTile
+ * (terrain/.../ortho/OrthoProducer.cpp:292-382) with the upsample shader
+ * (terrain/examples/terrain3/upsampleOrthoShader.glsl): 2x upsample of the
+ * parent with the (1,3,3,9)/16 masks floored to integers, the residual
+ * ((r - 128) * scale) or, at level 0, the root colour, then the rotated RGBA8
+ * noise layer added in RGB or HSV, written as 8-bit channels.  Tiles are W x W
+ * texels, W = tileSize + 4 with W a multiple of 4 (e.g. 196); an ortho storage is
+ * a one-channel storage (tp_storage_create(W, 1, ...)) whose 32-bit texels hold
+ * RGBA8, red in the low byte, so tp_storage_upload/download move them as they
+ * are.  Residual storages hold the same texels (OrthoCPUProducer tiles of fewer
+ * channels are read as GL does: missing green / blue 0, alpha 255). */
+typedef struct {
+    int32_t level, tx, ty;
+    int32_t out_slot;       /* ortho slot written */
+    int32_t parent_slot;    /* ortho slot of (level-1, tx/2, ty/2); -1 at level 0 */
+    int32_t residual_slot;  /* residual slot, -1 when the residual producer has no tile */
+    int32_t noise_rot;      /* 0..3 and 0..5: the tile's edge noise signs (tp_noise_select) */
+    int32_t noise_layer;
+    float noise_amp;        /* noiseAmp[level] (rs; 0 beyond the list) */
+    int32_t parent_job;     /* index of the job in this batch writing the parent, -1 if resident */
+    int32_t reserved[2];
+} tp_ortho_job;
+
+typedef struct {
+    float root_color[4];    /* rnoise / 255 (default 0.5) */
+    float noise_color[4];   /* cnoise / 255 (default 1) */
+    float scale;            /* residual scale (default 2) */
+    int32_t hsv;            /* noise added in HSV space */
+    int32_t reserved[2];
+} tp_ortho_params;
+
+/* createOrthoNoise (OrthoProducer.cpp:26-122): 6 layers of W x W RGBA8 bytes. */
+int tp_ortho_noise(int tile_width, uint8_t *out /* 6 * W * W * 4 */);
+/* Produces n ortho jobs in one persistent launch on `stream`; a job naming its
+ * parent's job (earlier in the list) is ordered after it.  `residuals` may be NULL
+ * when no job has a residual.  One batch per storage and stream at a time. */
+int tp_ortho_batch(tp_storage *ortho, tp_storage *residuals, const tp_ortho_params *params,
+                   const tp_ortho_job *jobs, int n, void *stream);
+/* Same with the job array in device memory (not validated on the host). */
+int tp_ortho_batch_device(tp_storage *ortho, tp_storage *residuals, const tp_ortho_params *params,
+                          const tp_ortho_job *jobs_dev, int n, void *stream);
+
+/* OrthoCPUProducer's pyramids (OrthoCPUProducer.cpp:70-236): a header of 7
+ * int32 {maxLevel, tileSize, channels, root, tx, ty, flags} (flags bit 0: DXT
+ * tiles, bit 1: tiles without border), 2 * ntiles int64 offsets, one
+ * single-strip deflate TIFF of (tileSize + 2 border)^2 x channels bytes per tile;
+ * tile id tx + ty 2^level + (4^level - 1) / 3 (:250-253). */
+typedef struct tp_ortho_dat tp_ortho_dat;
+int tp_ortho_dat_open(const char *path, tp_ortho_dat **out);
+int tp_ortho_dat_close(tp_ortho_dat *d);
+int tp_ortho_dat_info(const tp_ortho_dat *d, int *info8 /* the 7 header fields, ntiles */);
+/* Tile bytes (width^2 x channels, interleaved); DXT tiles give TP_E_BAD_ARG. */
+int tp_ortho_dat_read_tile(const tp_ortho_dat *d, int level, int tx, int ty, uint8_t *out, int capacity,
+                           int *width);
+/* The same tile as RGBA8 texels (width^2 words, missing channels as above). */
+int tp_ortho_dat_read_rgba(const tp_ortho_dat *d, int level, int tx, int ty, uint32_t *out, int capacity,
+                           int *width);
+
+/* ------------------------------------------------------------------------
  * Preprocess on the device (HeightMipmap.cpp:199-323, 399-559): residual
  * pyramids from a height field, as the reference's preprocess tool builds them.
  * tp_fbm_heights: a procedural value-noise fBm (octaves of base_cells * 2^o

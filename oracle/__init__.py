@@ -50,6 +50,16 @@ class Job(C.Structure):
     ]
 
 
+class OrthoJob(C.Structure):
+    _fields_ = [
+        ("W", C.c_int), ("level", C.c_int), ("tx", C.c_int), ("ty", C.c_int),
+        ("parent", C.c_void_p), ("residual", C.c_void_p), ("noise", C.c_void_p),
+        ("noise_rot", C.c_int), ("noise_amp", C.c_float),
+        ("root_color", C.c_float * 4), ("noise_color", C.c_float * 4),
+        ("scale", C.c_float), ("hsv", C.c_int), ("out", C.c_void_p),
+    ]
+
+
 def lib():
     global _LIB
     if _LIB is None:
@@ -67,6 +77,10 @@ def lib():
         L.or_cnoise2.argtypes = [C.c_float, C.c_float]
         L.or_cnoise2.restype = C.c_float
         L.or_noise_select.argtypes = [C.c_int] * 4 + [C.POINTER(C.c_int)] * 2
+        L.or_ortho_noise.argtypes = [C.c_int, C.c_void_p]
+        L.or_ortho_tile.argtypes = [C.POINTER(OrthoJob)]
+        L.or_ortho_tile_id.argtypes = [C.c_int, C.c_int, C.c_int]
+        L.or_ortho_tile_id.restype = C.c_int
         L.or_elevation_tile.argtypes = [C.POINTER(ElevTile)]
         L.or_elevation_tile_f64.argtypes = [C.POINTER(ElevTile), _f64p, _f64p, _f64p]
         L.or_cpu_elevation_tile.argtypes = [C.c_int] * 4 + [_f32p, C.c_int, _f32p, C.c_int,
@@ -128,6 +142,89 @@ def noise_select(face, level, tx, ty):
     r, l = C.c_int(), C.c_int()
     lib().or_noise_select(face, level, tx, ty, C.byref(r), C.byref(l))
     return r.value, l.value
+
+
+# ---------------------------------------------------------------- ortho
+def ortho_noise(W):
+    """createOrthoNoise: [6, W, W, 4] uint8."""
+    out = np.empty((6, W, W, 4), np.uint8)
+    lib().or_ortho_noise(W, out.ctypes.data)
+    return out
+
+
+def ortho_tile(W, level, tx, ty, parent, residual, noise_layer, noise_rot, noise_amp, root_color=(0.5,) * 4,
+               noise_color=(1.0,) * 4, scale=2.0, hsv=False):
+    """One ortho tile ([W, W, 4] uint8) as OrthoProducer::doCreateTile + the
+    upsample shader make it; parent None at level 0, residual None without one."""
+    out = np.empty((W, W, 4), np.uint8)
+    keep = []
+
+    def ptr(a):
+        if a is None:
+            return None
+        a = np.ascontiguousarray(a, np.uint8)
+        keep.append(a)
+        return a.ctypes.data
+    j = OrthoJob()
+    j.W, j.level, j.tx, j.ty = W, level, tx, ty
+    j.parent = ptr(parent) if level > 0 else None
+    j.residual = ptr(residual)
+    j.noise = ptr(noise_layer)
+    j.noise_rot, j.noise_amp = noise_rot, noise_amp
+    j.root_color[:] = [float(v) for v in root_color]
+    j.noise_color[:] = [float(v) for v in noise_color]
+    j.scale, j.hsv = scale, int(bool(hsv))
+    j.out = out.ctypes.data
+    lib().or_ortho_tile(C.byref(j))
+    return out
+
+
+class OrthoDatFile:
+    """Reader of OrthoCPUProducer's .dat pyramid (OrthoCPUProducer.cpp:82-114,
+    170-236): a 7-word int32 header {maxLevel, tileSize, channels, root, tx, ty,
+    flags} (flags bit 0: DXT tiles, bit 1: no border), 2 * ntiles int64 [start,
+    end) offsets relative to the end of the header, ntiles = (4^(maxLevel+1) - 1) / 3,
+    then one single-strip deflate TIFF of (tileSize + 2 border)^2 x channels bytes
+    per tile.  Pure Python (struct + zlib)."""
+
+    def __init__(self, data: bytes):
+        self.data = data
+        (self.max_level, self.tile_size, self.channels, self.root, self.root_tx, self.root_ty,
+         self.flags) = struct.unpack_from("<7i", data, 0)
+        self.dxt = (self.flags & 1) != 0
+        self.border = 0 if (self.flags & 2) else 2
+        self.ntiles = ((1 << (self.max_level * 2 + 2)) - 1) // 3
+        self.header = 7 * 4 + 2 * self.ntiles * 8
+        self.offsets = np.frombuffer(data, "<i8", self.ntiles * 2, 28)
+
+    @classmethod
+    def open(cls, path):
+        with open(path, "rb") as f:
+            return cls(f.read())
+
+    def tile_id(self, level, tx, ty):
+        return lib().or_ortho_tile_id(level, tx, ty)
+
+    def strip(self, level, tx, ty):
+        tid = self.tile_id(level, tx, ty)
+        a, b = int(self.offsets[2 * tid]), int(self.offsets[2 * tid + 1])
+        return self.data[self.header + a:self.header + b]
+
+    def tile(self, level, tx, ty):
+        """Decoded tile, shape (w, w, channels) uint8."""
+        w = self.tile_size + 2 * self.border
+        raw = decode_tiff_strip(self.strip(level, tx, ty))
+        return np.frombuffer(raw[:w * w * self.channels], np.uint8).reshape(w, w, self.channels)
+
+
+def rgba_words(tile):
+    """An (w, w, c) uint8 residual tile as the RGBA texels a GL texture of fewer
+    components returns: missing green / blue read 0, missing alpha 255."""
+    w, _, c = tile.shape
+    out = np.zeros((w, w, 4), np.uint8)
+    out[..., 3] = 255
+    out[..., :c] = tile
+    return out
 
 
 # ---------------------------------------------------------------- elevation

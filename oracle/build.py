@@ -15,7 +15,7 @@ LIB = os.path.join(OUT_DIR, "liboracle.so")
 
 
 def build(force: bool = False) -> str:
-    srcs = [os.path.join(HERE, "oracle.c"), os.path.join(HERE, "learned.c")]
+    srcs = [os.path.join(HERE, "oracle.c"), os.path.join(HERE, "learned.c"), os.path.join(HERE, "ortho.c")]
     hdr = os.path.join(HERE, "oracle.h")
     if (not force and os.path.exists(LIB)
             and os.path.getmtime(LIB) >= max([os.path.getmtime(p) for p in srcs] + [os.path.getmtime(hdr)])):

@@ -131,7 +131,30 @@ int or_learned_param_count(void);
 double or_learned_loss_grad(int W, int n, const float *params, const float *up, const float *target, const int *levels,
                             const float *sigma_in, const float *sigma_out, int emulate, float *pred_out, double *grad);
 
+/* ---- ortho (colour) tiles: ortho.c --------------------------------------
+ * or_ortho_noise: createOrthoNoise (OrthoProducer.cpp:26-122), 6 layers of
+ * W x W RGBA8.  or_ortho_tile: one OrthoProducer::doCreateTile
+ * (OrthoProducer.cpp:292-382) with terrain3/upsampleOrthoShader.glsl; tiles are
+ * dense W x W RGBA8 (4 bytes per texel, R first), W = tileSize + 4. */
+typedef struct {
+    int W, level, tx, ty;
+    const uint8_t *parent;    /* parent tile, NULL at level 0 */
+    const uint8_t *residual;  /* residual tile, NULL when the residual producer has none */
+    const uint8_t *noise;     /* the selected noise layer (W x W RGBA8) */
+    int noise_rot;            /* 0..3 */
+    float noise_amp;          /* noiseAmp[level] (rs) */
+    float root_color[4];      /* rnoise / 255 */
+    float noise_color[4];     /* cnoise / 255 */
+    float scale;              /* residual scale */
+    int hsv;
+    uint8_t *out;             /* W x W RGBA8 */
+} or_ortho_job;
+void or_ortho_noise(int W, uint8_t *out);
+void or_ortho_tile(const or_ortho_job *t);
+int  or_ortho_tile_id(int level, int tx, int ty);   /* OrthoCPUProducer.cpp:250-253 */
+
 #ifdef __cplusplus
 }
 #endif
+
 #endif

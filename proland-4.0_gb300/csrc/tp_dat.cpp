@@ -224,8 +224,10 @@ uint32_t rd32(const uint8_t *p, bool le)
               : (((uint32_t)p[0] << 24) | (p[1] << 16) | (p[2] << 8) | p[3]);
 }
 
+}  // namespace
+
 // Decodes strip 0 of a TIFF in memory into raw bytes.
-bool decode_tiff_strip(const uint8_t *t, size_t n, std::vector<uint8_t> &raw, size_t limit)
+bool tp::decode_tiff_strip(const uint8_t *t, size_t n, std::vector<uint8_t> &raw, size_t limit)
 {
     if (n < 8) return false;
     bool le;
@@ -266,8 +268,6 @@ bool decode_tiff_strip(const uint8_t *t, size_t n, std::vector<uint8_t> &raw, si
     }
     return false;
 }
-
-}  // namespace
 
 // ---------------------------------------------------------------- .dat file
 

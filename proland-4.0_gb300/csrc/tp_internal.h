@@ -22,6 +22,22 @@ int cuda_fail(const char *what, int err);
 // Rounds up to a multiple of m.
 inline int round_up(int v, int m) { return (v + m - 1) / m * m; }
 
+// Linear congruential generator of Proland's math/noise.h:50-68: the next seed is
+// (seed * 1103515245 + 12345) mod 2^31 (the reference's `long` arithmetic masked
+// to 31 bits gives this on 32- and 64-bit longs alike).
+struct Lcg {
+    uint32_t state;
+    explicit Lcg(uint32_t seed) : state(seed) {}
+    uint32_t next()
+    {
+        state = (uint32_t)(((uint64_t)state * 1103515245ull + 12345ull) & 0x7FFFFFFFull);
+        return state;
+    }
+    // uniform in [0, 1) with 24 bits: the top 24 of the 31-bit state
+    float unit() { return (float)(next() >> 7) / 16777216.0f; }
+    float signed_unit() { return unit() * 2.0f - 1.0f; }
+};
+
 }  // namespace tp
 
 // A pool of equally sized tile slots (device or pinned host memory).
@@ -45,6 +61,8 @@ struct tp_storage {
     void *staging = nullptr;
     size_t staging_bytes = 0;
     std::mutex copy_mu;
+    // launch state of the ortho batches that write into this storage
+    struct OrthoState *ortho = nullptr;
 };
 
 // A residual pyramid file held in memory (header fields and all its bytes).
@@ -165,5 +183,29 @@ int dat_tile_width(const tp_dat *d, int level);
 int dat_tile_id(const tp_dat *d, int level, int tx, int ty);
 int dat_tile_int16(const tp_dat *d, int level, int tx, int ty, std::vector<int16_t> &out, int *width);
 int dat_device_bytes(tp_dat *d, const uint8_t **out);
+// Strip 0 of a TIFF held in memory, decoded (deflate or none) into raw bytes, at
+// most `limit` of them; false for a corrupt or unsupported strip.
+bool decode_tiff_strip(const uint8_t *t, size_t n, std::vector<uint8_t> &raw, size_t limit);
+
+// One persistent ortho launch (tp_ortho.cu): tiles are RGBA8 texels packed in
+// 32-bit words; the noise table is [rotation][layer][row][pitch] words.
+struct OrthoLaunch {
+    const tp_ortho_job *jobs;  // device
+    int njobs;
+    int *counter;              // next job to take
+    int *done;                 // per-job completion (device)
+    uint32_t *tiles;
+    long long slot_stride;     // words
+    int pitch;                 // words per row
+    const uint32_t *res;
+    long long res_slot_stride;
+    int res_pitch;
+    const uint32_t *noise;
+    int W, win_pitch;
+    tp_ortho_params p;
+};
+int ortho_smem_bytes(int W, int *win_pitch);
+int launch_ortho(const OrthoLaunch &L, void *stream);
+void ortho_release(tp_storage *s);
 
 }  // namespace tp

@@ -13,21 +13,7 @@
 
 namespace {
 
-// Linear congruential generator of Proland's math/noise.h:50-68: the next seed is
-// (seed * 1103515245 + 12345) mod 2^31 (the reference's `long` arithmetic masked
-// to 31 bits gives this on 32- and 64-bit longs alike).
-struct Lcg {
-    uint32_t state;
-    explicit Lcg(uint32_t seed) : state(seed) {}
-    uint32_t next()
-    {
-        state = (uint32_t)(((uint64_t)state * 1103515245ull + 12345ull) & 0x7FFFFFFFull);
-        return state;
-    }
-    // uniform in [0, 1) with 24 bits: the top 24 of the 31-bit state
-    float unit() { return (float)(next() >> 7) / 16777216.0f; }
-    float signed_unit() { return unit() * 2.0f - 1.0f; }
-};
+using tp::Lcg;
 
 // 2D gradient noise with period 0 (math/noise.cpp:60-165).  Only the sign of its
 // value matters to the elevation producer.

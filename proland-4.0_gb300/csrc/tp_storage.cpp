@@ -91,6 +91,7 @@ extern "C" int tp_storage_destroy(tp_storage *s)
     }
     if (s->batch_frame) tp_frame_destroy(s->batch_frame);
     if (s->staging) cudaFree(s->staging);
+    tp::ortho_release(s);
     delete s;
     return TP_OK;
 }

@@ -8,7 +8,7 @@ import ctypes as C
 
 import numpy as np
 
-from ._lib import (ElevParams, HostTiles, TileJob, TPError, check, lib, LIB_PATH, RESIDUAL_SOURCE,  # noqa: F401
+from ._lib import (ElevParams, HostTiles, OrthoJob, OrthoParams, TileJob, TPError, check, lib, LIB_PATH, RESIDUAL_SOURCE,  # noqa: F401
                    TP_OK, TP_E_BAD_ARG, TP_E_CACHE_FULL, TP_E_MISSING_PARENT,
                    TP_E_TIMEOUT, TP_E_CUDA, TP_E_IO, TP_E_NO_DEVICE)
 
@@ -181,6 +181,96 @@ class HostPipeline:
         self._arr = (TileJob * n)(*jobs)
         self._io = io
         check(lib().tp_elevation_batch_host(self.handle, C.byref(params), self._arr, n, C.byref(io), stream))
+
+
+# ---------------------------------------------------------------- ortho tiles
+def ortho_noise(tile_width):
+    """createOrthoNoise: [6, W, W, 4] uint8."""
+    out = np.empty((6, tile_width, tile_width, 4), np.uint8)
+    check(lib().tp_ortho_noise(tile_width, out.ctypes.data))
+    return out
+
+
+def make_ortho_params(root_color=(0.5, 0.5, 0.5, 0.5), noise_color=(1.0, 1.0, 1.0, 1.0), scale=2.0, hsv=False):
+    """tp_ortho_params; colours in [0, 1] (the reference's rnoise / cnoise over 255)."""
+    p = OrthoParams()
+    p.root_color[:] = [float(v) for v in root_color]
+    p.noise_color[:] = [float(v) for v in noise_color]
+    p.scale, p.hsv = float(scale), int(bool(hsv))
+    return p
+
+
+def make_ortho_job(level, tx, ty, out_slot, parent_slot=-1, residual_slot=-1, noise_rot=0, noise_layer=0,
+                   noise_amp=0.0, parent_job=-1):
+    j = OrthoJob()
+    j.level, j.tx, j.ty = level, tx, ty
+    j.out_slot, j.parent_slot, j.residual_slot = out_slot, parent_slot, residual_slot
+    j.noise_rot, j.noise_layer, j.noise_amp, j.parent_job = noise_rot, noise_layer, float(noise_amp), parent_job
+    return j
+
+
+def ortho_batch(ortho, residuals, params, jobs, stream=None):
+    """Produces ortho jobs (a list of OrthoJob) in one launch (tp_ortho_batch)."""
+    arr = (OrthoJob * len(jobs))(*jobs)
+    check(lib().tp_ortho_batch(ortho.handle, residuals.handle if residuals else None, C.byref(params), arr,
+                               len(jobs), stream))
+
+
+def ortho_batch_device(ortho, residuals, params, jobs_dev_ptr, n, stream=None):
+    check(lib().tp_ortho_batch_device(ortho.handle, residuals.handle if residuals else None, C.byref(params),
+                                      jobs_dev_ptr, n, stream))
+
+
+def rgba_to_texels(tiles):
+    """[..., W, W, 4] uint8 -> [..., W, W] float32 view of the packed RGBA8 texels
+    (the storage's element type), for tp_storage_upload."""
+    a = np.ascontiguousarray(tiles, np.uint8)
+    return a.view(np.uint32).reshape(a.shape[:-1]).view(np.float32)
+
+
+def texels_to_rgba(texels):
+    """Inverse of rgba_to_texels."""
+    a = np.ascontiguousarray(texels, np.float32)
+    return a.view(np.uint8).reshape(a.shape + (4,))
+
+
+class OrthoDat:
+    """OrthoCPUProducer's .dat pyramid (tp_ortho_dat_*)."""
+
+    def __init__(self, path):
+        h = C.c_void_p()
+        check(lib().tp_ortho_dat_open(path.encode(), C.byref(h)))
+        self.handle = h
+        info = (C.c_int * 8)()
+        check(lib().tp_ortho_dat_info(h, info))
+        (self.max_level, self.tile_size, self.channels, self.root, self.root_tx, self.root_ty, self.flags,
+         self.ntiles) = list(info)
+        self.width = self.tile_size + (0 if self.flags & 2 else 4)
+
+    def close(self):
+        if self.handle:
+            lib().tp_ortho_dat_close(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def tile(self, level, tx, ty):
+        w = self.width
+        out = np.empty((w, w, self.channels), np.uint8)
+        got = C.c_int()
+        check(lib().tp_ortho_dat_read_tile(self.handle, level, tx, ty, out.ctypes.data, out.size, C.byref(got)))
+        return out
+
+    def tile_rgba(self, level, tx, ty):
+        w = self.width
+        out = np.empty((w, w, 4), np.uint8)
+        got = C.c_int()
+        check(lib().tp_ortho_dat_read_rgba(self.handle, level, tx, ty, out.ctypes.data, w * w, C.byref(got)))
+        return out
 
 
 class Frame:

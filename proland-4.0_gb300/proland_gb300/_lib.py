@@ -52,6 +52,24 @@ class ElevParams(C.Structure):
     ]
 
 
+class OrthoJob(C.Structure):
+    """tp_ortho_job"""
+    _fields_ = [
+        ("level", C.c_int32), ("tx", C.c_int32), ("ty", C.c_int32),
+        ("out_slot", C.c_int32), ("parent_slot", C.c_int32), ("residual_slot", C.c_int32),
+        ("noise_rot", C.c_int32), ("noise_layer", C.c_int32), ("noise_amp", C.c_float),
+        ("parent_job", C.c_int32), ("reserved", C.c_int32 * 2),
+    ]
+
+
+class OrthoParams(C.Structure):
+    """tp_ortho_params"""
+    _fields_ = [
+        ("root_color", C.c_float * 4), ("noise_color", C.c_float * 4), ("scale", C.c_float),
+        ("hsv", C.c_int32), ("reserved", C.c_int32 * 2),
+    ]
+
+
 class HostTiles(C.Structure):
     """tp_host_tiles"""
     _fields_ = [(n, C.c_void_p) for n in ("parent_zf", "parent_zm", "residual", "zf", "zc", "zm", "nx", "ny")]
@@ -99,6 +117,14 @@ def lib():
         "tp_pipeline_destroy": ([_vp], _i),
         "tp_elevation_batch_host": ([_vp, C.POINTER(ElevParams), C.POINTER(TileJob), _i, C.POINTER(HostTiles), _vp],
                                     _i),
+        "tp_ortho_noise": ([_i, _vp], _i),
+        "tp_ortho_batch": ([_vp, _vp, C.POINTER(OrthoParams), C.POINTER(OrthoJob), _i, _vp], _i),
+        "tp_ortho_batch_device": ([_vp, _vp, C.POINTER(OrthoParams), _vp, _i, _vp], _i),
+        "tp_ortho_dat_open": ([C.c_char_p, C.POINTER(_vp)], _i),
+        "tp_ortho_dat_close": ([_vp], _i),
+        "tp_ortho_dat_info": ([_vp, C.POINTER(_i)], _i),
+        "tp_ortho_dat_read_tile": ([_vp, _i, _i, _i, _vp, _i, C.POINTER(_i)], _i),
+        "tp_ortho_dat_read_rgba": ([_vp, _i, _i, _i, _vp, _i, C.POINTER(_i)], _i),
         "tp_frame_create": ([C.POINTER(_vp)], _i),
         "tp_frame_destroy": ([_vp], _i),
         "tp_frame_clear": ([_vp], _i),

@@ -9,6 +9,10 @@ int16 samples of those tiles (decoded here with Python's zlib, independently
 of the library's own inflate) and the header fields go to dem_golden.npz;
 sources.txt records the source files' SHA-256.
 
+The ortho fixture is cut the same way from the reference's RGB.dat (an
+OrthoCPUProducer pyramid, 196-wide RGBA tiles): tiles (0, 0, 0) and (1, 1, 0)
+kept in rgb_graph1_mini.dat, their decoded bytes in ortho_golden.npz.
+
     python tests/golden/make_golden.py /root/reference
 """
 import hashlib
@@ -27,6 +31,21 @@ SOURCES = {
     "edit3": "src/edit/examples/edit3/DEM.dat",
 }
 KEEP = [(0, 0, 0), (1, 0, 0), (2, 0, 0), (3, 0, 0), (4, 0, 0)]
+ORTHO_SOURCE = ("graph1", "src/graph/examples/graph1/RGB.dat")
+ORTHO_KEEP = [(0, 0, 0), (1, 1, 0)]
+
+
+def mini_ortho_dat(d):
+    offsets = np.zeros(2 * d.ntiles, np.int64)
+    blob = b""
+    for lvl, tx, ty in ORTHO_KEEP:
+        tid = d.tile_id(lvl, tx, ty)
+        strip = d.strip(lvl, tx, ty)
+        offsets[2 * tid] = len(blob)
+        blob += strip
+        offsets[2 * tid + 1] = len(blob)
+    head = struct.pack("<7i", d.max_level, d.tile_size, d.channels, d.root, d.root_tx, d.root_ty, d.flags)
+    return head + offsets.tobytes() + blob
 
 
 def mini_dat(d):
@@ -59,6 +78,17 @@ def main(ref_root):
         for lvl, tx, ty in KEEP:
             arrays["%s_L%d_%d_%d" % (name, lvl, tx, ty)] = d.tile_int16(lvl, tx, ty).copy()
     np.savez_compressed(os.path.join(HERE, "dem_golden.npz"), **arrays)
+    name, rel = ORTHO_SOURCE
+    data = open(os.path.join(ref_root, rel), "rb").read()
+    lines.append("%s  %s  %d bytes  sha256 %s" % (name, rel, len(data), hashlib.sha256(data).hexdigest()))
+    od = oracle.OrthoDatFile(data)
+    with open(os.path.join(HERE, "rgb_%s_mini.dat" % name), "wb") as f:
+        f.write(mini_ortho_dat(od))
+    oarr = {"header": np.array([od.max_level, od.tile_size, od.channels, od.root, od.root_tx, od.root_ty, od.flags,
+                                od.ntiles], np.int32)}
+    for lvl, tx, ty in ORTHO_KEEP:
+        oarr["L%d_%d_%d" % (lvl, tx, ty)] = od.tile(lvl, tx, ty).copy()
+    np.savez_compressed(os.path.join(HERE, "ortho_golden.npz"), **oarr)
     with open(os.path.join(HERE, "sources.txt"), "w") as f:
         f.write("\n".join(lines) + "\n")
 
