@@ -375,7 +375,8 @@ def ortho_section(tp, torch, stream, sh, args):
     orth.upload(n, 0, tp.rgba_to_texels(pool[idx % 48]), sh)
     res.upload(0, 0, tp.rgba_to_texels(rpool[idx % 64]), sh)
     params = tp.make_ortho_params(root_color=(60 / 255, 150 / 255, 20 / 255, 1.0),
-                                  noise_color=(70 / 255, 80 / 255, 100 / 255, 1.0), scale=2.0, hsv=True)
+                                  noise_color=(70 / 255, 80 / 255, 100 / 255, 1.0), scale=2.0,
+                                  hsv=not args.ortho_rgb)
     jobs = []
     for k in range(n):
         l = int(levels[k])
@@ -410,11 +411,13 @@ def ortho_section(tp, torch, stream, sh, args):
         j = jobs[k]
         want = oracle.ortho_tile(W, j.level, j.tx, j.ty, pool[k % 48], rpool[k % 64], table[j.noise_layer],
                                  j.noise_rot, j.noise_amp, root_color=list(params.root_color),
-                                 noise_color=list(params.noise_color), scale=params.scale, hsv=True)
+                                 noise_color=list(params.noise_color), scale=params.scale,
+                                 hsv=bool(params.hsv))
         got = tp.texels_to_rgba(orth.download(k, 1, 0)[0])
         ok = ok and bool(np.array_equal(got, want))
     cpu_rate = len(sample) / (time.perf_counter() - t0)
-    out = {"workload": "%d independent 196x196 RGBA8 ortho requests, levels 1-12, stored residuals, HSV noise" % n,
+    out = {"workload": "%d independent 196x196 RGBA8 ortho requests, levels 1-12, stored residuals, %s noise"
+                       % (n, "HSV" if params.hsv else "RGB"),
            "tiles_per_s": n / (ms / 1000.0), "ms_per_step": ms, "steps": steps,
            "algorithmic_bytes_per_tile": ORTHO_BYTES_PER_TILE,
            "roofline": {"bound": "hbm", "achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak,
@@ -577,6 +580,9 @@ def main():
     ap.add_argument("--learned-steps", type=int, default=400, help="training steps before the learned timings")
     ap.add_argument("--no-planet", action="store_true", help="skip the planet-scale mixed frame")
     ap.add_argument("--no-ortho", action="store_true", help="skip the ortho (colour) tile frame")
+    ap.add_argument("--ortho-only", action="store_true",
+                    help="run the ortho frame alone and print its object (for profiling)")
+    ap.add_argument("--ortho-rgb", action="store_true", help="ortho frame with RGB instead of HSV noise")
     ap.add_argument("--planet-requests", type=int, default=16384)
     args = ap.parse_args()
     if args.impl == "reference":
@@ -595,6 +601,10 @@ def main():
     warmup = max(args.warmup, 3)
 
     from proland_gb300 import replicas
+    if args.ortho_only:
+        stream = torch.cuda.Stream()
+        print(json.dumps({"ortho": ortho_section(tp, torch, stream, C.c_void_p(stream.cuda_stream), args)}))
+        return
     classes = make_frame(args.requests, replicas.rank_seed(args.seed, rank))
     stream = torch.cuda.Stream()
     sh = C.c_void_p(stream.cuda_stream)

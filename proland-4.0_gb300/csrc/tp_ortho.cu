@@ -44,13 +44,31 @@ __device__ __forceinline__ float s_(float a, float b) { return __fsub_rn(a, b); 
 __device__ __forceinline__ float d_(float a, float b) { return __fdiv_rn(a, b); }
 __device__ __forceinline__ float clamp01(float v) { return v < 0.0f ? 0.0f : (v > 1.0f ? 1.0f : v); }
 
-__device__ __forceinline__ float byte_of(uint32_t w, int c) { return (float)((w >> (8 * c)) & 255u); }
+// Byte c of w as a float, exactly: the byte placed in the mantissa of 2^23
+// (0x4B0000bb) minus 2^23.
+__device__ __forceinline__ float byte_of(uint32_t w, int c)
+{
+    return __fsub_rn(__uint_as_float(__byte_perm(w, 0x4B000000u, 0x7540u + c)), 8388608.0f);
+}
 
-// framebuffer write of result / 255 to an 8-bit channel
+// An integer 0 <= v < 2^23 as a float, exactly.
+__device__ __forceinline__ float int_to_f(uint32_t v) { return __fsub_rn(__uint_as_float(0x4B000000u | v), 8388608.0f); }
+
+// Framebuffer write of result / 255 to an 8-bit channel: clamp(result / 255, 0, 1)
+// times 255, rounded to nearest even.  Both roundings move a result in [0, 255]
+// by less than 3.1e-5, so away from the half-integers (1e-3 margin) the byte is
+// clamp(rint(result)); within the margin the two roundings are evaluated.
 __device__ __forceinline__ uint32_t unorm8(float result)
 {
-    const float f = clamp01(d_(result, 255.0f));
-    return (uint32_t)__float2int_rn(m_(f, 255.0f));
+    const float t = __fsub_rn(result, floorf(result));
+    float v;
+    if (fabsf(__fsub_rn(t, 0.5f)) > 1e-3f) {
+        v = fminf(fmaxf(result, 0.0f), 255.0f);
+    } else {
+        v = m_(clamp01(d_(result, 255.0f)), 255.0f);
+    }
+    // rint by the 1.5 * 2^23 addition (ties to even), the integer in the low bits
+    return __float_as_uint(__fadd_rn(v, 12582912.0f)) & 0x1FFu;
 }
 
 __device__ __forceinline__ void rgb_to_hsv(const float *rgb, float *hsv)
@@ -65,7 +83,7 @@ __device__ __forceinline__ void rgb_to_hsv(const float *rgb, float *hsv)
         hsv[1] = d_(delta, mx);
         float d[3];
 #pragma unroll
-        for (int c = 0; c < 3; ++c) d[c] = d_(a_(d_(s_(mx, rgb[c]), 6.0f), d_(delta, 2.0f)), delta);
+        for (int c = 0; c < 3; ++c) d[c] = d_(a_(d_(s_(mx, rgb[c]), 6.0f), m_(delta, 0.5f)), delta);  // delta / 2 exact
         if (rgb[0] == mx) hsv[0] = s_(d[2], d[1]);
         else if (rgb[1] == mx) hsv[0] = s_(a_(1.0f / 3.0f, d[0]), d[2]);
         else if (rgb[2] == mx) hsv[0] = s_(a_(2.0f / 3.0f, d[1]), d[0]);
@@ -95,13 +113,18 @@ __device__ __forceinline__ void hsv_to_rgb(const float *hsv, float *rgb)
 
 // One texel: r = residual / root colour / 128 as floats, c = floored parent mask
 // sum (when there is a parent), n = noise texel.
-__device__ __forceinline__ uint32_t texel(float (&r)[4], const float (&nv)[4], const float (&nc)[4], bool hsv)
+__device__ __forceinline__ uint32_t texel(float (&r)[4], const float (&nv)[4], const float (&nc)[4], bool hsv,
+                                          const float *inv255)
 {
     float out[4];
     if (hsv) {
         float rgb[3], h[3];
 #pragma unroll
-        for (int c = 0; c < 3; ++c) rgb[c] = d_(r[c], 255.0f);
+        for (int c = 0; c < 3; ++c) {
+            // k / 255 of the integers 0..255 from the table (the same correctly rounded quotients)
+            const bool tab = r[c] >= 0.0f && r[c] <= 255.0f && r[c] == floorf(r[c]);
+            rgb[c] = tab ? inv255[(int)r[c]] : d_(r[c], 255.0f);
+        }
         rgb_to_hsv(rgb, h);
         // 1 - smoothstep(0.4, 0.8, v); 0.8f - 0.4f is exactly 0.4f
         float t = clamp01(d_(s_(h[2], 0.4f), s_(0.8f, 0.4f)));
@@ -120,13 +143,16 @@ __device__ __forceinline__ uint32_t texel(float (&r)[4], const float (&nv)[4], c
 #pragma unroll
         for (int c = 0; c < 4; ++c) out[c] = a_(m_(nc[c], s_(nv[c], 128.0f)), r[c]);
     }
-    return unorm8(out[0]) | (unorm8(out[1]) << 8) | (unorm8(out[2]) << 16) | (unorm8(out[3]) << 24);
+    return (unorm8(out[0]) & 255u) | ((unorm8(out[1]) & 255u) << 8) | ((unorm8(out[2]) & 255u) << 16) |
+           ((unorm8(out[3]) & 255u) << 24);
 }
 
 __global__ void __launch_bounds__(kThreads) ortho_kernel(const tp::OrthoLaunch L)
 {
     extern __shared__ __align__(16) uint32_t win[];   // parent window, (W/2 + 2) rows of wp words
     __shared__ int unit;
+    __shared__ float inv255[256];
+    for (int k = threadIdx.x; k < 256; k += kThreads) inv255[k] = __fdiv_rn((float)k, 255.0f);
     const int W = L.W, n = W - 4, wp = L.win_pitch;
     const int NQ = W / 4;
     for (;;) {
@@ -207,23 +233,25 @@ __global__ void __launch_bounds__(kThreads) ortho_kernel(const tp::OrthoLaunch L
                 }
                 if (has_parent) {
                     // masks (1,3,3,9), (3,1,9,3), (3,9,1,3), (9,3,3,1) over the texels
-                    // (px, py), (px + 1, py), (px, py + 1), (px + 1, py + 1)
+                    // (px, py), (px + 1, py), (px, py + 1), (px + 1, py + 1): the integer
+                    // sums (exact, as in float) by byte dot products, channel by channel
                     const int lp = (k + 1) / 2;  // ((i0 + k + 1) / 2) - 2q
-                    const bool ox = k & 1, oy = j & 1;
-                    const float m0 = ox ? (oy ? 9.0f : 3.0f) : (oy ? 3.0f : 1.0f);
-                    const float m1 = ox ? (oy ? 3.0f : 1.0f) : (oy ? 9.0f : 3.0f);
-                    const float m2 = ox ? (oy ? 3.0f : 9.0f) : (oy ? 1.0f : 3.0f);
-                    const float m3 = ox ? (oy ? 1.0f : 3.0f) : (oy ? 3.0f : 9.0f);
+                    const int mi = (k & 1) + 2 * (j & 1);
+                    const uint32_t mw = mi == 0 ? 0x09030301u : mi == 1 ? 0x03090103u : mi == 2 ? 0x03010903u
+                                                                                            : 0x01030309u;
+                    // transpose the four texels into four channel words [t0, t1, t2, t3]
+                    const uint32_t t0 = pa[lp], t1 = pa[lp + 1], t2 = pb[lp], t3 = pb[lp + 1];
+                    const uint32_t lo01 = __byte_perm(t0, t1, 0x5140u), hi01 = __byte_perm(t0, t1, 0x7362u);
+                    const uint32_t lo23 = __byte_perm(t2, t3, 0x5140u), hi23 = __byte_perm(t2, t3, 0x7362u);
+                    const uint32_t ch[4] = {__byte_perm(lo01, lo23, 0x5410u), __byte_perm(lo01, lo23, 0x7632u),
+                                            __byte_perm(hi01, hi23, 0x5410u), __byte_perm(hi01, hi23, 0x7632u)};
 #pragma unroll
                     for (int c = 0; c < 4; ++c) {
-                        // integer-valued products and sums: exact in any order
-                        const float s = m0 * byte_of(pa[lp], c) + m1 * byte_of(pa[lp + 1], c) +
-                                        m2 * byte_of(pb[lp], c) + m3 * byte_of(pb[lp + 1], c);
-                        const float cc = floorf(s * 0.0625f);
+                        const float cc = int_to_f((uint32_t)__dp4a(ch[c], mw, 0u) >> 4);   // floor(s / 16)
                         r[c] = a_(m_(s_(r[c], 128.0f), rscale), cc);
                     }
                 }
-                o[k] = texel(r, nv, nc, hsv);
+                o[k] = texel(r, nv, nc, hsv, inv255);
             }
             *reinterpret_cast<uint4 *>(out + (long long)j * L.pitch + i0) = make_uint4(o[0], o[1], o[2], o[3]);
         }
