@@ -535,14 +535,14 @@ def planet_section(tp, torch, stream, sh, args, trained):
         t_all = time.perf_counter()
         for _ in range(steps):
             t0 = time.perf_counter()
-            for s0 in range(0, len(pf.learned_jobs), pf.chunk):
-                net.predict_residuals(pf.elev, pf.learned_jobs[s0:s0 + pf.chunk], pf.res, sh)
+            for arr in pf.learned_chunks:
+                net.predict_residuals(pf.elev, arr, pf.res, sh)
             stream.synchronize()
             t1 = time.perf_counter()
             pf.frame.graph_launch(sh)
             stream.synchronize()
             t2 = time.perf_counter()
-            tp.normal_batch(pf.elev, pf.nrm, pf.all_jobs, pf.root, sh)
+            tp.normal_batch(pf.elev, pf.nrm, pf.all_jobs_arr, pf.root, sh)
             stream.synchronize()
             t3 = time.perf_counter()
             parts["learned"] += t1 - t0

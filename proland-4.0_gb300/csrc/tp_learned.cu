@@ -15,6 +15,7 @@
 // operand tile brought in by TMA at the tap's offset; a CTA accumulates its blocks
 // in tensor memory and adds its sums to the gradient once at the end.
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 #include <map>
@@ -37,22 +38,74 @@ constexpr int kHaloBytes = kRowStride * kHaloY;             // one channel group
 constexpr int kGroupStride = (kHaloBytes + 127) / 128 * 128;  // 2944: TMA destinations 128-byte aligned
 constexpr int kBoxBytes = 8 * kBlockX * kBlockY * 2;        // one 8-channel group of a block: 2048
 
-// GELU in its tanh form, 0.5 z (1 + tanh(sqrt(2/pi) (z + 0.044715 z^3))), on the SFU's tanh.
-__device__ __forceinline__ float tanh_sfu(float x)
+// GELU in its tanh form, 0.5 z (1 + tanh(sqrt(2/pi) (z + 0.044715 z^3))), on channel
+// pairs: the polynomial in packed f32x2 arithmetic, tanh on the SFU as one
+// tanh.approx.f16x2 per pair (the precision class of tanh.approx.f32, about 2^-11
+// relative), the result back in f32.
+__device__ __forceinline__ uint64_t pk2(float a, float b)
 {
-    float y;
-    asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
-    return y;
+    uint64_t r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+    return r;
 }
-__device__ __forceinline__ float gelu(float z)
+__device__ __forceinline__ void upk2(uint64_t r, float &a, float &b)
 {
-    const float t = tanh_sfu(0.7978845608028654f * (z + 0.044715f * z * z * z));
-    return 0.5f * z * (1.0f + t);
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(r));
 }
-__device__ __forceinline__ float gelu_grad(float z)
+__device__ __forceinline__ uint64_t mul2(uint64_t a, uint64_t b)
 {
-    const float t = tanh_sfu(0.7978845608028654f * (z + 0.044715f * z * z * z));
-    return 0.5f * (1.0f + t) + 0.5f * z * (1.0f - t * t) * 0.7978845608028654f * (1.0f + 0.134145f * z * z);
+    uint64_t d;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ uint64_t add2(uint64_t a, uint64_t b)
+{
+    uint64_t d;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ uint64_t fma2(uint64_t a, uint64_t b, uint64_t c)
+{
+    uint64_t d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+    return d;
+}
+__device__ __forceinline__ uint64_t tanh2(uint64_t x)
+{
+    float a, b;
+    upk2(x, a, b);
+    __half2 h = __floats2half2_rn(a, b);
+    uint32_t u = *reinterpret_cast<uint32_t *>(&h), t;
+    asm("tanh.approx.f16x2 %0, %1;" : "=r"(t) : "r"(u));
+    const float2 f = __half22float2(*reinterpret_cast<__half2 *>(&t));
+    return pk2(f.x, f.y);
+}
+__device__ __forceinline__ uint64_t splat2(float v) { return pk2(v, v); }
+
+// (v[j], v[j+1]) <- gelu(v[j], v[j+1])
+__device__ __forceinline__ void gelu_pair(float &x, float &y)
+{
+    const uint64_t z = pk2(x, y);
+    const uint64_t z3 = mul2(mul2(z, z), z);
+    const uint64_t u = mul2(fma2(z3, splat2(0.044715f), z), splat2(0.7978845608028654f));
+    const uint64_t t = tanh2(u);
+    const uint64_t h = mul2(z, splat2(0.5f));
+    upk2(fma2(h, t, h), x, y);  // 0.5 z + 0.5 z t
+}
+
+// (g[j], g[j+1]) <- g * gelu'(z) with gelu'(z) = 0.5 (1 + t) + 0.5 z (1 - t^2) sqrt(2/pi) (1 + 0.134145 z^2)
+__device__ __forceinline__ void gelu_grad_pair(float &gx, float &gy, float zx, float zy)
+{
+    const uint64_t z = pk2(zx, zy);
+    const uint64_t z2 = mul2(z, z);
+    const uint64_t u = mul2(fma2(mul2(z2, z), splat2(0.044715f), z), splat2(0.7978845608028654f));
+    const uint64_t t = tanh2(u);
+    const uint64_t half_ = splat2(0.5f);
+    const uint64_t a = fma2(half_, t, half_);                                          // 0.5 (1 + t)
+    const uint64_t omt2 = fma2(mul2(t, t), splat2(-1.0f), splat2(1.0f));               // 1 - t^2
+    const uint64_t p = fma2(z2, splat2(0.134145f), splat2(1.0f));                       // 1 + 0.134145 z^2
+    const uint64_t b = mul2(mul2(mul2(z, half_), omt2), mul2(p, splat2(0.7978845608028654f)));
+    upk2(mul2(add2(a, b), pk2(gx, gy)), gx, gy);
 }
 
 __device__ __forceinline__ uint32_t pack2(float a, float b)
@@ -217,31 +270,26 @@ __global__ void __launch_bounds__(kRoleThreads) conv_kernel(const __grid_constan
             if (px < a.W && py < a.W) {
                 const size_t plane = (size_t)Wp * Wp, pix = (size_t)(py + 1) * Wp + (px + 1);
                 if (MODE == kHidden) {
-                    const float4 *b4 = reinterpret_cast<const float4 *>(bias_s);
+                    const float2 *b2 = reinterpret_cast<const float2 *>(bias_s);
                     if (a.emb) {
-                        const float4 *e4 = reinterpret_cast<const float4 *>(
+                        const float2 *e2 = reinterpret_cast<const float2 *>(
                             a.emb + (size_t)min(max(a.level[img], 0), kLevels - 1) * COUT);
 #pragma unroll
-                        for (int j = 0; j < COUT / 4; ++j) {
-                            const float4 bb = b4[j], ee = __ldg(e4 + j);
-                            acc[4 * j] += bb.x + ee.x;
-                            acc[4 * j + 1] += bb.y + ee.y;
-                            acc[4 * j + 2] += bb.z + ee.z;
-                            acc[4 * j + 3] += bb.w + ee.w;
+                        for (int j = 0; j < COUT / 2; ++j) {
+                            const float2 bb = b2[j], ee = __ldg(e2 + j);
+                            upk2(add2(pk2(acc[2 * j], acc[2 * j + 1]), add2(pk2(bb.x, bb.y), pk2(ee.x, ee.y))),
+                                 acc[2 * j], acc[2 * j + 1]);
                         }
                     } else {
 #pragma unroll
-                        for (int j = 0; j < COUT / 4; ++j) {
-                            const float4 bb = b4[j];
-                            acc[4 * j] += bb.x;
-                            acc[4 * j + 1] += bb.y;
-                            acc[4 * j + 2] += bb.z;
-                            acc[4 * j + 3] += bb.w;
+                        for (int j = 0; j < COUT / 2; ++j) {
+                            const float2 bb = b2[j];
+                            upk2(add2(pk2(acc[2 * j], acc[2 * j + 1]), pk2(bb.x, bb.y)), acc[2 * j], acc[2 * j + 1]);
                         }
                     }
                     if (a.zsave) store_bf16<COUT>(a.zsave, img, plane, pix, acc);
 #pragma unroll
-                    for (int j = 0; j < COUT; ++j) acc[j] = gelu(acc[j]);
+                    for (int j = 0; j < COUT; j += 2) gelu_pair(acc[j], acc[j + 1]);
                     store_bf16<COUT>(a.out, img, plane, pix, acc);
                 } else if (MODE == kLast) {
                     a.out_f32[((size_t)img * a.W + py) * a.W + px] = acc[0] + bias_s[0];
@@ -249,7 +297,7 @@ __global__ void __launch_bounds__(kRoleThreads) conv_kernel(const __grid_constan
                     float z[COUT];
                     load_bf16<COUT>(a.zprev, img, plane, pix, z);
 #pragma unroll
-                    for (int j = 0; j < COUT; ++j) acc[j] *= gelu_grad(z[j]);
+                    for (int j = 0; j < COUT; j += 2) gelu_grad_pair(acc[j], acc[j + 1], z[j], z[j + 1]);
                     store_bf16<COUT>(a.out, img, plane, pix, acc);
                 }
             }

@@ -116,10 +116,15 @@ def elevation_batch(elev, residuals, normals, params, jobs, stream=None):
                                    arr, len(jobs), stream))
 
 
+def job_array(jobs):
+    """A ctypes TileJob array of a job list (build once, pass to the batch calls)."""
+    return jobs if isinstance(jobs, C.Array) else (TileJob * len(jobs))(*jobs)
+
+
 def normal_batch(elev, normals, jobs, root_quad_size=0.0, stream=None):
     """Normal tiles of produced elevation tiles (tp_normal_batch); sphere normals
-    when root_quad_size > 0."""
-    arr = (TileJob * len(jobs))(*jobs)
+    when root_quad_size > 0.  jobs: a list of TileJob or a job_array."""
+    arr = job_array(jobs)
     check(lib().tp_normal_batch(elev.handle, normals.handle, arr, len(jobs), float(root_quad_size), stream))
 
 

@@ -180,7 +180,8 @@ class LearnedPredictor:
                                       _stream()))
 
     def predict_residuals(self, elev, jobs, residuals, stream=None):
-        arr = (TileJob * len(jobs))(*jobs)
+        """jobs: a list of TileJob, or a ctypes TileJob array built once by the caller."""
+        arr = jobs if isinstance(jobs, C.Array) else (TileJob * len(jobs))(*jobs)
         check(lib().tp_learned_predict_residuals(self.handle, elev.handle, arr, len(jobs), residuals.handle, stream))
 
 

@@ -73,13 +73,17 @@ class PlanetFrame:
         self.frame.add(self.elev, self.res, None, make_params(), flat)
         self.learned_jobs = [self.all_jobs[k] for k in self.learned_idx]
         self.chunk = chunk
+        # the frame's job arrays in C form, built once (a renderer keeps its requests so)
+        from . import job_array
+        self.all_jobs_arr = job_array(self.all_jobs)
+        self.learned_chunks = [job_array(self.learned_jobs[s:s + chunk]) for s in range(0, len(self.learned_jobs), chunk)]
 
     def produce(self, stream=None):
         if self.net is not None:
-            for s in range(0, len(self.learned_jobs), self.chunk):
-                self.net.predict_residuals(self.elev, self.learned_jobs[s:s + self.chunk], self.res, stream)
+            for arr in self.learned_chunks:
+                self.net.predict_residuals(self.elev, arr, self.res, stream)
         self.frame.graph_launch(stream)
-        normal_batch(self.elev, self.nrm, self.all_jobs, self.root, stream)
+        normal_batch(self.elev, self.nrm, self.all_jobs_arr, self.root, stream)
 
     def fp64_errors(self, oracle, per_level=2, seed=0):
         """Per level: max / RMS height error of zf and max / RMS normal-angle error
