@@ -372,6 +372,21 @@ int tp_ortho_batch(tp_storage *ortho, tp_storage *residuals, const tp_ortho_para
 int tp_ortho_batch_device(tp_storage *ortho, tp_storage *residuals, const tp_ortho_params *params,
                           const tp_ortho_job *jobs_dev, int n, void *stream);
 
+/* The ortho producers behind the TileCache / TileProducer protocol above
+ * (tp_producer_get_tile / put_tile / has_tile / border, tp_scheduler_run,
+ * tp_create_tiles).  tp_ortho_residual_producer_create is OrthoCPUProducer
+ * (OrthoCPUProducer.cpp:70-254): tiles of an ortho .dat file decoded on the host
+ * and uploaded as RGBA8 texels, or, with no file, zero tiles at levels 0 and 1;
+ * its cache holds one-channel slots of width tileSize + 2 border.
+ * tp_ortho_producer_create is OrthoProducer (OrthoProducer.cpp:145-382): a tile
+ * needs its parent (level > 0) and, where the residual producer has one, the
+ * residual tile of the same (level, tx, ty); noise_amp as its `noise` attribute,
+ * face as its `face` (tp_noise_select), max_level -1 for no limit (hasTile).  A
+ * scheduler run produces all queued ortho tiles in one launch, parents first. */
+int tp_ortho_residual_producer_create(tp_cache *cache, const char *file, tp_producer **out);
+int tp_ortho_producer_create(tp_cache *cache, tp_producer *residuals, const tp_ortho_params *params,
+                             const float *noise_amp, int n_noise, int face, int max_level, tp_producer **out);
+
 /* OrthoCPUProducer's pyramids (OrthoCPUProducer.cpp:70-236): a header of 7
  * int32 {maxLevel, tileSize, channels, root, tx, ty, flags} (flags bit 0: DXT
  * tiles, bit 1: tiles without border), 2 * ntiles int64 offsets, one

@@ -28,7 +28,7 @@
 
 namespace {
 
-enum Kind { kResidual = 0, kElevation = 1, kNormal = 2 };
+enum Kind { kResidual = 0, kElevation = 1, kNormal = 2, kOrthoResidual = 3, kOrtho = 4 };
 using TKey = std::tuple<int, int, int, int>;  // producer id, level, tx, ty
 
 int next_producer_id()
@@ -89,6 +89,13 @@ struct tp_producer {
     int normal_format = 2;  // 0..3 (NormalProducer.cpp:195); 0/1 add coarse normals
     int device_decode = 0;  // residual producer over a .dat file: decode tiles on the device
     int grid_mesh = 24;
+    // ortho residual producer (OrthoCPUProducer): tiles of an ortho .dat file, or zeros
+    tp_ortho_dat *odat = nullptr;
+    int ortho_max_level = 1;
+    int ortho_border = 2;
+    // ortho producer (OrthoProducer); residuals, noise_amp and face as above
+    tp_ortho_params oparams{};
+    int max_level = -1;
 };
 
 namespace {
@@ -232,6 +239,22 @@ int schedule(tp_producer *p, tp_tile *t)
                 }
                 t->dep_input_owner = p->residuals;
             }
+        }
+    } else if (p->kind == kOrtho) {
+        // OrthoProducer::startCreateTile (OrthoProducer.cpp:245-264): the parent tile and the
+        // residual tile of the same (level, tx, ty)
+        if (t->level > 0) {
+            t->dep_parent = get_tile(p, t->level - 1, t->tx / 2, t->ty / 2, nullptr, &err);
+            if (!t->dep_parent) return err ? err : tp::fail(TP_E_CACHE_FULL, "cache full (ortho parent)");
+            t->dep_parent_owner = p;
+        }
+        if (p->residuals && tp_producer_has_tile(p->residuals, t->level, t->tx, t->ty) == 1) {
+            t->dep_input = get_tile(p->residuals, t->level, t->tx, t->ty, nullptr, &err);
+            if (!t->dep_input) {
+                release_deps(t);
+                return err ? err : tp::fail(TP_E_CACHE_FULL, "cache full (ortho residual)");
+            }
+            t->dep_input_owner = p->residuals;
         }
     } else if (p->kind == kNormal) {
         t->dep_input = get_tile(p->elevations, t->level, t->tx, t->ty, nullptr, &err);
@@ -457,6 +480,57 @@ extern "C" int tp_normal_producer_create(tp_cache *cache, tp_producer *elevation
     return TP_OK;
 }
 
+extern "C" int tp_ortho_residual_producer_create(tp_cache *cache, const char *file, tp_producer **out)
+{
+    if (!cache || !out) return tp::fail(TP_E_BAD_ARG, "tp_ortho_residual_producer_create: bad arguments");
+    *out = nullptr;
+    if (cache->storage->channels != 1) return tp::fail(TP_E_BAD_ARG, "ortho residual cache must hold RGBA8 texels (1 channel)");
+    tp_ortho_dat *d = nullptr;
+    int max_level = 1, border = 2;  // OrthoCPUProducer.cpp:73-78: no file, zero tiles at levels 0 and 1
+    if (file && file[0]) {
+        int rc = tp_ortho_dat_open(file, &d);
+        if (rc) return rc;
+        int info[8];
+        tp_ortho_dat_info(d, info);
+        max_level = info[0];
+        border = (info[6] & 2) ? 0 : 2;
+        if ((info[6] & 1) || info[1] + 2 * border != cache->storage->W) {
+            tp_ortho_dat_close(d);
+            return tp::fail(TP_E_BAD_ARG, "ortho residual cache width must be the file's tileSize + 2 border (no DXT)");
+        }
+    }
+    tp_producer *p = new_producer(kOrthoResidual, cache);
+    p->odat = d;
+    p->own_dat = d != nullptr;
+    p->ortho_max_level = max_level;
+    p->ortho_border = border;
+    *out = p;
+    return TP_OK;
+}
+
+extern "C" int tp_ortho_producer_create(tp_cache *cache, tp_producer *residuals, const tp_ortho_params *params,
+                                        const float *noise_amp, int n_noise, int face, int max_level,
+                                        tp_producer **out)
+{
+    if (!cache || !params || !out || n_noise < 0 || (n_noise > 0 && !noise_amp) || max_level < -1)
+        return tp::fail(TP_E_BAD_ARG, "tp_ortho_producer_create: bad arguments");
+    *out = nullptr;
+    const tp_storage *s = cache->storage;
+    if (s->channels != 1 || s->W % 4 != 0)
+        return tp::fail(TP_E_BAD_ARG, "ortho cache must hold RGBA8 texels (1 channel) of a width that is a multiple of 4");
+    if (residuals && (residuals->kind != kOrthoResidual || residuals->cache->storage->W != s->W ||
+                      residuals->ortho_border != 2))
+        return tp::fail(TP_E_BAD_ARG, "ortho residuals must be an ortho residual producer of the same width, border 2");
+    tp_producer *p = new_producer(kOrtho, cache);
+    p->residuals = residuals;
+    p->oparams = *params;
+    p->noise_amp.assign(noise_amp, noise_amp + n_noise);
+    p->face = face;
+    p->max_level = max_level;
+    *out = p;
+    return TP_OK;
+}
+
 extern "C" int tp_residual_producer_set_device_decode(tp_producer *p, int on)
 {
     if (!p || p->kind != kResidual) return tp::fail(TP_E_BAD_ARG, "tp_residual_producer_set_device_decode: not a residual producer");
@@ -483,7 +557,8 @@ extern "C" int tp_producer_destroy(tp_producer *p)
         tp::g_producers.erase(p->id);
     }
     if (p->frame) tp_frame_destroy(p->frame);
-    if (p->own_dat) tp_dat_close(p->dat);
+    if (p->own_dat && p->dat) tp_dat_close(p->dat);
+    if (p->own_dat && p->odat) tp_ortho_dat_close(p->odat);
     delete p;
     return TP_OK;
 }
@@ -493,14 +568,15 @@ extern "C" int tp_producer_id(const tp_producer *p) { return p ? p->id : TP_E_BA
 extern "C" int tp_producer_border(const tp_producer *p)
 {
     if (!p) return TP_E_BAD_ARG;
-    return p->kind == kNormal ? 0 : 2;  // ElevationProducer.cpp:235-239, NormalProducer.cpp:124-127
+    if (p->kind == kOrthoResidual) return p->ortho_border;  // OrthoCPUProducer.cpp:98, 145-148
+    return p->kind == kNormal ? 0 : 2;  // ElevationProducer.cpp:235-239, NormalProducer.cpp:124-127, OrthoProducer.cpp:217-221
 }
 
 extern "C" int tp_producer_set_root_quad_size(tp_producer *p, float size)
 {
     if (!p || !(size > 0.0f)) return tp::fail(TP_E_BAD_ARG, "tp_producer_set_root_quad_size: bad arguments");
     p->root_quad_size = size;
-    if (p->kind == kElevation && p->residuals) p->residuals->root_quad_size = size;
+    if ((p->kind == kElevation || p->kind == kOrtho) && p->residuals) p->residuals->root_quad_size = size;
     if (p->kind == kNormal) tp_producer_set_root_quad_size(p->elevations, size);
     return TP_OK;
 }
@@ -509,6 +585,9 @@ extern "C" int tp_producer_has_tile(const tp_producer *p, int level, int tx, int
 {
     if (!p) return TP_E_BAD_ARG;
     if (p->kind == kResidual) return residual_has_tile(p, level, tx, ty) ? 1 : 0;
+    if (level < 0 || tx < 0 || ty < 0 || level > 30 || (tx >> level) != 0 || (ty >> level) != 0) return 0;
+    if (p->kind == kOrthoResidual) return level <= p->ortho_max_level ? 1 : 0;  // OrthoCPUProducer.cpp:151-154
+    if (p->kind == kOrtho) return p->max_level == -1 || level <= p->max_level ? 1 : 0;  // OrthoProducer.cpp:223-226
     if (p->kind == kNormal) return tp_producer_has_tile(p->elevations, level, tx, ty);
     return level >= 0 && tx >= 0 && ty >= 0 && (tx >> level) == 0 && (ty >> level) == 0 ? 1 : 0;
 }
@@ -845,6 +924,80 @@ int run_normals(tp_producer *np, void *stream)
     return TP_OK;
 }
 
+// OrthoCPUProducer::doCreateTile (OrthoCPUProducer.cpp:170-236): decoded tiles (or zeros
+// without a file) as RGBA8 texels, uploaded to their slots in one copy.
+int run_ortho_residuals(tp_producer *r, void *stream)
+{
+    if (r->queue.empty()) return TP_OK;
+    tp_storage *s = r->cache->storage;
+    const size_t per = (size_t)s->W * s->W;
+    std::vector<uint32_t> host(per * r->queue.size(), 0u);
+    std::vector<int> slots;
+    for (size_t k = 0; k < r->queue.size(); ++k) {
+        const tp_tile *t = r->queue[k];
+        if (r->odat) {
+            int w = 0;
+            int rc = tp_ortho_dat_read_rgba(r->odat, t->level, t->tx, t->ty, host.data() + k * per, (int)per, &w);
+            if (rc) return rc;
+        }
+        slots.push_back(t->slot);
+    }
+    if (s->on_device == 1) {
+        int rc = tp::staged_copy_slots(s, slots.data(), (int)slots.size(), 0,
+                                       reinterpret_cast<const float *>(host.data()), stream);
+        if (rc) return rc;
+        cudaError_t e = cudaStreamSynchronize(static_cast<cudaStream_t>(stream));
+        if (e != cudaSuccess) return tp::cuda_fail("cudaStreamSynchronize (ortho residual upload)", e);
+    }
+    for (tp_tile *t : r->queue) {
+        t->done = true;
+        t->queued = false;
+    }
+    r->queue.clear();
+    return TP_OK;
+}
+
+// OrthoProducer::doCreateTile (OrthoProducer.cpp:292-382) of every queued tile: one
+// persistent ortho launch, parents before children.
+int run_orthos(tp_producer *o, void *stream)
+{
+    if (o->queue.empty()) return TP_OK;
+    std::vector<tp_tile *> q = o->queue;
+    std::stable_sort(q.begin(), q.end(), [](const tp_tile *a, const tp_tile *b) { return a->level < b->level; });
+    std::map<const tp_tile *, int> index;
+    for (size_t k = 0; k < q.size(); ++k) index[q[k]] = (int)k;
+    std::vector<tp_ortho_job> jobs(q.size());
+    for (size_t k = 0; k < q.size(); ++k) {
+        const tp_tile *t = q[k];
+        tp_ortho_job &j = jobs[k];
+        std::memset(&j, 0, sizeof j);
+        j.level = t->level;
+        j.tx = t->tx;
+        j.ty = t->ty;
+        j.out_slot = t->slot;
+        j.parent_slot = t->dep_parent ? t->dep_parent->slot : -1;
+        j.parent_job = -1;
+        if (t->dep_parent) {
+            auto it = index.find(t->dep_parent);
+            if (it != index.end()) j.parent_job = it->second;
+            else if (!t->dep_parent->done) return tp::fail(TP_E_MISSING_PARENT, "ortho parent tile is not produced");
+        }
+        j.residual_slot = t->dep_input ? t->dep_input->slot : -1;
+        tp_noise_select(o->face, t->level, t->tx, t->ty, &j.noise_rot, &j.noise_layer);
+        j.noise_amp = t->level < (int)o->noise_amp.size() ? o->noise_amp[t->level] : 0.0f;
+    }
+    int rc = tp_ortho_batch(o->cache->storage, o->residuals ? o->residuals->cache->storage : nullptr, &o->oparams,
+                            jobs.data(), (int)jobs.size(), stream);
+    if (rc) return rc;
+    for (tp_tile *t : q) {
+        t->done = true;
+        t->queued = false;
+        release_deps(t);
+    }
+    o->queue.clear();
+    return TP_OK;
+}
+
 }  // namespace
 
 // Produces every queued tile of the given producers (and of the producers they
@@ -852,13 +1005,22 @@ int run_normals(tp_producer *np, void *stream)
 extern "C" int tp_scheduler_run(tp_producer *const *producers, int n, void *stream)
 {
     if (n < 0 || (n > 0 && !producers)) return tp::fail(TP_E_BAD_ARG, "tp_scheduler_run: bad arguments");
-    std::vector<tp_producer *> res, elev, nrm;
+    std::vector<tp_producer *> res, elev, nrm, ores, orth;
     auto add = [](std::vector<tp_producer *> &v, tp_producer *p) {
         if (p && std::find(v.begin(), v.end(), p) == v.end()) v.push_back(p);
     };
     for (int k = 0; k < n; ++k) {
         tp_producer *p = producers[k];
         if (!p) continue;
+        if (p->kind == kOrtho) {
+            add(orth, p);
+            if (p->residuals) add(ores, p->residuals);
+            continue;
+        }
+        if (p->kind == kOrthoResidual) {
+            add(ores, p);
+            continue;
+        }
         if (p->kind == kNormal) {
             add(nrm, p);
             p = p->elevations;
@@ -885,6 +1047,14 @@ extern "C" int tp_scheduler_run(tp_producer *const *producers, int n, void *stre
     }
     for (tp_producer *np : nrm) {
         int rc = run_normals(np, stream);
+        if (rc) return rc;
+    }
+    for (tp_producer *r : ores) {
+        int rc = run_ortho_residuals(r, stream);
+        if (rc) return rc;
+    }
+    for (tp_producer *o : orth) {
+        int rc = run_orthos(o, stream);
         if (rc) return rc;
     }
     return TP_OK;

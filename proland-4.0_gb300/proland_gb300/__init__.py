@@ -498,6 +498,29 @@ class NormalProducer(TileProducer):
         check(lib().tp_normal_producer_set_format(self.handle, fmt, grid_mesh))
 
 
+class OrthoResidualProducer(TileProducer):
+    """OrthoCPUProducer: RGBA8 tiles of an ortho .dat pyramid (or zero tiles without a
+    file) in a one-channel cache of width tileSize + 2 border."""
+
+    def __init__(self, cache, file=""):
+        h = C.c_void_p()
+        check(lib().tp_ortho_residual_producer_create(cache.handle, (file or "").encode(), C.byref(h)))
+        super().__init__(h, cache)
+
+
+class OrthoProducer(TileProducer):
+    """OrthoProducer: colour tiles upsampled from their parent, plus residuals and noise."""
+
+    def __init__(self, cache, residuals=None, params=None, noise_amp=(), face=1, max_level=-1):
+        h = C.c_void_p()
+        amps = (C.c_float * max(1, len(noise_amp)))(*noise_amp)
+        check(lib().tp_ortho_producer_create(cache.handle, residuals.handle if residuals else None,
+                                             C.byref(params or make_ortho_params()), amps, len(noise_amp), face,
+                                             max_level, C.byref(h)))
+        super().__init__(h, cache)
+        self.residuals = residuals
+
+
 def scheduler_run(producers, stream=None):
     """Produces every queued tile of the producers (tp_scheduler_run)."""
     arr = (C.c_void_p * len(producers))(*[p.handle for p in producers])

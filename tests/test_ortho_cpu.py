@@ -163,3 +163,34 @@ def test_hsv_mode_keeps_grey_and_darkens_little_on_bright(oracle_lib):
     out = oracle_lib.ortho_tile(W, 1, 0, 0, bright, None, table[1], 1, 255.0, noise_color=(0.3, 0.3, 0.3, 1.0),
                                 hsv=True)
     assert np.abs(out[..., :3].astype(int) - bright[..., :3].astype(int)).max() <= 1
+
+
+def test_ortho_producer_protocol_on_bookkeeping_storages(product):
+    """getTile of an ortho tile acquires its parent chain and its residual (where the
+    residual producer has one), queues them, and releases nothing until produced;
+    hasTile and getBorder follow OrthoProducer / OrthoCPUProducer."""
+    tp = product
+    W = 196
+    oc = tp.TileCache(tp.TileStorage(W, 1, 16, on_device=tp.TileStorage.BOOKKEEPING), "ortho")
+    rc = tp.TileCache(tp.TileStorage(W, 1, 8, on_device=tp.TileStorage.BOOKKEEPING), "orthoCpu")
+    res = tp.OrthoResidualProducer(rc, MINI)
+    orth = tp.OrthoProducer(oc, res, tp.make_ortho_params(), noise_amp=[255.0] * 17, face=1, max_level=5)
+    assert res.get_border() == 2 and orth.get_border() == 2
+    assert res.has_tile(1, 1, 0) and not res.has_tile(2, 0, 0)          # maxLevel of the file is 1
+    assert orth.has_tile(5, 31, 31) and not orth.has_tile(6, 0, 0)       # maxLevel attribute
+    t = orth.get_tile(2, 3, 1)
+    assert t is not None
+    # the tile, its parent (1, 1, 0) and grandparent (0, 0, 0) are queued; the residual
+    # producer queued the two levels it has
+    assert orth.queued() == 3 and res.queued() == 2
+    assert oc.get_used_tiles() == 3 and rc.get_used_tiles() == 2
+    # a second request of a sibling reuses the queued parents
+    t2 = orth.get_tile(2, 2, 1)
+    assert orth.queued() == 4 and res.queued() == 2
+    assert orth.put_tile(t2) == 0 and orth.put_tile(t) == 0
+    # no file: zero tiles at levels 0 and 1 only (OrthoCPUProducer with an empty name)
+    zc = tp.TileCache(tp.TileStorage(W, 1, 4, on_device=tp.TileStorage.BOOKKEEPING), "zeros")
+    z = tp.OrthoResidualProducer(zc)
+    assert z.has_tile(1, 1, 1) and not z.has_tile(2, 0, 0)
+    with pytest.raises(tp.TPError):
+        tp.OrthoProducer(tp.TileCache(tp.TileStorage(197, 1, 4, on_device=tp.TileStorage.BOOKKEEPING)), None)
