@@ -320,8 +320,12 @@ __device__ __forceinline__ void compute_unit(const tp::ClassLaunch &c, int job, 
             wr0 = pc - 1;
         };
         const bool edge = i0 + 3 >= W;  // the quad holding the last sample column and the padding
-        auto row = [&](int j, const uint2 h, auto odd_tag) {
+        // HP_ (the tile has a parent) and NZ_ (noise amplitude non-zero) are uniform per
+        // tile: the row code is specialised on them (no per-row tests of either)
+        auto row = [&](int j, const uint2 h, auto odd_tag, auto hp_tag, auto nz_tag) {
             constexpr bool ODD = decltype(odd_tag)::value;
+            constexpr bool HP_ = decltype(hp_tag)::value;
+            constexpr bool NZ_ = decltype(nz_tag)::value;
             float *brow = sbuf + (j - j0 + 1) * PE + i0;
             const float4 r4 = *reinterpret_cast<const float4 *>(brow);
             // (a tile without residual has a zeroed buffer: rscale * 0 == 0)
@@ -330,7 +334,7 @@ __device__ __forceinline__ void compute_unit(const tp::ClassLaunch &c, int job, 
             zf[1] = __fmul_rn(rscale, r4.y);
             zf[2] = __fmul_rn(rscale, r4.z);
             zf[3] = __fmul_rn(rscale, r4.w);
-            if (noisy) {
+            if constexpr (NZ_) {
                 const float2 n01 = __half22float2(*reinterpret_cast<const __half2 *>(&h.x));
                 const float2 n23 = __half22float2(*reinterpret_cast<const __half2 *>(&h.y));
                 const float nv[4] = {n01.x, n01.y, n23.x, n23.y};
@@ -355,7 +359,7 @@ __device__ __forceinline__ void compute_unit(const tp::ClassLaunch &c, int job, 
                 }
             }
             float zc[4] = {zf[0], zf[1], zf[2], zf[3]};
-            if (has_parent) {
+            if constexpr (HP_) {
                 float up[4];
                 if constexpr (!ODD) {
                     up[0] = P[1][1];
@@ -448,16 +452,36 @@ __device__ __forceinline__ void compute_unit(const tp::ClassLaunch &c, int job, 
         };
         using Even = std::integral_constant<bool, false>;
         using Odd = std::integral_constant<bool, true>;
-        // noise rows come from L2: the next row's quad is fetched one row ahead
-        uint2 nzh = make_uint2(0u, 0u);
-        if (noisy && rbeg < rend) nzh = __ldg(reinterpret_cast<const uint2 *>(c.noise + nzo + rbeg * PE));
+        // noise rows come from L2, each fetched one row ahead
+        auto strip = [&](auto hp_tag, auto nz_tag) {
+            constexpr bool HP_ = decltype(hp_tag)::value;
+            constexpr bool NZ_ = decltype(nz_tag)::value;
+            uint2 nzh = make_uint2(0u, 0u);
+            if constexpr (NZ_) {
+                if (rbeg < rend) nzh = __ldg(reinterpret_cast<const uint2 *>(c.noise + nzo + rbeg * PE));
+            }
+            auto step = [&](int j, auto odd_tag) {
+                const uint2 h = nzh;
+                if constexpr (NZ_) {
+                    if (j + 1 < rend) nzh = __ldg(reinterpret_cast<const uint2 *>(c.noise + nzo + (j + 1) * PE));
+                }
+                if constexpr (HP_) advance(j / 2 + 1 + dy - pr0);  // (even, odd) rows share the stencil centre row
+                row(j, h, odd_tag, hp_tag, nz_tag);
+            };
 #pragma unroll 1
-        for (int j = rbeg; j < rend; ++j) {
-            const uint2 h = nzh;
-            if (noisy && j + 1 < rend) nzh = __ldg(reinterpret_cast<const uint2 *>(c.noise + nzo + (j + 1) * PE));
-            if (has_parent) advance(j / 2 + 1 + dy - pr0);  // (even, odd) rows share the stencil centre row
-            if (j & 1) row(j, h, Odd{});
-            else row(j, h, Even{});
+            for (int j = rbeg; j < rend; ++j) {
+                if (j & 1) step(j, Odd{});
+                else step(j, Even{});
+            }
+        };
+        using T_ = std::integral_constant<bool, true>;
+        using F_ = std::integral_constant<bool, false>;
+        if (has_parent) {
+            if (noisy) strip(T_{}, T_{});
+            else strip(T_{}, F_{});
+        } else {
+            if (noisy) strip(F_{}, T_{});
+            else strip(F_{}, F_{});
         }
     }
     __syncthreads();
