@@ -20,8 +20,8 @@
 // each side), writing the band rows to HBM with 16-byte stores and each row's zm
 // over its residual in shared memory; every thread sweeps one column quad down a
 // strip of rows holding the four parent rows its stencil reads in registers.
-// Phase B forms the normals of the band rows from that zm: vertical neighbours
-// from the rows above and below, horizontal ones across quads by warp shuffles.
+// Phase B forms the normals of the band rows from that zm: each lane reads the
+// 8 columns around its quad of normals from the row and the rows above and below.
 //
 // Arithmetic follows the reference exactly:
 //  * stencil: CPUElevationProducer.cpp:202-238 (the same loops as
@@ -500,23 +500,20 @@ __device__ __forceinline__ void compute_unit(const tp::ClassLaunch &c, int job, 
             for (int base = 0; base < NQn; base += 32) {
                 const int m = base + lane;
                 const bool act = m < NQn;
-                const int e = act ? 4 * m + 2 : 2;  // elevation column of this quad's first normal
-                const float2 c01 = *reinterpret_cast<const float2 *>(cr + e);
-                const float2 c23 = *reinterpret_cast<const float2 *>(cr + e + 2);
-                const float2 u01 = *reinterpret_cast<const float2 *>(up + e);
-                const float2 u23 = *reinterpret_cast<const float2 *>(up + e + 2);
-                const float2 d01 = *reinterpret_cast<const float2 *>(dn + e);
-                const float2 d23 = *reinterpret_cast<const float2 *>(dn + e + 2);
-                // horizontal neighbours e - 1 and e + 4 live in the adjacent lanes' quads;
-                // the warp's first and last lanes read theirs from shared memory
-                const float lpatch = cr[e - 1], rpatch = cr[min(e + 4, PE - 1)];
-                float left = __shfl_up_sync(0xffffffffu, c23.y, 1);
-                float right = __shfl_down_sync(0xffffffffu, c01.x, 1);
-                left = lane == 0 ? lpatch : left;
-                right = (lane == 31 || m == NQn - 1) ? rpatch : right;
-                const float zr[6] = {left, c01.x, c01.y, c23.x, c23.y, right};
-                const float zu[4] = {u01.x, u01.y, u23.x, u23.y};
-                const float zd[4] = {d01.x, d01.y, d23.x, d23.y};
+                // elevation columns b .. b + 7 of the three rows as two aligned 16-byte loads
+                // each (conflict-free); this quad's normals sit at columns b + 2 .. b + 5 and
+                // read b + 1 .. b + 6.  b2 stays inside the row: a quad past the last normal
+                // column (its values unused) reads the row's last 16 bytes instead.
+                const int b = act ? 4 * m : 0, b2 = min(b + 4, PE - 4);
+                const float4 cA = *reinterpret_cast<const float4 *>(cr + b);
+                const float4 cB = *reinterpret_cast<const float4 *>(cr + b2);
+                const float4 uA = *reinterpret_cast<const float4 *>(up + b);
+                const float4 uB = *reinterpret_cast<const float4 *>(up + b2);
+                const float4 dA = *reinterpret_cast<const float4 *>(dn + b);
+                const float4 dB = *reinterpret_cast<const float4 *>(dn + b2);
+                const float zr[6] = {cA.y, cA.z, cA.w, cB.x, cB.y, cB.z};
+                const float zu[4] = {uA.z, uA.w, uB.x, uB.y};
+                const float zd[4] = {dA.z, dA.w, dB.x, dB.y};
                 float nx[4], ny[4];
 #pragma unroll
                 for (int k = 0; k < 4; ++k) {
