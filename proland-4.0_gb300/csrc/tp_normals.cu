@@ -58,13 +58,10 @@ __device__ __forceinline__ float sphere_blend(const tp::SphereFrame &f)
 }
 
 // getWorldPosition of terrain2/normalShader.glsl:56-73 (the patch's projective
-// mapping onto the sphere), for grid position (u, v) in samples and height h;
-// s = sphere_blend(f).
-__device__ __forceinline__ void sphere_pos(const tp::SphereFrame &f, float s, float n, float u, float v, float h,
-                                           float *out)
+// mapping onto the sphere), for grid position (u, v) = (un, vn) * n in samples
+// (un = u / n and vn = v / n, correctly rounded) and height h; s = sphere_blend(f).
+__device__ __forceinline__ void sphere_pos(const tp::SphereFrame &f, float s, float u, float v, float h, float *out)
 {
-    u = __fdiv_rn(u, n);
-    v = __fdiv_rn(v, n);
     const float U = s_(1.0f, u), V = s_(1.0f, v);
     const float al[4] = {m_(U, V), m_(u, V), m_(U, v), m_(u, v)};
     const float d = dot4(al, f.L);
@@ -91,12 +88,14 @@ __device__ __forceinline__ void sphere_pos(const tp::SphereFrame &f, float s, fl
 constexpr int kSphereBand = 16;
 constexpr int kSphereRing = kSphereBand + 2;
 
-__host__ __device__ constexpr int sphere_smem_floats(int W) { return 3 * kSphereRing * (W - 2); }
+// The ring, then the quotients k / n of the grid coordinates k in [-1, W - 4].
+__host__ __device__ constexpr int sphere_smem_floats(int W) { return 3 * kSphereRing * (W - 2) + (W - 2); }
 
 // Positions of grid rows v in [v0, v1) (v in [-1, W - 4]), columns u in [-1, W - 4],
-// heights from the zm plane (texel (u + 2, v + 2)), into the ring.
-__device__ __forceinline__ void sphere_rows(const tp::SphereFrame &F, float s, float nn, const float *__restrict__ zm,
-                                            int pitch, int W, int v0, int v1, float *ring)
+// heights from the zm plane (texel (u + 2, v + 2)), into the ring; qn[k + 1] = k / n.
+__device__ __forceinline__ void sphere_rows(const tp::SphereFrame &F, float s, const float *qn,
+                                            const float *__restrict__ zm, int pitch, int W, int v0, int v1,
+                                            float *ring)
 {
     const int PW = W - 2;
     float *X = ring, *Y = ring + kSphereRing * PW, *Z = ring + 2 * kSphereRing * PW;
@@ -105,7 +104,7 @@ __device__ __forceinline__ void sphere_rows(const tp::SphereFrame &F, float s, f
         const int r = i / PW;
         const int u = i - r * PW - 1, v = v0 + r;
         float o[3];
-        sphere_pos(F, s, nn, (float)u, (float)v, __ldg(zm + (long long)(v + 2) * pitch + (u + 2)), o);
+        sphere_pos(F, s, qn[u + 1], qn[v + 1], __ldg(zm + (long long)(v + 2) * pitch + (u + 2)), o);
         const int k = ((v + 1) % kSphereRing) * PW + (u + 1);
         X[k] = o[0];
         Y[k] = o[1];
@@ -143,10 +142,13 @@ __device__ __forceinline__ void sphere_tile(const tp::SphereFrame &F, const floa
     const int Wn = W - 4;
     const float nn = (float)(W - 5);
     const float s = sphere_blend(F);
-    sphere_rows(F, s, nn, zm, pitch, W, -1, min(kSphereBand, Wn) + 1, ring);
+    float *qn = ring + 3 * kSphereRing * (W - 2);
+    for (int k = threadIdx.x; k < W - 2; k += blockDim.x) qn[k] = __fdiv_rn((float)(k - 1), nn);
+    __syncthreads();
+    sphere_rows(F, s, qn, zm, pitch, W, -1, min(kSphereBand, Wn) + 1, ring);
     for (int q0 = 0; q0 < Wn; q0 += kSphereBand) {
         const int q1 = min(q0 + kSphereBand, Wn);
-        if (q0 > 0) sphere_rows(F, s, nn, zm, pitch, W, q0 + 1, q1 + 1, ring);
+        if (q0 > 0) sphere_rows(F, s, qn, zm, pitch, W, q0 + 1, q1 + 1, ring);
         __syncthreads();
         const int cnt = (q1 - q0) * Wn;
         for (int i = threadIdx.x; i < cnt; i += blockDim.x) {
