@@ -40,7 +40,9 @@ ROOT_QUAD = 100000.0          # meters: terrainNode size 50000 -> root quad 2 * 
 BYTES_PER_TILE = {101: 260960, 197: 1000544}   # algorithmic bytes (parent window, residual, elevation, normals)
 FALLBACK_HBM_GBS = 6800.0
 E2E_CHUNK = {101: 256, 197: 64}   # tiles per chunk of the host-buffer pipeline
-TRAFFIC_BYTES_PER_STEP = (207.4 + 574.2 + 238.1 + 741.3) * 1e6   # ncu dram__bytes_read/write of the two launches
+# ncu dram__bytes_read + dram__bytes_write of the two launches of one step (101-wide and
+# 197-wide classes) of the default 4096-request frame, from a one-pass launch list
+TRAFFIC_BYTES_PER_STEP = (208.2 + 573.8 + 240.1 + 741.6) * 1e6
 
 
 def hbm_peak():
@@ -718,8 +720,8 @@ def main():
     peak, peak_src = hbm_peak()
     alg = {fc.W: fc.n * BYTES_PER_TILE[fc.W] for fc in classes}
     achieved = sum(alg.values()) / (kernel_ms / 1000.0) / 1e9
-    # DRAM bytes of one step's launches (read + write) from the ncu launch list in
-    # profiles/frame_kernel_frame4096.md, for the default 4096-request frame only
+    # DRAM bytes of one step's launches (read + write) from an ncu launch list, measured
+    # for the default 4096-request frame only
     traffic = TRAFFIC_BYTES_PER_STEP if (args.requests == 4096 and args.seed == 2024) else None
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
