@@ -272,6 +272,14 @@ def residual_decode_rate(min_seconds=1.0):
     return res
 
 
+def workload_name(classes):
+    """The frame workload as both arms name it in their config."""
+    return ("frame: %d independent requests per GPU, levels 1-12, %d x 101 + %d x 197 tiles, "
+            "materialised fBm parents, residual sigma 2000*0.5^l, noise 300*0.55^l"
+            % (sum(fc.n for fc in classes), sum(fc.n for fc in classes if fc.W == 101),
+               sum(fc.n for fc in classes if fc.W == 197)))
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -296,8 +304,8 @@ def run_reference(args):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * total / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic",
-            "config": {"workload": "frame: %d requests, levels 1-12, 25%% 197-wide; CPU sample of %d tiles per step"
-                       % (args.requests, len(jobs)), "form": "plain"},
+            "config": {"workload": workload_name(classes), "form": "plain",
+                       "parallelism": "%d host threads, a bounded sample of the frame per step" % threads},
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
                              "sample": "%d tiles of the frame per step (3:1 101/197 mix)" % len(jobs)},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -727,10 +735,7 @@ def main():
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": "frame: %d independent requests per GPU, levels 1-12, %d x 101 + %d x 197 tiles, "
-                               "materialised fBm parents, residual sigma 2000*0.5^l, noise 300*0.55^l"
-                               % (tiles, sum(fc.n for fc in classes if fc.W == 101),
-                                  sum(fc.n for fc in classes if fc.W == 197)),
+        "config": {"workload": workload_name(classes),
                    "form": "plain", "l2": "inputs larger than L2 (%.2f GB per step)" % (sum(alg.values()) / 1e9),
                    "parallelism": "replicas" if world > 1 else "single GPU", "autotuned": tuned},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
