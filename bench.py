@@ -361,6 +361,20 @@ def learned_flops(W):
     return used, executed
 
 
+# HBM bytes of one W x W tile's forward pass as the kernels move them: the input channels
+# made from the upsampled tile (fp32 read, 16 bf16 channels written), then per layer the
+# bf16 activations of (W + 2)^2 pixels read (zero border included) and W^2 written, the
+# last layer's fp32 channel, and the residual scaled out (fp32 read and write)
+def learned_bytes(W):
+    px, pxb = W * W, (W + 2) * (W + 2)
+    b = px * 4 + px * 16 * 2                  # prep
+    b += pxb * 16 * 2 + px * 32 * 2           # layer 0 (16 -> 32)
+    b += 3 * (pxb * 32 * 2 + px * 32 * 2)     # layers 1-3 (32 -> 32)
+    b += pxb * 32 * 2 + px * 4                # layer 4 (32 -> 1 used)
+    b += 2 * px * 4                           # scale
+    return b
+
+
 ORTHO_W = 196
 ORTHO_BYTES_PER_TILE = 4 * ((ORTHO_W // 2 + 2) ** 2 + 2 * ORTHO_W * ORTHO_W)   # parent window, residual, output
 
@@ -512,6 +526,12 @@ def learned_section(tp, torch, stream, sh, args, plain_w101):
         "tensor": {"achieved_tflops": tflops, "executed_tflops": B * executed / (fwd_ms / 1000.0) / 1e12,
                    "peak_tflops": peak, "frac": tflops / peak,
                    "flops_per_tile": used, "executed_flops_per_tile": executed},
+        # each layer is a separate launch whose activations go through HBM: the forward
+        # pass is bound by those bytes (64 B per pixel in and out of each hidden layer)
+        "hbm": {"bytes_per_tile": learned_bytes(101),
+                "achieved_gbs": B * learned_bytes(101) / (fwd_ms / 1000.0) / 1e9,
+                "peak_gbs": hbm_peak()[0],
+                "frac": B * learned_bytes(101) / (fwd_ms / 1000.0) / 1e9 / hbm_peak()[0]},
         "train": {"steps": args.learned_steps, "batch": 64, "ms_per_step": train_ms,
                   "loss_first": float(np.mean(losses[:20])), "loss_last": float(np.mean(losses[-20:])),
                   "pairs": int(data["up"].shape[0]), "data": "5-level residual pyramid of a 12-octave fBm "
