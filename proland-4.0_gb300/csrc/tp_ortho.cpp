@@ -8,6 +8,7 @@
 #include <map>
 #include <mutex>
 #include <string>
+#include <tuple>
 #include <vector>
 
 #include "tp_internal.h"
@@ -83,9 +84,11 @@ bool valid_width(int W) { return W >= 8 && W <= 1024 && W % 4 == 0; }
 const uint32_t *device_ortho_noise(int W, int pitch, int *err)
 {
     static std::mutex mu;
-    static std::map<std::pair<int, int>, uint32_t *> tables;
+    static std::map<std::tuple<int, int, int>, uint32_t *> tables;  // (device, W, pitch)
+    int dev = 0;
+    cudaGetDevice(&dev);
     std::lock_guard<std::mutex> lk(mu);
-    auto it = tables.find({W, pitch});
+    auto it = tables.find(std::make_tuple(dev, W, pitch));
     if (it != tables.end()) return it->second;
     std::vector<uint8_t> t((size_t)6 * W * W * 4);
     build_ortho_noise(W, t.data());
@@ -113,7 +116,7 @@ const uint32_t *device_ortho_noise(int W, int pitch, int *err)
         *err = tp::cuda_fail("ortho noise table", e);
         return nullptr;
     }
-    tables[{W, pitch}] = d;
+    tables[std::make_tuple(dev, W, pitch)] = d;
     return d;
 }
 
