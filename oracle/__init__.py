@@ -353,9 +353,22 @@ def compute_residual(W, tx, ty, parent_approx, fine):
     return rq, enc, approx
 
 
-def run_jobs(jobs, nthreads):
+_TUNED = None
+
+
+def tuned_lib():
+    """The oracle built at -O3 -march=native on this machine (the timed CPU baseline)."""
+    global _TUNED
+    if _TUNED is None:
+        L = C.CDLL(_build.build_tuned())
+        L.or_run_jobs.argtypes = [C.POINTER(Job), C.c_int, C.c_int]
+        _TUNED = L
+    return _TUNED
+
+
+def run_jobs(jobs, nthreads, tuned=False):
     arr = (Job * len(jobs))(*jobs)
-    lib().or_run_jobs(arr, len(jobs), int(nthreads))
+    (tuned_lib() if tuned else lib()).or_run_jobs(arr, len(jobs), int(nthreads))
 
 
 # ---------------------------------------------------------------- .dat pyramid

@@ -29,5 +29,25 @@ def build(force: bool = False) -> str:
     return LIB
 
 
+TUNED_LIB = os.path.join(OUT_DIR, "liboracle_tuned.so")
+
+
+def build_tuned(force: bool = False) -> str:
+    """The same sources at -O3 -march=native (floating-point contraction still off),
+    built on the machine that runs them: the timed CPU baseline."""
+    srcs = [os.path.join(HERE, "oracle.c"), os.path.join(HERE, "learned.c"), os.path.join(HERE, "ortho.c")]
+    hdr = os.path.join(HERE, "oracle.h")
+    if (not force and os.path.exists(TUNED_LIB)
+            and os.path.getmtime(TUNED_LIB) >= max([os.path.getmtime(p) for p in srcs] + [os.path.getmtime(hdr)])):
+        return TUNED_LIB
+    os.makedirs(OUT_DIR, exist_ok=True)
+    tmp = TUNED_LIB + ".tmp%d" % os.getpid()
+    cmd = ["gcc", "-O3", "-march=native", "-std=c11", "-D_GNU_SOURCE", "-ffp-contract=off", "-fno-fast-math",
+           "-fPIC", "-shared", "-pthread", "-Wall", "-o", tmp, *srcs, "-lm"]
+    subprocess.check_call(cmd)
+    os.replace(tmp, TUNED_LIB)
+    return TUNED_LIB
+
+
 if __name__ == "__main__":
     print(build(force="--force" in sys.argv))
