@@ -168,8 +168,9 @@ class HostPipeline:
 
     def run(self, params, jobs, parent_zf, parent_zm, residual, zf, zc, zm, nx=None, ny=None, stream=None):
         """Enqueues the batch; synchronise `stream` (or call stream_check) before
-        reading the outputs.  Arrays must be C-contiguous float32 [n, W, W]
-        ([n, W-4, W-4] for nx, ny); parent_zm and residual may be None."""
+        reading the outputs, and keep every array alive until then (the copies read
+        and write them asynchronously).  Arrays must be C-contiguous float32
+        [n, W, W] ([n, W-4, W-4] for nx, ny); parent_zm and residual may be None."""
         n = len(jobs)
         W = self.tile_width
         io = HostTiles()
