@@ -123,7 +123,9 @@ int tp_elevation_batch_device(tp_storage *elev, tp_storage *residuals, tp_storag
  * jobs[k].out_slot and writes normal slot jobs[k].normal_slot (format 2), sample
  * spacing tile_meters / (W - 5).  root_quad_size > 0: the tiles lie on the sphere
  * of a cube-face planet of that root quad size (NormalProducer with deformation,
- * NormalProducer.cpp:215-273; terrain2/normalShader.glsl); 0: flat. */
+ * NormalProducer.cpp:215-273; terrain2/normalShader.glsl); 0: flat.  Returns once
+ * the launch has completed (it synchronises `stream`: the job array goes through a
+ * device buffer shared by all calls). */
 int tp_normal_batch(tp_storage *elev, tp_storage *normals, const tp_tile_job *jobs, int n, double root_quad_size,
                     void *stream);
 /* The same in any of the reference's normal formats (NormalProducer.cpp:195;
@@ -132,7 +134,7 @@ int tp_normal_batch(tp_storage *elev, tp_storage *normals, const tp_tile_job *jo
  * 0 and 1 need 4-channel normal slots, their coarse normals nc average the parent
  * normal tile (parent_normal_slots[k], or nc = nf when NULL or -1) at the
  * coarse-mesh vertices of grid_mesh (gridMeshSize, 24 in the examples).  Jobs are
- * produced level by level, parents first. */
+ * produced level by level, parents first; returns once they have completed. */
 int tp_normal_batch_format(tp_storage *elev, tp_storage *normals, const tp_tile_job *jobs, int n,
                            double root_quad_size, int format, const int *parent_normal_slots, int grid_mesh,
                            void *stream);
@@ -281,6 +283,12 @@ int tp_producer_prefetch_tile(tp_producer *p, int level, int tx, int ty);    /* 
 int tp_producer_invalidate_tiles(tp_producer *p);                             /* invalidateTiles */
 int tp_producer_queued(const tp_producer *p);                                  /* tiles waiting for production */
 int tp_tile_info(const tp_tile *t, int *level, int *tx, int *ty, int *slot, int *users, int *done);
+/* Produces every queued tile of the producers and of the producers they use, on
+ * `stream`: residual tiles first (host decode and one upload, or device decode),
+ * then each elevation producer's queue in one persistent launch (with the flat
+ * normals of the same tiles fused in), then the remaining normals, then ortho
+ * residuals and ortho tiles.  Residual uploads and normal launches synchronise
+ * `stream`; the elevation and ortho launches return at once. */
 int tp_scheduler_run(tp_producer *const *producers, int n, void *stream);
 /* Batched doCreateTile (TileProducer.h:331-378 in the frame form): acquires each
  * requested tile as tp_producer_get_tile does, then produces every queued tile of
@@ -318,7 +326,8 @@ int tp_inflate_zlib(const uint8_t *data, size_t n, uint8_t *out, size_t capacity
  * device once): tile k = (levels[k], txs[k], tys[k]) in the file's pyramid, or a zero
  * tile when levels[k] < 0, written as int16 x scale into slots[k] of `residuals` (a
  * 1-channel device storage of width tileSize + 5; smaller tiles below minLevel fill
- * the slot's lower-left corner, the rest is zero).  TP_E_IO for a corrupt strip. */
+ * the slot's lower-left corner, the rest is zero).  TP_E_IO for a corrupt strip
+ * (known when the call returns: it synchronises `stream`). */
 int tp_dat_decode_device(tp_dat *d, const int *levels, const int *txs, const int *tys, int n, float scale,
                          tp_storage *residuals, const int *slots, void *stream);
 
@@ -453,7 +462,8 @@ int tp_learned_gather(tp_learned *net, const float *up_src, const float *res_src
                       const int *dihedral, int n, float *up_out, float *res_out, void *stream);
 /* Learned residual tiles of n jobs (level >= 1, resident parent_slot, residual_slot
  * in `residuals`, a storage of the net's width): the jobs can then be produced by
- * tp_elevation_batch with those residual slots. */
+ * tp_elevation_batch with those residual slots.  Returns once the tiles are written
+ * (it synchronises `stream` and reports a kernel's failure). */
 int tp_learned_predict_residuals(tp_learned *net, tp_storage *elev, const tp_tile_job *jobs, int n,
                                  tp_storage *residuals, void *stream);
 
