@@ -314,6 +314,65 @@ int tp_residual_tile(tp_producer *p, int level, int tx, int ty, float *out, int 
  * C[16], N[16], L[4], W2T[9], R, size (normal producers with deform = 1 use it). */
 int tp_sphere_frame(double root_quad_size, int level, int tx, int ty, float *out47);
 
+/* ------------------------------------------------------------------------
+ * Elevation layers: the TileLayer draws over produced elevation tiles and the
+ * blend pass that folds them into zm (ElevationProducer.cpp:383-399: layers drawn
+ * under a LESS depth test into the tile's framebuffer, then blendShader).
+ * Supported layer: the road elevation layer (graph/.../dem/RoadElevationLayer.cpp:
+ * 388-437 with graph1/roadLayerElevationShader.glsl): a depth clear, then triangle
+ * meshes whose vertices are (x, y, altitude, u) -- x, y in the tile's clip
+ * coordinates ([-1, 1] spans the W x W texels), u the signed road-width coordinate,
+ * as ElevationGraphLayer::drawCurveAltitude builds them (ElevationGraphLayer.cpp:
+ * 82-380).  A fragment at d = |u| writes z = altitude + 0.03 (1 - smoothstep(0.98,
+ * 1, d)) and w = smoothstep(1, 2, d) at depth 0.1 d + 0.3.  The blend then sets zm
+ * to zf min(w, 1) + z (1 - min(w, 1)) (blend_mode 0: graph1/edit3/river1
+ * blendShader.glsl) or to the 3x3 box filter of that value, clamped at the tile
+ * edge (blend_mode 1: demo/shaders/elevation/blendShader.glsl).  zf and zc are not
+ * changed.  Rasterisation: window coordinates snapped to 1/256 texel, a texel is
+ * covered when its centre is inside the triangle (top-left rule for centres on an
+ * edge, y up), attributes interpolated at the texel centre as a0 + (a1 - a0) l1 +
+ * (a2 - a0) l2 from the barycentric weights l_k, fp32 depth,
+ * triangles drawn in order; vertices beyond 32768 texels of the tile's origin drop
+ * their triangle. */
+#define TP_TRIANGLES 0
+#define TP_TRIANGLE_STRIP 1
+typedef struct {
+    int32_t first_vertex;  /* first vertex of the mesh in the call's vertex array */
+    int32_t count;         /* vertices drawn (not indexed) or indices drawn (indexed) */
+    int32_t first_index;   /* first index in the call's index array; -1: not indexed.
+                              Indices count from first_vertex. */
+    int32_t mode;          /* TP_TRIANGLES or TP_TRIANGLE_STRIP */
+    int32_t clear_depth;   /* 1: the depth buffer is cleared to 1 before this mesh (a new layer) */
+    int32_t reserved[3];
+} tp_layer_mesh;
+typedef struct {
+    int32_t slot;          /* elevation slot (zf, zc, zm) whose zm the layers change */
+    int32_t first_mesh;    /* the tile's meshes, drawn in order; a mesh belongs to one job */
+    int32_t n_meshes;
+    int32_t reserved;
+} tp_layer_job;
+/* Draws the meshes of n tiles (one CTA per tile) and blends them into zm.  The
+ * framebuffer starts as (zf, zc, zm, w = 0) with depth 1, as after the upsample.
+ * `vertices` holds n_vertices x 4 floats.  Returns once the tiles are written (it
+ * synchronises `stream`: the meshes go through a device buffer shared by all calls). */
+int tp_elevation_layers(tp_storage *elev, const tp_layer_job *jobs, int n, const tp_layer_mesh *meshes,
+                        int n_meshes, const float *vertices, int n_vertices, const uint32_t *indices,
+                        int n_indices, int blend_mode, void *stream);
+/* Layers of an elevation producer (TileProducer::addLayer, TileProducer.h:281;
+ * TileLayer::doCreateTile, TileLayer.h:199): for each tile the producer makes,
+ * each layer's callback adds the meshes it draws for (level, tx, ty) to the
+ * builder; the first mesh a callback adds clears the depth buffer (the road
+ * layer's fb->clear of depth).  A producer with layers makes its tiles level by
+ * level, each level's launch followed by its layer pass, so that children read
+ * their parents' blended zm (coarse elevation zc), and computes normals after the
+ * blend.  blend_mode as above (0 by default). */
+typedef struct tp_layer_builder tp_layer_builder;
+int tp_layer_builder_add_mesh(tp_layer_builder *b, const float *vertices, int n_vertices, const uint32_t *indices,
+                              int n_indices, int mode);
+typedef int (*tp_layer_fn)(void *user, int level, int tx, int ty, tp_layer_builder *b);
+int tp_elevation_producer_add_layer(tp_producer *p, tp_layer_fn fn, void *user);
+int tp_elevation_producer_set_blend(tp_producer *p, int blend_mode);
+
 /* Residual pyramid files (ResidualProducer.cpp:93-107, 253-340): header
  * {minLevel, maxLevel, tileSize, rootLevel, rootTx, rootTy, ntiles} and int16
  * tiles decoded from their deflate TIFF strips. */

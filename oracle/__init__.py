@@ -60,6 +60,11 @@ class OrthoJob(C.Structure):
     ]
 
 
+class LayerMesh(C.Structure):
+    _fields_ = [("first_vertex", C.c_int), ("count", C.c_int), ("first_index", C.c_int), ("mode", C.c_int),
+                ("clear_depth", C.c_int)]
+
+
 def lib():
     global _LIB
     if _LIB is None:
@@ -81,6 +86,8 @@ def lib():
         L.or_ortho_tile.argtypes = [C.POINTER(OrthoJob)]
         L.or_ortho_tile_id.argtypes = [C.c_int, C.c_int, C.c_int]
         L.or_ortho_tile_id.restype = C.c_int
+        L.or_layer_tile.argtypes = [C.c_int, _f32p, _f32p, C.POINTER(LayerMesh), C.c_int, _f32p,
+                                    C.POINTER(C.c_uint32), C.c_int, _f32p]
         L.or_elevation_tile.argtypes = [C.POINTER(ElevTile)]
         L.or_elevation_tile_f64.argtypes = [C.POINTER(ElevTile), _f64p, _f64p, _f64p]
         L.or_cpu_elevation_tile.argtypes = [C.c_int] * 4 + [_f32p, C.c_int, _f32p, C.c_int,
@@ -176,6 +183,32 @@ def ortho_tile(W, level, tx, ty, parent, residual, noise_layer, noise_rot, noise
     j.scale, j.hsv = scale, int(bool(hsv))
     j.out = out.ctypes.data
     lib().or_ortho_tile(C.byref(j))
+    return out
+
+
+def layer_tile(W, zf, zm, meshes, blend_mode=0):
+    """zm of one elevation tile after its layers (or_layer_tile): meshes is a list of
+    (vertices [n, 4] (x, y, altitude, u) in clip coordinates, indices or None, mode
+    (0 triangles, 1 strip), clear_depth)."""
+    verts, idx, ms = [], [], []
+    nv = ni = 0
+    for v, ix, mode, clear in meshes:
+        v = np.ascontiguousarray(v, np.float32).reshape(-1, 4)
+        m = LayerMesh(nv, v.shape[0], -1, mode, int(clear))
+        if ix is not None:
+            ix = np.ascontiguousarray(ix, np.uint32)
+            m.first_index, m.count = ni, ix.size
+            idx.append(ix)
+            ni += ix.size
+        verts.append(v)
+        nv += v.shape[0]
+        ms.append(m)
+    va = np.concatenate(verts) if verts else np.zeros((1, 4), np.float32)
+    ia = np.concatenate(idx) if idx else np.zeros(1, np.uint32)
+    arr = (LayerMesh * max(1, len(ms)))(*ms)
+    out = np.empty((W, W), np.float32)
+    lib().or_layer_tile(W, _p(_f32(zf)), _p(_f32(zm)), arr, len(ms), _p(va), _p(ia, C.POINTER(C.c_uint32)),
+                        blend_mode, _p(out))
     return out
 
 

@@ -15,7 +15,8 @@ LIB = os.path.join(OUT_DIR, "liboracle.so")
 
 
 def build(force: bool = False) -> str:
-    srcs = [os.path.join(HERE, "oracle.c"), os.path.join(HERE, "learned.c"), os.path.join(HERE, "ortho.c")]
+    srcs = [os.path.join(HERE, "oracle.c"), os.path.join(HERE, "learned.c"), os.path.join(HERE, "ortho.c"),
+            os.path.join(HERE, "layers.c")]
     hdr = os.path.join(HERE, "oracle.h")
     if (not force and os.path.exists(LIB)
             and os.path.getmtime(LIB) >= max([os.path.getmtime(p) for p in srcs] + [os.path.getmtime(hdr)])):
@@ -35,7 +36,8 @@ TUNED_LIB = os.path.join(OUT_DIR, "liboracle_tuned.so")
 def build_tuned(force: bool = False) -> str:
     """The same sources at -O3 -march=native (floating-point contraction still off),
     built on the machine that runs them: the timed CPU baseline."""
-    srcs = [os.path.join(HERE, "oracle.c"), os.path.join(HERE, "learned.c"), os.path.join(HERE, "ortho.c")]
+    srcs = [os.path.join(HERE, "oracle.c"), os.path.join(HERE, "learned.c"), os.path.join(HERE, "ortho.c"),
+            os.path.join(HERE, "layers.c")]
     hdr = os.path.join(HERE, "oracle.h")
     if (not force and os.path.exists(TUNED_LIB)
             and os.path.getmtime(TUNED_LIB) >= max([os.path.getmtime(p) for p in srcs] + [os.path.getmtime(hdr)])):

@@ -153,6 +153,18 @@ void or_ortho_noise(int W, uint8_t *out);
 void or_ortho_tile(const or_ortho_job *t);
 int  or_ortho_tile_id(int level, int tx, int ty);   /* OrthoCPUProducer.cpp:250-253 */
 
+/* ---- elevation layers (layers.c): road layer meshes drawn into one tile and
+ * blended into zm (ElevationProducer.cpp:378-399, RoadElevationLayer.cpp:388-437,
+ * graph1/roadLayerElevationShader.glsl, graph1 and demo blendShader.glsl).
+ * Vertices are (x, y, altitude, u) in clip coordinates; indices count from the
+ * mesh's first vertex; mode 0 triangles, 1 triangle strip.  zf, zm, zm_out are
+ * dense W x W. ---- */
+typedef struct {
+    int first_vertex, count, first_index, mode, clear_depth;
+} or_layer_mesh;
+void or_layer_tile(int W, const float *zf, const float *zm, const or_layer_mesh *meshes, int n_meshes,
+                   const float *vertices, const uint32_t *indices, int blend_mode, float *zm_out);
+
 #ifdef __cplusplus
 }
 #endif

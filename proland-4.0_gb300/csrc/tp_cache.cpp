@@ -96,6 +96,17 @@ struct tp_producer {
     // ortho producer (OrthoProducer); residuals, noise_amp and face as above
     tp_ortho_params oparams{};
     int max_level = -1;
+    // elevation producer layers (TileProducer::addLayer) and the blend program
+    std::vector<std::pair<tp_layer_fn, void *>> layers;
+    int blend_mode = 0;
+};
+
+// Meshes that a producer's layers draw for one level's tiles.
+struct tp_layer_builder {
+    std::vector<tp_layer_mesh> meshes;
+    std::vector<float> vertices;
+    std::vector<uint32_t> indices;
+    bool layer_start = false;  // the next mesh is the first of a layer: it clears the depth buffer
 };
 
 namespace {
@@ -549,6 +560,46 @@ extern "C" int tp_normal_producer_set_format(tp_producer *p, int format, int gri
     return TP_OK;
 }
 
+extern "C" int tp_layer_builder_add_mesh(tp_layer_builder *b, const float *vertices, int n_vertices,
+                                         const uint32_t *indices, int n_indices, int mode)
+{
+    if (!b || n_vertices < 0 || (n_vertices > 0 && !vertices) || n_indices < 0 || (n_indices > 0 && !indices) ||
+        (mode != TP_TRIANGLES && mode != TP_TRIANGLE_STRIP))
+        return tp::fail(TP_E_BAD_ARG, "tp_layer_builder_add_mesh: bad arguments");
+    for (int k = 0; k < n_indices; ++k)
+        if (indices[k] >= (uint32_t)n_vertices) return tp::fail(TP_E_BAD_ARG, "tp_layer_builder_add_mesh: index out of range");
+    tp_layer_mesh m;
+    std::memset(&m, 0, sizeof m);
+    m.first_vertex = (int32_t)(b->vertices.size() / 4);
+    m.count = n_indices > 0 ? n_indices : n_vertices;
+    m.first_index = n_indices > 0 ? (int32_t)b->indices.size() : -1;
+    m.mode = mode;
+    m.clear_depth = b->layer_start ? 1 : 0;
+    b->layer_start = false;
+    b->vertices.insert(b->vertices.end(), vertices, vertices + 4 * (size_t)n_vertices);
+    b->indices.insert(b->indices.end(), indices, indices + n_indices);
+    b->meshes.push_back(m);
+    return TP_OK;
+}
+
+extern "C" int tp_elevation_producer_add_layer(tp_producer *p, tp_layer_fn fn, void *user)
+{
+    if (!p || p->kind != kElevation || !fn) return tp::fail(TP_E_BAD_ARG, "tp_elevation_producer_add_layer: bad arguments");
+    if (p->cache->storage->channels < 3)
+        return tp::fail(TP_E_BAD_ARG, "tp_elevation_producer_add_layer: layers need (zf, zc, zm) slots");
+    std::lock_guard<std::recursive_mutex> lk(p->cache->mu);
+    p->layers.emplace_back(fn, user);
+    return TP_OK;
+}
+
+extern "C" int tp_elevation_producer_set_blend(tp_producer *p, int blend_mode)
+{
+    if (!p || p->kind != kElevation || (blend_mode != 0 && blend_mode != 1))
+        return tp::fail(TP_E_BAD_ARG, "tp_elevation_producer_set_blend: bad arguments");
+    p->blend_mode = blend_mode;
+    return TP_OK;
+}
+
 extern "C" int tp_producer_destroy(tp_producer *p)
 {
     if (!p) return TP_OK;
@@ -770,52 +821,120 @@ int run_residuals(tp_producer *r, void *stream)
     return TP_OK;
 }
 
+// The tp_tile_job of an elevation tile; `index` maps tiles of the same launch to
+// their job numbers (a parent found there is named in parent_job).
+int elevation_job(const tp_producer *e, const tp_tile *t, const std::map<const tp_tile *, int> &index, int normal_slot,
+                  tp_tile_job &j)
+{
+    const int n = e->cache->storage->W - 5;
+    const int mod = e->residuals ? (e->residuals->cache->storage->W - 5) / n : 1;
+    std::memset(&j, 0, sizeof j);
+    j.level = t->level;
+    j.tx = t->tx;
+    j.ty = t->ty;
+    j.out_slot = t->slot;
+    j.parent_slot = t->dep_parent ? t->dep_parent->slot : -1;
+    j.parent_job = -1;
+    if (t->dep_parent) {
+        auto it = index.find(t->dep_parent);
+        if (it != index.end()) j.parent_job = it->second;
+        else if (!t->dep_parent->done) return tp::fail(TP_E_MISSING_PARENT, "elevation parent tile is not produced");
+    }
+    j.residual_slot = t->dep_input ? t->dep_input->slot : -1;
+    j.rx = (t->tx % mod) * n;
+    j.ry = (t->ty % mod) * n;
+    j.rscale = 1.0f;
+    j.normal_slot = normal_slot;
+    int rot = 0, layer = 0;
+    tp_noise_select(e->face, t->level, t->tx, t->ty, &rot, &layer);
+    j.noise_rot = rot;
+    j.noise_layer = layer;
+    j.noise_amp = t->level < (int)e->noise_amp.size() ? e->noise_amp[t->level] : 0.0f;
+    j.tile_meters = e->root_quad_size / (float)(1u << t->level);
+    return TP_OK;
+}
+
+// The layer pass of tiles just produced: each layer's meshes for each tile, drawn
+// and blended into zm (ElevationProducer.cpp:383-399).
+int run_layers(tp_producer *e, const std::vector<tp_tile *> &tiles, void *stream)
+{
+    tp_layer_builder b;
+    std::vector<tp_layer_job> jobs(tiles.size());
+    for (size_t k = 0; k < tiles.size(); ++k) {
+        const tp_tile *t = tiles[k];
+        jobs[k] = tp_layer_job{t->slot, (int32_t)b.meshes.size(), 0, 0};
+        for (const auto &l : e->layers) {
+            b.layer_start = true;
+            if (l.first(l.second, t->level, t->tx, t->ty, &b) != 0)
+                return tp::fail(TP_E_BAD_ARG, "elevation layer callback failed");
+        }
+        jobs[k].n_meshes = (int32_t)b.meshes.size() - jobs[k].first_mesh;
+    }
+    return tp_elevation_layers(e->cache->storage, jobs.data(), (int)jobs.size(), b.meshes.data(), (int)b.meshes.size(),
+                               b.vertices.data(), (int)(b.vertices.size() / 4), b.indices.data(),
+                               (int)b.indices.size(), e->blend_mode, stream);
+}
+
+void finish_tiles(const std::vector<tp_tile *> &tiles)
+{
+    for (tp_tile *t : tiles) {
+        t->done = true;
+        t->queued = false;
+        release_deps(t);
+    }
+}
+
 int run_elevations(tp_producer *e, tp_producer *normals, void *stream)
 {
     // normal tiles whose elevation tile is produced by this same launch are fused in
-    // (flat deformation; spherical normals run in their own kernel afterwards)
+    // (flat deformation; spherical normals run in their own kernel afterwards; a
+    // producer with layers changes zm after its launch, so its normals come later)
+    const bool layered = !e->layers.empty();
     std::map<const tp_tile *, tp_tile *> fused;  // elevation tile -> normal tile
-    if (normals && !normals->deform && normals->normal_format == 2)
+    if (!layered && normals && !normals->deform && normals->normal_format == 2)
         for (tp_tile *nt : normals->queue)
             if (nt->dep_input && nt->dep_input->queued) fused[nt->dep_input] = nt;
     if (e->queue.empty()) return TP_OK;
     if (!(e->root_quad_size > 0.0f)) return tp::fail(TP_E_BAD_ARG, "elevation producer: root quad size not set");
     std::vector<tp_tile *> q = e->queue;
     std::stable_sort(q.begin(), q.end(), [](const tp_tile *a, const tp_tile *b) { return a->level < b->level; });
+    if (!e->frame) tp_frame_create(&e->frame);
+    if (layered) {
+        // level by level: a level's launch, then its layer pass, then the next level
+        size_t k = 0;
+        int rc = TP_OK;
+        while (k < q.size() && rc == TP_OK) {
+            size_t k1 = k;
+            while (k1 < q.size() && q[k1]->level == q[k]->level) ++k1;
+            std::vector<tp_tile *> lvl(q.begin() + k, q.begin() + k1);
+            std::map<const tp_tile *, int> none;
+            std::vector<tp_tile_job> jobs(lvl.size());
+            for (size_t i = 0; i < lvl.size() && rc == TP_OK; ++i) rc = elevation_job(e, lvl[i], none, -1, jobs[i]);
+            if (rc == TP_OK) {
+                tp_frame_clear(e->frame);
+                rc = tp_frame_add(e->frame, e->cache->storage,
+                                  e->residuals ? e->residuals->cache->storage : nullptr, nullptr, &e->params,
+                                  jobs.data(), (int)jobs.size());
+            }
+            if (rc == TP_OK) rc = tp_frame_launch(e->frame, stream);
+            if (rc == TP_OK) rc = run_layers(e, lvl, stream);
+            if (rc == TP_OK) finish_tiles(lvl);
+            k = k1;
+        }
+        std::vector<tp_tile *> rest;
+        for (tp_tile *t : e->queue)
+            if (!t->done) rest.push_back(t);
+        e->queue.swap(rest);
+        return rc;
+    }
     std::map<const tp_tile *, int> index;
     for (size_t k = 0; k < q.size(); ++k) index[q[k]] = (int)k;
-    const int n = e->cache->storage->W - 5;
-    const int mod = e->residuals ? (e->residuals->cache->storage->W - 5) / n : 1;
     std::vector<tp_tile_job> jobs(q.size());
     for (size_t k = 0; k < q.size(); ++k) {
-        const tp_tile *t = q[k];
-        tp_tile_job &j = jobs[k];
-        std::memset(&j, 0, sizeof j);
-        j.level = t->level;
-        j.tx = t->tx;
-        j.ty = t->ty;
-        j.out_slot = t->slot;
-        j.parent_slot = t->dep_parent ? t->dep_parent->slot : -1;
-        j.parent_job = -1;
-        if (t->dep_parent) {
-            auto it = index.find(t->dep_parent);
-            if (it != index.end()) j.parent_job = it->second;
-            else if (!t->dep_parent->done) return tp::fail(TP_E_MISSING_PARENT, "elevation parent tile is not produced");
-        }
-        j.residual_slot = t->dep_input ? t->dep_input->slot : -1;
-        j.rx = (t->tx % mod) * n;
-        j.ry = (t->ty % mod) * n;
-        j.rscale = 1.0f;
-        auto f = fused.find(t);
-        j.normal_slot = f != fused.end() ? f->second->slot : -1;
-        int rot = 0, layer = 0;
-        tp_noise_select(e->face, t->level, t->tx, t->ty, &rot, &layer);
-        j.noise_rot = rot;
-        j.noise_layer = layer;
-        j.noise_amp = t->level < (int)e->noise_amp.size() ? e->noise_amp[t->level] : 0.0f;
-        j.tile_meters = e->root_quad_size / (float)(1u << t->level);
+        auto f = fused.find(q[k]);
+        int rc = elevation_job(e, q[k], index, f != fused.end() ? f->second->slot : -1, jobs[k]);
+        if (rc) return rc;
     }
-    if (!e->frame) tp_frame_create(&e->frame);
     tp_frame_clear(e->frame);
     int rc = tp_frame_add(e->frame, e->cache->storage, e->residuals ? e->residuals->cache->storage : nullptr,
                           normals && !fused.empty() ? normals->cache->storage : nullptr, &e->params, jobs.data(),
@@ -823,11 +942,7 @@ int run_elevations(tp_producer *e, tp_producer *normals, void *stream)
     if (rc) return rc;
     rc = tp_frame_launch(e->frame, stream);
     if (rc) return rc;
-    for (tp_tile *t : q) {
-        t->done = true;
-        t->queued = false;
-        release_deps(t);
-    }
+    finish_tiles(q);
     e->queue.clear();
     if (normals) {
         std::vector<tp_tile *> rest;

@@ -8,7 +8,7 @@ import ctypes as C
 
 import numpy as np
 
-from ._lib import (ElevParams, HostTiles, OrthoJob, OrthoParams, TileJob, TPError, check, lib, LIB_PATH, RESIDUAL_SOURCE,  # noqa: F401
+from ._lib import (ElevParams, HostTiles, LAYER_FN, LayerJob, LayerMesh, OrthoJob, OrthoParams, TileJob, TPError, check, lib, LIB_PATH, RESIDUAL_SOURCE,  # noqa: F401
                    TP_OK, TP_E_BAD_ARG, TP_E_CACHE_FULL, TP_E_MISSING_PARENT,
                    TP_E_TIMEOUT, TP_E_CUDA, TP_E_IO, TP_E_NO_DEVICE)
 
@@ -187,6 +187,41 @@ class HostPipeline:
         self._arr = (TileJob * n)(*jobs)
         self._io = io
         check(lib().tp_elevation_batch_host(self.handle, C.byref(params), self._arr, n, C.byref(io), stream))
+
+
+# ---------------------------------------------------------------- elevation layers
+TRIANGLES, TRIANGLE_STRIP = 0, 1
+
+
+def elevation_layers(elev, tiles, blend_mode=0, stream=None):
+    """Road layer meshes drawn into produced elevation tiles and blended into zm
+    (tp_elevation_layers).  tiles: list of (slot, meshes), meshes a list of
+    (vertices [n, 4] float32 (x, y, altitude, u) in clip coordinates, indices or None,
+    mode, clear_depth)."""
+    verts, idx, meshes, jobs = [], [], [], []
+    nv = ni = 0
+    for slot, ms in tiles:
+        jobs.append(LayerJob(slot, len(meshes), len(ms), 0))
+        for v, ix, mode, clear in ms:
+            v = np.ascontiguousarray(v, np.float32).reshape(-1, 4)
+            m = LayerMesh()
+            m.first_vertex, m.mode, m.clear_depth = nv, mode, int(clear)
+            if ix is None:
+                m.first_index, m.count = -1, v.shape[0]
+            else:
+                ix = np.ascontiguousarray(ix, np.uint32)
+                m.first_index, m.count = ni, ix.size
+                idx.append(ix)
+                ni += ix.size
+            verts.append(v)
+            nv += v.shape[0]
+            meshes.append(m)
+    va = np.concatenate(verts) if verts else np.zeros((0, 4), np.float32)
+    ia = np.concatenate(idx) if idx else np.zeros(0, np.uint32)
+    ja = (LayerJob * max(1, len(jobs)))(*jobs)
+    ma = (LayerMesh * max(1, len(meshes)))(*meshes)
+    check(lib().tp_elevation_layers(elev.handle, ja, len(jobs), ma, len(meshes), va.ctypes.data, nv,
+                                    ia.ctypes.data, ni, blend_mode, stream))
 
 
 # ---------------------------------------------------------------- ortho tiles
@@ -485,6 +520,32 @@ class ElevationProducer(TileProducer):
                                                  len(noise_amp), C.byref(params or make_params()), face, C.byref(h)))
         super().__init__(h, cache)
         self.residuals = residuals
+        self._layers = []
+
+    def add_layer(self, fn):
+        """TileProducer::addLayer with a road elevation layer: fn(level, tx, ty) returns
+        the meshes it draws on that tile, a list of (vertices [n, 4] float32, indices or
+        None, mode) -- see elevation_layers."""
+        def cb(user, level, tx, ty, builder):
+            try:
+                for verts, idx, mode in fn(level, tx, ty):
+                    v = np.ascontiguousarray(verts, np.float32).reshape(-1, 4)
+                    ix = None if idx is None else np.ascontiguousarray(idx, np.uint32)
+                    rc = lib().tp_layer_builder_add_mesh(builder, v.ctypes.data, v.shape[0],
+                                                         None if ix is None else ix.ctypes.data,
+                                                         0 if ix is None else ix.size, mode)
+                    if rc:
+                        return rc
+                return 0
+            except Exception:
+                return -1
+        c = LAYER_FN(cb)
+        self._layers.append(c)
+        check(lib().tp_elevation_producer_add_layer(self.handle, c, None))
+
+    def set_blend(self, mode):
+        """0: graph1/edit3 blendShader, 1: the demo's 3x3 filtered blend."""
+        check(lib().tp_elevation_producer_set_blend(self.handle, mode))
 
 
 class NormalProducer(TileProducer):

@@ -75,6 +75,18 @@ class HostTiles(C.Structure):
     _fields_ = [(n, C.c_void_p) for n in ("parent_zf", "parent_zm", "residual", "zf", "zc", "zm", "nx", "ny")]
 
 
+class LayerMesh(C.Structure):
+    """tp_layer_mesh"""
+    _fields_ = [("first_vertex", C.c_int32), ("count", C.c_int32), ("first_index", C.c_int32),
+                ("mode", C.c_int32), ("clear_depth", C.c_int32), ("reserved", C.c_int32 * 3)]
+
+
+class LayerJob(C.Structure):
+    """tp_layer_job"""
+    _fields_ = [("slot", C.c_int32), ("first_mesh", C.c_int32), ("n_meshes", C.c_int32), ("reserved", C.c_int32)]
+
+
+LAYER_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p)
 RESIDUAL_SOURCE = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_float), C.c_int)
 
 _LIB = None
@@ -192,6 +204,11 @@ def lib():
         "tp_learned_backward": ([_vp, _vp, _f32p, _vp], _i),
         "tp_learned_adam": ([_vp, C.c_float, _vp], _i),
         "tp_learned_gather": ([_vp, _vp, _vp, _i, C.POINTER(_i), C.POINTER(_i), _i, _vp, _vp, _vp], _i),
+        "tp_elevation_layers": ([_vp, C.POINTER(LayerJob), _i, C.POINTER(LayerMesh), _i, _vp, _i, _vp, _i, _i, _vp],
+                                _i),
+        "tp_layer_builder_add_mesh": ([_vp, _vp, _i, _vp, _i, _i], _i),
+        "tp_elevation_producer_add_layer": ([_vp, LAYER_FN, _vp], _i),
+        "tp_elevation_producer_set_blend": ([_vp, _i], _i),
         "tp_learned_predict_residuals": ([_vp, _vp, C.POINTER(TileJob), _i, _vp, _vp], _i),
     }
     for name, (args, res) in sig.items():
