@@ -473,6 +473,74 @@ def ortho_section(tp, torch, stream, sh, args):
     return out
 
 
+def layers_section(tp, torch, stream, sh, args):
+    """Elevation layer pass (tp_elevation_layers): 4096 produced 101-wide tiles, each
+    crossed by two roads of the road elevation layer (3-point polylines, widths 5-40 m,
+    on 1000 m tiles: strips of ~290 triangles, built by layers.road_strip), drawn and
+    blended into zm (graph1 blend).  A pass uploads its meshes from host memory, then
+    runs one CTA per tile; CUDA events on the stream around whole passes."""
+    import oracle
+    from proland_gb300 import layers
+    W, n = 101, 4096
+    rng = np.random.default_rng(args.seed + 5)
+    zf = (rng.standard_normal((64, W, W)) * 200.0).astype(np.float32)
+    zm = np.maximum(zf, np.float32(0.0))
+    elev = tp.TileStorage(W, 3, n)
+    pick = np.arange(n) % 64
+    elev.upload(0, tp.ZF, zf[pick], sh)
+    tiles = []
+    for k in range(n):
+        ms = []
+        for r in range(2):
+            a, b = rng.uniform(-200, 1200, 2), rng.uniform(-200, 1200, 2)
+            mid = (a + b) / 2 + rng.uniform(-150, 150, 2)
+            v = layers.road_strip([a, mid, b], rng.uniform(0, 300, 3), float(rng.uniform(5, 40)), (0.0, 0.0),
+                                  1000.0, W)
+            ms.append((v, None, tp.TRIANGLE_STRIP, r == 0))
+        tiles.append((k, ms))
+    batch = tp.LayerBatch(tiles)
+    ntri = sum(max(v.shape[0] - 2, 0) for _, ms in tiles for v, _, _, _ in ms)
+    # parity on a sample: one pass over fresh zm planes
+    elev.upload(0, tp.ZM, zm[pick], sh)
+    batch.run(elev, 0, sh)
+    tp.stream_check(sh)
+    ok = True
+    t0 = time.perf_counter()
+    sample = [0, 1, n // 2, n - 1]
+    for k in sample:
+        want = oracle.layer_tile(W, zf[pick[k]], zm[pick[k]], tiles[k][1], 0)
+        ok = ok and bool(np.array_equal(elev.download(k, 1, tp.ZM, stream=sh)[0], want))
+    cpu_rate = len(sample) / (time.perf_counter() - t0)
+    batch.pin(torch).to_device(torch)
+
+    def timed(fn, steps=10):
+        for _ in range(3):
+            fn()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(steps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        tp.stream_check(sh)
+        return e0.elapsed_time(e1) / steps
+    ms_dev = timed(lambda: batch.run_device(elev, 0, sh))
+    ms_host = timed(lambda: batch.run(elev, 0, sh))
+    mesh_bytes = batch.n_vertices * 16
+    out = {"workload": "layer pass over %d produced 101x101 tiles, 2 road strips each (%d triangles)" % (n, ntri),
+           "tiles_per_s": n / (ms_dev / 1000.0), "triangles_per_s": ntri / (ms_dev / 1000.0),
+           "ms_per_pass": ms_dev, "pass": "meshes resident on the device (tp_elevation_layers_device)",
+           "host_meshes": {"ms_per_pass": ms_host, "tiles_per_s": n / (ms_host / 1000.0),
+                           "mesh_bytes_uploaded_per_pass": mesh_bytes,
+                           "pass": "meshes in pinned host memory, uploaded by each pass (tp_elevation_layers)"},
+           "steps": 10, "texel_bytes_per_tile": 12 * W * W,
+           "identical_to_oracle_on_sample": ok,
+           "cpu_single_thread_oracle_tiles_per_s": cpu_rate}
+    elev.close()
+    return out
+
+
 def learned_section(tp, torch, stream, sh, args, plain_w101):
     """The learned-residual form beside the plain one: a net trained briefly on a
     5-level residual pyramid (device preprocess of a procedural fBm), its per-level
@@ -634,6 +702,9 @@ def main():
                     help="run the ortho frame alone and print its object (for profiling)")
     ap.add_argument("--ortho-rgb", action="store_true", help="ortho frame with RGB instead of HSV noise")
     ap.add_argument("--planet-requests", type=int, default=16384)
+    ap.add_argument("--no-layers", action="store_true", help="skip the elevation layer pass")
+    ap.add_argument("--layers-only", action="store_true",
+                    help="run the elevation layer pass alone and print its object (for profiling)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -651,6 +722,10 @@ def main():
     warmup = max(args.warmup, 3)
 
     from proland_gb300 import replicas
+    if args.layers_only:
+        stream = torch.cuda.Stream()
+        print(json.dumps({"layers": layers_section(tp, torch, stream, C.c_void_p(stream.cuda_stream), args)}))
+        return
     if args.ortho_only:
         stream = torch.cuda.Stream()
         print(json.dumps({"ortho": ortho_section(tp, torch, stream, C.c_void_p(stream.cuda_stream), args)}))
@@ -794,6 +869,8 @@ def main():
     }
     if not args.no_ortho:
         line["ortho"] = ortho_section(tp, torch, stream, sh, args)
+    if not args.no_layers:
+        line["layers"] = layers_section(tp, torch, stream, sh, args)
     if not args.no_learned:
         trained, line["learned"] = learned_section(tp, torch, stream, sh, args, per_width.get("W101"))
         if not args.no_planet:

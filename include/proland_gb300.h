@@ -286,9 +286,10 @@ int tp_tile_info(const tp_tile *t, int *level, int *tx, int *ty, int *slot, int 
 /* Produces every queued tile of the producers and of the producers they use, on
  * `stream`: residual tiles first (host decode and one upload, or device decode),
  * then each elevation producer's queue in one persistent launch (with the flat
- * normals of the same tiles fused in), then the remaining normals, then ortho
- * residuals and ortho tiles.  Residual uploads and normal launches synchronise
- * `stream`; the elevation and ortho launches return at once. */
+ * normals of the same tiles fused in; a producer with layers: one launch and one
+ * layer pass per level, normals afterwards), then the remaining normals, then
+ * ortho residuals and ortho tiles.  Residual uploads, layer passes and normal
+ * launches synchronise `stream`; the elevation and ortho launches return at once. */
 int tp_scheduler_run(tp_producer *const *producers, int n, void *stream);
 /* Batched doCreateTile (TileProducer.h:331-378 in the frame form): acquires each
  * requested tile as tp_producer_get_tile does, then produces every queued tile of
@@ -358,6 +359,12 @@ typedef struct {
 int tp_elevation_layers(tp_storage *elev, const tp_layer_job *jobs, int n, const tp_layer_mesh *meshes,
                         int n_meshes, const float *vertices, int n_vertices, const uint32_t *indices,
                         int n_indices, int blend_mode, void *stream);
+/* The same with the vertex and index arrays in device memory (e.g. meshes built on
+ * the device); jobs and meshes stay in host memory.  Index values are not checked on
+ * the host: one past the vertex array drops its triangle. */
+int tp_elevation_layers_device(tp_storage *elev, const tp_layer_job *jobs, int n, const tp_layer_mesh *meshes,
+                               int n_meshes, const float *vertices_dev, int n_vertices, const uint32_t *indices_dev,
+                               int n_indices, int blend_mode, void *stream);
 /* Layers of an elevation producer (TileProducer::addLayer, TileProducer.h:281;
  * TileLayer::doCreateTile, TileLayer.h:199): for each tile the producer makes,
  * each layer's callback adds the meshes it draws for (level, tx, ty) to the

@@ -18,9 +18,10 @@
 //
 // Here one CTA produces one tile: the tile's z, w and depth live in shared memory
 // (row bands of at most ~140 KB for wide tiles), triangles are set up 256 at a time
-// (one per thread) and rasterised in order, each pixel owned by one thread (rows by
-// warp, columns by lane), so the per-pixel order of primitives is the draw order,
-// as GL guarantees.  Rasterisation rules (the reference leaves them to the GL
+// (one per thread) and rasterised in order.  Each warp owns a block of rows and
+// walks, for every triangle, the texels of the triangle's box in its rows, spread
+// over its lanes; every texel is written by one warp only, in triangle order, so the
+// per-texel order of primitives is the draw order, as GL guarantees.  Rasterisation rules (the reference leaves them to the GL
 // driver): vertex window coordinates snapped to 1/256 texel, coverage of the texel
 // centre by exact integer edge functions with a top-left rule (y up, row 0 at the
 // bottom), attributes interpolated at the texel centre in the plane form
@@ -37,7 +38,8 @@
 
 namespace {
 
-constexpr int kThreads = 256;
+constexpr int kThreads = 1024;
+constexpr int kChunk = 256;   // triangles set up at once (one per thread of the first kChunk)
 constexpr int kWarps = kThreads / 32;
 constexpr int kSubpixel = 256;              // 8 sub-texel bits
 constexpr float kMaxSnapped = 8388608.0f;   // |window coordinate| * 256 <= 2^23
@@ -50,16 +52,22 @@ struct DevJob {
     int slot, first_mesh, n_meshes, ntri;
 };
 
-// One triangle after set-up (counter-clockwise, snapped).
-struct Tri {
-    int X[3], Y[3];
-    float alt[3], u[3];
+// One triangle after set-up (counter-clockwise, snapped): edge q (from vertex q + 1
+// to vertex q + 2, the weight of vertex q) is E_q = A_q px + B_q py + C_q at the
+// sub-texel point (px, py), exact in 64 bits.
+struct __align__(16) Tri {
+    long long C[3];
+    int A[3], B[3];
+    float a0, da1, da2;      // altitude at vertex 0, and vertex 1, 2 minus vertex 0
+    float u0, du1, du2;      // road-width coordinate likewise
+    float area;              // twice the area, as float
     int ix0, ix1, jy0, jy1;  // texel bounding box, clipped to the tile
-    int bias[3];             // 0 for a top-left edge (ties covered), 1 otherwise
-    float area;              // twice the signed area, as float
-    int flags;               // bit 0 valid, bit 1 clear depth before this triangle
-    int pad;
+    int bits;                // bits 0-2: edge q is not top-left (ties not covered);
+                             // bit 3 valid; bit 4 clear depth before this triangle
+    uint32_t inv_cols;       // ceil(2^32 / box width) for box widths >= 2 (t / width = umulhi(t, inv))
+    int pad[3];
 };
+constexpr int kValid = 8, kClear = 16;
 
 __device__ __forceinline__ int floor_div(int a, int b) { return a >= 0 ? a / b : -((-a + b - 1) / b); }
 
@@ -84,9 +92,8 @@ __device__ __forceinline__ long long edge_fn(int xa, int ya, int xb, int yb, int
 }
 
 __device__ void setup(Tri &t, const DevJob &J, const DevMesh *meshes, const float4 *verts, const uint32_t *idx,
-                      int g, int W)
+                      int nv, int g, int W)
 {
-    t.flags = 0;
     int m = J.first_mesh;
     const int mend = J.first_mesh + J.n_meshes;
     while (m + 1 < mend && meshes[m + 1].tri_base <= g) ++m;
@@ -103,59 +110,85 @@ __device__ void setup(Tri &t, const DevJob &J, const DevMesh *meshes, const floa
         c[1] = 3 * k + 1;
         c[2] = 3 * k + 2;
     }
+    t.bits = (k == 0 && M.clear) ? kClear : 0;
     float4 v[3];
-#pragma unroll
-    for (int q = 0; q < 3; ++q) {
-        const int vi = M.first_index >= 0 ? (int)idx[M.first_index + c[q]] : c[q];
-        v[q] = verts[M.first_vertex + vi];
-    }
-    const int clear = (k == 0 && M.clear) ? 2 : 0;
-    t.flags = clear;
     bool ok = true;
 #pragma unroll
     for (int q = 0; q < 3; ++q) {
-        ok = ok && snap(v[q].x, W, &t.X[q]);
-        ok = ok && snap(v[q].y, W, &t.Y[q]);
-        t.alt[q] = v[q].z;
-        t.u[q] = v[q].w;
+        // an index past the vertex array (device-built meshes are not checked on the
+        // host) drops the triangle
+        const uint32_t vi = M.first_index >= 0 ? idx[M.first_index + c[q]] : (uint32_t)c[q];
+        ok = ok && (long long)M.first_vertex + vi < (long long)nv;
+        v[q] = ok ? verts[M.first_vertex + vi] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    }
+    int X[3], Y[3];
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+        ok = ok && snap(v[q].x, W, &X[q]);
+        ok = ok && snap(v[q].y, W, &Y[q]);
     }
     if (!ok) return;
-    long long a2 = edge_fn(t.X[0], t.Y[0], t.X[1], t.Y[1], t.X[2], t.Y[2]);
+    long long a2 = edge_fn(X[0], Y[0], X[1], Y[1], X[2], Y[2]);
     if (a2 == 0) return;
     if (a2 < 0) {  // no face culling: clockwise triangles are drawn as their mirror
-        int s = t.X[1]; t.X[1] = t.X[2]; t.X[2] = s;
-        s = t.Y[1]; t.Y[1] = t.Y[2]; t.Y[2] = s;
-        float f = t.alt[1]; t.alt[1] = t.alt[2]; t.alt[2] = f;
-        f = t.u[1]; t.u[1] = t.u[2]; t.u[2] = f;
+        int s = X[1]; X[1] = X[2]; X[2] = s;
+        s = Y[1]; Y[1] = Y[2]; Y[2] = s;
+        const float4 f = v[1]; v[1] = v[2]; v[2] = f;
         a2 = -a2;
     }
     t.area = __ll2float_rn(a2);
-    // edge q runs from vertex q + 1 to vertex q + 2 (the weight of vertex q)
+    t.a0 = v[0].z;
+    t.da1 = __fsub_rn(v[1].z, v[0].z);
+    t.da2 = __fsub_rn(v[2].z, v[0].z);
+    t.u0 = v[0].w;
+    t.du1 = __fsub_rn(v[1].w, v[0].w);
+    t.du2 = __fsub_rn(v[2].w, v[0].w);
 #pragma unroll
     for (int q = 0; q < 3; ++q) {
         const int a = (q + 1) % 3, b = (q + 2) % 3;
-        const int dx = t.X[b] - t.X[a], dy = t.Y[b] - t.Y[a];
-        t.bias[q] = (dy < 0 || (dy == 0 && dx < 0)) ? 0 : 1;
+        const int dx = X[b] - X[a], dy = Y[b] - Y[a];
+        t.A[q] = -dy;
+        t.B[q] = dx;
+        t.C[q] = (long long)dy * X[a] - (long long)dx * Y[a];
+        if (!(dy < 0 || (dy == 0 && dx < 0))) t.bits |= 1 << q;
     }
-    const int xmin = min(t.X[0], min(t.X[1], t.X[2])), xmax = max(t.X[0], max(t.X[1], t.X[2]));
-    const int ymin = min(t.Y[0], min(t.Y[1], t.Y[2])), ymax = max(t.Y[0], max(t.Y[1], t.Y[2]));
+    const int xmin = min(X[0], min(X[1], X[2])), xmax = max(X[0], max(X[1], X[2]));
+    const int ymin = min(Y[0], min(Y[1], Y[2])), ymax = max(Y[0], max(Y[1], Y[2]));
     const int h = kSubpixel / 2;
     t.ix0 = max(floor_div(xmin - h + kSubpixel - 1, kSubpixel), 0);
     t.ix1 = min(floor_div(xmax - h, kSubpixel), W - 1);
     t.jy0 = max(floor_div(ymin - h + kSubpixel - 1, kSubpixel), 0);
     t.jy1 = min(floor_div(ymax - h, kSubpixel), W - 1);
     if (t.ix0 > t.ix1 || t.jy0 > t.jy1) return;
-    t.flags |= 1;
+    const uint32_t cols = (uint32_t)(t.ix1 - t.ix0 + 1);
+    t.inv_cols = cols >= 2 ? 0xFFFFFFFFu / cols + 1u : 0u;
+    t.bits |= kValid;
+}
+
+// smoothstep(0.98, 1, d) of the road fragment program, each operation rounded; the
+// division only where the result is not clamped (the same bits as always dividing)
+__device__ __forceinline__ float road_edge_step(float d)
+{
+    if (d <= 0.98f) return 0.0f;
+    if (d >= 1.0f) return 1.0f;
+    return smoothstep_rn(0.98f, 1.0f, d);
+}
+
+// smoothstep(1, 2, d): the division by 2 - 1 = 1 is exact
+__device__ __forceinline__ float road_blend_step(float d)
+{
+    float t = fminf(fmaxf(__fsub_rn(d, 1.0f), 0.0f), 1.0f);
+    return __fmul_rn(__fmul_rn(t, t), __fsub_rn(3.0f, __fmul_rn(2.0f, t)));
 }
 
 __global__ void __launch_bounds__(kThreads)
 layers_kernel(float *elev, int W, int pitch, long long plane_stride, long long slot_stride, const DevJob *jobs,
-              const DevMesh *meshes, const float4 *verts, const uint32_t *idx, int blend_mode, int band_rows)
+              const DevMesh *meshes, const float4 *verts, const uint32_t *idx, int nv, int blend_mode, int band_rows)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     Tri *tris = reinterpret_cast<Tri *>(smem_raw);
     const int span = (band_rows + 2) * W;
-    float *zl = reinterpret_cast<float *>(tris + kThreads);
+    float *zl = reinterpret_cast<float *>(tris + kChunk);
     float *wv = zl + span;
     float *dep = wv + span;
     // the original zm of each band's last row, which the next band reads as its
@@ -169,6 +202,8 @@ layers_kernel(float *elev, int W, int pitch, long long plane_stride, long long s
     for (int b0 = 0, band = 0; b0 < W; b0 += band_rows, ++band) {
         const int b1 = min(b0 + band_rows, W);
         const int h0 = max(b0 - 1, 0), h1 = min(b1 + 1, W);
+        // warp `warp` owns the texels of rows [my_lo, my_hi) of the band and its halo
+        const int my_lo = h0 + warp * (h1 - h0) / kWarps, my_hi = h0 + (warp + 1) * (h1 - h0) / kWarps;
         float *save_now = saved + (band & 1) * W;
         const float *save_prev = saved + ((band + 1) & 1) * W;
         // the framebuffer before the layers: z = zm, w = 0, depth cleared to 1
@@ -180,42 +215,53 @@ layers_kernel(float *elev, int W, int pitch, long long plane_stride, long long s
             wv[t] = 0.0f;
             dep[t] = 1.0f;
         }
-        for (int base = 0; base < J.ntri; base += kThreads) {
+        for (int base = 0; base < J.ntri; base += kChunk) {
             __syncthreads();
-            if (base + (int)threadIdx.x < J.ntri) setup(tris[threadIdx.x], J, meshes, verts, idx, base + threadIdx.x, W);
+            if (threadIdx.x < kChunk && base + (int)threadIdx.x < J.ntri)
+                setup(tris[threadIdx.x], J, meshes, verts, idx, nv, base + threadIdx.x, W);
             __syncthreads();
-            const int cnt = min(kThreads, J.ntri - base);
-            for (int k = 0; k < cnt; ++k) {
-                const Tri &T = tris[k];
-                const int flags = T.flags;
-                if (flags & 2) {  // a new layer: its own pixels' depth back to 1
-                    for (int r = h0 + ((warp - h0) & (kWarps - 1)); r < h1; r += kWarps)
-                        for (int cc = lane; cc < W; cc += 32) dep[(r - h0) * W + cc] = 1.0f;
+            const int cnt = min(kChunk, J.ntri - base);
+            // each warp picks, 32 at a time, the triangles it must visit in order: those
+            // whose box meets its rows, and depth clears
+            for (int wb = 0; wb < cnt; wb += 32) {
+                bool want = false;
+                if (wb + lane < cnt) {
+                    const Tri &q = tris[wb + lane];
+                    want = (q.bits & kClear) || ((q.bits & kValid) && q.jy0 < my_hi && q.jy1 >= my_lo);
                 }
-                if (!(flags & 1)) continue;
-                const int lo = max(T.jy0, h0), hi = min(T.jy1, h1 - 1);
-                for (int r = lo + ((warp - lo) & (kWarps - 1)); r <= hi; r += kWarps) {
-                    const int py = r * kSubpixel + kSubpixel / 2;
-                    for (int i = T.ix0 + ((lane - T.ix0) & 31); i <= T.ix1; i += 32) {
-                        const int px = i * kSubpixel + kSubpixel / 2;
-                        const long long e0 = edge_fn(T.X[1], T.Y[1], T.X[2], T.Y[2], px, py);
-                        const long long e1 = edge_fn(T.X[2], T.Y[2], T.X[0], T.Y[0], px, py);
-                        const long long e2 = edge_fn(T.X[0], T.Y[0], T.X[1], T.Y[1], px, py);
-                        if (e0 < T.bias[0] || e1 < T.bias[1] || e2 < T.bias[2]) continue;
+                uint32_t mask = __ballot_sync(0xffffffffu, want);
+                while (mask) {  // (mask is the same in all lanes)
+                    __syncwarp();  // a texel's earlier writes are seen by the lane that reads it next
+                    const Tri T = tris[wb + __ffs(mask) - 1];
+                    mask &= mask - 1u;
+                    if (T.bits & kClear) {  // a new layer: its own texels' depth back to 1
+                        for (int t = lane; t < (my_hi - my_lo) * W; t += 32) dep[(my_lo - h0) * W + t] = 1.0f;
+                        __syncwarp();
+                    }
+                    if (!(T.bits & kValid)) continue;
+                    const int lo = max(T.jy0, my_lo), hi = min(T.jy1, my_hi - 1);
+                    // the box rows of this warp, flattened over the lanes
+                    const int cols = T.ix1 - T.ix0 + 1, count = (hi - lo + 1) * cols;
+                    for (int t = lane; t < count; t += 32) {
+                        const int q = cols >= 2 ? (int)__umulhi((uint32_t)t, T.inv_cols) : t;
+                        const int r = lo + q, i = T.ix0 + (t - q * cols);
+                        const int px = i * kSubpixel + kSubpixel / 2, py = r * kSubpixel + kSubpixel / 2;
+                        const long long e0 = T.C[0] + (long long)T.A[0] * px + (long long)T.B[0] * py;
+                        const long long e1 = T.C[1] + (long long)T.A[1] * px + (long long)T.B[1] * py;
+                        const long long e2 = T.C[2] + (long long)T.A[2] * px + (long long)T.B[2] * py;
+                        if (e0 < (T.bits & 1) || e1 < ((T.bits >> 1) & 1) || e2 < ((T.bits >> 2) & 1)) continue;
                         // plane form a0 + (a1 - a0) l1 + (a2 - a0) l2: constant attributes stay exact
                         const float l1 = __fdiv_rn(__ll2float_rn(e1), T.area);
                         const float l2 = __fdiv_rn(__ll2float_rn(e2), T.area);
-                        const float alt = __fadd_rn(__fadd_rn(T.alt[0], __fmul_rn(__fsub_rn(T.alt[1], T.alt[0]), l1)),
-                                                    __fmul_rn(__fsub_rn(T.alt[2], T.alt[0]), l2));
-                        const float u = __fadd_rn(__fadd_rn(T.u[0], __fmul_rn(__fsub_rn(T.u[1], T.u[0]), l1)),
-                                                  __fmul_rn(__fsub_rn(T.u[2], T.u[0]), l2));
+                        const float u = __fadd_rn(__fadd_rn(T.u0, __fmul_rn(T.du1, l1)), __fmul_rn(T.du2, l2));
                         const float d = fabsf(u);
                         const float depth = fminf(fmaxf(__fadd_rn(__fmul_rn(d, 0.1f), 0.3f), 0.0f), 1.0f);
                         const int p = (r - h0) * W + i;
                         if (!(depth < dep[p])) continue;
+                        const float alt = __fadd_rn(__fadd_rn(T.a0, __fmul_rn(T.da1, l1)), __fmul_rn(T.da2, l2));
                         dep[p] = depth;
-                        zl[p] = __fadd_rn(alt, __fmul_rn(0.03f, __fsub_rn(1.0f, smoothstep_rn(0.98f, 1.0f, d))));
-                        wv[p] = smoothstep_rn(1.0f, 2.0f, d);
+                        zl[p] = __fadd_rn(alt, __fmul_rn(0.03f, __fsub_rn(1.0f, road_edge_step(d))));
+                        wv[p] = road_blend_step(d);
                     }
                 }
             }
@@ -259,11 +305,12 @@ int band_rows_for(int W)
     return rows >= W ? W : rows;
 }
 
-}  // namespace
-
-extern "C" int tp_elevation_layers(tp_storage *elev, const tp_layer_job *jobs, int n, const tp_layer_mesh *meshes,
-                                   int n_meshes, const float *vertices, int n_vertices, const uint32_t *indices,
-                                   int n_indices, int blend_mode, void *stream)
+// Validates and numbers the meshes, copies what is in host memory into a device
+// buffer shared by all calls, launches, and waits for the launch (the buffer is
+// reused by the next call).  Vertices / indices are read in place when `*_dev`.
+int run_layers(tp_storage *elev, const tp_layer_job *jobs, int n, const tp_layer_mesh *meshes, int n_meshes,
+               const float *vertices, bool vert_dev, int n_vertices, const uint32_t *indices, bool idx_dev,
+               int n_indices, int blend_mode, void *stream)
 {
     using tp::fail;
     if (!elev || n < 0 || (n > 0 && !jobs) || n_meshes < 0 || (n_meshes > 0 && !meshes) || n_vertices < 0 ||
@@ -287,9 +334,10 @@ extern "C" int tp_elevation_layers(tp_storage *elev, const tp_layer_job *jobs, i
         if (M.first_index >= 0) {
             if ((long long)M.first_index + used > n_indices)
                 return fail(TP_E_BAD_ARG, "tp_elevation_layers: mesh indices out of range");
-            for (int k = 0; k < used; ++k)
-                if ((long long)M.first_vertex + indices[M.first_index + k] >= n_vertices)
-                    return fail(TP_E_BAD_ARG, "tp_elevation_layers: vertex index out of range");
+            if (!idx_dev)
+                for (int k = 0; k < used; ++k)
+                    if ((long long)M.first_vertex + indices[M.first_index + k] >= n_vertices)
+                        return fail(TP_E_BAD_ARG, "tp_elevation_layers: vertex index out of range");
         } else if ((long long)M.first_vertex + used > n_vertices) {
             return fail(TP_E_BAD_ARG, "tp_elevation_layers: mesh vertices out of range");
         }
@@ -324,8 +372,8 @@ extern "C" int tp_elevation_layers(tp_storage *elev, const tp_layer_job *jobs, i
     std::lock_guard<std::mutex> lk(mu);
     auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
     const size_t bj = al(sizeof(DevJob) * n), bm = al(sizeof(DevMesh) * (n_meshes ? n_meshes : 1));
-    const size_t bv = al(sizeof(float) * 4 * (size_t)(n_vertices ? n_vertices : 1));
-    const size_t bi = al(sizeof(uint32_t) * (size_t)(n_indices ? n_indices : 1));
+    const size_t bv = vert_dev ? 0 : al(sizeof(float) * 4 * (size_t)(n_vertices ? n_vertices : 1));
+    const size_t bi = idx_dev ? 0 : al(sizeof(uint32_t) * (size_t)(n_indices ? n_indices : 1));
     const size_t need = bj + bm + bv + bi;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     if (dcap < need) {
@@ -339,28 +387,48 @@ extern "C" int tp_elevation_layers(tp_storage *elev, const tp_layer_job *jobs, i
         if (e != cudaSuccess) return tp::cuda_fail("cudaMalloc (layer meshes)", e);
         dcap = need;
     }
+    const float4 *dv = vert_dev ? reinterpret_cast<const float4 *>(vertices)
+                                : reinterpret_cast<const float4 *>(dbuf + bj + bm);
+    const uint32_t *di = idx_dev ? indices : reinterpret_cast<const uint32_t *>(dbuf + bj + bm + bv);
     cudaError_t e = cudaMemcpyAsync(dbuf, dj.data(), sizeof(DevJob) * n, cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess && n_meshes)
         e = cudaMemcpyAsync(dbuf + bj, dm.data(), sizeof(DevMesh) * n_meshes, cudaMemcpyHostToDevice, s);
-    if (e == cudaSuccess && n_vertices)
+    if (e == cudaSuccess && n_vertices && !vert_dev)
         e = cudaMemcpyAsync(dbuf + bj + bm, vertices, sizeof(float) * 4 * (size_t)n_vertices, cudaMemcpyHostToDevice, s);
-    if (e == cudaSuccess && n_indices)
+    if (e == cudaSuccess && n_indices && !idx_dev)
         e = cudaMemcpyAsync(dbuf + bj + bm + bv, indices, sizeof(uint32_t) * (size_t)n_indices, cudaMemcpyHostToDevice,
                             s);
     if (e != cudaSuccess) return tp::cuda_fail("cudaMemcpyAsync (layer meshes)", e);
     const int rows = band_rows_for(W);
-    const size_t smem = sizeof(Tri) * kThreads + sizeof(float) * (3 * (size_t)(rows + 2) * W + 2 * (size_t)W);
+    const size_t smem = sizeof(Tri) * kChunk + sizeof(float) * (3 * (size_t)(rows + 2) * W + 2 * (size_t)W);
     e = cudaFuncSetAttribute(layers_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return tp::cuda_fail("cudaFuncSetAttribute (layers)", e);
     layers_kernel<<<n, kThreads, smem, s>>>(elev->base, W, elev->pitch, elev->plane_stride, elev->slot_stride,
                                             reinterpret_cast<const DevJob *>(dbuf),
-                                            reinterpret_cast<const DevMesh *>(dbuf + bj),
-                                            reinterpret_cast<const float4 *>(dbuf + bj + bm),
-                                            reinterpret_cast<const uint32_t *>(dbuf + bj + bm + bv), blend_mode, rows);
+                                            reinterpret_cast<const DevMesh *>(dbuf + bj), dv, di, n_vertices,
+                                            blend_mode, rows);
     e = cudaGetLastError();
     if (e != cudaSuccess) return tp::cuda_fail("layers kernel launch", e);
-    // the mesh buffer is reused by the next call
     e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) return tp::cuda_fail("cudaStreamSynchronize (layers)", e);
     return TP_OK;
+}
+
+}  // namespace
+
+extern "C" int tp_elevation_layers(tp_storage *elev, const tp_layer_job *jobs, int n, const tp_layer_mesh *meshes,
+                                   int n_meshes, const float *vertices, int n_vertices, const uint32_t *indices,
+                                   int n_indices, int blend_mode, void *stream)
+{
+    return run_layers(elev, jobs, n, meshes, n_meshes, vertices, false, n_vertices, indices, false, n_indices,
+                      blend_mode, stream);
+}
+
+extern "C" int tp_elevation_layers_device(tp_storage *elev, const tp_layer_job *jobs, int n,
+                                          const tp_layer_mesh *meshes, int n_meshes, const float *vertices_dev,
+                                          int n_vertices, const uint32_t *indices_dev, int n_indices, int blend_mode,
+                                          void *stream)
+{
+    return run_layers(elev, jobs, n, meshes, n_meshes, vertices_dev, true, n_vertices, indices_dev, true, n_indices,
+                      blend_mode, stream);
 }

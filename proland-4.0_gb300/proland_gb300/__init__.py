@@ -193,35 +193,69 @@ class HostPipeline:
 TRIANGLES, TRIANGLE_STRIP = 0, 1
 
 
+class LayerBatch:
+    """The meshes of a layer pass, packed once for tp_elevation_layers.  tiles: list of
+    (slot, meshes), meshes a list of (vertices [n, 4] float32 (x, y, altitude, u) in
+    clip coordinates, indices or None, mode, clear_depth)."""
+
+    def __init__(self, tiles):
+        verts, idx, meshes, jobs = [], [], [], []
+        nv = ni = 0
+        for slot, ms in tiles:
+            jobs.append(LayerJob(slot, len(meshes), len(ms), 0))
+            for v, ix, mode, clear in ms:
+                v = np.ascontiguousarray(v, np.float32).reshape(-1, 4)
+                m = LayerMesh()
+                m.first_vertex, m.mode, m.clear_depth = nv, mode, int(clear)
+                if ix is None:
+                    m.first_index, m.count = -1, v.shape[0]
+                else:
+                    ix = np.ascontiguousarray(ix, np.uint32)
+                    m.first_index, m.count = ni, ix.size
+                    idx.append(ix)
+                    ni += ix.size
+                verts.append(v)
+                nv += v.shape[0]
+                meshes.append(m)
+        self.vertices = np.concatenate(verts) if verts else np.zeros((0, 4), np.float32)
+        self.indices = np.concatenate(idx) if idx else np.zeros(0, np.uint32)
+        self.jobs = (LayerJob * max(1, len(jobs)))(*jobs)
+        self.meshes = (LayerMesh * max(1, len(meshes)))(*meshes)
+        self.n_jobs, self.n_meshes, self.n_vertices, self.n_indices = len(jobs), len(meshes), nv, ni
+
+    def pin(self, torch):
+        """Moves the vertex and index arrays into pinned host memory (asynchronous uploads)."""
+        for name in ("vertices", "indices"):
+            a = getattr(self, name)
+            t = torch.empty(a.shape, dtype=torch.float32 if a.dtype == np.float32 else torch.int32,
+                            pin_memory=True)
+            pinned = t.numpy().view(a.dtype)
+            pinned[...] = a
+            setattr(self, name, pinned)
+            setattr(self, "_" + name + "_pinned", t)
+        return self
+
+    def to_device(self, torch):
+        """Device copies of the vertex and index arrays, for run_device."""
+        self._dv = torch.from_numpy(np.ascontiguousarray(self.vertices)).cuda()
+        self._di = torch.from_numpy(np.ascontiguousarray(self.indices).view(np.int32)).cuda()
+        return self
+
+    def run(self, elev, blend_mode=0, stream=None):
+        check(lib().tp_elevation_layers(elev.handle, self.jobs, self.n_jobs, self.meshes, self.n_meshes,
+                                        self.vertices.ctypes.data, self.n_vertices, self.indices.ctypes.data,
+                                        self.n_indices, blend_mode, stream))
+
+    def run_device(self, elev, blend_mode=0, stream=None):
+        check(lib().tp_elevation_layers_device(elev.handle, self.jobs, self.n_jobs, self.meshes, self.n_meshes,
+                                               C.c_void_p(self._dv.data_ptr()), self.n_vertices,
+                                               C.c_void_p(self._di.data_ptr()), self.n_indices, blend_mode, stream))
+
+
 def elevation_layers(elev, tiles, blend_mode=0, stream=None):
     """Road layer meshes drawn into produced elevation tiles and blended into zm
-    (tp_elevation_layers).  tiles: list of (slot, meshes), meshes a list of
-    (vertices [n, 4] float32 (x, y, altitude, u) in clip coordinates, indices or None,
-    mode, clear_depth)."""
-    verts, idx, meshes, jobs = [], [], [], []
-    nv = ni = 0
-    for slot, ms in tiles:
-        jobs.append(LayerJob(slot, len(meshes), len(ms), 0))
-        for v, ix, mode, clear in ms:
-            v = np.ascontiguousarray(v, np.float32).reshape(-1, 4)
-            m = LayerMesh()
-            m.first_vertex, m.mode, m.clear_depth = nv, mode, int(clear)
-            if ix is None:
-                m.first_index, m.count = -1, v.shape[0]
-            else:
-                ix = np.ascontiguousarray(ix, np.uint32)
-                m.first_index, m.count = ni, ix.size
-                idx.append(ix)
-                ni += ix.size
-            verts.append(v)
-            nv += v.shape[0]
-            meshes.append(m)
-    va = np.concatenate(verts) if verts else np.zeros((0, 4), np.float32)
-    ia = np.concatenate(idx) if idx else np.zeros(0, np.uint32)
-    ja = (LayerJob * max(1, len(jobs)))(*jobs)
-    ma = (LayerMesh * max(1, len(meshes)))(*meshes)
-    check(lib().tp_elevation_layers(elev.handle, ja, len(jobs), ma, len(meshes), va.ctypes.data, nv,
-                                    ia.ctypes.data, ni, blend_mode, stream))
+    (tp_elevation_layers); tiles as for LayerBatch."""
+    LayerBatch(tiles).run(elev, blend_mode, stream)
 
 
 # ---------------------------------------------------------------- ortho tiles

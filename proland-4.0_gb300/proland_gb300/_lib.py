@@ -206,6 +206,8 @@ def lib():
         "tp_learned_gather": ([_vp, _vp, _vp, _i, C.POINTER(_i), C.POINTER(_i), _i, _vp, _vp, _vp], _i),
         "tp_elevation_layers": ([_vp, C.POINTER(LayerJob), _i, C.POINTER(LayerMesh), _i, _vp, _i, _vp, _i, _i, _vp],
                                 _i),
+        "tp_elevation_layers_device": ([_vp, C.POINTER(LayerJob), _i, C.POINTER(LayerMesh), _i, _vp, _i, _vp, _i,
+                                        _i, _vp], _i),
         "tp_layer_builder_add_mesh": ([_vp, _vp, _i, _vp, _i, _i], _i),
         "tp_elevation_producer_add_layer": ([_vp, LAYER_FN, _vp], _i),
         "tp_elevation_producer_set_blend": ([_vp, _i], _i),

@@ -18,6 +18,14 @@
         printf("ok %s\n", what);                                            \
     } while (0)
 
+/* A layer callback: one triangle strip (never called here: nothing is produced without a GPU). */
+static int road_layer(void *user, int level, int tx, int ty, tp_layer_builder *b)
+{
+    static const float v[16] = {-1, -0.1f, 10, -3, -1, 0.1f, 10, 3, 1, -0.1f, 10, -3, 1, 0.1f, 10, 3};
+    (void)user; (void)level; (void)tx; (void)ty;
+    return tp_layer_builder_add_mesh(b, v, 4, NULL, 0, TP_TRIANGLE_STRIP);
+}
+
 int main(int argc, char **argv)
 {
     if (argc < 3) {
@@ -77,6 +85,12 @@ int main(int argc, char **argv)
               tp_normal_producer_create(nc, elev, 0, &nrm) == TP_OK,
           "producers");
     CHECK(tp_producer_border(elev) == 2 && tp_producer_border(nrm) == 0, "borders");
+    /* a road layer on the elevation producer (TileProducer::addLayer); only elevation
+     * producers take layers, and the blend program is 0 or 1 */
+    CHECK(tp_elevation_producer_add_layer(elev, road_layer, NULL) == TP_OK &&
+              tp_elevation_producer_add_layer(nrm, road_layer, NULL) == TP_E_BAD_ARG &&
+              tp_elevation_producer_set_blend(elev, 1) == TP_OK && tp_elevation_producer_set_blend(elev, 2) == TP_E_BAD_ARG,
+          "layers");
     tp_tile *t = tp_producer_get_tile(nrm, 2, 1, 3);
     int level, tx, ty, slot, users, done;
     CHECK(t != NULL && tp_tile_info(t, &level, &tx, &ty, &slot, &users, &done) == TP_OK && level == 2 && users == 1 &&

@@ -140,3 +140,37 @@ def test_layered_producer_levels(gpu, oracle_lib, blend_mode):
         enx, eny = orc.normals_flat(W, want[t][2], ROOT / (1 << t[0]))
         assert_normals_close(ns.download(h.slot, 1, tp.NX)[0], enx, "nx %s" % (t,))
         assert_normals_close(ns.download(h.slot, 1, tp.NY)[0], eny, "ny %s" % (t,))
+
+
+def test_device_meshes_same_as_host(gpu, oracle_lib):
+    """tp_elevation_layers_device reads the meshes from device memory: the same tiles;
+    an index past the vertex array drops its triangle there."""
+    import torch
+    tp = gpu
+    W, n = 101, 4
+    rng = np.random.default_rng(11)
+    zf = (rng.standard_normal((n, W, W)) * 200.0).astype(np.float32)
+    zm = np.maximum(zf, np.float32(0.0))
+    elev = tp.TileStorage(W, 3, n)
+    meshes = [tile_meshes(rng, W, k) for k in range(n)]
+    batch = tp.LayerBatch(list(zip(range(n), meshes)))
+    outs = []
+    for run in (lambda: batch.run(elev), lambda: batch.to_device(torch).run_device(elev)):
+        elev.upload(0, tp.ZF, zf)
+        elev.upload(0, tp.ZM, zm)
+        run()
+        tp.stream_check()
+        outs.append(elev.download(0, n, tp.ZM))
+    assert np.array_equal(outs[0], outs[1])
+    for k in range(n):
+        assert np.array_equal(outs[0][k], oracle_lib.layer_tile(W, zf[k], zm[k], meshes[k], 0))
+    # one triangle whose third index is out of range, next to a valid one
+    v = np.array([[-0.5, -0.5, 50, 0], [0.5, -0.5, 50, 0], [0.0, 0.5, 50, 0]], np.float32)
+    bad = tp.LayerBatch([(0, [(v, np.array([0, 1, 2, 0, 1, 3], np.uint32), tp.TRIANGLES, True)])])
+    bad.to_device(torch)
+    elev.upload(0, tp.ZF, zf[:1])
+    elev.upload(0, tp.ZM, zm[:1])
+    bad.run_device(elev)
+    tp.stream_check()
+    want = oracle_lib.layer_tile(W, zf[0], zm[0], [(v, np.array([0, 1, 2], np.uint32), 0, True)], 0)
+    assert np.array_equal(elev.download(0, 1, tp.ZM)[0], want)
