@@ -743,7 +743,7 @@ def main():
         fc.dev_jobs.copy_(torch.frombuffer(bytearray(bytes(arr)), dtype=torch.uint8))
     torch.cuda.synchronize()
 
-    # the whole frame (both tile widths) is one persistent launch, replayed from a CUDA graph
+    # the whole frame (one persistent launch per tile width, the two overlapping), replayed from a CUDA graph
     frame = tp.Frame()
     for fc in classes:
         frame.add_device(fc.elev, fc.res, fc.nrm, params, C.c_void_p(fc.dev_jobs.data_ptr()), fc.n,
@@ -786,6 +786,24 @@ def main():
     ms_step = ms_total / args.steps
     tiles = sum(fc.n for fc in classes)
     value = replicas.whole_job_rate(tiles, ms_step, world)
+
+    # the same frame with the two launches one after the other, for comparison
+    separate_ms = None
+    if len(classes) == 2:
+        frame.overlap_classes(False)
+        with torch.cuda.stream(stream):
+            for _ in range(warmup):
+                frame.graph_launch(sh)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(args.steps):
+            frame.graph_launch(sh)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        tp.stream_check(sh)
+        separate_ms = e0.elapsed_time(e1) / args.steps
+        frame.overlap_classes(True)
 
     # per tile width: each width alone in its own frame, same tuned shape
     per_width = {}
@@ -854,8 +872,11 @@ def main():
                    "form": "plain", "l2": "inputs larger than L2 (%.2f GB per step)" % (sum(alg.values()) / 1e9),
                    "parallelism": "replicas" if world > 1 else "single GPU", "autotuned": tuned},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": traffic, "peak_source": peak_src, "kernel": "frame_kernel (one persistent launch per tile width, replayed from a CUDA graph)",
+                     "traffic": traffic, "peak_source": peak_src,
+                     "kernel": "frame_kernel (one persistent launch per tile width, the two on forked "
+                               "streams of a CUDA graph)",
                      "kernel_ms": kernel_ms, "units_per_launch": frame.units(), "per_width": per_width,
+                     "serialised_launches_ms_per_step": separate_ms,
                      "algorithmic_bytes_per_step": sum(alg.values())},
         "e2e": {"value": world * tiles / (e2e_step / 1000.0), "unit": UNIT, "ms_per_step": e2e_step,
                 "h2d_bytes_per_step": sum(fc.h2d_bytes for fc in classes),

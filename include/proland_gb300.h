@@ -210,6 +210,12 @@ int tp_frame_add_device(tp_frame *f, tp_storage *elev, tp_storage *residuals, tp
 int tp_frame_launch(tp_frame *f, void *stream);
 int tp_frame_graph_launch(tp_frame *f, void *stream);
 int tp_frame_units(const tp_frame *f);   /* work units of one launch */
+/* A frame with two tile widths launches the second width's persistent kernel on a
+ * stream forked from `stream` and joined back into it (in a graph: two parallel
+ * kernel nodes), so that its CTAs start while the first kernel's last wave drains;
+ * the widths share no data.  on = 0 launches them one after the other on `stream`.
+ * Overlap is the default. */
+int tp_frame_overlap_classes(tp_frame *f, int on);
 /* Autotuner: times each tile width's launch under every candidate work-unit
  * shape -- band height (whole tile vs 2..6 bands), one or two shared-memory
  * stages per CTA, two or three CTAs per SM -- `repeats` times each, on the

@@ -30,6 +30,11 @@ struct tp_frame {
     tp_tile_job *jobs_buf = nullptr;
     size_t jobs_buf_count = 0;
     bool uploaded = false;
+    // two tile widths: their launches on forked streams, so that the CTAs of one
+    // start while the other's last wave drains
+    bool overlap = true;
+    cudaStream_t side = nullptr;
+    cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
     // CUDA graph of (reset + launch), built on first tp_frame_graph_launch
     cudaGraphExec_t graph = nullptr;
     cudaStream_t graph_stream = nullptr;
@@ -261,6 +266,24 @@ int enqueue(tp_frame *f, const tp::FrameLaunch *F, void *stream)
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     cudaError_t e = cudaMemsetAsync(f->flags, 0, sizeof(int) * f->flags_count, s);
     if (e != cudaSuccess) return tp::cuda_fail("cudaMemsetAsync (frame flags)", e);
+    int active = 0;
+    for (int c = 0; c < f->nclasses; ++c) active += F[c].c.njobs * F[c].c.bands > 0 ? 1 : 0;
+    // the classes share no data: with two of them, the second goes on a side stream
+    // forked from (and joined back into) `stream`; in a graph capture this makes
+    // two parallel kernel nodes
+    const bool fork = f->overlap && active == 2;
+    if (fork) {
+        if (!f->side) {
+            e = cudaStreamCreateWithFlags(&f->side, cudaStreamNonBlocking);
+            if (e == cudaSuccess) e = cudaEventCreateWithFlags(&f->fork_ev, cudaEventDisableTiming);
+            if (e == cudaSuccess) e = cudaEventCreateWithFlags(&f->join_ev, cudaEventDisableTiming);
+            if (e != cudaSuccess) return tp::cuda_fail("frame side stream", e);
+        }
+        e = cudaEventRecord(f->fork_ev, s);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(f->side, f->fork_ev, 0);
+        if (e != cudaSuccess) return tp::cuda_fail("frame fork", e);
+    }
+    int launched = 0;
     for (int c = 0; c < f->nclasses; ++c) {
         const tp::FrameLaunch &L = F[c];
         const int units = L.c.njobs * L.c.bands;
@@ -270,8 +293,14 @@ int enqueue(tp_frame *f, const tp::FrameLaunch *F, void *stream)
         if (rc) return rc;
         if (per_sm < 1) return tp::fail(TP_E_BAD_ARG, "frame: the kernel's stage does not fit in shared memory");
         const int grid = std::min(units, per_sm * sm_count());
-        rc = tp::launch_frame(L, f->cls[c].pmap, f->cls[c].rmap, grid, stream);
+        rc = tp::launch_frame(L, f->cls[c].pmap, f->cls[c].rmap, grid, fork && launched == 1 ? f->side : stream);
         if (rc) return rc;
+        ++launched;
+    }
+    if (fork) {
+        e = cudaEventRecord(f->join_ev, f->side);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(s, f->join_ev, 0);
+        if (e != cudaSuccess) return tp::cuda_fail("frame join", e);
     }
     return TP_OK;
 }
@@ -326,9 +355,23 @@ extern "C" int tp_frame_destroy(tp_frame *f)
 {
     if (!f) return TP_OK;
     drop_graph(f);
+    if (f->side) {
+        cudaStreamSynchronize(f->side);
+        cudaStreamDestroy(f->side);
+        cudaEventDestroy(f->fork_ev);
+        cudaEventDestroy(f->join_ev);
+    }
     if (f->flags) cudaFree(f->flags);
     if (f->jobs_buf) cudaFree(f->jobs_buf);
     delete f;
+    return TP_OK;
+}
+
+extern "C" int tp_frame_overlap_classes(tp_frame *f, int on)
+{
+    if (!f) return tp::fail(TP_E_BAD_ARG, "tp_frame_overlap_classes: frame is NULL");
+    if (f->overlap != (on != 0)) drop_graph(f);
+    f->overlap = on != 0;
     return TP_OK;
 }
 

@@ -385,6 +385,10 @@ class Frame:
     def graph_launch(self, stream=None):
         check(lib().tp_frame_graph_launch(self.handle, stream))
 
+    def overlap_classes(self, on=True):
+        """Two tile widths' launches on forked streams (default) or one after the other."""
+        check(lib().tp_frame_overlap_classes(self.handle, int(bool(on))))
+
     def units(self):
         return check(lib().tp_frame_units(self.handle))
 

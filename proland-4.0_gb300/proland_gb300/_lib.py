@@ -147,6 +147,7 @@ def lib():
         "tp_frame_launch": ([_vp, _vp], _i),
         "tp_frame_graph_launch": ([_vp, _vp], _i),
         "tp_frame_units": ([_vp], _i),
+        "tp_frame_overlap_classes": ([_vp, _i], _i),
         "tp_frame_autotune": ([_vp, _vp, _i], _i),
         "tp_frame_config": ([_vp, _i, C.POINTER(_i), C.POINTER(_i), C.POINTER(_i)], _i),
         "tp_status": ([C.POINTER(_i), _i], _i),
