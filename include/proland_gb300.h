@@ -452,6 +452,11 @@ int tp_ortho_batch(tp_storage *ortho, tp_storage *residuals, const tp_ortho_para
 /* Same with the job array in device memory (not validated on the host). */
 int tp_ortho_batch_device(tp_storage *ortho, tp_storage *residuals, const tp_ortho_params *params,
                           const tp_ortho_job *jobs_dev, int n, void *stream);
+/* Self-check of the known-divisor division the ortho kernel uses for its constant
+ * divisors (6, 255, 0.4): compares it with the correctly rounded division for all
+ * 2^32 dividends on the device; *mismatches receives the number of differing
+ * results (0 expected) and *first_mismatch the bits of the first one (or ~0). */
+int tp_division_self_test(float divisor, unsigned long long *mismatches, uint32_t *first_mismatch);
 
 /* The ortho producers behind the TileCache / TileProducer protocol above
  * (tp_producer_get_tile / put_tile / has_tile / border, tp_scheduler_run,

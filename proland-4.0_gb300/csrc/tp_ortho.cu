@@ -44,6 +44,26 @@ __device__ __forceinline__ float s_(float a, float b) { return __fsub_rn(a, b); 
 __device__ __forceinline__ float d_(float a, float b) { return __fdiv_rn(a, b); }
 __device__ __forceinline__ float clamp01(float v) { return v < 0.0f ? 0.0f : (v > 1.0f ? 1.0f : v); }
 
+// x / y for a divisor known in advance, with z = RN(1 / y): q = RN(x z), the exact
+// remainder r = x - q y by one FMA, then RN(q + r z) -- the one-correction scheme
+// for known divisors of Brisebarre, Muller and Raina (IEEE Trans. Computers 53(8),
+// 2004), which returns the correctly rounded quotient for every x when y passes
+// their test.  Outside 2^-96 <= |x| <= 2^96 (and for infinities and NaN) the
+// correctly rounded division is called (y > 0).  tp_division_self_test compares it with
+// the correctly rounded division over all 2^32 x for the divisors used here.
+__device__ __forceinline__ float div_known(float x, float y, float z)
+{
+    const float ax = fabsf(x);
+    if (ax <= 0x1p96f && ax >= 0x1p-96f) {
+        const float q = __fmul_rn(x, z);
+        const float r = __fmaf_rn(-q, y, x);
+        return __fmaf_rn(r, z, q);
+    }
+    if (ax == 0.0f) return __fmul_rn(x, z);  // +-0 / y = +-0 (y > 0)
+    return __fdiv_rn(x, y);
+}
+constexpr float kInv6 = 1.0f / 6.0f, kInv255 = 1.0f / 255.0f, kInv04 = 1.0f / 0.4f;
+
 // Byte c of w as a float, exactly: the byte placed in the mantissa of 2^23
 // (0x4B0000bb) minus 2^23.
 __device__ __forceinline__ float byte_of(uint32_t w, int c)
@@ -83,7 +103,8 @@ __device__ __forceinline__ void rgb_to_hsv(const float *rgb, float *hsv)
         hsv[1] = d_(delta, mx);
         float d[3];
 #pragma unroll
-        for (int c = 0; c < 3; ++c) d[c] = d_(a_(d_(s_(mx, rgb[c]), 6.0f), m_(delta, 0.5f)), delta);  // delta / 2 exact
+        for (int c = 0; c < 3; ++c)
+            d[c] = d_(a_(div_known(s_(mx, rgb[c]), 6.0f, kInv6), m_(delta, 0.5f)), delta);  // delta / 2 exact
         if (rgb[0] == mx) hsv[0] = s_(d[2], d[1]);
         else if (rgb[1] == mx) hsv[0] = s_(a_(1.0f / 3.0f, d[0]), d[2]);
         else if (rgb[2] == mx) hsv[0] = s_(a_(2.0f / 3.0f, d[1]), d[0]);
@@ -127,11 +148,12 @@ __device__ __forceinline__ uint32_t texel(float (&r)[4], const float (&nv)[4], c
         }
         rgb_to_hsv(rgb, h);
         // 1 - smoothstep(0.4, 0.8, v); 0.8f - 0.4f is exactly 0.4f
-        float t = clamp01(d_(s_(h[2], 0.4f), s_(0.8f, 0.4f)));
+        float t = clamp01(div_known(s_(h[2], 0.4f), 0.4f, kInv04));
         t = m_(m_(t, t), s_(3.0f, m_(2.0f, t)));
         const float k = s_(1.0f, t);
 #pragma unroll
-        for (int c = 0; c < 3; ++c) h[c] = m_(h[c], a_(1.0f, d_(m_(m_(k, nc[c]), s_(nv[c], 128.0f)), 255.0f)));
+        for (int c = 0; c < 3; ++c)
+            h[c] = m_(h[c], a_(1.0f, div_known(m_(m_(k, nc[c]), s_(nv[c], 128.0f)), 255.0f, kInv255)));
         h[0] = s_(h[0], floorf(h[0]));
         h[1] = clamp01(h[1]);
         h[2] = clamp01(h[2]);
@@ -307,3 +329,51 @@ int launch_ortho(const OrthoLaunch &L, void *stream)
 }
 
 }  // namespace tp
+
+namespace {
+
+__global__ void division_check_kernel(float y, float z, unsigned long long *mismatches, uint32_t *first)
+{
+    unsigned long long bad = 0;
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t b = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; b <= 0xFFFFFFFFull; b += stride) {
+        const float x = __uint_as_float((uint32_t)b);
+        const float f = div_known(x, y, z), e = __fdiv_rn(x, y);
+        const bool same = __float_as_uint(f) == __float_as_uint(e) || (f != f && e != e);
+        if (!same) {
+            ++bad;
+            atomicMin(first, (uint32_t)b);
+        }
+    }
+    if (bad) atomicAdd(mismatches, bad);
+}
+
+}  // namespace
+
+extern "C" int tp_division_self_test(float divisor, unsigned long long *mismatches, uint32_t *first_mismatch)
+{
+    if (!mismatches || !(divisor > 0.0f) || !(divisor < 1e30f))
+        return tp::fail(TP_E_BAD_ARG, "tp_division_self_test: bad arguments");
+    unsigned long long *d_count = nullptr;
+    cudaError_t e = cudaMalloc(&d_count, sizeof(unsigned long long) + sizeof(uint32_t));
+    if (e != cudaSuccess) return tp::cuda_fail("cudaMalloc (division check)", e);
+    uint32_t *d_first = reinterpret_cast<uint32_t *>(d_count + 1);
+    const unsigned long long zero = 0;
+    const uint32_t none = 0xFFFFFFFFu;
+    cudaMemcpy(d_count, &zero, sizeof zero, cudaMemcpyHostToDevice);
+    cudaMemcpy(d_first, &none, sizeof none, cudaMemcpyHostToDevice);
+    int dev = 0, sms = 1;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const float z = 1.0f / divisor;  // correctly rounded on the host as on the device
+    division_check_kernel<<<sms * 8, 256>>>(divisor, z, d_count, d_first);
+    e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    if (e == cudaSuccess) e = cudaMemcpy(mismatches, d_count, sizeof(unsigned long long), cudaMemcpyDeviceToHost);
+    uint32_t first = none;
+    if (e == cudaSuccess) e = cudaMemcpy(&first, d_first, sizeof first, cudaMemcpyDeviceToHost);
+    cudaFree(d_count);
+    if (e != cudaSuccess) return tp::cuda_fail("division check", e);
+    if (first_mismatch) *first_mismatch = first;
+    return TP_OK;
+}

@@ -259,6 +259,14 @@ def elevation_layers(elev, tiles, blend_mode=0, stream=None):
 
 
 # ---------------------------------------------------------------- ortho tiles
+def division_self_test(divisor):
+    """(mismatches, first mismatching dividend bits) of the ortho kernel's known-divisor
+    division against the correctly rounded one, over all 2^32 dividends."""
+    n, first = C.c_ulonglong(), C.c_uint32()
+    check(lib().tp_division_self_test(divisor, C.byref(n), C.byref(first)))
+    return n.value, first.value
+
+
 def ortho_noise(tile_width):
     """createOrthoNoise: [6, W, W, 4] uint8."""
     out = np.empty((6, tile_width, tile_width, 4), np.uint8)

@@ -128,3 +128,11 @@ def test_bad_jobs_are_rejected(gpu):
     with pytest.raises(tp.TPError):
         tp.ortho_batch(tp.TileStorage(197, 1, 2), None, params, [tp.make_ortho_job(0, 0, 0, out_slot=0)])
     tp.stream_check()
+
+
+@pytest.mark.parametrize("divisor", [6.0, 255.0, 0.4])
+def test_known_divisor_division_is_correctly_rounded(gpu, divisor):
+    """The HSV path divides by 6, 255 and 0.4 with a multiply and one FMA correction:
+    it must equal the correctly rounded division for every one of the 2^32 dividends."""
+    mismatches, first = gpu.division_self_test(divisor)
+    assert mismatches == 0, "%d dividends differ (first 0x%08x)" % (mismatches, first)
