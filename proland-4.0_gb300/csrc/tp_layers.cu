@@ -39,7 +39,7 @@
 namespace {
 
 constexpr int kThreads = 1024;
-constexpr int kChunk = 256;   // triangles set up at once (one per thread of the first kChunk)
+constexpr int kChunk = 512;   // triangles set up at once (one per thread of the first kChunk)
 constexpr int kWarps = kThreads / 32;
 constexpr int kSubpixel = 256;              // 8 sub-texel bits
 constexpr float kMaxSnapped = 8388608.0f;   // |window coordinate| * 256 <= 2^23
