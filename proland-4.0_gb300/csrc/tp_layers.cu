@@ -16,13 +16,14 @@
 // (graph1/blendShader.glsl, edit3, river1), or by the 3x3 box filter of that blend
 // (demo/shaders/elevation/blendShader.glsl).
 //
-// Here one CTA produces one tile: the tile's z, w and depth live in shared memory
-// (row bands of at most ~140 KB for wide tiles), triangles are set up 256 at a time
-// (one per thread) and rasterised in order.  Each warp owns a block of rows and
-// walks, for every triangle, the texels of the triangle's box in its rows, spread
-// over its lanes; every texel is written by one warp only, in triangle order, so the
-// per-texel order of primitives is the draw order, as GL guarantees.  Rasterisation rules (the reference leaves them to the GL
-// driver): vertex window coordinates snapped to 1/256 texel, coverage of the texel
+// Here one CTA produces one tile: the CTA sets up all the tile's triangles (records
+// in global scratch), then, per depth-clear segment, its warps take triangles in
+// turn and keep per texel, in shared memory, the least (depth, triangle number) key
+// of the fragments (GL's LESS test keeps the first fragment of least depth), and a
+// resolve pass writes z and w of the winning fragments; then the blend.  Texel
+// state (key, z, w: 16 bytes) for the whole tile, or row bands of wide tiles.
+// Rasterisation rules (the reference leaves them to the GL driver): vertex window
+// coordinates snapped to 1/256 texel, coverage of the texel
 // centre by exact integer edge functions with a top-left rule (y up, row 0 at the
 // bottom), attributes interpolated at the texel centre in the plane form
 // a0 + (a1 - a0) l1 + (a2 - a0) l2 of the barycentric weights l_k, fp32 depth.
@@ -39,7 +40,6 @@
 namespace {
 
 constexpr int kThreads = 1024;
-constexpr int kChunk = 512;   // triangles set up at once (one per thread of the first kChunk)
 constexpr int kWarps = kThreads / 32;
 constexpr int kSubpixel = 256;              // 8 sub-texel bits
 constexpr float kMaxSnapped = 8388608.0f;   // |window coordinate| * 256 <= 2^23
@@ -50,6 +50,7 @@ struct DevMesh {
 };
 struct DevJob {
     int slot, first_mesh, n_meshes, ntri;
+    long long tri_offset;  // the tile's first triangle record in the call's scratch
 };
 
 // One triangle after set-up (counter-clockwise, snapped): edge q (from vertex q + 1
@@ -181,109 +182,123 @@ __device__ __forceinline__ float road_blend_step(float d)
     return __fmul_rn(__fmul_rn(t, t), __fsub_rn(3.0f, __fmul_rn(2.0f, t)));
 }
 
+// The fragment of triangle T at the centre of texel (i, r), if T covers it: the
+// barycentric weights l1, l2 (plane form), the road-width distance d and the depth.
+__device__ __forceinline__ bool fragment(const Tri &T, int i, int r, float &l1, float &l2, float &d, float &depth)
+{
+    const int px = i * kSubpixel + kSubpixel / 2, py = r * kSubpixel + kSubpixel / 2;
+    const long long e0 = T.C[0] + (long long)T.A[0] * px + (long long)T.B[0] * py;
+    const long long e1 = T.C[1] + (long long)T.A[1] * px + (long long)T.B[1] * py;
+    const long long e2 = T.C[2] + (long long)T.A[2] * px + (long long)T.B[2] * py;
+    if (e0 < (T.bits & 1) || e1 < ((T.bits >> 1) & 1) || e2 < ((T.bits >> 2) & 1)) return false;
+    // plane form a0 + (a1 - a0) l1 + (a2 - a0) l2: constant attributes stay exact
+    l1 = __fdiv_rn(__ll2float_rn(e1), T.area);
+    l2 = __fdiv_rn(__ll2float_rn(e2), T.area);
+    const float u = __fadd_rn(__fadd_rn(T.u0, __fmul_rn(T.du1, l1)), __fmul_rn(T.du2, l2));
+    d = fabsf(u);
+    depth = fminf(fmaxf(__fadd_rn(__fmul_rn(d, 0.1f), 0.3f), 0.0f), 1.0f);
+    return true;
+}
+
+// Within a depth-clear segment, GL's LESS test leaves at a texel the first fragment
+// of least depth below the cleared 1: the least (depth bits, triangle number) key,
+// depth >= 0 ordering its bits as it orders the floats.  So the triangles of a
+// segment are drawn in any order by a 64-bit atomic minimum per covered texel, and
+// a resolve pass writes z and w of each texel's winning fragment.
 __global__ void __launch_bounds__(kThreads)
 layers_kernel(float *elev, int W, int pitch, long long plane_stride, long long slot_stride, const DevJob *jobs,
-              const DevMesh *meshes, const float4 *verts, const uint32_t *idx, int nv, int blend_mode, int band_rows)
+              const DevMesh *meshes, const float4 *verts, const uint32_t *idx, int nv, int blend_mode, int band_rows,
+              Tri *scratch)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    Tri *tris = reinterpret_cast<Tri *>(smem_raw);
     const int span = (band_rows + 2) * W;
-    float *zl = reinterpret_cast<float *>(tris + kChunk);
+    unsigned long long *key = reinterpret_cast<unsigned long long *>(smem_raw);
+    float *zl = reinterpret_cast<float *>(key + span);
     float *wv = zl + span;
-    float *dep = wv + span;
+    float *bl = reinterpret_cast<float *>(key);  // the blend values, once the keys are done
     // the original zm of each band's last row, which the next band reads as its
     // lower halo after this band has written its output (two rows, alternating)
-    float *saved = dep + span;
+    float *saved = wv + span;
     const DevJob J = jobs[blockIdx.x];
     float *zf_plane = elev + (long long)J.slot * slot_stride;
     float *zm_plane = zf_plane + 2 * plane_stride;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    Tri *tt = scratch + J.tri_offset;
+    for (int g = threadIdx.x; g < J.ntri; g += kThreads) setup(tt[g], J, meshes, verts, idx, nv, g, W);
+    __syncthreads();
 
+    const int mend = J.first_mesh + J.n_meshes;
     for (int b0 = 0, band = 0; b0 < W; b0 += band_rows, ++band) {
         const int b1 = min(b0 + band_rows, W);
         const int h0 = max(b0 - 1, 0), h1 = min(b1 + 1, W);
-        // warp `warp` owns the texels of rows [my_lo, my_hi) of the band and its halo
-        const int my_lo = h0 + warp * (h1 - h0) / kWarps, my_hi = h0 + (warp + 1) * (h1 - h0) / kWarps;
+        const int nt = (h1 - h0) * W;
         float *save_now = saved + (band & 1) * W;
         const float *save_prev = saved + ((band + 1) & 1) * W;
-        // the framebuffer before the layers: z = zm, w = 0, depth cleared to 1
-        for (int t = threadIdx.x; t < (h1 - h0) * W; t += kThreads) {
+        // the framebuffer before the layers: z = zm, w = 0
+        for (int t = threadIdx.x; t < nt; t += kThreads) {
             const int r = h0 + t / W, cc = t - (t / W) * W;
             const float z = (b0 > 0 && r == h0) ? save_prev[cc] : zm_plane[(long long)r * pitch + cc];
             if (r == b1 - 1) save_now[cc] = z;
             zl[t] = z;
             wv[t] = 0.0f;
-            dep[t] = 1.0f;
         }
-        for (int base = 0; base < J.ntri; base += kChunk) {
+        // segments: runs of meshes, a new one at each mesh that clears the depth buffer
+        for (int m = J.first_mesh; m < mend;) {
+            int m2 = m + 1;
+            while (m2 < mend && !meshes[m2].clear) ++m2;
+            const int seg0 = meshes[m].tri_base, seg1 = m2 < mend ? meshes[m2].tri_base : J.ntri;
+            m = m2;
+            if (seg0 == seg1) continue;
+            for (int t = threadIdx.x; t < nt; t += kThreads) key[t] = ~0ull;
             __syncthreads();
-            if (threadIdx.x < kChunk && base + (int)threadIdx.x < J.ntri)
-                setup(tris[threadIdx.x], J, meshes, verts, idx, nv, base + threadIdx.x, W);
-            __syncthreads();
-            const int cnt = min(kChunk, J.ntri - base);
-            // each warp picks, 32 at a time, the triangles it must visit in order: those
-            // whose box meets its rows, and depth clears
-            for (int wb = 0; wb < cnt; wb += 32) {
-                bool want = false;
-                if (wb + lane < cnt) {
-                    const Tri &q = tris[wb + lane];
-                    want = (q.bits & kClear) || ((q.bits & kValid) && q.jy0 < my_hi && q.jy1 >= my_lo);
-                }
-                uint32_t mask = __ballot_sync(0xffffffffu, want);
-                while (mask) {  // (mask is the same in all lanes)
-                    __syncwarp();  // a texel's earlier writes are seen by the lane that reads it next
-                    const Tri T = tris[wb + __ffs(mask) - 1];
-                    mask &= mask - 1u;
-                    if (T.bits & kClear) {  // a new layer: its own texels' depth back to 1
-                        for (int t = lane; t < (my_hi - my_lo) * W; t += 32) dep[(my_lo - h0) * W + t] = 1.0f;
-                        __syncwarp();
-                    }
-                    if (!(T.bits & kValid)) continue;
-                    const int lo = max(T.jy0, my_lo), hi = min(T.jy1, my_hi - 1);
-                    // the box rows of this warp, flattened over the lanes
-                    const int cols = T.ix1 - T.ix0 + 1, count = (hi - lo + 1) * cols;
-                    for (int t = lane; t < count; t += 32) {
-                        const int q = cols >= 2 ? (int)__umulhi((uint32_t)t, T.inv_cols) : t;
-                        const int r = lo + q, i = T.ix0 + (t - q * cols);
-                        const int px = i * kSubpixel + kSubpixel / 2, py = r * kSubpixel + kSubpixel / 2;
-                        const long long e0 = T.C[0] + (long long)T.A[0] * px + (long long)T.B[0] * py;
-                        const long long e1 = T.C[1] + (long long)T.A[1] * px + (long long)T.B[1] * py;
-                        const long long e2 = T.C[2] + (long long)T.A[2] * px + (long long)T.B[2] * py;
-                        if (e0 < (T.bits & 1) || e1 < ((T.bits >> 1) & 1) || e2 < ((T.bits >> 2) & 1)) continue;
-                        // plane form a0 + (a1 - a0) l1 + (a2 - a0) l2: constant attributes stay exact
-                        const float l1 = __fdiv_rn(__ll2float_rn(e1), T.area);
-                        const float l2 = __fdiv_rn(__ll2float_rn(e2), T.area);
-                        const float u = __fadd_rn(__fadd_rn(T.u0, __fmul_rn(T.du1, l1)), __fmul_rn(T.du2, l2));
-                        const float d = fabsf(u);
-                        const float depth = fminf(fmaxf(__fadd_rn(__fmul_rn(d, 0.1f), 0.3f), 0.0f), 1.0f);
-                        const int p = (r - h0) * W + i;
-                        if (!(depth < dep[p])) continue;
-                        const float alt = __fadd_rn(__fadd_rn(T.a0, __fmul_rn(T.da1, l1)), __fmul_rn(T.da2, l2));
-                        dep[p] = depth;
-                        zl[p] = __fadd_rn(alt, __fmul_rn(0.03f, __fsub_rn(1.0f, road_edge_step(d))));
-                        wv[p] = road_blend_step(d);
-                    }
+            // one warp per triangle, the texels of its box spread over the lanes
+            for (int g = seg0 + warp; g < seg1; g += kWarps) {
+                const Tri T = tt[g];
+                if (!(T.bits & kValid)) continue;
+                const int lo = max(T.jy0, h0), hi = min(T.jy1, h1 - 1);
+                if (lo > hi) continue;
+                const int cols = T.ix1 - T.ix0 + 1, count = (hi - lo + 1) * cols;
+                const unsigned long long tag = (unsigned long long)(uint32_t)(g - seg0);
+                for (int t = lane; t < count; t += 32) {
+                    const int q = cols >= 2 ? (int)__umulhi((uint32_t)t, T.inv_cols) : t;
+                    const int r = lo + q, i = T.ix0 + (t - q * cols);
+                    float l1, l2, d, depth;
+                    if (!fragment(T, i, r, l1, l2, d, depth) || !(depth < 1.0f)) continue;
+                    atomicMin(key + (r - h0) * W + i, ((unsigned long long)__float_as_uint(depth) << 32) | tag);
                 }
             }
+            __syncthreads();
+            // resolve: z and w of the winning fragment (the same operations, the same bits)
+            for (int t = threadIdx.x; t < nt; t += kThreads) {
+                const unsigned long long k = key[t];
+                if (k == ~0ull) continue;
+                const Tri &T = tt[seg0 + (int)(uint32_t)k];
+                const int r = h0 + t / W, i = t - (t / W) * W;
+                float l1, l2, d, depth;
+                fragment(T, i, r, l1, l2, d, depth);
+                const float alt = __fadd_rn(__fadd_rn(T.a0, __fmul_rn(T.da1, l1)), __fmul_rn(T.da2, l2));
+                zl[t] = __fadd_rn(alt, __fmul_rn(0.03f, __fsub_rn(1.0f, road_edge_step(d))));
+                wv[t] = road_blend_step(d);
+            }
+            __syncthreads();
         }
-        __syncthreads();
-        // blend(v) = zf min(w, 1) + z (1 - min(w, 1)), kept in the depth array
-        for (int t = threadIdx.x; t < (h1 - h0) * W; t += kThreads) {
+        // blend(v) = zf min(w, 1) + z (1 - min(w, 1))
+        for (int t = threadIdx.x; t < nt; t += kThreads) {
             const int r = h0 + t / W, cc = t - (t / W) * W;
             const float b = fminf(wv[t], 1.0f);
-            dep[t] = __fadd_rn(__fmul_rn(zf_plane[(long long)r * pitch + cc], b), __fmul_rn(zl[t], __fsub_rn(1.0f, b)));
+            bl[t] = __fadd_rn(__fmul_rn(zf_plane[(long long)r * pitch + cc], b), __fmul_rn(zl[t], __fsub_rn(1.0f, b)));
         }
         __syncthreads();
         for (int t = threadIdx.x; t < (b1 - b0) * W; t += kThreads) {
             const int r = b0 + t / W, cc = t - (t / W) * W;
             float out;
             if (blend_mode == 0) {
-                out = dep[(r - h0) * W + cc];
+                out = bl[(r - h0) * W + cc];
             } else {
                 // texture reads clamped to the edge; sums in the shader's order
                 auto at = [&](int dr, int dc) {
                     const int rr = min(max(r + dr, 0), W - 1), c2 = min(max(cc + dc, 0), W - 1);
-                    return dep[(rr - h0) * W + c2];
+                    return bl[(rr - h0) * W + c2];
                 };
                 const float sx = at(0, 0);
                 const float sy = __fadd_rn(__fadd_rn(__fadd_rn(at(0, 1), at(0, -1)), at(1, 0)), at(-1, 0));
@@ -297,12 +312,15 @@ layers_kernel(float *elev, int W, int pitch, long long plane_stride, long long s
     }
 }
 
-// Rows per band: the band's z, w and depth (with a row of halo on each side) in
-// about 140 KB of shared memory.
+// Rows per band: the band's keys, z and w (16 bytes per texel, with a row of halo on
+// each side) in about 200 KB of shared memory, bands of equal height.
 int band_rows_for(int W)
 {
-    const int rows = 140000 / (12 * W) - 2;
-    return rows >= W ? W : rows;
+    const int max_rows = 200000 / (16 * W) - 2;
+    if (max_rows < 1) return 0;
+    if (max_rows >= W) return W;
+    const int bands = (W + max_rows - 1) / max_rows;
+    return (W + bands - 1) / bands;
 }
 
 // Validates and numbers the meshes, copies what is in host memory into a device
@@ -344,6 +362,7 @@ int run_layers(tp_storage *elev, const tp_layer_job *jobs, int n, const tp_layer
         dm[m] = DevMesh{M.first_vertex, M.first_index, M.mode, ntri, 0, M.clear_depth ? 1 : 0, {0, 0}};
     }
     std::vector<DevJob> dj(n);
+    long long total_tri = 0;
     for (int k = 0; k < n; ++k) {
         const tp_layer_job &j = jobs[k];
         if (j.slot < 0 || j.slot >= elev->capacity || j.first_mesh < 0 || j.n_meshes < 0 ||
@@ -363,7 +382,8 @@ int run_layers(tp_storage *elev, const tp_layer_job *jobs, int n, const tp_layer
             if (dm[m].ntri > 0) pending_clear = 0;
             tri += dm[m].ntri;
         }
-        dj[k] = DevJob{j.slot, j.first_mesh, j.n_meshes, tri};
+        dj[k] = DevJob{j.slot, j.first_mesh, j.n_meshes, tri, total_tri};
+        total_tri += tri;
     }
 
     static std::mutex mu;
@@ -374,7 +394,8 @@ int run_layers(tp_storage *elev, const tp_layer_job *jobs, int n, const tp_layer
     const size_t bj = al(sizeof(DevJob) * n), bm = al(sizeof(DevMesh) * (n_meshes ? n_meshes : 1));
     const size_t bv = vert_dev ? 0 : al(sizeof(float) * 4 * (size_t)(n_vertices ? n_vertices : 1));
     const size_t bi = idx_dev ? 0 : al(sizeof(uint32_t) * (size_t)(n_indices ? n_indices : 1));
-    const size_t need = bj + bm + bv + bi;
+    const size_t bt = al(sizeof(Tri) * (size_t)(total_tri ? total_tri : 1));  // triangle records
+    const size_t need = bj + bm + bv + bi + bt;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     if (dcap < need) {
         if (dbuf) {
@@ -400,13 +421,13 @@ int run_layers(tp_storage *elev, const tp_layer_job *jobs, int n, const tp_layer
                             s);
     if (e != cudaSuccess) return tp::cuda_fail("cudaMemcpyAsync (layer meshes)", e);
     const int rows = band_rows_for(W);
-    const size_t smem = sizeof(Tri) * kChunk + sizeof(float) * (3 * (size_t)(rows + 2) * W + 2 * (size_t)W);
+    const size_t smem = 16 * (size_t)(rows + 2) * W + sizeof(float) * 2 * (size_t)W;
     e = cudaFuncSetAttribute(layers_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return tp::cuda_fail("cudaFuncSetAttribute (layers)", e);
     layers_kernel<<<n, kThreads, smem, s>>>(elev->base, W, elev->pitch, elev->plane_stride, elev->slot_stride,
                                             reinterpret_cast<const DevJob *>(dbuf),
                                             reinterpret_cast<const DevMesh *>(dbuf + bj), dv, di, n_vertices,
-                                            blend_mode, rows);
+                                            blend_mode, rows, reinterpret_cast<Tri *>(dbuf + bj + bm + bv + bi));
     e = cudaGetLastError();
     if (e != cudaSuccess) return tp::cuda_fail("layers kernel launch", e);
     e = cudaStreamSynchronize(s);
