@@ -31,6 +31,7 @@
 // gives the same bits.
 #include <cuda_runtime.h>
 
+#include <cstddef>
 #include <cstring>
 #include <mutex>
 #include <vector>
@@ -182,6 +183,38 @@ __device__ __forceinline__ float road_blend_step(float d)
     return __fmul_rn(__fmul_rn(t, t), __fsub_rn(3.0f, __fmul_rn(2.0f, t)));
 }
 
+constexpr int kTriWords = (int)(sizeof(Tri) / 4);
+
+// The triangle record whose 32-bit word k lane k holds (lanes 0 .. kTriWords - 1),
+// as every lane's copy: the fields the rasteriser reads, by shuffles.
+__device__ __forceinline__ Tri tri_from_lanes(uint32_t w)
+{
+    auto word = [&](int k) { return __shfl_sync(0xffffffffu, w, k); };
+    auto wide = [&](int k) { return (long long)(((unsigned long long)word(k + 1) << 32) | word(k)); };
+    Tri t;
+    const int c0 = (int)(offsetof(Tri, C) / 4), a0 = (int)(offsetof(Tri, A) / 4), b0 = (int)(offsetof(Tri, B) / 4);
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+        t.C[q] = wide(c0 + 2 * q);
+        t.A[q] = (int)word(a0 + q);
+        t.B[q] = (int)word(b0 + q);
+    }
+    t.a0 = __uint_as_float(word(offsetof(Tri, a0) / 4));
+    t.da1 = __uint_as_float(word(offsetof(Tri, da1) / 4));
+    t.da2 = __uint_as_float(word(offsetof(Tri, da2) / 4));
+    t.u0 = __uint_as_float(word(offsetof(Tri, u0) / 4));
+    t.du1 = __uint_as_float(word(offsetof(Tri, du1) / 4));
+    t.du2 = __uint_as_float(word(offsetof(Tri, du2) / 4));
+    t.area = __uint_as_float(word(offsetof(Tri, area) / 4));
+    t.ix0 = (int)word(offsetof(Tri, ix0) / 4);
+    t.ix1 = (int)word(offsetof(Tri, ix1) / 4);
+    t.jy0 = (int)word(offsetof(Tri, jy0) / 4);
+    t.jy1 = (int)word(offsetof(Tri, jy1) / 4);
+    t.bits = (int)word(offsetof(Tri, bits) / 4);
+    t.inv_cols = word(offsetof(Tri, inv_cols) / 4);
+    return t;
+}
+
 // The fragment of triangle T at the centre of texel (i, r), if T covers it: the
 // barycentric weights l1, l2 (plane form), the road-width distance d and the depth.
 __device__ __forceinline__ bool fragment(const Tri &T, int i, int r, float &l1, float &l2, float &d, float &depth)
@@ -251,9 +284,17 @@ layers_kernel(float *elev, int W, int pitch, long long plane_stride, long long s
             if (seg0 == seg1) continue;
             for (int t = threadIdx.x; t < nt; t += kThreads) key[t] = ~0ull;
             __syncthreads();
-            // one warp per triangle, the texels of its box spread over the lanes
-            for (int g = seg0 + warp; g < seg1; g += kWarps) {
-                const Tri T = tt[g];
+            // one warp per triangle, the texels of its box spread over the lanes; a
+            // triangle's record is read one word per lane, the next one a step ahead,
+            // and its fields broadcast by shuffles
+            const uint32_t *tw = reinterpret_cast<const uint32_t *>(tt);
+            int g = seg0 + warp;
+            uint32_t cur = (g < seg1 && lane < kTriWords) ? tw[(size_t)g * kTriWords + lane] : 0u;
+            for (; g < seg1; g += kWarps) {
+                const uint32_t nxt =
+                    (g + kWarps < seg1 && lane < kTriWords) ? tw[(size_t)(g + kWarps) * kTriWords + lane] : 0u;
+                const Tri T = tri_from_lanes(cur);
+                cur = nxt;
                 if (!(T.bits & kValid)) continue;
                 const int lo = max(T.jy0, h0), hi = min(T.jy1, h1 - 1);
                 if (lo > hi) continue;
