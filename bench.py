@@ -142,15 +142,27 @@ class ClockSampler:
             self.path = os.path.join(ROOT, "gpurun_out", "bench_clocks_%d.csv" % os.getpid())
             self.f = open(self.path, "w")
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.dev), "--query-gpu=" + self.QUERY,
-                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                          "--format=csv,noheader,nounits", "-lms", "50"],
                                          stdout=self.f, stderr=subprocess.DEVNULL)
         except Exception:
             self.proc = None
+            return
+        # the timed region starts once the sampler is running; its samples so far are
+        # left out of the record
+        t0 = time.time()
+        self.skip = 0
+        while time.time() - t0 < 5.0 and self.proc.poll() is None:
+            self.f.flush()
+            with open(self.path) as r:
+                n = sum(1 for _ in r)
+            if n > 0:
+                self.skip = n
+                break
+            time.sleep(0.02)
 
     def stop(self):
         if not self.proc:
             return None
-        time.sleep(0.25)
         self.proc.terminate()
         try:
             self.proc.wait(timeout=5)
@@ -159,7 +171,7 @@ class ClockSampler:
         self.f.close()
         sm, mx, reasons = [], None, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for line in open(self.path):
+        for line in list(open(self.path))[self.skip:]:
             parts = [p.strip() for p in line.split(",")]
             if len(parts) < 9:
                 continue
@@ -685,7 +697,7 @@ def planet_section(tp, torch, stream, sh, args, trained):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--steps", type=int, default=2000)
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--requests", type=int, default=4096)
