@@ -138,8 +138,8 @@ class ClockSampler:
 
     def start(self):
         try:
-            os.makedirs(os.path.join(ROOT, "gpurun_out"), exist_ok=True)
-            self.path = os.path.join(ROOT, "gpurun_out", "bench_clocks_%d.csv" % os.getpid())
+            import tempfile
+            self.path = os.path.join(tempfile.gettempdir(), "bench_clocks_%d.csv" % os.getpid())
             self.f = open(self.path, "w")
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.dev), "--query-gpu=" + self.QUERY,
                                           "--format=csv,noheader,nounits", "-lms", "50"],
