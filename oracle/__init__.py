@@ -3,7 +3,7 @@
 ctypes bindings over oracle/_build/liboracle.so (the C restatement in
 oracle.c) plus a pure-Python reader of the reference's ``.dat`` residual
 pyramids.  Only tests/, ``__graft_entry__.smoke()`` and bench.py's CPU-baseline
-leg use this package, always as the checker; the product does not import it.
+leg use this package, always as the reference results; the product does not import it.
 """
 import ctypes as C
 import os

@@ -2,7 +2,7 @@
  * CPU oracle for the terrain tile-production path -- TEST INFRASTRUCTURE ONLY.
  *
  * This is a plain-C restatement of the arithmetic of Proland 4.0's elevation,
- * residual and normal producers.  It is the checker the CUDA product is compared
+ * residual and normal producers.  It is what the CUDA product is compared
  * against; the product never links, loads or calls it.  Only the test-suite,
  * the smoke check and the CPU-baseline leg of the benchmark use it.
  *
