@@ -364,7 +364,10 @@ def fp64_errors(tp, classes):
     """Max error of a few produced tiles against the FP64 evaluation of the same
     definition (and of the normals computed from FP64 elevations)."""
     import oracle
-    out = {"zf_abs": 0.0, "zf_rel": 0.0, "normal_abs": 0.0, "tiles": 0}
+    out = {"zf_abs": 0.0, "zf_rel": 0.0, "normal_abs": 0.0, "tiles": 0,
+           # reporting only: how far the GL path's LINEAR fetches at +0.25-texel offsets
+           # would move the normals from the texel-exact finite differences computed here
+           "normal_abs_vs_gl_linear_sampling": 0.0}
     for fc in classes:
         table = oracle.dem_noise(fc.W)
         for k in range(min(4, fc.n)):
@@ -379,6 +382,10 @@ def fp64_errors(tp, classes):
             out["zf_abs"] = max(out["zf_abs"], float(e.max()))
             out["zf_rel"] = max(out["zf_rel"], float((e / np.maximum(np.abs(d_zf), 1.0)).max()))
             out["normal_abs"] = max(out["normal_abs"], float(np.abs(nx - dnx).max()))
+            zm = fc.elev.download(k, 1, tp.ZM)[0]
+            lnx, _ = oracle.normals_flat_gl_linear(fc.W, zm, j.tile_meters)
+            out["normal_abs_vs_gl_linear_sampling"] = max(out["normal_abs_vs_gl_linear_sampling"],
+                                                          float(np.abs(nx - lnx).max()))
             out["tiles"] += 1
     return out
 

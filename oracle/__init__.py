@@ -93,6 +93,7 @@ def lib():
         L.or_cpu_elevation_tile.argtypes = [C.c_int] * 4 + [_f32p, C.c_int, _f32p, C.c_int,
                                                             C.c_int, C.c_int, _f32p, C.c_int]
         L.or_normals_flat.argtypes = [C.c_int, _f32p, C.c_int, C.c_float, C.c_int, _f32p, _f32p, C.c_int]
+        L.or_normals_flat_gl_linear.argtypes = [C.c_int, _f32p, C.c_int, C.c_float, _f32p, _f32p, C.c_int]
         L.or_normals_flat_f64.argtypes = [C.c_int, _f64p, C.c_int, C.c_double, _f64p, _f64p, C.c_int]
         L.or_sphere_frame_make.argtypes = [C.c_double, C.c_int, C.c_int, C.c_int, C.POINTER(SphereFrame)]
         L.or_normals_sphere.argtypes = [C.c_int, _f32p, C.c_int, C.POINTER(SphereFrame), _f32p, _f32p, C.c_int]
@@ -317,6 +318,17 @@ def normals_flat(W, zm, tile_meters, fmt=2):
     nx = np.empty((n1, n1), np.float32)
     ny = np.empty((n1, n1), np.float32)
     lib().or_normals_flat(W, _p(zm), zm.shape[1], float(tile_meters), fmt, _p(nx), _p(ny), n1)
+    return nx, ny
+
+
+def normals_flat_gl_linear(W, zm, tile_meters):
+    """Normals as the GL path samples zm (LINEAR storage, +0.25-texel offsets): for
+    reporting the difference to the texel-exact finite differences only."""
+    zm = _f32(zm)
+    n1 = W - 4
+    nx = np.empty((n1, n1), np.float32)
+    ny = np.empty((n1, n1), np.float32)
+    lib().or_normals_flat_gl_linear(W, _p(zm), zm.shape[1], float(tile_meters), _p(nx), _p(ny), n1)
     return nx, ny
 
 

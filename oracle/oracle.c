@@ -487,6 +487,34 @@ void or_normals_flat(int W, const float *zm, int zm_pitch, float tile_meters,
         }
 }
 
+/* The same normals as the reference's GL path samples zm: terrain1/normalShader.glsl
+ * fetches texel X at (X + 0.25) / width (NormalProducer.cpp:210-213) from a LINEAR
+ * storage (terrain1/helloworld.xml:30-32), so each fetch is the bilinear blend of
+ * texels X - 1 and X with weights 0.25 / 0.75 in each direction.  For reporting how
+ * far that sampling is from the texel-exact finite differences the product
+ * computes; nothing is compared against it. */
+static float gl_linear_fetch(const float *zm, int pitch, int X, int Y)
+{
+    const float *r0 = zm + (size_t)(Y - 1) * pitch, *r1 = zm + (size_t)Y * pitch;
+    return 0.0625f * r0[X - 1] + 0.1875f * r0[X] + 0.1875f * r1[X - 1] + 0.5625f * r1[X];
+}
+
+void or_normals_flat_gl_linear(int W, const float *zm, int zm_pitch, float tile_meters, float *nx, float *ny,
+                               int out_pitch)
+{
+    int n = W - 5;
+    float h2 = 2.0f * (tile_meters / (float)n);
+    for (int q = 0; q <= n; ++q)
+        for (int p = 0; p <= n; ++p) {
+            const int X = p + 2, Y = q + 2;
+            float ax = -(gl_linear_fetch(zm, zm_pitch, X + 1, Y) - gl_linear_fetch(zm, zm_pitch, X - 1, Y));
+            float ay = -(gl_linear_fetch(zm, zm_pitch, X, Y + 1) - gl_linear_fetch(zm, zm_pitch, X, Y - 1));
+            float inv = 1.0f / sqrtf(ax * ax + ay * ay + h2 * h2);
+            nx[p + (size_t)q * out_pitch] = ax * inv;
+            ny[p + (size_t)q * out_pitch] = ay * inv;
+        }
+}
+
 void or_normals_flat_f64(int W, const double *zm, int zm_pitch, double tile_meters,
                          double *nx, double *ny, int out_pitch)
 {

@@ -75,6 +75,10 @@ void or_cpu_elevation_tile(int W, int level, int tx, int ty,
  * format 2: two signed fp32 planes; format 3: RG8 unsigned (values written as floats 0..255). */
 void or_normals_flat(int W, const float *zm, int zm_pitch, float tile_meters,
                      int format, float *nx, float *ny, int out_pitch);
+/* Reporting only: the normals with the GL path's LINEAR fetches at +0.25-texel
+ * offsets (NormalProducer.cpp:210-213; see oracle.c). */
+void or_normals_flat_gl_linear(int W, const float *zm, int zm_pitch, float tile_meters, float *nx, float *ny,
+                               int out_pitch);
 void or_normals_flat_f64(int W, const double *zm, int zm_pitch, double tile_meters,
                          double *nx, double *ny, int out_pitch);
 

@@ -118,3 +118,20 @@ def test_fp64_twin(oracle_lib):
     b = oracle_lib.elevation_tile(W, 5, 3, 4, parent, None, res, noise=t[2], noise_rot=3, noise_amp=-15.0, f64=True)
     for x, y in zip(a, b):
         assert np.abs(x - y).max() < 1e-3
+
+
+def test_gl_linear_sampling_emulation(oracle_lib):
+    """The reporting-only emulation of the GL path's LINEAR fetches at +0.25-texel
+    offsets: on a plane it gives the texel-exact normals (finite differences of a
+    plane do not depend on the sampling offset); on a rough surface it moves them."""
+    import numpy as np
+    W, meters = 101, 1000.0
+    y, x = np.mgrid[0:W, 0:W].astype(np.float64)
+    plane = (3.0 * x - 2.0 * y + 40.0).astype(np.float32)
+    pnx, pny = oracle_lib.normals_flat(W, plane, meters)
+    lnx, lny = oracle_lib.normals_flat_gl_linear(W, plane, meters)
+    assert np.abs(pnx - lnx).max() < 1e-6 and np.abs(pny - lny).max() < 1e-6
+    rough = np.random.default_rng(2).standard_normal((W, W)).astype(np.float32) * 20.0
+    pnx, _ = oracle_lib.normals_flat(W, rough, meters)
+    lnx, _ = oracle_lib.normals_flat_gl_linear(W, rough, meters)
+    assert np.abs(pnx - lnx).max() > 1e-3
