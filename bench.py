@@ -405,9 +405,12 @@ def learned_flops(W):
 # bf16 activations of (W + 2)^2 pixels read (zero border included) and W^2 written, the
 # last layer's fp32 channel, and the residual scaled out (fp32 read and write)
 def learned_bytes(W):
+    """HBM bytes per W x W tile of an inference pass: the tile means, the first layer
+    (its input channels made from the fp32 upsampled tile), three hidden layers, the
+    last layer and the output scaling."""
     px, pxb = W * W, (W + 2) * (W + 2)
-    b = px * 4 + px * 16 * 2                  # prep
-    b += pxb * 16 * 2 + px * 32 * 2           # layer 0 (16 -> 32)
+    b = px * 4                                # tile means
+    b += px * 4 + px * 32 * 2                 # layer 0 (upsampled tile in, 32 channels out)
     b += 3 * (pxb * 32 * 2 + px * 32 * 2)     # layers 1-3 (32 -> 32)
     b += pxb * 32 * 2 + px * 4                # layer 4 (32 -> 1 used)
     b += 2 * px * 4                           # scale

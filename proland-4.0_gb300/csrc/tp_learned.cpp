@@ -24,7 +24,7 @@ struct tp_learned {
     uint8_t *fwd[kLayers] = {}, *bwd[kLayers] = {};
     float *sigma_in = nullptr, *sigma_out = nullptr;
     __nv_bfloat16 *x0 = nullptr, *act[4] = {}, *z[4] = {}, *dz4 = nullptr, *dza = nullptr, *dzb = nullptr;
-    float *pred = nullptr, *loss = nullptr, *up = nullptr;
+    float *pred = nullptr, *loss = nullptr, *up = nullptr, *mean = nullptr;
     int *levels = nullptr, *status = nullptr, *aux = nullptr;
     CUtensorMap h_x0, h_act[4], h_dz4, h_dza, h_dzb;  // 10 x 18 halo boxes (convolutions)
     CUtensorMap b_x0, b_act[4], b_dz4, b_dza, b_dzb;  // 8 x 16 block boxes (weight gradients)
@@ -111,7 +111,10 @@ int forward(tp_learned *net, int n, bool training, cudaStream_t s)
         int rc = pack(net, s);
         if (rc) return rc;
     }
-    launch_prep(net->up, net->levels, net->sigma_in, net->W, n, net->x0, s);
+    // training keeps the first layer's input image (its weight gradient reads it);
+    // inference makes the input channels inside the first convolution
+    if (training) launch_prep(net->up, net->levels, net->sigma_in, net->W, n, net->x0, s);
+    else launch_means(net->up, net->W, n, net->mean, s);
     const CUtensorMap *in[kLayers] = {&net->h_x0, &net->h_act[0], &net->h_act[1], &net->h_act[2], &net->h_act[3]};
     for (int l = 0; l < kLayers; ++l) {
         ConvLaunch a = conv_args(net, n);
@@ -124,7 +127,14 @@ int forward(tp_learned *net, int n, bool training, cudaStream_t s)
         } else {
             a.out_f32 = net->pred;
         }
-        int rc = launch_conv(kCin[l], kCout[l], l < kLayers - 1 ? kHidden : kLast, a, in[l], s);
+        int mode = l < kLayers - 1 ? kHidden : kLast;
+        if (l == 0 && !training) {
+            mode = kFirst;
+            a.up = net->up;
+            a.mean = net->mean;
+            a.sigma_in = net->sigma_in;
+        }
+        int rc = launch_conv(kCin[l], kCout[l], mode, a, in[l], s);
         if (rc) return rc;
     }
     net->nimg = n;
@@ -195,6 +205,7 @@ extern "C" int tp_learned_create(int tile_width, int max_batch, tp_learned **out
     A(&net->dzb, px * 32);
     A(&net->pred, tile);
     A(&net->up, tile);
+    A(&net->mean, max_batch);
     A(&net->loss, 1);
     A(&net->levels, max_batch);
     A(&net->status, 1);

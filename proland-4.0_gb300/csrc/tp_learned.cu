@@ -203,7 +203,57 @@ __global__ void __launch_bounds__(kRoleThreads) conv_kernel(const __grid_constan
     const int per_img = a.tiles_x * a.tiles_y, total = a.nimg * per_img;
     const int mine = my_tiles(total);
 
-    if (warp == 0) {
+    if (MODE == kFirst && warp == 0) {
+        // producer: the input channels of tile i's halo made from the upsampled parent
+        // (the values launch_prep writes: (up - mean) / sigma_in, x and y parity, 1; 0
+        // outside the image), written as bf16 into stage i % kConvStages; channels 8-15
+        // are zero in every stage
+        for (int s = 0; s < kConvStages; ++s)
+            for (int p = lane; p < kHaloX * kHaloY; p += 32)
+                *reinterpret_cast<uint4 *>(halo + s * STAGE + kGroupStride + p * 16) = make_uint4(0u, 0u, 0u, 0u);
+        int i = 0;
+        for (; i < mine; ++i) {
+            const int s = i % kConvStages;
+            if (i >= kConvStages &&
+                !__all_sync(0xffffffffu, mbar_wait_abortable(&empty[s], ((i / kConvStages) - 1) & 1, abort)))
+                break;
+            const int t = blockIdx.x + i * gridDim.x;
+            const int img = t / per_img, rem = t - img * per_img;
+            const int by = rem / a.tiles_x, bx = rem - by * a.tiles_x;
+            const float *u = a.up + (size_t)img * a.W * a.W;
+            // all loads of the tile first (one latency), then the conversions
+            constexpr int kPer = (kHaloX * kHaloY + 31) / 32;
+            float val[kPer];
+            int xs[kPer], ys[kPer];
+            const float mean = __ldg(a.mean + img);
+            const int lv = __ldg(a.level + img);
+#pragma unroll
+            for (int k = 0; k < kPer; ++k) {
+                const int p = lane + 32 * k;
+                const int hy = p / kHaloX, hx = p - hy * kHaloX;
+                xs[k] = bx * kBlockX + hx - 1;
+                ys[k] = by * kBlockY + hy - 1;
+                const bool in = p < kHaloX * kHaloY && xs[k] >= 0 && ys[k] >= 0 && xs[k] < a.W && ys[k] < a.W;
+                val[k] = in ? __ldg(u + (size_t)ys[k] * a.W + xs[k]) : 0.0f;
+                if (!in) xs[k] = -1;
+            }
+            const float inv = 1.0f / __ldg(a.sigma_in + min(max(lv, 0), kLevels - 1));
+#pragma unroll
+            for (int k = 0; k < kPer; ++k) {
+                const int p = lane + 32 * k;
+                if (p >= kHaloX * kHaloY) break;
+                uint4 v = make_uint4(0u, 0u, 0u, 0u);
+                if (xs[k] >= 0) {
+                    v.x = pack2((val[k] - mean) * inv, (float)(xs[k] & 1));
+                    v.y = pack2((float)(ys[k] & 1), 1.0f);
+                }
+                *reinterpret_cast<uint4 *>(halo + s * STAGE + p * 16) = v;
+            }
+            fence_proxy_async_smem();  // the generic-proxy writes, before the tensor cores read them
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&full[s]);
+        }
+    } else if (warp == 0) {
         if (lane == 0) {  // producer: halo of tile i into stage i % kConvStages
             int i = 0;
             for (; i < mine; ++i) {
@@ -269,7 +319,7 @@ __global__ void __launch_bounds__(kRoleThreads) conv_kernel(const __grid_constan
             const int px = bx * kBlockX + (m & 7), py = by * kBlockY + (m >> 3);
             if (px < a.W && py < a.W) {
                 const size_t plane = (size_t)Wp * Wp, pix = (size_t)(py + 1) * Wp + (px + 1);
-                if (MODE == kHidden) {
+                if (MODE == kHidden || MODE == kFirst) {
                     const float2 *b2 = reinterpret_cast<const float2 *>(bias_s);
                     if (a.emb) {
                         const float2 *e2 = reinterpret_cast<const float2 *>(
@@ -551,10 +601,10 @@ __global__ void pack_kernel(const float *w, int cin, int cout, uint8_t *fwd, uin
     }
 }
 
-__global__ void prep_kernel(const float *up, const int *level, const float *sigma_in, int W, __nv_bfloat16 *x0)
+// Mean of one tile by a block of 256 threads: strided per-thread sums in double, then
+// a tree over the threads (the same order wherever it is used).
+__device__ float tile_mean(const float *u, int n)
 {
-    const int img = blockIdx.x, n = W * W;
-    const float *u = up + (size_t)img * n;
     __shared__ double part[256];
     double s = 0.0;
     for (int i = threadIdx.x; i < n; i += blockDim.x) s += u[i];
@@ -564,7 +614,21 @@ __global__ void prep_kernel(const float *up, const int *level, const float *sigm
         if (threadIdx.x < k) part[threadIdx.x] += part[threadIdx.x + k];
         __syncthreads();
     }
-    const float mean = (float)(part[0] / n);
+    return (float)(part[0] / n);
+}
+
+__global__ void mean_kernel(const float *up, int W, float *mean)
+{
+    const int n = W * W;
+    const float m = tile_mean(up + (size_t)blockIdx.x * n, n);
+    if (threadIdx.x == 0) mean[blockIdx.x] = m;
+}
+
+__global__ void prep_kernel(const float *up, const int *level, const float *sigma_in, int W, __nv_bfloat16 *x0)
+{
+    const int img = blockIdx.x, n = W * W;
+    const float *u = up + (size_t)img * n;
+    const float mean = tile_mean(u, n);
     const float inv = 1.0f / sigma_in[min(max(level[img], 0), kLevels - 1)];
     const int Wp = W + 2;
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
@@ -666,6 +730,7 @@ inline unsigned blocks_for(size_t n, int t) { return (unsigned)((n + t - 1) / t)
 int launch_conv(int cin, int cout, int mode, const ConvLaunch &a, const CUtensorMap *halo, cudaStream_t s)
 {
     if (cin == 16 && cout == 32 && mode == kHidden) return conv_instance<16, 32, kHidden>(a, halo, s);
+    if (cin == 16 && cout == 32 && mode == kFirst) return conv_instance<16, 32, kFirst>(a, halo, s);
     if (cin == 32 && cout == 32 && mode == kHidden) return conv_instance<32, 32, kHidden>(a, halo, s);
     if (cin == 32 && cout == 16 && mode == kLast) return conv_instance<32, 16, kLast>(a, halo, s);
     if (cin == 16 && cout == 32 && mode == kBackData) return conv_instance<16, 32, kBackData>(a, halo, s);
@@ -691,6 +756,11 @@ void launch_prep(const float *up, const int *level, const float *sigma_in, int W
                  cudaStream_t s)
 {
     if (nimg > 0) prep_kernel<<<nimg, 256, 0, s>>>(up, level, sigma_in, W, x0);
+}
+
+void launch_means(const float *up, int W, int nimg, float *mean, cudaStream_t s)
+{
+    if (nimg > 0) mean_kernel<<<nimg, 256, 0, s>>>(up, W, mean);
 }
 
 void launch_loss(const float *pred, const float *target, const int *level, const float *sigma_out, int W, int nimg,

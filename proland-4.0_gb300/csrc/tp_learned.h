@@ -34,6 +34,11 @@ struct ConvLaunch {
     const __nv_bfloat16 *zprev;  // mode 2: the previous layer's saved pre-activation
     float *out_f32;              // mode 1: [nimg][W][W] output channel 0
     int *status;
+    // mode 3 (first layer of an inference pass): the input channels made from the
+    // upsampled parent tiles instead of read from an activation image
+    const float *up;             // [nimg][W][W]
+    const float *mean;           // [nimg] tile means
+    const float *sigma_in;       // [kLevels]
 };
 
 // Weight gradient of one layer over a batch: dW[co][tap][ci] += sum_p dZ[p][co] X[p + tap][ci].
@@ -46,7 +51,7 @@ struct WgradLaunch {
     int *status;
 };
 
-enum ConvMode { kHidden = 0, kLast = 1, kBackData = 2 };
+enum ConvMode { kHidden = 0, kLast = 1, kBackData = 2, kFirst = 3 };
 
 int launch_conv(int cin, int cout, int mode, const ConvLaunch &a, const CUtensorMap *halo, cudaStream_t s);
 int launch_wgrad(int cin, int cout, const WgradLaunch &a, const CUtensorMap *xbox, const CUtensorMap *zbox,
@@ -57,6 +62,8 @@ int encode_act_map(void *base, int W, int channels, int nimg, int box_x, int box
 void launch_pack(const float *w, int cin, int cout, uint8_t *fwd, uint8_t *bwd, cudaStream_t s);
 void launch_prep(const float *up, const int *level, const float *sigma_in, int W, int nimg, __nv_bfloat16 *x0,
                  cudaStream_t s);
+// Per-tile means of the upsampled parents (the same sums as launch_prep's).
+void launch_means(const float *up, int W, int nimg, float *mean, cudaStream_t s);
 void launch_loss(const float *pred, const float *target, const int *level, const float *sigma_out, int W, int nimg,
                  __nv_bfloat16 *dz, float *loss, cudaStream_t s);
 void launch_adam(float *p, const float *g, float *m, float *v, const float *mask, int n, float lr, float b1, float b2,

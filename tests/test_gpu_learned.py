@@ -107,6 +107,22 @@ def test_forward_backward_match_oracle(L, oracle_lib, W, n):
     net.close()
 
 
+@pytest.mark.parametrize("W,n", [(21, 3), (37, 2), (101, 4)])
+def test_inference_input_channels_made_in_the_first_layer(L, W, n):
+    """An inference pass builds the first layer's input channels inside the first
+    convolution (no input image): the same bits as the training pass, which writes the
+    input image and reads it back."""
+    levels, up, _, si, so = _case(W, n, seed=W + 1)
+    net = L.LearnedPredictor(tile_width=W, max_batch=4, seed=7)
+    net.set_sigmas(si, so)
+    up_d = torch.from_numpy(up).cuda()
+    train_out = net.forward(up_d, levels, training=True).clone()
+    infer_out = net.forward(up_d, levels, training=False)
+    torch.cuda.synchronize()
+    assert torch.equal(train_out, infer_out)
+    net.close()
+
+
 def test_adam_lowers_the_loss_of_a_fixed_batch(L):
     W, n = 37, 4
     levels, up, target, si, so = _case(W, n, seed=3)
