@@ -39,7 +39,7 @@ UNIT = "tiles/s"
 ROOT_QUAD = 100000.0          # meters: terrainNode size 50000 -> root quad 2 * size
 BYTES_PER_TILE = {101: 260960, 197: 1000544}   # algorithmic bytes (parent window, residual, elevation, normals)
 FALLBACK_HBM_GBS = 6800.0
-E2E_CHUNK = {101: 256, 197: 64}   # tiles per chunk of the host-buffer pipeline
+E2E_CHUNK = {101: 512, 197: 128}   # tiles per chunk of the host-buffer pipeline (swept: 64-512 / 16-128)
 # ncu dram__bytes_read + dram__bytes_write of the two launches of one step (101-wide and
 # 197-wide classes) of the default 4096-request frame, from a one-pass launch list
 TRAFFIC_BYTES_PER_STEP = (208.2 + 573.8 + 240.1 + 741.6) * 1e6
