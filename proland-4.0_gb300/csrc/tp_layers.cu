@@ -73,6 +73,11 @@ constexpr int kValid = 8, kClear = 16;
 
 __device__ __forceinline__ int floor_div(int a, int b) { return a >= 0 ? a / b : -((-a + b - 1) / b); }
 
+// t / d by a multiply-high: m = ceil(2^32 / d) gives floor(t / d) == umulhi(t, m) for
+// 2 <= d <= 4096 and every t below 2^20 (m d = 2^32 + e with 0 < e <= d, and t e < 2^32).
+__device__ __forceinline__ uint32_t div_magic(int d) { return 0xFFFFFFFFu / (uint32_t)d + 1u; }
+__device__ __forceinline__ int div_by(int t, uint32_t m) { return (int)__umulhi((uint32_t)t, m); }
+
 __device__ __forceinline__ bool snap(float c, int W, int *out)
 {
     const float w = __fmul_rn(__fmul_rn(__fadd_rn(c, 1.0f), 0.5f * (float)W), (float)kSubpixel);
@@ -256,6 +261,7 @@ layers_kernel(float *elev, int W, int pitch, long long plane_stride, long long s
     float *zf_plane = elev + (long long)J.slot * slot_stride;
     float *zm_plane = zf_plane + 2 * plane_stride;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t wmag = div_magic(W);  // texel t of a band: row t / W
     Tri *tt = scratch + J.tri_offset;
     for (int g = threadIdx.x; g < J.ntri; g += kThreads) setup(tt[g], J, meshes, verts, idx, nv, g, W);
     __syncthreads();
@@ -269,7 +275,7 @@ layers_kernel(float *elev, int W, int pitch, long long plane_stride, long long s
         const float *save_prev = saved + ((band + 1) & 1) * W;
         // the framebuffer before the layers: z = zm, w = 0
         for (int t = threadIdx.x; t < nt; t += kThreads) {
-            const int r = h0 + t / W, cc = t - (t / W) * W;
+            const int tr = div_by(t, wmag), r = h0 + tr, cc = t - tr * W;
             const float z = (b0 > 0 && r == h0) ? save_prev[cc] : zm_plane[(long long)r * pitch + cc];
             if (r == b1 - 1) save_now[cc] = z;
             zl[t] = z;
@@ -314,7 +320,7 @@ layers_kernel(float *elev, int W, int pitch, long long plane_stride, long long s
                 const unsigned long long k = key[t];
                 if (k == ~0ull) continue;
                 const Tri &T = tt[seg0 + (int)(uint32_t)k];
-                const int r = h0 + t / W, i = t - (t / W) * W;
+                const int tr = div_by(t, wmag), r = h0 + tr, i = t - tr * W;
                 float l1, l2, d, depth;
                 fragment(T, i, r, l1, l2, d, depth);
                 const float alt = __fadd_rn(__fadd_rn(T.a0, __fmul_rn(T.da1, l1)), __fmul_rn(T.da2, l2));
@@ -325,13 +331,13 @@ layers_kernel(float *elev, int W, int pitch, long long plane_stride, long long s
         }
         // blend(v) = zf min(w, 1) + z (1 - min(w, 1))
         for (int t = threadIdx.x; t < nt; t += kThreads) {
-            const int r = h0 + t / W, cc = t - (t / W) * W;
+            const int tr = div_by(t, wmag), r = h0 + tr, cc = t - tr * W;
             const float b = fminf(wv[t], 1.0f);
             bl[t] = __fadd_rn(__fmul_rn(zf_plane[(long long)r * pitch + cc], b), __fmul_rn(zl[t], __fsub_rn(1.0f, b)));
         }
         __syncthreads();
         for (int t = threadIdx.x; t < (b1 - b0) * W; t += kThreads) {
-            const int r = b0 + t / W, cc = t - (t / W) * W;
+            const int tr = div_by(t, wmag), r = b0 + tr, cc = t - tr * W;
             float out;
             if (blend_mode == 0) {
                 out = bl[(r - h0) * W + cc];

@@ -82,6 +82,12 @@ __device__ __forceinline__ void sphere_pos(const tp::SphereFrame &f, float s, fl
     for (int r = 0; r < 3; ++r) out[r] = a_(cp[r], m_(hp, up[r]));
 }
 
+// m = ceil(2^32 / d) for 2 <= d <= 4096, so that floor(t / d) == umulhi(t, m): with
+// m d = 2^32 + e, 0 < e <= d, t m / 2^32 = t / d + t e / (d 2^32), and the last term is
+// below 1 / d when t e < 2^32, i.e. for every t below 2^20 (checked exhaustively for
+// t < 80000); a band's flattened indices stay below 18 x 4094.
+__device__ __forceinline__ uint32_t div_magic(int d) { return 0xFFFFFFFFu / (uint32_t)d + 1u; }
+
 // Rows of world positions per band of normal rows (kSphereBand rows), kept in a
 // shared-memory ring of kSphereBand + 2 rows: each grid position is evaluated once
 // and read by the four normals around it.
@@ -100,12 +106,13 @@ __device__ __forceinline__ void sphere_rows(const tp::SphereFrame &F, float s, c
     const int PW = W - 2;
     float *X = ring, *Y = ring + kSphereRing * PW, *Z = ring + 2 * kSphereRing * PW;
     const int cnt = (v1 - v0) * PW;
+    const uint32_t inv = div_magic(PW);
     for (int i = threadIdx.x; i < cnt; i += blockDim.x) {
-        const int r = i / PW;
-        const int u = i - r * PW - 1, v = v0 + r;
+        const int r = (int)__umulhi((uint32_t)i, inv);  // i / PW
+        const int c = i - r * PW, v = v0 + r;            // c = u + 1
         float o[3];
-        sphere_pos(F, s, qn[u + 1], qn[v + 1], __ldg(zm + (long long)(v + 2) * pitch + (u + 2)), o);
-        const int k = ((v + 1) % kSphereRing) * PW + (u + 1);
+        sphere_pos(F, s, qn[c], qn[v + 1], __ldg(zm + (long long)(v + 2) * pitch + (c + 1)), o);
+        const int k = ((v + 1) % kSphereRing) * PW + c;
         X[k] = o[0];
         Y[k] = o[1];
         Z[k] = o[2];
@@ -151,8 +158,10 @@ __device__ __forceinline__ void sphere_tile(const tp::SphereFrame &F, const floa
         if (q0 > 0) sphere_rows(F, s, qn, zm, pitch, W, q0 + 1, q1 + 1, ring);
         __syncthreads();
         const int cnt = (q1 - q0) * Wn;
+        const uint32_t inv = div_magic(Wn);
         for (int i = threadIdx.x; i < cnt; i += blockDim.x) {
-            const int q = q0 + i / Wn, p = i % Wn;
+            const int r = (int)__umulhi((uint32_t)i, inv);  // i / Wn
+            const int q = q0 + r, p = i - r * Wn;
             float vx, vy;
             sphere_normal(F, ring, W, p, q, vx, vy);
             epi(p, q, vx, vy);

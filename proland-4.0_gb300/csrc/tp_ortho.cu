@@ -177,6 +177,8 @@ __global__ void __launch_bounds__(kThreads) ortho_kernel(const tp::OrthoLaunch L
     for (int k = threadIdx.x; k < 256; k += kThreads) inv255[k] = __fdiv_rn((float)k, 255.0f);
     const int W = L.W, n = W - 4, wp = L.win_pitch;
     const int NQ = W / 4;
+    // t / NQ by a multiply-high with ceil(2^32 / NQ): exact for t < 2^20 and NQ <= 4096
+    const uint32_t nq_magic = 0xFFFFFFFFu / (uint32_t)NQ + 1u;
     for (;;) {
         if (threadIdx.x == 0) {
             unit = atomicAdd(L.counter, 1);
@@ -228,7 +230,7 @@ __global__ void __launch_bounds__(kThreads) ortho_kernel(const tp::OrthoLaunch L
         const uint32_t *noise = L.noise + (long long)(J.noise_rot * 6 + J.noise_layer) * W * L.pitch;
         uint32_t *out = L.tiles + (long long)J.out_slot * L.slot_stride;
         for (int t = threadIdx.x; t < W * NQ; t += kThreads) {
-            const int j = t / NQ, q = t - j * NQ, i0 = 4 * q;
+            const int j = (int)__umulhi((uint32_t)t, nq_magic), q = t - j * NQ, i0 = 4 * q;  // j = t / NQ
             const uint4 nq = __ldg(reinterpret_cast<const uint4 *>(noise + (long long)j * L.pitch + i0));
             uint4 rq = make_uint4(0u, 0u, 0u, 0u);
             if (has_res) rq = __ldg(reinterpret_cast<const uint4 *>(res + (long long)j * L.res_pitch + i0));
