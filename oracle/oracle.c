@@ -8,6 +8,7 @@
 
 #include <math.h>
 #include <pthread.h>
+#include <stdatomic.h>
 #include <stddef.h>
 #include <stdlib.h>
 #include <string.h>
@@ -800,6 +801,7 @@ void or_normals_sphere_f64(int W, const double *zm, int zm_pitch, double D, int 
 typedef struct {
     const or_job *jobs;
     int begin, end;
+    atomic_int *next;  /* shared job counter: threads take jobs one at a time */
 } or_span;
 
 static void run_one(const or_job *b)
@@ -819,7 +821,17 @@ static void run_one(const or_job *b)
 static void *run_span(void *arg)
 {
     or_span *s = (or_span *)arg;
-    for (int k = s->begin; k < s->end; ++k) run_one(&s->jobs[k]);
+    if (!s->next) {
+        for (int k = s->begin; k < s->end; ++k) run_one(&s->jobs[k]);
+        return NULL;
+    }
+    /* jobs of different tile widths differ ~4x in work: taking them one at a time
+     * keeps every thread busy until the batch is done */
+    for (;;) {
+        const int k = atomic_fetch_add(s->next, 1);
+        if (k >= s->end) break;
+        run_one(&s->jobs[k]);
+    }
     return NULL;
 }
 
@@ -828,16 +840,19 @@ void or_run_jobs(const or_job *jobs, int n, int nthreads)
     if (nthreads < 1) nthreads = 1;
     if (nthreads > 256) nthreads = 256;
     if (nthreads == 1) {
-        or_span s = {jobs, 0, n};
+        or_span s = {jobs, 0, n, NULL};
         run_span(&s);
         return;
     }
     pthread_t th[256];
     or_span sp[256];
+    atomic_int next;
+    atomic_init(&next, 0);
     for (int k = 0; k < nthreads; ++k) {
         sp[k].jobs = jobs;
-        sp[k].begin = (int)((long long)n * k / nthreads);
-        sp[k].end = (int)((long long)n * (k + 1) / nthreads);
+        sp[k].begin = 0;
+        sp[k].end = n;
+        sp[k].next = &next;
         pthread_create(&th[k], NULL, run_span, &sp[k]);
     }
     for (int k = 0; k < nthreads; ++k) pthread_join(th[k], NULL);
