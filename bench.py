@@ -246,7 +246,7 @@ def time_cpu(classes, min_seconds=4.0):
     threads = os.cpu_count() or 1
     keep = []
     # keep the 101/197 mix of the frame: 3 : 1
-    jobs = cpu_jobs(classes, {101: 12 * threads, 197: 4 * threads}, keep)
+    jobs = cpu_jobs(classes, {101: 24 * threads, 197: 8 * threads}, keep)   # the reference arm's sample
     same = tuned_matches(jobs)
     oracle.run_jobs(jobs[:threads], threads, tuned=True)          # warm-up
     t0 = time.perf_counter()
