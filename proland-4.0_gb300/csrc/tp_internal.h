@@ -149,6 +149,12 @@ struct PlaneXfers {
     PlaneXfer p[kMaxPlaneXfers];
     int n;
 };
+// A growable device buffer per (current device, id) for calls that stage host arrays on
+// the device; callers serialise their own uses (and synchronise their stream before
+// the buffer is handed out again).  Grows by a free and a new allocation after a
+// synchronisation of `stream`.
+enum ScratchId { kScratchNormals = 0, kScratchNormalFormats = 1, kScratchLayers = 2 };
+int device_scratch(int id, size_t bytes, void *stream, char **out);
 // Runs the x.n plane copies in one launch on `stream`.
 int launch_repack_planes(const PlaneXfers &x, void *stream);
 

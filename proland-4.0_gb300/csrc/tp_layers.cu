@@ -434,8 +434,6 @@ int run_layers(tp_storage *elev, const tp_layer_job *jobs, int n, const tp_layer
     }
 
     static std::mutex mu;
-    static char *dbuf = nullptr;
-    static size_t dcap = 0;
     std::lock_guard<std::mutex> lk(mu);
     auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
     const size_t bj = al(sizeof(DevJob) * n), bm = al(sizeof(DevMesh) * (n_meshes ? n_meshes : 1));
@@ -444,16 +442,10 @@ int run_layers(tp_storage *elev, const tp_layer_job *jobs, int n, const tp_layer
     const size_t bt = al(sizeof(Tri) * (size_t)(total_tri ? total_tri : 1));  // triangle records
     const size_t need = bj + bm + bv + bi + bt;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
-    if (dcap < need) {
-        if (dbuf) {
-            cudaStreamSynchronize(s);
-            cudaFree(dbuf);
-        }
-        dbuf = nullptr;
-        dcap = 0;
-        cudaError_t e = cudaMalloc(&dbuf, need);
-        if (e != cudaSuccess) return tp::cuda_fail("cudaMalloc (layer meshes)", e);
-        dcap = need;
+    char *dbuf = nullptr;
+    {
+        int rc = tp::device_scratch(tp::kScratchLayers, need, stream, &dbuf);
+        if (rc) return rc;
     }
     const float4 *dv = vert_dev ? reinterpret_cast<const float4 *>(vertices)
                                 : reinterpret_cast<const float4 *>(dbuf + bj + bm);

@@ -334,8 +334,6 @@ int launch_normals_format(tp_storage *elev, tp_storage *nrm, const int *eslots, 
     const int Wn = elev->W - 4;
     if (grid_mesh < 1 || (Wn - 1) / grid_mesh < 1) return fail(TP_E_BAD_ARG, "normals: bad grid mesh size");
     static std::mutex mu;
-    static char *dbuf = nullptr;
-    static size_t dcap = 0;
     std::lock_guard<std::mutex> lk(mu);
     std::vector<NormalJob> h(count);
     for (int k = 0; k < count; ++k) {
@@ -348,16 +346,10 @@ int launch_normals_format(tp_storage *elev, tp_storage *nrm, const int *eslots, 
     const size_t jobs_bytes = (sizeof(NormalJob) * count + 255) & ~(size_t)255;
     const size_t frames_bytes = frames ? ((sizeof(SphereFrame) * count + 255) & ~(size_t)255) : 0;
     const size_t need = jobs_bytes + frames_bytes + (p2t ? sizeof(float) * 9 * count : 0);
-    if (dcap < need) {
-        if (dbuf) {
-            cudaStreamSynchronize(s);
-            cudaFree(dbuf);
-        }
-        dbuf = nullptr;
-        dcap = 0;
-        cudaError_t e = cudaMalloc(&dbuf, need);
-        if (e != cudaSuccess) return cuda_fail("cudaMalloc (normal jobs)", e);
-        dcap = need;
+    char *dbuf = nullptr;
+    {
+        int rc = device_scratch(kScratchNormalFormats, need, stream, &dbuf);
+        if (rc) return rc;
     }
     cudaError_t e = cudaMemcpyAsync(dbuf, h.data(), sizeof(NormalJob) * count, cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess && frames)
@@ -388,8 +380,6 @@ int launch_normals(tp_storage *elev, tp_storage *nrm, const int *eslots, const i
 {
     if (count <= 0) return TP_OK;
     static std::mutex mu;
-    static char *dbuf = nullptr;
-    static size_t dcap = 0;
     std::lock_guard<std::mutex> lk(mu);
     std::vector<NormalJob> h(count);
     for (int k = 0; k < count; ++k) {
@@ -400,16 +390,10 @@ int launch_normals(tp_storage *elev, tp_storage *nrm, const int *eslots, const i
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     const size_t jobs_bytes = (sizeof(NormalJob) * count + 255) & ~(size_t)255;
     const size_t need = jobs_bytes + (frames ? sizeof(SphereFrame) * count : 0);
-    if (dcap < need) {
-        if (dbuf) {
-            cudaStreamSynchronize(s);
-            cudaFree(dbuf);
-        }
-        dbuf = nullptr;
-        dcap = 0;
-        cudaError_t e = cudaMalloc(&dbuf, need);
-        if (e != cudaSuccess) return cuda_fail("cudaMalloc (normal jobs)", e);
-        dcap = need;
+    char *dbuf = nullptr;
+    {
+        int rc = device_scratch(kScratchNormals, need, stream, &dbuf);
+        if (rc) return rc;
     }
     cudaError_t e = cudaMemcpyAsync(dbuf, h.data(), sizeof(NormalJob) * count, cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess && frames)

@@ -1,0 +1,39 @@
+// Growable device buffers for calls that stage their host arrays (job lists, meshes)
+// on the device before a launch: one buffer per (device, purpose), so that a process
+// that switches devices never hands one device's memory to another's kernels.
+#include <cuda_runtime.h>
+
+#include <map>
+#include <mutex>
+#include <utility>
+
+#include "tp_internal.h"
+
+namespace tp {
+
+int device_scratch(int id, size_t bytes, void *stream, char **out)
+{
+    static std::mutex mu;
+    static std::map<std::pair<int, int>, std::pair<char *, size_t>> bufs;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return cuda_fail("cudaGetDevice (scratch)", e);
+    std::lock_guard<std::mutex> lk(mu);
+    auto &b = bufs[std::make_pair(dev, id)];
+    if (b.second < bytes) {
+        if (b.first) {
+            // the previous user's launch may still read it
+            cudaStreamSynchronize(static_cast<cudaStream_t>(stream));
+            cudaFree(b.first);
+        }
+        b = std::make_pair(nullptr, (size_t)0);
+        char *p = nullptr;
+        e = cudaMalloc(&p, bytes);
+        if (e != cudaSuccess) return cuda_fail("cudaMalloc (scratch)", e);
+        b = std::make_pair(p, bytes);
+    }
+    *out = b.first;
+    return TP_OK;
+}
+
+}  // namespace tp
