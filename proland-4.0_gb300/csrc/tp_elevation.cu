@@ -737,12 +737,15 @@ static KernelFn pick(int stages, int minb, bool mod)
 static int ensure_smem_attr(KernelFn fn, size_t smem)
 {
     static std::mutex mu;
-    static std::map<KernelFn, size_t> have;
+    static std::map<std::pair<int, KernelFn>, size_t> have;  // per device and kernel
+    int dev = 0;
+    cudaGetDevice(&dev);
     std::lock_guard<std::mutex> lk(mu);
-    if (smem <= have[fn]) return TP_OK;
+    size_t &h = have[std::make_pair(dev, fn)];
+    if (smem <= h) return TP_OK;
     cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return cuda_fail("cudaFuncSetAttribute", e);
-    have[fn] = smem;
+    h = smem;
     return TP_OK;
 }
 

@@ -42,17 +42,7 @@ struct tp_frame {
 
 namespace {
 
-int sm_count()
-{
-    static int n = 0;
-    if (n == 0) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
-        if (n <= 0) n = 1;
-    }
-    return n;
-}
+int sm_count() { return tp::device_sm_count(); }
 
 // Validates a class's storages and parameters and fills its launch layout.
 int setup_class(tp_frame::Class &k)

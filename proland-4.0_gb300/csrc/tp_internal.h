@@ -155,6 +155,8 @@ struct PlaneXfers {
 // synchronisation of `stream`.
 enum ScratchId { kScratchNormals = 0, kScratchNormalFormats = 1, kScratchLayers = 2 };
 int device_scratch(int id, size_t bytes, void *stream, char **out);
+// Multiprocessors of the current device (cached per device).
+int device_sm_count();
 // Runs the x.n plane copies in one launch on `stream`.
 int launch_repack_planes(const PlaneXfers &x, void *stream);
 

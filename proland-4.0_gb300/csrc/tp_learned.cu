@@ -501,17 +501,7 @@ __global__ void __launch_bounds__(kRoleThreads) wgrad_kernel(const __grid_consta
 }
 
 // ---------------------------------------------------------------- launch helpers
-int sm_count()
-{
-    static int n = 0;
-    if (!n) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
-        if (n <= 0) n = 1;
-    }
-    return n;
-}
+int sm_count() { return tp::device_sm_count(); }
 
 // CTAs of `kernel` resident on one SM, from its shared memory, registers, threads
 // and tensor-memory columns.  The runtime's occupancy query assumes one CTA per SM
@@ -522,9 +512,11 @@ template <typename K>
 int grid_for(K kernel, int smem, int tmem_cols, int units, int *grid)
 {
     static std::mutex mu;
-    static std::map<const void *, int> cache;  // per kernel instance
+    static std::map<std::pair<int, const void *>, int> cache;  // per device and kernel instance
+    int dev = 0;
+    cudaGetDevice(&dev);
     std::lock_guard<std::mutex> lk(mu);
-    int &per_sm = cache[reinterpret_cast<const void *>(kernel)];
+    int &per_sm = cache[std::make_pair(dev, reinterpret_cast<const void *>(kernel))];
     if (!per_sm) {
         cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
         if (e == cudaSuccess)

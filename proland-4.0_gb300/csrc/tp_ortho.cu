@@ -17,6 +17,7 @@
 
 #include <algorithm>
 #include <cstring>
+#include <map>
 #include <mutex>
 #include <vector>
 
@@ -300,30 +301,34 @@ int ortho_smem_bytes(int W, int *win_pitch)
 
 int launch_ortho(const OrthoLaunch &L, void *stream)
 {
+    // per device: SM count, the shared-memory limit set on the kernel, CTAs per SM
+    struct DevState {
+        int sms = 0, per_sm = 0, smem_set = 0;
+    };
     static std::mutex mu;
-    static int sms = 0, per_sm = 0, smem_set = 0;
+    static std::map<int, DevState> states;
     int pitch = 0;
     const int smem = ortho_smem_bytes(L.W, &pitch);
+    int dev = 0;
+    cudaGetDevice(&dev);
+    int grid = 1;
     {
         std::lock_guard<std::mutex> lk(mu);
-        if (sms == 0) {
-            int dev = 0;
-            cudaGetDevice(&dev);
-            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        }
-        if (smem > smem_set) {
+        DevState &st = states[dev];
+        if (st.sms == 0) cudaDeviceGetAttribute(&st.sms, cudaDevAttrMultiProcessorCount, dev);
+        if (smem > st.smem_set) {
             cudaError_t e = cudaFuncSetAttribute(ortho_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
             if (e != cudaSuccess) return cuda_fail("cudaFuncSetAttribute (ortho)", e);
-            smem_set = smem;
-            per_sm = 0;
+            st.smem_set = smem;
+            st.per_sm = 0;
         }
-        if (per_sm == 0) {
-            cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ortho_kernel, kThreads, smem_set);
+        if (st.per_sm == 0) {
+            cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&st.per_sm, ortho_kernel, kThreads, st.smem_set);
             if (e != cudaSuccess) return cuda_fail("occupancy (ortho)", e);
-            if (per_sm < 1) return fail(TP_E_BAD_ARG, "ortho: the parent window does not fit in shared memory");
+            if (st.per_sm < 1) return fail(TP_E_BAD_ARG, "ortho: the parent window does not fit in shared memory");
         }
+        grid = std::max(1, std::min(L.njobs, st.per_sm * st.sms));
     }
-    const int grid = std::max(1, std::min(L.njobs, per_sm * sms));
     ortho_kernel<<<grid, kThreads, smem, static_cast<cudaStream_t>(stream)>>>(L);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_fail("ortho kernel launch", e);

@@ -1,6 +1,7 @@
-// Growable device buffers for calls that stage their host arrays (job lists, meshes)
-// on the device before a launch: one buffer per (device, purpose), so that a process
-// that switches devices never hands one device's memory to another's kernels.
+// Per-device state of the host side: growable device buffers for calls that stage
+// their host arrays (job lists, meshes) on the device before a launch -- one buffer
+// per (device, purpose), so that a process that switches devices never hands one
+// device's memory to another's kernels -- and the devices' SM counts.
 #include <cuda_runtime.h>
 
 #include <map>
@@ -34,6 +35,21 @@ int device_scratch(int id, size_t bytes, void *stream, char **out)
     }
     *out = b.first;
     return TP_OK;
+}
+
+int device_sm_count()
+{
+    static std::mutex mu;
+    static std::map<int, int> counts;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    std::lock_guard<std::mutex> lk(mu);
+    int &n = counts[dev];
+    if (n <= 0) {
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+        if (n <= 0) n = 1;
+    }
+    return n;
 }
 
 }  // namespace tp
