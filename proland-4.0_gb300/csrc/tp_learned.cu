@@ -151,7 +151,7 @@ __device__ __forceinline__ void load_bf16(const __nv_bfloat16 *base, int img, si
 // Roles of a CTA: warp 0 issues the TMA copies, warp 1 the tensor-core MMAs (and owns
 // the tensor memory), warps 2-5 (one per tensor-memory lane quadrant) run the epilogue.
 constexpr int kRoleThreads = 192;
-constexpr int kConvStages = 4;
+constexpr int kConvStages = 3;
 
 template <int CIN, int COUT>
 constexpr int conv_smem_bytes()
