@@ -197,6 +197,8 @@ int tp_elevation_batch_host(tp_pipeline *p, const tp_elev_params *params, const 
  * graph on its first call and replays it afterwards; the job arrays are
  * uploaded once, before the capture.  One frame per stream at a time. */
 typedef struct tp_frame tp_frame;
+/* The storages named by tp_frame_add must outlive every launch of the frame (its
+ * tensor maps and job arrays point into them); destroy or clear the frame first. */
 int tp_frame_create(tp_frame **out);
 int tp_frame_destroy(tp_frame *f);
 int tp_frame_clear(tp_frame *f);

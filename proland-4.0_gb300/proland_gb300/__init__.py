@@ -370,6 +370,7 @@ class Frame:
         if self.handle:
             lib().tp_frame_destroy(self.handle)
             self.handle = None
+        self._keep = []
 
     def __del__(self):
         try:
@@ -381,11 +382,13 @@ class Frame:
         arr = (TileJob * len(jobs))(*jobs)
         check(lib().tp_frame_add(self.handle, elev.handle, residuals.handle if residuals else None,
                                  normals.handle if normals else None, C.byref(params), arr, len(jobs)))
+        self._keep.append((elev, residuals, normals))  # the launches read these storages
 
     def add_device(self, elev, residuals, normals, params, jobs_dev_ptr, n, has_dependencies=True):
         check(lib().tp_frame_add_device(self.handle, elev.handle, residuals.handle if residuals else None,
                                         normals.handle if normals else None, C.byref(params), jobs_dev_ptr, n,
                                         int(has_dependencies)))
+        self._keep.append((elev, residuals, normals))
 
     def launch(self, stream=None):
         check(lib().tp_frame_launch(self.handle, stream))
