@@ -260,6 +260,9 @@ typedef struct tp_dat tp_dat;
  * residual tile (level, tx, ty); returns 0 on success. */
 typedef int (*tp_residual_source)(void *user, int level, int tx, int ty, float *out, int width);
 
+/* A cache uses its storage, a producer its cache and the producers it reads (residuals,
+ * elevations): each must outlive what uses it (destroy producers, then caches, then
+ * storages). */
 int tp_cache_create(tp_storage *storage, const char *name, tp_cache **out);
 int tp_cache_destroy(tp_cache *c);
 int tp_cache_used_tiles(tp_cache *c);     /* getUsedTiles */
