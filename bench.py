@@ -16,7 +16,8 @@ flush is needed between steps.
 
 --impl reference times the reference's CPU path for this hot path (the C
 restatement of CPUElevationProducer::doCreateTile plus the shader's noise, zc,
-zm and normal arithmetic) on all host cores, on a bounded sample per step.
+zm and normal arithmetic) on all host cores over the whole frame per step,
+from inputs drawn with the same seeds; it loads the oracle only.
 """
 import argparse
 import ctypes as C
@@ -55,27 +56,50 @@ def hbm_peak():
 
 
 # ------------------------------------------------------------------ workload
-class FrameClass:
-    """All requests of one tile width, laid out in slots: outputs [0, n), parents [n, 2n)."""
+def synthetic_inputs():
+    """The numpy generator of the synthetic inputs (proland_gb300/workloads.py), loaded
+    from its file: both arms draw the same seeded frame from it, and the reference arm
+    does not import the package (nor, through it, the CUDA library)."""
+    import importlib.util
+    name = "tp_synthetic_inputs"
+    if name not in sys.modules:
+        spec = importlib.util.spec_from_file_location(name, os.path.join(PKG, "proland_gb300", "workloads.py"))
+        mod = importlib.util.module_from_spec(spec)
+        spec.loader.exec_module(mod)
+        sys.modules[name] = mod
+    return sys.modules[name]
 
-    def __init__(self, W, levels, tx, ty, seed, n_unique_parents=48):
-        from proland_gb300 import workloads
-        import proland_gb300 as tp
+
+class FrameClass:
+    """All requests of one tile width, laid out in slots: outputs [0, n), parents [n, 2n).
+
+    `select(face, level, tx, ty) -> (rotation, layer)` is the noise-layer choice of
+    ElevationProducer.cpp:345-376: the library's for the GPU arm, the oracle's for the
+    reference arm (the two are tested identical)."""
+
+    def __init__(self, W, levels, tx, ty, seed, select, n_unique_parents=48):
+        wl = synthetic_inputs()
         self.W, self.n = W, len(levels)
         self.levels, self.tx, self.ty = levels, tx, ty
-        uz, um = workloads.fbm_parent_tiles(min(n_unique_parents, self.n), W, seed)
+        uz, um = wl.fbm_parent_tiles(min(n_unique_parents, self.n), W, seed)
         pick = np.arange(self.n) % uz.shape[0]
         self.parent_zf = uz[pick]
         self.parent_zm = um[pick]
-        self.residual = workloads.residual_tiles(levels, W, seed + 1)
-        self.jobs = []
-        for k in range(self.n):
-            l = int(levels[k])
-            rot, layer = tp.noise_select(1, l, int(tx[k]), int(ty[k]))
-            self.jobs.append(tp.make_job(l, int(tx[k]), int(ty[k]), out_slot=k, parent_slot=self.n + k,
-                                         residual_slot=k, normal_slot=k, noise_rot=rot, noise_layer=layer,
-                                         noise_amp=float(workloads.noise_amplitude(l)),
-                                         tile_meters=ROOT_QUAD / (1 << l)))
+        self.residual = wl.residual_tiles(levels, W, seed + 1)
+        sel = [select(1, int(l), int(x), int(y)) for l, x, y in zip(levels, tx, ty)]
+        self.noise_rot = np.array([r for r, _ in sel], np.int32)
+        self.noise_layer = np.array([k for _, k in sel], np.int32)
+        self.noise_amp = np.array([wl.noise_amplitude(int(l)) for l in levels], np.float32)
+        self.tile_meters = np.array([ROOT_QUAD / (1 << int(l)) for l in levels], np.float32)
+        self.jobs = None
+
+    def make_jobs(self, tp):
+        """The library's job records (tp_tile_job) of this class."""
+        self.jobs = [tp.make_job(int(self.levels[k]), int(self.tx[k]), int(self.ty[k]), out_slot=k,
+                                 parent_slot=self.n + k, residual_slot=k, normal_slot=k,
+                                 noise_rot=int(self.noise_rot[k]), noise_layer=int(self.noise_layer[k]),
+                                 noise_amp=float(self.noise_amp[k]), tile_meters=float(self.tile_meters[k]))
+                     for k in range(self.n)]
 
     def allocate(self, tp):
         self.elev = tp.TileStorage(self.W, 3, 2 * self.n)
@@ -114,15 +138,22 @@ class FrameClass:
         self.d2h_bytes = n * (3 * W * W + 2 * (W - 4) ** 2) * 4
 
 
-def make_frame(nreq, seed):
-    from proland_gb300 import workloads
-    levels, tx, ty, wide = workloads.frame_requests(nreq, seed)
+def make_frame(nreq, seed, select):
+    levels, tx, ty, wide = synthetic_inputs().frame_requests(nreq, seed)
     classes = []
     for W, sel in ((101, ~wide), (197, wide)):
         idx = np.nonzero(sel)[0]
         if len(idx):
-            classes.append(FrameClass(W, levels[idx], tx[idx], ty[idx], seed + W))
+            classes.append(FrameClass(W, levels[idx], tx[idx], ty[idx], seed + W, select))
     return classes
+
+
+def frame_config(classes, world):
+    """The `config` object both arms print for the frame workload."""
+    alg = sum(fc.n * BYTES_PER_TILE[fc.W] for fc in classes)
+    return {"workload": workload_name(classes), "form": "plain",
+            "l2": "inputs larger than L2 (%.2f GB per step)" % (alg / 1e9),
+            "parallelism": "replicas" if world > 1 else "single GPU"}
 
 
 # ------------------------------------------------------------------ clocks
@@ -190,31 +221,29 @@ class ClockSampler:
 
 
 # ------------------------------------------------------------------ CPU path
-def cpu_jobs(classes, limit_per_class, outs_keepalive):
-    """or_job descriptors for the first `limit_per_class` requests of each class."""
+def cpu_jobs(classes, outs_keepalive):
+    """The oracle's job records (or_job) of every request of the frame, with host
+    output tiles; the same inputs, noise choice and amplitudes as the device frame."""
     import oracle
     jobs = []
+    fp = oracle._f32p
     for fc in classes:
-        W = fc.W
+        W, m = fc.W, fc.n
         table = oracle.dem_noise(W)
-        outs_keepalive.append(table)
-        m = min(limit_per_class[W], fc.n)
         zf = np.empty((m, W, W), np.float32); zc = np.empty_like(zf); zm = np.empty_like(zf)
         nx = np.empty((m, W - 4, W - 4), np.float32); ny = np.empty_like(nx)
-        outs_keepalive += [zf, zc, zm, nx, ny]
-        fp = oracle._f32p
+        outs_keepalive += [table, zf, zc, zm, nx, ny]
         for k in range(m):
-            j = fc.jobs[k]
             b = oracle.Job()
-            b.W, b.level, b.tx, b.ty = W, j.level, j.tx, j.ty
+            b.W, b.level, b.tx, b.ty = W, int(fc.levels[k]), int(fc.tx[k]), int(fc.ty[k])
             b.parent_zf = fc.parent_zf[k].ctypes.data_as(fp)
             b.parent_zm = fc.parent_zm[k].ctypes.data_as(fp)
             b.parent_pitch = W
             b.residual = fc.residual[k].ctypes.data_as(fp)
             b.res_pitch, b.rx, b.ry, b.rscale = W, 0, 0, 1.0
-            b.noise = table[j.noise_layer].ctypes.data_as(fp)
-            b.noise_rot, b.noise_amp = j.noise_rot, j.noise_amp
-            b.tile_meters = j.tile_meters
+            b.noise = table[int(fc.noise_layer[k])].ctypes.data_as(fp)
+            b.noise_rot, b.noise_amp = int(fc.noise_rot[k]), float(fc.noise_amp[k])
+            b.tile_meters = float(fc.tile_meters[k])
             b.out_zf, b.out_zc, b.out_zm = (a[k].ctypes.data_as(fp) for a in (zf, zc, zm))
             b.out_pitch = W
             b.out_nx, b.out_ny = nx[k].ctypes.data_as(fp), ny[k].ctypes.data_as(fp)
@@ -229,8 +258,9 @@ def tuned_matches(jobs, sample=4):
     pick = [jobs[0], next(j for j in jobs if j.W == 197)][:sample]
 
     def outputs(job):
-        n = job.W * job.W
-        return [np.ctypeslib.as_array(getattr(job, f), shape=(n,)).copy() for f in ("out_zf", "out_zc", "out_zm")]
+        n, m = job.W * job.W, (job.W - 4) ** 2
+        return ([np.ctypeslib.as_array(getattr(job, f), shape=(n,)).copy() for f in ("out_zf", "out_zc", "out_zm")]
+                + [np.ctypeslib.as_array(getattr(job, f), shape=(m,)).copy() for f in ("out_nx", "out_ny")])
     oracle.run_jobs(pick, 1)
     want = [outputs(j) for j in pick]
     oracle.run_jobs(pick, 1, tuned=True)
@@ -238,17 +268,20 @@ def tuned_matches(jobs, sample=4):
     return all(np.array_equal(a, b) for wa, ga in zip(want, got) for a, b in zip(wa, ga))
 
 
+CPU_BUILD = "gcc -O3 -ffp-contract=off on this host (no machine-specific flags)"
+
+
 def time_cpu(classes, min_seconds=4.0):
-    """Tiles/s of the CPU path on all host threads over a bounded sample."""
+    """Tiles/s of the CPU path on all host threads: whole frames, repeated for about
+    `min_seconds` (the GPU arm's `cpu_baseline`)."""
     import oracle
     from oracle import build as obuild
     obuild.build()
     threads = os.cpu_count() or 1
     keep = []
-    # keep the 101/197 mix of the frame: 3 : 1
-    jobs = cpu_jobs(classes, {101: 24 * threads, 197: 8 * threads}, keep)   # the reference arm's sample
+    jobs = cpu_jobs(classes, keep)
     same = tuned_matches(jobs)
-    oracle.run_jobs(jobs[:threads], threads, tuned=True)          # warm-up
+    oracle.run_jobs(jobs[:4 * threads], threads, tuned=True)          # warm-up
     t0 = time.perf_counter()
     reps = 0
     while True:
@@ -258,11 +291,11 @@ def time_cpu(classes, min_seconds=4.0):
         if el >= min_seconds:
             break
     out = {"value": reps * len(jobs) / el, "unit": UNIT, "cores": threads, "kind": "port",
-           "sample": "%d tiles (%d x 101, %d x 197) of the frame, %d repetitions, %.1f s" % (
+           "sample": "the whole frame (%d tiles: %d x 101, %d x 197), %d repetitions, %.1f s" % (
                len(jobs), sum(1 for j in jobs if j.W == 101), sum(1 for j in jobs if j.W == 197), reps, el),
-           "build": "gcc -O3 -march=native -ffp-contract=off on this host", "same_results_as_oracle": same}
-    # one thread, same mix
-    one = jobs[:12] + [j for j in jobs if j.W == 197][:4]
+           "build": CPU_BUILD, "same_results_as_oracle": same}
+    # one thread, the frame's 3:1 mix
+    one = [j for j in jobs if j.W == 101][:12] + [j for j in jobs if j.W == 197][:4]
     t0 = time.perf_counter()
     reps = 0
     while time.perf_counter() - t0 < min_seconds / 2:
@@ -310,16 +343,21 @@ def workload_name(classes):
 
 
 def run_reference(args):
+    """The reference's CPU path for this hot path (the oracle's restatement of
+    CPUElevationProducer::doCreateTile with the shader's noise, zc, zm and normal
+    arithmetic) over the whole frame per step, on all host threads.  Builds the frame
+    from numpy and the oracle only: nothing of the GPU library is loaded."""
     rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
     if rank != 0:
         return
-    classes = make_frame(args.requests, args.seed)
     import oracle
     from oracle import build as obuild
     obuild.build()
+    classes = make_frame(args.requests, args.seed, oracle.noise_select)
     threads = os.cpu_count() or 1
     keep = []
-    jobs = cpu_jobs(classes, {101: 24 * threads, 197: 8 * threads}, keep)
+    jobs = cpu_jobs(classes, keep)
     same = tuned_matches(jobs)
     for _ in range(max(args.warmup, 1)):
         oracle.run_jobs(jobs, threads, tuned=True)
@@ -334,12 +372,10 @@ def run_reference(args):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * total / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic",
-            "config": {"workload": workload_name(classes), "form": "plain",
-                       "parallelism": "%d host threads, a bounded sample of the frame per step" % threads},
+            "config": frame_config(classes, world),
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                             "sample": "%d tiles of the frame per step (3:1 101/197 mix)" % len(jobs),
-                             "build": "gcc -O3 -march=native -ffp-contract=off on this host",
-                             "same_results_as_oracle": same},
+                             "sample": "the whole frame (%d tiles) per step" % len(jobs),
+                             "build": CPU_BUILD, "same_results_as_oracle": same},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 
@@ -759,11 +795,12 @@ def main():
         stream = torch.cuda.Stream()
         print(json.dumps({"ortho": ortho_section(tp, torch, stream, C.c_void_p(stream.cuda_stream), args)}))
         return
-    classes = make_frame(args.requests, replicas.rank_seed(args.seed, rank))
+    classes = make_frame(args.requests, replicas.rank_seed(args.seed, rank), tp.noise_select)
     stream = torch.cuda.Stream()
     sh = C.c_void_p(stream.cuda_stream)
     params = tp.make_params()
     for fc in classes:
+        fc.make_jobs(tp)
         fc.allocate(tp)
         fc.pin(torch)
         fc.upload_inputs(tp, sh)
@@ -897,14 +934,13 @@ def main():
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": workload_name(classes),
-                   "form": "plain", "l2": "inputs larger than L2 (%.2f GB per step)" % (sum(alg.values()) / 1e9),
-                   "parallelism": "replicas" if world > 1 else "single GPU", "autotuned": tuned},
+        "config": frame_config(classes, world),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": traffic, "peak_source": peak_src,
                      "kernel": "frame_kernel (one persistent launch per tile width, the two on forked "
                                "streams of a CUDA graph)",
                      "kernel_ms": kernel_ms, "units_per_launch": frame.units(), "per_width": per_width,
+                     "autotuned": tuned,
                      "serialised_launches_ms_per_step": separate_ms,
                      "algorithmic_bytes_per_step": sum(alg.values())},
         "e2e": {"value": world * tiles / (e2e_step / 1000.0), "unit": UNIT, "ms_per_step": e2e_step,

@@ -402,7 +402,7 @@ _TUNED = None
 
 
 def tuned_lib():
-    """The oracle built at -O3 -march=native on this machine (the timed CPU baseline)."""
+    """The oracle built at -O3 on this machine (the timed CPU baseline)."""
     global _TUNED
     if _TUNED is None:
         L = C.CDLL(_build.build_tuned())

@@ -34,8 +34,9 @@ TUNED_LIB = os.path.join(OUT_DIR, "liboracle_tuned.so")
 
 
 def build_tuned(force: bool = False) -> str:
-    """The same sources at -O3 -march=native (floating-point contraction still off),
-    built on the machine that runs them: the timed CPU baseline."""
+    """The same sources at -O3 (floating-point contraction still off), built on the
+    machine that runs them: the timed CPU baseline.  No machine-specific flag, so that
+    the build gives the same bits on x86-64 and aarch64 hosts."""
     srcs = [os.path.join(HERE, "oracle.c"), os.path.join(HERE, "learned.c"), os.path.join(HERE, "ortho.c"),
             os.path.join(HERE, "layers.c")]
     hdr = os.path.join(HERE, "oracle.h")
@@ -44,7 +45,7 @@ def build_tuned(force: bool = False) -> str:
         return TUNED_LIB
     os.makedirs(OUT_DIR, exist_ok=True)
     tmp = TUNED_LIB + ".tmp%d" % os.getpid()
-    cmd = ["gcc", "-O3", "-march=native", "-std=c11", "-D_GNU_SOURCE", "-ffp-contract=off", "-fno-fast-math",
+    cmd = ["gcc", "-O3", "-std=c11", "-D_GNU_SOURCE", "-ffp-contract=off", "-fno-fast-math",
            "-fPIC", "-shared", "-pthread", "-Wall", "-o", tmp, *srcs, "-lm"]
     subprocess.check_call(cmd)
     os.replace(tmp, TUNED_LIB)
