@@ -141,13 +141,16 @@ int tp_normal_batch_format(tp_storage *elev, tp_storage *normals, const tp_tile_
 /* Same as tp_elevation_batch, allocating nothing.  (No counterpart in the
  * reference: its producers draw on GL textures created up front.)  For callers
  * that may not allocate while producing tiles: the kernel's scratch (work
- * counter, completion counts, job records, fp16 noise table) is one static
- * device array of 3,387,648 bytes, shared by all calls on a device.  At most
- * 4096 jobs per call and tile widths up to 253; more is rejected with
- * TP_E_BAD_ARG.  The first call on a device, and the first call for each tile
- * width (it writes that width's noise table into the array), do set-up and
- * should come before any stream capture.  Calls issued one after another on one
- * stream are ordered; calls that overlap on the device race on the array. */
+ * counter, completion counts, job records, fp16 noise tables) is one static
+ * device array of 5,783,296 bytes, shared by all calls on a device.  At most
+ * 4096 jobs per call and tile widths up to 253; the array keeps the noise table
+ * of each width used so far (written once, by the first call with that width;
+ * widths 101, 197 and 253 together fill the room for tables).  More is rejected
+ * with TP_E_BAD_ARG.  The first call on a device, and the first call for each
+ * tile width, do set-up and should come before any stream capture.  The job
+ * records are taken from `jobs` before the call returns (the array may be
+ * refilled or freed at once, pinned or not).  Calls issued one after another on
+ * one stream are ordered; calls that overlap on the device race on the array. */
 int tp_elevation_batch_noalloc(tp_storage *elev, tp_storage *residuals, tp_storage *normals,
                                const tp_elev_params *params, const tp_tile_job *jobs, int n,
                                void *stream);

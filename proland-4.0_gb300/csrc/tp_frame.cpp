@@ -47,78 +47,16 @@ int sm_count() { return tp::device_sm_count(); }
 // Validates a class's storages and parameters and fills its launch layout.
 int setup_class(tp_frame::Class &k)
 {
-    tp_storage *elev = k.elev, *res = k.res, *nrm = k.nrm;
-    const tp_elev_params *p = &k.params;
-    if (!elev) return tp::fail(TP_E_BAD_ARG, "frame: an elevation storage is required");
-    if (elev->on_device != 1 || elev->channels != 3)
-        return tp::fail(TP_E_BAD_ARG, "frame: elevation storage must be a device storage with 3 channels");
-    const int W = elev->W, n = W - 5;
-    if (n < 8 || n % 8 != 0) return tp::fail(TP_E_BAD_ARG, "frame: tile width must be 8k + 5");
-    if (W > 253) return tp::fail(TP_E_BAD_ARG, "frame: tile width above 253 is not supported");
-    if (p->grid_size < 1 || n % p->grid_size != 0)
-        return tp::fail(TP_E_BAD_ARG, "frame: grid_size must divide the tile size");
-    if (p->noise_mode != 0 && p->noise_mode != 1) return tp::fail(TP_E_BAD_ARG, "frame: bad noise_mode");
-    if (res) {
-        if (res->on_device != 1 || res->channels != 1)
-            return tp::fail(TP_E_BAD_ARG, "frame: residual storage must be 1-channel device storage");
-        if ((res->W - 5) % n != 0)
-            return tp::fail(TP_E_BAD_ARG, "frame: residual tile size must be a multiple of the tile size");
-    }
-    if (nrm) {
-        if (nrm->on_device != 1 || nrm->channels != 2 || nrm->W != W - 4)
-            return tp::fail(TP_E_BAD_ARG, "frame: normal storage must be 2-channel device storage of width W - 4");
-        if (p->normal_format != 2)
-            return tp::fail(TP_E_BAD_ARG, "frame: only normal format 2 (signed fp32) is supported");
-    }
-    tp::ClassLaunch &L = k.L;
-    std::memset(&L, 0, sizeof L);
-    L.elev = elev->base;
-    L.W = W;
-    L.pitch = elev->pitch;
-    L.plane_stride = elev->plane_stride;
-    L.slot_stride = elev->slot_stride;
-    if (nrm) {
-        L.nrm = nrm->base;
-        L.nrm_pitch = nrm->pitch;
-        L.nrm_plane_stride = nrm->plane_stride;
-        L.nrm_slot_stride = nrm->slot_stride;
-    }
-    int err = TP_OK;
-    L.noise = tp::device_noise_table(W, &err);
-    if (!L.noise) return err;
-    const int g = n / p->grid_size;
-    L.g = g;
-    L.gshift = -1;
-    if ((g & (g - 1)) == 0) {
-        int sh = 0;
-        while ((1 << sh) < 2 * g) ++sh;
-        L.gshift = sh;
-    }
-    L.flip = p->flip ? 1 : 0;
-    L.no_clamp = p->no_clamp ? 1 : 0;
-    L.noise_mode = p->noise_mode;
-    // band height: whole 101-wide tiles, quarters of 197-wide ones, unless asked
-    int br = p->band_rows > 0 ? p->band_rows : (W <= 128 ? W : (W + 3) / 4);
-    br = std::min(std::max(br, 8), W);
-    L.bands = (W + br - 1) / br;
-    br = (W + L.bands - 1) / L.bands;  // the tallest band actually produced
-    if (br + 2 > 256) return tp::fail(TP_E_BAD_ARG, "frame: band taller than a TMA box");
-    const int PE = elev->pitch;
-    L.buf_floats = tp::round_up((br + 2) * PE, 32);
-    // parent zf window: columns [d, d + n/2 + 5] (stencil and modulated-noise taps),
-    // rows from the first computed row's parent row, (br + 1)/2 + 5 of them
-    L.par_pitch = tp::round_up(n / 2 + 6, 4);
-    L.par_rows = (br + 1) / 2 + 5;
-    if (L.par_pitch > 256 || L.par_rows > 256) return tp::fail(TP_E_BAD_ARG, "frame: parent window above a TMA box");
-    L.par_floats = tp::round_up(L.par_pitch * L.par_rows, 32);
-    const int kmax = (n + 2 + g) / (2 * g);  // largest coarse-mesh index of a sample
-    L.ck = kmax + 2;
-    L.res_box_bytes = (uint32_t)(sizeof(float) * PE * (br + 2));
-    L.par_box_bytes = (uint32_t)(sizeof(float) * L.par_pitch * L.par_rows);
-    int rc = tp::tensor_map(elev, L.par_pitch, L.par_rows, &k.pmap);
+    int br = 0;
+    int rc = tp::class_layout(k.elev, k.res, k.nrm, &k.params, "frame", &k.L, &br);
     if (rc) return rc;
-    if (res) {
-        rc = tp::tensor_map(res, PE, br + 2, &k.rmap);
+    int err = TP_OK;
+    k.L.noise = tp::device_noise_table(k.elev->W, &err);
+    if (!k.L.noise) return err;
+    rc = tp::tensor_map(k.elev, k.L.par_pitch, k.L.par_rows, &k.pmap);
+    if (rc) return rc;
+    if (k.res) {
+        rc = tp::tensor_map(k.res, k.elev->pitch, br + 2, &k.rmap);
         if (rc) return rc;
     } else {
         k.rmap = k.pmap;  // never used: jobs without a residual storage have no residual slot
@@ -324,6 +262,77 @@ int add_class(tp_frame *f, tp_storage *elev, tp_storage *res, tp_storage *nrm, c
 }
 
 }  // namespace
+
+int tp::class_layout(tp_storage *elev, tp_storage *res, tp_storage *nrm, const tp_elev_params *p, const char *who,
+                     tp::ClassLaunch *out, int *band_rows)
+{
+    char buf[200];
+    auto bad = [&](const char *what) {
+        snprintf(buf, sizeof buf, "%s: %s", who, what);
+        return tp::fail(TP_E_BAD_ARG, buf);
+    };
+    if (!elev || !p) return bad("an elevation storage and params are required");
+    if (elev->on_device != 1 || elev->channels != 3) return bad("elevation storage must be a device storage with 3 channels");
+    const int W = elev->W, n = W - 5;
+    if (n < 8 || n % 8 != 0) return bad("tile width must be 8k + 5");
+    if (W > 253) return bad("tile width above 253 is not supported");
+    if (p->grid_size < 1 || n % p->grid_size != 0) return bad("grid_size must divide the tile size");
+    if (p->noise_mode != 0 && p->noise_mode != 1) return bad("bad noise_mode");
+    if (res) {
+        if (res->on_device != 1 || res->channels != 1) return bad("residual storage must be 1-channel device storage");
+        if ((res->W - 5) % n != 0) return bad("residual tile size must be a multiple of the tile size");
+    }
+    if (nrm) {
+        if (nrm->on_device != 1 || nrm->channels != 2 || nrm->W != W - 4)
+            return bad("normal storage must be 2-channel device storage of width W - 4");
+        if (p->normal_format != 2) return bad("only normal format 2 (signed fp32) is supported");
+    }
+    tp::ClassLaunch L;
+    std::memset(&L, 0, sizeof L);
+    L.elev = elev->base;
+    L.W = W;
+    L.pitch = elev->pitch;
+    L.plane_stride = elev->plane_stride;
+    L.slot_stride = elev->slot_stride;
+    if (nrm) {
+        L.nrm = nrm->base;
+        L.nrm_pitch = nrm->pitch;
+        L.nrm_plane_stride = nrm->plane_stride;
+        L.nrm_slot_stride = nrm->slot_stride;
+    }
+    const int g = n / p->grid_size;
+    L.g = g;
+    L.gshift = -1;
+    if ((g & (g - 1)) == 0) {
+        int sh = 0;
+        while ((1 << sh) < 2 * g) ++sh;
+        L.gshift = sh;
+    }
+    L.flip = p->flip ? 1 : 0;
+    L.no_clamp = p->no_clamp ? 1 : 0;
+    L.noise_mode = p->noise_mode;
+    // band height: whole 101-wide tiles, quarters of 197-wide ones, unless asked
+    int br = p->band_rows > 0 ? p->band_rows : (W <= 128 ? W : (W + 3) / 4);
+    br = std::min(std::max(br, 8), W);
+    L.bands = (W + br - 1) / br;
+    br = (W + L.bands - 1) / L.bands;  // the tallest band actually produced
+    if (br + 2 > 256) return bad("band taller than a TMA box");
+    const int PE = elev->pitch;
+    L.buf_floats = tp::round_up((br + 2) * PE, 32);
+    // parent zf window: columns [d, d + n/2 + 5] (stencil and modulated-noise taps),
+    // rows from the first computed row's parent row, (br + 1)/2 + 5 of them
+    L.par_pitch = tp::round_up(n / 2 + 6, 4);
+    L.par_rows = (br + 1) / 2 + 5;
+    if (L.par_pitch > 256 || L.par_rows > 256) return bad("parent window above a TMA box");
+    L.par_floats = tp::round_up(L.par_pitch * L.par_rows, 32);
+    const int kmax = (n + 2 + g) / (2 * g);  // largest coarse-mesh index of a sample
+    L.ck = kmax + 2;
+    L.res_box_bytes = (uint32_t)(sizeof(float) * PE * (br + 2));
+    L.par_box_bytes = (uint32_t)(sizeof(float) * L.par_pitch * L.par_rows);
+    *out = L;
+    *band_rows = br;
+    return TP_OK;
+}
 
 int tp::check_batch_jobs(tp_storage *elev, tp_storage *res, tp_storage *nrm, const tp_tile_job *jobs, int n)
 {

@@ -129,6 +129,13 @@ struct FrameLaunch {
 };
 
 int launch_frame(const FrameLaunch &f, const CUtensorMap *pmap, const CUtensorMap *rmap, int grid, void *stream);
+// Validates one tile width's storages and parameters and fills its launch layout
+// (band rows, shared-memory windows, coarse-mesh lattice); `noise`, `jobs`, `done`
+// and the tensor maps are left to the caller.  `band_rows` receives the tallest
+// band (the residual box is band_rows + 2 rows of the elevation pitch).  Error
+// messages start with `who`.
+int class_layout(tp_storage *elev, tp_storage *res, tp_storage *nrm, const tp_elev_params *p, const char *who,
+                 ClassLaunch *out, int *band_rows);
 int frame_occupancy(int stage_floats, int stages, int minb, bool mod, int *blocks_per_sm);
 
 // Copies `count` slots' plane `channel` between a dense host array and the slots

@@ -14,15 +14,22 @@
 // touches is the caller's (tile storages, job array, stream) or that array.
 //
 // Limits: at most kMaxJobs jobs per call and tile widths up to kMaxWidth (the
-// widest tile the frame kernel supports).  Larger requests are rejected with
-// TP_E_BAD_ARG before anything is enqueued.
+// widest tile the frame kernel supports).  The array also holds the noise table
+// of every tile width used so far on the device, each written once, by the first
+// call with that width, and never rewritten; widths 101, 197 and 253 together
+// fill the space for tables.  Larger requests, and a width whose table no longer
+// fits, are rejected with TP_E_BAD_ARG before anything is enqueued.
 //
 // Set-up: the first call on a device resolves the array's device address with
 // cudaGetSymbolAddress while that device is current (this also loads the
 // module onto the device), and the first call for a tile width writes that
-// width's noise table into the array (a call with another width writes its
-// own, replacing it).  Those set-up calls should come before any stream
-// capture.
+// width's noise table into the array.  Those set-up calls should come before
+// any stream capture.
+//
+// Job records: the call copies them into a file-scope host array (pageable
+// memory, under a mutex) and from there to the device array, so the copy has
+// left the caller's buffer when the call returns: the caller may refill or free
+// its job array at once, pinned or not.
 //
 // Sharing: every call on a device uses the same array.  The counter and the
 // completion counts must start at zero and are cleared on the call's stream
@@ -46,28 +53,39 @@ constexpr int kMaxJobs = 4096;
 constexpr int kMaxWidth = 253;
 constexpr int kMaxNoisePitch = (kMaxWidth + 7) / 8 * 8;
 constexpr int kMaxDevices = 64;
+constexpr int kMaxTables = 8;
 
-// byte layout of the array: [counter, padded to 256 | completion counts | jobs | noise]
+// bytes of one width's pre-rotated fp16 noise table, rounded to 256
+constexpr size_t noise_table_bytes(int W)
+{
+    return (sizeof(__half) * 4 * 6 * (size_t)W * ((W + 7) / 8 * 8) + 255) / 256 * 256;
+}
+
+// byte layout of the array: [counter, padded to 256 | completion counts | jobs | noise tables]
 constexpr size_t kDoneOffset = 256;
 constexpr size_t kJobsOffset = kDoneOffset + sizeof(int) * kMaxJobs;
 constexpr size_t kNoiseOffset = kJobsOffset + sizeof(tp_tile_job) * kMaxJobs;
-constexpr size_t kNoiseBytes = sizeof(__half) * 4 * 6 * (size_t)kMaxWidth * kMaxNoisePitch;
-constexpr size_t kScratchBytes = kNoiseOffset + kNoiseBytes;  // 3,387,648 bytes
+constexpr size_t kNoiseBytes = noise_table_bytes(101) + noise_table_bytes(197) + noise_table_bytes(253);
+constexpr size_t kScratchBytes = kNoiseOffset + kNoiseBytes;  // 5,783,296 bytes
 static_assert(kJobsOffset % 256 == 0 && kNoiseOffset % 256 == 0, "scratch regions stay 256-byte aligned");
-static_assert(kScratchBytes <= (4u << 20), "the static scratch stays below 4 MiB");
+static_assert(kScratchBytes <= (6u << 20), "the static scratch stays below 6 MiB");
 
 __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 
 struct DeviceScratch {
     unsigned char *base = nullptr;  // device address of g_noalloc_scratch on this device
-    int noise_width = 0;            // tile width whose noise table the array holds
+    int ntables = 0;                // noise tables written so far, in order of first use
+    int table_width[kMaxTables] = {};
+    size_t table_offset[kMaxTables] = {};
+    size_t noise_used = 0;          // bytes of the noise region taken
 };
 
 std::mutex g_mu;
 DeviceScratch g_devices[kMaxDevices];
-// host images of a noise table, written under g_mu during set-up only
+// host images written under g_mu: a noise table during set-up, the job records of a call
 float g_host_base[6 * kMaxWidth * kMaxWidth];
 __half g_host_rot[4 * 6 * kMaxWidth * kMaxNoisePitch];
+tp_tile_job g_host_jobs[kMaxJobs];
 
 // The pre-rotated fp16 layout the frame kernel reads ([rotation][layer][row][pitch],
 // pitch = W rounded up to 8; entry (r, l, j, i) is the texel sample (i, j) reads
@@ -91,9 +109,9 @@ void rotate_noise(int W, const float *base, __half *rot)
                 }
 }
 
-// Per-device set-up (address of the array; noise table of width W), with the
-// device current.  Called under g_mu.
-int setup(int W, cudaStream_t s, DeviceScratch **out)
+// Per-device set-up (address of the array; noise table of width W, written once),
+// with the device current.  Called under g_mu.  `noise` receives the table.
+int setup(int W, cudaStream_t s, DeviceScratch **out, const __half **noise)
 {
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
@@ -106,89 +124,34 @@ int setup(int W, cudaStream_t s, DeviceScratch **out)
         if (e != cudaSuccess) return tp::cuda_fail("tp_elevation_batch_noalloc: cudaGetSymbolAddress", e);
         d.base = static_cast<unsigned char *>(p);
     }
-    if (d.noise_width != W) {
-        tp::build_dem_noise(W, g_host_base);
-        rotate_noise(W, g_host_base, g_host_rot);
-        // ordered on the caller's stream after earlier calls that read the old table
-        e = cudaMemcpyAsync(d.base + kNoiseOffset, g_host_rot, sizeof(__half) * 4 * 6 * (size_t)W * tp::round_up(W, 8),
-                            cudaMemcpyHostToDevice, s);
-        if (e != cudaSuccess) return tp::cuda_fail("tp_elevation_batch_noalloc: noise table copy", e);
-        e = cudaStreamSynchronize(s);  // the host image is rewritten by the next set-up
-        if (e != cudaSuccess) return tp::cuda_fail("tp_elevation_batch_noalloc: noise table copy", e);
-        d.noise_width = W;
+    for (int t = 0; t < d.ntables; ++t)
+        if (d.table_width[t] == W) {
+            *out = &d;
+            *noise = reinterpret_cast<const __half *>(d.base + kNoiseOffset + d.table_offset[t]);
+            return TP_OK;
+        }
+    const size_t bytes = noise_table_bytes(W);
+    if (d.ntables == kMaxTables || d.noise_used + bytes > kNoiseBytes) {
+        char buf[200];
+        snprintf(buf, sizeof buf,
+                 "tp_elevation_batch_noalloc: no room left in the static scratch for the noise table of width %d "
+                 "(%zu of %zu bytes taken by %d earlier widths)", W, d.noise_used, kNoiseBytes, d.ntables);
+        return tp::fail(TP_E_BAD_ARG, buf);
     }
+    tp::build_dem_noise(W, g_host_base);
+    rotate_noise(W, g_host_base, g_host_rot);
+    const size_t off = d.noise_used;
+    e = cudaMemcpyAsync(d.base + kNoiseOffset + off, g_host_rot, sizeof(__half) * 4 * 6 * (size_t)W * tp::round_up(W, 8),
+                        cudaMemcpyHostToDevice, s);
+    if (e != cudaSuccess) return tp::cuda_fail("tp_elevation_batch_noalloc: noise table copy", e);
+    e = cudaStreamSynchronize(s);  // the host image is rewritten by the next set-up
+    if (e != cudaSuccess) return tp::cuda_fail("tp_elevation_batch_noalloc: noise table copy", e);
+    d.table_width[d.ntables] = W;
+    d.table_offset[d.ntables] = off;
+    ++d.ntables;
+    d.noise_used += bytes;
     *out = &d;
-    return TP_OK;
-}
-
-// The launch layout of one tile width, by the rules the frame's class set-up
-// applies (band height, shared-memory windows, coarse-mesh lattice), with the
-// noise table taken from the array and tensor maps encoded on the caller's stack.
-int layout(tp_storage *elev, tp_storage *res, tp_storage *nrm, const tp_elev_params *p, const __half *noise,
-           tp::ClassLaunch *out, CUtensorMap *pmap, CUtensorMap *rmap)
-{
-    if (!elev || !p) return tp::fail(TP_E_BAD_ARG, "tp_elevation_batch_noalloc: elevation storage and params are required");
-    if (elev->on_device != 1 || elev->channels != 3)
-        return tp::fail(TP_E_BAD_ARG, "tp_elevation_batch_noalloc: elevation storage must be a device storage with 3 channels");
-    const int W = elev->W, n = W - 5;
-    if (n < 8 || n % 8 != 0) return tp::fail(TP_E_BAD_ARG, "tp_elevation_batch_noalloc: tile width must be 8k + 5");
-    if (W > kMaxWidth) return tp::fail(TP_E_BAD_ARG, "tp_elevation_batch_noalloc: tile width above 253");
-    if (p->grid_size < 1 || n % p->grid_size != 0)
-        return tp::fail(TP_E_BAD_ARG, "tp_elevation_batch_noalloc: grid_size must divide the tile size");
-    if (p->noise_mode != 0 && p->noise_mode != 1) return tp::fail(TP_E_BAD_ARG, "tp_elevation_batch_noalloc: bad noise_mode");
-    if (res && (res->on_device != 1 || res->channels != 1 || (res->W - 5) % n != 0))
-        return tp::fail(TP_E_BAD_ARG, "tp_elevation_batch_noalloc: residual storage must be 1-channel device storage "
-                                      "whose tile size is a multiple of the tile size");
-    if (nrm && (nrm->on_device != 1 || nrm->channels != 2 || nrm->W != W - 4 || p->normal_format != 2))
-        return tp::fail(TP_E_BAD_ARG, "tp_elevation_batch_noalloc: normal storage must be 2-channel device storage "
-                                      "of width W - 4, normal format 2");
-    tp::ClassLaunch L;
-    std::memset(&L, 0, sizeof L);
-    L.elev = elev->base;
-    L.W = W;
-    L.pitch = elev->pitch;
-    L.plane_stride = elev->plane_stride;
-    L.slot_stride = elev->slot_stride;
-    if (nrm) {
-        L.nrm = nrm->base;
-        L.nrm_pitch = nrm->pitch;
-        L.nrm_plane_stride = nrm->plane_stride;
-        L.nrm_slot_stride = nrm->slot_stride;
-    }
-    L.noise = noise;
-    const int g = n / p->grid_size;
-    L.g = g;
-    L.gshift = -1;
-    if ((g & (g - 1)) == 0) {
-        int sh = 0;
-        while ((1 << sh) < 2 * g) ++sh;
-        L.gshift = sh;
-    }
-    L.flip = p->flip ? 1 : 0;
-    L.no_clamp = p->no_clamp ? 1 : 0;
-    L.noise_mode = p->noise_mode;
-    int br = p->band_rows > 0 ? p->band_rows : (W <= 128 ? W : (W + 3) / 4);
-    br = std::min(std::max(br, 8), W);
-    L.bands = (W + br - 1) / br;
-    br = (W + L.bands - 1) / L.bands;
-    if (br + 2 > 256) return tp::fail(TP_E_BAD_ARG, "tp_elevation_batch_noalloc: band taller than a TMA box");
-    const int PE = elev->pitch;
-    L.buf_floats = tp::round_up((br + 2) * PE, 32);
-    L.par_pitch = tp::round_up(n / 2 + 6, 4);
-    L.par_rows = (br + 1) / 2 + 5;
-    L.par_floats = tp::round_up(L.par_pitch * L.par_rows, 32);
-    L.ck = (n + 2 + g) / (2 * g) + 2;
-    L.res_box_bytes = (uint32_t)(sizeof(float) * PE * (br + 2));
-    L.par_box_bytes = (uint32_t)(sizeof(float) * L.par_pitch * L.par_rows);
-    int rc = tp::encode_tensor_map(elev, L.par_pitch, L.par_rows, pmap);
-    if (rc) return rc;
-    if (res) {
-        rc = tp::encode_tensor_map(res, PE, br + 2, rmap);
-        if (rc) return rc;
-    } else {
-        *rmap = *pmap;  // never read: jobs without a residual storage have no residual slot
-    }
-    *out = L;
+    *noise = reinterpret_cast<const __half *>(d.base + kNoiseOffset + off);
     return TP_OK;
 }
 
@@ -211,19 +174,41 @@ extern "C" int tp_elevation_batch_noalloc(tp_storage *elev, tp_storage *residual
     int rc = tp::check_batch_jobs(elev, residuals, normals, jobs, n);
     if (rc) return rc;
     if (n == 0) return TP_OK;
+    tp::FrameLaunch F;
+    std::memset(&F, 0, sizeof F);
+    int br = 0;
+    rc = tp::class_layout(elev, residuals, normals, params, "tp_elevation_batch_noalloc", &F.c, &br);
+    if (rc) return rc;
+    CUtensorMap pmap, rmap;
+    rc = tp::encode_tensor_map(elev, F.c.par_pitch, F.c.par_rows, &pmap);
+    if (rc) return rc;
+    if (residuals) {
+        rc = tp::encode_tensor_map(residuals, elev->pitch, br + 2, &rmap);
+        if (rc) return rc;
+    } else {
+        rmap = pmap;  // never read: jobs without a residual storage have no residual slot
+    }
+    F.stage_floats = F.c.buf_floats + F.c.par_floats + tp::round_up(F.c.ck * F.c.ck, 32);
+    F.stages = params->stages == 2 ? 2 : 1;
+    const size_t per_cta = sizeof(float) * (size_t)F.stage_floats * F.stages + 128 + 1024;
+    F.minb = 3 * per_cta <= 227 * 1024 ? 3 : 2;
+    int per_sm = 0;
+    rc = tp::frame_occupancy(F.stage_floats, F.stages, F.minb, F.c.noise_mode == 1, &per_sm);
+    if (rc) return rc;
+    if (per_sm < 1) return tp::fail(TP_E_BAD_ARG, "tp_elevation_batch_noalloc: the kernel's stage does not fit in shared memory");
+    F.any_deps = 0;
+    for (int i = 0; i < n; ++i)
+        if (jobs[i].parent_job >= 0) F.any_deps = 1;
+
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     std::lock_guard<std::mutex> lk(g_mu);
     DeviceScratch *d = nullptr;
-    rc = setup(elev->W, s, &d);
+    rc = setup(elev->W, s, &d, &F.c.noise);
     if (rc) return rc;
-    tp::FrameLaunch F;
-    std::memset(&F, 0, sizeof F);
-    CUtensorMap pmap, rmap;
-    rc = layout(elev, residuals, normals, params, reinterpret_cast<const __half *>(d->base + kNoiseOffset), &F.c, &pmap,
-                &rmap);
-    if (rc) return rc;
+    // through pageable host memory: the copy has taken the records when it returns
+    std::memcpy(g_host_jobs, jobs, sizeof(tp_tile_job) * n);
     tp_tile_job *jobs_dev = reinterpret_cast<tp_tile_job *>(d->base + kJobsOffset);
-    cudaError_t e = cudaMemcpyAsync(jobs_dev, jobs, sizeof(tp_tile_job) * n, cudaMemcpyHostToDevice, s);
+    cudaError_t e = cudaMemcpyAsync(jobs_dev, g_host_jobs, sizeof(tp_tile_job) * n, cudaMemcpyHostToDevice, s);
     if (e != cudaSuccess) return tp::cuda_fail("tp_elevation_batch_noalloc: job copy", e);
     // the counter and the completion counts start at zero
     e = cudaMemsetAsync(d->base, 0, kDoneOffset + sizeof(int) * n, s);
@@ -232,17 +217,6 @@ extern "C" int tp_elevation_batch_noalloc(tp_storage *elev, tp_storage *residual
     F.c.njobs = n;
     F.c.done = reinterpret_cast<int *>(d->base + kDoneOffset);
     F.counter = reinterpret_cast<int *>(d->base);
-    F.stage_floats = F.c.buf_floats + F.c.par_floats + tp::round_up(F.c.ck * F.c.ck, 32);
-    F.any_deps = 0;
-    for (int i = 0; i < n; ++i)
-        if (jobs[i].parent_job >= 0) F.any_deps = 1;
-    F.stages = params->stages == 2 ? 2 : 1;
-    const size_t per_cta = sizeof(float) * (size_t)F.stage_floats * F.stages + 128 + 1024;
-    F.minb = 3 * per_cta <= 227 * 1024 ? 3 : 2;
-    int per_sm = 0;
-    rc = tp::frame_occupancy(F.stage_floats, F.stages, F.minb, F.c.noise_mode == 1, &per_sm);
-    if (rc) return rc;
-    if (per_sm < 1) return tp::fail(TP_E_BAD_ARG, "tp_elevation_batch_noalloc: the kernel's stage does not fit in shared memory");
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);

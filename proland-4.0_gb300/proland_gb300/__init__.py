@@ -109,8 +109,8 @@ def make_job(level, tx, ty, out_slot, parent_slot=-1, residual_slot=-1, rx=0, ry
 
 
 def elevation_batch(elev, residuals, normals, params, jobs, stream=None):
-    """Produces the jobs (a list of TileJob) in one batch (tp_elevation_batch)."""
-    arr = (TileJob * len(jobs))(*jobs)
+    """Produces the jobs (a list or ctypes array of TileJob) in one batch (tp_elevation_batch)."""
+    arr = job_array(jobs)
     check(lib().tp_elevation_batch(elev.handle, residuals.handle if residuals else None,
                                    normals.handle if normals else None, C.byref(params),
                                    arr, len(jobs), stream))

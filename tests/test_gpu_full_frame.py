@@ -3,10 +3,13 @@ uniform in 1-12, a quarter of them 197-wide, fBm parents, residuals
 N(0, (2000 * 0.5^l)^2) and noise 300 * 0.55^l, produced by one persistent launch
 per tile width (CUDA graph).
 
-The oracle checks a seeded sample of the tiles bit for bit; every tile is checked
-by properties that hold whatever the size: zm is exactly max(zf, 0), normals are
-finite with nx^2 + ny^2 < 1, and the host-buffer pipeline (chunked copies around
-the same kernel) returns the same bytes as the whole-frame launch."""
+The oracle produces every tile of the frame on all host threads: each tile's zf,
+zc and zm are bit-identical to it and its normals within 1e-4.  Every tile is
+also checked by properties that hold whatever the size (zm is exactly max(zf, 0),
+normals are finite with nx^2 + ny^2 < 1), and the host-buffer pipeline (chunked
+copies around the same kernel) returns the same bytes as the whole-frame launch."""
+import os
+
 import numpy as np
 import pytest
 
@@ -30,6 +33,30 @@ def frame_class(tp, W, levels, tx, ty, seed):
                                 normal_slot=k, noise_rot=rot, noise_layer=layer,
                                 noise_amp=float(workloads.noise_amplitude(l)), tile_meters=ROOT_QUAD / (1 << l)))
     return pz, pm, res, jobs
+
+
+def oracle_frame(orc, W, pz, pm, res, jobs):
+    """Every tile of one width through the oracle's threaded batch runner:
+    (zf, zc, zm, nx, ny) arrays of [n, ...]."""
+    n = len(jobs)
+    table = orc.dem_noise(W)
+    zf, zc, zm = (np.empty((n, W, W), np.float32) for _ in range(3))
+    nx, ny = (np.empty((n, W - 4, W - 4), np.float32) for _ in range(2))
+    fp = orc._f32p
+    recs = []
+    for k, j in enumerate(jobs):
+        b = orc.Job()
+        b.W, b.level, b.tx, b.ty = W, j.level, j.tx, j.ty
+        b.parent_zf, b.parent_zm, b.parent_pitch = pz[k].ctypes.data_as(fp), pm[k].ctypes.data_as(fp), W
+        b.residual, b.res_pitch, b.rx, b.ry, b.rscale = res[k].ctypes.data_as(fp), W, 0, 0, 1.0
+        b.noise, b.noise_rot, b.noise_amp = table[j.noise_layer].ctypes.data_as(fp), j.noise_rot, j.noise_amp
+        b.tile_meters = j.tile_meters
+        b.out_zf, b.out_zc, b.out_zm = (a[k].ctypes.data_as(fp) for a in (zf, zc, zm))
+        b.out_pitch = W
+        b.out_nx, b.out_ny, b.nrm_pitch = nx[k].ctypes.data_as(fp), ny[k].ctypes.data_as(fp), W - 4
+        recs.append(b)
+    orc.run_jobs(recs, os.cpu_count() or 1)
+    return zf, zc, zm, nx, ny
 
 
 def test_full_size_batched_frame(gpu, oracle_lib):
@@ -63,18 +90,16 @@ def test_full_size_batched_frame(gpu, oracle_lib):
         assert np.array_equal(zm, np.maximum(zf, np.float32(0.0))), "zm != max(zf, 0)"
         assert np.isfinite(zf).all() and np.isfinite(nx).all() and np.isfinite(ny).all()
         assert float((nx.astype(np.float64) ** 2 + ny.astype(np.float64) ** 2).max()) < 1.0
-        # sampled tiles against the oracle, bit for bit (normals within 1e-4)
-        table = oracle_lib.dem_noise(W)
+        # every tile against the oracle: elevations bit for bit, normals within 1e-4
         zc = elev.download(0, n, tp.ZC)
-        for k in rng.choice(n, 24, replace=False):
-            j = jobs[int(k)]
-            ezf, ezc, ezm = oracle_lib.elevation_tile(W, j.level, j.tx, j.ty, pz[k], pm[k], res[k],
-                                                      noise=table[j.noise_layer], noise_rot=j.noise_rot,
-                                                      noise_amp=j.noise_amp)
-            assert np.array_equal(zf[k], ezf) and np.array_equal(zc[k], ezc) and np.array_equal(zm[k], ezm), \
-                "tile %d (level %d, W %d)" % (k, j.level, W)
-            enx, eny = oracle_lib.normals_flat(W, ezm, float(j.tile_meters))
-            assert np.abs(nx[k] - enx).max() <= 1e-4 and np.abs(ny[k] - eny).max() <= 1e-4
+        ezf, ezc, ezm, enx, eny = oracle_frame(oracle_lib, W, pz, pm, res, jobs)
+        for name, got, want in (("zf", zf, ezf), ("zc", zc, ezc), ("zm", zm, ezm)):
+            bad = np.nonzero((got != want).reshape(n, -1).any(axis=1))[0]
+            assert bad.size == 0, "%s of %d tiles differs (W %d), first %s" % (name, bad.size, W, bad[:5])
+        for name, got, want in (("nx", nx, enx), ("ny", ny, eny)):
+            err = np.abs(got - want).reshape(n, -1).max(axis=1)
+            assert float(err.max()) <= 1e-4, "%s: %d tiles off by more than 1e-4 (W %d)" % (
+                name, int((err > 1e-4).sum()), W)
         # the host-buffer pipeline over all tiles of this width equals the whole-frame launch
         pipe = tp.HostPipeline(W, chunk=256 if W == 101 else 64)
         outs = [np.empty((n, W, W), np.float32) for _ in range(3)] + \
