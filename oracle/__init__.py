@@ -569,3 +569,37 @@ def quadtree_requests(cam, root, max_level, split, dist_factor=1.0, ground=0.0):
 
     visit(0, 0, 0, -root / 2.0, -root / 2.0, root)
     return out
+
+
+# ---------------------------------------------------------------- the reference's own code
+_REF = None
+
+
+def ref_lib():
+    """oracle/_ref/libref.so: pieces of the reference's C++ compiled from its sources by
+    oracle/ref_build.py (noise.cpp, createDemNoise, the noise-layer choice, the CPU
+    elevation loop, HeightMipmap's residual functions), or None where the reference
+    tree is absent.  Used only to check the oracle's restatement."""
+    global _REF
+    if _REF is None:
+        from . import ref_build
+        path = ref_build.build()
+        if path is None or not os.path.exists(path):
+            return None
+        L = C.CDLL(path)
+        L.ref_lrandom.argtypes = [C.POINTER(C.c_long)]
+        L.ref_lrandom.restype = C.c_long
+        L.ref_frandom.argtypes = [C.POINTER(C.c_long)]
+        L.ref_frandom.restype = C.c_float
+        L.ref_cnoise2.argtypes = [C.c_float, C.c_float]
+        L.ref_cnoise2.restype = C.c_float
+        L.ref_dem_noise.argtypes = [C.c_int, _f32p]
+        L.ref_noise_select.argtypes = [C.c_int] * 4 + [C.POINTER(C.c_int)] * 2
+        L.ref_cpu_elevation_tile.argtypes = [C.c_int] * 4 + [_f32p, C.c_int, _f32p, _f32p, C.POINTER(C.c_int)]
+        L.ref_compute_residual.argtypes = [C.c_int, C.c_int, _f32p, _f32p, C.c_int, C.c_int, C.c_int, _f32p,
+                                           _f32p, _f32p]
+        L.ref_encode_residual.argtypes = [C.c_int, C.c_int, C.c_int, _f32p, C.c_void_p]
+        L.ref_compute_approx_tile.argtypes = [C.c_int, C.c_int, _f32p, _f32p, C.c_int, C.c_int, C.c_int, _f32p,
+                                              _f32p]
+        _REF = L
+    return _REF

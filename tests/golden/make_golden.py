@@ -13,7 +13,7 @@ The ortho fixture is cut the same way from the reference's RGB.dat (an
 OrthoCPUProducer pyramid, 196-wide RGBA tiles): tiles (0, 0, 0) and (1, 1, 0)
 kept in rgb_graph1_mini.dat, their decoded bytes in ortho_golden.npz.
 
-    python tests/golden/make_golden.py /root/reference
+    python tests/golden/make_golden.py <reference checkout>
 """
 import hashlib
 import os
@@ -94,4 +94,6 @@ def main(ref_root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_golden.py <reference checkout>")
+    main(sys.argv[1])

@@ -1,0 +1,134 @@
+"""The oracle's restatement against the reference's own code, compiled from its
+sources by oracle/ref_build.py (oracle/_ref/libref.so): the LCG and cnoise of
+math/noise.h / noise.cpp, createDemNoise's table (ElevationProducer.cpp:50-133),
+the noise-layer choice (ElevationProducer.cpp:345-376), CPUElevationProducer's
+residual addressing and stencil loop (CPUElevationProducer.cpp:178-245) and
+HeightMipmap's residual / encode / approximation functions (HeightMipmap.cpp:449-559).
+Every comparison is bit for bit.  The product's host-side noise code is checked
+against the same compiled reference; its CUDA kernels are checked against the
+oracle by the GPU tests, which this pin anchors.
+
+Runs where the reference tree is present (this is where the oracle is pinned);
+skipped elsewhere."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+
+@pytest.fixture(scope="module")
+def ref(oracle_lib):
+    L = oracle_lib.ref_lib()
+    if L is None:
+        pytest.skip("the reference sources are not on this machine")
+    return L
+
+
+def _f(a):
+    return a.ctypes.data_as(C.POINTER(C.c_float))
+
+
+def test_lrandom_and_frandom(ref, oracle_lib):
+    for seed in (1234567, 7654321, 5647381, 12345, 1, 2 ** 31 - 2):
+        a, b = C.c_long(seed), C.c_long(seed)
+        for _ in range(5000):
+            assert ref.ref_lrandom(C.byref(a)) == oracle_lib.lib().or_lrandom(C.byref(b))
+        a, b = C.c_long(seed), C.c_long(seed)
+        got = [ref.ref_frandom(C.byref(a)) for _ in range(5000)]
+        want = [oracle_lib.lib().or_frandom(C.byref(b)) for _ in range(5000)]
+        assert np.array_equal(np.float32(got), np.float32(want))
+
+
+@pytest.mark.parametrize("W", [13, 21, 37, 101, 197, 253])
+def test_dem_noise_table(ref, oracle_lib, product, W):
+    """createDemNoise's float table, rounded to fp16 as its R16F texture stores it,
+    is the oracle's table and the product's."""
+    raw = np.empty((6, W, W), np.float32)
+    ref.ref_dem_noise(W, _f(raw))
+    as_r16f = raw.astype(np.float16).astype(np.float32)
+    assert np.array_equal(oracle_lib.dem_noise(W), as_r16f)
+    assert np.array_equal(product.dem_noise(W), as_r16f)
+
+
+def test_cnoise(ref, oracle_lib, product):
+    rng = np.random.default_rng(1)
+    pts = list(rng.uniform(-5000, 5000, (3000, 2)).astype(np.float32))
+    # the points the layer choice evaluates: integers and half-integers
+    pts += [(np.float32(x + h), np.float32(y + v)) for x in range(-40, 40, 3) for y in range(-40, 70, 5)
+            for h in (0.0, 0.5) for v in (0.0, 0.5)]
+    for x, y in pts:
+        want = np.float32(ref.ref_cnoise2(float(x), float(y)))
+        assert np.float32(oracle_lib.cnoise(x, y)) == want, (x, y)
+        assert np.float32(product.cnoise(x, y)) == want, (x, y)
+
+
+def test_noise_layer_choice(ref, oracle_lib, product):
+    """Every face (0 flat, 1-6 cube faces), levels 0-12, the tile edges and random tiles."""
+    rng = np.random.default_rng(2)
+    r, l = C.c_int(), C.c_int()
+    for face in range(7):
+        for level in range(13):
+            m = 1 << level
+            coords = {(0, 0), (m - 1, 0), (0, m - 1), (m - 1, m - 1)}
+            coords |= {(int(rng.integers(0, m)), int(rng.integers(0, m))) for _ in range(min(m * m, 40))}
+            for tx, ty in coords:
+                ref.ref_noise_select(face, level, tx, ty, C.byref(r), C.byref(l))
+                want = (r.value, l.value)
+                assert oracle_lib.noise_select(face, level, tx, ty) == want, (face, level, tx, ty)
+                assert product.noise_select(face, level, tx, ty) == want, (face, level, tx, ty)
+
+
+@pytest.mark.parametrize("W,Wr", [(101, 101), (101, 197), (197, 197), (21, 21), (21, 37)])
+def test_cpu_elevation_loop(ref, oracle_lib, W, Wr):
+    """CPUElevationProducer::doCreateTile's residual tile choice (tx / mod, ty / mod),
+    offsets (rx, ry) and stencil, against the oracle's loop, for every parity of the
+    tile coordinates, with and without a residual, at level 0 and below."""
+    rng = np.random.default_rng(W * 1000 + Wr)
+    n = W - 5
+    mod = (Wr - 5) // n
+    asked = (C.c_int * 3)()
+    for level in (0, 1, 2, 5, 11):
+        m = 1 << level
+        for tx, ty in {(0, 0), (1, 0), (0, 1), (1, 1), (m - 1, m - 1),
+                       (int(rng.integers(0, m)), int(rng.integers(0, m)))}:
+            parent = (rng.standard_normal((W, W)) * 1000.0).astype(np.float32)
+            for with_res in (True, False):
+                resid = (rng.standard_normal((Wr, Wr)) * 50.0).astype(np.float32) if with_res else None
+                out = np.empty((W, W), np.float32)
+                ref.ref_cpu_elevation_tile(W, level, tx, ty, _f(parent), Wr, _f(resid) if with_res else None,
+                                           _f(out), asked)
+                assert tuple(asked) == (level, tx // mod, ty // mod)
+                want = oracle_lib.cpu_elevation_tile(W, level, tx, ty, parent if level > 0 else None, resid,
+                                                     (tx % mod) * n, (ty % mod) * n)
+                assert np.array_equal(out, want), (level, tx, ty, with_res)
+                # the shader-semantics oracle the GPU tests compare with: its zf without
+                # noise is this loop's output (the reference's CPU / GPU pairing)
+                if level > 0:
+                    zf, _, _ = oracle_lib.elevation_tile(W, level, tx, ty, parent, np.maximum(parent, 0), resid,
+                                                         rx=(tx % mod) * n, ry=(ty % mod) * n,
+                                                         grid_g=max(n // 24, 1))
+                    assert np.array_equal(zf, out), (level, tx, ty, with_res)
+
+
+@pytest.mark.parametrize("W", [101, 197])
+def test_heightmipmap_residual_encode_approx(ref, oracle_lib, W):
+    """HeightMipmap's residual (fine minus the stencil of the parent approximation),
+    its int16 encoding (round to nearest, little-endian bytes) and the approximation
+    (stencil plus quantised residual), against the oracle's preprocess restatement."""
+    rng = np.random.default_rng(W)
+    n = W - 5
+    for tx, ty in ((0, 0), (1, 0), (0, 1), (1, 1), (6, 3)):
+        parent = (rng.standard_normal((W, W)) * 800.0).astype(np.float32)
+        fine = (rng.standard_normal((W, W)) * 800.0 + 3.0).astype(np.float32)
+        rq, enc, approx = oracle_lib.compute_residual(W, tx, ty, parent, fine)
+        res = np.empty((W, W), np.float32)
+        mx, mean = C.c_float(), C.c_float()
+        ref.ref_compute_residual(n, n, _f(parent), _f(fine.copy()), 3, tx, ty, _f(res), C.byref(mx), C.byref(mean))
+        raw = np.zeros((W, W, 2), np.uint8)
+        ref.ref_encode_residual(n, n, 3, _f(res), raw.ctypes.data)
+        assert np.array_equal(res, rq)
+        assert np.array_equal(raw.reshape(-1).view("<i2").reshape(W, W), enc)
+        tile = fine.copy()
+        err = C.c_float()
+        ref.ref_compute_approx_tile(n, n, _f(parent), _f(res), 3, tx, ty, _f(tile), C.byref(err))
+        assert np.array_equal(tile, approx)
