@@ -599,6 +599,202 @@ def layers_section(tp, torch, stream, sh, args):
     return out
 
 
+def quadtree_case(levels, W, seed_root=1):
+    """Configuration 0's inputs: the tiles of a levels 0..`levels` quadtree (parents
+    first), the root's residual an 8-octave fBm tile, level l's residuals
+    N(0, (2000 * 0.5^l)^2) with seed 2 + l."""
+    wl = synthetic_inputs()
+    tiles = [(l, x, y) for l in range(levels + 1) for y in range(1 << l) for x in range(1 << l)]
+    resid = np.empty((len(tiles), W, W), np.float32)
+    resid[0] = wl.value_noise_fbm((W, W), octaves=8, seed=seed_root)
+    k = 1
+    for l in range(1, levels + 1):
+        m = 4 ** l
+        resid[k:k + m] = wl.residual_tiles([l] * m, W, seed=2 + l)
+        k += m
+    return tiles, resid
+
+
+def quadtree_bytes(tiles, W):
+    """Algorithmic bytes of producing `tiles` (the root has no parent window)."""
+    return sum(BYTES_PER_TILE[W] - (2 * ((W - 5) // 2 + 5) ** 2 * 4 if l == 0 else 0) for l, _, _ in tiles)
+
+
+def quadtree_section(tp, torch, stream, sh, args):
+    """Configuration 0 as a timed frame: the whole levels 0-5 quadtree (1365 tiles of
+    101^2, fBm root, residuals, noise off, normals for every tile) in ONE persistent
+    launch whose jobs wait in the kernel for their parent's completion counter
+    (parents before children), autotuned and replayed from a CUDA graph; beside it
+    the same tiles as one launch per level (six launches in stream order, no
+    in-kernel waits).  CUDA events on the launch stream around K whole quadtrees."""
+    W, L, D = 101, 5, 50000.0
+    tiles, resid = quadtree_case(L, W)
+    n = len(tiles)
+    index = {t: k for k, t in enumerate(tiles)}
+    elev, res, nrm = tp.TileStorage(W, 3, n), tp.TileStorage(W, 1, n), tp.TileStorage(W - 4, 2, n)
+    res.upload(0, 0, resid, sh)
+    jobs = []
+    for k, (l, x, y) in enumerate(tiles):
+        pj = index[(l - 1, x // 2, y // 2)] if l > 0 else -1
+        jobs.append(tp.make_job(l, x, y, out_slot=k, parent_slot=pj, residual_slot=k, normal_slot=k,
+                                tile_meters=D / (1 << l), parent_job=pj))
+    params = tp.make_params()
+    steps = max(args.steps // 4, 20)
+    alg = quadtree_bytes(tiles, W)
+    peak, src = hbm_peak()
+
+    def timed(run):
+        with torch.cuda.stream(stream):
+            for _ in range(5):
+                run()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(steps):
+            run()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        tp.stream_check(sh)
+        return e0.elapsed_time(e1) / steps
+
+    one = tp.Frame()
+    one.add(elev, res, nrm, params, jobs)
+    one.autotune(sh, repeats=5)
+    ms_one = timed(lambda: one.graph_launch(sh))
+    shape = one.config(0)
+    zf_one = elev.download(0, n, tp.ZF)
+    waves = []
+    first = 0
+    for l in range(L + 1):
+        m = 4 ** l
+        f = tp.Frame()
+        f.add(elev, res, nrm, params, [tp.make_job(j.level, j.tx, j.ty, out_slot=j.out_slot, parent_slot=j.parent_slot,
+                                                   residual_slot=j.residual_slot, normal_slot=j.normal_slot,
+                                                   tile_meters=j.tile_meters) for j in jobs[first:first + m]])
+        f.autotune(sh, repeats=3)
+        waves.append(f)
+        first += m
+
+    def run_waves():
+        for f in waves:
+            f.graph_launch(sh)
+    ms_waves = timed(run_waves)
+    same = bool(np.array_equal(elev.download(0, n, tp.ZF), zf_one))
+    for f in waves:
+        f.close()
+    one.close()
+    best = min(ms_one, ms_waves)
+    gbs = alg / (best / 1000.0) / 1e9
+    out = {"workload": "levels 0-%d quadtree, %d tiles of %dx%d, fBm root, residuals, noise off, normals" % (L, n, W, W),
+           "tiles": n, "algorithmic_bytes": alg, "steps": steps,
+           "one_launch": {"ms": ms_one, "tiles_per_s": n / (ms_one / 1000.0),
+                          "achieved_gbs": alg / (ms_one / 1000.0) / 1e9,
+                          "frac": alg / (ms_one / 1000.0) / 1e9 / peak, "shape": shape,
+                          "form": "one persistent launch, parents before children, in-kernel waits on the "
+                                  "parent's completion counter, CUDA graph"},
+           "level_waves": {"ms": ms_waves, "tiles_per_s": n / (ms_waves / 1000.0),
+                           "achieved_gbs": alg / (ms_waves / 1000.0) / 1e9,
+                           "frac": alg / (ms_waves / 1000.0) / 1e9 / peak,
+                           "form": "one launch per level (6), each a CUDA graph, in stream order"},
+           "same_tiles": same,
+           "tiles_per_s": n / (best / 1000.0),
+           "roofline": {"bound": "hbm", "achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak,
+                        "peak_source": src}}
+    elev.close(); res.close(); nrm.close()
+    return out
+
+
+def streaming_section(tp, torch, stream, sh, args):
+    """Configuration 2 as timed frames: the seeded camera path of 600 frames from 10 km
+    down to 50 m over a level 0-14 quadtree (root 50 km), 8192-slot caches, through the
+    native TileSampler over the elevation and normal producers (tp_sampler_update:
+    release the vanished quads' tiles, acquire the new ones, one scheduler run:
+    synthetic residuals made on the device, one
+    persistent elevation launch with the flat normals fused, parents first).  The
+    frames' quadtree requests are generated before the timed run (TerrainQuad's split
+    rule, timed apart); each frame is timed on the host around the update and a
+    stream synchronisation, its device work by CUDA events on the stream."""
+    from proland_gb300 import streaming as S
+    W, slots, frames = 101, 8192, 600
+    cams = S.camera_path(frames)
+    t0 = time.perf_counter()
+    reqs = [np.ascontiguousarray(np.asarray(S.quadtree_requests(c), np.int32)) for c in cams]
+    req_ms = 1000.0 * (time.perf_counter() - t0) / frames
+    amps = [300.0 * 0.55 ** l for l in range(S.MAX_LEVEL + 1)]
+
+    def chain(n_slots, seed):
+        rs, es, ns = tp.TileStorage(W, 1, n_slots), tp.TileStorage(W, 3, n_slots), tp.TileStorage(W - 4, 2, n_slots)
+        rc, ec, nc = tp.TileCache(rs, "residual"), tp.TileCache(es, "elevation"), tp.TileCache(ns, "normal")
+        r = tp.ResidualProducer(rc, synthetic=(2000.0, 0.5, seed))
+        e = tp.ElevationProducer(ec, r, noise_amp=amps, params=tp.make_params(), face=0)
+        n = tp.NormalProducer(nc, e)
+        for p in (e, n):
+            p.set_root_quad_size(S.ROOT_SIZE)
+        return [rs, es, ns, rc, ec, nc, r, e, n], tp.TileSampler(e, n)
+
+    L = tp.lib()
+    n_new = C.c_int()
+
+    def update(smp, a):
+        rc = L.tp_sampler_update(smp.handle, a.ctypes.data_as(C.POINTER(C.c_int32)), a.shape[0], sh, C.byref(n_new))
+        tp.check(rc)
+        return n_new.value
+
+    # warm-up: a few frames of the path on a separate chain
+    objs, smp = chain(slots, args.seed + 11)
+    for f in range(0, 40, 4):
+        update(smp, reqs[f])
+    stream.synchronize()
+    smp.close()
+    objs, smp = chain(slots, args.seed + 12)
+    tp.trace_host_times(reset=True)
+    old_flags = tp.trace_set(2)
+    host_ms, dev_ms, news = [], [], []
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(frames)]
+    torch.cuda.synchronize()
+    t_all = time.perf_counter()
+    for f in range(frames):
+        t0 = time.perf_counter()
+        evs[f][0].record(stream)
+        news.append(update(smp, reqs[f]))
+        evs[f][1].record(stream)
+        stream.synchronize()
+        host_ms.append(1000.0 * (time.perf_counter() - t0))
+    total_ms = 1000.0 * (time.perf_counter() - t_all)
+    tp.trace_set(old_flags)
+    phases = {k: {"ms_per_frame": 1000.0 * v[0] / frames, "calls": v[1]}
+              for k, v in tp.trace_host_times(reset=True).items() if v[1]}
+    tp.stream_check(sh)
+    dev_ms = [a.elapsed_time(b) for a, b in evs]
+    smp.close()
+    tiles = int(sum(news))
+    per_tile = BYTES_PER_TILE[W] + W * W * 4        # elevation + normal tile, plus the synthetic residual written
+    alg = tiles * per_tile
+    gpu_s = sum(dev_ms) / 1000.0
+    peak, src = hbm_peak()
+    busy = [d for d, k in zip(dev_ms, news) if k > 0]
+    return {"workload": "camera path of %d frames, 10 km -> 50 m, level 0-14 quadtree, %d-slot caches, "
+                        "101x101 elevation + normal tiles, synthetic residuals, noise 300*0.55^l" % (frames, slots),
+            "frames": frames, "new_tiles": tiles, "new_tiles_per_frame": {"mean": tiles / frames, "max": int(max(news)),
+                                                                          "min": int(min(news))},
+            "quadtree_tiles_per_frame": {"mean": float(np.mean([len(r) for r in reqs])),
+                                         "max": int(max(len(r) for r in reqs))},
+            "tiles_per_s": tiles / (total_ms / 1000.0),
+            "frame_ms": {"p50": float(np.percentile(host_ms, 50)), "p99": float(np.percentile(host_ms, 99)),
+                         "max": float(max(host_ms)), "mean": float(np.mean(host_ms))},
+            "device_ms_per_frame": {"p50": float(np.percentile(dev_ms, 50)), "p99": float(np.percentile(dev_ms, 99)),
+                                    "mean": float(np.mean(dev_ms))},
+            "device_tiles_per_s": tiles / gpu_s if gpu_s > 0 else None,
+            "request_generation_ms_per_frame": req_ms,
+            "host_phases": phases,
+            "algorithmic_bytes_per_tile": per_tile,
+            "roofline": {"bound": "hbm", "achieved": alg / gpu_s / 1e9 if gpu_s > 0 else None, "peak": peak,
+                         "unit": "GB/s", "frac": alg / gpu_s / 1e9 / peak if gpu_s > 0 else None, "peak_source": src,
+                         "over": "device time of the frames' updates (CUDA events)",
+                         "busy_frames_device_ms_p50": float(np.percentile(busy, 50)) if busy else None},
+            "timing": "host clock per frame around tp_sampler_update + stream synchronisation; requests precomputed"}
+
+
 def learned_section(tp, torch, stream, sh, args, plain_w101):
     """The learned-residual form beside the plain one: a net trained on the residual
     pyramid of a procedural 12-octave fBm sampled on 96 x 2^7 + 1 points (device
@@ -768,6 +964,12 @@ def main():
     ap.add_argument("--ortho-rgb", action="store_true", help="ortho frame with RGB instead of HSV noise")
     ap.add_argument("--planet-requests", type=int, default=16384)
     ap.add_argument("--no-layers", action="store_true", help="skip the elevation layer pass")
+    ap.add_argument("--no-quadtree", action="store_true", help="skip the dependency-ordered quadtree frame")
+    ap.add_argument("--no-streaming", action="store_true", help="skip the view-driven streaming frames")
+    ap.add_argument("--streaming-only", action="store_true",
+                    help="run the view-driven streaming frames alone and print their object")
+    ap.add_argument("--quadtree-only", action="store_true",
+                    help="run the dependency-ordered quadtree frame alone and print its object")
     ap.add_argument("--layers-only", action="store_true",
                     help="run the elevation layer pass alone and print its object (for profiling)")
     args = ap.parse_args()
@@ -790,6 +992,14 @@ def main():
     if args.layers_only:
         stream = torch.cuda.Stream()
         print(json.dumps({"layers": layers_section(tp, torch, stream, C.c_void_p(stream.cuda_stream), args)}))
+        return
+    if args.streaming_only:
+        stream = torch.cuda.Stream()
+        print(json.dumps({"streaming": streaming_section(tp, torch, stream, C.c_void_p(stream.cuda_stream), args)}))
+        return
+    if args.quadtree_only:
+        stream = torch.cuda.Stream()
+        print(json.dumps({"quadtree": quadtree_section(tp, torch, stream, C.c_void_p(stream.cuda_stream), args)}))
         return
     if args.ortho_only:
         stream = torch.cuda.Stream()
@@ -953,6 +1163,10 @@ def main():
         "clocks": clk,
         "max_err_vs_fp64": fp64_errors(tp, classes),
     }
+    if not args.no_quadtree:
+        line["quadtree"] = quadtree_section(tp, torch, stream, sh, args)
+    if not args.no_streaming:
+        line["streaming"] = streaming_section(tp, torch, stream, sh, args)
     if not args.no_ortho:
         line["ortho"] = ortho_section(tp, torch, stream, sh, args)
     if not args.no_layers:

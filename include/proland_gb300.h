@@ -274,6 +274,14 @@ int tp_cache_stats(tp_cache *c, long long *queries, long long *misses);
 
 int tp_residual_producer_create(tp_cache *cache, const char *file, int delta, float zscale, tp_producer **out);
 int tp_residual_producer_set_source(tp_producer *p, tp_residual_source fn, void *user);
+/* A residual producer whose tiles are synthetic: iid samples of zero mean and
+ * standard deviation sigma0 * ratio^level per tile (sum of twelve uniforms, an
+ * approximately normal law bounded by 6 sigma), a counter-based function of
+ * (seed, level, tx, ty, sample), made on the device in the scheduler run (on the
+ * host for host storages and tp_residual_tile).  The stand-in for a residual
+ * pyramid that the streaming and quadtree workloads use (the reference's
+ * ResidualProducer reads them from a .dat file, ResidualProducer.cpp:268-340). */
+int tp_residual_producer_set_synthetic(tp_producer *p, double sigma0, double ratio, unsigned seed);
 /* A residual producer over a .dat file decodes its tiles on the device (1) or on
  * the host (0, the default). */
 int tp_residual_producer_set_device_decode(tp_producer *p, int on);
@@ -315,6 +323,38 @@ typedef struct {
 } tp_tile_req;
 int tp_create_tiles(tp_producer *p, const tp_tile_req *reqs, int n, tp_tile **tiles_out, void *stream);
 int tp_create_tile(tp_producer *p, int level, int tx, int ty, tp_tile **tile_out, void *stream);
+/* The TileSamplers of one terrain node (core/.../terrain/TileSampler.cpp:416-461,
+ * TileSampler::getTiles walking the terrain quadtree, one sampler per producer):
+ * a sampler holds one user on each of its producers' tiles (e.g. elevations and
+ * normals) of every quad of the current quadtree.  tp_sampler_update takes the next
+ * frame's quadtree (requests parents first, e.g. from tp_quadtree_requests): it
+ * releases the tiles of quads that disappeared (putTile: they join the caches'
+ * LRUs), acquires the new quads' tiles (getTile, producers in the order given) and
+ * produces them in one scheduler run on `stream` (normal tiles of new elevation
+ * tiles fused into the elevation launch); *new_count receives the number of new
+ * quads.  On failure (TP_E_CACHE_FULL) no tile of the update stays acquired.
+ * tp_sampler_new_tiles copies the last update's new quads (returns their count);
+ * tp_sampler_find returns a held tile of producer number `producer`.  Destroying
+ * the sampler releases every tile it holds. */
+typedef struct tp_sampler tp_sampler;
+int tp_sampler_create(tp_producer *const *producers, int n, tp_sampler **out);
+int tp_sampler_destroy(tp_sampler *s);
+int tp_sampler_update(tp_sampler *s, const tp_tile_req *reqs, int n, void *stream, int *new_count);
+int tp_sampler_new_tiles(const tp_sampler *s, tp_tile_req *out, int capacity);
+int tp_sampler_held(const tp_sampler *s);
+tp_tile *tp_sampler_find(const tp_sampler *s, int producer, int level, int tx, int ty);
+
+/* Tracing (the reference logs per-tile lines on its "DEM" topic, ElevationProducer.cpp:282-286,
+ * and counts cache queries and misses; it has no timer): flags bit 0 wraps the library's
+ * launches and host phases in NVTX ranges (seen by Nsight tools), bit 1 accumulates host
+ * time per phase (sampler release / acquire, residuals, elevation jobs, frame set-up, frame
+ * launch, finish, normals, layers, learned).  The TP_TRACE environment variable sets the
+ * flags at load.  tp_trace_set returns the previous flags; tp_trace_host_times copies up to
+ * n phases' seconds and call counts (optionally resetting them) and returns the number of
+ * phases; tp_trace_phase_name names phase i. */
+int tp_trace_set(int flags);
+int tp_trace_host_times(double *seconds, long long *calls, int n, int reset);
+const char *tp_trace_phase_name(int phase);
 /* The tiles of a terrain quadtree for one camera position (the TileSampler's
  * requests): TerrainQuad::update's split rule (TerrainQuad.cpp:80-105) with
  * TerrainNode::getCameraDist (TerrainNode.cpp:92-97), root quad [-size/2, size/2]^2,

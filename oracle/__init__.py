@@ -109,6 +109,7 @@ def lib():
                                       C.c_int]
         _i16p = C.POINTER(C.c_int16)
         L.or_fbm_heights.argtypes = [C.c_int, C.c_int, C.c_int, C.c_float, C.c_float, C.c_uint32, _i16p]
+        L.or_synthetic_residual.argtypes = [C.c_uint32, C.c_int, C.c_int, C.c_int, C.c_float, C.c_int, _f32p]
         L.or_level_tile.argtypes = [_i16p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_float, _f32p]
         L.or_learned_param_count.restype = C.c_int
         L.or_learned_loss_grad.argtypes = [C.c_int, C.c_int, _f32p, _f32p, _f32p, C.POINTER(C.c_int), _f32p, _f32p,
@@ -513,6 +514,14 @@ def residual_chain_root(dat, delta, zscale=1.0):
 
 
 # ---------------------------------------------------------------- preprocess and learned net
+def synthetic_residual(seed, level, tx, ty, sigma, W):
+    """The product's synthetic residual tile (tp_residual_producer_set_synthetic) for a
+    tile of standard deviation `sigma` (a float32 value)."""
+    out = np.empty((W, W), np.float32)
+    lib().or_synthetic_residual(C.c_uint32(seed), level, tx, ty, C.c_float(sigma), W, _p(out))
+    return out
+
+
 def fbm_heights(size, octaves=12, base_cells=4, amplitude=4000.0, quantum=0.25, seed=1):
     """The device preprocess's procedural fBm height field as int16 (size x size)."""
     out = np.empty((size, size), np.int16)

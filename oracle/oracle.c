@@ -887,3 +887,34 @@ void or_residual_upsample(int n, int tilesize, int tx, int ty, const float *pare
         for (int i = 0; i <= tilesize + 4; ++i)
             out[i + (size_t)j * n] = upsample_sample(parent, n, i, j, px, py);
 }
+
+/* ---------------------------------------------------------------- synthetic residuals
+ * The product's synthetic residual source (tp_residual_producer_set_synthetic):
+ * per tile key h(seed ^ h(level ^ h(tx ^ h(ty)))), per sample s = i + j W the
+ * twelve 16-bit halves of h(key + 6 s + m), m = 0..5, as (k + 0.5) / 65536; their
+ * sum minus 6 (exact in float) times sigma. */
+static uint32_t syn_hash(uint32_t x)
+{
+    x ^= x >> 16;
+    x *= 0x7feb352du;
+    x ^= x >> 15;
+    x *= 0x846ca68bu;
+    x ^= x >> 16;
+    return x;
+}
+
+void or_synthetic_residual(uint32_t seed, int level, int tx, int ty, float sigma, int W, float *out)
+{
+    const uint32_t key = syn_hash(seed ^ syn_hash((uint32_t)level ^ syn_hash((uint32_t)tx ^ syn_hash((uint32_t)ty))));
+    for (int j = 0; j < W; ++j)
+        for (int i = 0; i < W; ++i) {
+            const uint32_t s = (uint32_t)(i + j * W);
+            float acc = 0.0f;
+            for (uint32_t m = 0; m < 6; ++m) {
+                const uint32_t h = syn_hash(key + 6u * s + m);
+                acc += ((float)(h >> 16) + 0.5f) / 65536.0f;
+                acc += ((float)(h & 0xffffu) + 0.5f) / 65536.0f;
+            }
+            out[i + j * W] = (acc - 6.0f) * sigma;
+        }
+}

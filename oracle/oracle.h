@@ -129,6 +129,8 @@ void or_normals_full(int W, const float *zm, int zm_pitch, float tile_meters, co
                      int ppitch, float *o0, float *o1, float *o2, float *o3, int out_pitch);
 
 /* ---- learned.c: device preprocess height field, level tiles, learned net ---- */
+/* the product's synthetic residual tile (sum of twelve 16-bit uniforms - 6) x sigma */
+void or_synthetic_residual(uint32_t seed, int level, int tx, int ty, float sigma, int W, float *out);
 void or_fbm_heights(int size, int octaves, int base_cells, float amplitude, float quantum, uint32_t seed, int16_t *out);
 void or_level_tile(const int16_t *base, int ts, int max_level, int level, int tx, int ty, float scale, float *out);
 int or_learned_param_count(void);

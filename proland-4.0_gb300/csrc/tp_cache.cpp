@@ -22,14 +22,35 @@
 #include <mutex>
 #include <string>
 #include <tuple>
+#include <unordered_map>
+#include <unordered_set>
 #include <vector>
 
 #include "tp_internal.h"
+#include "tp_trace.h"
 
 namespace {
 
 enum Kind { kResidual = 0, kElevation = 1, kNormal = 2, kOrthoResidual = 3, kOrtho = 4 };
-using TKey = std::tuple<int, int, int, int>;  // producer id, level, tx, ty
+// tile id (producer id, level, tx, ty), TileCache.h:80-86
+struct TKey {
+    uint64_t a, b;  // (producer id, level), (tx, ty)
+    TKey(int producer, int level, int tx, int ty)
+        : a(((uint64_t)(uint32_t)producer << 32) | (uint32_t)level), b(((uint64_t)(uint32_t)tx << 32) | (uint32_t)ty)
+    {
+    }
+    bool operator==(const TKey &o) const { return a == o.a && b == o.b; }
+};
+struct TKeyHash {
+    size_t operator()(const TKey &k) const
+    {
+        uint64_t x = k.a * 0x9e3779b97f4a7c15ull ^ (k.b + 0x632be59bd9b4e019ull + (k.a << 6) + (k.a >> 2));
+        x ^= x >> 31;
+        x *= 0xbf58476d1ce4e5b9ull;
+        x ^= x >> 29;
+        return (size_t)x;
+    }
+};
 
 int next_producer_id()
 {
@@ -52,16 +73,38 @@ struct tp_tile {
     tp_producer *dep_parent_owner = nullptr;
     tp_tile *dep_input = nullptr;  // residual tile (elevation) or elevation tile (normal)
     tp_producer *dep_input_owner = nullptr;
+    // the cache's list of unused tiles (users == 0), least recently used first
+    tp_tile *lru_prev = nullptr, *lru_next = nullptr;
 };
 
 struct tp_cache {
     tp_storage *storage = nullptr;
     std::string name;
     std::recursive_mutex mu;
-    std::map<TKey, tp_tile *> used;
-    std::list<tp_tile *> lru;  // unused tiles, least recently used first
-    std::map<TKey, std::list<tp_tile *>::iterator> unused;
+    // every tile holding a slot: used (users > 0) or unused (users == 0, in the LRU list)
+    std::unordered_map<TKey, tp_tile *, TKeyHash> tiles;
+    tp_tile *lru_head = nullptr, *lru_tail = nullptr;
+    int n_unused = 0;
     long long queries = 0, misses = 0;
+
+    void lru_push_back(tp_tile *t)
+    {
+        t->lru_prev = lru_tail;
+        t->lru_next = nullptr;
+        if (lru_tail) lru_tail->lru_next = t;
+        else lru_head = t;
+        lru_tail = t;
+        ++n_unused;
+    }
+    void lru_unlink(tp_tile *t)
+    {
+        if (t->lru_prev) t->lru_prev->lru_next = t->lru_next;
+        else lru_head = t->lru_next;
+        if (t->lru_next) t->lru_next->lru_prev = t->lru_prev;
+        else lru_tail = t->lru_prev;
+        t->lru_prev = t->lru_next = nullptr;
+        --n_unused;
+    }
 };
 
 struct tp_producer {
@@ -88,6 +131,10 @@ struct tp_producer {
     int deform = 0;
     int normal_format = 2;  // 0..3 (NormalProducer.cpp:195); 0/1 add coarse normals
     int device_decode = 0;  // residual producer over a .dat file: decode tiles on the device
+    // residual producer with synthetic tiles: sigma0 * ratio^level, generator seed
+    bool synthetic = false;
+    double syn_sigma0 = 0.0, syn_ratio = 1.0;
+    uint32_t syn_seed = 0;
     int grid_mesh = 24;
     // ortho residual producer (OrthoCPUProducer): tiles of an ortho .dat file, or zeros
     tp_ortho_dat *odat = nullptr;
@@ -156,39 +203,36 @@ tp_tile *get_tile(tp_producer *p, int level, int tx, int ty, int *users_before, 
     std::lock_guard<std::recursive_mutex> lk(c->mu);
     const TKey k = key_of(p, level, tx, ty);
     tp_tile *t = nullptr;
-    auto u = c->used.find(k);
-    if (u != c->used.end()) {
+    auto u = c->tiles.find(k);
+    if (u != c->tiles.end()) {
         t = u->second;
+        if (t->users == 0) {
+            ++c->queries;
+            c->lru_unlink(t);  // an unused tile in the cache: used again
+        }
     } else {
         ++c->queries;
-        auto it = c->unused.find(k);
-        if (it != c->unused.end()) {
-            t = *it->second;
-            c->lru.erase(it->second);
-            c->unused.erase(it);
-        } else {
-            int slot = tp_storage_new_slot(c->storage);
-            if (slot < 0 && !c->lru.empty()) {
-                // recycle the least recently used unused tile's slot
-                tp_tile *old = c->lru.front();
-                c->lru.pop_front();
-                c->unused.erase(TKey(old->producer_id, old->level, old->tx, old->ty));
-                slot = old->slot;
-                forget_tile(old, tp::producer_by_id(old->producer_id));
-            }
-            if (slot < 0) {
-                if (err) *err = tp::fail(TP_E_CACHE_FULL, "Insufficient tile cache size (" + c->name + ")");
-                return nullptr;
-            }
-            ++c->misses;
-            t = new tp_tile;
-            t->producer_id = p->id;
-            t->level = level;
-            t->tx = tx;
-            t->ty = ty;
-            t->slot = slot;
+        int slot = tp_storage_new_slot(c->storage);
+        if (slot < 0 && c->lru_head) {
+            // recycle the least recently used unused tile's slot
+            tp_tile *old = c->lru_head;
+            c->lru_unlink(old);
+            c->tiles.erase(TKey(old->producer_id, old->level, old->tx, old->ty));
+            slot = old->slot;
+            forget_tile(old, tp::producer_by_id(old->producer_id));
         }
-        c->used[k] = t;
+        if (slot < 0) {
+            if (err) *err = tp::fail(TP_E_CACHE_FULL, "Insufficient tile cache size (" + c->name + ")");
+            return nullptr;
+        }
+        ++c->misses;
+        t = new tp_tile;
+        t->producer_id = p->id;
+        t->level = level;
+        t->tx = tx;
+        t->ty = ty;
+        t->slot = slot;
+        c->tiles.emplace(k, t);
     }
     if (users_before) *users_before = t->users;
     t->users += 1;
@@ -210,12 +254,7 @@ int put_tile(tp_producer *p, tp_tile *t)
     tp_cache *c = p->cache;
     std::lock_guard<std::recursive_mutex> lk(c->mu);
     t->users -= 1;
-    if (t->users == 0) {
-        const TKey k = key_of(p, t->level, t->tx, t->ty);
-        c->used.erase(k);
-        c->lru.push_back(t);
-        c->unused[k] = std::prev(c->lru.end());
-    }
+    if (t->users == 0) c->lru_push_back(t);  // kept in the cache, unused
     return t->users;
 }
 
@@ -288,7 +327,7 @@ int schedule(tp_producer *p, tp_tile *t)
 // ResidualProducer::hasTile (ResidualProducer.cpp:161-175).
 bool residual_has_tile(const tp_producer *r, int level, int tx, int ty)
 {
-    if (!r->dat) return true;  // synthetic source or zero residuals: every tile exists
+    if (r->synthetic || !r->dat) return true;  // synthetic source or zero residuals: every tile exists
     const int l = level + r->delta - r->dat->root_level;
     return l >= 0 && (tx >> l) == r->dat->root_tx && (ty >> l) == r->dat->root_ty && l <= r->dat->max_level;
 }
@@ -325,10 +364,19 @@ void upsample_small(int level_tilesize, int tx, int ty, const float *parent, flo
 
 // ResidualProducer::doCreateTile + readTile (ResidualProducer.cpp:177-232,
 // 268-340) into a dense Wr x Wr host tile.
+float synthetic_sigma(const tp_producer *r, int level)
+{
+    return (float)(r->syn_sigma0 * std::pow(r->syn_ratio, (double)level));
+}
+
 int produce_residual(tp_producer *r, const tp_tile *t, float *out)
 {
     const int Wr = r->cache->storage->W;
     std::fill(out, out + (size_t)Wr * Wr, 0.0f);
+    if (r->synthetic) {
+        tp::synthetic_residual_host(r->syn_seed, t->level, t->tx, t->ty, synthetic_sigma(r, t->level), Wr, out, Wr);
+        return TP_OK;
+    }
     if (r->source) {
         int rc = r->source(r->source_user, t->level, t->tx, t->ty, out, Wr);
         return rc ? tp::fail(TP_E_IO, "residual source callback failed") : TP_OK;
@@ -382,8 +430,7 @@ extern "C" int tp_cache_create(tp_storage *storage, const char *name, tp_cache *
 extern "C" int tp_cache_destroy(tp_cache *c)
 {
     if (!c) return TP_OK;
-    for (auto &kv : c->used) delete kv.second;
-    for (tp_tile *t : c->lru) delete t;
+    for (auto &kv : c->tiles) delete kv.second;
     delete c;
     return TP_OK;
 }
@@ -392,14 +439,14 @@ extern "C" int tp_cache_used_tiles(tp_cache *c)
 {
     if (!c) return TP_E_BAD_ARG;
     std::lock_guard<std::recursive_mutex> lk(c->mu);
-    return (int)c->used.size();
+    return (int)c->tiles.size() - c->n_unused;
 }
 
 extern "C" int tp_cache_unused_tiles(tp_cache *c)
 {
     if (!c) return TP_E_BAD_ARG;
     std::lock_guard<std::recursive_mutex> lk(c->mu);
-    return (int)c->lru.size();
+    return c->n_unused;
 }
 
 extern "C" int tp_cache_stats(tp_cache *c, long long *queries, long long *misses)
@@ -542,6 +589,18 @@ extern "C" int tp_ortho_producer_create(tp_cache *cache, tp_producer *residuals,
     return TP_OK;
 }
 
+extern "C" int tp_residual_producer_set_synthetic(tp_producer *p, double sigma0, double ratio, unsigned seed)
+{
+    if (!p || p->kind != kResidual) return tp::fail(TP_E_BAD_ARG, "tp_residual_producer_set_synthetic: not a residual producer");
+    if (!(sigma0 >= 0.0) || !(ratio > 0.0)) return tp::fail(TP_E_BAD_ARG, "tp_residual_producer_set_synthetic: bad sigma");
+    std::lock_guard<std::recursive_mutex> lk(p->cache->mu);
+    p->synthetic = true;
+    p->syn_sigma0 = sigma0;
+    p->syn_ratio = ratio;
+    p->syn_seed = seed;
+    return TP_OK;
+}
+
 extern "C" int tp_residual_producer_set_device_decode(tp_producer *p, int on)
 {
     if (!p || p->kind != kResidual) return tp::fail(TP_E_BAD_ARG, "tp_residual_producer_set_device_decode: not a residual producer");
@@ -660,12 +719,8 @@ extern "C" tp_tile *tp_producer_find_tile(tp_producer *p, int level, int tx, int
     std::lock_guard<std::recursive_mutex> lk(c->mu);
     const TKey k = key_of(p, level, tx, ty);
     tp_tile *t = nullptr;
-    auto u = c->used.find(k);
-    if (u != c->used.end()) t = u->second;
-    if (!t && include_cache) {
-        auto it = c->unused.find(k);
-        if (it != c->unused.end()) t = *it->second;
-    }
+    auto u = c->tiles.find(k);
+    if (u != c->tiles.end() && (u->second->users > 0 || include_cache)) t = u->second;
     if (t && done && !t->done) t = nullptr;
     return t;
 }
@@ -687,7 +742,7 @@ extern "C" int tp_producer_prefetch_tile(tp_producer *p, int level, int tx, int 
     tp_cache *c = p->cache;
     std::lock_guard<std::recursive_mutex> lk(c->mu);
     const TKey k = key_of(p, level, tx, ty);
-    if (c->used.count(k) || c->unused.count(k)) return 0;
+    if (c->tiles.count(k)) return 0;
     int err = TP_OK;
     tp_tile *t = get_tile(p, level, tx, ty, nullptr, &err);
     if (!t) return err == TP_E_CACHE_FULL ? 0 : err;
@@ -702,15 +757,21 @@ extern "C" int tp_producer_invalidate_tiles(tp_producer *p)
     if (!p) return tp::fail(TP_E_BAD_ARG, "tp_producer_invalidate_tiles: bad arguments");
     tp_cache *c = p->cache;
     std::lock_guard<std::recursive_mutex> lk(c->mu);
-    for (auto &kv : c->used)
-        if (kv.second->producer_id == p->id) {
-            kv.second->done = false;
-            if (!kv.second->queued) {
-                int rc = schedule(p, kv.second);
-                if (rc) return rc;
-            }
+    // collected first: scheduling acquires tiles, which changes the table
+    std::vector<tp_tile *> mine;
+    for (auto &kv : c->tiles)
+        if (kv.second->producer_id == p->id && kv.second->users > 0) mine.push_back(kv.second);
+    std::sort(mine.begin(), mine.end(), [](const tp_tile *x, const tp_tile *y) {
+        return std::make_tuple(x->level, x->ty, x->tx) < std::make_tuple(y->level, y->ty, y->tx);
+    });
+    for (tp_tile *t : mine) {
+        t->done = false;
+        if (!t->queued) {
+            int rc = schedule(p, t);
+            if (rc) return rc;
         }
-    for (tp_tile *t : c->lru)
+    }
+    for (tp_tile *t = c->lru_head; t; t = t->lru_next)
         if (t->producer_id == p->id) t->done = false;
     return TP_OK;
 }
@@ -792,9 +853,33 @@ int run_residuals_device(tp_producer *r, void *stream)
     return TP_OK;
 }
 
+int run_residuals_synthetic(tp_producer *r, void *stream)
+{
+    std::vector<int> slots, lv, txs, tys;
+    std::vector<float> sig;
+    for (tp_tile *t : r->queue) {
+        slots.push_back(t->slot);
+        lv.push_back(t->level);
+        txs.push_back(t->tx);
+        tys.push_back(t->ty);
+        sig.push_back(synthetic_sigma(r, t->level));
+    }
+    int rc = tp::synthetic_residuals_device(r->cache->storage, r->syn_seed, slots.data(), lv.data(), txs.data(),
+                                            tys.data(), sig.data(), (int)slots.size(), stream);
+    if (rc) return rc;
+    for (tp_tile *t : r->queue) {
+        t->done = true;
+        t->queued = false;
+    }
+    r->queue.clear();
+    return TP_OK;
+}
+
 int run_residuals(tp_producer *r, void *stream)
 {
     if (r->queue.empty()) return TP_OK;
+    tp::TraceScope ts("residuals", tp::kPhResiduals);
+    if (r->synthetic && r->cache->storage->on_device == 1) return run_residuals_synthetic(r, stream);
     if (r->dat && r->device_decode && r->cache->storage->on_device == 1) return run_residuals_device(r, stream);
     tp_storage *s = r->cache->storage;
     const int Wr = s->W;
@@ -823,7 +908,7 @@ int run_residuals(tp_producer *r, void *stream)
 
 // The tp_tile_job of an elevation tile; `index` maps tiles of the same launch to
 // their job numbers (a parent found there is named in parent_job).
-int elevation_job(const tp_producer *e, const tp_tile *t, const std::map<const tp_tile *, int> &index, int normal_slot,
+int elevation_job(const tp_producer *e, const tp_tile *t, const std::unordered_map<const tp_tile *, int> &index, int normal_slot,
                   tp_tile_job &j)
 {
     const int n = e->cache->storage->W - 5;
@@ -858,6 +943,7 @@ int elevation_job(const tp_producer *e, const tp_tile *t, const std::map<const t
 // and blended into zm (ElevationProducer.cpp:383-399).
 int run_layers(tp_producer *e, const std::vector<tp_tile *> &tiles, void *stream)
 {
+    tp::TraceScope ts("layers", tp::kPhLayers);
     tp_layer_builder b;
     std::vector<tp_layer_job> jobs(tiles.size());
     for (size_t k = 0; k < tiles.size(); ++k) {
@@ -890,7 +976,7 @@ int run_elevations(tp_producer *e, tp_producer *normals, void *stream)
     // (flat deformation; spherical normals run in their own kernel afterwards; a
     // producer with layers changes zm after its launch, so its normals come later)
     const bool layered = !e->layers.empty();
-    std::map<const tp_tile *, tp_tile *> fused;  // elevation tile -> normal tile
+    std::unordered_map<const tp_tile *, tp_tile *> fused;  // elevation tile -> normal tile
     if (!layered && normals && !normals->deform && normals->normal_format == 2)
         for (tp_tile *nt : normals->queue)
             if (nt->dep_input && nt->dep_input->queued) fused[nt->dep_input] = nt;
@@ -907,7 +993,7 @@ int run_elevations(tp_producer *e, tp_producer *normals, void *stream)
             size_t k1 = k;
             while (k1 < q.size() && q[k1]->level == q[k]->level) ++k1;
             std::vector<tp_tile *> lvl(q.begin() + k, q.begin() + k1);
-            std::map<const tp_tile *, int> none;
+            std::unordered_map<const tp_tile *, int> none;
             std::vector<tp_tile_job> jobs(lvl.size());
             for (size_t i = 0; i < lvl.size() && rc == TP_OK; ++i) rc = elevation_job(e, lvl[i], none, -1, jobs[i]);
             if (rc == TP_OK) {
@@ -927,30 +1013,41 @@ int run_elevations(tp_producer *e, tp_producer *normals, void *stream)
         e->queue.swap(rest);
         return rc;
     }
-    std::map<const tp_tile *, int> index;
-    for (size_t k = 0; k < q.size(); ++k) index[q[k]] = (int)k;
     std::vector<tp_tile_job> jobs(q.size());
-    for (size_t k = 0; k < q.size(); ++k) {
-        auto f = fused.find(q[k]);
-        int rc = elevation_job(e, q[k], index, f != fused.end() ? f->second->slot : -1, jobs[k]);
+    {
+        tp::TraceScope ts("elevation jobs", tp::kPhElevJobs);
+        std::unordered_map<const tp_tile *, int> index;
+        index.reserve(q.size() * 2);
+        for (size_t k = 0; k < q.size(); ++k) index[q[k]] = (int)k;
+        for (size_t k = 0; k < q.size(); ++k) {
+            auto f = fused.find(q[k]);
+            int rc = elevation_job(e, q[k], index, f != fused.end() ? f->second->slot : -1, jobs[k]);
+            if (rc) return rc;
+        }
+    }
+    {
+        tp::TraceScope ts("frame setup", tp::kPhFrameSetup);
+        tp_frame_clear(e->frame);
+        int rc = tp_frame_add(e->frame, e->cache->storage, e->residuals ? e->residuals->cache->storage : nullptr,
+                              normals && !fused.empty() ? normals->cache->storage : nullptr, &e->params, jobs.data(),
+                              (int)jobs.size());
         if (rc) return rc;
     }
-    tp_frame_clear(e->frame);
-    int rc = tp_frame_add(e->frame, e->cache->storage, e->residuals ? e->residuals->cache->storage : nullptr,
-                          normals && !fused.empty() ? normals->cache->storage : nullptr, &e->params, jobs.data(),
-                          (int)jobs.size());
-    if (rc) return rc;
-    rc = tp_frame_launch(e->frame, stream);
-    if (rc) return rc;
+    {
+        tp::TraceScope ts("elevation launch", tp::kPhFrameLaunch);
+        int rc = tp_frame_launch(e->frame, stream);
+        if (rc) return rc;
+    }
+    tp::TraceScope ts("finish", tp::kPhFinish);
     finish_tiles(q);
     e->queue.clear();
     if (normals) {
+        std::unordered_set<const tp_tile *> fused_normals;
+        fused_normals.reserve(fused.size() * 2);
+        for (auto &kv : fused) fused_normals.insert(kv.second);
         std::vector<tp_tile *> rest;
         for (tp_tile *nt : normals->queue) {
-            bool was_fused = false;
-            for (auto &kv : fused)
-                if (kv.second == nt) was_fused = true;
-            if (was_fused) {
+            if (fused_normals.count(nt)) {
                 nt->done = true;
                 nt->queued = false;
                 release_deps(nt);
@@ -1010,6 +1107,7 @@ int run_normals_format(tp_producer *np, void *stream)
 
 int run_normals(tp_producer *np, void *stream)
 {
+    tp::TraceScope ts("normals", tp::kPhNormals);
     if (np->queue.empty()) return TP_OK;
     tp_producer *e = np->elevations;
     if (!(e->root_quad_size > 0.0f)) return tp::fail(TP_E_BAD_ARG, "normal producer: root quad size not set");
@@ -1304,6 +1402,153 @@ extern "C" int tp_create_tile(tp_producer *p, int level, int tx, int ty, tp_tile
 {
     const tp_tile_req r = {level, tx, ty};
     return tp_create_tiles(p, &r, 1, tile_out, stream);
+}
+
+// ---------------------------------------------------------------- sampler
+// The TileSamplers of one terrain node (TileSampler::getTiles, TileSampler.cpp:416-461):
+// one user held on each producer's tile of every quad of the current quadtree; per
+// update, the tiles of quads that disappeared are released (to the caches' LRUs), the
+// new quads' tiles acquired (getTile, in request order: parents first; producers in
+// the order given) and all produced by one scheduler run, so that normal tiles of
+// new elevation tiles are fused into the elevation launch.
+struct tp_sampler {
+    static constexpr int kMaxProducers = 8;
+    struct Quad {
+        uint64_t key;
+        uint32_t stamp;  // the last update whose quadtree held it
+        tp_tile *tiles[kMaxProducers];
+    };
+    std::vector<tp_producer *> producers;
+    std::vector<Quad> held;                        // dense: released quads swap with the last one
+    std::unordered_map<uint64_t, uint32_t> index;  // quad key -> position in `held`
+    uint32_t frame = 0;
+    std::vector<tp_tile_req> fresh;  // the last update's new quads
+};
+
+namespace {
+uint64_t req_key(int level, int tx, int ty)
+{
+    return ((uint64_t)level << 58) | ((uint64_t)(uint32_t)tx << 29) | (uint64_t)(uint32_t)ty;
+}
+
+void sampler_drop(tp_sampler *s, size_t pos, bool cancel)
+{
+    tp_sampler::Quad &q = s->held[pos];
+    for (size_t p = 0; p < s->producers.size(); ++p) {
+        put_tile(s->producers[p], q.tiles[p]);
+        if (cancel) cancel_orphan(s->producers[p], q.tiles[p]);
+    }
+    s->index.erase(q.key);
+    if (pos + 1 != s->held.size()) {
+        q = s->held.back();
+        s->index[q.key] = (uint32_t)pos;
+    }
+    s->held.pop_back();
+}
+}  // namespace
+
+extern "C" int tp_sampler_create(tp_producer *const *producers, int n, tp_sampler **out)
+{
+    if (!producers || n < 1 || n > tp_sampler::kMaxProducers || !out)
+        return tp::fail(TP_E_BAD_ARG, "tp_sampler_create: bad arguments");
+    for (int i = 0; i < n; ++i)
+        if (!producers[i]) return tp::fail(TP_E_BAD_ARG, "tp_sampler_create: a producer is NULL");
+    *out = new tp_sampler;
+    (*out)->producers.assign(producers, producers + n);
+    (*out)->index.reserve(16384);
+    return TP_OK;
+}
+
+extern "C" int tp_sampler_destroy(tp_sampler *s)
+{
+    if (!s) return TP_OK;
+    for (auto &q : s->held)
+        for (size_t i = 0; i < s->producers.size(); ++i) put_tile(s->producers[i], q.tiles[i]);
+    delete s;
+    return TP_OK;
+}
+
+extern "C" int tp_sampler_update(tp_sampler *s, const tp_tile_req *reqs, int n, void *stream, int *new_count)
+{
+    if (!s || n < 0 || (n > 0 && !reqs)) return tp::fail(TP_E_BAD_ARG, "tp_sampler_update: bad arguments");
+    for (int i = 0; i < n; ++i) {
+        const tp_tile_req &r = reqs[i];
+        if (r.level < 0 || r.level > 29 || r.tx < 0 || r.ty < 0 || (r.tx >> r.level) != 0 || (r.ty >> r.level) != 0)
+            return tp::fail(TP_E_BAD_ARG, "tp_sampler_update: bad quadtree coordinates");
+    }
+    const size_t np = s->producers.size();
+    const uint32_t frame = ++s->frame;
+    std::vector<int> fresh_idx;
+    {
+        // quads kept: stamped; quads that disappeared: their tiles go back to the caches
+        // first, so that their slots can take the new tiles
+        tp::TraceScope ts("sampler release", tp::kPhSamplerRelease);
+        for (int i = 0; i < n; ++i) {
+            auto it = s->index.find(req_key(reqs[i].level, reqs[i].tx, reqs[i].ty));
+            if (it != s->index.end()) s->held[it->second].stamp = frame;
+            else fresh_idx.push_back(i);
+        }
+        for (size_t pos = s->held.size(); pos-- > 0;)
+            if (s->held[pos].stamp != frame) sampler_drop(s, pos, false);
+    }
+    s->fresh.clear();
+    const size_t kept = s->held.size();
+    int rc = TP_OK;
+    {
+        tp::TraceScope ts("sampler acquire", tp::kPhSamplerAcquire);
+        for (int i : fresh_idx) {
+            const tp_tile_req &r = reqs[i];
+            const uint64_t k = req_key(r.level, r.tx, r.ty);
+            if (s->index.count(k)) continue;  // requested twice
+            tp_sampler::Quad q;
+            q.key = k;
+            q.stamp = frame;
+            size_t got = 0;
+            for (; got < np; ++got) {
+                q.tiles[got] = get_tile(s->producers[got], r.level, r.tx, r.ty, nullptr, &rc);
+                if (!q.tiles[got]) break;
+            }
+            if (got < np) {
+                if (rc == TP_OK) rc = tp::fail(TP_E_CACHE_FULL, "tp_sampler_update: tile cache full");
+                for (size_t p = 0; p < got; ++p) {
+                    put_tile(s->producers[p], q.tiles[p]);
+                    cancel_orphan(s->producers[p], q.tiles[p]);
+                }
+                break;
+            }
+            s->index.emplace(k, (uint32_t)s->held.size());
+            s->held.push_back(q);
+            s->fresh.push_back(r);
+        }
+    }
+    if (rc == TP_OK) rc = tp_scheduler_run(s->producers.data(), (int)np, stream);
+    if (rc != TP_OK) {
+        // no tile of this update stays acquired (the new quads sit after `kept`)
+        const std::string msg = tp_last_error();
+        while (s->held.size() > kept) sampler_drop(s, s->held.size() - 1, true);
+        s->fresh.clear();
+        return tp::fail(rc, msg);
+    }
+    if (new_count) *new_count = (int)s->fresh.size();
+    return TP_OK;
+}
+
+extern "C" int tp_sampler_new_tiles(const tp_sampler *s, tp_tile_req *out, int capacity)
+{
+    if (!s || capacity < 0 || (capacity > 0 && !out)) return tp::fail(TP_E_BAD_ARG, "tp_sampler_new_tiles: bad arguments");
+    const int n = (int)s->fresh.size();
+    std::copy(s->fresh.begin(), s->fresh.begin() + std::min(n, capacity), out);
+    return n;
+}
+
+extern "C" int tp_sampler_held(const tp_sampler *s) { return s ? (int)s->held.size() : TP_E_BAD_ARG; }
+
+extern "C" tp_tile *tp_sampler_find(const tp_sampler *s, int producer, int level, int tx, int ty)
+{
+    if (!s || producer < 0 || producer >= (int)s->producers.size() || level < 0 || level > 29 || tx < 0 || ty < 0)
+        return nullptr;
+    auto it = s->index.find(req_key(level, tx, ty));
+    return it == s->index.end() ? nullptr : s->held[it->second].tiles[producer];
 }
 
 extern "C" int tp_sphere_frame(double root_quad_size, int level, int tx, int ty, float *out47)

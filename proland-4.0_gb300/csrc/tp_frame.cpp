@@ -9,6 +9,7 @@
 #include <vector>
 
 #include "tp_internal.h"
+#include "tp_trace.h"
 
 struct tp_frame {
     struct Class {
@@ -400,6 +401,7 @@ extern "C" int tp_frame_add_device(tp_frame *f, tp_storage *elev, tp_storage *re
 
 extern "C" int tp_frame_launch(tp_frame *f, void *stream)
 {
+    tp::TraceScope trace("frame launch", -1);
     if (!f) return tp::fail(TP_E_BAD_ARG, "tp_frame_launch: frame is NULL");
     tp::FrameLaunch F[2];
     int rc = prepare(f, F, stream);
@@ -409,6 +411,7 @@ extern "C" int tp_frame_launch(tp_frame *f, void *stream)
 
 extern "C" int tp_frame_graph_launch(tp_frame *f, void *stream)
 {
+    tp::TraceScope trace("frame graph launch", -1);
     if (!f) return tp::fail(TP_E_BAD_ARG, "tp_frame_graph_launch: frame is NULL");
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     if (!f->graph || f->graph_stream != s) {

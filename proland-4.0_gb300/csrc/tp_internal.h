@@ -160,8 +160,13 @@ struct PlaneXfers {
 // the device; callers serialise their own uses (and synchronise their stream before
 // the buffer is handed out again).  Grows by a free and a new allocation after a
 // synchronisation of `stream`.
-enum ScratchId { kScratchNormals = 0, kScratchNormalFormats = 1, kScratchLayers = 2 };
+enum ScratchId { kScratchNormals = 0, kScratchNormalFormats = 1, kScratchLayers = 2, kScratchSynth = 3 };
 int device_scratch(int id, size_t bytes, void *stream, char **out);
+// Synthetic residual tiles (generator in tp_synth.h): into residual slots on the
+// device, or one tile into host memory (row pitch `pitch` floats); same bits.
+int synthetic_residuals_device(tp_storage *s, uint32_t seed, const int *slots, const int *levels, const int *txs,
+                               const int *tys, const float *sigmas, int n, void *stream);
+void synthetic_residual_host(uint32_t seed, int level, int tx, int ty, float sigma, int W, float *out, int pitch);
 // Multiprocessors of the current device (cached per device).
 int device_sm_count();
 // Runs the x.n plane copies in one launch on `stream`.

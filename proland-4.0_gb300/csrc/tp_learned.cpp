@@ -12,6 +12,7 @@
 #include <vector>
 
 #include "tp_internal.h"
+#include "tp_trace.h"
 #include "tp_learned.h"
 
 using namespace tp::learned;
@@ -317,6 +318,7 @@ extern "C" int tp_learned_set_sigmas(tp_learned *net, const float *sigma_in, con
 extern "C" int tp_learned_forward(tp_learned *net, const float *up_dev, const int *levels, int n, int training,
                                   float *out_dev, void *stream)
 {
+    tp::TraceScope trace("learned forward", tp::kPhLearned);
     if (!net || !up_dev || !levels || n < 1 || n > net->cap) return tp::fail(TP_E_BAD_ARG, "tp_learned_forward: bad arguments");
     int rc = check_levels(levels, n);
     if (rc) return rc;
@@ -333,6 +335,7 @@ extern "C" int tp_learned_forward(tp_learned *net, const float *up_dev, const in
 
 extern "C" int tp_learned_backward(tp_learned *net, const float *target_dev, float *loss, void *stream)
 {
+    tp::TraceScope trace("learned backward", tp::kPhLearned);
     if (!net || !target_dev) return tp::fail(TP_E_BAD_ARG, "tp_learned_backward: bad arguments");
     if (!net->trained_forward || net->nimg < 1)
         return tp::fail(TP_E_BAD_ARG, "tp_learned_backward: needs a forward pass with training = 1 first");
@@ -371,6 +374,7 @@ extern "C" int tp_learned_backward(tp_learned *net, const float *target_dev, flo
 
 extern "C" int tp_learned_adam(tp_learned *net, float lr, void *stream)
 {
+    tp::TraceScope trace("learned adam", tp::kPhLearned);
     if (!net || !(lr > 0.0f)) return tp::fail(TP_E_BAD_ARG, "tp_learned_adam: bad arguments");
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     ++net->step;
@@ -398,6 +402,7 @@ extern "C" int tp_learned_gather(tp_learned *net, const float *up_src, const flo
 extern "C" int tp_learned_predict_residuals(tp_learned *net, tp_storage *elev, const tp_tile_job *jobs, int n,
                                             tp_storage *residuals, void *stream)
 {
+    tp::TraceScope trace("learned residuals", tp::kPhLearned);
     if (!net || !elev || !jobs || !residuals || n < 1 || n > net->cap)
         return tp::fail(TP_E_BAD_ARG, "tp_learned_predict_residuals: bad arguments");
     if (elev->on_device != 1 || elev->channels != 3 || elev->W != net->W || residuals->on_device != 1 ||

@@ -10,6 +10,7 @@
 #include <vector>
 
 #include "tp_internal.h"
+#include "tp_trace.h"
 
 namespace {
 
@@ -424,6 +425,7 @@ int launch_normals(tp_storage *elev, tp_storage *nrm, const int *eslots, const i
 extern "C" int tp_normal_batch(tp_storage *elev, tp_storage *normals, const tp_tile_job *jobs, int n,
                                double root_quad_size, void *stream)
 {
+    tp::TraceScope trace("normal batch", -1);
     if (!elev || !normals || n < 0 || (n > 0 && !jobs)) return tp::fail(TP_E_BAD_ARG, "tp_normal_batch: bad arguments");
     if (elev->on_device != 1 || elev->channels != 3 || normals->on_device != 1 || normals->channels != 2 ||
         normals->W != elev->W - 4)

@@ -528,10 +528,61 @@ class TileProducer:
         return Tile(h.value)
 
 
+class TileSampler:
+    """The TileSamplers of one terrain node (tp_sampler_*) over one or more producers
+    (e.g. an elevation and a normal producer): `update` takes the next frame's
+    quadtree requests (parents first), releases the tiles of quads that disappeared,
+    acquires and produces the new quads' tiles in one scheduler run, and returns the
+    new quads [(level, tx, ty), ...]."""
+
+    def __init__(self, *producers):
+        h = C.c_void_p()
+        arr = (C.c_void_p * len(producers))(*[p.handle for p in producers])
+        check(lib().tp_sampler_create(arr, len(producers), C.byref(h)))
+        self.handle, self.producers = h, producers
+
+    def update(self, requests, stream=None):
+        reqs = np.ascontiguousarray(np.asarray(requests, np.int32).reshape(-1, 3))
+        n = C.c_int()
+        check(lib().tp_sampler_update(self.handle, reqs.ctypes.data_as(C.POINTER(C.c_int32)), reqs.shape[0],
+                                      stream, C.byref(n)))
+        out = np.empty((max(n.value, 1), 3), np.int32)
+        check(lib().tp_sampler_new_tiles(self.handle, out.ctypes.data_as(C.POINTER(C.c_int32)), n.value))
+        return [tuple(int(v) for v in r) for r in out[:n.value]]
+
+    def held(self):
+        return check(lib().tp_sampler_held(self.handle))
+
+    def find(self, level, tx, ty, producer=0):
+        """The held tile (level, tx, ty) of producer number `producer`, or None."""
+        h = lib().tp_sampler_find(self.handle, producer, level, tx, ty)
+        return Tile(h) if h else None
+
+    def close(self):
+        if self.handle:
+            lib().tp_sampler_destroy(self.handle)
+            self.handle = None
+
+
+def trace_set(flags):
+    """Tracing flags (tp_trace_set): bit 0 NVTX ranges, bit 1 host phase timers."""
+    return check(lib().tp_trace_set(int(flags)))
+
+
+def trace_host_times(reset=False):
+    """{phase: (seconds, calls)} of the host phase timers (tp_trace_host_times)."""
+    n = 16
+    secs, calls = (C.c_double * n)(), (C.c_longlong * n)()
+    k = check(lib().tp_trace_host_times(secs, calls, n, int(reset)))
+    return {lib().tp_trace_phase_name(i).decode(): (secs[i], calls[i]) for i in range(k)}
+
+
 class ResidualProducer(TileProducer):
     """ResidualProducer: a .dat pyramid, a host callback or zero residuals."""
 
-    def __init__(self, cache, file="", delta=0, zscale=1.0, source=None, device_decode=False):
+    def __init__(self, cache, file="", delta=0, zscale=1.0, source=None, device_decode=False, synthetic=None):
+        """synthetic: (sigma0, ratio, seed) for synthetic tiles of standard deviation
+        sigma0 * ratio^level made on the device (tp_residual_producer_set_synthetic)."""
         h = C.c_void_p()
         check(lib().tp_residual_producer_create(cache.handle, (file or "").encode(), delta, zscale, C.byref(h)))
         super().__init__(h, cache)
@@ -540,6 +591,9 @@ class ResidualProducer(TileProducer):
             self.set_source(source)
         if device_decode:
             check(lib().tp_residual_producer_set_device_decode(h, 1))
+        if synthetic is not None:
+            sigma0, ratio, seed = synthetic
+            check(lib().tp_residual_producer_set_synthetic(h, float(sigma0), float(ratio), int(seed)))
 
     def tile(self, level, tx, ty):
         """The residual tile as computed on the host (tp_residual_tile)."""

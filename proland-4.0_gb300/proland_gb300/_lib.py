@@ -188,6 +188,16 @@ def lib():
         "tp_dat_decode_device": ([_vp, C.POINTER(_i), C.POINTER(_i), C.POINTER(_i), _i, C.c_float, _vp,
                                   C.POINTER(_i), _vp], _i),
         "tp_residual_producer_set_device_decode": ([_vp, _i], _i),
+        "tp_residual_producer_set_synthetic": ([_vp, C.c_double, C.c_double, C.c_uint], _i),
+        "tp_sampler_create": ([C.POINTER(_vp), _i, C.POINTER(_vp)], _i),
+        "tp_sampler_destroy": ([_vp], _i),
+        "tp_sampler_update": ([_vp, C.POINTER(C.c_int32), _i, _vp, C.POINTER(_i)], _i),
+        "tp_sampler_new_tiles": ([_vp, C.POINTER(C.c_int32), _i], _i),
+        "tp_sampler_held": ([_vp], _i),
+        "tp_sampler_find": ([_vp, _i, _i, _i, _i], _vp),
+        "tp_trace_set": ([_i], _i),
+        "tp_trace_host_times": ([C.POINTER(C.c_double), C.POINTER(C.c_longlong), _i, _i], _i),
+        "tp_trace_phase_name": ([_i], C.c_char_p),
         "tp_inflate_zlib": ([_vp, C.c_size_t, _vp, C.c_size_t, C.POINTER(C.c_size_t)], _i),
         "tp_dem_noise": ([_i, _f32p], _i),
         "tp_cnoise": ([C.c_float, C.c_float], C.c_float),
