@@ -553,6 +553,17 @@ int tp_fbm_heights(int size, int octaves, int base_cells, float amplitude, float
 int tp_preprocess_level(const int16_t *base_dev, int tile_size, int max_level, int level, float scale,
                         const float *parent_approx_dev, float *approx_dev, float *upsampled_dev,
                         float *residual_dev, int16_t *encoded_dev, void *stream);
+/* (upsampled parent, residual) tile pairs at any level of the same procedural fBm,
+ * sampled in double precision on the tiles' own windows (no base grid, no
+ * quantisation): sample (i, j) of tile (level, tx, ty) is the field at
+ * ((i + ts tx - 2), (j + ts ty - 2)) / (ts 2^level); up = the interpolating stencil
+ * of the parent tile's fp32 samples (CPUElevationProducer.cpp:194-245 order), res =
+ * the child's sample in double - up, rounded once; fine = the child's samples (may be
+ * NULL).  Deep levels (below the finest octave's cells, where a base grid would not
+ * fit in memory) have truth this way.  Outputs are [n][ts + 5][ts + 5] device
+ * arrays; levels >= 1. */
+int tp_fbm_pairs(int octaves, int base_cells, float amplitude, uint32_t seed, int tile_size, const int *levels,
+                 const int *txs, const int *tys, int n, float *up_dev, float *res_dev, float *fine_dev, void *stream);
 
 /* ------------------------------------------------------------------------
  * Learned residual predictor (no counterpart in the reference: it stands in for

@@ -109,6 +109,8 @@ def lib():
                                       C.c_int]
         _i16p = C.POINTER(C.c_int16)
         L.or_fbm_heights.argtypes = [C.c_int, C.c_int, C.c_int, C.c_float, C.c_float, C.c_uint32, _i16p]
+        L.or_fbm_pair.argtypes = [C.c_int, C.c_int, C.c_float, C.c_uint32, C.c_int, C.c_int, C.c_int, C.c_int,
+                                  _f32p, _f32p, _f32p]
         L.or_synthetic_residual.argtypes = [C.c_uint32, C.c_int, C.c_int, C.c_int, C.c_float, C.c_int, _f32p]
         L.or_level_tile.argtypes = [_i16p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_float, _f32p]
         L.or_learned_param_count.restype = C.c_int
@@ -514,6 +516,14 @@ def residual_chain_root(dat, delta, zscale=1.0):
 
 
 # ---------------------------------------------------------------- preprocess and learned net
+def fbm_pair(level, tx, ty, seed=1, tile_size=96, octaves=12, base_cells=4, amplitude=4000.0):
+    """(up, res, fine) of one tile of the procedural fBm at any level (tp_fbm_pairs)."""
+    W = tile_size + 5
+    out = [np.empty((W, W), np.float32) for _ in range(3)]
+    lib().or_fbm_pair(octaves, base_cells, amplitude, C.c_uint32(seed), tile_size, level, tx, ty, *[_p(o) for o in out])
+    return tuple(out)
+
+
 def synthetic_residual(seed, level, tx, ty, sigma, W):
     """The product's synthetic residual tile (tp_residual_producer_set_synthetic) for a
     tile of standard deviation `sigma` (a float32 value)."""

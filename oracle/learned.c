@@ -32,6 +32,29 @@ static float lattice(uint32_t x, uint32_t y, uint32_t z)
     return (float)(h >> 8) * (1.0f / 8388608.0f) - 1.0f;
 }
 
+/* The same field in double precision at domain point (u, v), in metres (the
+ * product's windowed sampler for deep levels; each operation rounded alone). */
+double or_fbm_f64(double u, double v, int octaves, int base_cells, double norm, uint32_t seed)
+{
+    double sum = 0.0, amp = 1.0;
+    for (int o = 0; o < octaves; ++o) {
+        const double cells = (double)(base_cells << o);
+        const double gx = u * cells, gy = v * cells;
+        const double fx0 = floor(gx), fy0 = floor(gy);
+        const uint32_t ix = (uint32_t)(long long)fx0, iy = (uint32_t)(long long)fy0, oz = seed * 977u + (uint32_t)o;
+        double fx = gx - fx0, fy = gy - fy0;
+        fx = (fx * fx) * (3.0 - 2.0 * fx);
+        fy = (fy * fy) * (3.0 - 2.0 * fy);
+        const double v00 = lattice(ix, iy, oz), v10 = lattice(ix + 1, iy, oz);
+        const double v01 = lattice(ix, iy + 1, oz), v11 = lattice(ix + 1, iy + 1, oz);
+        const double a0 = v00 + (v10 - v00) * fx;
+        const double a1 = v01 + (v11 - v01) * fx;
+        sum = sum + amp * (a0 + (a1 - a0) * fy);
+        amp *= 0.5;
+    }
+    return sum * norm;
+}
+
 void or_fbm_heights(int size, int octaves, int base_cells, float amplitude, float quantum, uint32_t seed, int16_t *out)
 {
     const float norm = (float)((double)amplitude / (2.0 - ldexp(1.0, 1 - octaves)));
@@ -217,7 +240,9 @@ double or_learned_loss_grad(int W, int n, const float *params, const float *up, 
     for (int l = 0; l < NL - 1; ++l) Zs[l] = (double *)calloc(P * COUT[l], sizeof(double));
     double *Zt = (double *)malloc(sizeof(double) * P * 32);
     double *pred = (double *)malloc(sizeof(double) * P);
-    /* input channels: height (minus the tile mean, over sigma_in), x parity, y parity, 1 */
+    /* input channels: height (minus the tile mean, over sigma_in), x parity, y parity, 1,
+     * the second differences u[x-1] + u[x+1] - 2 u[x] along x and y (0 on the edge
+     * columns / rows) over sigma_out, in float before the bf16 rounding */
     for (int img = 0; img < n; ++img) {
         const float *u = up + img * np;
         double s = 0.0;
@@ -225,12 +250,19 @@ double or_learned_loss_grad(int W, int n, const float *params, const float *up, 
         const int lev = levels[img];
         for (size_t i = 0; i < np; ++i) {
             const int y = (int)(i / W), x = (int)(i % W);
+            const int ex = x > 0 && x < W - 1, ey = y > 0 && y < W - 1;
             double *xi = X[0] + (img * np + i) * 16;
             if (emulate) {
-                const float mean = (float)(s / (double)np), inv = 1.0f / sigma_in[lev];
+                const float mean = (float)(s / (double)np), inv = 1.0f / sigma_in[lev], inv2 = 1.0f / sigma_out[lev];
                 xi[0] = bf16r((u[i] - mean) * inv);
+                const float d2x = ex ? (u[i - 1] + u[i + 1]) - 2.0f * u[i] : 0.0f;
+                const float d2y = ey ? (u[i - W] + u[i + W]) - 2.0f * u[i] : 0.0f;
+                xi[4] = bf16r(d2x * inv2);
+                xi[5] = bf16r(d2y * inv2);
             } else {
                 xi[0] = ((double)u[i] - s / (double)np) / (double)sigma_in[lev];
+                xi[4] = ex ? ((double)u[i - 1] + u[i + 1] - 2.0 * u[i]) / (double)sigma_out[lev] : 0.0;
+                xi[5] = ey ? ((double)u[i - W] + u[i + W] - 2.0 * u[i]) / (double)sigma_out[lev] : 0.0;
             }
             xi[1] = x & 1;
             xi[2] = y & 1;

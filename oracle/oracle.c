@@ -918,3 +918,31 @@ void or_synthetic_residual(uint32_t seed, int level, int tx, int ty, float sigma
             out[i + j * W] = (acc - 6.0f) * sigma;
         }
 }
+
+/* ---------------------------------------------------------------- deep-level pairs
+ * The product's tp_fbm_pairs for one tile: the field (or_fbm_f64) on the parent's
+ * and the child's windows, up = the stencil of the (fp32) parent, res = child - up
+ * formed in double and rounded once. */
+void or_fbm_pair(int octaves, int base_cells, float amplitude, uint32_t seed, int ts, int level, int tx, int ty,
+                 float *up, float *res, float *fine)
+{
+    const int W = ts + 5;
+    const double norm = (double)amplitude / (2.0 - ldexp(1.0, 1 - octaves));
+    const double ps = 1.0 / ((double)ts * (double)(1u << (level - 1))), cs = 1.0 / ((double)ts * (double)(1u << level));
+    float *parent = (float *)malloc(sizeof(float) * W * W);
+    for (int j = 0; j < W; ++j)
+        for (int i = 0; i < W; ++i)
+            parent[i + j * W] = (float)or_fbm_f64((double)(i + ts * (tx / 2) - 2) * ps, (double)(j + ts * (ty / 2) - 2) * ps,
+                                                  octaves, base_cells, norm, seed);
+    const int px = 1 + (tx % 2) * ts / 2, py = 1 + (ty % 2) * ts / 2;
+    for (int j = 0; j < W; ++j)
+        for (int i = 0; i < W; ++i) {
+            const double f = or_fbm_f64((double)(i + ts * tx - 2) * cs, (double)(j + ts * ty - 2) * cs, octaves,
+                                        base_cells, norm, seed);
+            const float z = upsample_sample(parent, W, i, j, px, py);
+            up[i + j * W] = z;
+            res[i + j * W] = (float)(f - (double)z);
+            if (fine) fine[i + j * W] = (float)f;
+        }
+    free(parent);
+}

@@ -131,6 +131,11 @@ void or_normals_full(int W, const float *zm, int zm_pitch, float tile_meters, co
 /* ---- learned.c: device preprocess height field, level tiles, learned net ---- */
 /* the product's synthetic residual tile (sum of twelve 16-bit uniforms - 6) x sigma */
 void or_synthetic_residual(uint32_t seed, int level, int tx, int ty, float sigma, int W, float *out);
+/* the fBm in double precision at (u, v), metres; norm = amplitude / (2 - 2^(1 - octaves)) */
+double or_fbm_f64(double u, double v, int octaves, int base_cells, double norm, uint32_t seed);
+/* one (upsampled parent, residual) pair of the field at any level (tp_fbm_pairs) */
+void or_fbm_pair(int octaves, int base_cells, float amplitude, uint32_t seed, int ts, int level, int tx, int ty,
+                 float *up, float *res, float *fine);
 void or_fbm_heights(int size, int octaves, int base_cells, float amplitude, float quantum, uint32_t seed, int16_t *out);
 void or_level_tile(const int16_t *base, int ts, int max_level, int level, int tx, int ty, float scale, float *out);
 int or_learned_param_count(void);

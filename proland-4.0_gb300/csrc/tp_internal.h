@@ -160,7 +160,7 @@ struct PlaneXfers {
 // the device; callers serialise their own uses (and synchronise their stream before
 // the buffer is handed out again).  Grows by a free and a new allocation after a
 // synchronisation of `stream`.
-enum ScratchId { kScratchNormals = 0, kScratchNormalFormats = 1, kScratchLayers = 2, kScratchSynth = 3 };
+enum ScratchId { kScratchNormals = 0, kScratchNormalFormats = 1, kScratchLayers = 2, kScratchSynth = 3, kScratchPairs = 4 };
 int device_scratch(int id, size_t bytes, void *stream, char **out);
 // Synthetic residual tiles (generator in tp_synth.h): into residual slots on the
 // device, or one tile into host memory (row pitch `pitch` floats); same bits.

@@ -114,7 +114,7 @@ int forward(tp_learned *net, int n, bool training, cudaStream_t s)
     }
     // training keeps the first layer's input image (its weight gradient reads it);
     // inference makes the input channels inside the first convolution
-    if (training) launch_prep(net->up, net->levels, net->sigma_in, net->W, n, net->x0, s);
+    if (training) launch_prep(net->up, net->levels, net->sigma_in, net->sigma_out, net->W, n, net->x0, s);
     else launch_means(net->up, net->W, n, net->mean, s);
     const CUtensorMap *in[kLayers] = {&net->h_x0, &net->h_act[0], &net->h_act[1], &net->h_act[2], &net->h_act[3]};
     for (int l = 0; l < kLayers; ++l) {
@@ -134,6 +134,7 @@ int forward(tp_learned *net, int n, bool training, cudaStream_t s)
             a.up = net->up;
             a.mean = net->mean;
             a.sigma_in = net->sigma_in;
+            a.sigma_out = net->sigma_out;
         }
         int rc = launch_conv(kCin[l], kCout[l], mode, a, in[l], s);
         if (rc) return rc;

@@ -205,9 +205,9 @@ __global__ void __launch_bounds__(kRoleThreads) conv_kernel(const __grid_constan
 
     if (MODE == kFirst && warp == 0) {
         // producer: the input channels of tile i's halo made from the upsampled parent
-        // (the values launch_prep writes: (up - mean) / sigma_in, x and y parity, 1; 0
-        // outside the image), written as bf16 into stage i % kConvStages; channels 8-15
-        // are zero in every stage
+        // (the values launch_prep writes: (up - mean) / sigma_in, x and y parity, 1, the
+        // second differences along x and y over sigma_out; 0 outside the image), written
+        // as bf16 into stage i % kConvStages; channels 8-15 are zero in every stage
         for (int s = 0; s < kConvStages; ++s)
             for (int p = lane; p < kHaloX * kHaloY; p += 32)
                 *reinterpret_cast<uint4 *>(halo + s * STAGE + kGroupStride + p * 16) = make_uint4(0u, 0u, 0u, 0u);
@@ -223,7 +223,7 @@ __global__ void __launch_bounds__(kRoleThreads) conv_kernel(const __grid_constan
             const float *u = a.up + (size_t)img * a.W * a.W;
             // all loads of the tile first (one latency), then the conversions
             constexpr int kPer = (kHaloX * kHaloY + 31) / 32;
-            float val[kPer];
+            float val[kPer], d2x[kPer], d2y[kPer];
             int xs[kPer], ys[kPer];
             const float mean = __ldg(a.mean + img);
             const int lv = __ldg(a.level + img);
@@ -234,10 +234,17 @@ __global__ void __launch_bounds__(kRoleThreads) conv_kernel(const __grid_constan
                 xs[k] = bx * kBlockX + hx - 1;
                 ys[k] = by * kBlockY + hy - 1;
                 const bool in = p < kHaloX * kHaloY && xs[k] >= 0 && ys[k] >= 0 && xs[k] < a.W && ys[k] < a.W;
-                val[k] = in ? __ldg(u + (size_t)ys[k] * a.W + xs[k]) : 0.0f;
+                const float *c = u + (size_t)ys[k] * a.W + xs[k];
+                val[k] = in ? __ldg(c) : 0.0f;
+                const bool ix = in && xs[k] > 0 && xs[k] < a.W - 1, iy = in && ys[k] > 0 && ys[k] < a.W - 1;
+                d2x[k] = ix ? __fadd_rn(__ldg(c - 1), __ldg(c + 1)) : 0.0f;
+                d2y[k] = iy ? __fadd_rn(__ldg(c - a.W), __ldg(c + a.W)) : 0.0f;
+                if (ix) d2x[k] = __fsub_rn(d2x[k], __fmul_rn(2.0f, val[k]));
+                if (iy) d2y[k] = __fsub_rn(d2y[k], __fmul_rn(2.0f, val[k]));
                 if (!in) xs[k] = -1;
             }
-            const float inv = 1.0f / __ldg(a.sigma_in + min(max(lv, 0), kLevels - 1));
+            const int lc = min(max(lv, 0), kLevels - 1);
+            const float inv = 1.0f / __ldg(a.sigma_in + lc), inv2 = 1.0f / __ldg(a.sigma_out + lc);
 #pragma unroll
             for (int k = 0; k < kPer; ++k) {
                 const int p = lane + 32 * k;
@@ -246,6 +253,7 @@ __global__ void __launch_bounds__(kRoleThreads) conv_kernel(const __grid_constan
                 if (xs[k] >= 0) {
                     v.x = pack2((val[k] - mean) * inv, (float)(xs[k] & 1));
                     v.y = pack2((float)(ys[k] & 1), 1.0f);
+                    v.z = pack2(__fmul_rn(d2x[k], inv2), __fmul_rn(d2y[k], inv2));
                 }
                 *reinterpret_cast<uint4 *>(halo + s * STAGE + p * 16) = v;
             }
@@ -616,16 +624,22 @@ __global__ void mean_kernel(const float *up, int W, float *mean)
     if (threadIdx.x == 0) mean[blockIdx.x] = m;
 }
 
-__global__ void prep_kernel(const float *up, const int *level, const float *sigma_in, int W, __nv_bfloat16 *x0)
+__global__ void prep_kernel(const float *up, const int *level, const float *sigma_in, const float *sigma_out, int W,
+                            __nv_bfloat16 *x0)
 {
     const int img = blockIdx.x, n = W * W;
     const float *u = up + (size_t)img * n;
     const float mean = tile_mean(u, n);
-    const float inv = 1.0f / sigma_in[min(max(level[img], 0), kLevels - 1)];
+    const int lc = min(max(level[img], 0), kLevels - 1);
+    const float inv = 1.0f / sigma_in[lc], inv2 = 1.0f / sigma_out[lc];
     const int Wp = W + 2;
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
         const int y = i / W, x = i - y * W;
-        float v[16] = {(u[i] - mean) * inv, (float)(x & 1), (float)(y & 1), 1.0f};
+        // second differences in fp32 (0 on the tile's edge rows / columns)
+        const float d2x = x > 0 && x < W - 1 ? __fsub_rn(__fadd_rn(u[i - 1], u[i + 1]), __fmul_rn(2.0f, u[i])) : 0.0f;
+        const float d2y = y > 0 && y < W - 1 ? __fsub_rn(__fadd_rn(u[i - W], u[i + W]), __fmul_rn(2.0f, u[i])) : 0.0f;
+        float v[16] = {(u[i] - mean) * inv, (float)(x & 1), (float)(y & 1), 1.0f, __fmul_rn(d2x, inv2),
+                       __fmul_rn(d2y, inv2)};
         store_bf16<16>(x0, img, (size_t)Wp * Wp, (size_t)(y + 1) * Wp + x + 1, v);
     }
 }
@@ -744,10 +758,11 @@ void launch_pack(const float *w, int cin, int cout, uint8_t *fwd, uint8_t *bwd, 
     pack_kernel<<<blocks_for(n, 256), 256, 0, s>>>(w, cin, cout, fwd, bwd);
 }
 
-void launch_prep(const float *up, const int *level, const float *sigma_in, int W, int nimg, __nv_bfloat16 *x0,
+void launch_prep(const float *up, const int *level, const float *sigma_in, const float *sigma_out, int W, int nimg,
+                 __nv_bfloat16 *x0,
                  cudaStream_t s)
 {
-    if (nimg > 0) prep_kernel<<<nimg, 256, 0, s>>>(up, level, sigma_in, W, x0);
+    if (nimg > 0) prep_kernel<<<nimg, 256, 0, s>>>(up, level, sigma_in, sigma_out, W, x0);
 }
 
 void launch_means(const float *up, int W, int nimg, float *mean, cudaStream_t s)

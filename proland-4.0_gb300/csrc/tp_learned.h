@@ -13,10 +13,13 @@ namespace tp {
 namespace learned {
 
 constexpr int kLayers = 5;
-constexpr int kCin[kLayers] = {16, 32, 32, 32, 32};    // layer 0 input: 4 used channels, padded to 16
+constexpr int kCin[kLayers] = {16, 32, 32, 32, 32};    // layer 0 input: 6 used channels, padded to 16
 constexpr int kCout[kLayers] = {32, 32, 32, 32, 16};   // last layer: 1 used channel, padded to 16
 constexpr int kLevels = 24;                            // rows of the level embedding / sigma tables
-constexpr int kInputChannels = 4;                      // height, x parity, y parity, ones
+// height, x parity, y parity, ones, and the second differences of the upsampled
+// tile along x and y over the level's output sigma (computed in fp32 before the bf16
+// rounding: they keep the curvature that a bf16 height loses at deep levels)
+constexpr int kInputChannels = 6;
 
 // Pixel blocks of the convolutions: 8 columns x 16 rows = one 128-row MMA tile.
 constexpr int kBlockX = 8, kBlockY = 16;
@@ -39,6 +42,7 @@ struct ConvLaunch {
     const float *up;             // [nimg][W][W]
     const float *mean;           // [nimg] tile means
     const float *sigma_in;       // [kLevels]
+    const float *sigma_out;      // [kLevels] (scale of the second-difference channels)
 };
 
 // Weight gradient of one layer over a batch: dW[co][tap][ci] += sum_p dZ[p][co] X[p + tap][ci].
@@ -60,8 +64,8 @@ int encode_act_map(void *base, int W, int channels, int nimg, int box_x, int box
 
 // small kernels
 void launch_pack(const float *w, int cin, int cout, uint8_t *fwd, uint8_t *bwd, cudaStream_t s);
-void launch_prep(const float *up, const int *level, const float *sigma_in, int W, int nimg, __nv_bfloat16 *x0,
-                 cudaStream_t s);
+void launch_prep(const float *up, const int *level, const float *sigma_in, const float *sigma_out, int W, int nimg,
+                 __nv_bfloat16 *x0, cudaStream_t s);
 // Per-tile means of the upsampled parents (the same sums as launch_prep's).
 void launch_means(const float *up, int W, int nimg, float *mean, cudaStream_t s);
 void launch_loss(const float *pred, const float *target, const int *level, const float *sigma_out, int W, int nimg,

@@ -17,6 +17,7 @@
 #include <stdint.h>
 
 #include <cmath>
+#include <vector>
 
 #include "tp_internal.h"
 #include "tp_stencil.h"
@@ -90,6 +91,106 @@ __global__ void level_kernel(const int16_t *base, int base_size, int ts, int max
 }
 
 }  // namespace
+
+namespace {
+
+// The same procedural fBm as fbm_kernel, evaluated in double precision at domain
+// point (u, v) and returned in metres (no quantisation): deep levels sample it far
+// below the finest octave's cells, where single-precision coordinates would add
+// noise larger than the residuals.
+__device__ double fbm_f64(double u, double v, int octaves, int base_cells, double norm, uint32_t seed)
+{
+    double sum = 0.0, amp = 1.0;
+    for (int o = 0; o < octaves; ++o) {
+        const double cells = (double)(base_cells << o);
+        const double gx = __dmul_rn(u, cells), gy = __dmul_rn(v, cells);
+        const double fx0 = floor(gx), fy0 = floor(gy);
+        const uint32_t ix = (uint32_t)(long long)fx0, iy = (uint32_t)(long long)fy0, oz = seed * 977u + (uint32_t)o;
+        double fx = __dsub_rn(gx, fx0), fy = __dsub_rn(gy, fy0);
+        fx = __dmul_rn(__dmul_rn(fx, fx), __dsub_rn(3.0, __dmul_rn(2.0, fx)));
+        fy = __dmul_rn(__dmul_rn(fy, fy), __dsub_rn(3.0, __dmul_rn(2.0, fy)));
+        const double v00 = lattice(ix, iy, oz), v10 = lattice(ix + 1, iy, oz);
+        const double v01 = lattice(ix, iy + 1, oz), v11 = lattice(ix + 1, iy + 1, oz);
+        const double a0 = __dadd_rn(v00, __dmul_rn(__dsub_rn(v10, v00), fx));
+        const double a1 = __dadd_rn(v01, __dmul_rn(__dsub_rn(v11, v01), fx));
+        sum = __dadd_rn(sum, __dmul_rn(amp, __dadd_rn(a0, __dmul_rn(__dsub_rn(a1, a0), fy))));
+        amp *= 0.5;
+    }
+    return __dmul_rn(sum, norm);
+}
+
+struct PairTile {
+    int level, tx, ty;
+};
+
+// One CTA per pair: the parent tile (level - 1) of the field into shared memory (fp32,
+// as a produced parent tile is), then the child tile: up = stencil of the parent
+// (CPUElevationProducer order, fp32), res = the field's child sample (double) - up,
+// rounded once to fp32: at deep levels the residual is far below the fp32 spacing of
+// km-scale heights, so it is formed before any rounding of the child sample.
+// Sample (i, j) of tile (level, tx, ty) is the field at
+// ((i + ts tx - 2), (j + ts ty - 2)) / (ts 2^level).
+__global__ void __launch_bounds__(256) pair_kernel(const PairTile *tiles, int ts, int octaves, int base_cells,
+                                                   double norm, uint32_t seed, float *up, float *res, float *fine)
+{
+    extern __shared__ float parent[];
+    const PairTile T = tiles[blockIdx.x];
+    const int W = ts + 5;
+    const int ptx = T.tx / 2, pty = T.ty / 2;
+    const double ps = 1.0 / ((double)ts * (double)(1u << (T.level - 1))), cs = 1.0 / ((double)ts * (double)(1u << T.level));
+    for (int p = threadIdx.x; p < W * W; p += blockDim.x) {
+        const int j = p / W, i = p - j * W;
+        parent[p] = (float)fbm_f64(__dmul_rn((double)(i + ts * ptx - 2), ps), __dmul_rn((double)(j + ts * pty - 2), ps),
+                                   octaves, base_cells, norm, seed);
+    }
+    __syncthreads();
+    const int px = 1 + (T.tx % 2) * ts / 2, py = 1 + (T.ty % 2) * ts / 2;
+    const size_t o0 = (size_t)blockIdx.x * W * W;
+    for (int p = threadIdx.x; p < W * W; p += blockDim.x) {
+        const int j = p / W, i = p - j * W;
+        const double f = fbm_f64(__dmul_rn((double)(i + ts * T.tx - 2), cs), __dmul_rn((double)(j + ts * T.ty - 2), cs),
+                                 octaves, base_cells, norm, seed);
+        const float z = tp::upsample_cpu_order(parent, W, i, j, px, py);
+        up[o0 + p] = z;
+        res[o0 + p] = (float)__dsub_rn(f, (double)z);  // the residual in double, then rounded once
+        if (fine) fine[o0 + p] = (float)f;
+    }
+}
+
+}  // namespace
+
+extern "C" int tp_fbm_pairs(int octaves, int base_cells, float amplitude, uint32_t seed, int tile_size, const int *levels,
+                            const int *txs, const int *tys, int n, float *up_dev, float *res_dev, float *fine_dev,
+                            void *stream)
+{
+    if (octaves < 1 || octaves > 20 || base_cells < 1 || ((long long)base_cells << (octaves - 1)) > (1 << 24) ||
+        tile_size < 8 || tile_size % 2 != 0 || tile_size > 252 || n < 0 || (n > 0 && (!levels || !txs || !tys)) ||
+        (n > 0 && (!up_dev || !res_dev)))
+        return tp::fail(TP_E_BAD_ARG, "tp_fbm_pairs: bad arguments");
+    if (n == 0) return TP_OK;
+    std::vector<PairTile> h((size_t)n);
+    for (int k = 0; k < n; ++k) {
+        if (levels[k] < 1 || levels[k] > 24 || txs[k] < 0 || tys[k] < 0 || (txs[k] >> levels[k]) != 0 ||
+            (tys[k] >> levels[k]) != 0)
+            return tp::fail(TP_E_BAD_ARG, "tp_fbm_pairs: bad tile");
+        h[k] = PairTile{levels[k], txs[k], tys[k]};
+    }
+    char *dbuf = nullptr;
+    int rc = tp::device_scratch(tp::kScratchPairs, sizeof(PairTile) * (size_t)n, stream, &dbuf);
+    if (rc) return rc;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    cudaError_t e = cudaMemcpyAsync(dbuf, h.data(), sizeof(PairTile) * (size_t)n, cudaMemcpyHostToDevice, s);
+    if (e != cudaSuccess) return tp::cuda_fail("tp_fbm_pairs: tile copy", e);
+    const int W = tile_size + 5;
+    const size_t smem = sizeof(float) * (size_t)W * W;
+    e = cudaFuncSetAttribute(pair_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return tp::cuda_fail("tp_fbm_pairs: shared memory", e);
+    const double norm = (double)amplitude / (2.0 - std::ldexp(1.0, 1 - octaves));
+    pair_kernel<<<n, 256, smem, s>>>(reinterpret_cast<const PairTile *>(dbuf), tile_size, octaves, base_cells, norm, seed,
+                                     up_dev, res_dev, fine_dev);
+    e = cudaGetLastError();
+    return e == cudaSuccess ? TP_OK : tp::cuda_fail("tp_fbm_pairs", e);
+}
 
 extern "C" int tp_fbm_heights(int size, int octaves, int base_cells, float amplitude, float quantum, uint32_t seed,
                               int16_t *out_dev, void *stream)

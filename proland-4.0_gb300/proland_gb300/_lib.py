@@ -204,6 +204,8 @@ def lib():
         "tp_noise_select": ([_i, _i, _i, _i, C.POINTER(_i), C.POINTER(_i)], _i),
         "tp_fbm_heights": ([_i, _i, _i, C.c_float, C.c_float, C.c_uint32, _vp, _vp], _i),
         "tp_preprocess_level": ([_vp, _i, _i, _i, C.c_float, _vp, _vp, _vp, _vp, _vp, _vp], _i),
+        "tp_fbm_pairs": ([_i, _i, C.c_float, C.c_uint32, _i, C.POINTER(_i), C.POINTER(_i), C.POINTER(_i), _i, _vp, _vp,
+                          _vp, _vp], _i),
         "tp_learned_create": ([_i, _i, C.POINTER(_vp)], _i),
         "tp_learned_destroy": ([_vp], _i),
         "tp_learned_param_count": ([_vp], _i),

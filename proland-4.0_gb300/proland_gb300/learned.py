@@ -82,6 +82,44 @@ def build_pyramid(max_level, tile_size=96, octaves=12, base_cells=4, amplitude=4
             "tile": np.concatenate(tiles), "quantum": quantum, "tile_size": tile_size}
 
 
+def deep_pairs(levels, per_level, seed=1, tile_seed=0, tile_size=96, octaves=12, base_cells=4, amplitude=4000.0):
+    """(upsampled parent, residual) pairs at any levels of the same procedural fBm
+    (tp_fbm_pairs: the field sampled in double precision on each tile's window, the
+    residual formed before rounding): `per_level` tiles per level at random interior
+    positions (drawn with `tile_seed`), as a dict like build_pyramid's."""
+    rng = np.random.default_rng(tile_seed)
+    lv, txs, tys = [], [], []
+    for l in levels:
+        m = 1 << int(l)
+        lo, hi = (1, m - 1) if m > 2 else (0, m)
+        lv += [int(l)] * per_level
+        txs += [int(v) for v in rng.integers(lo, hi, per_level)]
+        tys += [int(v) for v in rng.integers(lo, hi, per_level)]
+    n, W = len(lv), tile_size + 5
+    up = torch.empty((n, W, W), dtype=torch.float32, device="cuda")
+    res = torch.empty_like(up)
+    arr = lambda v: (C.c_int * n)(*v)  # noqa: E731
+    check(lib().tp_fbm_pairs(octaves, base_cells, amplitude, seed, tile_size, arr(lv), arr(txs), arr(tys), n, _ptr(up),
+                             _ptr(res), None, _stream()))
+    return {"up": up, "res": res, "level": np.array(lv, np.int32), "tile": np.stack([lv, txs, tys], 1),
+            "tile_size": tile_size}
+
+
+def merge(*datas):
+    """One training set of several pair sets (build_pyramid / deep_pairs dicts)."""
+    return {"up": torch.cat([d["up"] for d in datas]), "res": torch.cat([d["res"] for d in datas]),
+            "level": np.concatenate([d["level"] for d in datas]), "tile": np.concatenate([d["tile"] for d in datas]),
+            "tile_size": datas[0]["tile_size"]}
+
+
+def select_levels(data, levels):
+    """The pairs of `data` at the given levels."""
+    idx = np.nonzero(np.isin(data["level"], list(levels)))[0]
+    sel = torch.from_numpy(idx).cuda()
+    return {"up": data["up"].index_select(0, sel), "res": data["res"].index_select(0, sel),
+            "level": data["level"][idx], "tile": data["tile"][idx], "tile_size": data["tile_size"]}
+
+
 def level_sigmas(data, nlevels=24, extrapolate=0.5):
     """Per-level input sigma (RMS of the mean-removed upsampled tile) and output sigma
     (RMS of the residual); levels without data continue the last level by the
@@ -217,7 +255,9 @@ def train(net, data, steps, batch=256, lr=3e-4, seed=0, log_every=0, lr_final=No
 def evaluate(net, data, sigma_out, batch=None):
     """Per level: RMS and max height error of the learned residuals, of the plain
     method without residual (error = the residual itself), and the RMS of the
-    normal-angle error of both (finite differences over the interior)."""
+    normal-angle error of both (finite differences over the interior).  `sigma` is
+    the RMS of the residuals evaluated (the plain method's RMS error), and
+    `rms_over_sigma` the learned error in that unit."""
     lv = data["level"]
     batch = min(batch or net.max_batch, net.max_batch)
     out = {}
@@ -243,7 +283,8 @@ def evaluate(net, data, sigma_out, batch=None):
             count += res.numel()
         ni = count * ((net.W - 2) / net.W) ** 2
         out[int(l)] = {"rms_learned": (se_l / count) ** 0.5, "rms_plain": (se_p / count) ** 0.5,
-                       "max_learned": mx_l, "max_plain": mx_p, "sigma": float(sigma_out[l]),
+                       "max_learned": mx_l, "max_plain": mx_p, "sigma": (se_p / count) ** 0.5,
+                       "rms_over_sigma": (se_l / max(se_p, 1e-30)) ** 0.5, "tiles": int(len(idx)),
                        "angle_rms_learned": (ang_l / ni) ** 0.5, "angle_rms_plain": (ang_p / ni) ** 0.5}
     return out
 
