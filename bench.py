@@ -41,9 +41,20 @@ ROOT_QUAD = 100000.0          # meters: terrainNode size 50000 -> root quad 2 * 
 BYTES_PER_TILE = {101: 260960, 197: 1000544}   # algorithmic bytes (parent window, residual, elevation, normals)
 FALLBACK_HBM_GBS = 6800.0
 E2E_CHUNK = {101: 512, 197: 128}   # tiles per chunk of the host-buffer pipeline (swept: 64-512 / 16-128)
-# ncu dram__bytes_read + dram__bytes_write of the two launches of one step (101-wide and
-# 197-wide classes) of the default 4096-request frame, from a one-pass launch list
-TRAFFIC_BYTES_PER_STEP = (208.2 + 573.8 + 240.1 + 741.6) * 1e6
+TRAFFIC_PROFILE = os.path.join(ROOT, "profiles", "frame_kernel_traffic.txt")
+
+
+def traffic_per_tile():
+    """DRAM bytes (read + write) per tile of each width, as measured by the ncu capture
+    summarised in profiles/frame_kernel_traffic.txt (its `per_tile` line), or None."""
+    try:
+        with open(TRAFFIC_PROFILE) as f:
+            for line in f:
+                if line.startswith("per_tile"):
+                    return {int(k[1:]): float(v) for k, v in (t.split("=") for t in line.split()[1:])}
+    except (OSError, ValueError):
+        pass
+    return None
 
 
 def hbm_peak():
@@ -988,6 +999,9 @@ def main():
     ap.add_argument("--no-layers", action="store_true", help="skip the elevation layer pass")
     ap.add_argument("--no-quadtree", action="store_true", help="skip the dependency-ordered quadtree frame")
     ap.add_argument("--no-streaming", action="store_true", help="skip the view-driven streaming frames")
+    ap.add_argument("--frame-only", action="store_true",
+                    help="the frame's device-resident launches alone (warm-up + steps), for profiling: prints "
+                         "ms per step and the tiles of each width")
     ap.add_argument("--streaming-only", action="store_true",
                     help="run the view-driven streaming frames alone and print their object")
     ap.add_argument("--quadtree-only", action="store_true",
@@ -1054,6 +1068,22 @@ def main():
     if not args.no_autotune:
         frame.autotune(sh, repeats=5)
     tuned = {"W%d" % fc.W: frame.config(i) for i, fc in enumerate(classes)}
+    if args.frame_only:
+        with torch.cuda.stream(stream):
+            for _ in range(warmup):
+                frame.graph_launch(sh)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(args.steps):
+            frame.graph_launch(sh)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        tp.stream_check(sh)
+        print(json.dumps({"frame_only": {"ms_per_step": e0.elapsed_time(e1) / args.steps, "warmup": warmup,
+                                         "steps": args.steps, "tiles": {"W%d" % fc.W: fc.n for fc in classes},
+                                         "shapes": tuned}}))
+        return
 
     def step(events=None):
         if events is not None:
@@ -1150,6 +1180,21 @@ def main():
     for st in e2e_streams:
         tp.stream_check(C.c_void_p(st.cuda_stream))
     e2e_check = check_host_outputs(classes) if pipes else None
+    # the same frame returning zf and the normals only (zc, zm left on the device: the
+    # reference's CPU producer fills zf only, and zm = max(zf, 0) is rebuilt on the host)
+    e2e_min_ms = []
+    for s in range(args.e2e_steps + 1 if args.e2e_steps > 0 else 0):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for fc, pipe, st in zip(classes, pipes, e2e_streams):
+            pipe.run(params, fc.jobs, fc.h_parent_zf, None, fc.h_residual, fc.h_zf, None, None, fc.h_nx, fc.h_ny,
+                     C.c_void_p(st.cuda_stream))
+        for st in e2e_streams:
+            st.synchronize()
+        if s >= 1:
+            e2e_min_ms.append(1000.0 * (time.perf_counter() - t0))
+    for st in e2e_streams:
+        tp.stream_check(C.c_void_p(st.cuda_stream))
     for pipe in pipes:
         pipe.close()
     e2e_step = float(np.mean(e2e_ms)) if e2e_ms else float("nan")
@@ -1163,9 +1208,10 @@ def main():
     peak, peak_src = hbm_peak()
     alg = {fc.W: fc.n * BYTES_PER_TILE[fc.W] for fc in classes}
     achieved = sum(alg.values()) / (kernel_ms / 1000.0) / 1e9
-    # DRAM bytes of one step's launches (read + write) from an ncu launch list, measured
-    # for the default 4096-request frame only
-    traffic = TRAFFIC_BYTES_PER_STEP if (args.requests == 4096 and args.seed == 2024) else None
+    # DRAM bytes of one step's launches (read + write): the per-tile traffic of a small
+    # capture of the same kernel (profiles/frame_kernel_traffic.txt) times this frame's tiles
+    pt = traffic_per_tile()
+    traffic = sum(pt[fc.W] * fc.n for fc in classes) if pt and all(fc.W in pt for fc in classes) else None
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
@@ -1173,6 +1219,8 @@ def main():
         "config": frame_config(classes, world),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": traffic, "peak_source": peak_src,
+                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum per tile of a 1024-request "
+                                       "capture (profiles/frame_kernel_traffic.txt), times this frame's tiles",
                      "kernel": "frame_kernel (one persistent launch per tile width, the two on forked "
                                "streams of a CUDA graph)",
                      "kernel_ms": kernel_ms, "units_per_launch": frame.units(), "per_width": per_width,
@@ -1184,7 +1232,14 @@ def main():
                 "d2h_bytes_per_step": sum(fc.d2h_bytes for fc in classes),
                 "path": "tp_elevation_batch_host per tile width (chunks of %s tiles, copies overlapping launches)"
                         % "/".join(str(E2E_CHUNK[fc.W]) for fc in classes),
-                "identical_to_device_run": e2e_check},
+                "identical_to_device_run": e2e_check,
+                "planes": "zf, zc, zm, nx, ny",
+                "zf_and_normals_only": {
+                    "value": (world * tiles / (float(np.mean(e2e_min_ms)) / 1000.0)) if e2e_min_ms else None,
+                    "unit": UNIT, "ms_per_step": float(np.mean(e2e_min_ms)) if e2e_min_ms else None,
+                    "h2d_bytes_per_step": sum(fc.h2d_bytes for fc in classes),
+                    "d2h_bytes_per_step": sum(fc.n * (fc.W * fc.W + 2 * (fc.W - 4) ** 2) * 4 for fc in classes),
+                    "planes": "zf, nx, ny (zc, zm not copied back)"}},
         "gpu_launches": args.steps * len(classes),
         "clocks": clk,
         "max_err_vs_fp64": fp64_errors(tp, classes),

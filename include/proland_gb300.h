@@ -176,7 +176,9 @@ typedef struct {
                                 (max(zf, 0), or zf under no_clamp), as the parent's
                                 own production wrote it */
     const float *residual;   /* [n][W][W] residual tiles; NULL when no job has one */
-    float *zf, *zc, *zm;     /* [n][W][W] outputs */
+    float *zf, *zc, *zm;     /* [n][W][W] outputs; zc and zm may be NULL (not copied back:
+                                CPUElevationProducer::doCreateTile, CPUElevationProducer.cpp:240-243,
+                                fills zf only, and zm = max(zf, 0), or zf under no_clamp) */
     float *nx, *ny;          /* [n][W-4][W-4] normal outputs (format 2); NULL: none */
 } tp_host_tiles;
 /* Produces n independent jobs (parent_job must be -1) from host tiles into host
@@ -584,6 +586,12 @@ int tp_learned_get_params(tp_learned *net, float *host, int count);
 int tp_learned_set_params(tp_learned *net, const float *host, int count);
 int tp_learned_get_grads(tp_learned *net, float *host, int count);
 int tp_learned_set_sigmas(tp_learned *net, const float *sigma_in, const float *sigma_out, int nlevels);
+/* Checkpoints (training resumed where it stopped): Adam's first and second moments
+ * (param_count floats each) and its step count, and the per-level sigmas (up to 24
+ * levels).  With tp_learned_get_params / set_params they are the whole training state. */
+int tp_learned_get_state(tp_learned *net, float *m, float *v, int count, int *step);
+int tp_learned_set_state(tp_learned *net, const float *m, const float *v, int count, int step);
+int tp_learned_get_sigmas(tp_learned *net, float *sigma_in, float *sigma_out, int nlevels);
 /* Predicted residuals (metres) into out_dev (may be NULL); training = 1 keeps
  * what tp_learned_backward needs. */
 int tp_learned_forward(tp_learned *net, const float *up_dev, const int *levels, int n, int training,

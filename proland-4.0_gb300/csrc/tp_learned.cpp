@@ -305,6 +305,36 @@ extern "C" int tp_learned_get_grads(tp_learned *net, float *host, int count)
     return e == cudaSuccess ? TP_OK : tp::cuda_fail("tp_learned_get_grads", e);
 }
 
+extern "C" int tp_learned_get_state(tp_learned *net, float *m, float *v, int count, int *step)
+{
+    if (!net || !m || !v || !step || count != net->nparams) return tp::fail(TP_E_BAD_ARG, "tp_learned_get_state: bad arguments");
+    cudaError_t e = cudaMemcpy(m, net->m, sizeof(float) * count, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(v, net->v, sizeof(float) * count, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return tp::cuda_fail("tp_learned_get_state", e);
+    *step = net->step;
+    return TP_OK;
+}
+
+extern "C" int tp_learned_set_state(tp_learned *net, const float *m, const float *v, int count, int step)
+{
+    if (!net || !m || !v || count != net->nparams || step < 0)
+        return tp::fail(TP_E_BAD_ARG, "tp_learned_set_state: bad arguments");
+    cudaError_t e = cudaMemcpy(net->m, m, sizeof(float) * count, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(net->v, v, sizeof(float) * count, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return tp::cuda_fail("tp_learned_set_state", e);
+    net->step = step;
+    return TP_OK;
+}
+
+extern "C" int tp_learned_get_sigmas(tp_learned *net, float *sigma_in, float *sigma_out, int nlevels)
+{
+    if (!net || !sigma_in || !sigma_out || nlevels < 1 || nlevels > kLevels)
+        return tp::fail(TP_E_BAD_ARG, "tp_learned_get_sigmas: bad arguments");
+    cudaError_t e = cudaMemcpy(sigma_in, net->sigma_in, sizeof(float) * nlevels, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(sigma_out, net->sigma_out, sizeof(float) * nlevels, cudaMemcpyDeviceToHost);
+    return e == cudaSuccess ? TP_OK : tp::cuda_fail("tp_learned_get_sigmas", e);
+}
+
 extern "C" int tp_learned_set_sigmas(tp_learned *net, const float *sigma_in, const float *sigma_out, int nlevels)
 {
     if (!net || !sigma_in || !sigma_out || nlevels < 1 || nlevels > kLevels)

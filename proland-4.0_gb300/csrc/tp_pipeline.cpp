@@ -177,7 +177,9 @@ int run_chunk(tp_pipeline *p, ChunkBuf &c, const tp_elev_params *params, const t
     if ((rc = tp_frame_launch(c.frame, p->comp))) return rc;
     if ((rc = wait(p->comp, c.out_free))) return rc;
     tp::PlaneXfers out{};
-    for (int ch = 0; ch < 3; ++ch) out.p[out.n++] = slot_xfer(c.out_stage + ch * tile * C, c.elev, 0, ch, m, false);
+    float *outs[3] = {io->zf, io->zc, io->zm};  // zc and zm may be left out (NULL)
+    for (int ch = 0; ch < 3; ++ch)
+        if (outs[ch]) out.p[out.n++] = slot_xfer(c.out_stage + ch * tile * C, c.elev, 0, ch, m, false);
     float *nstage = c.out_stage + 3 * tile * C;
     if (normals)
         for (int ch = 0; ch < 2; ++ch) out.p[out.n++] = slot_xfer(nstage + ch * ntile * C, c.nrm, 0, ch, m, false);
@@ -185,10 +187,9 @@ int run_chunk(tp_pipeline *p, ChunkBuf &c, const tp_elev_params *params, const t
     if ((rc = record(c.out_ready, p->comp))) return rc;
     // downloads
     if ((rc = wait(p->down, c.out_ready))) return rc;
-    float *outs[3] = {io->zf, io->zc, io->zm};
     for (int ch = 0; ch < 3; ++ch)
-        if ((rc = copy(outs[ch] + off * tile, c.out_stage + ch * tile * C, sizeof(float) * tile * m,
-                       cudaMemcpyDeviceToHost, p->down)))
+        if (outs[ch] && (rc = copy(outs[ch] + off * tile, c.out_stage + ch * tile * C, sizeof(float) * tile * m,
+                                   cudaMemcpyDeviceToHost, p->down)))
             return rc;
     if (normals) {
         float *nouts[2] = {io->nx, io->ny};
@@ -259,8 +260,8 @@ extern "C" int tp_elevation_batch_host(tp_pipeline *p, const tp_elev_params *par
     if (!p || !params || !io || n < 0 || (n > 0 && !jobs))
         return tp::fail(TP_E_BAD_ARG, "tp_elevation_batch_host: bad arguments");
     if (n == 0) return TP_OK;
-    if (!io->zf || !io->zc || !io->zm || (!io->nx) != (!io->ny))
-        return tp::fail(TP_E_BAD_ARG, "tp_elevation_batch_host: zf, zc, zm outputs (and nx with ny) are required");
+    if (!io->zf || (!io->nx) != (!io->ny))
+        return tp::fail(TP_E_BAD_ARG, "tp_elevation_batch_host: the zf output (and nx with ny) is required");
     if (io->nx && params->normal_format != 2)
         return tp::fail(TP_E_BAD_ARG, "tp_elevation_batch_host: normals are produced in format 2 only");
     bool any_residual = false, any_parent = false;

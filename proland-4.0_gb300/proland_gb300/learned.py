@@ -16,6 +16,8 @@ Device buffers are torch CUDA tensors (plumbing); every computation runs in the
 library's kernels.
 """
 import ctypes as C
+import json
+import os
 
 import numpy as np
 
@@ -182,6 +184,39 @@ class LearnedPredictor:
         p = np.ascontiguousarray(p, np.float32)
         check(lib().tp_learned_set_params(self.handle, p.ctypes.data_as(_f32p), p.size))
 
+    CHECKPOINT_FORMAT = "proland_gb300.learned/1"
+
+    def save(self, path, **extra):
+        """Writes the whole training state -- parameters, Adam's moments and step count,
+        the per-level sigmas -- and any `extra` arrays to the .npz file `path`
+        (through a temporary file, so that a crash leaves the previous checkpoint)."""
+        n = self.param_count
+        m, v, step = np.empty(n, np.float32), np.empty(n, np.float32), C.c_int()
+        check(lib().tp_learned_get_state(self.handle, m.ctypes.data_as(_f32p), v.ctypes.data_as(_f32p), n,
+                                         C.byref(step)))
+        si, so = np.empty(24, np.float32), np.empty(24, np.float32)
+        check(lib().tp_learned_get_sigmas(self.handle, si.ctypes.data_as(_f32p), so.ctypes.data_as(_f32p), 24))
+        tmp = path + ".tmp.npz"
+        np.savez(tmp, format=np.array(self.CHECKPOINT_FORMAT), params=self.get_params(), adam_m=m, adam_v=v,
+                 adam_step=np.array(step.value), sigma_in=si, sigma_out=so, **extra)
+        os.replace(tmp, path)
+
+    def load_state(self, path):
+        """Restores a state written by `save`; returns its extra entries."""
+        with np.load(path, allow_pickle=False) as f:
+            d = {k: f[k] for k in f.files}
+        if str(d.get("format")) != self.CHECKPOINT_FORMAT:
+            raise ValueError("%s: not a learned-predictor checkpoint" % path)
+        if d["params"].size != self.param_count:
+            raise ValueError("%s: %d parameters, the net has %d" % (path, d["params"].size, self.param_count))
+        self.set_params(d["params"])
+        m, v = np.ascontiguousarray(d["adam_m"], np.float32), np.ascontiguousarray(d["adam_v"], np.float32)
+        check(lib().tp_learned_set_state(self.handle, m.ctypes.data_as(_f32p), v.ctypes.data_as(_f32p), m.size,
+                                         int(d["adam_step"])))
+        self.set_sigmas(d["sigma_in"], d["sigma_out"])
+        return {k: d[k] for k in d if k not in ("format", "params", "adam_m", "adam_v", "adam_step", "sigma_in",
+                                                "sigma_out")}
+
     def get_grads(self):
         out = np.empty(self.param_count, np.float32)
         check(lib().tp_learned_get_grads(self.handle, out.ctypes.data_as(_f32p), out.size))
@@ -223,19 +258,28 @@ class LearnedPredictor:
         check(lib().tp_learned_predict_residuals(self.handle, elev.handle, arr, len(jobs), residuals.handle, stream))
 
 
-def train(net, data, steps, batch=256, lr=3e-4, seed=0, log_every=0, lr_final=None, balance_levels=True):
+def train(net, data, steps, batch=256, lr=3e-4, seed=0, log_every=0, lr_final=None, balance_levels=True,
+          checkpoint=None, checkpoint_every=0, resume_from=None):
     """Adam on random (tile, symmetry) pairs of `data`; returns the loss history.
     With lr_final the rate decays geometrically to it over the run; with
     balance_levels each sample first draws a level uniformly (a pyramid holds 4x
-    more tiles per level), then a tile of that level."""
+    more tiles per level), then a tile of that level.  Every `checkpoint_every`
+    steps the training state (net.save, plus the step, the sampler's random state
+    and the losses so far) goes to `checkpoint` (a path, formatted with step=...);
+    `resume_from` continues a run from such a file with the same batches and rates."""
     rng = np.random.default_rng(seed)
     N = data["up"].shape[0]
     W = net.W
     by_level = [np.nonzero(data["level"] == l)[0] for l in np.unique(data["level"])]
     up_b = torch.empty((batch, W, W), dtype=torch.float32, device="cuda")
     res_b = torch.empty_like(up_b)
-    losses = []
-    for s in range(steps):
+    losses, start = [], 0
+    if resume_from is not None:
+        extra = net.load_state(resume_from)
+        start = int(extra["train_step"])
+        rng.bit_generator.state = json.loads(str(extra["rng_state"]))
+        losses = [float(x) for x in extra["losses"]]
+    for s in range(start, steps):
         if balance_levels:
             pick = rng.integers(0, len(by_level), batch)
             src = np.array([by_level[k][rng.integers(0, len(by_level[k]))] for k in pick])
@@ -249,6 +293,9 @@ def train(net, data, steps, batch=256, lr=3e-4, seed=0, log_every=0, lr_final=No
         net.adam(rate)
         if log_every and (s + 1) % log_every == 0:
             print("step %d loss %.4f" % (s + 1, float(np.mean(losses[-log_every:]))))
+        if checkpoint and checkpoint_every and (s + 1) % checkpoint_every == 0:
+            net.save(checkpoint.format(step=s + 1), train_step=np.array(s + 1),
+                     rng_state=np.array(json.dumps(rng.bit_generator.state)), losses=np.array(losses))
     return losses
 
 

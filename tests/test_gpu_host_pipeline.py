@@ -120,6 +120,28 @@ def test_host_pipeline_matches_oracle(gpu, oracle_lib):
         assert_normals_close(got[4][k], eny, tag + " ny")
 
 
+def test_host_pipeline_zf_and_normals_only(gpu):
+    """zc and zm left out (NULL): zf and the normals are the full form's, and the
+    arrays given for zc / zm in the full call are not what this call writes."""
+    tp = gpu
+    W, n = 101, 9
+    params = tp.make_params()
+    jobs, pz, pm, res = make_inputs(tp, W, n, seed=23)
+    pipe = tp.HostPipeline(W, chunk=4)
+    full = host_outputs(n, W)
+    pipe.run(params, jobs, pz, pm, res, *full)
+    tp.stream_check()
+    zf = np.full((n, W, W), -7.0, np.float32)
+    nx = np.full((n, W - 4, W - 4), -7.0, np.float32)
+    ny = np.full_like(nx, -7.0)
+    pipe.run(params, jobs, pz, pm, res, zf, None, None, nx, ny)
+    tp.stream_check()
+    assert np.array_equal(zf, full[0]) and np.array_equal(nx, full[3]) and np.array_equal(ny, full[4])
+    # zm is rebuilt on the host as the kernel writes it
+    assert np.array_equal(np.maximum(zf, np.float32(0.0)), full[2])
+    pipe.close()
+
+
 def test_host_pipeline_rejects_bad_calls(gpu):
     tp = gpu
     W = 101
