@@ -589,6 +589,10 @@ int tp_learned_set_sigmas(tp_learned *net, const float *sigma_in, const float *s
 /* Checkpoints (training resumed where it stopped): Adam's first and second moments
  * (param_count floats each) and its step count, and the per-level sigmas (up to 24
  * levels).  With tp_learned_get_params / set_params they are the whole training state. */
+/* Inference by fused layer pairs (1: layers 0 + 1 and 2 + 3 in one launch each, the
+ * hidden activations between the two layers of a pair kept in shared memory) or one
+ * launch per layer (0, the default: faster on GB300).  Both give the same bits. */
+int tp_learned_set_fused(tp_learned *net, int on);
 int tp_learned_get_state(tp_learned *net, float *m, float *v, int count, int *step);
 int tp_learned_set_state(tp_learned *net, const float *m, const float *v, int count, int step);
 int tp_learned_get_sigmas(tp_learned *net, float *sigma_in, float *sigma_out, int nlevels);

@@ -29,6 +29,8 @@ struct tp_learned {
     int *levels = nullptr, *status = nullptr, *aux = nullptr;
     CUtensorMap h_x0, h_act[4], h_dz4, h_dza, h_dzb;  // 10 x 18 halo boxes (convolutions)
     CUtensorMap b_x0, b_act[4], b_dz4, b_dza, b_dzb;  // 8 x 16 block boxes (weight gradients)
+    CUtensorMap w_act[4];                             // 12 x 20 halo boxes (fused pairs' inputs)
+    bool fused = false;  // inference runs layers (0, 1) and (2, 3) as fused pairs (slower on GB300, kept selectable)
     int step = 0, nimg = 0;
     bool packed = false, trained_forward = false;
     std::vector<void *> allocs;
@@ -116,6 +118,42 @@ int forward(tp_learned *net, int n, bool training, cudaStream_t s)
     // inference makes the input channels inside the first convolution
     if (training) launch_prep(net->up, net->levels, net->sigma_in, net->sigma_out, net->W, n, net->x0, s);
     else launch_means(net->up, net->W, n, net->mean, s);
+    if (!training && net->fused) {
+        // layers 0 + 1 and 2 + 3 as fused pairs (their hidden activations stay on chip),
+        // then the last layer
+        for (int pair = 0; pair < 2; ++pair) {
+            FusedLaunch f;
+            std::memset(&f, 0, sizeof f);
+            f.W = net->W;
+            f.nimg = n;
+            f.tiles_x = net->tiles_x;
+            f.tiles_y = (net->W + kFusedBlockY - 1) / kFusedBlockY;
+            f.level = net->levels;
+            f.status = net->status;
+            const int la = 2 * pair, lb = la + 1;
+            f.wpack_a = net->fwd[la];
+            f.wpack_b = net->fwd[lb];
+            f.bias_a = net->params + net->boff[la];
+            f.bias_b = net->params + net->boff[lb];
+            f.emb = la == 0 ? net->params + net->emb_off : nullptr;
+            f.out = net->act[lb];
+            f.up = net->up;
+            f.mean = net->mean;
+            f.sigma_in = net->sigma_in;
+            f.sigma_out = net->sigma_out;
+            int rc = launch_fused(pair == 0, f, &net->w_act[pair == 0 ? 0 : la - 1], s);
+            if (rc) return rc;
+        }
+        ConvLaunch a = conv_args(net, n);
+        a.wpack = net->fwd[kLayers - 1];
+        a.bias = net->params + net->boff[kLayers - 1];
+        a.out_f32 = net->pred;
+        int rc = launch_conv(kCin[kLayers - 1], kCout[kLayers - 1], kLast, a, &net->h_act[kLayers - 2], s);
+        if (rc) return rc;
+        net->nimg = n;
+        net->trained_forward = false;
+        return TP_OK;
+    }
     const CUtensorMap *in[kLayers] = {&net->h_x0, &net->h_act[0], &net->h_act[1], &net->h_act[2], &net->h_act[3]};
     for (int l = 0; l < kLayers; ++l) {
         ConvLaunch a = conv_args(net, n);
@@ -220,6 +258,8 @@ extern "C" int tp_learned_create(int tile_width, int max_batch, tp_learned **out
         };
         M(net->x0, 16, &net->h_x0, &net->b_x0);
         for (int l = 0; l < 4; ++l) M(net->act[l], 32, &net->h_act[l], &net->b_act[l]);
+        for (int l = 0; l < 4; ++l)
+            if (rc == TP_OK) rc = encode_act_map(net->act[l], W, 32, B, kWideX, kWideY, &net->w_act[l]);
         M(net->dz4, 16, &net->h_dz4, &net->b_dz4);
         M(net->dza, 32, &net->h_dza, &net->b_dza);
         M(net->dzb, 32, &net->h_dzb, &net->b_dzb);
@@ -303,6 +343,13 @@ extern "C" int tp_learned_get_grads(tp_learned *net, float *host, int count)
     if (!net || !host || count != net->nparams) return tp::fail(TP_E_BAD_ARG, "tp_learned_get_grads: bad arguments");
     cudaError_t e = cudaMemcpy(host, net->grads, sizeof(float) * count, cudaMemcpyDeviceToHost);
     return e == cudaSuccess ? TP_OK : tp::cuda_fail("tp_learned_get_grads", e);
+}
+
+extern "C" int tp_learned_set_fused(tp_learned *net, int on)
+{
+    if (!net) return tp::fail(TP_E_BAD_ARG, "tp_learned_set_fused: net is NULL");
+    net->fused = on != 0;
+    return TP_OK;
 }
 
 extern "C" int tp_learned_get_state(tp_learned *net, float *m, float *v, int count, int *step)

@@ -367,6 +367,338 @@ __global__ void __launch_bounds__(kRoleThreads) conv_kernel(const __grid_constan
     if (warp == 1) tmem_dealloc(tmem, 64);
 }
 
+// ---------------------------------------------------------------- fused pairs (inference)
+// Two consecutive convolutions in one launch.  For the 8 x 14 output block of the
+// second layer (B), the first layer (A) is computed on the block's 10 x 16 halo as
+// two overlapping 8 x 16 MMA tiles, at columns 0 and 2 of that halo, from a 12 x 18
+// input halo; the second tile contributes columns 8 and 9 only, whose 8 rows per warp
+// the epilogue gathers across the warp's 32 lanes before the GELU.  A's epilogue
+// (bias, level embedding, GELU, bf16) writes its outputs into shared memory in the
+// K-major layout B's MMAs read, zero outside the image as the activation image's
+// border is, so the hidden activations never reach HBM.
+//
+// Roles: warp 0 stages the input halos, warp 1 issues the MMAs (A(i), then B(i - 1)),
+// warps 2-5 and 6-9 are two epilogue groups: group i % 2 finishes block i (A's
+// epilogue, then B's), so that two blocks' epilogue chains run at once.  Each group
+// owns 128 tensor-memory columns (A's two tiles, B's tile) and one B-operand halo.
+// Every wait is bounded (abort flag).
+constexpr int kFusedStages = 3;
+constexpr int kFusedThreads = 320;
+constexpr int kWideRow = kWideX * 16;                                // 192 bytes per row of one channel group
+constexpr int kWideGroup = (kWideRow * kWideY + 127) / 128 * 128;    // 3456
+constexpr int kWinX = kWideX + 2, kWinY = kWideY + 2;                // fp32 window of the first pair's producer
+constexpr uint32_t kFusedCols = 256;
+
+template <int CINA>
+constexpr int fused_smem_bytes()
+{
+    return kFusedStages * (CINA / 8) * kWideGroup + 2 * 4 * kGroupStride + 9 * CINA * 32 * 2 + 9 * 32 * 32 * 2 +
+           kWinX * kWinY * 4 + 512;
+}
+
+// bias (+ level embedding), GELU: the kHidden / kFirst epilogue's operations, on the
+// channels [c0, c0 + N) held in acc[0, N)
+template <int N>
+__device__ __forceinline__ void hidden_epilogue(float *acc, const float *bias, const float *emb_row)
+{
+    if (emb_row) {
+#pragma unroll
+        for (int j = 0; j < N; j += 2)
+            upk2(add2(pk2(acc[j], acc[j + 1]), add2(pk2(bias[j], bias[j + 1]), pk2(__ldg(emb_row + j), __ldg(emb_row + j + 1)))),
+                 acc[j], acc[j + 1]);
+    } else {
+#pragma unroll
+        for (int j = 0; j < N; j += 2) upk2(add2(pk2(acc[j], acc[j + 1]), pk2(bias[j], bias[j + 1])), acc[j], acc[j + 1]);
+    }
+#pragma unroll
+    for (int j = 0; j < N; j += 2) gelu_pair(acc[j], acc[j + 1]);
+}
+
+template <bool FIRST>
+__global__ void __launch_bounds__(kFusedThreads, 2) fused_kernel(const __grid_constant__ CUtensorMap xmap,
+                                                                 const FusedLaunch a)
+{
+    constexpr int CINA = FIRST ? 16 : 32;
+    constexpr int NCGA = CINA / 8, KSA = CINA / 16, NMMA_A = 9 * KSA, NMMA_B = 18;
+    constexpr int STAGE = NCGA * kWideGroup;
+    constexpr int HB = 4 * kGroupStride;                           // one B-operand halo, 32 channels
+    constexpr int WA = NMMA_A * 32 * 32, WB = NMMA_B * 32 * 32;    // packed weights, bytes
+    extern __shared__ __align__(1024) uint8_t smem[];
+    uint8_t *ha = smem;
+    uint8_t *hb = ha + kFusedStages * STAGE;
+    uint8_t *wa = hb + 2 * HB;
+    uint8_t *wb = wa + WA;
+    float *win = reinterpret_cast<float *>(wb + WB);
+    uint64_t *full = reinterpret_cast<uint64_t *>(win + kWinX * kWinY);
+    uint64_t *empty = full + kFusedStages;
+    uint64_t *accA_full = empty + kFusedStages, *accA_empty = accA_full + 2;
+    uint64_t *hb_full = accA_empty + 2, *hb_empty = hb_full + 2;
+    uint64_t *accB_full = hb_empty + 2, *accB_empty = accB_full + 2;
+    uint32_t *tslot = reinterpret_cast<uint32_t *>(accB_empty + 2);
+    volatile int *abort = reinterpret_cast<volatile int *>(tslot + 1);
+    float *bias_s = reinterpret_cast<float *>(tslot + 4);  // [64]: layer A's then layer B's biases
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+
+    for (int i = tid; i < WA / 16; i += kFusedThreads)
+        reinterpret_cast<uint4 *>(wa)[i] = reinterpret_cast<const uint4 *>(a.wpack_a)[i];
+    for (int i = tid; i < WB / 16; i += kFusedThreads)
+        reinterpret_cast<uint4 *>(wb)[i] = reinterpret_cast<const uint4 *>(a.wpack_b)[i];
+    if (tid < 32) {
+        bias_s[tid] = a.bias_a[tid];
+        bias_s[32 + tid] = a.bias_b[tid];
+    }
+    // rows 16 and 17 of B's operand halo feed only the two unused rows of B's MMA tile
+    for (int i = tid; i < 2 * 4 * 2 * kHaloX; i += kFusedThreads) {
+        const int px = i % kHaloX, row = 16 + (i / kHaloX) % 2, g = (i / (2 * kHaloX)) % 4, h = i / (8 * kHaloX);
+        *reinterpret_cast<uint4 *>(hb + h * HB + g * kGroupStride + row * kRowStride + px * 16) = make_uint4(0u, 0u, 0u, 0u);
+    }
+    if (tid == 0) {
+        for (int s = 0; s < kFusedStages; ++s) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], 1);
+        }
+        for (int b = 0; b < 2; ++b) {
+            mbar_init(&accA_full[b], 1);
+            mbar_init(&accA_empty[b], 128);
+            mbar_init(&hb_full[b], 128);
+            mbar_init(&hb_empty[b], 1);
+            mbar_init(&accB_full[b], 1);
+            mbar_init(&accB_empty[b], 128);
+        }
+        *abort = 0;
+    }
+    if (warp == 1) tmem_alloc(tslot, kFusedCols);
+    fence_proxy_async_smem();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tslot;
+    const int per_img = a.tiles_x * a.tiles_y, total = a.nimg * per_img;
+    const int mine = my_tiles(total);
+
+    if (FIRST && warp == 0) {
+        // producer: layer 0's input channels on the 12 x 18 halo, from a 14 x 20 window of
+        // the upsampled tile staged in shared memory (the same values and operations as the
+        // kFirst producer); channels 8-15 are zero in every stage
+        for (int s = 0; s < kFusedStages; ++s)
+            for (int p = lane; p < kWideX * kWideY; p += 32)
+                *reinterpret_cast<uint4 *>(ha + s * STAGE + kWideGroup + p * 16) = make_uint4(0u, 0u, 0u, 0u);
+        for (int i = 0; i < mine; ++i) {
+            const int s = i % kFusedStages;
+            if (i >= kFusedStages &&
+                !__all_sync(0xffffffffu, mbar_wait_abortable(&empty[s], ((i / kFusedStages) - 1) & 1, abort)))
+                break;
+            const int t = blockIdx.x + i * gridDim.x;
+            const int img = t / per_img, rem = t - img * per_img;
+            const int by = rem / a.tiles_x, bx = rem - by * a.tiles_x;
+            const float *u = a.up + (size_t)img * a.W * a.W;
+            const int x0 = bx * kBlockX - 3, y0 = by * kFusedBlockY - 3;  // window origin (image pixels)
+            {
+                constexpr int kWinPer = (kWinX * kWinY + 31) / 32;
+                float w[kWinPer];
+#pragma unroll
+                for (int k = 0; k < kWinPer; ++k) {  // all loads first (one latency), then the stores
+                    const int p = lane + 32 * k;
+                    const int wy = p / kWinX, wx = p - wy * kWinX;
+                    const int gx = x0 + wx, gy = y0 + wy;
+                    w[k] = p < kWinX * kWinY && gx >= 0 && gy >= 0 && gx < a.W && gy < a.W
+                               ? __ldg(u + (size_t)gy * a.W + gx) : 0.0f;
+                }
+#pragma unroll
+                for (int k = 0; k < kWinPer; ++k)
+                    if (lane + 32 * k < kWinX * kWinY) win[lane + 32 * k] = w[k];
+            }
+            __syncwarp();
+            const float mean = __ldg(a.mean + img);
+            const int lc = min(max(__ldg(a.level + img), 0), kLevels - 1);
+            const float inv = 1.0f / __ldg(a.sigma_in + lc), inv2 = 1.0f / __ldg(a.sigma_out + lc);
+            for (int p = lane; p < kWideX * kWideY; p += 32) {
+                const int hy = p / kWideX, hx = p - hy * kWideX;
+                const int gx = x0 + 1 + hx, gy = y0 + 1 + hy;
+                uint4 v = make_uint4(0u, 0u, 0u, 0u);
+                if (gx >= 0 && gy >= 0 && gx < a.W && gy < a.W) {
+                    const int c = (hy + 1) * kWinX + hx + 1;
+                    const float val = win[c];
+                    const float d2x = gx > 0 && gx < a.W - 1
+                                          ? __fsub_rn(__fadd_rn(win[c - 1], win[c + 1]), __fmul_rn(2.0f, val)) : 0.0f;
+                    const float d2y = gy > 0 && gy < a.W - 1
+                                          ? __fsub_rn(__fadd_rn(win[c - kWinX], win[c + kWinX]), __fmul_rn(2.0f, val))
+                                          : 0.0f;
+                    v.x = pack2((val - mean) * inv, (float)(gx & 1));
+                    v.y = pack2((float)(gy & 1), 1.0f);
+                    v.z = pack2(__fmul_rn(d2x, inv2), __fmul_rn(d2y, inv2));
+                }
+                *reinterpret_cast<uint4 *>(ha + s * STAGE + p * 16) = v;
+            }
+            fence_proxy_async_smem();  // the generic-proxy writes, before the tensor cores read them
+            __syncwarp();              // and every lane is done with the window before it is refilled
+            if (lane == 0) mbar_arrive(&full[s]);
+        }
+    } else if (warp == 0) {
+        if (lane == 0) {  // producer: the 12 x 18 input halo of block i, 4 channel groups
+            int i = 0;
+            for (; i < mine; ++i) {
+                const int s = i % kFusedStages;
+                if (i >= kFusedStages && !mbar_wait_abortable(&empty[s], ((i / kFusedStages) - 1) & 1, abort)) break;
+                const int t = blockIdx.x + i * gridDim.x;
+                const int img = t / per_img, rem = t - img * per_img;
+                const int by = rem / a.tiles_x, bx = rem - by * a.tiles_x;
+                mbar_expect_tx(&full[s], 4 * kWideRow * kWideY);
+#pragma unroll
+                for (int cg = 0; cg < 4; ++cg)  // the bordered image's pixel (bx 8 - 1, by 14 - 1): image pixel - 2
+                    tma_load_3d(ha + s * STAGE + cg * kWideGroup, &xmap, (bx * kBlockX - 1) * 8, by * kFusedBlockY - 1,
+                                img * 4 + cg, &full[s]);
+            }
+            if (*abort)  // copies in flight land before the CTA leaves
+                for (int k = i > kFusedStages ? i - kFusedStages : 0; k < i; ++k)
+                    mbar_wait(&full[k % kFusedStages], (k / kFusedStages) & 1);
+        }
+    } else if (warp == 1) {
+        if (lane == 0) {  // MMA issuer: A(i) and B(j) each as soon as their inputs are ready
+            constexpr uint32_t idesc = idesc_bf16(128, 32, 0, 0);
+            const uint32_t wa_a = smem_u32(wa), wb_a = smem_u32(wb);
+            int na = 0, nb = 0;  // the next blocks of layer A and of layer B to issue
+            unsigned idle = 0;
+            while (nb < mine) {
+                bool issued = false;
+                // B first: it unblocks an epilogue chain, and MMAs run in issue order
+                if (nb < na) {
+                    const int h = nb & 1;
+                    if (mbar_try(&hb_full[h], (nb >> 1) & 1) && (nb < 2 || mbar_try(&accB_empty[h], ((nb >> 1) - 1) & 1))) {
+                        tc_fence_after();
+                        const uint32_t h_a = smem_u32(hb + h * HB);
+#pragma unroll
+                        for (int q = 0; q < NMMA_B; ++q) {
+                            const int tap = q / 2, st = q - tap * 2;
+                            const int dy = tap / 3, dx = tap - dy * 3;
+                            const uint64_t ad =
+                                sdesc(h_a + 2 * st * kGroupStride + dy * kRowStride + dx * 16, kGroupStride, kRowStride);
+                            const uint64_t bd = sdesc(wb_a + q * 32 * 32, 128, 256);
+                            mma_bf16(tmem + 128 * h + 64, ad, bd, idesc, q > 0 ? 1u : 0u);
+                        }
+                        mma_commit(&hb_empty[h]);
+                        mma_commit(&accB_full[h]);
+                        ++nb;
+                        issued = true;
+                    }
+                }
+                if (na < mine) {
+                    const int s = na % kFusedStages, b = na & 1;
+                    if (mbar_try(&full[s], (na / kFusedStages) & 1) &&
+                        (na < 2 || mbar_try(&accA_empty[b], ((na >> 1) - 1) & 1))) {
+                        tc_fence_after();
+                        const uint32_t h_a = smem_u32(ha + s * STAGE);
+#pragma unroll
+                        for (int T = 0; T < 2; ++T) {
+                            const int o = 2 * T;  // tile origin: column o, row 0 of the 10 x 16 region
+#pragma unroll
+                            for (int q = 0; q < NMMA_A; ++q) {
+                                const int tap = q / KSA, st = q - tap * KSA;
+                                const int dy = tap / 3, dx = tap - dy * 3;
+                                const uint64_t ad = sdesc(h_a + 2 * st * kWideGroup + dy * kWideRow + (o + dx) * 16,
+                                                          kWideGroup, kWideRow);
+                                const uint64_t bd = sdesc(wa_a + q * 32 * 32, 128, 256);
+                                mma_bf16(tmem + 128 * b + 32 * T, ad, bd, idesc, q > 0 ? 1u : 0u);
+                            }
+                        }
+                        mma_commit(&empty[s]);
+                        mma_commit(&accA_full[b]);
+                        ++na;
+                        issued = true;
+                    }
+                }
+                if (issued) {
+                    idle = 0;
+                } else if (*abort) {
+                    break;
+                } else if (++idle > (1u << 22)) {  // nothing became ready: give up
+                    *abort = 1;
+                    break;
+                }
+            }
+            if (*abort) {  // the MMAs issued complete before the tensor memory is freed
+                if (na > 0) mbar_wait(&empty[(na - 1) % kFusedStages], ((na - 1) / kFusedStages) & 1);
+                if (nb > 0) mbar_wait(&hb_empty[(nb - 1) & 1], ((nb - 1) >> 1) & 1);
+            }
+        }
+    } else {  // epilogue group g = block parity; rows 32 q .. 32 q + 31 of each accumulator
+        const int g = (warp - 2) >> 2, q = warp & 3, m = q * 32 + lane;
+        const uint32_t lanes = (uint32_t)(q * 32) << 16;
+        const int Wp = a.W + 2;
+        const size_t plane = (size_t)Wp * Wp;
+        uint8_t *dst = hb + g * HB;
+        for (int i = g; i < mine; i += 2) {
+            // layer A's two tiles
+            if (!__all_sync(0xffffffffu, mbar_wait_abortable(&accA_full[g], (i >> 1) & 1, abort))) break;
+            if (i >= 2 && !__all_sync(0xffffffffu, mbar_wait_abortable(&hb_empty[g], ((i >> 1) - 1) & 1, abort))) break;
+            tc_fence_after();
+            const int t = blockIdx.x + i * gridDim.x;
+            const int img = t / per_img, rem = t - img * per_img;
+            const int by = rem / a.tiles_x, bx = rem - by * a.tiles_x;
+            const float *emb_row = a.emb ? a.emb + (size_t)min(max(__ldg(a.level + img), 0), kLevels - 1) * 32 : nullptr;
+            float acc[32];
+            tmem_ld32(tmem + 128 * g + lanes, acc);
+            {  // first tile: the region's columns 0-7, rows 0-15, one pixel per thread
+                const int rx = m & 7, ry = m >> 3;
+                const int gx = bx * kBlockX - 1 + rx, gy = by * kFusedBlockY - 1 + ry;
+                uint4 u[4] = {make_uint4(0u, 0u, 0u, 0u), make_uint4(0u, 0u, 0u, 0u), make_uint4(0u, 0u, 0u, 0u),
+                              make_uint4(0u, 0u, 0u, 0u)};
+                if (gx >= 0 && gy >= 0 && gx < a.W && gy < a.W) {
+                    hidden_epilogue<32>(acc, bias_s, emb_row);
+#pragma unroll
+                    for (int c = 0; c < 4; ++c)
+                        u[c] = make_uint4(pack2(acc[8 * c + 0], acc[8 * c + 1]), pack2(acc[8 * c + 2], acc[8 * c + 3]),
+                                          pack2(acc[8 * c + 4], acc[8 * c + 5]), pack2(acc[8 * c + 6], acc[8 * c + 7]));
+                }
+#pragma unroll
+                for (int c = 0; c < 4; ++c)
+                    *reinterpret_cast<uint4 *>(dst + c * kGroupStride + ry * kRowStride + rx * 16) = u[c];
+            }
+            tmem_ld32(tmem + 128 * g + 32 + lanes, acc);
+            tc_fence_before();
+            mbar_arrive(&accA_empty[g]);
+            {  // second tile: only its rows at columns 8 and 9 of the region (lanes 6, 7 of each
+               // 8-lane row group: 8 rows per warp), spread over the warp: lane l takes row
+               // (l >> 2) of those 8 and channels 8 (l & 3) .. 8 (l & 3) + 7
+                const int j = lane >> 2, cg = lane & 3;
+                const int src = 8 * (j >> 1) + 6 + (j & 1);
+                float v[8];
+#pragma unroll
+                for (int c = 0; c < 32; ++c) {
+                    const float x = __shfl_sync(0xffffffffu, acc[c], src);
+                    if ((c >> 3) == cg) v[c & 7] = x;
+                }
+                const int ms = q * 32 + src;
+                const int rx = 2 + (ms & 7), ry = ms >> 3;  // rx is 8 or 9
+                const int gx = bx * kBlockX - 1 + rx, gy = by * kFusedBlockY - 1 + ry;
+                uint4 u = make_uint4(0u, 0u, 0u, 0u);
+                if (gx >= 0 && gy >= 0 && gx < a.W && gy < a.W) {
+                    hidden_epilogue<8>(v, bias_s + 8 * cg, emb_row ? emb_row + 8 * cg : nullptr);
+                    u = make_uint4(pack2(v[0], v[1]), pack2(v[2], v[3]), pack2(v[4], v[5]), pack2(v[6], v[7]));
+                }
+                *reinterpret_cast<uint4 *>(dst + cg * kGroupStride + ry * kRowStride + rx * 16) = u;
+            }
+            fence_proxy_async_smem();  // generic writes of B's operand, before the tensor cores read it
+            mbar_arrive(&hb_full[g]);
+            // layer B
+            if (!__all_sync(0xffffffffu, mbar_wait_abortable(&accB_full[g], (i >> 1) & 1, abort))) break;
+            tc_fence_after();
+            tmem_ld32(tmem + 128 * g + 64 + lanes, acc);
+            tc_fence_before();
+            mbar_arrive(&accB_empty[g]);
+            const int px = bx * kBlockX + (m & 7), py = by * kFusedBlockY + (m >> 3);
+            if ((m >> 3) < kFusedBlockY && px < a.W && py < a.W) {
+                hidden_epilogue<32>(acc, bias_s + 32, nullptr);
+                store_bf16<32>(a.out, img, plane, (size_t)(py + 1) * Wp + (px + 1), acc);
+            }
+        }
+    }
+    __syncthreads();
+    if (tid == 0 && *abort) atomicExch(a.status, TP_E_TIMEOUT);
+    tc_fence_after();
+    if (warp == 1) tmem_dealloc(tmem, kFusedCols);
+}
+
 template <int CIN, int COUT>
 constexpr int wgrad_tiles()
 {
@@ -517,7 +849,7 @@ int sm_count() { return tp::device_sm_count(); }
 // as their columns fit in the SM's 512.  An overestimate only queues CTAs (they
 // never wait on one another).
 template <typename K>
-int grid_for(K kernel, int smem, int tmem_cols, int units, int *grid)
+int grid_for(K kernel, int smem, int tmem_cols, int units, int *grid, int threads = kRoleThreads)
 {
     static std::mutex mu;
     static std::map<std::pair<int, const void *>, int> cache;  // per device and kernel instance
@@ -539,11 +871,11 @@ int grid_for(K kernel, int smem, int tmem_cols, int units, int *grid)
         cudaDeviceGetAttribute(&regs_sm, cudaDevAttrMaxRegistersPerMultiprocessor, dev);
         cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev);
         cudaDeviceGetAttribute(&threads_sm, cudaDevAttrMaxThreadsPerMultiProcessor, dev);
-        const int warps = (kRoleThreads + 31) / 32;
+        const int warps = (threads + 31) / 32;
         const int regs_warp = (fa.numRegs * 32 + 255) / 256 * 256;
         int n = smem_sm / (smem + (int)fa.sharedSizeBytes + reserved);
         n = std::min(n, regs_sm / std::max(1, regs_warp * warps));
-        n = std::min(n, threads_sm / kRoleThreads);
+        n = std::min(n, threads_sm / threads);
         n = std::min(n, 512 / tmem_cols);
         if (n < 1) return tp::fail(TP_E_BAD_ARG, "learned: kernel does not fit on an SM");
         per_sm = n;
@@ -564,6 +896,20 @@ int conv_instance(const ConvLaunch &a, const CUtensorMap *halo, cudaStream_t s)
     conv_kernel<CIN, COUT, MODE><<<grid, kRoleThreads, smem, s>>>(*halo, a);
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? TP_OK : tp::cuda_fail("conv kernel launch", e);
+}
+
+template <bool FIRST>
+int fused_instance(const FusedLaunch &a, const CUtensorMap *wide, cudaStream_t s)
+{
+    const int units = a.nimg * a.tiles_x * a.tiles_y;
+    if (units <= 0) return TP_OK;
+    constexpr int smem = fused_smem_bytes<FIRST ? 16 : 32>();
+    int grid = 0;
+    int rc = grid_for(fused_kernel<FIRST>, smem, (int)kFusedCols, units, &grid, kFusedThreads);
+    if (rc) return rc;
+    fused_kernel<FIRST><<<grid, kFusedThreads, smem, s>>>(*wide, a);
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? TP_OK : tp::cuda_fail("fused convolution launch", e);
 }
 
 template <int CIN, int COUT>
@@ -607,7 +953,17 @@ __device__ float tile_mean(const float *u, int n)
 {
     __shared__ double part[256];
     double s = 0.0;
-    for (int i = threadIdx.x; i < n; i += blockDim.x) s += u[i];
+    // each thread's values in the same order as one strided loop, loaded 8 at a time
+    // ahead of the (dependent) additions
+    int i = threadIdx.x;
+    for (; i + 7 * (int)blockDim.x < n; i += 8 * blockDim.x) {
+        float v[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) v[k] = __ldg(u + i + k * blockDim.x);
+#pragma unroll
+        for (int k = 0; k < 8; ++k) s += v[k];
+    }
+    for (; i < n; i += blockDim.x) s += u[i];
     part[threadIdx.x] = s;
     __syncthreads();
     for (int k = blockDim.x / 2; k > 0; k >>= 1) {
@@ -742,6 +1098,11 @@ int launch_conv(int cin, int cout, int mode, const ConvLaunch &a, const CUtensor
     if (cin == 16 && cout == 32 && mode == kBackData) return conv_instance<16, 32, kBackData>(a, halo, s);
     if (cin == 32 && cout == 32 && mode == kBackData) return conv_instance<32, 32, kBackData>(a, halo, s);
     return tp::fail(TP_E_BAD_ARG, "learned: no convolution instance for this shape");
+}
+
+int launch_fused(bool first, const FusedLaunch &a, const CUtensorMap *wide, cudaStream_t s)
+{
+    return first ? fused_instance<true>(a, wide, s) : fused_instance<false>(a, wide, s);
 }
 
 int launch_wgrad(int cin, int cout, const WgradLaunch &a, const CUtensorMap *xb, const CUtensorMap *zb, cudaStream_t s)

@@ -45,6 +45,21 @@ struct ConvLaunch {
     const float *sigma_out;      // [kLevels] (scale of the second-difference channels)
 };
 
+// Two consecutive convolutions of an inference pass in one launch (the first 16 -> 32
+// with its input made from the upsampled tiles, or a hidden 32 -> 32 reading an
+// activation image, then a hidden 32 -> 32): the first layer's outputs on the block's
+// 10 x 18 halo stay in shared memory as the second layer's operand.
+struct FusedLaunch {
+    int W, nimg, tiles_x, tiles_y;
+    const uint8_t *wpack_a, *wpack_b;  // packed B operands of the two layers
+    const float *bias_a, *bias_b;      // [32] each
+    const float *emb;                  // [kLevels][32] level embedding of the first layer, or null
+    const int *level;                  // [nimg]
+    __nv_bfloat16 *out;                // the second layer's activation image
+    int *status;
+    const float *up, *mean, *sigma_in, *sigma_out;  // first-layer input (first pair only)
+};
+
 // Weight gradient of one layer over a batch: dW[co][tap][ci] += sum_p dZ[p][co] X[p + tap][ci].
 struct WgradLaunch {
     int W, nimg, tiles_x, tiles_y;
@@ -61,6 +76,14 @@ int launch_conv(int cin, int cout, int mode, const ConvLaunch &a, const CUtensor
 int launch_wgrad(int cin, int cout, const WgradLaunch &a, const CUtensorMap *xbox, const CUtensorMap *zbox,
                  cudaStream_t s);
 int encode_act_map(void *base, int W, int channels, int nimg, int box_x, int box_y, CUtensorMap *out);
+// first: the pair starting at layer 0 (input from the upsampled tiles); else a pair of
+// hidden layers whose input is read through `wide` (12 x 20 pixel boxes of 32 channels)
+int launch_fused(bool first, const FusedLaunch &a, const CUtensorMap *wide, cudaStream_t s);
+// A fused pair's output block is 8 x 14 pixels (its second layer's MMA tile keeps the 8 x 16
+// shape, two rows unused), so that the first layer's 10 x 16 region is covered exactly by two
+// 8 x 16 MMA tiles at columns 0 and 2; its input halo is 12 x 18.
+constexpr int kFusedBlockY = kBlockY - 2;
+constexpr int kWideX = kBlockX + 4, kWideY = kFusedBlockY + 4;
 
 // small kernels
 void launch_pack(const float *w, int cin, int cout, uint8_t *fwd, uint8_t *bwd, cudaStream_t s);

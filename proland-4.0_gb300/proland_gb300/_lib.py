@@ -214,6 +214,7 @@ def lib():
         "tp_learned_set_params": ([_vp, _f32p, _i], _i),
         "tp_learned_get_grads": ([_vp, _f32p, _i], _i),
         "tp_learned_set_sigmas": ([_vp, _f32p, _f32p, _i], _i),
+        "tp_learned_set_fused": ([_vp, _i], _i),
         "tp_learned_get_state": ([_vp, _vp, _vp, _i, C.POINTER(_i)], _i),
         "tp_learned_set_state": ([_vp, _vp, _vp, _i, _i], _i),
         "tp_learned_get_sigmas": ([_vp, _vp, _vp, _i], _i),

@@ -184,6 +184,10 @@ class LearnedPredictor:
         p = np.ascontiguousarray(p, np.float32)
         check(lib().tp_learned_set_params(self.handle, p.ctypes.data_as(_f32p), p.size))
 
+    def set_fused(self, on=True):
+        """Inference by fused layer pairs, or one launch per layer (the default; same bits)."""
+        check(lib().tp_learned_set_fused(self.handle, int(bool(on))))
+
     CHECKPOINT_FORMAT = "proland_gb300.learned/1"
 
     def save(self, path, **extra):

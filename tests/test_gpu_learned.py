@@ -123,6 +123,31 @@ def test_inference_input_channels_made_in_the_first_layer(L, W, n):
     net.close()
 
 
+@pytest.mark.parametrize("W,n", [(21, 5), (101, 256), (197, 64)])
+def test_fused_pairs_give_the_per_layer_bits(L, W, n):
+    """Inference by fused layer pairs (layers 0 + 1 and 2 + 3 in one launch each, the
+    hidden activations kept in shared memory) gives the bits of one launch per layer,
+    over batches large enough that every CTA runs many blocks through its rings."""
+    rng = np.random.default_rng(W * 7 + n)
+    levels = [int(v) for v in rng.integers(1, 13, n)]
+    up = (rng.standard_normal((n, W, W)) * 300.0 + 1000.0).astype(np.float32)
+    up += np.cumsum(rng.standard_normal((n, W, W)).astype(np.float32), axis=2)
+    si = np.full(24, 300.0, np.float32)
+    so = np.geomspace(200.0, 0.01, 24).astype(np.float32)
+    net = L.LearnedPredictor(tile_width=W, max_batch=n, seed=5)
+    net.set_sigmas(si, so)
+    up_d = torch.from_numpy(up).cuda()
+    net.set_fused(False)
+    per_layer = net.forward(up_d, levels).clone()
+    net.set_fused(True)
+    fused = net.forward(up_d, levels)
+    torch.cuda.synchronize()
+    assert torch.isfinite(fused).all()
+    diff = (fused != per_layer).sum().item()
+    assert diff == 0, "%d of %d outputs differ" % (diff, fused.numel())
+    net.close()
+
+
 def test_adam_lowers_the_loss_of_a_fixed_batch(L):
     W, n = 37, 4
     levels, up, target, si, so = _case(W, n, seed=3)
