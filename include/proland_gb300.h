@@ -507,6 +507,13 @@ int tp_ortho_batch_device(tp_storage *ortho, tp_storage *residuals, const tp_ort
  * 2^32 dividends on the device; *mismatches receives the number of differing
  * results (0 expected) and *first_mismatch the bits of the first one (or ~0). */
 int tp_division_self_test(float divisor, unsigned long long *mismatches, uint32_t *first_mismatch);
+/* The sphere-normal kernel's quotients with a shared denominator (the correctly
+ * rounded reciprocal of the denominator, then one exact-remainder correction per
+ * numerator) against the correctly rounded division: n_random pseudo-random pairs
+ * (all signs, exponents -64..63) and every positive dividend for each of the given
+ * divisors; *mismatches receives the number of differing quotients. */
+int tp_sphere_division_self_test(unsigned long long n_random, unsigned seed, const float *divisors, int n_divisors,
+                                 unsigned long long *mismatches, unsigned long long *first_mismatch);
 
 /* The ortho producers behind the TileCache / TileProducer protocol above
  * (tp_producer_get_tile / put_tile / has_tile / border, tp_scheduler_run,

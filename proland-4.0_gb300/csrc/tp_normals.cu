@@ -58,6 +58,24 @@ __device__ __forceinline__ float sphere_blend(const tp::SphereFrame &f)
     return m_(m_(s, s), s_(3.0f, m_(2.0f, s)));
 }
 
+// x / y correctly rounded, given z = RN(1 / y) (__frcp_rn): q = RN(x z) is within one
+// ulp of x / y, the remainder x - q y is exact (one FMA), and RN(q + r z) is the
+// correctly rounded quotient (Markstein's theorem, round to nearest).  x or y outside
+// [2^-60, 2^60] in magnitude take the division itself: inside, the quotient and the
+// remainder stay normal numbers, as the theorem assumes.  tp_sphere_division_self_test
+// compares it with __fdiv_rn.
+__device__ __forceinline__ float div_rcp(float x, float y, float z)
+{
+    const float ax = fabsf(x), ay = fabsf(y);
+    if (ax <= 0x1p60f && ax >= 0x1p-60f && ay <= 0x1p60f && ay >= 0x1p-60f) {
+        const float q = __fmul_rn(x, z);
+        const float r = __fmaf_rn(-q, y, x);
+        return __fmaf_rn(r, z, q);
+    }
+    if (ax == 0.0f && ay != 0.0f) return __fmul_rn(x, z);  // +-0 / y: the sign of x / y
+    return __fdiv_rn(x, y);
+}
+
 // getWorldPosition of terrain2/normalShader.glsl:56-73 (the patch's projective
 // mapping onto the sphere), for grid position (u, v) = (un, vn) * n in samples
 // (un = u / n and vn = v / n, correctly rounded) and height h; s = sphere_blend(f).
@@ -66,9 +84,10 @@ __device__ __forceinline__ void sphere_pos(const tp::SphereFrame &f, float s, fl
     const float U = s_(1.0f, u), V = s_(1.0f, v);
     const float al[4] = {m_(U, V), m_(u, V), m_(U, v), m_(u, v)};
     const float d = dot4(al, f.L);
+    const float rd = __frcp_rn(d);  // the four quotients share the denominator
     float ap[4];
 #pragma unroll
-    for (int k = 0; k < 4; ++k) ap[k] = __fdiv_rn(m_(al[k], f.L[k]), d);
+    for (int k = 0; k < 4; ++k) ap[k] = div_rcp(m_(al[k], f.L[k]), d, rd);
     float up[3], cp[3];
 #pragma unroll
     for (int r = 0; r < 3; ++r) {
@@ -133,7 +152,7 @@ __device__ __forceinline__ void sphere_normal(const tp::SphereFrame &F, const fl
     const float b[3] = {s_(X[i3], X[i2]), s_(Y[i3], Y[i2]), s_(Z[i3], Z[i2])};
     float cr[3] = {s_(m_(a[1], b[2]), m_(a[2], b[1])), s_(m_(a[2], b[0]), m_(a[0], b[2])),
                    s_(m_(a[0], b[1]), m_(a[1], b[0]))};
-    const float inv = __fdiv_rn(1.0f, __fsqrt_rn(dot3(cr, cr)));
+    const float inv = __frcp_rn(__fsqrt_rn(dot3(cr, cr)));  // RN(1 / s), as 1.0f / s is
     cr[0] = m_(cr[0], inv);
     cr[1] = m_(cr[1], inv);
     cr[2] = m_(cr[2], inv);
@@ -495,5 +514,90 @@ extern "C" int tp_normal_batch_format(tp_storage *elev, tp_storage *normals, con
                                            root_quad_size > 0.0 ? p2t.data() : nullptr);
         if (rc) return rc;
     }
+    return TP_OK;
+}
+
+namespace {
+
+// Random (x, y) pairs: sign, exponent in [-64, 63] and mantissa from a counter hash,
+// and for every pair the quotient of div_rcp against __fdiv_rn.
+__device__ __forceinline__ uint32_t st_hash(uint32_t x)
+{
+    x ^= x >> 16;
+    x *= 0x7feb352du;
+    x ^= x >> 15;
+    x *= 0x846ca68bu;
+    x ^= x >> 16;
+    return x;
+}
+
+__device__ __forceinline__ float st_float(uint32_t h, uint32_t m)
+{
+    return __uint_as_float((h & 0x80000000u) | ((uint32_t)(127 - 64 + (int)((h >> 24) & 127)) << 23) | (m & 0x7FFFFFu));
+}
+
+__global__ void sphere_division_check_kernel(uint64_t n, uint32_t seed, unsigned long long *mismatches,
+                                             unsigned long long *first)
+{
+    unsigned long long bad = 0;
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        const uint32_t a = st_hash((uint32_t)i ^ seed), b = st_hash((uint32_t)(i >> 32) + 0x9E3779B9u * (uint32_t)i + seed);
+        const float x = st_float(a, st_hash(a + 1u)), y = st_float(b, st_hash(b + 7u));
+        const float f = div_rcp(x, y, __frcp_rn(y)), e = __fdiv_rn(x, y);
+        if (__float_as_uint(f) != __float_as_uint(e)) {
+            ++bad;
+            atomicMin(first, (unsigned long long)i);
+        }
+    }
+    if (bad) atomicAdd(mismatches, bad);
+}
+
+// Every positive x (all 2^31 bit patterns below +inf) against one divisor y.
+__global__ void sphere_division_sweep_kernel(float y, unsigned long long *mismatches, unsigned long long *first)
+{
+    unsigned long long bad = 0;
+    const float z = __frcp_rn(y);
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t b = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; b < 0x7F800000ull; b += stride) {
+        const float x = __uint_as_float((uint32_t)b);
+        const float f = div_rcp(x, y, z), e = __fdiv_rn(x, y);
+        if (__float_as_uint(f) != __float_as_uint(e)) {
+            ++bad;
+            atomicMin(first, (unsigned long long)b);
+        }
+    }
+    if (bad) atomicAdd(mismatches, bad);
+}
+
+}  // namespace
+
+extern "C" int tp_sphere_division_self_test(unsigned long long n_random, unsigned seed, const float *divisors,
+                                            int n_divisors, unsigned long long *mismatches,
+                                            unsigned long long *first_mismatch)
+{
+    if (!mismatches || n_divisors < 0 || (n_divisors > 0 && !divisors))
+        return tp::fail(TP_E_BAD_ARG, "tp_sphere_division_self_test: bad arguments");
+    unsigned long long *d = nullptr;
+    cudaError_t e = cudaMalloc(&d, 2 * sizeof(unsigned long long));
+    if (e != cudaSuccess) return tp::cuda_fail("cudaMalloc (division self-test)", e);
+    const unsigned long long init[2] = {0ull, ~0ull};
+    e = cudaMemcpy(d, init, sizeof init, cudaMemcpyHostToDevice);
+    const int grid = tp::device_sm_count() * 8;
+    if (e == cudaSuccess && n_random > 0) {
+        sphere_division_check_kernel<<<grid, 256>>>(n_random, seed, d, d + 1);
+        e = cudaGetLastError();
+    }
+    for (int k = 0; k < n_divisors && e == cudaSuccess; ++k) {
+        sphere_division_sweep_kernel<<<grid, 256>>>(divisors[k], d, d + 1);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    unsigned long long out[2] = {0ull, 0ull};
+    if (e == cudaSuccess) e = cudaMemcpy(out, d, sizeof out, cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    if (e != cudaSuccess) return tp::cuda_fail("division self-test", e);
+    *mismatches = out[0];
+    if (first_mismatch) *first_mismatch = out[1];
     return TP_OK;
 }

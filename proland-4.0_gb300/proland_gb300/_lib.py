@@ -135,6 +135,8 @@ def lib():
         "tp_ortho_residual_producer_create": ([_vp, C.c_char_p, C.POINTER(_vp)], _i),
         "tp_ortho_producer_create": ([_vp, _vp, C.POINTER(OrthoParams), _f32p, _i, _i, _i, C.POINTER(_vp)], _i),
         "tp_division_self_test": ([C.c_float, C.POINTER(C.c_ulonglong), C.POINTER(C.c_uint32)], _i),
+        "tp_sphere_division_self_test": ([C.c_ulonglong, C.c_uint, _f32p, _i, C.POINTER(C.c_ulonglong),
+                                          C.POINTER(C.c_ulonglong)], _i),
         "tp_ortho_dat_open": ([C.c_char_p, C.POINTER(_vp)], _i),
         "tp_ortho_dat_close": ([_vp], _i),
         "tp_ortho_dat_info": ([_vp, C.POINTER(_i)], _i),
