@@ -36,6 +36,7 @@ extern "C" {
 #define TP_E_CUDA (-5)           /* a CUDA runtime call failed */
 #define TP_E_IO (-6)             /* residual file missing, truncated or corrupt */
 #define TP_E_NO_DEVICE (-7)      /* no CUDA device (the library has no CPU fallback) */
+#define TP_E_BOUNDS (-8)         /* debug builds: a device-side index check failed (the access was skipped) */
 
 const char *tp_last_error(void);
 /* Library version, and whether the CUDA kernels can run here (1) or not (0). */
@@ -52,6 +53,19 @@ int tp_device_available(void);
 typedef struct tp_storage tp_storage;
 int tp_storage_create(int tile_width, int channels, int capacity, int on_device, tp_storage **out);
 int tp_storage_destroy(tp_storage *s);
+/* Debug builds (libproland_gb300_debug.so, built with TP_DEBUG; see build.py): every
+ * storage's slots sit between two guard regions of a fixed byte pattern, and the
+ * kernels that take device job arrays check each job's slot and parent indexes
+ * against the storages' capacities before using them (a bad job sets the status
+ * word to TP_E_BOUNDS and is skipped).  tp_build_is_debug returns 1 in debug
+ * builds; tp_storage_check_guards returns TP_OK while the guards are intact (always
+ * in release builds) and TP_E_BOUNDS once a write crossed them;
+ * tp_debug_check_capacity lowers the capacity the device-side checks use (debug
+ * builds only; 0 restores it), so that a test can plant an out-of-range slot that
+ * still lies inside the allocation. */
+int tp_build_is_debug(void);
+int tp_storage_check_guards(const tp_storage *s);
+int tp_debug_check_capacity(tp_storage *s, int capacity);
 int tp_storage_tile_size(const tp_storage *s);   /* getTileSize */
 int tp_storage_capacity(const tp_storage *s);    /* getCapacity */
 int tp_storage_free_slots(const tp_storage *s);  /* getFreeSlots */

@@ -188,7 +188,25 @@ struct UnitInfo {
     int valid;    // 0: past the end of the frame
     int job;      // job index
     int band;
+    int skip;     // debug builds: the job failed its index checks and is not produced
 };
+
+#ifdef TP_DEBUG
+// Debug builds: a job's indexes against the storages and the job list before any of
+// them addresses memory; a bad job sets the status word to TP_E_BOUNDS.
+__device__ bool job_in_bounds(const tp::ClassLaunch &c, int job)
+{
+    const tp_tile_job &J = c.jobs[job];
+    const bool ok = J.out_slot >= 0 && J.out_slot < c.elev_cap && J.level >= 0 && J.level <= 30 &&
+                    (J.level == 0 || (J.parent_slot >= 0 && J.parent_slot < c.elev_cap)) &&
+                    (J.residual_slot < 0 || J.residual_slot < c.res_cap) &&
+                    (J.normal_slot < 0 || c.nrm == nullptr || J.normal_slot < c.nrm_cap) &&
+                    J.parent_job >= -1 && J.parent_job < job && J.noise_layer >= 0 && J.noise_layer < 6 &&
+                    J.noise_rot >= 0 && J.noise_rot < 4;
+    if (!ok) report(TP_E_BOUNDS);
+    return ok;
+}
+#endif
 
 // Thread 0: wait (bounded) until the parent job's bands are complete, then issue
 // the TMA copies of unit (job, band) into `stage`, completing on `bar`.
@@ -562,13 +580,18 @@ frame_kernel(const __grid_constant__ CUtensorMap pmap, const __grid_constant__ C
         // start the reserved unit; its parent has a smaller index, taken earlier by a
         // running CTA, so waiting for it (bounded) cannot deadlock
         if (threadIdx.x == 0) {
-            UnitInfo x{0, 0, 0};
+            UnitInfo x{0, 0, 0, 0};
             const int u = reserved;
             if (u < units) {
                 x.valid = 1;
                 x.job = u / c.bands;
                 x.band = u - x.job * c.bands;
-                issue_copies(c, &pmap, &rmap, x.job, x.band, stage, &bar);
+#ifdef TP_DEBUG
+                x.skip = job_in_bounds(c, x.job) ? 0 : 1;
+                if (x.skip) mbar_arrive(&bar);  // the unit's phase completes with no copy
+                else
+#endif
+                    issue_copies(c, &pmap, &rmap, x.job, x.band, stage, &bar);
             }
             info = x;
         }
@@ -576,7 +599,7 @@ frame_kernel(const __grid_constant__ CUtensorMap pmap, const __grid_constant__ C
         const UnitInfo x = info;
         if (!x.valid) break;
         if (threadIdx.x == 0) reserved = atomicAdd(f.counter, 1);
-        issue_lattice(c, x.job, stage);
+        if (!x.skip) issue_lattice(c, x.job, stage);
         cp_async_commit();
         // warp 0 polls the mbarrier; the other warps wait at the CTA barrier below
         if (threadIdx.x < 32) {
@@ -594,7 +617,7 @@ frame_kernel(const __grid_constant__ CUtensorMap pmap, const __grid_constant__ C
             for (int t = threadIdx.x; t < c.buf_floats; t += kThreads) stage[t] = 0.0f;
             __syncthreads();
         }
-        compute_unit<MOD>(c, x.job, x.band, stage);
+        if (!x.skip) compute_unit<MOD>(c, x.job, x.band, stage);
         if (f.any_deps) fence_proxy_async_global();
         __syncthreads();  // the stage is free again; all of this unit's stores are issued
         if (f.any_deps && threadIdx.x == 0) {
@@ -724,6 +747,9 @@ using KernelFn = void (*)(const CUtensorMap, const CUtensorMap, const FrameLaunc
 // The kernel instance of a (stages, CTAs-per-SM target, modulated-noise) choice.
 static KernelFn pick(int stages, int minb, bool mod)
 {
+#ifdef TP_DEBUG
+    stages = 1;  // the index checks are in the single-stage kernel
+#endif
     if (stages >= 2) {
         if (minb >= 3) return mod ? frame_kernel2<3, true> : frame_kernel2<3, false>;
         return mod ? frame_kernel2<2, true> : frame_kernel2<2, false>;
@@ -770,6 +796,25 @@ int frame_occupancy(int stage_floats, int stages, int minb, bool mod, int *block
     if (rc) return rc;
     cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, fn, kThreads, smem);
     if (e != cudaSuccess) return cuda_fail("cudaOccupancyMaxActiveBlocksPerMultiprocessor", e);
+    return TP_OK;
+}
+
+int status_device_ptr(int **out)
+{
+    static std::mutex mu;
+    static std::map<int, int *> ptrs;  // per device
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return cuda_fail("cudaGetDevice (status)", e);
+    std::lock_guard<std::mutex> lk(mu);
+    int *&p = ptrs[dev];
+    if (!p) {
+        void *q = nullptr;
+        e = cudaGetSymbolAddress(&q, g_tp_status);
+        if (e != cudaSuccess) return cuda_fail("cudaGetSymbolAddress (status)", e);
+        p = static_cast<int *>(q);
+    }
+    *out = p;
     return TP_OK;
 }
 

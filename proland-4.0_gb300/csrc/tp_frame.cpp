@@ -291,6 +291,9 @@ int tp::class_layout(tp_storage *elev, tp_storage *res, tp_storage *nrm, const t
     tp::ClassLaunch L;
     std::memset(&L, 0, sizeof L);
     L.elev = elev->base;
+    L.elev_cap = tp::checked_capacity(elev);
+    L.res_cap = tp::checked_capacity(res);
+    L.nrm_cap = tp::checked_capacity(nrm);
     L.W = W;
     L.pitch = elev->pitch;
     L.plane_stride = elev->plane_stride;

@@ -50,6 +50,8 @@ struct tp_storage {
     long long slot_stride = 0;   // channels * plane_stride floats
     int on_device = 1;            // 1 device memory, 0 pinned host memory, 2 none (bookkeeping only)
     float *base = nullptr;
+    float *alloc = nullptr;      // the allocation: base, preceded (debug builds) by a guard region
+    int check_cap = 0;           // debug builds: the capacity the device-side checks use (0: capacity)
     std::vector<int> free_list;  // stack of free slot indices
     std::vector<uint8_t> in_use;
     std::mutex mu;
@@ -110,6 +112,7 @@ struct ClassLaunch {
     long long nrm_plane_stride, nrm_slot_stride;
     const __half *noise;
     int g, gshift, flip, no_clamp, noise_mode;
+    int elev_cap, res_cap, nrm_cap;  // slots the device-side checks of debug builds accept
     // shared-memory layout of a unit within a stage
     int buf_floats;           // (band rows + 2) * pitch, rounded to 128 bytes
     int par_pitch, par_rows;  // parent zf window
@@ -142,6 +145,10 @@ int frame_occupancy(int stage_floats, int stages, int minb, bool mod, int *block
 // through the storage's staging buffer (one linear copy + a repack kernel).
 int staged_copy(tp_storage *s, int first, int count, int channel, float *host, bool up, void *stream);
 int read_status(int *status, bool clear);
+// The device address of the status word (kernels of other files report through it).
+int status_device_ptr(int **out);
+// The capacity a storage's device-side checks use (debug builds).
+inline int checked_capacity(const tp_storage *s) { return s ? (s->check_cap > 0 ? s->check_cap : s->capacity) : 0; }
 // One plane copy of repack_planes: `count` tiles of `rows` rows of `width` floats.
 struct PlaneXfer {
     const float *src;
@@ -223,6 +230,8 @@ struct OrthoLaunch {
     const uint32_t *noise;
     int W, win_pitch;
     tp_ortho_params p;
+    int *status;               // the device status word
+    int cap, res_cap;          // slots the device-side checks of debug builds accept
 };
 int ortho_smem_bytes(int W, int *win_pitch);
 int launch_ortho(const OrthoLaunch &L, void *stream);

@@ -11,6 +11,7 @@
 
 #include "tp_internal.h"
 #include "tp_trace.h"
+#include "tp_div.h"
 
 namespace {
 
@@ -58,24 +59,6 @@ __device__ __forceinline__ float sphere_blend(const tp::SphereFrame &f)
     return m_(m_(s, s), s_(3.0f, m_(2.0f, s)));
 }
 
-// x / y correctly rounded, given z = RN(1 / y) (__frcp_rn): q = RN(x z) is within one
-// ulp of x / y, the remainder x - q y is exact (one FMA), and RN(q + r z) is the
-// correctly rounded quotient (Markstein's theorem, round to nearest).  x or y outside
-// [2^-60, 2^60] in magnitude take the division itself: inside, the quotient and the
-// remainder stay normal numbers, as the theorem assumes.  tp_sphere_division_self_test
-// compares it with __fdiv_rn.
-__device__ __forceinline__ float div_rcp(float x, float y, float z)
-{
-    const float ax = fabsf(x), ay = fabsf(y);
-    if (ax <= 0x1p60f && ax >= 0x1p-60f && ay <= 0x1p60f && ay >= 0x1p-60f) {
-        const float q = __fmul_rn(x, z);
-        const float r = __fmaf_rn(-q, y, x);
-        return __fmaf_rn(r, z, q);
-    }
-    if (ax == 0.0f && ay != 0.0f) return __fmul_rn(x, z);  // +-0 / y: the sign of x / y
-    return __fdiv_rn(x, y);
-}
-
 // getWorldPosition of terrain2/normalShader.glsl:56-73 (the patch's projective
 // mapping onto the sphere), for grid position (u, v) = (un, vn) * n in samples
 // (un = u / n and vn = v / n, correctly rounded) and height h; s = sphere_blend(f).
@@ -87,7 +70,7 @@ __device__ __forceinline__ void sphere_pos(const tp::SphereFrame &f, float s, fl
     const float rd = __frcp_rn(d);  // the four quotients share the denominator
     float ap[4];
 #pragma unroll
-    for (int k = 0; k < 4; ++k) ap[k] = div_rcp(m_(al[k], f.L[k]), d, rd);
+    for (int k = 0; k < 4; ++k) ap[k] = tp::div_rcp(m_(al[k], f.L[k]), d, rd);
     float up[3], cp[3];
 #pragma unroll
     for (int r = 0; r < 3; ++r) {
@@ -544,7 +527,7 @@ __global__ void sphere_division_check_kernel(uint64_t n, uint32_t seed, unsigned
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
         const uint32_t a = st_hash((uint32_t)i ^ seed), b = st_hash((uint32_t)(i >> 32) + 0x9E3779B9u * (uint32_t)i + seed);
         const float x = st_float(a, st_hash(a + 1u)), y = st_float(b, st_hash(b + 7u));
-        const float f = div_rcp(x, y, __frcp_rn(y)), e = __fdiv_rn(x, y);
+        const float f = tp::div_rcp(x, y, __frcp_rn(y)), e = __fdiv_rn(x, y);
         if (__float_as_uint(f) != __float_as_uint(e)) {
             ++bad;
             atomicMin(first, (unsigned long long)i);
@@ -561,7 +544,7 @@ __global__ void sphere_division_sweep_kernel(float y, unsigned long long *mismat
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
     for (uint64_t b = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; b < 0x7F800000ull; b += stride) {
         const float x = __uint_as_float((uint32_t)b);
-        const float f = div_rcp(x, y, z), e = __fdiv_rn(x, y);
+        const float f = tp::div_rcp(x, y, z), e = __fdiv_rn(x, y);
         if (__float_as_uint(f) != __float_as_uint(e)) {
             ++bad;
             atomicMin(first, (unsigned long long)b);

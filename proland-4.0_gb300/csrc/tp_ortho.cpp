@@ -216,6 +216,10 @@ int ortho_batch(tp_storage *o, tp_storage *r, const tp_ortho_params *p, const tp
     L.W = o->W;
     tp::ortho_smem_bytes(o->W, &L.win_pitch);
     L.p = *p;
+    L.cap = tp::checked_capacity(o);
+    L.res_cap = tp::checked_capacity(r);
+    rc = tp::status_device_ptr(&L.status);
+    if (rc) return rc;
     return tp::launch_ortho(L, stream);
 }
 

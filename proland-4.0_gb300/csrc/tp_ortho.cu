@@ -22,15 +22,16 @@
 #include <vector>
 
 #include "tp_internal.h"
-
-extern __device__ int g_tp_status;
+#include "tp_div.h"
 
 namespace {
 
 constexpr int kThreads = 256;
 constexpr unsigned kDepLimit = 1u << 22;  // dependency polls (64 ns back-off) before giving up
 
-__device__ __forceinline__ void report(int code) { atomicCAS(&g_tp_status, 0, code); }
+// The library's status word lives in another file's device memory: its address comes
+// with the launch.
+__device__ __forceinline__ void report(int *status, int code) { atomicCAS(status, 0, code); }
 
 __device__ __forceinline__ int ld_acquire(const int *p)
 {
@@ -102,10 +103,11 @@ __device__ __forceinline__ void rgb_to_hsv(const float *rgb, float *hsv)
     hsv[2] = mx;
     if (delta != 0.0f) {
         hsv[1] = d_(delta, mx);
+        const float rdelta = __frcp_rn(delta);  // the three quotients below share the divisor
         float d[3];
 #pragma unroll
-        for (int c = 0; c < 3; ++c)
-            d[c] = d_(a_(div_known(s_(mx, rgb[c]), 6.0f, kInv6), m_(delta, 0.5f)), delta);  // delta / 2 exact
+        for (int c = 0; c < 3; ++c)  // delta / 2 exact
+            d[c] = tp::div_rcp(a_(div_known(s_(mx, rgb[c]), 6.0f, kInv6), m_(delta, 0.5f)), delta, rdelta);
         if (rgb[0] == mx) hsv[0] = s_(d[2], d[1]);
         else if (rgb[1] == mx) hsv[0] = s_(a_(1.0f / 3.0f, d[0]), d[2]);
         else if (rgb[2] == mx) hsv[0] = s_(a_(2.0f / 3.0f, d[1]), d[0]);
@@ -180,16 +182,32 @@ __global__ void __launch_bounds__(kThreads) ortho_kernel(const tp::OrthoLaunch L
     const int NQ = W / 4;
     // t / NQ by a multiply-high with ceil(2^32 / NQ): exact for t < 2^20 and NQ <= 4096
     const uint32_t nq_magic = 0xFFFFFFFFu / (uint32_t)NQ + 1u;
+    __shared__ int skip;
     for (;;) {
         if (threadIdx.x == 0) {
             unit = atomicAdd(L.counter, 1);
+            skip = 0;
             if (unit < L.njobs) {
                 const int pj = L.jobs[unit].parent_job;
+#ifdef TP_DEBUG
+                // debug builds: the job's indexes before any of them addresses memory
+                const tp_ortho_job &J = L.jobs[unit];
+                const bool ok = J.out_slot >= 0 && J.out_slot < L.cap && J.level >= 0 && J.level <= 30 &&
+                                (J.level == 0 || (J.parent_slot >= 0 && J.parent_slot < L.cap)) &&
+                                (J.residual_slot < 0 || J.residual_slot < L.res_cap) && pj >= -1 && pj < unit &&
+                                J.noise_layer >= 0 && J.noise_layer < 6 && J.noise_rot >= 0 && J.noise_rot < 4;
+                if (!ok) {
+                    report(L.status, TP_E_BOUNDS);
+                    skip = 1;
+                }
+                if (pj >= 0 && ok) {
+#else
                 if (pj >= 0) {
+#endif
                     unsigned k = 0;
                     while (ld_acquire(L.done + pj) < 1) {
                         if (++k > kDepLimit) {
-                            report(TP_E_TIMEOUT);
+                            report(L.status, TP_E_TIMEOUT);
                             break;
                         }
                         __nanosleep(64);
@@ -201,6 +219,14 @@ __global__ void __launch_bounds__(kThreads) ortho_kernel(const tp::OrthoLaunch L
         __syncthreads();
         const int u = unit;
         if (u >= L.njobs) break;
+        if (skip) {  // debug builds: a job that failed its checks counts as done, unproduced
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                __threadfence();
+                atomicAdd(L.done + u, 1);
+            }
+            continue;
+        }
         const tp_ortho_job J = L.jobs[u];
         const bool has_parent = J.level > 0;
         const bool has_res = J.residual_slot >= 0;

@@ -44,6 +44,58 @@ extern "C" int tp_device_available(void)
 }
 
 // ---------------------------------------------------------------- storage
+namespace {
+// Debug builds put a guard region of a fixed byte before and after every storage's
+// slots; release builds none.
+#ifdef TP_DEBUG
+constexpr size_t kGuardBytes = 65536;
+#else
+constexpr size_t kGuardBytes = 0;
+#endif
+constexpr int kGuardByte = 0xA5;
+}  // namespace
+
+extern "C" int tp_build_is_debug(void)
+{
+#ifdef TP_DEBUG
+    return 1;
+#else
+    return 0;
+#endif
+}
+
+extern "C" int tp_storage_check_guards(const tp_storage *s)
+{
+    if (!s) return tp::fail(TP_E_BAD_ARG, "tp_storage_check_guards: storage is NULL");
+    if (!kGuardBytes || !s->alloc) return TP_OK;
+    const size_t bytes = sizeof(float) * (size_t)s->slot_stride * s->capacity;
+    std::string g(2 * kGuardBytes, '\0');
+    cudaError_t e = cudaMemcpy(&g[0], s->alloc, kGuardBytes, cudaMemcpyDefault);
+    if (e == cudaSuccess)
+        e = cudaMemcpy(&g[kGuardBytes], reinterpret_cast<const char *>(s->base) + bytes, kGuardBytes, cudaMemcpyDefault);
+    if (e != cudaSuccess) return tp::cuda_fail("tp_storage_check_guards", e);
+    for (size_t i = 0; i < g.size(); ++i)
+        if ((unsigned char)g[i] != kGuardByte) {
+            char buf[160];
+            snprintf(buf, sizeof buf, "tp_storage_check_guards: guard byte %zu %s the slots was overwritten",
+                     i < kGuardBytes ? kGuardBytes - i : i - kGuardBytes + 1, i < kGuardBytes ? "before" : "after");
+            return tp::fail(TP_E_BOUNDS, buf);
+        }
+    return TP_OK;
+}
+
+extern "C" int tp_debug_check_capacity(tp_storage *s, int capacity)
+{
+#ifdef TP_DEBUG
+    if (!s || capacity < 0 || capacity > s->capacity) return tp::fail(TP_E_BAD_ARG, "tp_debug_check_capacity: bad arguments");
+    s->check_cap = capacity;
+    return TP_OK;
+#else
+    (void)s;
+    (void)capacity;
+    return tp::fail(TP_E_BAD_ARG, "tp_debug_check_capacity: debug builds only");
+#endif
+}
 extern "C" int tp_storage_create(int tile_width, int channels, int capacity, int on_device, tp_storage **out)
 {
     if (!out) return tp::fail(TP_E_BAD_ARG, "tp_storage_create: out is NULL");
@@ -62,15 +114,28 @@ extern "C" int tp_storage_create(int tile_width, int channels, int capacity, int
     s->on_device = on_device;
     size_t bytes = sizeof(float) * (size_t)s->slot_stride * capacity;
     if (on_device != 2) {
-        cudaError_t e = on_device == 1 ? cudaMalloc(&s->base, bytes) : cudaMallocHost(&s->base, bytes);
+        const size_t total = bytes + 2 * kGuardBytes;
+        void *p = nullptr;
+        cudaError_t e = on_device == 1 ? cudaMalloc(&p, total) : cudaMallocHost(&p, total);
         if (e != cudaSuccess) {
             delete s;
             return tp::cuda_fail("tp_storage_create: allocation", e);
         }
-        e = on_device == 1 ? cudaMemset(s->base, 0, bytes) : (std::memset(s->base, 0, bytes), cudaSuccess);
+        s->alloc = static_cast<float *>(p);
+        s->base = s->alloc + kGuardBytes / sizeof(float);
+        if (on_device == 1) {
+            e = cudaMemset(s->base, 0, bytes);
+            if (e == cudaSuccess && kGuardBytes) e = cudaMemset(s->alloc, kGuardByte, kGuardBytes);
+            if (e == cudaSuccess && kGuardBytes)
+                e = cudaMemset(reinterpret_cast<char *>(s->base) + bytes, kGuardByte, kGuardBytes);
+        } else {
+            std::memset(s->base, 0, bytes);
+            std::memset(s->alloc, kGuardByte, kGuardBytes);
+            std::memset(reinterpret_cast<char *>(s->base) + bytes, kGuardByte, kGuardBytes);
+        }
         if (e != cudaSuccess) {
-            if (on_device == 1) cudaFree(s->base);
-            else cudaFreeHost(s->base);
+            if (on_device == 1) cudaFree(s->alloc);
+            else cudaFreeHost(s->alloc);
             delete s;
             return tp::cuda_fail("tp_storage_create: memset", e);
         }
@@ -85,9 +150,9 @@ extern "C" int tp_storage_create(int tile_width, int channels, int capacity, int
 extern "C" int tp_storage_destroy(tp_storage *s)
 {
     if (!s) return TP_OK;
-    if (s->base) {
-        if (s->on_device == 1) cudaFree(s->base);
-        else if (s->on_device == 0) cudaFreeHost(s->base);
+    if (s->alloc) {
+        if (s->on_device == 1) cudaFree(s->alloc);
+        else if (s->on_device == 0) cudaFreeHost(s->alloc);
     }
     if (s->batch_frame) tp_frame_destroy(s->batch_frame);
     if (s->staging) cudaFree(s->staging);

@@ -10,7 +10,7 @@ import numpy as np
 
 from ._lib import (ElevParams, HostTiles, LAYER_FN, LayerJob, LayerMesh, OrthoJob, OrthoParams, TileJob, TPError, check, lib, LIB_PATH, RESIDUAL_SOURCE,  # noqa: F401
                    TP_OK, TP_E_BAD_ARG, TP_E_CACHE_FULL, TP_E_MISSING_PARENT,
-                   TP_E_TIMEOUT, TP_E_CUDA, TP_E_IO, TP_E_NO_DEVICE)
+                   TP_E_TIMEOUT, TP_E_CUDA, TP_E_IO, TP_E_NO_DEVICE, TP_E_BOUNDS)
 
 ZF, ZC, ZM = 0, 1, 2      # planes of an elevation slot (the reference's RGB32F texel)
 NX, NY = 0, 1             # planes of a normal slot (format 2)

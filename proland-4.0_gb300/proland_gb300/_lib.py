@@ -7,7 +7,9 @@ import ctypes as C
 import os
 
 PKG_ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-LIB_PATH = os.path.join(PKG_ROOT, "lib", "libproland_gb300.so")
+# PROLAND_GB300_DEBUG=1 selects the debug build (device-side bounds checks, storage guards)
+DEBUG = os.environ.get("PROLAND_GB300_DEBUG", "0") == "1"
+LIB_PATH = os.path.join(PKG_ROOT, "lib", "libproland_gb300_debug.so" if DEBUG else "libproland_gb300.so")
 
 TP_OK = 0
 TP_E_BAD_ARG = -1
@@ -17,11 +19,12 @@ TP_E_TIMEOUT = -4
 TP_E_CUDA = -5
 TP_E_IO = -6
 TP_E_NO_DEVICE = -7
+TP_E_BOUNDS = -8
 
 ERROR_NAMES = {
     TP_E_BAD_ARG: "TP_E_BAD_ARG", TP_E_CACHE_FULL: "TP_E_CACHE_FULL",
     TP_E_MISSING_PARENT: "TP_E_MISSING_PARENT", TP_E_TIMEOUT: "TP_E_TIMEOUT",
-    TP_E_CUDA: "TP_E_CUDA", TP_E_IO: "TP_E_IO", TP_E_NO_DEVICE: "TP_E_NO_DEVICE",
+    TP_E_CUDA: "TP_E_CUDA", TP_E_IO: "TP_E_IO", TP_E_NO_DEVICE: "TP_E_NO_DEVICE", TP_E_BOUNDS: "TP_E_BOUNDS",
 }
 
 
@@ -106,6 +109,9 @@ def lib():
     sig = {
         "tp_last_error": ([], C.c_char_p),
         "tp_version": ([], _i),
+        "tp_build_is_debug": ([], _i),
+        "tp_storage_check_guards": ([_vp], _i),
+        "tp_debug_check_capacity": ([_vp, _i], _i),
         "tp_device_available": ([], _i),
         "tp_storage_create": ([_i, _i, _i, _i, C.POINTER(_vp)], _i),
         "tp_storage_destroy": ([_vp], _i),
