@@ -542,33 +542,41 @@ def ortho_section(tp, torch, stream, sh, args):
     return out
 
 
-def layers_section(tp, torch, stream, sh, args):
-    """Elevation layer pass (tp_elevation_layers): 4096 produced 101-wide tiles, each
-    crossed by two roads of the road elevation layer (3-point polylines, widths 5-40 m,
-    on 1000 m tiles: strips of ~290 triangles, built by layers.road_strip), drawn and
-    blended into zm (graph1 blend).  A pass uploads its meshes from host memory, then
-    runs one CTA per tile; CUDA events on the stream around whole passes."""
-    import oracle
-    from proland_gb300 import layers
-    W, n = 101, 4096
-    rng = np.random.default_rng(args.seed + 5)
-    zf = (rng.standard_normal((64, W, W)) * 200.0).astype(np.float32)
-    zm = np.maximum(zf, np.float32(0.0))
+def water_meshes(layers, rng, W, size=1000.0):
+    """One tile of the water elevation layer (layers.water_layer): a lake of 9 points
+    with a 6-point island (filled under the odd winding rule, both boundaries drawn),
+    a crossing curve under NOTEQUAL and a 3-point river with caps under LESS."""
+    def ring(cx, cy, r, n):
+        ang = np.sort(rng.uniform(0, 2 * np.pi, n))
+        rad = r * rng.uniform(0.6, 1.0, n)
+        return np.column_stack([cx + rad * np.cos(ang), cy + rad * np.sin(ang)])
+    outer = ring(size * rng.uniform(0.3, 0.7), size * rng.uniform(0.3, 0.7), size * 0.3, 9)
+    island = ring(outer[:, 0].mean(), outer[:, 1].mean(), size * 0.06, 6)
+    curves = [([(-100.0, size * rng.uniform(0, 1)), (size + 100.0, size * rng.uniform(0, 1))],
+               rng.uniform(0, 50, 2), float(rng.uniform(10, 60)))]
+    river = ([(size * rng.uniform(-0.1, 1.1), -50.0), (size * rng.uniform(0.2, 0.8), size * rng.uniform(0.3, 0.7)),
+              (size * rng.uniform(-0.1, 1.1), size + 50.0)], rng.uniform(-20, 80, 3), float(rng.uniform(8, 40)),
+             True, True)
+    ms = layers.water_layer((0.0, 0.0), size, W, areas=[[outer, island]],
+                            boundaries=[(np.vstack([outer, outer[:1]]), 1), (np.vstack([island, island[:1]]), 0)],
+                            curves=curves, rivers=[river])
+    return [(v, ix, mode, i == 0, prog, state, fd) for i, (v, ix, mode, prog, state, fd) in enumerate(ms)]
+
+
+def layer_pass_case(tp, torch, stream, sh, oracle, W, zf, zm, tiles, what):
+    """One layer workload: parity of a sample against the oracle, then passes timed
+    with CUDA events on the stream, meshes resident on the device and uploaded from
+    pinned host memory."""
+    n = len(tiles)
     elev = tp.TileStorage(W, 3, n)
-    pick = np.arange(n) % 64
+    pick = np.arange(n) % len(zf)
     elev.upload(0, tp.ZF, zf[pick], sh)
-    tiles = []
-    for k in range(n):
-        ms = []
-        for r in range(2):
-            a, b = rng.uniform(-200, 1200, 2), rng.uniform(-200, 1200, 2)
-            mid = (a + b) / 2 + rng.uniform(-150, 150, 2)
-            v = layers.road_strip([a, mid, b], rng.uniform(0, 300, 3), float(rng.uniform(5, 40)), (0.0, 0.0),
-                                  1000.0, W)
-            ms.append((v, None, tp.TRIANGLE_STRIP, r == 0))
-        tiles.append((k, ms))
     batch = tp.LayerBatch(tiles)
-    ntri = sum(max(v.shape[0] - 2, 0) for _, ms in tiles for v, _, _, _ in ms)
+    ntri = 0
+    for _, ms in tiles:
+        for m in ms:
+            cnt = len(m[1]) if m[1] is not None else len(m[0])
+            ntri += cnt // 3 if m[2] == tp.TRIANGLES else max(cnt - 2, 0)
     # parity on a sample: one pass over fresh zm planes
     elev.upload(0, tp.ZM, zm[pick], sh)
     batch.run(elev, 0, sh)
@@ -596,17 +604,48 @@ def layers_section(tp, torch, stream, sh, args):
         return e0.elapsed_time(e1) / steps
     ms_dev = timed(lambda: batch.run_device(elev, 0, sh))
     ms_host = timed(lambda: batch.run(elev, 0, sh))
-    mesh_bytes = batch.n_vertices * 16
-    out = {"workload": "layer pass over %d produced 101x101 tiles, 2 road strips each (%d triangles)" % (n, ntri),
+    out = {"workload": "layer pass over %d produced %dx%d tiles, %s (%d triangles)" % (n, W, W, what, ntri),
            "tiles_per_s": n / (ms_dev / 1000.0), "triangles_per_s": ntri / (ms_dev / 1000.0),
            "ms_per_pass": ms_dev, "pass": "meshes resident on the device (tp_elevation_layers_device)",
            "host_meshes": {"ms_per_pass": ms_host, "tiles_per_s": n / (ms_host / 1000.0),
-                           "mesh_bytes_uploaded_per_pass": mesh_bytes,
+                           "mesh_bytes_uploaded_per_pass": batch.n_vertices * 16 + batch.n_indices * 4,
                            "pass": "meshes in pinned host memory, uploaded by each pass (tp_elevation_layers)"},
            "steps": 10, "texel_bytes_per_tile": 12 * W * W,
            "identical_to_oracle_on_sample": ok,
            "cpu_single_thread_oracle_tiles_per_s": cpu_rate}
     elev.close()
+    return out
+
+
+def layers_section(tp, torch, stream, sh, args):
+    """Elevation layer passes (tp_elevation_layers) over 4096 produced 101-wide tiles,
+    blended into zm (graph1 blend): the road layer, two roads per tile (3-point
+    polylines, widths 5-40 m, on 1000 m tiles: strips of ~290 triangles, built by
+    layers.road_strip); and the water layer (layers.water_layer: lake fill and
+    boundaries under ALWAYS, a curve under NOTEQUAL, a river with caps under LESS;
+    256 distinct tiles, repeated).  A pass uploads its meshes from host memory, then
+    runs one CTA per tile; CUDA events on the stream around whole passes."""
+    import oracle
+    from proland_gb300 import layers
+    W, n = 101, 4096
+    rng = np.random.default_rng(args.seed + 5)
+    zf = (rng.standard_normal((64, W, W)) * 200.0).astype(np.float32)
+    zm = np.maximum(zf, np.float32(0.0))
+    tiles = []
+    for k in range(n):
+        ms = []
+        for r in range(2):
+            a, b = rng.uniform(-200, 1200, 2), rng.uniform(-200, 1200, 2)
+            mid = (a + b) / 2 + rng.uniform(-150, 150, 2)
+            v = layers.road_strip([a, mid, b], rng.uniform(0, 300, 3), float(rng.uniform(5, 40)), (0.0, 0.0),
+                                  1000.0, W)
+            ms.append((v, None, tp.TRIANGLE_STRIP, r == 0))
+        tiles.append((k, ms))
+    out = layer_pass_case(tp, torch, stream, sh, oracle, W, zf, zm, tiles, "2 road strips each")
+    distinct = [water_meshes(layers, rng, W) for _ in range(256)]
+    out["water"] = layer_pass_case(tp, torch, stream, sh, oracle, W, zf, zm,
+                                   [(k, distinct[k % 256]) for k in range(n)],
+                                   "the water layer's passes (lake, island, curve, capped river)")
     return out
 
 

@@ -388,25 +388,52 @@ int tp_sphere_frame(double root_quad_size, int level, int tx, int ty, float *out
 /* ------------------------------------------------------------------------
  * Elevation layers: the TileLayer draws over produced elevation tiles and the
  * blend pass that folds them into zm (ElevationProducer.cpp:383-399: layers drawn
- * under a LESS depth test into the tile's framebuffer, then blendShader).
- * Supported layer: the road elevation layer (graph/.../dem/RoadElevationLayer.cpp:
- * 388-437 with graph1/roadLayerElevationShader.glsl): a depth clear, then triangle
- * meshes whose vertices are (x, y, altitude, u) -- x, y in the tile's clip
- * coordinates ([-1, 1] spans the W x W texels), u the signed road-width coordinate,
- * as ElevationGraphLayer::drawCurveAltitude builds them (ElevationGraphLayer.cpp:
- * 82-380).  A fragment at d = |u| writes z = altitude + 0.03 (1 - smoothstep(0.98,
- * 1, d)) and w = smoothstep(1, 2, d) at depth 0.1 d + 0.3.  The blend then sets zm
- * to zf min(w, 1) + z (1 - min(w, 1)) (blend_mode 0: graph1/edit3/river1
- * blendShader.glsl) or to the 3x3 box filter of that value, clamped at the tile
- * edge (blend_mode 1: demo/shaders/elevation/blendShader.glsl).  zf and zc are not
- * changed.  Rasterisation: window coordinates snapped to 1/256 texel, a texel is
+ * into the tile's framebuffer, which holds (zf, zc, zm, w = 0) with depth 1 after
+ * the upsample, then blendShader).  The blend sets zm to zf min(w, 1) + z (1 -
+ * min(w, 1)) (blend_mode 0: graph1/edit3/river1 blendShader.glsl) or to the 3x3 box
+ * filter of that value, clamped at the tile edge (blend_mode 1:
+ * demo/shaders/elevation/blendShader.glsl).  zf and zc are not changed (the layers
+ * mask them).
+ *
+ * Meshes are triangles whose vertices are (x, y, a, u) -- x, y in the tile's clip
+ * coordinates ([-1, 1] spans the W x W texels), a and u the two interpolated
+ * attributes -- drawn in order, each with a fragment program and a pass state:
+ *  - TP_LAYER_ROAD, the road elevation layer (RoadElevationLayer.cpp:388-437 with
+ *    graph1/roadLayerElevationShader.glsl): a = altitude, u = signed road-width
+ *    coordinate, as ElevationGraphLayer::drawCurveAltitude builds them
+ *    (ElevationGraphLayer.cpp:82-380).  At d = |u|: z = a + 0.03 (1 - smoothstep(0.98,
+ *    1, d)), w = smoothstep(1, 2, d), depth 0.1 d + 0.3.
+ *  - TP_LAYER_WATER, _WATER_RIVER, _WATER_LARGE, the water elevation layer
+ *    (WaterElevationLayer.cpp:240-350 with river1/waterLayerElevationShader.glsl,
+ *    uniform river = 0, 1, 2): a = st.x, u = st.y, d = |u|; z = a (river 0) or
+ *    (a - 1) + max(d - 1, 0); w = smoothstep(1, 2, d); depth 0.1 d + 0.3 (river 0),
+ *    0.1 d + 0.15 (river 1) or 1 (river 2).
+ *  - TP_LAYER_FILL (river1/fillShader.glsl): z = a, w = u (the colour's blue and
+ *    alpha: give every vertex the same two values), depth fill_depth.
+ * Fragment depths are clamped to [0, 1].  The pass state (tp_layer_mesh.state) is a
+ * depth test (TP_DEPTH_LESS, _ALWAYS, _NOTEQUAL against the stored depth) and write
+ * masks (TP_NO_DEPTH_WRITE, TP_NO_Z_WRITE, TP_NO_W_WRITE), as the layers set them
+ * with setDepthTest / setDepthMask / setColorMask; 0 is the road layer's (LESS,
+ * depth, z and w written).  NOTEQUAL with depth writes is refused (TP_E_BAD_ARG).
+ * clear_depth clears the depth buffer to 1 before its mesh (the layers' fb->clear of
+ * depth).  Rasterisation: window coordinates snapped to 1/256 texel, a texel is
  * covered when its centre is inside the triangle (top-left rule for centres on an
  * edge, y up), attributes interpolated at the texel centre as a0 + (a1 - a0) l1 +
- * (a2 - a0) l2 from the barycentric weights l_k, fp32 depth,
- * triangles drawn in order; vertices beyond 32768 texels of the tile's origin drop
- * their triangle. */
+ * (a2 - a0) l2 from the barycentric weights l_k, fp32 depth, triangles drawn in
+ * order; vertices beyond 32768 texels of the tile's origin drop their triangle. */
 #define TP_TRIANGLES 0
 #define TP_TRIANGLE_STRIP 1
+#define TP_LAYER_ROAD 0
+#define TP_LAYER_WATER 1
+#define TP_LAYER_WATER_RIVER 2
+#define TP_LAYER_WATER_LARGE 3
+#define TP_LAYER_FILL 4
+#define TP_DEPTH_LESS 0
+#define TP_DEPTH_ALWAYS 1
+#define TP_DEPTH_NOTEQUAL 2
+#define TP_NO_DEPTH_WRITE 4
+#define TP_NO_Z_WRITE 8
+#define TP_NO_W_WRITE 16
 typedef struct {
     int32_t first_vertex;  /* first vertex of the mesh in the call's vertex array */
     int32_t count;         /* vertices drawn (not indexed) or indices drawn (indexed) */
@@ -414,7 +441,9 @@ typedef struct {
                               Indices count from first_vertex. */
     int32_t mode;          /* TP_TRIANGLES or TP_TRIANGLE_STRIP */
     int32_t clear_depth;   /* 1: the depth buffer is cleared to 1 before this mesh (a new layer) */
-    int32_t reserved[3];
+    int32_t program;       /* TP_LAYER_* fragment program */
+    int32_t state;         /* TP_DEPTH_* test | TP_NO_* write masks */
+    float fill_depth;      /* the depth TP_LAYER_FILL writes */
 } tp_layer_mesh;
 typedef struct {
     int32_t slot;          /* elevation slot (zf, zc, zm) whose zm the layers change */
@@ -446,6 +475,10 @@ int tp_elevation_layers_device(tp_storage *elev, const tp_layer_job *jobs, int n
 typedef struct tp_layer_builder tp_layer_builder;
 int tp_layer_builder_add_mesh(tp_layer_builder *b, const float *vertices, int n_vertices, const uint32_t *indices,
                               int n_indices, int mode);
+/* The fragment program and pass state of the meshes a callback adds next (the
+ * program choice and the setDepthTest / setDepthMask / setColorMask calls of a layer's
+ * doCreateTile); each callback starts with the road layer's (TP_LAYER_ROAD, 0, 0). */
+int tp_layer_builder_set_pass(tp_layer_builder *b, int program, int state, float fill_depth);
 typedef int (*tp_layer_fn)(void *user, int level, int tx, int ty, tp_layer_builder *b);
 int tp_elevation_producer_add_layer(tp_producer *p, tp_layer_fn fn, void *user);
 int tp_elevation_producer_set_blend(tp_producer *p, int blend_mode);

@@ -62,7 +62,7 @@ class OrthoJob(C.Structure):
 
 class LayerMesh(C.Structure):
     _fields_ = [("first_vertex", C.c_int), ("count", C.c_int), ("first_index", C.c_int), ("mode", C.c_int),
-                ("clear_depth", C.c_int)]
+                ("clear_depth", C.c_int), ("program", C.c_int), ("state", C.c_int), ("fill_depth", C.c_float)]
 
 
 def lib():
@@ -192,13 +192,15 @@ def ortho_tile(W, level, tx, ty, parent, residual, noise_layer, noise_rot, noise
 
 def layer_tile(W, zf, zm, meshes, blend_mode=0):
     """zm of one elevation tile after its layers (or_layer_tile): meshes is a list of
-    (vertices [n, 4] (x, y, altitude, u) in clip coordinates, indices or None, mode
-    (0 triangles, 1 strip), clear_depth)."""
+    (vertices [n, 4] (x, y, a, u) in clip coordinates, indices or None, mode
+    (0 triangles, 1 strip), clear_depth[, program, state, fill_depth])."""
     verts, idx, ms = [], [], []
     nv = ni = 0
-    for v, ix, mode, clear in meshes:
+    for mesh in meshes:
+        v, ix, mode, clear = mesh[:4]
+        program, state, fill_depth = tuple(mesh[4:]) if len(mesh) > 4 else (0, 0, 0.0)
         v = np.ascontiguousarray(v, np.float32).reshape(-1, 4)
-        m = LayerMesh(nv, v.shape[0], -1, mode, int(clear))
+        m = LayerMesh(nv, v.shape[0], -1, mode, int(clear), int(program), int(state), float(fill_depth))
         if ix is not None:
             ix = np.ascontiguousarray(ix, np.uint32)
             m.first_index, m.count = ni, ix.size

@@ -11,6 +11,10 @@
  *  - the road elevation layer: src/graph/sources/proland/dem/RoadElevationLayer.cpp:388-437
  *    (depth cleared, colour mask z and w) with
  *    src/graph/examples/graph1/roadLayerElevationShader.glsl (fragment z, w, depth);
+ *  - the water elevation layer: src/graph/sources/proland/dem/WaterElevationLayer.cpp:
+ *    240-350 (its passes' depth tests, depth and colour masks) with
+ *    src/river/examples/river1/waterLayerElevationShader.glsl (river = 0, 1, 2) and
+ *    src/river/examples/river1/fillShader.glsl;
  *  - the blend programs: src/graph/examples/graph1/blendShader.glsl (mode 0) and
  *    src/demo/shaders/elevation/blendShader.glsl (mode 1, 3x3 box filter, texture
  *    reads clamped to the edge).
@@ -21,8 +25,9 @@
  * integer edge functions, centres on an edge covered for top and left edges only (y
  * up, counter-clockwise after reordering), attributes interpolated as
  * a0 + (a1 - a0) l1 + (a2 - a0) l2 with l_k = e_k / (2 area) in float (a constant
- * attribute stays exact), fp32 depth, triangles in
- * draw order (GL's strip order (k+1, k, k+2) for odd k).  Parity with the GL path
+ * attribute stays exact), fp32 depth clamped to [0, 1], triangles and their fragments
+ * in draw order (GL's strip order (k+1, k, k+2) for odd k), each fragment tested
+ * against the depth stored at its texel and written through the masks.  Parity with the GL path
  * is unpinned: the reference has no fixture for it.
  */
 #include "oracle.h"
@@ -55,9 +60,41 @@ static long long edge(int xa, int ya, int xb, int yb, int px, int py)
     return (long long)(xb - xa) * (long long)(py - ya) - (long long)(yb - ya) * (long long)(px - xa);
 }
 
-static void draw_triangle(int W, const float *v0, const float *v1, const float *v2, float *z, float *w, float *depth)
+static float clamp01(float x) { return fminf(fmaxf(x, 0.0f), 1.0f); }
+
+/* depth, z and w of a fragment of a mesh's program at attributes (a, u) */
+static void fragment_program(const or_layer_mesh *M, float a, float u, float *dp, float *z, float *w)
 {
-    int X[3], Y[3];
+    const float d = fabsf(u);
+    switch (M->program) {
+    case 0: /* roadLayerElevationShader */
+        *z = a + 0.03f * (1.0f - smoothstep_f(0.98f, 1.0f, d));
+        *w = smoothstep_f(1.0f, 2.0f, d);
+        *dp = clamp01(d * 0.1f + 0.3f);
+        break;
+    case 4: /* fillShader: the colour's blue and alpha, the depth uniform */
+        *z = a;
+        *w = u;
+        *dp = clamp01(M->fill_depth);
+        break;
+    default: { /* waterLayerElevationShader, river = program - 1 */
+        const int river = M->program - 1;
+        float zz = a;
+        if (river != 0) {
+            const float e = d - 1.0f;
+            zz = (zz - 1.0f) + (e > 0.0f ? e : 0.0f);
+        }
+        *z = zz;
+        *w = smoothstep_f(1.0f, 2.0f, d);
+        *dp = river == 2 ? 1.0f : river == 1 ? clamp01(d * 0.1f + 0.15f) : clamp01(d * 0.1f + 0.3f);
+        break;
+    }
+    }
+}
+
+static void draw_triangle(int W, const or_layer_mesh *M, const float *v0, const float *v1, const float *v2, float *z,
+                          float *w, float *depth)
+{    int X[3], Y[3];
     float alt[3], u[3];
     const float *v[3] = {v0, v1, v2};
     for (int q = 0; q < 3; ++q) {
@@ -106,15 +143,15 @@ static void draw_triangle(int W, const float *v0, const float *v1, const float *
             const float l1 = (float)e[1] / area, l2 = (float)e[2] / area;
             const float a = alt[0] + (alt[1] - alt[0]) * l1 + (alt[2] - alt[0]) * l2;
             const float uu = u[0] + (u[1] - u[0]) * l1 + (u[2] - u[0]) * l2;
-            const float d = fabsf(uu);
-            float dp = d * 0.1f + 0.3f;
-            if (dp < 0.0f) dp = 0.0f;
-            if (dp > 1.0f) dp = 1.0f;
+            float dp, fz, fw;
+            fragment_program(M, a, uu, &dp, &fz, &fw);
             const int p = j * W + i;
-            if (!(dp < depth[p])) continue;   /* LESS */
-            depth[p] = dp;
-            z[p] = a + 0.03f * (1.0f - smoothstep_f(0.98f, 1.0f, d));
-            w[p] = smoothstep_f(1.0f, 2.0f, d);
+            const int test = M->state & 3;
+            if (test == 0 && !(dp < depth[p])) continue;   /* LESS */
+            if (test == 2 && !(dp != depth[p])) continue;  /* NOTEQUAL */
+            if (!(M->state & 4)) depth[p] = dp;
+            if (!(M->state & 8)) z[p] = fz;
+            if (!(M->state & 16)) w[p] = fw;
         }
 }
 
@@ -152,7 +189,7 @@ void or_layer_tile(int W, const float *zf, const float *zm, const or_layer_mesh 
                 const int vi = M->first_index >= 0 ? (int)indices[M->first_index + c[q]] : c[q];
                 v[q] = vertices + 4 * (size_t)(M->first_vertex + vi);
             }
-            draw_triangle(W, v[0], v[1], v[2], z, w, depth);
+            draw_triangle(W, M, v[0], v[1], v[2], z, w, depth);
         }
     }
     for (size_t p = 0; p < N; ++p) {

@@ -164,14 +164,18 @@ void or_ortho_noise(int W, uint8_t *out);
 void or_ortho_tile(const or_ortho_job *t);
 int  or_ortho_tile_id(int level, int tx, int ty);   /* OrthoCPUProducer.cpp:250-253 */
 
-/* ---- elevation layers (layers.c): road layer meshes drawn into one tile and
- * blended into zm (ElevationProducer.cpp:378-399, RoadElevationLayer.cpp:388-437,
- * graph1/roadLayerElevationShader.glsl, graph1 and demo blendShader.glsl).
- * Vertices are (x, y, altitude, u) in clip coordinates; indices count from the
- * mesh's first vertex; mode 0 triangles, 1 triangle strip.  zf, zm, zm_out are
- * dense W x W. ---- */
+/* ---- elevation layers (layers.c): road and water layer meshes drawn into one
+ * tile and blended into zm (ElevationProducer.cpp:378-399, RoadElevationLayer.cpp:
+ * 388-437, WaterElevationLayer.cpp:240-350, graph1/roadLayerElevationShader.glsl,
+ * river1/waterLayerElevationShader.glsl and fillShader.glsl, graph1 and demo
+ * blendShader.glsl).  Vertices are (x, y, a, u) in clip coordinates; indices count
+ * from the mesh's first vertex; mode 0 triangles, 1 triangle strip; program 0 road,
+ * 1-3 water with river = 0-2, 4 fill; state: depth test in bits 0-1 (0 LESS, 1
+ * ALWAYS, 2 NOTEQUAL), 4 no depth write, 8 no z write, 16 no w write.  zf, zm,
+ * zm_out are dense W x W. ---- */
 typedef struct {
-    int first_vertex, count, first_index, mode, clear_depth;
+    int first_vertex, count, first_index, mode, clear_depth, program, state;
+    float fill_depth;
 } or_layer_mesh;
 void or_layer_tile(int W, const float *zf, const float *zm, const or_layer_mesh *meshes, int n_meshes,
                    const float *vertices, const uint32_t *indices, int blend_mode, float *zm_out);

@@ -154,6 +154,8 @@ struct tp_layer_builder {
     std::vector<float> vertices;
     std::vector<uint32_t> indices;
     bool layer_start = false;  // the next mesh is the first of a layer: it clears the depth buffer
+    int program = TP_LAYER_ROAD, state = 0;  // the next meshes' fragment program and pass state
+    float fill_depth = 0.0f;
 };
 
 namespace {
@@ -634,10 +636,24 @@ extern "C" int tp_layer_builder_add_mesh(tp_layer_builder *b, const float *verti
     m.first_index = n_indices > 0 ? (int32_t)b->indices.size() : -1;
     m.mode = mode;
     m.clear_depth = b->layer_start ? 1 : 0;
+    m.program = b->program;
+    m.state = b->state;
+    m.fill_depth = b->fill_depth;
     b->layer_start = false;
     b->vertices.insert(b->vertices.end(), vertices, vertices + 4 * (size_t)n_vertices);
     b->indices.insert(b->indices.end(), indices, indices + n_indices);
     b->meshes.push_back(m);
+    return TP_OK;
+}
+
+extern "C" int tp_layer_builder_set_pass(tp_layer_builder *b, int program, int state, float fill_depth)
+{
+    if (!b) return tp::fail(TP_E_BAD_ARG, "tp_layer_builder_set_pass: bad arguments");
+    const int rc = tp::check_layer_pass(program, state, fill_depth, "tp_layer_builder_set_pass");
+    if (rc) return rc;
+    b->program = program;
+    b->state = state;
+    b->fill_depth = fill_depth;
     return TP_OK;
 }
 
@@ -951,6 +967,9 @@ int run_layers(tp_producer *e, const std::vector<tp_tile *> &tiles, void *stream
         jobs[k] = tp_layer_job{t->slot, (int32_t)b.meshes.size(), 0, 0};
         for (const auto &l : e->layers) {
             b.layer_start = true;
+            b.program = TP_LAYER_ROAD;
+            b.state = 0;
+            b.fill_depth = 0.0f;
             if (l.first(l.second, t->level, t->tx, t->ty, &b) != 0)
                 return tp::fail(TP_E_BAD_ARG, "elevation layer callback failed");
         }

@@ -148,6 +148,9 @@ int read_status(int *status, bool clear);
 // The device address of the status word (kernels of other files report through it).
 int status_device_ptr(int **out);
 // The capacity a storage's device-side checks use (debug builds).
+// A layer mesh's fragment program, pass state and fill depth (tp_layer_mesh), checked
+// by tp_elevation_layers and tp_layer_builder_set_pass: TP_OK or TP_E_BAD_ARG.
+int check_layer_pass(int program, int state, float fill_depth, const char *who);
 inline int checked_capacity(const tp_storage *s) { return s ? (s->check_cap > 0 ? s->check_cap : s->capacity) : 0; }
 // One plane copy of repack_planes: `count` tiles of `rows` rows of `width` floats.
 struct PlaneXfer {

@@ -191,22 +191,31 @@ class HostPipeline:
 
 # ---------------------------------------------------------------- elevation layers
 TRIANGLES, TRIANGLE_STRIP = 0, 1
+# fragment programs: the road layer's, the water layer's with river = 0, 1, 2, the fill
+LAYER_ROAD, LAYER_WATER, LAYER_WATER_RIVER, LAYER_WATER_LARGE, LAYER_FILL = 0, 1, 2, 3, 4
+# pass state: a depth test and write masks (0: LESS, depth, z and w written)
+DEPTH_LESS, DEPTH_ALWAYS, DEPTH_NOTEQUAL = 0, 1, 2
+NO_DEPTH_WRITE, NO_Z_WRITE, NO_W_WRITE = 4, 8, 16
 
 
 class LayerBatch:
     """The meshes of a layer pass, packed once for tp_elevation_layers.  tiles: list of
-    (slot, meshes), meshes a list of (vertices [n, 4] float32 (x, y, altitude, u) in
-    clip coordinates, indices or None, mode, clear_depth)."""
+    (slot, meshes), meshes a list of (vertices [n, 4] float32 (x, y, a, u) in clip
+    coordinates, indices or None, mode, clear_depth[, program, state, fill_depth]);
+    without the last three, the road layer's program and state."""
 
     def __init__(self, tiles):
         verts, idx, meshes, jobs = [], [], [], []
         nv = ni = 0
         for slot, ms in tiles:
             jobs.append(LayerJob(slot, len(meshes), len(ms), 0))
-            for v, ix, mode, clear in ms:
+            for mesh in ms:
+                v, ix, mode, clear = mesh[:4]
+                program, state, fill_depth = tuple(mesh[4:]) if len(mesh) > 4 else (LAYER_ROAD, 0, 0.0)
                 v = np.ascontiguousarray(v, np.float32).reshape(-1, 4)
                 m = LayerMesh()
                 m.first_vertex, m.mode, m.clear_depth = nv, mode, int(clear)
+                m.program, m.state, m.fill_depth = int(program), int(state), float(fill_depth)
                 if ix is None:
                     m.first_index, m.count = -1, v.shape[0]
                 else:
@@ -253,8 +262,8 @@ class LayerBatch:
 
 
 def elevation_layers(elev, tiles, blend_mode=0, stream=None):
-    """Road layer meshes drawn into produced elevation tiles and blended into zm
-    (tp_elevation_layers); tiles as for LayerBatch."""
+    """Road and water layer meshes drawn into produced elevation tiles and blended
+    into zm (tp_elevation_layers); tiles as for LayerBatch."""
     LayerBatch(tiles).run(elev, blend_mode, stream)
 
 
@@ -626,12 +635,17 @@ class ElevationProducer(TileProducer):
         self._layers = []
 
     def add_layer(self, fn):
-        """TileProducer::addLayer with a road elevation layer: fn(level, tx, ty) returns
-        the meshes it draws on that tile, a list of (vertices [n, 4] float32, indices or
-        None, mode) -- see elevation_layers."""
+        """TileProducer::addLayer with a road or water elevation layer: fn(level, tx, ty)
+        returns the meshes it draws on that tile, a list of (vertices [n, 4] float32,
+        indices or None, mode[, program, state, fill_depth]) -- see elevation_layers."""
         def cb(user, level, tx, ty, builder):
             try:
-                for verts, idx, mode in fn(level, tx, ty):
+                for mesh in fn(level, tx, ty):
+                    verts, idx, mode = mesh[:3]
+                    program, state, fill_depth = tuple(mesh[3:]) if len(mesh) > 3 else (LAYER_ROAD, 0, 0.0)
+                    rc = lib().tp_layer_builder_set_pass(builder, int(program), int(state), float(fill_depth))
+                    if rc:
+                        return rc
                     v = np.ascontiguousarray(verts, np.float32).reshape(-1, 4)
                     ix = None if idx is None else np.ascontiguousarray(idx, np.uint32)
                     rc = lib().tp_layer_builder_add_mesh(builder, v.ctypes.data, v.shape[0],

@@ -81,7 +81,8 @@ class HostTiles(C.Structure):
 class LayerMesh(C.Structure):
     """tp_layer_mesh"""
     _fields_ = [("first_vertex", C.c_int32), ("count", C.c_int32), ("first_index", C.c_int32),
-                ("mode", C.c_int32), ("clear_depth", C.c_int32), ("reserved", C.c_int32 * 3)]
+                ("mode", C.c_int32), ("clear_depth", C.c_int32), ("program", C.c_int32), ("state", C.c_int32),
+                ("fill_depth", C.c_float)]
 
 
 class LayerJob(C.Structure):
@@ -235,6 +236,7 @@ def lib():
         "tp_elevation_layers_device": ([_vp, C.POINTER(LayerJob), _i, C.POINTER(LayerMesh), _i, _vp, _i, _vp, _i,
                                         _i, _vp], _i),
         "tp_layer_builder_add_mesh": ([_vp, _vp, _i, _vp, _i, _i], _i),
+        "tp_layer_builder_set_pass": ([_vp, _i, _i, C.c_float], _i),
         "tp_elevation_producer_add_layer": ([_vp, LAYER_FN, _vp], _i),
         "tp_elevation_producer_set_blend": ([_vp, _i], _i),
         "tp_learned_predict_residuals": ([_vp, _vp, C.POINTER(TileJob), _i, _vp, _vp], _i),
