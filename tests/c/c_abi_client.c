@@ -33,6 +33,8 @@ int main(int argc, char **argv)
         return 2;
     }
     CHECK(tp_version() > 0, "version");
+    CHECK(tp_layer_builder_set_pass(NULL, TP_LAYER_FILL, TP_DEPTH_ALWAYS | TP_NO_Z_WRITE, 0.02f) == TP_E_BAD_ARG,
+          "layer pass state needs a builder");
 
     /* createDemNoise and createOrthoNoise tables */
     float *dem = malloc(sizeof(float) * 6 * 101 * 101);
