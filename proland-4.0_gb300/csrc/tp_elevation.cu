@@ -261,8 +261,13 @@ __device__ __forceinline__ void issue_lattice(const tp::ClassLaunch &c, int job,
 // All threads: produce unit (job, band) from `stage` (its copies complete).
 // MOD: the class uses the slope/curvature-modulated noise (a separate kernel
 // instantiation keeps its 4x4 neighbourhood out of the common path's registers).
+// `release` (the job's completion counter, or null when no job of the launch waits
+// on another): incremented once the band's elevation rows are written, before the
+// normal phase -- a child reads only its parent's zf and zm, so it can start while
+// the parent forms its normals.
 template <bool MOD>
-__device__ __forceinline__ void compute_unit(const tp::ClassLaunch &c, int job, int band, float *stage)
+__device__ __forceinline__ void compute_unit(const tp::ClassLaunch &c, int job, int band, float *stage,
+                                             int *release)
 {
     const tp_tile_job J = c.jobs[job];
     const int W = c.W, n = W - 5, PE = c.pitch, g = c.g, gs = c.gshift;
@@ -502,7 +507,12 @@ __device__ __forceinline__ void compute_unit(const tp::ClassLaunch &c, int job, 
             else strip(F_{}, F_{});
         }
     }
+    if (release) fence_proxy_async_global();  // our generic-proxy writes before a child's TMA reads
     __syncthreads();
+    if (release && threadIdx.x == 0) {
+        __threadfence();
+        atomicAdd(release, 1);  // release: this band's elevation rows are complete
+    }
 
     // ---- phase B: normals of rows jn in [max(j0, 2), min(j1, W - 2)), one warp per row
     if (c.nrm != nullptr && J.normal_slot >= 0) {
@@ -617,13 +627,9 @@ frame_kernel(const __grid_constant__ CUtensorMap pmap, const __grid_constant__ C
             for (int t = threadIdx.x; t < c.buf_floats; t += kThreads) stage[t] = 0.0f;
             __syncthreads();
         }
-        if (!x.skip) compute_unit<MOD>(c, x.job, x.band, stage);
-        if (f.any_deps) fence_proxy_async_global();
-        __syncthreads();  // the stage is free again; all of this unit's stores are issued
-        if (f.any_deps && threadIdx.x == 0) {
-            __threadfence();
-            atomicAdd(c.done + x.job, 1);  // release: this band of the tile is complete
-        }
+        if (!x.skip) compute_unit<MOD>(c, x.job, x.band, stage, f.any_deps ? c.done + x.job : nullptr);
+        __syncthreads();  // the stage is free again
+        if (x.skip && f.any_deps && threadIdx.x == 0) atomicAdd(c.done + x.job, 1);  // a skipped unit is complete
     }
     cp_async_wait_all();
 }
@@ -714,14 +720,9 @@ frame_kernel2(const __grid_constant__ CUtensorMap pmap, const __grid_constant__ 
             for (int t = threadIdx.x; t < c.buf_floats; t += kThreads) scur[t] = 0.0f;
             __syncthreads();
         }
-        compute_unit<MOD>(c, x.job, x.band, scur);
-        if (f.any_deps) fence_proxy_async_global();
+        compute_unit<MOD>(c, x.job, x.band, scur, f.any_deps ? c.done + x.job : nullptr);
         __syncthreads();
         if (threadIdx.x == 0) {
-            if (f.any_deps) {
-                __threadfence();
-                atomicAdd(c.done + x.job, 1);  // release: this band of the tile is complete
-            }
             if (y_valid && !y_issued) {
                 issue_copies(c, &pmap, &rmap, info[nxt].job, info[nxt].band, snxt, &bars[nxt]);
                 issued[nxt] = 1;
