@@ -165,7 +165,9 @@ TKey key_of(const tp_producer *p, int level, int tx, int ty) { return TKey(p->id
 void release_deps(tp_tile *t);
 
 // Drops a tile that is being recycled: its queued production is cancelled.
-void forget_tile(tp_tile *t, tp_producer *owner)
+// A recycled tile that was still queued (acquired, then released before its
+// production ran) leaves its producer's queue and releases what it had acquired.
+void unqueue_tile(tp_tile *t, tp_producer *owner)
 {
     if (t->queued && owner) {
         auto &q = owner->queue;
@@ -173,7 +175,6 @@ void forget_tile(tp_tile *t, tp_producer *owner)
         t->queued = false;
         release_deps(t);
     }
-    delete t;
 }
 
 }  // namespace
@@ -216,25 +217,32 @@ tp_tile *get_tile(tp_producer *p, int level, int tx, int ty, int *users_before, 
         ++c->queries;
         int slot = tp_storage_new_slot(c->storage);
         if (slot < 0 && c->lru_head) {
-            // recycle the least recently used unused tile's slot
+            // recycle the least recently used unused tile: its slot, its record and its
+            // hash-table node (re-keyed in place: no allocation per new tile)
             tp_tile *old = c->lru_head;
             c->lru_unlink(old);
-            c->tiles.erase(TKey(old->producer_id, old->level, old->tx, old->ty));
+            auto node = c->tiles.extract(TKey(old->producer_id, old->level, old->tx, old->ty));
             slot = old->slot;
-            forget_tile(old, tp::producer_by_id(old->producer_id));
+            if (old->queued) unqueue_tile(old, tp::producer_by_id(old->producer_id));
+            *old = tp_tile{};
+            t = old;
+            node.key() = k;
+            c->tiles.insert(std::move(node));
         }
         if (slot < 0) {
             if (err) *err = tp::fail(TP_E_CACHE_FULL, "Insufficient tile cache size (" + c->name + ")");
             return nullptr;
         }
         ++c->misses;
-        t = new tp_tile;
+        if (!t) {
+            t = new tp_tile;
+            c->tiles.emplace(k, t);
+        }
         t->producer_id = p->id;
         t->level = level;
         t->tx = tx;
         t->ty = ty;
         t->slot = slot;
-        c->tiles.emplace(k, t);
     }
     if (users_before) *users_before = t->users;
     t->users += 1;
@@ -425,6 +433,7 @@ extern "C" int tp_cache_create(tp_storage *storage, const char *name, tp_cache *
     auto *c = new tp_cache;
     c->storage = storage;
     c->name = name ? name : "";
+    c->tiles.reserve((size_t)storage->capacity);  // one entry per slot at most: no rehash
     *out = c;
     return TP_OK;
 }
@@ -1439,7 +1448,9 @@ struct tp_sampler {
     };
     std::vector<tp_producer *> producers;
     std::vector<Quad> held;                        // dense: released quads swap with the last one
-    std::unordered_map<uint64_t, uint32_t> index;  // quad key -> position in `held`
+    using Index = std::unordered_map<uint64_t, uint32_t>;
+    Index index;                                   // quad key -> position in `held`
+    std::vector<Index::node_type> spare;           // nodes of released quads, re-keyed for new ones
     uint32_t frame = 0;
     std::vector<tp_tile_req> fresh;  // the last update's new quads
 };
@@ -1457,7 +1468,8 @@ void sampler_drop(tp_sampler *s, size_t pos, bool cancel)
         put_tile(s->producers[p], q.tiles[p]);
         if (cancel) cancel_orphan(s->producers[p], q.tiles[p]);
     }
-    s->index.erase(q.key);
+    auto node = s->index.extract(q.key);
+    if (!node.empty()) s->spare.push_back(std::move(node));
     if (pos + 1 != s->held.size()) {
         q = s->held.back();
         s->index[q.key] = (uint32_t)pos;
@@ -1535,7 +1547,15 @@ extern "C" int tp_sampler_update(tp_sampler *s, const tp_tile_req *reqs, int n, 
                 }
                 break;
             }
-            s->index.emplace(k, (uint32_t)s->held.size());
+            if (!s->spare.empty()) {
+                auto node = std::move(s->spare.back());
+                s->spare.pop_back();
+                node.key() = k;
+                node.mapped() = (uint32_t)s->held.size();
+                s->index.insert(std::move(node));
+            } else {
+                s->index.emplace(k, (uint32_t)s->held.size());
+            }
             s->held.push_back(q);
             s->fresh.push_back(r);
         }
