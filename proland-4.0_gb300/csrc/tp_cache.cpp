@@ -52,6 +52,83 @@ struct TKeyHash {
     }
 };
 
+// The cache's tiles by key: open addressing with linear probing, the keys held in
+// the table itself (one cache line touched per lookup in the common case instead of
+// a bucket array and a list node), a power-of-two capacity of at least twice the
+// entries, deletion by backward shift (no tombstones).
+template <class V>
+class TileTable {
+public:
+    void reserve(size_t n)
+    {
+        size_t cap = 16;
+        while (cap < 2 * n) cap <<= 1;
+        if (cap > slots_.size()) rehash(cap);
+    }
+    size_t size() const { return size_; }
+    V *find(const TKey &k) const
+    {
+        if (slots_.empty()) return nullptr;
+        for (size_t i = TKeyHash()(k) & mask_;; i = (i + 1) & mask_) {
+            const Slot &e = slots_[i];
+            if (!e.v) return nullptr;
+            if (e.k == k) return e.v;
+        }
+    }
+    void insert(const TKey &k, V *v)  // k is not in the table
+    {
+        if (2 * (size_ + 1) > slots_.size()) rehash(slots_.empty() ? 16 : 2 * slots_.size());
+        size_t i = TKeyHash()(k) & mask_;
+        while (slots_[i].v) i = (i + 1) & mask_;
+        slots_[i] = Slot{k, v};
+        ++size_;
+    }
+    void erase(const TKey &k)
+    {
+        if (slots_.empty()) return;
+        size_t i = TKeyHash()(k) & mask_;
+        for (;; i = (i + 1) & mask_) {
+            if (!slots_[i].v) return;
+            if (slots_[i].k == k) break;
+        }
+        // backward shift: move later entries of the probe run into the hole when their
+        // home position does not lie cyclically in (hole, their position]
+        size_t hole = i;
+        for (size_t j = (i + 1) & mask_; slots_[j].v; j = (j + 1) & mask_) {
+            const size_t home = TKeyHash()(slots_[j].k) & mask_;
+            const bool stays = hole <= j ? (home > hole && home <= j) : (home > hole || home <= j);
+            if (stays) continue;
+            slots_[hole] = slots_[j];
+            hole = j;
+        }
+        slots_[hole] = Slot{TKey(0, 0, 0, 0), nullptr};
+        --size_;
+    }
+    template <class F>
+    void for_each(F f) const
+    {
+        for (const Slot &e : slots_)
+            if (e.v) f(e.v);
+    }
+
+private:
+    struct Slot {
+        TKey k;
+        V *v;
+    };
+    void rehash(size_t cap)
+    {
+        std::vector<Slot> old(cap, Slot{TKey(0, 0, 0, 0), nullptr});
+        old.swap(slots_);
+        mask_ = cap - 1;
+        size_ = 0;
+        for (const Slot &e : old)
+            if (e.v) insert(e.k, e.v);
+    }
+    std::vector<Slot> slots_;
+    size_t mask_ = 0, size_ = 0;
+};
+
 int next_producer_id()
 {
     static std::mutex mu;
@@ -82,7 +159,7 @@ struct tp_cache {
     std::string name;
     std::recursive_mutex mu;
     // every tile holding a slot: used (users > 0) or unused (users == 0, in the LRU list)
-    std::unordered_map<TKey, tp_tile *, TKeyHash> tiles;
+    TileTable<tp_tile> tiles;
     tp_tile *lru_head = nullptr, *lru_tail = nullptr;
     int n_unused = 0;
     long long queries = 0, misses = 0;
@@ -206,9 +283,7 @@ tp_tile *get_tile(tp_producer *p, int level, int tx, int ty, int *users_before, 
     std::lock_guard<std::recursive_mutex> lk(c->mu);
     const TKey k = key_of(p, level, tx, ty);
     tp_tile *t = nullptr;
-    auto u = c->tiles.find(k);
-    if (u != c->tiles.end()) {
-        t = u->second;
+    if ((t = c->tiles.find(k)) != nullptr) {
         if (t->users == 0) {
             ++c->queries;
             c->lru_unlink(t);  // an unused tile in the cache: used again
@@ -217,17 +292,16 @@ tp_tile *get_tile(tp_producer *p, int level, int tx, int ty, int *users_before, 
         ++c->queries;
         int slot = tp_storage_new_slot(c->storage);
         if (slot < 0 && c->lru_head) {
-            // recycle the least recently used unused tile: its slot, its record and its
-            // hash-table node (re-keyed in place: no allocation per new tile)
+            // recycle the least recently used unused tile: its slot and its record (no
+            // allocation per new tile)
             tp_tile *old = c->lru_head;
             c->lru_unlink(old);
-            auto node = c->tiles.extract(TKey(old->producer_id, old->level, old->tx, old->ty));
+            c->tiles.erase(TKey(old->producer_id, old->level, old->tx, old->ty));
             slot = old->slot;
             if (old->queued) unqueue_tile(old, tp::producer_by_id(old->producer_id));
             *old = tp_tile{};
             t = old;
-            node.key() = k;
-            c->tiles.insert(std::move(node));
+            c->tiles.insert(k, t);
         }
         if (slot < 0) {
             if (err) *err = tp::fail(TP_E_CACHE_FULL, "Insufficient tile cache size (" + c->name + ")");
@@ -236,7 +310,7 @@ tp_tile *get_tile(tp_producer *p, int level, int tx, int ty, int *users_before, 
         ++c->misses;
         if (!t) {
             t = new tp_tile;
-            c->tiles.emplace(k, t);
+            c->tiles.insert(k, t);
         }
         t->producer_id = p->id;
         t->level = level;
@@ -441,7 +515,7 @@ extern "C" int tp_cache_create(tp_storage *storage, const char *name, tp_cache *
 extern "C" int tp_cache_destroy(tp_cache *c)
 {
     if (!c) return TP_OK;
-    for (auto &kv : c->tiles) delete kv.second;
+    c->tiles.for_each([](tp_tile *t) { delete t; });
     delete c;
     return TP_OK;
 }
@@ -743,9 +817,8 @@ extern "C" tp_tile *tp_producer_find_tile(tp_producer *p, int level, int tx, int
     tp_cache *c = p->cache;
     std::lock_guard<std::recursive_mutex> lk(c->mu);
     const TKey k = key_of(p, level, tx, ty);
-    tp_tile *t = nullptr;
-    auto u = c->tiles.find(k);
-    if (u != c->tiles.end() && (u->second->users > 0 || include_cache)) t = u->second;
+    tp_tile *t = c->tiles.find(k);
+    if (t && !(t->users > 0 || include_cache)) t = nullptr;
     if (t && done && !t->done) t = nullptr;
     return t;
 }
@@ -767,7 +840,7 @@ extern "C" int tp_producer_prefetch_tile(tp_producer *p, int level, int tx, int 
     tp_cache *c = p->cache;
     std::lock_guard<std::recursive_mutex> lk(c->mu);
     const TKey k = key_of(p, level, tx, ty);
-    if (c->tiles.count(k)) return 0;
+    if (c->tiles.find(k)) return 0;
     int err = TP_OK;
     tp_tile *t = get_tile(p, level, tx, ty, nullptr, &err);
     if (!t) return err == TP_E_CACHE_FULL ? 0 : err;
@@ -784,8 +857,9 @@ extern "C" int tp_producer_invalidate_tiles(tp_producer *p)
     std::lock_guard<std::recursive_mutex> lk(c->mu);
     // collected first: scheduling acquires tiles, which changes the table
     std::vector<tp_tile *> mine;
-    for (auto &kv : c->tiles)
-        if (kv.second->producer_id == p->id && kv.second->users > 0) mine.push_back(kv.second);
+    c->tiles.for_each([&](tp_tile *t) {
+        if (t->producer_id == p->id && t->users > 0) mine.push_back(t);
+    });
     std::sort(mine.begin(), mine.end(), [](const tp_tile *x, const tp_tile *y) {
         return std::make_tuple(x->level, x->ty, x->tx) < std::make_tuple(y->level, y->ty, y->tx);
     });

@@ -129,3 +129,55 @@ def test_bad_arguments(product):
         e.prefetch_tile(-1, 0, 0)
     with pytest.raises(tp.TPError):
         tp.NormalProducer(ec, e)         # 3-channel cache: not a normal cache
+
+
+def test_random_operations_match_a_model(product):
+    """A long random sequence of getTile / putTile on a small cache (many evictions,
+    re-used keys, tiles evicted while still queued) against a model of TileCache's
+    semantics: users counts, the LRU order of unused tiles, recycling the oldest
+    unused tile when no slot is free, NULL when every tile is used."""
+    import random
+    tp = product
+    cap = 24
+    rs = tp.TileStorage(101, 1, cap, on_device=BOOK)
+    rc = tp.TileCache(rs, "residuals")
+    r = tp.ResidualProducer(rc)
+    rng = random.Random(7)
+    keys = [(l, x, y) for l in (3, 4) for x in range(6) for y in range(6)]
+    users, lru, held = {}, [], []      # model: key -> users; unused keys, oldest first
+    for step in range(4000):
+        if held and (rng.random() < 0.45 or len(held) >= cap):
+            t, key = held.pop(rng.randrange(len(held)))
+            left = r.put_tile(t)
+            users[key] -= 1
+            assert left == users[key]
+            if users[key] == 0:
+                lru.append(key)
+        else:
+            key = rng.choice(keys)
+            t = r.get_tile(*key)
+            if key in users:
+                if users[key] == 0:
+                    lru.remove(key)
+                users[key] += 1
+            elif len(users) < cap:
+                users[key] = 1
+            elif lru:
+                del users[lru.pop(0)]          # the oldest unused tile gives its slot
+                users[key] = 1
+            else:
+                assert t is None
+                continue
+            assert t is not None and t.info()["users"] == users[key], (step, key)
+            held.append((t, key))
+        if step % 97 == 0:
+            assert rc.get_used_tiles() == sum(1 for u in users.values() if u > 0)
+            assert rc.get_unused_tiles() == len(lru)
+            for k in keys:
+                f = r.find_tile(*k, include_cache=True)
+                assert (f is not None) == (k in users), (step, k)
+                if f is not None:
+                    assert f.info()["users"] == users[k]
+    for t, _ in held:
+        r.put_tile(t)
+    assert rc.get_used_tiles() == 0
