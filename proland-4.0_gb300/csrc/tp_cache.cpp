@@ -1513,6 +1513,82 @@ extern "C" int tp_create_tile(tp_producer *p, int level, int tx, int ty, tp_tile
 // new quads' tiles acquired (getTile, in request order: parents first; producers in
 // the order given) and all produced by one scheduler run, so that normal tiles of
 // new elevation tiles are fused into the elevation launch.
+// A sampler's quads by key (uint64 -> position in its dense array): the same open
+// addressing as the tiles' table, the empty mark a position of all ones.
+class QuadIndex {
+public:
+    void reserve(size_t n)
+    {
+        size_t cap = 16;
+        while (cap < 2 * n) cap <<= 1;
+        if (cap > slots_.size()) rehash(cap);
+    }
+    uint32_t *find(uint64_t k)
+    {
+        if (slots_.empty()) return nullptr;
+        for (size_t i = hash(k) & mask_;; i = (i + 1) & mask_) {
+            Slot &e = slots_[i];
+            if (e.v == kEmpty) return nullptr;
+            if (e.k == k) return &e.v;
+        }
+    }
+    const uint32_t *find(uint64_t k) const { return const_cast<QuadIndex *>(this)->find(k); }
+    void insert(uint64_t k, uint32_t v)  // k is not in the index
+    {
+        if (2 * (size_ + 1) > slots_.size()) rehash(slots_.empty() ? 16 : 2 * slots_.size());
+        size_t i = hash(k) & mask_;
+        while (slots_[i].v != kEmpty) i = (i + 1) & mask_;
+        slots_[i] = Slot{k, v};
+        ++size_;
+    }
+    void erase(uint64_t k)
+    {
+        if (slots_.empty()) return;
+        size_t i = hash(k) & mask_;
+        for (;; i = (i + 1) & mask_) {
+            if (slots_[i].v == kEmpty) return;
+            if (slots_[i].k == k) break;
+        }
+        size_t hole = i;
+        for (size_t j = (i + 1) & mask_; slots_[j].v != kEmpty; j = (j + 1) & mask_) {
+            const size_t home = hash(slots_[j].k) & mask_;
+            const bool stays = hole <= j ? (home > hole && home <= j) : (home > hole || home <= j);
+            if (stays) continue;
+            slots_[hole] = slots_[j];
+            hole = j;
+        }
+        slots_[hole] = Slot{0, kEmpty};
+        --size_;
+    }
+
+private:
+    static constexpr uint32_t kEmpty = 0xFFFFFFFFu;
+    struct Slot {
+        uint64_t k;
+        uint32_t v;
+    };
+    static size_t hash(uint64_t x)
+    {
+        x ^= x >> 31;
+        x *= 0xbf58476d1ce4e5b9ull;
+        x ^= x >> 29;
+        x *= 0x94d049bb133111ebull;
+        x ^= x >> 32;
+        return (size_t)x;
+    }
+    void rehash(size_t cap)
+    {
+        std::vector<Slot> old(cap, Slot{0, kEmpty});
+        old.swap(slots_);
+        mask_ = cap - 1;
+        size_ = 0;
+        for (const Slot &e : old)
+            if (e.v != kEmpty) insert(e.k, e.v);
+    }
+    std::vector<Slot> slots_;
+    size_t mask_ = 0, size_ = 0;
+};
+
 struct tp_sampler {
     static constexpr int kMaxProducers = 8;
     struct Quad {
@@ -1522,9 +1598,7 @@ struct tp_sampler {
     };
     std::vector<tp_producer *> producers;
     std::vector<Quad> held;                        // dense: released quads swap with the last one
-    using Index = std::unordered_map<uint64_t, uint32_t>;
-    Index index;                                   // quad key -> position in `held`
-    std::vector<Index::node_type> spare;           // nodes of released quads, re-keyed for new ones
+    QuadIndex index;                               // quad key -> position in `held`
     uint32_t frame = 0;
     std::vector<tp_tile_req> fresh;  // the last update's new quads
 };
@@ -1542,11 +1616,10 @@ void sampler_drop(tp_sampler *s, size_t pos, bool cancel)
         put_tile(s->producers[p], q.tiles[p]);
         if (cancel) cancel_orphan(s->producers[p], q.tiles[p]);
     }
-    auto node = s->index.extract(q.key);
-    if (!node.empty()) s->spare.push_back(std::move(node));
+    s->index.erase(q.key);
     if (pos + 1 != s->held.size()) {
         q = s->held.back();
-        s->index[q.key] = (uint32_t)pos;
+        *s->index.find(q.key) = (uint32_t)pos;
     }
     s->held.pop_back();
 }
@@ -1589,8 +1662,8 @@ extern "C" int tp_sampler_update(tp_sampler *s, const tp_tile_req *reqs, int n, 
         // first, so that their slots can take the new tiles
         tp::TraceScope ts("sampler release", tp::kPhSamplerRelease);
         for (int i = 0; i < n; ++i) {
-            auto it = s->index.find(req_key(reqs[i].level, reqs[i].tx, reqs[i].ty));
-            if (it != s->index.end()) s->held[it->second].stamp = frame;
+            const uint32_t *at = s->index.find(req_key(reqs[i].level, reqs[i].tx, reqs[i].ty));
+            if (at) s->held[*at].stamp = frame;
             else fresh_idx.push_back(i);
         }
         for (size_t pos = s->held.size(); pos-- > 0;)
@@ -1604,7 +1677,7 @@ extern "C" int tp_sampler_update(tp_sampler *s, const tp_tile_req *reqs, int n, 
         for (int i : fresh_idx) {
             const tp_tile_req &r = reqs[i];
             const uint64_t k = req_key(r.level, r.tx, r.ty);
-            if (s->index.count(k)) continue;  // requested twice
+            if (s->index.find(k)) continue;  // requested twice
             tp_sampler::Quad q;
             q.key = k;
             q.stamp = frame;
@@ -1621,15 +1694,7 @@ extern "C" int tp_sampler_update(tp_sampler *s, const tp_tile_req *reqs, int n, 
                 }
                 break;
             }
-            if (!s->spare.empty()) {
-                auto node = std::move(s->spare.back());
-                s->spare.pop_back();
-                node.key() = k;
-                node.mapped() = (uint32_t)s->held.size();
-                s->index.insert(std::move(node));
-            } else {
-                s->index.emplace(k, (uint32_t)s->held.size());
-            }
+            s->index.insert(k, (uint32_t)s->held.size());
             s->held.push_back(q);
             s->fresh.push_back(r);
         }
@@ -1660,8 +1725,8 @@ extern "C" tp_tile *tp_sampler_find(const tp_sampler *s, int producer, int level
 {
     if (!s || producer < 0 || producer >= (int)s->producers.size() || level < 0 || level > 29 || tx < 0 || ty < 0)
         return nullptr;
-    auto it = s->index.find(req_key(level, tx, ty));
-    return it == s->index.end() ? nullptr : s->held[it->second].tiles[producer];
+    const uint32_t *at = s->index.find(req_key(level, tx, ty));
+    return at ? s->held[*at].tiles[producer] : nullptr;
 }
 
 extern "C" int tp_sphere_frame(double root_quad_size, int level, int tx, int ty, float *out47)

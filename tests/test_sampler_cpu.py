@@ -78,3 +78,34 @@ def test_synthetic_residuals_host_match_oracle(product):
     assert not np.array_equal(r.tile(3, 5, 2), r.tile(3, 5, 3))
     assert not np.array_equal(oracle.synthetic_residual(17, 3, 5, 2, 1.0, 101),
                               oracle.synthetic_residual(18, 3, 5, 2, 1.0, 101))
+
+
+def test_sampler_random_updates(product):
+    """Random quadtrees, one update each: the new quads are exactly those not held
+    before (in request order), every requested quad is found afterwards and no other."""
+    import random
+    tp = product
+    rs, rc, r = residual_setup(tp, 512)
+    s = tp.TileSampler(r)
+    rng = random.Random(3)
+    universe = [(l, x, y) for l in range(5) for x in range(1 << l) for y in range(1 << l)]
+    before = set()
+    for step in range(60):
+        req = []
+        for _ in range(rng.randrange(1, 40)):
+            l, x, y = rng.choice(universe)
+            while l >= 0:
+                req.append((l, x, y))
+                l, x, y = l - 1, x // 2, y // 2
+        want_new, seen = [], set()
+        for t in req:
+            if t not in before and t not in seen:
+                want_new.append(t)
+            seen.add(t)
+        assert s.update(req) == want_new, step
+        assert s.held() == len(seen) and rc.get_used_tiles() == len(seen)
+        for t in universe:
+            assert (s.find(*t) is not None) == (t in seen), (step, t)
+        before = seen
+    s.close()
+    assert rc.get_used_tiles() == 0
