@@ -1017,7 +1017,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--requests", type=int, default=4096)
     ap.add_argument("--seed", type=int, default=2024)
-    ap.add_argument("--e2e-steps", type=int, default=5)
+    ap.add_argument("--e2e-steps", type=int, default=30)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default work-unit shapes")
     ap.add_argument("--no-per-width", action="store_true", help="skip the per-width timings")
@@ -1272,6 +1272,8 @@ def main():
                 "path": "tp_elevation_batch_host per tile width (chunks of %s tiles, copies overlapping launches)"
                         % "/".join(str(E2E_CHUNK[fc.W]) for fc in classes),
                 "identical_to_device_run": e2e_check,
+                "step_ms": {"min": min(e2e_ms), "median": float(np.median(e2e_ms)), "max": max(e2e_ms),
+                            "steps": len(e2e_ms)} if e2e_ms else None,
                 "planes": "zf, zc, zm, nx, ny",
                 "zf_and_normals_only": {
                     "value": (world * tiles / (float(np.mean(e2e_min_ms)) / 1000.0)) if e2e_min_ms else None,
