@@ -152,6 +152,10 @@ struct tp_tile {
     tp_producer *dep_input_owner = nullptr;
     // the cache's list of unused tiles (users == 0), least recently used first
     tp_tile *lru_prev = nullptr, *lru_next = nullptr;
+    // while an elevation launch is being built: the tile's job index in it (-1 when it
+    // is not in the launch) and the normal tile whose normals the launch fuses in
+    int job = -1;
+    tp_tile *fused_normal = nullptr;
 };
 
 struct tp_cache {
@@ -1007,8 +1011,9 @@ int run_residuals(tp_producer *r, void *stream)
 
 // The tp_tile_job of an elevation tile; `index` maps tiles of the same launch to
 // their job numbers (a parent found there is named in parent_job).
-int elevation_job(const tp_producer *e, const tp_tile *t, const std::unordered_map<const tp_tile *, int> &index, int normal_slot,
-                  tp_tile_job &j)
+// The job of tile t; a parent in the same launch (its `job` set) becomes the job's
+// parent_job, any other parent must be produced already.
+int elevation_job(const tp_producer *e, const tp_tile *t, int normal_slot, tp_tile_job &j)
 {
     const int n = e->cache->storage->W - 5;
     const int mod = e->residuals ? (e->residuals->cache->storage->W - 5) / n : 1;
@@ -1020,8 +1025,7 @@ int elevation_job(const tp_producer *e, const tp_tile *t, const std::unordered_m
     j.parent_slot = t->dep_parent ? t->dep_parent->slot : -1;
     j.parent_job = -1;
     if (t->dep_parent) {
-        auto it = index.find(t->dep_parent);
-        if (it != index.end()) j.parent_job = it->second;
+        if (t->dep_parent->job >= 0) j.parent_job = t->dep_parent->job;
         else if (!t->dep_parent->done) return tp::fail(TP_E_MISSING_PARENT, "elevation parent tile is not produced");
     }
     j.residual_slot = t->dep_input ? t->dep_input->slot : -1;
@@ -1078,13 +1082,27 @@ int run_elevations(tp_producer *e, tp_producer *normals, void *stream)
     // (flat deformation; spherical normals run in their own kernel afterwards; a
     // producer with layers changes zm after its launch, so its normals come later)
     const bool layered = !e->layers.empty();
-    std::unordered_map<const tp_tile *, tp_tile *> fused;  // elevation tile -> normal tile
+    // marks on the tiles (elevation tile -> its fused normal tile, tile -> job index),
+    // cleared on every way out
+    std::vector<tp_tile *> fused;  // elevation tiles with a fused normal tile
+    std::vector<tp_tile *> q;
+    struct Clear {
+        std::vector<tp_tile *> &f, &q;
+        ~Clear()
+        {
+            for (tp_tile *t : f) t->fused_normal = nullptr;
+            for (tp_tile *t : q) t->job = -1;
+        }
+    } clear_marks{fused, q};
     if (!layered && normals && !normals->deform && normals->normal_format == 2)
         for (tp_tile *nt : normals->queue)
-            if (nt->dep_input && nt->dep_input->queued) fused[nt->dep_input] = nt;
+            if (nt->dep_input && nt->dep_input->queued && !nt->dep_input->fused_normal) {
+                nt->dep_input->fused_normal = nt;
+                fused.push_back(nt->dep_input);
+            }
     if (e->queue.empty()) return TP_OK;
     if (!(e->root_quad_size > 0.0f)) return tp::fail(TP_E_BAD_ARG, "elevation producer: root quad size not set");
-    std::vector<tp_tile *> q = e->queue;
+    q = e->queue;
     std::stable_sort(q.begin(), q.end(), [](const tp_tile *a, const tp_tile *b) { return a->level < b->level; });
     if (!e->frame) tp_frame_create(&e->frame);
     if (layered) {
@@ -1095,9 +1113,8 @@ int run_elevations(tp_producer *e, tp_producer *normals, void *stream)
             size_t k1 = k;
             while (k1 < q.size() && q[k1]->level == q[k]->level) ++k1;
             std::vector<tp_tile *> lvl(q.begin() + k, q.begin() + k1);
-            std::unordered_map<const tp_tile *, int> none;
             std::vector<tp_tile_job> jobs(lvl.size());
-            for (size_t i = 0; i < lvl.size() && rc == TP_OK; ++i) rc = elevation_job(e, lvl[i], none, -1, jobs[i]);
+            for (size_t i = 0; i < lvl.size() && rc == TP_OK; ++i) rc = elevation_job(e, lvl[i], -1, jobs[i]);
             if (rc == TP_OK) {
                 tp_frame_clear(e->frame);
                 rc = tp_frame_add(e->frame, e->cache->storage,
@@ -1118,12 +1135,9 @@ int run_elevations(tp_producer *e, tp_producer *normals, void *stream)
     std::vector<tp_tile_job> jobs(q.size());
     {
         tp::TraceScope ts("elevation jobs", tp::kPhElevJobs);
-        std::unordered_map<const tp_tile *, int> index;
-        index.reserve(q.size() * 2);
-        for (size_t k = 0; k < q.size(); ++k) index[q[k]] = (int)k;
+        for (size_t k = 0; k < q.size(); ++k) q[k]->job = (int)k;
         for (size_t k = 0; k < q.size(); ++k) {
-            auto f = fused.find(q[k]);
-            int rc = elevation_job(e, q[k], index, f != fused.end() ? f->second->slot : -1, jobs[k]);
+            int rc = elevation_job(e, q[k], q[k]->fused_normal ? q[k]->fused_normal->slot : -1, jobs[k]);
             if (rc) return rc;
         }
     }
@@ -1144,12 +1158,9 @@ int run_elevations(tp_producer *e, tp_producer *normals, void *stream)
     finish_tiles(q);
     e->queue.clear();
     if (normals) {
-        std::unordered_set<const tp_tile *> fused_normals;
-        fused_normals.reserve(fused.size() * 2);
-        for (auto &kv : fused) fused_normals.insert(kv.second);
         std::vector<tp_tile *> rest;
         for (tp_tile *nt : normals->queue) {
-            if (fused_normals.count(nt)) {
+            if (nt->dep_input && nt->dep_input->fused_normal == nt) {
                 nt->done = true;
                 nt->queued = false;
                 release_deps(nt);
