@@ -514,54 +514,55 @@ __device__ __forceinline__ void compute_unit(const tp::ClassLaunch &c, int job, 
         atomicAdd(release, 1);  // release: this band's elevation rows are complete
     }
 
-    // ---- phase B: normals of rows jn in [max(j0, 2), min(j1, W - 2)), one warp per row
+    // ---- phase B: normals of rows jn in [max(j0, 2), min(j1, W - 2)): the (row, column
+    // quad) items of the band spread over all threads, so that every lane has a quad
+    // (one warp per row left 7 of 32 lanes idle on a 25-quad row)
     if (c.nrm != nullptr && J.normal_slot >= 0) {
-        const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
         const int Wn = W - 4, NQn = c.nrm_pitch / 4;
         float *onx = c.nrm + (long long)J.normal_slot * c.nrm_slot_stride;
         float *ony = onx + c.nrm_plane_stride;
         const float h2 = __fmul_rn(2.0f, __fdiv_rn(J.tile_meters, (float)n));
         const float hh = h2 * h2;
-        for (int jn = max(j0, 2) + warp; jn < min(j1, W - 2); jn += kWarps) {
+        const int jn0 = max(j0, 2), items = max(min(j1, W - 2) - jn0, 0) * NQn;
+        // idx / NQn by a multiply-high with ceil(2^32 / NQn): exact for 2 <= NQn <= 64 and
+        // idx < 2^16 (rows <= 253 of at most 64 quads)
+        const uint32_t mq = NQn > 1 ? 0xFFFFFFFFu / (uint32_t)NQn + 1u : 0u;
+        for (int idx = threadIdx.x; idx < items; idx += kThreads) {
+            const int r = NQn > 1 ? (int)__umulhi((uint32_t)idx, mq) : idx, m = idx - r * NQn;
+            const int jn = jn0 + r;
             const float *cr = sbuf + (jn - j0 + 1) * PE;
             const float *up = cr + PE, *dn = cr - PE;
-            for (int base = 0; base < NQn; base += 32) {
-                const int m = base + lane;
-                const bool act = m < NQn;
-                // elevation columns b .. b + 7 of the three rows as two aligned 16-byte loads
-                // each (conflict-free); this quad's normals sit at columns b + 2 .. b + 5 and
-                // read b + 1 .. b + 6.  b2 stays inside the row: a quad past the last normal
-                // column (its values unused) reads the row's last 16 bytes instead.
-                const int b = act ? 4 * m : 0, b2 = min(b + 4, PE - 4);
-                const float4 cA = *reinterpret_cast<const float4 *>(cr + b);
-                const float4 cB = *reinterpret_cast<const float4 *>(cr + b2);
-                const float4 uA = *reinterpret_cast<const float4 *>(up + b);
-                const float4 uB = *reinterpret_cast<const float4 *>(up + b2);
-                const float4 dA = *reinterpret_cast<const float4 *>(dn + b);
-                const float4 dB = *reinterpret_cast<const float4 *>(dn + b2);
-                const float zr[6] = {cA.y, cA.z, cA.w, cB.x, cB.y, cB.z};
-                const float zu[4] = {uA.z, uA.w, uB.x, uB.y};
-                const float zd[4] = {dA.z, dA.w, dB.x, dB.y};
-                float nx[4], ny[4];
+            // elevation columns b .. b + 7 of the three rows as two aligned 16-byte loads
+            // each; this quad's normals sit at columns b + 2 .. b + 5 and read b + 1 .. b + 6.
+            // b2 stays inside the row: a quad past the last normal column (its values
+            // unused) reads the row's last 16 bytes instead.
+            const int b = 4 * m, b2 = min(b + 4, PE - 4);
+            const float4 cA = *reinterpret_cast<const float4 *>(cr + b);
+            const float4 cB = *reinterpret_cast<const float4 *>(cr + b2);
+            const float4 uA = *reinterpret_cast<const float4 *>(up + b);
+            const float4 uB = *reinterpret_cast<const float4 *>(up + b2);
+            const float4 dA = *reinterpret_cast<const float4 *>(dn + b);
+            const float4 dB = *reinterpret_cast<const float4 *>(dn + b2);
+            const float zr[6] = {cA.y, cA.z, cA.w, cB.x, cB.y, cB.z};
+            const float zu[4] = {uA.z, uA.w, uB.x, uB.y};
+            const float zd[4] = {dA.z, dA.w, dB.x, dB.y};
+            float nx[4], ny[4];
 #pragma unroll
-                for (int k = 0; k < 4; ++k) {
-                    const float ax = -__fsub_rn(zr[k + 2], zr[k]);
-                    const float ay = -__fsub_rn(zu[k], zd[k]);
-                    const float inv = rsqrtf(ax * ax + ay * ay + hh);
-                    nx[k] = ax * inv;
-                    ny[k] = ay * inv;
-                }
-                if (4 * m + 3 >= Wn) {
-#pragma unroll
-                    for (int k = 0; k < 4; ++k)
-                        if (4 * m + k >= Wn) nx[k] = ny[k] = 0.0f;
-                }
-                if (act) {
-                    const int o = (jn - 2) * c.nrm_pitch + 4 * m;
-                    *reinterpret_cast<float4 *>(onx + o) = make_float4(nx[0], nx[1], nx[2], nx[3]);
-                    *reinterpret_cast<float4 *>(ony + o) = make_float4(ny[0], ny[1], ny[2], ny[3]);
-                }
+            for (int k = 0; k < 4; ++k) {
+                const float ax = -__fsub_rn(zr[k + 2], zr[k]);
+                const float ay = -__fsub_rn(zu[k], zd[k]);
+                const float inv = rsqrtf(ax * ax + ay * ay + hh);
+                nx[k] = ax * inv;
+                ny[k] = ay * inv;
             }
+            if (4 * m + 3 >= Wn) {
+#pragma unroll
+                for (int k = 0; k < 4; ++k)
+                    if (4 * m + k >= Wn) nx[k] = ny[k] = 0.0f;
+            }
+            const int o = (jn - 2) * c.nrm_pitch + 4 * m;
+            *reinterpret_cast<float4 *>(onx + o) = make_float4(nx[0], nx[1], nx[2], nx[3]);
+            *reinterpret_cast<float4 *>(ony + o) = make_float4(ny[0], ny[1], ny[2], ny[3]);
         }
     }
 }
