@@ -227,7 +227,7 @@ __device__ void issue_copies(const tp::ClassLaunch &c, const CUtensorMap *pmap, 
     }
     const int n = c.W - 5;
     const int dx = (J.tx & 1) * (n / 2), dy = (J.ty & 1) * (n / 2);
-    const int j0 = (band * c.W) / c.bands;
+    const int j0 = band * c.band_rows;
     const int ja = max(j0 - 1, 0);
     const bool has_parent = J.level > 0, has_res = J.residual_slot >= 0;
     uint32_t bytes = 0;
@@ -273,7 +273,7 @@ __device__ __forceinline__ void compute_unit(const tp::ClassLaunch &c, int job, 
     const int W = c.W, n = W - 5, PE = c.pitch, g = c.g, gs = c.gshift;
     const int dx = (J.tx & 1) * (n / 2), dy = (J.ty & 1) * (n / 2);
     const bool has_parent = J.level > 0, has_res = J.residual_slot >= 0;
-    const int j0 = (band * W) / c.bands, j1 = ((band + 1) * W) / c.bands;
+    const int j0 = band * c.band_rows, j1 = min(j0 + c.band_rows, W);
     const int ja = max(j0 - 1, 0), jb = min(j1, W - 1);
     const int pr0 = ja / 2 + dy;  // first parent row of the window
     float *sbuf = stage;                        // residual rows, then zm rows

@@ -315,11 +315,12 @@ int tp::class_layout(tp_storage *elev, tp_storage *res, tp_storage *nrm, const t
     L.flip = p->flip ? 1 : 0;
     L.no_clamp = p->no_clamp ? 1 : 0;
     L.noise_mode = p->noise_mode;
-    // band height: whole 101-wide tiles, quarters of 197-wide ones, unless asked
+    // band height: whole 101-wide tiles, quarters of 197-wide ones, unless asked; the
+    // bands are br rows each, the last one the rest
     int br = p->band_rows > 0 ? p->band_rows : (W <= 128 ? W : (W + 3) / 4);
     br = std::min(std::max(br, 8), W);
     L.bands = (W + br - 1) / br;
-    br = (W + L.bands - 1) / L.bands;  // the tallest band actually produced
+    L.band_rows = br;
     if (br + 2 > 256) return bad("band taller than a TMA box");
     const int PE = elev->pitch;
     L.buf_floats = tp::round_up((br + 2) * PE, 32);
@@ -524,6 +525,13 @@ extern "C" int tp_frame_autotune(tp_frame *f, void *stream, int repeats)
         const int W = k.elev->W;
         std::vector<int> bands = W <= 128 ? std::vector<int>{W, (W + 1) / 2, (W + 2) / 3, (W + 3) / 4}
                                           : std::vector<int>{(W + 1) / 2, (W + 2) / 3, (W + 3) / 4, (W + 4) / 5, (W + 5) / 6};
+        // heights whose rows with the two halo rows fill the elevation phase's strips
+        // exactly: strips = 256 threads / column quads, each an even number of rows
+        {
+            const int strips = std::max(1, tp::kFrameThreads / (k.elev->pitch / 4));
+            for (int r = 2 * strips - 2; r <= W / 2; r += 2 * strips)
+                if (r >= 16 && std::find(bands.begin(), bands.end(), r) == bands.end()) bands.push_back(r);
+        }
         const tp_elev_params orig = k.params;
         const int orig_minb = k.minb_override;
         float best = 1e30f;
@@ -564,7 +572,7 @@ extern "C" int tp_frame_config(const tp_frame *f, int klass, int *band_rows, int
 {
     if (!f || klass < 0 || klass >= f->nclasses) return tp::fail(TP_E_BAD_ARG, "tp_frame_config: bad class");
     const auto &k = f->cls[klass];
-    if (band_rows) *band_rows = (k.elev->W + k.L.bands - 1) / k.L.bands;
+    if (band_rows) *band_rows = k.L.band_rows;
     if (stages) *stages = k.params.stages == 2 ? 2 : 1;
     if (ctas_per_sm) {
         const size_t per_cta = sizeof(float) * (size_t)stage_floats_of(k.L) * (k.params.stages == 2 ? 2 : 1) + 128 + 1024;

@@ -103,6 +103,7 @@ struct ClassLaunch {
     const tp_tile_job *jobs;  // device
     int njobs;
     int bands;                // row bands per tile
+    int band_rows;            // rows of every band but the last, which takes the rest
     int *done;                // per-job count of completed bands (device)
     float *elev;
     int W, pitch;
