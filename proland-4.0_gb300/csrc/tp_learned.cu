@@ -152,6 +152,11 @@ __device__ __forceinline__ void load_bf16(const __nv_bfloat16 *base, int img, si
 // the tensor memory), warps 2-5 (one per tensor-memory lane quadrant) run the epilogue.
 constexpr int kRoleThreads = 192;
 constexpr int kConvStages = 3;
+// The first layer of an inference pass makes its input channels itself: a second
+// producer warp (warp 6) takes every other block, so that one block's loads overlap
+// another's arithmetic.
+template <int MODE>
+constexpr int conv_threads() { return MODE == kFirst ? kRoleThreads + 32 : kRoleThreads; }
 
 template <int CIN, int COUT>
 constexpr int conv_smem_bytes()
@@ -163,8 +168,10 @@ constexpr int conv_smem_bytes()
 __device__ __forceinline__ int my_tiles(int total) { return (total - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x; }
 
 template <int CIN, int COUT, int MODE>
-__global__ void __launch_bounds__(kRoleThreads) conv_kernel(const __grid_constant__ CUtensorMap xmap, const ConvLaunch a)
+__global__ void __launch_bounds__(conv_threads<MODE>()) conv_kernel(const __grid_constant__ CUtensorMap xmap,
+                                                                    const ConvLaunch a)
 {
+    constexpr int kThreadsC = conv_threads<MODE>();
     extern __shared__ __align__(1024) uint8_t smem[];
     constexpr int NCG = CIN / 8, KSTEPS = CIN / 16, NMMA = 9 * KSTEPS;
     constexpr int STAGE = NCG * kGroupStride;
@@ -180,9 +187,14 @@ __global__ void __launch_bounds__(kRoleThreads) conv_kernel(const __grid_constan
     float *bias_s = reinterpret_cast<float *>(tslot + 4);  // 16-byte aligned, COUT floats
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 
-    for (int i = tid; i < BBYTES / 16; i += kRoleThreads)
+    for (int i = tid; i < BBYTES / 16; i += kThreadsC)
         reinterpret_cast<uint4 *>(bsm)[i] = reinterpret_cast<const uint4 *>(a.wpack)[i];
     if (tid < COUT) bias_s[tid] = a.bias ? a.bias[tid] : 0.0f;
+    if (MODE == kFirst)  // channels 8-15 of every stage are zero (before any MMA reads a stage)
+        for (int i = tid; i < kConvStages * kHaloX * kHaloY; i += kThreadsC) {
+            const int st = i / (kHaloX * kHaloY), p = i - st * (kHaloX * kHaloY);
+            *reinterpret_cast<uint4 *>(halo + st * STAGE + kGroupStride + p * 16) = make_uint4(0u, 0u, 0u, 0u);
+        }
     if (tid == 0) {
         for (int s = 0; s < kConvStages; ++s) {
             mbar_init(&full[s], 1);
@@ -203,16 +215,13 @@ __global__ void __launch_bounds__(kRoleThreads) conv_kernel(const __grid_constan
     const int per_img = a.tiles_x * a.tiles_y, total = a.nimg * per_img;
     const int mine = my_tiles(total);
 
-    if (MODE == kFirst && warp == 0) {
-        // producer: the input channels of tile i's halo made from the upsampled parent
+    if (MODE == kFirst && (warp == 0 || warp == 6)) {
+        // producers: the input channels of tile i's halo made from the upsampled parent
         // (the values launch_prep writes: (up - mean) / sigma_in, x and y parity, 1, the
         // second differences along x and y over sigma_out; 0 outside the image), written
-        // as bf16 into stage i % kConvStages; channels 8-15 are zero in every stage
-        for (int s = 0; s < kConvStages; ++s)
-            for (int p = lane; p < kHaloX * kHaloY; p += 32)
-                *reinterpret_cast<uint4 *>(halo + s * STAGE + kGroupStride + p * 16) = make_uint4(0u, 0u, 0u, 0u);
-        int i = 0;
-        for (; i < mine; ++i) {
+        // as bf16 into stage i % kConvStages; warp 0 makes the even tiles, warp 6 the odd
+        int i = warp == 0 ? 0 : 1;
+        for (; i < mine; i += 2) {
             const int s = i % kConvStages;
             if (i >= kConvStages &&
                 !__all_sync(0xffffffffu, mbar_wait_abortable(&empty[s], ((i / kConvStages) - 1) & 1, abort)))
@@ -891,9 +900,9 @@ int conv_instance(const ConvLaunch &a, const CUtensorMap *halo, cudaStream_t s)
     if (units <= 0) return TP_OK;
     constexpr int smem = conv_smem_bytes<CIN, COUT>();
     int grid = 0;
-    int rc = grid_for(conv_kernel<CIN, COUT, MODE>, smem, 64, units, &grid);
+    int rc = grid_for(conv_kernel<CIN, COUT, MODE>, smem, 64, units, &grid, conv_threads<MODE>());
     if (rc) return rc;
-    conv_kernel<CIN, COUT, MODE><<<grid, kRoleThreads, smem, s>>>(*halo, a);
+    conv_kernel<CIN, COUT, MODE><<<grid, conv_threads<MODE>(), smem, s>>>(*halo, a);
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? TP_OK : tp::cuda_fail("conv kernel launch", e);
 }
