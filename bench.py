@@ -892,6 +892,7 @@ def learned_section(tp, torch, stream, sh, args, plain_w101):
             net.forward(up, lv, out=out)
         e1.record(stream)
         torch.cuda.synchronize()
+        net.check()
         fwd_ms = e0.elapsed_time(e1) / reps
         # learned-form tiles: residuals predicted into slots, then the elevation kernel
         elev = tp.TileStorage(W, 3, B + 1)

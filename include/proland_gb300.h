@@ -651,9 +651,16 @@ int tp_learned_get_state(tp_learned *net, float *m, float *v, int count, int *st
 int tp_learned_set_state(tp_learned *net, const float *m, const float *v, int count, int step);
 int tp_learned_get_sigmas(tp_learned *net, float *sigma_in, float *sigma_out, int nlevels);
 /* Predicted residuals (metres) into out_dev (may be NULL); training = 1 keeps
- * what tp_learned_backward needs. */
+ * what tp_learned_backward needs.  An inference pass (training = 0) is enqueued on
+ * `stream` and the call returns (the caller orders its reads of out_dev on the
+ * stream); a kernel's failure in it is reported by the next call that synchronises:
+ * tp_learned_check, a training pass, tp_learned_backward, tp_learned_predict_residuals.
+ * A training pass returns once complete.  The net's buffers serve all its passes:
+ * passes issued on different streams must be ordered by the caller. */
 int tp_learned_forward(tp_learned *net, const float *up_dev, const int *levels, int n, int training,
                        float *out_dev, void *stream);
+/* Synchronises `stream` and reports a kernel failure of the net's earlier passes. */
+int tp_learned_check(tp_learned *net, void *stream);
 /* Gradients of the mean squared error (in units of the level sigmas) against
  * target residuals (metres) of the last training forward pass; *loss = that error. */
 int tp_learned_backward(tp_learned *net, const float *target_dev, float *loss, void *stream);

@@ -408,7 +408,15 @@ extern "C" int tp_learned_forward(tp_learned *net, const float *up_dev, const in
     rc = forward(net, n, training != 0, s);
     if (rc) return rc;
     if (out_dev) launch_scale_out(net->pred, net->levels, net->sigma_out, net->W, n, out_dev, s);
-    return check_status(net, s);
+    // an inference pass is left running on the stream (passes in a row overlap their launch
+    // gaps); its kernels' failures are reported by the next call that synchronises
+    return training ? check_status(net, s) : TP_OK;
+}
+
+extern "C" int tp_learned_check(tp_learned *net, void *stream)
+{
+    if (!net) return tp::fail(TP_E_BAD_ARG, "tp_learned_check: bad arguments");
+    return check_status(net, static_cast<cudaStream_t>(stream));
 }
 
 extern "C" int tp_learned_backward(tp_learned *net, const float *target_dev, float *loss, void *stream)

@@ -228,6 +228,7 @@ def lib():
         "tp_learned_set_state": ([_vp, _vp, _vp, _i, _i], _i),
         "tp_learned_get_sigmas": ([_vp, _vp, _vp, _i], _i),
         "tp_learned_forward": ([_vp, _vp, C.POINTER(_i), _i, _i, _vp, _vp], _i),
+        "tp_learned_check": ([_vp, _vp], _i),
         "tp_learned_backward": ([_vp, _vp, _f32p, _vp], _i),
         "tp_learned_adam": ([_vp, C.c_float, _vp], _i),
         "tp_learned_gather": ([_vp, _vp, _vp, _i, C.POINTER(_i), C.POINTER(_i), _i, _vp, _vp, _vp], _i),

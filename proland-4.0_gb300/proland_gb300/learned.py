@@ -232,13 +232,19 @@ class LearnedPredictor:
         check(lib().tp_learned_set_sigmas(self.handle, si.ctypes.data_as(_f32p), so.ctypes.data_as(_f32p), si.size))
 
     def forward(self, up, levels, training=False, out=None):
-        """Residuals (metres) predicted for the upsampled tiles `up` [n, W, W]."""
+        """Residuals (metres) predicted for the upsampled tiles `up` [n, W, W].  An
+        inference pass is enqueued on the current stream (a kernel failure in it is
+        raised by the next synchronising call, e.g. check())."""
         n = up.shape[0]
         lv = (C.c_int * n)(*[int(v) for v in levels])
         if out is None:
             out = torch.empty_like(up)
         check(lib().tp_learned_forward(self.handle, _ptr(up), lv, n, int(training), _ptr(out), _stream()))
         return out
+
+    def check(self):
+        """Waits for the current stream and raises a kernel failure of earlier passes."""
+        check(lib().tp_learned_check(self.handle, _stream()))
 
     def backward(self, target):
         loss = C.c_float()
