@@ -123,6 +123,32 @@ def test_inference_input_channels_made_in_the_first_layer(L, W, n):
     net.close()
 
 
+def test_inference_passes_in_a_row(L):
+    """Inference passes are enqueued without a host synchronisation and share the net's
+    buffers: passes issued back to back on one stream (different inputs, levels and
+    batch sizes) give the results of each pass run alone, and check() reports no
+    failure."""
+    W = 101
+    net = L.LearnedPredictor(tile_width=W, max_batch=64, seed=11)
+    cases = []
+    for k, n in enumerate((64, 17, 40, 64)):
+        levels, up, _, si, so = _case(W, n, seed=200 + k)
+        if k == 0:
+            net.set_sigmas(si, so)
+        cases.append((torch.from_numpy(up).cuda(), levels))
+    alone = []
+    for up_d, levels in cases:
+        alone.append(net.forward(up_d, levels).clone())
+        net.check()
+    outs = [torch.empty_like(up_d) for up_d, _ in cases]
+    for (up_d, levels), out in zip(cases, outs):
+        net.forward(up_d, levels, out=out)
+    net.check()
+    for a, b in zip(alone, outs):
+        assert torch.equal(a, b)
+    net.close()
+
+
 @pytest.mark.parametrize("W,n", [(21, 5), (101, 256), (197, 64)])
 def test_fused_pairs_give_the_per_layer_bits(L, W, n):
     """Inference by fused layer pairs (layers 0 + 1 and 2 + 3 in one launch each, the
