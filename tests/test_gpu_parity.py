@@ -73,9 +73,11 @@ def test_stencil_residual_normals(gpu, oracle_lib, W):
 
 
 @pytest.mark.parametrize("W,band_rows,stages", [(101, 26, 1), (101, 51, 2), (197, 99, 1), (197, 140, 1),
-                                                 (197, 33, 2), (101, 101, 2)])
+                                                 (197, 33, 2), (101, 101, 2), (197, 98, 1), (101, 50, 2),
+                                                 (197, 48, 1), (197, 58, 2)])
 def test_band_heights(gpu, oracle_lib, W, band_rows, stages):
-    """Every band split of a tile, single- or double-buffered, produces the same bits."""
+    """Every band split of a tile, single- or double-buffered, produces the same bits
+    (bands of band_rows rows, the last one the rest: down to one row)."""
     cases = [Case(W, lvl, tx, ty, seed=lvl + 5 * tx, noise_amp=-20.0) for lvl, tx, ty in [(1, 1, 0), (4, 7, 12), (0, 0, 0)]]
     run_cases(gpu, oracle_lib, cases, gpu.make_params(band_rows=band_rows, flip=True, stages=stages))
 
