@@ -320,6 +320,8 @@ int tp_producer_put_tile(tp_producer *p, tp_tile *t);                          /
 int tp_producer_prefetch_tile(tp_producer *p, int level, int tx, int ty);    /* prefetchTile */
 int tp_producer_invalidate_tiles(tp_producer *p);                             /* invalidateTiles */
 int tp_producer_queued(const tp_producer *p);                                  /* tiles waiting for production */
+/* A held tile's coordinates, slot, users and state, read without the cache's lock:
+ * for inspection while no other thread acquires or releases that tile. */
 int tp_tile_info(const tp_tile *t, int *level, int *tx, int *ty, int *slot, int *users, int *done);
 /* Produces every queued tile of the producers and of the producers they use, on
  * `stream`: residual tiles first (host decode and one upload, or device decode),

@@ -829,8 +829,11 @@ extern "C" tp_tile *tp_producer_find_tile(tp_producer *p, int level, int tx, int
 
 extern "C" int tp_producer_put_tile(tp_producer *p, tp_tile *t)
 {
-    if (!p || !t || t->producer_id != p->id || t->users <= 0)
-        return tp::fail(TP_E_BAD_ARG, "tp_producer_put_tile: tile not held");
+    if (!p || !t) return tp::fail(TP_E_BAD_ARG, "tp_producer_put_tile: tile not held");
+    // the tile's owner and users are read under its cache's lock: other threads change
+    // them (a queued tile releasing what it acquired, a recycled record)
+    std::lock_guard<std::recursive_mutex> lk(p->cache->mu);
+    if (t->producer_id != p->id || t->users <= 0) return tp::fail(TP_E_BAD_ARG, "tp_producer_put_tile: tile not held");
     return put_tile(p, t);
 }
 
@@ -879,7 +882,12 @@ extern "C" int tp_producer_invalidate_tiles(tp_producer *p)
     return TP_OK;
 }
 
-extern "C" int tp_producer_queued(const tp_producer *p) { return p ? (int)p->queue.size() : TP_E_BAD_ARG; }
+extern "C" int tp_producer_queued(const tp_producer *p)
+{
+    if (!p) return TP_E_BAD_ARG;
+    std::lock_guard<std::recursive_mutex> lk(p->cache->mu);  // queues change under the cache's lock
+    return (int)p->queue.size();
+}
 
 // ResidualProducer::doCreateTile on a host tile: the residual tile (level, tx, ty)
 // as the producer would upload it (width = the residual cache's tile width).
