@@ -4,7 +4,9 @@ sources are compiled with the sanitizer, linked with the CUDA objects of the nor
 build and the static CUDA runtime, and driven by tests/c/cache_stress.cpp (threads
 acquiring, releasing, prefetching and looking up tiles of shared producers on
 bookkeeping-only storages, an invalidating thread, a sampling thread).  CPU only;
-the run must end cleanly with no sanitizer report."""
+the run must end cleanly with no sanitizer report.  Under AddressSanitizer the
+residual and ortho pyramid readers and the inflate decoder also read damaged and
+truncated copies of the test fixtures (tests/c/dat_fuzz.cpp)."""
 import concurrent.futures as cf
 import glob
 import os
@@ -42,19 +44,27 @@ def test_cache_protocol_under_sanitizer(product, tmp_path, kind):
               "-I", os.path.join(CUDA, "include")] + flags
     jobs = []
     objs = []
-    for src in sorted(glob.glob(os.path.join(PKG, "csrc", "*.cpp"))) + [os.path.join(HERE, "c", "cache_stress.cpp")]:
+    drivers = ["cache_stress.cpp"] + (["dat_fuzz.cpp"] if kind == "address" else [])
+    lib_objs = []
+    for src in sorted(glob.glob(os.path.join(PKG, "csrc", "*.cpp"))) + [os.path.join(HERE, "c", d) for d in drivers]:
         obj = str(tmp_path / (os.path.basename(src) + ".o"))
-        objs.append(obj)
+        (objs if os.path.basename(src) in drivers else lib_objs).append(obj)
         jobs.append(["g++", "-c", src, "-o", obj] + common)
     with cf.ThreadPoolExecutor(max_workers=8) as ex:
         for rc, cmd, err in ex.map(_compile, jobs):
             assert rc == 0, (cmd, err)
-    exe = str(tmp_path / "cache_stress")
-    link = ["g++"] + flags + objs + cu_objs + [static_rt, "-ldl", "-lpthread", "-lrt", "-o", exe]
-    r = subprocess.run(link, capture_output=True, text=True)
-    assert r.returncode == 0, r.stderr[-3000:]
-    run = subprocess.run([exe], capture_output=True, text=True, timeout=600, env=dict(os.environ, **env_extra))
-    out = run.stdout + run.stderr
-    assert run.returncode == 0, out[-6000:]
-    assert "cache stress ok" in run.stdout
-    assert "Sanitizer" not in run.stderr and "runtime error" not in run.stderr, run.stderr[-6000:]
+    env = dict(os.environ, **env_extra)
+    for drv, obj in zip(drivers, objs):
+        exe = str(tmp_path / drv[:-4])
+        link = ["g++"] + flags + [obj] + lib_objs + cu_objs + [static_rt, "-ldl", "-lpthread", "-lrt", "-o", exe]
+        r = subprocess.run(link, capture_output=True, text=True)
+        assert r.returncode == 0, r.stderr[-3000:]
+        args = [exe]
+        if drv == "dat_fuzz.cpp":
+            args += [os.path.join(HERE, "golden", "dem_terrain4_mini.dat"),
+                     os.path.join(HERE, "golden", "rgb_graph1_mini.dat"), str(tmp_path / "fuzz.dat"), "1500"]
+        run = subprocess.run(args, capture_output=True, text=True, timeout=600, env=env)
+        out = run.stdout + run.stderr
+        assert run.returncode == 0, (drv, out[-6000:])
+        assert ("cache stress ok" if drv == "cache_stress.cpp" else "dat fuzz ok") in run.stdout
+        assert "Sanitizer" not in run.stderr and "runtime error" not in run.stderr, (drv, run.stderr[-6000:])
