@@ -34,7 +34,8 @@ namespace {
 enum Kind { kResidual = 0, kElevation = 1, kNormal = 2, kOrthoResidual = 3, kOrtho = 4 };
 // tile id (producer id, level, tx, ty), TileCache.h:80-86
 struct TKey {
-    uint64_t a, b;  // (producer id, level), (tx, ty)
+    uint64_t a = 0, b = 0;  // (producer id, level), (tx, ty)
+    TKey() = default;
     TKey(int producer, int level, int tx, int ty)
         : a(((uint64_t)(uint32_t)producer << 32) | (uint32_t)level), b(((uint64_t)(uint32_t)tx << 32) | (uint32_t)ty)
     {
@@ -52,13 +53,15 @@ struct TKeyHash {
     }
 };
 
-// The cache's tiles by key: open addressing with linear probing, the keys held in
-// the table itself (one cache line touched per lookup in the common case instead of
-// a bucket array and a list node), a power-of-two capacity of at least twice the
-// entries, deletion by backward shift (no tombstones).
-template <class V>
-class TileTable {
+// Key -> value tables of the caches (tile key -> tile) and samplers (quad key ->
+// position): open addressing with linear probing, the keys held in the table itself
+// (one cache line touched per lookup in the common case instead of a bucket array and
+// a list node), a power-of-two capacity of at least twice the entries, deletion by
+// backward shift (no tombstones).  A slot is empty when its value equals `empty`.
+template <class K, class V, class Hash>
+class FlatTable {
 public:
+    explicit FlatTable(V empty) : empty_(empty) {}
     void reserve(size_t n)
     {
         size_t cap = 16;
@@ -66,67 +69,70 @@ public:
         if (cap > slots_.size()) rehash(cap);
     }
     size_t size() const { return size_; }
-    V *find(const TKey &k) const
+    // the value's slot, or null
+    V *find(const K &k)
     {
         if (slots_.empty()) return nullptr;
-        for (size_t i = TKeyHash()(k) & mask_;; i = (i + 1) & mask_) {
-            const Slot &e = slots_[i];
-            if (!e.v) return nullptr;
-            if (e.k == k) return e.v;
+        for (size_t i = Hash()(k) & mask_;; i = (i + 1) & mask_) {
+            Slot &e = slots_[i];
+            if (e.v == empty_) return nullptr;
+            if (e.k == k) return &e.v;
         }
     }
-    void insert(const TKey &k, V *v)  // k is not in the table
+    const V *find(const K &k) const { return const_cast<FlatTable *>(this)->find(k); }
+    void insert(const K &k, V v)  // k is not in the table
     {
         if (2 * (size_ + 1) > slots_.size()) rehash(slots_.empty() ? 16 : 2 * slots_.size());
-        size_t i = TKeyHash()(k) & mask_;
-        while (slots_[i].v) i = (i + 1) & mask_;
+        size_t i = Hash()(k) & mask_;
+        while (slots_[i].v != empty_) i = (i + 1) & mask_;
         slots_[i] = Slot{k, v};
         ++size_;
     }
-    void erase(const TKey &k)
+    void erase(const K &k)
     {
         if (slots_.empty()) return;
-        size_t i = TKeyHash()(k) & mask_;
+        size_t i = Hash()(k) & mask_;
         for (;; i = (i + 1) & mask_) {
-            if (!slots_[i].v) return;
+            if (slots_[i].v == empty_) return;
             if (slots_[i].k == k) break;
         }
         // backward shift: move later entries of the probe run into the hole when their
         // home position does not lie cyclically in (hole, their position]
         size_t hole = i;
-        for (size_t j = (i + 1) & mask_; slots_[j].v; j = (j + 1) & mask_) {
-            const size_t home = TKeyHash()(slots_[j].k) & mask_;
+        for (size_t j = (i + 1) & mask_; slots_[j].v != empty_; j = (j + 1) & mask_) {
+            const size_t home = Hash()(slots_[j].k) & mask_;
             const bool stays = hole <= j ? (home > hole && home <= j) : (home > hole || home <= j);
             if (stays) continue;
             slots_[hole] = slots_[j];
             hole = j;
         }
-        slots_[hole] = Slot{TKey(0, 0, 0, 0), nullptr};
+        slots_[hole] = Slot{K{}, empty_};
         --size_;
     }
     template <class F>
     void for_each(F f) const
     {
         for (const Slot &e : slots_)
-            if (e.v) f(e.v);
+            if (e.v != empty_) f(e.v);
     }
 
 private:
     struct Slot {
-        TKey k;
-        V *v;
+        K k;
+        V v;
     };
     void rehash(size_t cap)
     {
-        std::vector<Slot> old(cap, Slot{TKey(0, 0, 0, 0), nullptr});
+        std::vector<Slot> old(cap, Slot{K{}, empty_});
         old.swap(slots_);
         mask_ = cap - 1;
         size_ = 0;
         for (const Slot &e : old)
-            if (e.v) insert(e.k, e.v);
+            if (e.v != empty_) insert(e.k, e.v);
     }
     std::vector<Slot> slots_;
     size_t mask_ = 0, size_ = 0;
+    V empty_;
 };
 
 int next_producer_id()
@@ -163,7 +169,7 @@ struct tp_cache {
     std::string name;
     std::recursive_mutex mu;
     // every tile holding a slot: used (users > 0) or unused (users == 0, in the LRU list)
-    TileTable<tp_tile> tiles;
+    FlatTable<TKey, tp_tile *, TKeyHash> tiles{nullptr};
     tp_tile *lru_head = nullptr, *lru_tail = nullptr;
     int n_unused = 0;
     long long queries = 0, misses = 0;
@@ -287,7 +293,8 @@ tp_tile *get_tile(tp_producer *p, int level, int tx, int ty, int *users_before, 
     std::lock_guard<std::recursive_mutex> lk(c->mu);
     const TKey k = key_of(p, level, tx, ty);
     tp_tile *t = nullptr;
-    if ((t = c->tiles.find(k)) != nullptr) {
+    if (tp_tile **found = c->tiles.find(k)) {
+        t = *found;
         if (t->users == 0) {
             ++c->queries;
             c->lru_unlink(t);  // an unused tile in the cache: used again
@@ -821,7 +828,8 @@ extern "C" tp_tile *tp_producer_find_tile(tp_producer *p, int level, int tx, int
     tp_cache *c = p->cache;
     std::lock_guard<std::recursive_mutex> lk(c->mu);
     const TKey k = key_of(p, level, tx, ty);
-    tp_tile *t = c->tiles.find(k);
+    tp_tile *const *found = c->tiles.find(k);
+    tp_tile *t = found ? *found : nullptr;
     if (t && !(t->users > 0 || include_cache)) t = nullptr;
     if (t && done && !t->done) t = nullptr;
     return t;
@@ -1532,61 +1540,9 @@ extern "C" int tp_create_tile(tp_producer *p, int level, int tx, int ty, tp_tile
 // new quads' tiles acquired (getTile, in request order: parents first; producers in
 // the order given) and all produced by one scheduler run, so that normal tiles of
 // new elevation tiles are fused into the elevation launch.
-// A sampler's quads by key (uint64 -> position in its dense array): the same open
-// addressing as the tiles' table, the empty mark a position of all ones.
-class QuadIndex {
-public:
-    void reserve(size_t n)
-    {
-        size_t cap = 16;
-        while (cap < 2 * n) cap <<= 1;
-        if (cap > slots_.size()) rehash(cap);
-    }
-    uint32_t *find(uint64_t k)
-    {
-        if (slots_.empty()) return nullptr;
-        for (size_t i = hash(k) & mask_;; i = (i + 1) & mask_) {
-            Slot &e = slots_[i];
-            if (e.v == kEmpty) return nullptr;
-            if (e.k == k) return &e.v;
-        }
-    }
-    const uint32_t *find(uint64_t k) const { return const_cast<QuadIndex *>(this)->find(k); }
-    void insert(uint64_t k, uint32_t v)  // k is not in the index
-    {
-        if (2 * (size_ + 1) > slots_.size()) rehash(slots_.empty() ? 16 : 2 * slots_.size());
-        size_t i = hash(k) & mask_;
-        while (slots_[i].v != kEmpty) i = (i + 1) & mask_;
-        slots_[i] = Slot{k, v};
-        ++size_;
-    }
-    void erase(uint64_t k)
-    {
-        if (slots_.empty()) return;
-        size_t i = hash(k) & mask_;
-        for (;; i = (i + 1) & mask_) {
-            if (slots_[i].v == kEmpty) return;
-            if (slots_[i].k == k) break;
-        }
-        size_t hole = i;
-        for (size_t j = (i + 1) & mask_; slots_[j].v != kEmpty; j = (j + 1) & mask_) {
-            const size_t home = hash(slots_[j].k) & mask_;
-            const bool stays = hole <= j ? (home > hole && home <= j) : (home > hole || home <= j);
-            if (stays) continue;
-            slots_[hole] = slots_[j];
-            hole = j;
-        }
-        slots_[hole] = Slot{0, kEmpty};
-        --size_;
-    }
-
-private:
-    static constexpr uint32_t kEmpty = 0xFFFFFFFFu;
-    struct Slot {
-        uint64_t k;
-        uint32_t v;
-    };
-    static size_t hash(uint64_t x)
+// A quad key's hash (splitmix64's finaliser).
+struct QuadHash {
+    size_t operator()(uint64_t x) const
     {
         x ^= x >> 31;
         x *= 0xbf58476d1ce4e5b9ull;
@@ -1595,17 +1551,6 @@ private:
         x ^= x >> 32;
         return (size_t)x;
     }
-    void rehash(size_t cap)
-    {
-        std::vector<Slot> old(cap, Slot{0, kEmpty});
-        old.swap(slots_);
-        mask_ = cap - 1;
-        size_ = 0;
-        for (const Slot &e : old)
-            if (e.v != kEmpty) insert(e.k, e.v);
-    }
-    std::vector<Slot> slots_;
-    size_t mask_ = 0, size_ = 0;
 };
 
 struct tp_sampler {
@@ -1617,7 +1562,7 @@ struct tp_sampler {
     };
     std::vector<tp_producer *> producers;
     std::vector<Quad> held;                        // dense: released quads swap with the last one
-    QuadIndex index;                               // quad key -> position in `held`
+    FlatTable<uint64_t, uint32_t, QuadHash> index{0xFFFFFFFFu};  // quad key -> position in `held`
     uint32_t frame = 0;
     std::vector<tp_tile_req> fresh;  // the last update's new quads
 };
