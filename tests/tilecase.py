@@ -2,7 +2,7 @@
 the C ABI and the same tiles through the CPU oracle."""
 import numpy as np
 
-ELEV_TOL_REL = 1e-5      # fp32 elevations vs the oracle (north-star tolerance)
+ELEV_TOL_REL = 1e-5      # fp32 elevations vs the oracle: 1e-5 relative (asserted beside bit identity)
 NORMAL_TOL_ABS = 1e-4    # normals vs the oracle
 
 
