@@ -215,3 +215,89 @@ def test_host_rejects_bad_pass_states(product):
         tp.elevation_layers(elev, [(0, [(v, None, 0, True, LARGE, NOTEQUAL | NO_DEPTH | NO_W, 0.0)])])
     assert "device elevation storage" in tp.lib().tp_last_error().decode()
     assert tp.lib().tp_layer_builder_set_pass(None, 0, 0, 0.0) == tp.TP_E_BAD_ARG
+
+
+def _odd_winding(px, py, contours):
+    """Crossing-number parity of the points (px, py) against the contours (x, y up)."""
+    inside = np.zeros(px.shape, bool)
+    for c in contours:
+        c = np.asarray(c, np.float64)
+        x0, y0 = c[:, 0], c[:, 1]
+        x1, y1 = np.roll(x0, -1), np.roll(y0, -1)
+        for a, b, c2, d in zip(x0, y0, x1, y1):
+            if b == d:
+                continue
+            cond = (py >= min(b, d)) & (py < max(b, d))
+            xc = a + (py - b) * (c2 - a) / (d - b)
+            inside ^= cond & (px < xc)
+    return inside
+
+
+def _edge_distance(px, py, contours):
+    dist = np.full(px.shape, np.inf)
+    for c in contours:
+        c = np.asarray(c, np.float64)
+        for (a, b), (c2, d) in zip(c, np.roll(c, -1, axis=0)):
+            vx, vy = c2 - a, d - b
+            t = np.clip(((px - a) * vx + (py - b) * vy) / max(vx * vx + vy * vy, 1e-30), 0.0, 1.0)
+            dist = np.minimum(dist, np.hypot(px - (a + t * vx), py - (b + t * vy)))
+    return dist
+
+
+@pytest.mark.parametrize("seed", range(6))
+def test_fill_triangles_cover_the_odd_winding_region(product, oracle_lib, seed):
+    """Random star-shaped and self-crossing contours (one to three, nested or
+    overlapping): every texel centre further than 0.05 texel from all edges is filled
+    exactly when its crossing count is odd."""
+    from proland_gb300 import layers
+    rng = np.random.default_rng(seed)
+    tr = (0.5 * W, 0.5 * W, 2.0 / W, 1.0)       # world = window coordinates
+    contours = []
+    for _ in range(int(rng.integers(1, 4))):
+        cx, cy, r = rng.uniform(25, 76, 2).tolist() + [float(rng.uniform(10, 40))]
+        n = int(rng.integers(3, 12))
+        ang = rng.uniform(0, 2 * np.pi, n)
+        if rng.uniform() < 0.6:
+            ang = np.sort(ang)                   # star-shaped; unsorted angles cross themselves
+        rad = r * rng.uniform(0.3, 1.0, n)
+        contours.append(np.column_stack([cx + rad * np.cos(ang), cy + rad * np.sin(ang)]))
+    zf, zm = tile_inputs(20 + seed)
+    v = layers.fill_triangles(contours, tr, 0.0, 1.0)
+    out = oracle_lib.layer_tile(W, zf, zm, [mesh(v, FILL, ALWAYS, 0.02, clear=True)])
+    j, i = np.mgrid[0:W, 0:W] + 0.5
+    inside = _odd_winding(i, j, contours)
+    clear = _edge_distance(i, j, contours) > 0.05
+    covered = out == zf                          # w = 1: zm became zf
+    same_value = zf == zm                         # texels where zf == zm cannot tell
+    check = clear & ~same_value
+    assert check.sum() > 5000
+    assert np.array_equal(covered[check], inside[check])
+
+
+@pytest.mark.parametrize("seed", range(4))
+def test_road_strip_covers_its_total_width(product, oracle_lib, seed):
+    """A straight road of constant altitude at a random angle: the texels within half of
+    TOTALWIDTH of its axis (0.05 texel margin) change, those beyond do not.  The tile is
+    96 world units across (W = 101, border 2), so world units are texels."""
+    from proland_gb300 import layers
+    rng = np.random.default_rng(40 + seed)
+    size = 96.0
+    ang = float(rng.uniform(0, np.pi))
+    c = np.array([48.0, 48.0]) + rng.uniform(-15, 15, 2)
+    d = np.array([np.cos(ang), np.sin(ang)])
+    pts = [c - 150 * d, c, c + 150 * d]
+    width = float(rng.uniform(3, 12))
+    v = layers.road_strip(pts, [5000.0] * 3, width, (0.0, 0.0), size, W)
+    scale = layers.tile_transform((0.0, 0.0), size, W)[3]
+    half = float(layers.base_width(width, scale)) * 3.0 / 2.0
+    zf, _ = tile_inputs(60 + seed)
+    zm = zf + np.float32(1000.0)   # zm apart from zf: the strip's outer third blends to zf exactly
+    out = oracle_lib.layer_tile(W, zf, zm, [(v, None, 1, True)])
+    j, i = np.mgrid[0:W, 0:W] + 0.5
+    # window = world + 2.5: the tile's origin sits at the 2-texel border plus the half texel
+    px, py = i - 2.5 - c[0], j - 2.5 - c[1]
+    dist = np.abs(px * d[1] - py * d[0])
+    assert (dist < half - 0.05).sum() > 200
+    changed = out != zm
+    assert changed[dist < half - 0.05].all()
+    assert not changed[dist > half + 0.05].any()
