@@ -301,3 +301,30 @@ def test_road_strip_covers_its_total_width(product, oracle_lib, seed):
     changed = out != zm
     assert changed[dist < half - 0.05].all()
     assert not changed[dist > half + 0.05].any()
+
+
+@pytest.mark.parametrize("seed", range(4))
+def test_boundary_strip_covers_twelve_units_on_its_right(product, oracle_lib, seed):
+    """drawCurve with part (0, 12, 1, 2) along a straight curve at a random angle: the
+    strip spans the 12 world units on the curve's right (u from 1 on the curve to 2),
+    so under river = 1 (w = smoothstep(1, 2, u), alpha only) the texels strictly inside
+    that band change and the texels elsewhere do not.  World units are texels here."""
+    from proland_gb300 import layers
+    rng = np.random.default_rng(80 + seed)
+    tr = layers.tile_transform((0.0, 0.0), 96.0, W)
+    ang = float(rng.uniform(0, 2 * np.pi))
+    c = np.array([48.0, 48.0]) + rng.uniform(-10, 10, 2)
+    d = np.array([np.cos(ang), np.sin(ang)])
+    pts = [c - 150 * d, c, c + 150 * d]
+    v = layers.curve_part_strip(pts, (0.0, 12.0, 1.0, 2.0), tr)
+    zf, _ = tile_inputs(90 + seed)
+    zm = zf + np.float32(1000.0)
+    out = oracle_lib.layer_tile(W, zf, zm, [mesh(v, RIVER, ALWAYS | NO_Z, clear=True, mode=1)])
+    j, i = np.mgrid[0:W, 0:W] + 0.5
+    px, py = i - 2.5 - c[0], j - 2.5 - c[1]
+    right = px * d[1] - py * d[0]        # offset along (dy, -dx): the strip's side
+    changed = out != zm
+    inside = (right > 0.3) & (right < 11.95)
+    assert inside.sum() > 500
+    assert changed[inside].all()
+    assert not changed[(right < -0.05) | (right > 12.05)].any()
