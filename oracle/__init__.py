@@ -599,7 +599,8 @@ _REF = None
 def ref_lib():
     """oracle/_ref/libref.so: pieces of the reference's C++ compiled from its sources by
     oracle/ref_build.py (noise.cpp, createDemNoise, the noise-layer choice, the CPU
-    elevation loop, HeightMipmap's residual functions), or None where the reference
+    elevation loop, HeightMipmap's residual functions, and the GPU producers'
+    doCreateTile functions running their shaders as C++), or None where the reference
     tree is absent.  Used only to check the oracle's restatement."""
     global _REF
     if _REF is None:
@@ -622,5 +623,8 @@ def ref_lib():
         L.ref_encode_residual.argtypes = [C.c_int, C.c_int, C.c_int, _f32p, C.c_void_p]
         L.ref_compute_approx_tile.argtypes = [C.c_int, C.c_int, _f32p, _f32p, C.c_int, C.c_int, C.c_int, _f32p,
                                               _f32p]
+        L.ref_gl_elevation_tile.argtypes = [C.c_int] * 6 + [_f32p, _f32p, C.c_int, _f32p, _f32p, C.c_int,
+                                                            C.c_float, C.c_int, C.c_int, _f32p]
+        L.ref_gl_normal_tile.argtypes = [C.c_int] * 5 + [_f32p, C.c_int, _f32p, C.c_float, C.c_int, C.c_int, _f32p]
         _REF = L
     return _REF

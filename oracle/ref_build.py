@@ -25,6 +25,25 @@ as they are written, read from the reference tree at build time:
   the member functions as written, on a stand-in class holding ``tileSize`` and
   ``topLevelSize``.
 
+The GPU path, in a second unit (``ref_gpu.cpp``):
+
+* ``ElevationProducer::doCreateTile`` (``ElevationProducer.cpp:280-405``) and
+  ``NormalProducer::doCreateTile`` (``NormalProducer.cpp:164-281``), the functions
+  as written, with the uniform look-ups of their ``init`` functions, on stand-ins
+  for the Ork engine types they call (``oracle/ref_stubs/ork_gl.h``: uniforms that
+  write into the shader's variables, a framebuffer whose ``drawQuad`` runs the
+  fragment shader at every pixel, slots backed by float arrays, Ork's vector and
+  matrix arithmetic);
+* the shaders those functions draw -- the upsample shaders of terrain1, terrain2,
+  terrain4 (flipped diagonals) and the demo (modulated noise, with and without
+  ``NO_CLAMP``), the normal shaders of terrain1, terrain2 (sphere) and the demo
+  (coarse normals, four output formats) -- rewritten mechanically into C++ by
+  ``oracle/ref_glsl.py`` and compiled against ``oracle/ref_stubs/glsl.h``.
+
+Texture sampling is the choice the oracle makes (nearest texel, clamped to the
+edge; the noise array wraps), as the reference's GL filtering is not part of its
+source.
+
 Each piece is located by its text (a signature or the first and last
 statements), so the recipe fails loudly if the reference differs.  The extracted
 text goes to oracle/_ref/gen/ (git-ignored) and is compiled with
@@ -266,22 +285,316 @@ extern "C" void ref_compute_approx_tile(int tile_size, int top_level_size, float
     return path
 
 
+# ---- the GPU path: producers' doCreateTile with the shaders they draw ------------------
+NORMAL_CPP = "src/terrain/sources/proland/dem/NormalProducer.cpp"
+# variant index -> (name, shader, extra defines); the indices are the first argument
+# of ref_gl_elevation_tile / ref_gl_normal_tile
+UPSAMPLE_SHADERS = [
+    ("terrain1", "src/terrain/examples/terrain1/upsampleShader.glsl", ()),
+    ("terrain2", "src/terrain/examples/terrain2/upsampleShader.glsl", ()),
+    ("terrain4", "src/terrain/examples/terrain4/upsampleShader.glsl", ()),
+    ("demo", "src/demo/shaders/elevation/upsampleShader.glsl", ()),
+    ("demo_noclamp", "src/demo/shaders/elevation/upsampleShader.glsl", ("NO_CLAMP",)),
+]
+NORMAL_SHADERS = [
+    ("terrain1", "src/terrain/examples/terrain1/normalShader.glsl", ()),
+    ("terrain2", "src/terrain/examples/terrain2/normalShader.glsl", ()),
+    ("demo", "src/demo/shaders/elevation/normalShader.glsl", ()),
+]
+
+_GPU_PRELUDE = r"""
+namespace refgl {
+Logger *Logger::DEBUG_LOGGER = nullptr;
+using proland::cnoise;
+
+// The members ElevationProducer::doCreateTile and its init's uniform look-ups use
+// (ElevationProducer.h), on the stand-in producer.
+struct ElevationProducer : TileProducer {
+    ptr<FrameBuffer> frameBuffer;
+    ptr<TileProducer> residualTiles;
+    ptr<Texture2D> demTexture, layerTexture, residualTexture;
+    ptr<Program> upsample, blend;
+    ptr<Texture2DArray> noiseTexture;
+    vector<float> noiseAmp;
+    int gridMeshSize = 24;
+    bool flipDiagonals = false;
+    int face = 0;
+    float *residualTile = nullptr;
+    ptr<Uniform4f> tileWSDFU;
+    ptr<UniformSampler> coarseLevelSamplerU;
+    ptr<Uniform4f> coarseLevelOSLU;
+    ptr<UniformSampler> residualSamplerU;
+    ptr<Uniform4f> residualOSHU;
+    ptr<UniformSampler> noiseSamplerU;
+    ptr<Uniform4f> noiseUVLHU;
+    ptr<UniformSampler> blendCoarseLevelSamplerU;
+    ptr<Uniform1f> blendScaleU;
+    void bind_uniforms();
+    bool doCreateTile(int level, int tx, int ty, TileStorage::Slot *data);
+};
+
+// The members NormalProducer::doCreateTile and its init's look-ups use (NormalProducer.h).
+struct NormalProducer : TileProducer {
+    ptr<FrameBuffer> frameBuffer;
+    ptr<TileProducer> elevationTiles;
+    ptr<Program> normals;
+    bool deform = false;
+    int gridMeshSize = 24;
+    ptr<Uniform3f> tileSDFU;
+    ptr<UniformSampler> elevationSamplerU;
+    ptr<Uniform4f> elevationOSLU;
+    ptr<UniformSampler> normalSamplerU;
+    ptr<Uniform4f> normalOSLU;
+    ptr<UniformMatrix4f> patchCornersU;
+    ptr<UniformMatrix4f> patchVerticalsU;
+    ptr<Uniform4f> patchCornerNormsU;
+    ptr<UniformMatrix3f> worldToTangentFrameU;
+    ptr<UniformMatrix3f> parentToTangentFrameU;
+    ptr<Uniform4f> deformU;
+    void bind_uniforms();
+    bool doCreateTile(int level, int tx, int ty, TileStorage::Slot *data);
+};
+}  // namespace refgl
+"""
+
+_GPU_DRIVERS = r"""
+namespace {
+// samplers a producer leaves unset read this texture (a single zero texel)
+refgl::Texture g_zero_texture;
+
+void reset_samplers(const refgl::UniformEntry *table)
+{
+    static const float zero[4] = {0, 0, 0, 0};
+    g_zero_texture.view.data = zero;
+    g_zero_texture.view.w = g_zero_texture.view.h = g_zero_texture.view.layers = 1;
+    g_zero_texture.view.comps = 4;
+    for (const refgl::UniformEntry *e = table; e->name; ++e) {
+        if (e->kind == refgl::U_SAMPLER2D) ((glsl::sampler2D *)e->dst)->t = &g_zero_texture.view;
+        if (e->kind == refgl::U_SAMPLER2DARRAY) ((glsl::sampler2DArray *)e->dst)->t = &g_zero_texture.view;
+    }
+}
+}  // namespace
+
+// One elevation tile through ElevationProducer::doCreateTile and the upsample shader
+// `variant`: parent_rgba the parent slot's four channels (zf, zc, zm, 0; W*W*4, level > 0),
+// residual the residual producer's tile (residual_width^2; NULL: the producer has no
+// tile there; residual_width 0: no residual producer), noise the six noise layers
+// (W*W each, as the R16F texture holds them), noise_amp the per-level amplitudes.
+// out_rgba: the produced slot, W*W*4.  Returns 0.
+extern "C" int ref_gl_elevation_tile(int variant, int W, int level, int tx, int ty, int face,
+                                     const float *parent_rgba, const float *residual, int residual_width,
+                                     const float *noise, const float *noise_amp, int n_amp, float root_quad_size,
+                                     int grid_mesh_size, int flip, float *out_rgba)
+{
+    using namespace refgl;
+    if (variant < 0 || variant >= (int)(sizeof(g_upsample) / sizeof(g_upsample[0]))) return 1;
+    GPUTileStorage storage;
+    storage.tileSize = W;
+    TileCache cache;
+    cache.storage = &storage;
+    Texture2DArray parentTex, outTex, noiseTex;
+    parentTex.alloc(W, W, 2, 4, false);
+    outTex.alloc(W, W, 3, 4, false);
+    noiseTex.alloc(W, W, 6, 1, true);
+    std::memcpy(noiseTex.store.data(), noise, sizeof(float) * 6 * W * W);
+    Texture2D residualTex, demTex;
+    residualTex.alloc(W, W, 1, 1, false);
+    demTex.alloc(W, W, 1, 4, false);
+    FrameBuffer fb;
+    fb.init(W);
+    Program prog;
+    prog.table = g_upsample[variant].table;
+    prog.run = g_upsample[variant].run;
+    reset_samplers(prog.table);
+
+    ElevationProducer e;
+    e.cache = &cache;
+    e.rootQuadSize = root_quad_size;
+    e.frameBuffer = &fb;
+    e.upsample = &prog;
+    e.noiseTexture = &noiseTex;
+    e.residualTexture = &residualTex;
+    e.demTexture = &demTex;
+    e.noiseAmp.assign(noise_amp, noise_amp + n_amp);
+    e.gridMeshSize = grid_mesh_size;
+    e.flipDiagonals = flip != 0;
+    e.face = face;
+    std::vector<float> residualTile((size_t)W * W);
+    e.residualTile = residualTile.data();
+
+    GPUTileStorage::GPUSlot parentSlot, outSlot;
+    parentSlot.owner = outSlot.owner = &storage;
+    parentSlot.t = &parentTex;
+    parentSlot.l = 1;
+    outSlot.t = &outTex;
+    outSlot.l = 2;
+    if (level > 0) {
+        std::memcpy(&parentTex.store[(size_t)W * W * 4], parent_rgba, sizeof(float) * W * W * 4);
+        e.tiles[std::make_tuple(level - 1, tx / 2, ty / 2)].data = &parentSlot;
+    }
+    CPUTileStorage<float> rstorage;
+    rstorage.tileSize = residual_width;
+    TileCache rcache;
+    rcache.storage = &rstorage;
+    TileProducer rproducer;
+    rproducer.cache = &rcache;
+    CPUTileStorage<float>::CPUSlot rslot;
+    rslot.owner = &rstorage;
+    rslot.data = (float *)residual;
+    if (residual_width > 0) {
+        e.residualTiles = &rproducer;
+        if (residual) {
+            const int mod = (residual_width - 5) / (W - 5);
+            rproducer.tiles[std::make_tuple(level, tx / mod, ty / mod)].data = &rslot;
+        }
+    }
+    e.bind_uniforms();
+    if (!e.doCreateTile(level, tx, ty, &outSlot)) return 2;
+    std::memcpy(out_rgba, &outTex.store[(size_t)2 * W * W * 4], sizeof(float) * W * W * 4);
+    return 0;
+}
+
+// One normal tile through NormalProducer::doCreateTile and the normal shader `variant`:
+// elev_rgba the elevation slot (W*W*4), format 0-3 the normal storage's (RGBA32F, RGBA8,
+// RG32F, RG8), parent the parent normal slot (Wn*Wn*components, Wn = W - 4; level > 0;
+// NULL: zeros), deform the spherical flag.  out: the produced slot, Wn*Wn*components.  Returns 0.
+extern "C" int ref_gl_normal_tile(int variant, int W, int level, int tx, int ty, const float *elev_rgba, int format,
+                                  const float *parent, float root_quad_size, int grid_mesh_size, int deform,
+                                  float *out)
+{
+    using namespace refgl;
+    if (variant < 0 || variant >= (int)(sizeof(g_normal) / sizeof(g_normal[0])) || format < 0 || format > 3) return 1;
+    static const TextureInternalFormat formats[4] = {RGBA32F, RGBA8, RG32F, RG8};
+    const int Wn = W - 4, comps = format < 2 ? 4 : 2;
+    GPUTileStorage estorage, nstorage;
+    estorage.tileSize = W;
+    nstorage.tileSize = Wn;
+    TileCache ecache, ncache;
+    ecache.storage = &estorage;
+    ncache.storage = &nstorage;
+    Texture2DArray elevTex, normTex;
+    elevTex.alloc(W, W, 2, 4, false);
+    normTex.alloc(Wn, Wn, 2, comps, false);
+    normTex.format = formats[format];
+    nstorage.texture0 = &normTex;
+    FrameBuffer fb;
+    fb.init(Wn);
+    Program prog;
+    prog.table = g_normal[variant].table;
+    prog.run = g_normal[variant].run;
+    reset_samplers(prog.table);
+
+    TileProducer elevations;
+    elevations.cache = &ecache;
+    elevations.border = 2;
+    GPUTileStorage::GPUSlot eslot, pslot, oslot;
+    eslot.owner = &estorage;
+    eslot.t = &elevTex;
+    eslot.l = 1;
+    std::memcpy(&elevTex.store[(size_t)W * W * 4], elev_rgba, sizeof(float) * W * W * 4);
+    elevations.tiles[std::make_tuple(level, tx, ty)].data = &eslot;
+
+    NormalProducer n;
+    n.cache = &ncache;
+    n.rootQuadSize = root_quad_size;
+    n.frameBuffer = &fb;
+    n.elevationTiles = &elevations;
+    n.normals = &prog;
+    n.deform = deform != 0;
+    n.gridMeshSize = grid_mesh_size;
+    pslot.owner = oslot.owner = &nstorage;
+    pslot.t = oslot.t = &normTex;
+    pslot.l = 0;
+    oslot.l = 1;
+    if (level > 0) {  // doCreateTile asserts the parent normal tile is in the cache
+        if (parent) std::memcpy(normTex.store.data(), parent, sizeof(float) * Wn * Wn * comps);
+        n.tiles[std::make_tuple(level - 1, tx / 2, ty / 2)].data = &pslot;
+    }
+    n.bind_uniforms();
+    if (!n.doCreateTile(level, tx, ty, &oslot)) return 2;
+    std::memcpy(out, &normTex.store[(size_t)Wn * Wn * comps], sizeof(float) * Wn * Wn * comps);
+    return 0;
+}
+"""
+
+
+def _load_sibling(name):
+    """oracle/<name>.py by path (this file also runs as a script and is loaded by path)."""
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("oracle_" + name, os.path.join(HERE, name + ".py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
+
+
+def generate_gpu(root):
+    """oracle/_ref/gen/ref_gpu.cpp: the shaders as C++, the producers' init look-ups and
+    doCreateTile functions as written, the drivers."""
+    ref_glsl = _load_sibling("ref_glsl")
+    elev = _read(root, ELEV_CPP)
+    norm = _read(root, NORMAL_CPP)
+    src = ["// generated by oracle/ref_build.py from the reference's sources\n#include <cstring>\n#include <vector>\n"
+           "#include \"ork_gl.h\"\n#include \"proland/math/noise.h\"\n"]
+    shader_parts, tables = [], {"g_upsample": [], "g_normal": []}
+    for kind, shaders in (("g_upsample", UPSAMPLE_SHADERS), ("g_normal", NORMAL_SHADERS)):
+        for name, rel, defines in shaders:
+            ns = "%s_%s" % (kind[2:], name)
+            body, uniforms, _ = ref_glsl.shader_to_cpp(_read(root, rel), ns, "_FRAGMENT_", defines)
+            shader_parts.append("// %s\n%s%s%s" % (rel, body, ref_glsl.uniform_table(ns, uniforms),
+                                                  ref_glsl.quad_runner(ns)))
+            tables[kind].append(ns)
+    src.extend(shader_parts)
+    src.append(_GPU_PRELUDE)
+    src.append("namespace {\nstruct ProgramSource { const refgl::UniformEntry *table; void (*run)(refgl::FrameBuffer &); };\n")
+    for kind, names in tables.items():
+        src.append("const ProgramSource %s[] = {%s};\n" % (kind, ", ".join("{%s_uniforms, %s_run}" % (n, n)
+                                                                             for n in names)))
+    src.append("}  // namespace\n")
+    ups, ups_line = extract_block(elev, 'this->tileWSDFU = upsample->getUniform4f("tileWSDF");',
+                                  'this->noiseUVLHU = upsample->getUniform4f("noiseUVLH");',
+                                  after="void ElevationProducer::init(")
+    dct, dct_line = extract_function(elev, r"bool\s+ElevationProducer::doCreateTile\s*\(")
+    nups, nups_line = extract_block(norm, 'this->tileSDFU = normals->getUniform3f("tileSDF");',
+                                    'this->deformU = normals->getUniform4f("deform");',
+                                    after="void NormalProducer::init(")
+    ndct, ndct_line = extract_function(norm, r"bool\s+NormalProducer::doCreateTile\s*\(")
+    src.append("namespace refgl {\n")
+    src.append("// %s:%d\nvoid ElevationProducer::bind_uniforms()\n{\n%s}\n" % (ELEV_CPP, ups_line, ups))
+    src.append("// %s:%d\n%s" % (ELEV_CPP, dct_line, dct))
+    src.append("// %s:%d\nvoid NormalProducer::bind_uniforms()\n{\n%s}\n" % (NORMAL_CPP, nups_line, nups))
+    src.append("// %s:%d\n%s" % (NORMAL_CPP, ndct_line, ndct))
+    src.append("}  // namespace refgl\n")
+    src.append(_GPU_DRIVERS)
+    os.makedirs(GEN_DIR, exist_ok=True)
+    path = os.path.join(GEN_DIR, "ref_gpu.cpp")
+    with open(path, "w") as f:
+        f.write("".join(src))
+    return path
+
+
 def build(root=DEFAULT_ROOT, force=False):
     """Compiles libref.so when the reference tree is present; returns its path, or
     None without the reference (the GPU machine has none; the pin runs where it is)."""
     if not os.path.isdir(os.path.join(root, "src")):
         return LIB if os.path.exists(LIB) else None
-    srcs = [os.path.join(root, NOISE_CPP), os.path.join(root, ELEV_CPP), os.path.join(root, CPU_ELEV_CPP),
-            os.path.join(root, MIPMAP_CPP), os.path.abspath(__file__), os.path.join(HERE, "ref_stubs", "pmath.h")]
+    srcs = [os.path.join(root, p) for p in (NOISE_CPP, ELEV_CPP, CPU_ELEV_CPP, MIPMAP_CPP, NORMAL_CPP)]
+    srcs += [os.path.join(root, rel) for _, rel, _ in UPSAMPLE_SHADERS + NORMAL_SHADERS]
+    srcs += [os.path.abspath(__file__), os.path.join(HERE, "ref_glsl.py")]
+    srcs += [os.path.join(HERE, "ref_stubs", h) for h in ("pmath.h", "glsl.h", "ork_gl.h")]
     if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= max(os.path.getmtime(p) for p in srcs):
         return LIB
     gen = generate(root)
+    gen_gpu = generate_gpu(root)
     tmp = LIB + ".tmp%d" % os.getpid()
-    cmd = ["g++", "-O2", "-std=c++14", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared", "-w",
-           "-I", os.path.join(HERE, "ref_stubs"), "-I", os.path.join(root, NOISE_DIR),
-           "-I", os.path.join(root, "src/core/sources/proland/math"),
-           "-o", tmp, gen, os.path.join(root, NOISE_CPP)]
-    subprocess.check_call(cmd)
+    inc = ["-I", os.path.join(HERE, "ref_stubs"), "-I", os.path.join(root, NOISE_DIR),
+           "-I", os.path.join(root, "src/core/sources/proland/math")]
+    flags = ["-O2", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-w"]
+    objs = []
+    for unit, std in ((gen, "c++14"), (gen_gpu, "c++17"), (os.path.join(root, NOISE_CPP), "c++14")):
+        obj = os.path.join(GEN_DIR, os.path.basename(unit) + ".o")
+        subprocess.check_call(["g++", "-c", "-std=" + std] + flags + inc + ["-o", obj, unit])
+        objs.append(obj)
+    subprocess.check_call(["g++", "-shared", "-o", tmp] + objs)
     os.replace(tmp, LIB)
     return LIB
 

@@ -1,0 +1,232 @@
+"""The oracle's restatement of the shader path against the reference's own GPU path,
+compiled here by oracle/ref_build.py: ElevationProducer::doCreateTile and
+NormalProducer::doCreateTile as written (their uniform set-up, the noise-layer
+choice, the residual window, the FP64 sphere patch frames) drawing the reference's
+upsample and normal shaders, rewritten mechanically as C++ (oracle/ref_glsl.py)
+against the GLSL stand-in oracle/ref_stubs/glsl.h.
+
+What is compared, and how tightly:
+
+* elevation tiles, every upsample shader (terrain1, terrain2, terrain4 with
+  flipped diagonals, the demo's modulated noise with and without NO_CLAMP):
+  zc bit for bit always; zf and zm bit for bit when the parent tile holds
+  integers, where both the shader's 4x4 matrix dot product and the CPU producer's
+  stencil order (CPUElevationProducer.cpp:202-238, which the oracle and the
+  product follow) are exact; with arbitrary floats zf within a few units in the
+  last place -- the two summation orders;
+* normal tiles on the sphere (terrain2 and demo shaders, NormalProducer's FP64
+  patch frames): float tiles within 2 units in the last place (GLSL's
+  normalize divides by the length, the oracle multiplies by its reciprocal),
+  8-bit tiles the same but for an odd texel one step apart; coarse normals bit
+  for bit;
+* flat normal tiles: the shader forms absolute world positions in float
+  (normalShader.glsl getWorldPosition) and differences them, the oracle uses the
+  exact sample spacing 2h; float normals agree within that position rounding
+  (the bound below), 8-bit normals within one step; coarse normals (nc) bit for
+  bit.
+
+Texture sampling is the oracle's documented choice (the nearest texel) on both
+sides.  Runs where the reference tree is present; skipped elsewhere."""
+import numpy as np
+import pytest
+
+UPSAMPLE = {"terrain1": 0, "terrain2": 1, "terrain4": 2, "demo": 3, "demo_noclamp": 4}
+NOISE_MODE = {"terrain1": 0, "terrain4": 0, "terrain2": 1, "demo": 1, "demo_noclamp": 1}
+FLIPS = {"terrain4", "demo", "demo_noclamp"}            # shaders that read tileWSDF.w
+NORMAL = {"terrain1": 0, "terrain2": 1, "demo": 2}
+# the reference's example amplitudes (terrain2/helloworld.xml), both signs
+AMPS = np.array([-3250, -1590, -1125, -795, -561, -397, -140, -100, 15, 8, 5, 2.5], np.float32)
+
+
+@pytest.fixture(scope="module")
+def ref(oracle_lib):
+    L = oracle_lib.ref_lib()
+    if L is None or not hasattr(L, "ref_gl_elevation_tile"):
+        pytest.skip("the reference sources are not on this machine")
+    return L
+
+
+def _p(a):
+    import ctypes as C
+    return None if a is None else a.ctypes.data_as(C.POINTER(C.c_float))
+
+
+@pytest.fixture(scope="module")
+def noise_tables(ref):
+    """createDemNoise's table as the R16F texture holds it, per tile width."""
+    out = {}
+    for W in (37, 101, 197):
+        raw = np.empty((6, W, W), np.float32)
+        ref.ref_dem_noise(W, _p(raw))
+        out[W] = raw.astype(np.float16).astype(np.float32)
+    return out
+
+
+def gl_elevation(ref, variant, W, level, tx, ty, face, parent, residual, rw, noise, root, grid, flip):
+    prgba = None
+    if parent is not None:
+        prgba = np.ascontiguousarray(np.stack(list(parent) + [np.zeros_like(parent[0])], -1), np.float32)
+    res = None if residual is None else np.ascontiguousarray(residual, np.float32)
+    out = np.empty((W, W, 4), np.float32)
+    rc = ref.ref_gl_elevation_tile(UPSAMPLE[variant], W, level, tx, ty, face, _p(prgba), _p(res), rw, _p(noise),
+                                   _p(AMPS), len(AMPS), root, grid, int(flip), _p(out))
+    assert rc == 0
+    return out[..., 0], out[..., 1], out[..., 2], out[..., 3]
+
+
+def oracle_elevation(orc, variant, W, level, tx, ty, face, parent, residual, rw, noise, root, grid, flip):
+    rot, layer = orc.noise_select(face, level, tx, ty)
+    amp = float(AMPS[level]) if level < len(AMPS) else 0.0
+    mps = np.float32(np.float32(root / (1 << level)) / np.float32(W - 5))   # tileWSDF.y
+    rx = ry = 0
+    if residual is not None:
+        mod = (rw - 5) // (W - 5)
+        rx, ry = (tx % mod) * (W - 5), (ty % mod) * (W - 5)
+    return orc.elevation_tile(W, level, tx, ty, parent[0] if parent else None, parent[2] if parent else None,
+                              residual, rx=rx, ry=ry, noise=noise[layer], noise_rot=rot, noise_amp=amp,
+                              noise_mode=NOISE_MODE[variant], meters_per_sample=float(mps),
+                              grid_g=(W - 5) // grid, flip=flip, no_clamp=variant == "demo_noclamp")
+
+
+TILES = [(0, 0, 0), (1, 1, 0), (2, 3, 1), (5, 17, 30), (9, 300, 511), (11, 2047, 6), (14, 9001, 16383)]
+
+
+def _case(rng, W, level, integer, noclamp, rw_kind):
+    parent = None
+    if level > 0:
+        zf = (rng.integers(-300, 300, (W, W)) if integer else rng.standard_normal((W, W)) * 150.0).astype(np.float32)
+        zc = (rng.standard_normal((W, W)) * 150.0).astype(np.float32)
+        zm = zf.copy() if noclamp else np.maximum(zf, np.float32(0.0))
+        parent = (zf, zc, zm)
+    rw = {"same": W, "double": 2 * W - 5, "missing": W, "none": 0}[rw_kind]
+    residual = None
+    if rw_kind in ("same", "double"):
+        residual = (rng.standard_normal((rw, rw)) * 40.0).astype(np.float32)
+    return parent, residual, rw
+
+
+@pytest.mark.parametrize("variant", sorted(UPSAMPLE))
+@pytest.mark.parametrize("W,grid", [(101, 24), (197, 24), (37, 8)])
+def test_elevation_tiles_bit_exact_on_integer_parents(ref, oracle_lib, noise_tables, variant, W, grid):
+    rng = np.random.default_rng(W + 7 * UPSAMPLE[variant])
+    faces = range(1, 7) if variant == "terrain2" else [0]
+    for k, (level, tx, ty) in enumerate(TILES):
+        for rw_kind in ("same", "double", "missing", "none"):
+            face = list(faces)[k % len(faces)]
+            flip = variant in FLIPS and (k + len(rw_kind)) % 2 == 0
+            parent, residual, rw = _case(rng, W, level, True, variant == "demo_noclamp", rw_kind)
+            args = (variant, W, level, tx, ty, face, parent, residual, rw, noise_tables[W], 60000.0, grid, flip)
+            got = gl_elevation(ref, *args)
+            want = oracle_elevation(oracle_lib, *args)
+            for name, g, w in zip(("zf", "zc", "zm"), got, want):
+                assert np.array_equal(g, w), (name, variant, W, level, tx, ty, rw_kind, flip)
+            assert not np.any(got[3]), "the fourth channel is written 0"
+
+
+@pytest.mark.parametrize("variant", sorted(UPSAMPLE))
+def test_elevation_tiles_on_float_parents(ref, oracle_lib, noise_tables, variant):
+    """Arbitrary float parents: zc bit for bit, zf within a few ulps of the window's
+    magnitude (the shader sums the 16 weighted samples column by column, the CPU
+    producer rows of (a + b) * 9 - (c + d), / 16), zm = max(zf, 0) of its own zf."""
+    rng = np.random.default_rng(11 + UPSAMPLE[variant])
+    W, grid = 101, 24
+    identical = total = 0
+    for k, (level, tx, ty) in enumerate(TILES[1:]):
+        flip = variant in FLIPS and k % 2 == 0
+        parent, residual, rw = _case(rng, W, level, False, variant == "demo_noclamp", "same")
+        args = (variant, W, level, tx, ty, 0, parent, residual, rw, noise_tables[W], 60000.0, grid, flip)
+        zf, zc, zm, _ = gl_elevation(ref, *args)
+        wf, wc, wm = oracle_elevation(oracle_lib, *args)
+        assert np.array_equal(zc, wc), (variant, level)
+        scale = np.float32(2.0 * np.abs(parent[0]).max() + np.abs(wf).max())
+        assert np.abs(zf - wf).max() <= 8 * np.spacing(scale), (variant, level, np.abs(zf - wf).max())
+        assert np.array_equal(zm, zf if variant == "demo_noclamp" else np.maximum(zf, np.float32(0.0)))
+        identical += int(np.sum(zf == wf))
+        total += zf.size
+    # the even-even samples copy a parent sample and the odd rows or columns of a
+    # 1D stencil often round the same way: most samples agree exactly
+    assert identical >= 0.5 * total
+
+
+def gl_normals(ref, variant, W, level, tx, ty, zm, fmt, parent, root, grid, deform):
+    Wn, comps = W - 4, (4 if fmt < 2 else 2)
+    erg = np.ascontiguousarray(np.stack([zm, zm, zm, np.zeros_like(zm)], -1), np.float32)
+    par = None if parent is None else np.ascontiguousarray(np.stack(parent, -1), np.float32)
+    out = np.empty((Wn, Wn, comps), np.float32)
+    rc = ref.ref_gl_normal_tile(NORMAL[variant], W, level, tx, ty, _p(erg), fmt, _p(par), root, grid, int(deform),
+                                _p(out))
+    assert rc == 0
+    return [out[..., k] for k in range(comps)]
+
+
+def _normal_case(rng, W, level, fmt, amp=30.0):
+    Wn = W - 4
+    zm = (rng.standard_normal((W, W)) * amp).astype(np.float32)
+    parent = None
+    if level > 0 and fmt < 2:
+        parent = [np.clip(rng.standard_normal((Wn, Wn)) * 0.3, -0.7, 0.7).astype(np.float32) for _ in range(4)]
+        if fmt == 1:   # an RGBA8 parent holds k / 255
+            parent = [(np.floor(np.clip(v * 0.5 + 0.5, 0, 1) * 255 + 0.5) / 255).astype(np.float32) for v in parent]
+    return zm, parent
+
+
+NORMAL_TILES = [(0, 0, 0, 1000.0), (1, 1, 0, 1000.0), (3, 5, 2, 10000.0), (6, 33, 60, 50000.0),
+                (10, 700, 300, 6.4e6), (14, 9000, 5000, 6.4e6)]
+
+
+@pytest.mark.parametrize("variant,fmt", [("terrain2", 3), ("demo", 3), ("demo", 1), ("demo", 0)])
+def test_sphere_normal_tiles(ref, oracle_lib, variant, fmt):
+    rng = np.random.default_rng(40 + fmt)
+    W, grid = 101, 24
+    for level, tx, ty, root in NORMAL_TILES:
+        zm, parent = _normal_case(rng, W, level, fmt)
+        got = gl_normals(ref, variant, W, level, tx, ty, zm, fmt, parent, root, grid, True)
+        want = oracle_lib.normals_full(W, zm, root / (1 << level), fmt, tx, ty,
+                                       parent=None if parent is None else parent[:2], root_quad_size=root,
+                                       level=level, grid_mesh=grid)
+        for k, (g, w) in enumerate(zip(got, want)):
+            d = np.abs(g - w)
+            if k >= 2 and level > 0:
+                assert np.array_equal(g, w), (variant, fmt, level, k)   # the coarse normals
+            elif fmt in (1, 3):
+                # the float normals below differ by an ulp or two (GLSL's normalize is
+                # v / length(v), the oracle's v * (1 / length(v))), which moves a value
+                # across an 8-bit rounding boundary now and then
+                assert d.max() <= 1.0 / 255 + 1e-6 and np.mean(d > 0) <= 0.001, (variant, fmt, level, k)
+            else:
+                assert d.max() <= 2 * np.spacing(np.float32(1.0)), (variant, fmt, level, k)
+
+
+def flat_position_bound(root, level, tx, ty, W):
+    """How far the shader's normals can be from the exact-spacing ones: each world
+    position x0 + D u rounds to half an ulp of its magnitude, so a central difference
+    of 2h carries a relative error up to ulp(|x0| + D) / 2h, and the unit normal's
+    components move by about twice that."""
+    D = root / (1 << level)
+    x0 = tx / (1 << level) * root - root / 2
+    y0 = ty / (1 << level) * root - root / 2
+    h = D / (W - 5)
+    mag = np.float32(max(abs(x0), abs(y0)) + D)
+    return float(4 * np.spacing(mag) / (2 * h) + 4 * np.spacing(np.float32(1.0)))
+
+
+@pytest.mark.parametrize("variant,fmt", [("terrain1", 3), ("demo", 0), ("demo", 1), ("demo", 2), ("demo", 3)])
+def test_flat_normal_tiles(ref, oracle_lib, variant, fmt):
+    rng = np.random.default_rng(60 + fmt + 7 * NORMAL[variant])
+    W, grid = 101, 24
+    for level, tx, ty, root in NORMAL_TILES:
+        zm, parent = _normal_case(rng, W, level, fmt)
+        got = gl_normals(ref, variant, W, level, tx, ty, zm, fmt, parent, root, grid, False)
+        want = oracle_lib.normals_full(W, zm, root / (1 << level), fmt, tx, ty,
+                                       parent=None if parent is None else parent[:2], level=level, grid_mesh=grid)
+        bound = flat_position_bound(root, level, tx, ty, W)
+        for k, (g, w) in enumerate(zip(got, want)):
+            d = np.abs(g - w)
+            if k >= 2 and level > 0:
+                assert np.array_equal(g, w), ("nc", variant, fmt, level, k)   # the coarse normals
+            elif fmt in (1, 3):
+                assert d.max() <= 1.0 / 255 + 1e-6, (variant, fmt, level, k)
+                if root <= 50000.0:
+                    assert np.mean(d > 0) <= 0.005, (variant, fmt, level, k, np.mean(d > 0))
+            else:
+                assert d.max() <= bound, (variant, fmt, level, k, d.max(), bound)
