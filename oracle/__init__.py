@@ -88,6 +88,8 @@ def lib():
         L.or_ortho_tile_id.restype = C.c_int
         L.or_layer_tile.argtypes = [C.c_int, _f32p, _f32p, C.POINTER(LayerMesh), C.c_int, _f32p,
                                     C.POINTER(C.c_uint32), C.c_int, _f32p]
+        L.or_layer_fragment.argtypes = [C.c_int, C.c_float, C.c_float, C.c_float, _f32p]
+        L.or_layer_blend.argtypes = [C.c_int, _f32p, _f32p, _f32p, C.c_int, _f32p]
         L.or_elevation_tile.argtypes = [C.POINTER(ElevTile)]
         L.or_elevation_tile_f64.argtypes = [C.POINTER(ElevTile), _f64p, _f64p, _f64p]
         L.or_cpu_elevation_tile.argtypes = [C.c_int] * 4 + [_f32p, C.c_int, _f32p, C.c_int,
@@ -215,6 +217,20 @@ def layer_tile(W, zf, zm, meshes, blend_mode=0):
     out = np.empty((W, W), np.float32)
     lib().or_layer_tile(W, _p(_f32(zf)), _p(_f32(zm)), arr, len(ms), _p(va), _p(ia, C.POINTER(C.c_uint32)),
                         blend_mode, _p(out))
+    return out
+
+
+def layer_fragment(program, a, u, fill_depth=0.0):
+    """(depth clamped to [0, 1], z, w) of one fragment of a layer program."""
+    out = np.empty(3, np.float32)
+    lib().or_layer_fragment(int(program), float(fill_depth), float(a), float(u), _p(out))
+    return tuple(float(v) for v in out)
+
+
+def layer_blend(W, zf, z, w, blend_mode=0):
+    """The blend pass alone: zm from zf and the layers' z and w planes."""
+    out = np.empty((W, W), np.float32)
+    lib().or_layer_blend(W, _p(_f32(zf)), _p(_f32(z)), _p(_f32(w)), blend_mode, _p(out))
     return out
 
 
@@ -626,5 +642,9 @@ def ref_lib():
         L.ref_gl_elevation_tile.argtypes = [C.c_int] * 6 + [_f32p, _f32p, C.c_int, _f32p, _f32p, C.c_int,
                                                             C.c_float, C.c_int, C.c_int, _f32p]
         L.ref_gl_normal_tile.argtypes = [C.c_int] * 5 + [_f32p, C.c_int, _f32p, C.c_float, C.c_int, C.c_int, _f32p]
+        L.ref_gl_elevation_tile_layers.argtypes = [C.c_int] * 7 + [_f32p, _f32p, C.c_int, _f32p, _f32p, C.c_int,
+                                                                   C.c_float, C.c_int, C.c_int, _f32p, _f32p, _f32p]
+        L.ref_gl_layer_fragment.argtypes = [C.c_int, C.c_int, C.c_float, _f32p, C.c_float, C.c_float, _f32p,
+                                            C.POINTER(C.c_float)]
         _REF = L
     return _REF

@@ -162,7 +162,6 @@ void or_layer_tile(int W, const float *zf, const float *zm, const or_layer_mesh 
     float *z = (float *)malloc(N * sizeof(float));
     float *w = (float *)malloc(N * sizeof(float));
     float *depth = (float *)malloc(N * sizeof(float));
-    float *bl = (float *)malloc(N * sizeof(float));
     for (size_t p = 0; p < N; ++p) {
         z[p] = zm[p];
         w[p] = 0.0f;
@@ -192,6 +191,25 @@ void or_layer_tile(int W, const float *zf, const float *zm, const or_layer_mesh 
             draw_triangle(W, M, v[0], v[1], v[2], z, w, depth);
         }
     }
+    or_layer_blend(W, zf, z, w, blend_mode, zm_out);
+    free(z);
+    free(w);
+    free(depth);
+}
+
+void or_layer_fragment(int program, float fill_depth, float a, float u, float *out)
+{
+    or_layer_mesh M;
+    memset(&M, 0, sizeof(M));
+    M.program = program;
+    M.fill_depth = fill_depth;
+    fragment_program(&M, a, u, &out[0], &out[1], &out[2]);
+}
+
+void or_layer_blend(int W, const float *zf, const float *z, const float *w, int blend_mode, float *zm_out)
+{
+    const size_t N = (size_t)W * W;
+    float *bl = (float *)malloc(N * sizeof(float));
     for (size_t p = 0; p < N; ++p) {
         const float b = w[p] < 1.0f ? w[p] : 1.0f;
         bl[p] = zf[p] * b + z[p] * (1.0f - b);
@@ -211,8 +229,5 @@ void or_layer_tile(int W, const float *zf, const float *zm, const or_layer_mesh 
             const float f = 1.0f / 9.0f;
             zm_out[j * W + i] = sx * f + sy * f + sz * f;
         }
-    free(z);
-    free(w);
-    free(depth);
     free(bl);
 }

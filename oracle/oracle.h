@@ -179,6 +179,11 @@ typedef struct {
 } or_layer_mesh;
 void or_layer_tile(int W, const float *zf, const float *zm, const or_layer_mesh *meshes, int n_meshes,
                    const float *vertices, const uint32_t *indices, int blend_mode, float *zm_out);
+/* one fragment of `program` at the interpolated attributes (a, u): out = (depth
+ * clamped to [0, 1], z, w) */
+void or_layer_fragment(int program, float fill_depth, float a, float u, float *out);
+/* the blend pass alone, from the layers' z and w planes (dense W x W) */
+void or_layer_blend(int W, const float *zf, const float *z, const float *w, int blend_mode, float *zm_out);
 
 #ifdef __cplusplus
 }

@@ -116,6 +116,24 @@ def extract_block(text, first, last, after=None):
     return "\n".join(lines[s:e + 1]) + "\n", s + 1
 
 
+def extract_braced(text, first, after):
+    """From the line containing `first` (after `after`) through its closing brace."""
+    lines = text.splitlines()
+    base = next((i for i, l in enumerate(lines) if after in l), None)
+    if base is None:
+        raise RuntimeError("reference anchor not found: %s" % after)
+    s = next((i for i in range(base, len(lines)) if first in lines[i]), None)
+    if s is None:
+        raise RuntimeError("reference statement not found: %s" % first)
+    depth = 0
+    for k in range(s, len(lines)):
+        code = _strip_comment(lines[k])
+        depth += code.count("{") - code.count("}")
+        if depth == 0:
+            return "\n".join(lines[s:k + 1]) + "\n", s + 1
+    raise RuntimeError("unbalanced braces after: %s" % first)
+
+
 def extract_loop_to_end(text, first, after):
     """From the line containing `first` (after `after`) through the end of the first
     `for` loop that starts at or after it (brace matched)."""
@@ -301,6 +319,19 @@ NORMAL_SHADERS = [
     ("terrain2", "src/terrain/examples/terrain2/normalShader.glsl", ()),
     ("demo", "src/demo/shaders/elevation/normalShader.glsl", ()),
 ]
+# the blend programs ElevationProducer draws after the layers (index: ref_gl_elevation_tile_layers)
+BLEND_SHADERS = [
+    ("graph1", "src/graph/examples/graph1/blendShader.glsl", ()),
+    ("demo", "src/demo/shaders/elevation/blendShader.glsl", ()),
+]
+# the layers' fragment programs (index: ref_gl_layer_fragment)
+LAYER_SHADERS = [
+    ("road_graph1", "src/graph/examples/graph1/roadLayerElevationShader.glsl", ()),
+    ("road_demo", "src/demo/shaders/elevation/roadLayerElevationShader.glsl", ()),
+    ("water_river1", "src/river/examples/river1/waterLayerElevationShader.glsl", ()),
+    ("water_demo", "src/demo/shaders/elevation/waterLayerElevationShader.glsl", ()),
+    ("fill", "src/river/examples/river1/fillShader.glsl", ()),
+]
 
 _GPU_PRELUDE = r"""
 namespace refgl {
@@ -375,19 +406,30 @@ void reset_samplers(const refgl::UniformEntry *table)
 }
 }  // namespace
 
-// One elevation tile through ElevationProducer::doCreateTile and the upsample shader
-// `variant`: parent_rgba the parent slot's four channels (zf, zc, zm, 0; W*W*4, level > 0),
-// residual the residual producer's tile (residual_width^2; NULL: the producer has no
-// tile there; residual_width 0: no residual producer), noise the six noise layers
-// (W*W each, as the R16F texture holds them), noise_amp the per-level amplitudes.
-// out_rgba: the produced slot, W*W*4.  Returns 0.
-extern "C" int ref_gl_elevation_tile(int variant, int W, int level, int tx, int ty, int face,
-                                     const float *parent_rgba, const float *residual, int residual_width,
-                                     const float *noise, const float *noise_amp, int n_amp, float root_quad_size,
-                                     int grid_mesh_size, int flip, float *out_rgba)
+namespace {
+struct LayerPlanes {
+    refgl::FrameBuffer *fb;
+    const float *z, *w;
+};
+// what the layers drew: z and w into the colour attachment being drawn (COLOR0)
+void draw_layer_planes(void *arg)
+{
+    const LayerPlanes &L = *(const LayerPlanes *)arg;
+    std::vector<float> &c = L.fb->color[L.fb->draw];
+    for (int p = 0; p < L.fb->w * L.fb->h; ++p) {
+        c[(size_t)p * 4 + 2] = L.z[p];
+        c[(size_t)p * 4 + 3] = L.w[p];
+    }
+}
+
+int elevation_tile(int variant, int W, int level, int tx, int ty, int face, const float *parent_rgba,
+                   const float *residual, int residual_width, const float *noise, const float *noise_amp, int n_amp,
+                   float root_quad_size, int grid_mesh_size, int flip, int blend_variant, const float *layer_z,
+                   const float *layer_w, float *out_rgba)
 {
     using namespace refgl;
     if (variant < 0 || variant >= (int)(sizeof(g_upsample) / sizeof(g_upsample[0]))) return 1;
+    if (blend_variant >= (int)(sizeof(g_blend) / sizeof(g_blend[0]))) return 1;
     GPUTileStorage storage;
     storage.tileSize = W;
     TileCache cache;
@@ -448,9 +490,72 @@ extern "C" int ref_gl_elevation_tile(int variant, int W, int level, int tx, int 
             rproducer.tiles[std::make_tuple(level, tx / mod, ty / mod)].data = &rslot;
         }
     }
+    Program blendProg;
+    LayerPlanes planes{&fb, layer_z, layer_w};
+    if (blend_variant >= 0) {
+        // the framebuffer's COLOR0 is demTexture, which the blend program reads
+        demTex.view.data = fb.color[0].data();
+        blendProg.table = g_blend[blend_variant].table;
+        blendProg.run = g_blend[blend_variant].run;
+        reset_samplers(blendProg.table);
+        e.blend = &blendProg;
+        e.layer_hook = draw_layer_planes;
+        e.layer_arg = &planes;
+    }
     e.bind_uniforms();
     if (!e.doCreateTile(level, tx, ty, &outSlot)) return 2;
     std::memcpy(out_rgba, &outTex.store[(size_t)2 * W * W * 4], sizeof(float) * W * W * 4);
+    return 0;
+}
+}  // namespace
+
+// One elevation tile through ElevationProducer::doCreateTile and the upsample shader
+// `variant`: parent_rgba the parent slot's four channels (zf, zc, zm, 0; W*W*4, level > 0),
+// residual the residual producer's tile (residual_width^2; NULL: the producer has no
+// tile there; residual_width 0: no residual producer), noise the six noise layers
+// (W*W each, as the R16F texture holds them), noise_amp the per-level amplitudes.
+// out_rgba: the produced slot, W*W*4.  Returns 0.
+extern "C" int ref_gl_elevation_tile(int variant, int W, int level, int tx, int ty, int face,
+                                     const float *parent_rgba, const float *residual, int residual_width,
+                                     const float *noise, const float *noise_amp, int n_amp, float root_quad_size,
+                                     int grid_mesh_size, int flip, float *out_rgba)
+{
+    return elevation_tile(variant, W, level, tx, ty, face, parent_rgba, residual, residual_width, noise, noise_amp,
+                          n_amp, root_quad_size, grid_mesh_size, flip, -1, nullptr, nullptr, out_rgba);
+}
+
+// The same tile by a producer with layers: the layers draw layer_z and layer_w (W*W
+// each) into the z and w channels, then doCreateTile draws the blend program
+// `blend_variant` into COLOR1 and copies that into the slot.
+extern "C" int ref_gl_elevation_tile_layers(int variant, int blend_variant, int W, int level, int tx, int ty,
+                                            int face, const float *parent_rgba, const float *residual,
+                                            int residual_width, const float *noise, const float *noise_amp,
+                                            int n_amp, float root_quad_size, int grid_mesh_size, int flip,
+                                            const float *layer_z, const float *layer_w, float *out_rgba)
+{
+    if (blend_variant < 0) return 1;
+    return elevation_tile(variant, W, level, tx, ty, face, parent_rgba, residual, residual_width, noise, noise_amp,
+                          n_amp, root_quad_size, grid_mesh_size, flip, blend_variant, layer_z, layer_w, out_rgba);
+}
+
+// One fragment of the layer program `shader` (LAYER_SHADERS order) at the interpolated
+// varying st: uniforms river (water programs), depth and color (fill program); data
+// (4 floats) and the fragment depth it writes.  Returns 0.
+extern "C" int ref_gl_layer_fragment(int shader, int river, float depth, const float *color, float st_x, float st_y,
+                                     float *data, float *frag_depth)
+{
+    if (shader < 0 || shader >= (int)(sizeof(g_layer) / sizeof(g_layer[0]))) return 1;
+    for (const refgl::UniformEntry *e = g_layer[shader].table; e->name; ++e) {
+        const std::string n = e->name;
+        if (n == "river") *(int *)e->dst = river;
+        if (n == "depth") *(float *)e->dst = depth;
+        if (n == "color") std::memcpy(e->dst, color, 4 * sizeof(float));
+        if (n == "tileOffset") {   // both layers set (0, 0, 1): vertices are in clip coordinates
+            static const float identity[3] = {0.0f, 0.0f, 1.0f};
+            std::memcpy(e->dst, identity, sizeof(identity));
+        }
+    }
+    g_layer[shader].fragment(st_x, st_y, data, frag_depth);
     return 0;
 }
 
@@ -535,31 +640,46 @@ def generate_gpu(root):
     norm = _read(root, NORMAL_CPP)
     src = ["// generated by oracle/ref_build.py from the reference's sources\n#include <cstring>\n#include <vector>\n"
            "#include \"ork_gl.h\"\n#include \"proland/math/noise.h\"\n"]
-    shader_parts, tables = [], {"g_upsample": [], "g_normal": []}
-    for kind, shaders in (("g_upsample", UPSAMPLE_SHADERS), ("g_normal", NORMAL_SHADERS)):
+    shader_parts, tables = [], {"g_upsample": [], "g_normal": [], "g_blend": []}
+    # full-screen quads: st in pixels (upsample, normals) or in [0, 1] (blend), as
+    # each program's vertex shader makes it
+    for kind, shaders, unit in (("g_upsample", UPSAMPLE_SHADERS, False), ("g_normal", NORMAL_SHADERS, False),
+                                ("g_blend", BLEND_SHADERS, True)):
         for name, rel, defines in shaders:
             ns = "%s_%s" % (kind[2:], name)
             body, uniforms, _ = ref_glsl.shader_to_cpp(_read(root, rel), ns, "_FRAGMENT_", defines)
             shader_parts.append("// %s\n%s%s%s" % (rel, body, ref_glsl.uniform_table(ns, uniforms),
-                                                  ref_glsl.quad_runner(ns)))
+                                                  ref_glsl.quad_runner(ns, unit)))
             tables[kind].append(ns)
+    layers = []
+    for name, rel, defines in LAYER_SHADERS:
+        ns = "layer_%s" % name
+        body, uniforms, others = ref_glsl.shader_to_cpp(_read(root, rel), ns, "_FRAGMENT_", defines)
+        shader_parts.append("// %s\n%s%s%s" % (rel, body, ref_glsl.uniform_table(ns, uniforms),
+                                              ref_glsl.fragment_call(ns, any(n == "st" for _, n in others))))
+        layers.append(ns)
     src.extend(shader_parts)
     src.append(_GPU_PRELUDE)
     src.append("namespace {\nstruct ProgramSource { const refgl::UniformEntry *table; void (*run)(refgl::FrameBuffer &); };\n")
     for kind, names in tables.items():
         src.append("const ProgramSource %s[] = {%s};\n" % (kind, ", ".join("{%s_uniforms, %s_run}" % (n, n)
                                                                              for n in names)))
+    src.append("struct FragmentSource { const refgl::UniformEntry *table; void (*fragment)(float, float, float *, "
+               "float *); };\nconst FragmentSource g_layer[] = {%s};\n"
+               % ", ".join("{%s_uniforms, %s_fragment}" % (n, n) for n in layers))
     src.append("}  // namespace\n")
     ups, ups_line = extract_block(elev, 'this->tileWSDFU = upsample->getUniform4f("tileWSDF");',
                                   'this->noiseUVLHU = upsample->getUniform4f("noiseUVLH");',
                                   after="void ElevationProducer::init(")
+    bls, bls_line = extract_braced(elev, "if (this->blend != NULL) {", after="void ElevationProducer::init(")
     dct, dct_line = extract_function(elev, r"bool\s+ElevationProducer::doCreateTile\s*\(")
     nups, nups_line = extract_block(norm, 'this->tileSDFU = normals->getUniform3f("tileSDF");',
                                     'this->deformU = normals->getUniform4f("deform");',
                                     after="void NormalProducer::init(")
     ndct, ndct_line = extract_function(norm, r"bool\s+NormalProducer::doCreateTile\s*\(")
     src.append("namespace refgl {\n")
-    src.append("// %s:%d\nvoid ElevationProducer::bind_uniforms()\n{\n%s}\n" % (ELEV_CPP, ups_line, ups))
+    src.append("void ElevationProducer::bind_uniforms()\n{\n// %s:%d\n%s// %s:%d\n%s}\n"
+               % (ELEV_CPP, ups_line, ups, ELEV_CPP, bls_line, bls))
     src.append("// %s:%d\n%s" % (ELEV_CPP, dct_line, dct))
     src.append("// %s:%d\nvoid NormalProducer::bind_uniforms()\n{\n%s}\n" % (NORMAL_CPP, nups_line, nups))
     src.append("// %s:%d\n%s" % (NORMAL_CPP, ndct_line, ndct))
@@ -578,7 +698,8 @@ def build(root=DEFAULT_ROOT, force=False):
     if not os.path.isdir(os.path.join(root, "src")):
         return LIB if os.path.exists(LIB) else None
     srcs = [os.path.join(root, p) for p in (NOISE_CPP, ELEV_CPP, CPU_ELEV_CPP, MIPMAP_CPP, NORMAL_CPP)]
-    srcs += [os.path.join(root, rel) for _, rel, _ in UPSAMPLE_SHADERS + NORMAL_SHADERS]
+    srcs += [os.path.join(root, rel) for _, rel, _ in UPSAMPLE_SHADERS + NORMAL_SHADERS + BLEND_SHADERS +
+             LAYER_SHADERS]
     srcs += [os.path.abspath(__file__), os.path.join(HERE, "ref_glsl.py")]
     srcs += [os.path.join(HERE, "ref_stubs", h) for h in ("pmath.h", "glsl.h", "ork_gl.h")]
     if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= max(os.path.getmtime(p) for p in srcs):

@@ -167,16 +167,34 @@ def uniform_table(ns, uniforms):
             % (ns, "\n".join(rows)))
 
 
-def quad_runner(ns):
-    """drawQuad of a full-screen quad: the fragment shader at every pixel centre."""
+def quad_runner(ns, unit=False):
+    """drawQuad of a full-screen quad: the fragment shader at every pixel centre, with
+    st the centre in pixels, or divided by the viewport size when `unit` (the vertex
+    shaders make st = (vertex.xy * 0.5 + 0.5) * tileWidth or vertex.xy * 0.5 + 0.5)."""
+    sx = "((float)i + 0.5f) / (float)fb.w" if unit else "(float)i + 0.5f"
+    sy = "((float)j + 0.5f) / (float)fb.h" if unit else "(float)j + 0.5f"
     return """static void %(ns)s_run(refgl::FrameBuffer &fb)
 {
     for (int j = 0; j < fb.h; ++j)
         for (int i = 0; i < fb.w; ++i) {
-            glsl::%(ns)s::st = glsl::vec2((float)i + 0.5f, (float)j + 0.5f);
+            glsl::%(ns)s::st = glsl::vec2(%(sx)s, %(sy)s);
             glsl::%(ns)s::gl_FragCoord = glsl::vec4((float)i + 0.5f, (float)j + 0.5f, 0.0f, 1.0f);
             glsl::%(ns)s::shader_main();
             fb.write(i, j, glsl::%(ns)s::data.c);
         }
 }
-""" % {"ns": ns}
+""" % {"ns": ns, "sx": sx, "sy": sy}
+
+
+def fragment_call(ns, has_st):
+    """One fragment at the interpolated varying st: data and gl_FragDepth (NaN when
+    the shader leaves it unwritten)."""
+    return """static void %(ns)s_fragment(float sx, float sy, float *data, float *depth)
+{
+    %(st)s
+    glsl::%(ns)s::gl_FragDepth = std::nanf("");
+    glsl::%(ns)s::shader_main();
+    for (int k = 0; k < 4; ++k) data[k] = glsl::%(ns)s::data.c[k];
+    *depth = glsl::%(ns)s::gl_FragDepth;
+}
+""" % {"ns": ns, "st": ("glsl::%s::st = glsl::vec2(sx, sy);" % ns) if has_st else "(void)sx; (void)sy;"}

@@ -14,7 +14,8 @@
 //   pixel (i, j) of the viewport with the varying st = (i + 0.5, j + 0.5), the
 //   pixel centre of the full-screen quad, and stores `data` into the colour
 //   attachment; clear() fills it with the clear colour.
-// * GPUSlot::copyPixels copies the colour attachment into the slot's layer.
+// * GPUSlot::copyPixels copies the read colour attachment into the slot's layer.
+// * TileProducer::doCreateTile (drawing the layers) runs a hook the harness gives.
 // * Texture2D::setSubImage copies float pixels in.
 // * vec3<T>, vec4<T>, mat3<T>, mat4<T>: component-wise arithmetic in T;
 //   length = sqrt(x*x + y*y + z*z), normalize divides each component by it
@@ -279,7 +280,7 @@ struct Program {
 struct FrameBuffer {
     int w = 0, h = 0;
     vector<float> color[2];  // RGBA float attachments COLOR0, COLOR1
-    int draw = 0;
+    int draw = 0, read = 0;
     float clear_color[4] = {0, 0, 0, 0};
     void init(int W)
     {
@@ -303,7 +304,7 @@ struct FrameBuffer {
     }
     void setDepthTest(bool, Function = LESS) {}
     void setDrawBuffer(BufferId b) { draw = b == COLOR1 ? 1 : 0; }
-    void setReadBuffer(BufferId) {}
+    void setReadBuffer(BufferId b) { read = b == COLOR1 ? 1 : 0; }
 };
 
 // ---- tile storage, cache and producers ------------------------------------------------------
@@ -337,7 +338,7 @@ struct GPUTileStorage : TileStorage {
             for (int j = 0; j < h; ++j)
                 for (int i = 0; i < w; ++i)
                     for (int k = 0; k < comps; ++k) {
-                        float v = fb->color[fb->draw][((size_t)(y + j) * fb->w + x + i) * 4 + k];
+                        float v = fb->color[fb->read][((size_t)(y + j) * fb->w + x + i) * 4 + k];
                         if (unorm8) v = std::floor((v < 0.0f ? 0.0f : (v > 1.0f ? 1.0f : v)) * 255.0f + 0.5f) / 255.0f;
                         tx.store[(((size_t)l * tx.view.h + y + j) * tx.view.w + x + i) * comps + k] = v;
                     }
@@ -377,8 +378,16 @@ struct TileProducer {
     float getRootQuadSize() { return rootQuadSize; }
     int getBorder() { return border; }
     int getId() { return 0; }
-    bool hasLayers() { return false; }
-    bool doCreateTile(int, int, int, TileStorage::Slot *) { return true; }
+    // the layers: what TileProducer::doCreateTile draws is supplied by the harness
+    // (layer_hook, run when the producer has layers)
+    void (*layer_hook)(void *) = nullptr;
+    void *layer_arg = nullptr;
+    bool hasLayers() { return layer_hook != nullptr; }
+    bool doCreateTile(int, int, int, TileStorage::Slot *)
+    {
+        if (layer_hook) layer_hook(layer_arg);
+        return true;
+    }
 };
 
 }  // namespace refgl

@@ -23,7 +23,10 @@ What is compared, and how tightly:
   (normalShader.glsl getWorldPosition) and differences them, the oracle uses the
   exact sample spacing 2h; float normals agree within that position rounding
   (the bound below), 8-bit normals within one step; coarse normals (nc) bit for
-  bit.
+  bit;
+* the layers' fragment programs (road, water with river = 0, 1, 2, fill) bit for
+  bit, and a producer with layers: the blend programs of graph1 and the demo
+  drawn by ElevationProducer::doCreateTile after given layer planes, bit for bit.
 
 Texture sampling is the oracle's documented choice (the nearest texel) on both
 sides.  Runs where the reference tree is present; skipped elsewhere."""
@@ -230,3 +233,90 @@ def test_flat_normal_tiles(ref, oracle_lib, variant, fmt):
                     assert np.mean(d > 0) <= 0.005, (variant, fmt, level, k, np.mean(d > 0))
             else:
                 assert d.max() <= bound, (variant, fmt, level, k, d.max(), bound)
+
+
+LAYER = {"road_graph1": 0, "road_demo": 1, "water_river1": 2, "water_demo": 3, "fill": 4}
+BLEND = {"graph1": 0, "demo": 1}
+
+
+def gl_fragment(ref, shader, st, river=0, depth=0.0, color=(0.0, 0.0, 0.0, 0.0)):
+    import ctypes as C
+    data = np.empty(4, np.float32)
+    fd = C.c_float()
+    col = np.asarray(color, np.float32)
+    assert ref.ref_gl_layer_fragment(LAYER[shader], river, depth, _p(col), float(st[0]), float(st[1]), _p(data),
+                                     C.byref(fd)) == 0
+    return data, fd.value
+
+
+def _attributes(rng, n):
+    """Interpolated (altitude, signed width coordinate) pairs, the smoothstep edges included."""
+    a = rng.uniform(-500.0, 3000.0, n).astype(np.float32)
+    u = rng.uniform(-3.0, 3.0, n).astype(np.float32)
+    edges = np.float32([0.0, 0.98, 0.99, 1.0, 1.5, 2.0, 2.5])
+    u[:2 * len(edges)] = np.concatenate([edges, -edges])
+    return a, u
+
+
+@pytest.mark.parametrize("shader", ["road_graph1", "road_demo", "water_river1", "water_demo"])
+def test_layer_fragment_programs(ref, oracle_lib, shader):
+    """The road and water layers' fragment shaders at random interpolated attributes
+    against the oracle's programs: z and w bit for bit, the written depth once the
+    depth buffer clamps it to [0, 1]; x and y written 0 (masked off by the layers)."""
+    a, u = _attributes(np.random.default_rng(LAYER[shader]), 3000)
+    rivers = [0] if shader.startswith("road") else [0, 1, 2]
+    for river in rivers:
+        program = 0 if shader.startswith("road") else 1 + river
+        for ai, ui in zip(a, u):
+            data, fd = gl_fragment(ref, shader, (ai, ui), river=river)
+            dp, z, w = oracle_lib.layer_fragment(program, ai, ui)
+            assert (np.float32(data[2]), np.float32(data[3])) == (np.float32(z), np.float32(w)), (shader, river, ai, ui)
+            assert np.float32(min(max(fd, 0.0), 1.0)) == np.float32(dp), (shader, river, ai, ui, fd, dp)
+            assert data[0] == 0.0 and data[1] == 0.0
+
+
+def test_fill_fragment_program(ref, oracle_lib):
+    """fillShader writes its colour uniform and depth uniform; the oracle's fill program
+    carries the colour's z and w as the mesh's attributes and the depth as its
+    fill depth (WaterElevationLayer.cpp:273-276 sets colour 0 and depth 0.02)."""
+    rng = np.random.default_rng(5)
+    cases = [((0.0, 0.0, 0.0, 0.0), 0.02)] + [(tuple(rng.uniform(-100, 100, 4)), float(d))
+                                             for d in rng.uniform(-0.5, 1.5, 40)]
+    for color, depth in cases:
+        data, fd = gl_fragment(ref, "fill", (0.0, 0.0), depth=depth, color=color)
+        col = np.float32(color)
+        dp, z, w = oracle_lib.layer_fragment(4, col[2], col[3], fill_depth=depth)
+        assert np.array_equal(data, col)
+        assert (np.float32(z), np.float32(w)) == (col[2], col[3])
+        assert np.float32(min(max(fd, 0.0), 1.0)) == np.float32(dp)
+
+
+@pytest.mark.parametrize("blend", sorted(BLEND))
+@pytest.mark.parametrize("variant", ["terrain1", "demo"])
+def test_layered_tiles_blend(ref, oracle_lib, noise_tables, variant, blend):
+    """A producer with layers: ElevationProducer::doCreateTile draws the upsample quad,
+    the layers (here: given z and w planes written into the z and w channels), then the
+    blend program into COLOR1, and copies COLOR1 into the slot.  zf and zc pass
+    through, the layers' w is kept in the fourth channel, and zm is the oracle's blend
+    of the oracle's zf with the layers' planes -- bit for bit on integer parents."""
+    import ctypes as C
+    rng = np.random.default_rng(3 + BLEND[blend] + 5 * UPSAMPLE[variant])
+    W, grid = 101, 24
+    for k, (level, tx, ty) in enumerate(TILES[:5]):
+        parent, residual, rw = _case(rng, W, level, True, False, "same")
+        z = (rng.standard_normal((W, W)) * 200.0).astype(np.float32)
+        w = rng.choice(np.float32([0.0, 0.0, 0.25, 0.5, 1.0, 1.0, 1.7]), (W, W)).astype(np.float32)
+        w[rng.uniform(size=(W, W)) < 0.3] = np.float32(rng.uniform())
+        prgba = None
+        if parent is not None:
+            prgba = np.ascontiguousarray(np.stack(list(parent) + [np.zeros_like(parent[0])], -1), np.float32)
+        out = np.empty((W, W, 4), np.float32)
+        rc = ref.ref_gl_elevation_tile_layers(UPSAMPLE[variant], BLEND[blend], W, level, tx, ty, 0, _p(prgba),
+                                              _p(residual), rw, _p(noise_tables[W]), _p(AMPS), len(AMPS),
+                                              C.c_float(60000.0), grid, 0, _p(z), _p(w), _p(out))
+        assert rc == 0
+        wf, wc, _ = oracle_elevation(oracle_lib, variant, W, level, tx, ty, 0, parent, residual, rw,
+                                     noise_tables[W], 60000.0, grid, False)
+        assert np.array_equal(out[..., 0], wf) and np.array_equal(out[..., 1], wc), (variant, level)
+        assert np.array_equal(out[..., 2], oracle_lib.layer_blend(W, wf, z, w, BLEND[blend])), (variant, blend, level)
+        assert np.array_equal(out[..., 3], w)
