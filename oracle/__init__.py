@@ -646,5 +646,8 @@ def ref_lib():
                                                                    C.c_float, C.c_int, C.c_int, _f32p, _f32p, _f32p]
         L.ref_gl_layer_fragment.argtypes = [C.c_int, C.c_int, C.c_float, _f32p, C.c_float, C.c_float, _f32p,
                                             C.POINTER(C.c_float)]
+        L.ref_ortho_noise.argtypes = [C.c_int, C.c_void_p]
+        L.ref_gl_ortho_tile.argtypes = [C.c_int] * 6 + [C.c_void_p] * 3 + [_f32p, C.c_int, _f32p, _f32p, C.c_int,
+                                                                            C.c_float, _f32p]
         _REF = L
     return _REF

@@ -27,17 +27,22 @@ as they are written, read from the reference tree at build time:
 
 The GPU path, in a second unit (``ref_gpu.cpp``):
 
-* ``ElevationProducer::doCreateTile`` (``ElevationProducer.cpp:280-405``) and
+* ``ElevationProducer::doCreateTile`` (``ElevationProducer.cpp:280-405``, its layered
+  branch included, the layers themselves given) and
   ``NormalProducer::doCreateTile`` (``NormalProducer.cpp:164-281``), the functions
   as written, with the uniform look-ups of their ``init`` functions, on stand-ins
   for the Ork engine types they call (``oracle/ref_stubs/ork_gl.h``: uniforms that
   write into the shader's variables, a framebuffer whose ``drawQuad`` runs the
   fragment shader at every pixel, slots backed by float arrays, Ork's vector and
   matrix arithmetic);
+* ``OrthoProducer::doCreateTile`` (``ortho/OrthoProducer.cpp:273-385``) the same way,
+  and ``createOrthoNoise`` (``:26-122``) in the first unit;
 * the shaders those functions draw -- the upsample shaders of terrain1, terrain2,
   terrain4 (flipped diagonals) and the demo (modulated noise, with and without
   ``NO_CLAMP``), the normal shaders of terrain1, terrain2 (sphere) and the demo
-  (coarse normals, four output formats) -- rewritten mechanically into C++ by
+  (coarse normals, four output formats), the blend shaders of graph1 and the demo,
+  the ortho upsample shaders of terrain3 and the demo -- and the layers' fragment
+  shaders (road, water, fill), rewritten mechanically into C++ by
   ``oracle/ref_glsl.py`` and compiled against ``oracle/ref_stubs/glsl.h``.
 
 Texture sampling is the choice the oracle makes (nearest texel, clamped to the
@@ -70,6 +75,7 @@ NOISE_DIR = "src/core/sources"
 ELEV_CPP = "src/terrain/sources/proland/dem/ElevationProducer.cpp"
 CPU_ELEV_CPP = "src/terrain/sources/proland/dem/CPUElevationProducer.cpp"
 MIPMAP_CPP = "src/terrain/sources/proland/preprocess/terrain/HeightMipmap.cpp"
+ORTHO_CPP = "src/terrain/sources/proland/ortho/OrthoProducer.cpp"
 
 
 def _read(root, rel):
@@ -168,16 +174,17 @@ using namespace std;
 namespace proland {
 // createDemNoise builds a texture from its float array: these stand-ins copy the
 // array out instead.
-static float *g_captured = nullptr;
-enum { R16F, RED, FLOAT, REPEAT, NEAREST };
+static void *g_captured = nullptr;
+enum { R16F, RED, FLOAT, REPEAT, NEAREST, RGBA8, RGBA, UNSIGNED_BYTE };
 struct CPUBuffer { const void *data; explicit CPUBuffer(const void *d) : data(d) {} };
 struct Buffer { struct Parameters {}; };
 struct Texture { struct Parameters {
     Parameters &wrapS(int) { return *this; } Parameters &wrapT(int) { return *this; }
     Parameters &min(int) { return *this; } Parameters &mag(int) { return *this; } }; };
 struct Texture2DArray {
-    Texture2DArray(int w, int h, int layers, int, int, int, Texture::Parameters, Buffer::Parameters, CPUBuffer b) {
-        if (g_captured) memcpy(g_captured, b.data, sizeof(float) * (size_t)w * h * layers);
+    Texture2DArray(int w, int h, int layers, int, int, int type, Texture::Parameters, Buffer::Parameters, CPUBuffer b) {
+        const size_t texel = type == UNSIGNED_BYTE ? 4 : sizeof(float);   // RGBA bytes or one float
+        if (g_captured) memcpy(g_captured, b.data, texel * (size_t)w * h * layers);
     }
 };
 template <class T> struct ptr {
@@ -220,6 +227,8 @@ def generate(root):
     cpu = _read(root, CPU_ELEV_CPP)
     mip = _read(root, MIPMAP_CPP)
     dem, dem_line = extract_function(elev, r"ptr<Texture2DArray>\s+createDemNoise\s*\(\s*int\s+tileWidth\s*\)")
+    orn, orn_line = extract_function(_read(root, ORTHO_CPP),
+                                     r"ptr<Texture2DArray>\s+createOrthoNoise\s*\(\s*int\s+tileWidth\s*\)")
     sel, sel_line = extract_block(elev, "int noiseL = 0;", "noiseL = noiseLs[noiseL];",
                                   after="bool ElevationProducer::doCreateTile(")
     loop, loop_line = extract_loop_to_end(cpu, "int residualTileWidth =", after="bool CPUElevationProducer::doCreateTile(")
@@ -229,6 +238,7 @@ def generate(root):
         fns.append(("HeightMipmap.cpp:%d" % line, body))
     src = [_PRELUDE]
     src.append("namespace proland {\n// %s:%d\n%s}  // namespace proland\n" % (ELEV_CPP, dem_line, dem))
+    src.append("namespace proland {\n// %s:%d\n%s}  // namespace proland\n" % (ORTHO_CPP, orn_line, orn))
     src.append(r"""
 extern "C" long ref_lrandom(long *seed) { return proland::lrandom(seed); }
 extern "C" float ref_frandom(long *seed) { return proland::frandom(seed); }
@@ -237,6 +247,12 @@ extern "C" void ref_dem_noise(int W, float *out)
 {
     proland::g_captured = out;
     proland::createDemNoise(W);
+    proland::g_captured = nullptr;
+}
+extern "C" void ref_ortho_noise(int W, unsigned char *out)
+{
+    proland::g_captured = out;
+    proland::createOrthoNoise(W);
     proland::g_captured = nullptr;
 }
 """)
@@ -324,6 +340,11 @@ BLEND_SHADERS = [
     ("graph1", "src/graph/examples/graph1/blendShader.glsl", ()),
     ("demo", "src/demo/shaders/elevation/blendShader.glsl", ()),
 ]
+# the ortho producer's upsample programs (index: ref_gl_ortho_tile)
+ORTHO_SHADERS = [
+    ("terrain3", "src/terrain/examples/terrain3/upsampleOrthoShader.glsl", ()),
+    ("demo", "src/demo/shaders/ortho/upsampleOrthoShader.glsl", ()),
+]
 # the layers' fragment programs (index: ref_gl_layer_fragment)
 LAYER_SHADERS = [
     ("road_graph1", "src/graph/examples/graph1/roadLayerElevationShader.glsl", ()),
@@ -382,6 +403,33 @@ struct NormalProducer : TileProducer {
     ptr<UniformMatrix3f> worldToTangentFrameU;
     ptr<UniformMatrix3f> parentToTangentFrameU;
     ptr<Uniform4f> deformU;
+    void bind_uniforms();
+    bool doCreateTile(int level, int tx, int ty, TileStorage::Slot *data);
+};
+
+// The members OrthoProducer::doCreateTile and its init's look-ups use (OrthoProducer.h).
+struct OrthoProducer : TileProducer {
+    ptr<FrameBuffer> frameBuffer;
+    ptr<TileProducer> residualTiles;
+    ptr<Texture2D> orthoTexture, residualTexture;
+    int face = 0;
+    ptr<Program> upsample;
+    int channels = 4;
+    int maxLevel = -1;
+    ptr<Texture2DArray> noiseTexture;
+    vec4f rootNoiseColor, noiseColor;
+    vector<float> noiseAmp;
+    bool noiseHsv = false;
+    float scale = 1.0f;
+    ptr<Uniform1f> tileWidthU;
+    ptr<UniformSampler> coarseLevelSamplerU;
+    ptr<Uniform4f> coarseLevelOSLU;
+    ptr<UniformSampler> residualSamplerU;
+    ptr<Uniform4f> residualOSHU;
+    ptr<UniformSampler> noiseSamplerU;
+    ptr<Uniform4i> noiseUVLHU;
+    ptr<Uniform4f> noiseColorU;
+    ptr<Uniform4f> rootNoiseColorU;
     void bind_uniforms();
     bool doCreateTile(int level, int tx, int ty, TileStorage::Slot *data);
 };
@@ -538,6 +586,81 @@ extern "C" int ref_gl_elevation_tile_layers(int variant, int blend_variant, int 
                           n_amp, root_quad_size, grid_mesh_size, flip, blend_variant, layer_z, layer_w, out_rgba);
 }
 
+// One ortho tile through OrthoProducer::doCreateTile and the upsample shader `variant`:
+// parent the parent slot's RGBA8 texels (W*W*4 bytes; level > 0), residual the residual
+// producer's RGBA8 tile (W*W*4 bytes; NULL: the producer has no tile there), noise
+// createOrthoNoise's six RGBA8 layers, noise_amp the per-level amplitudes, the colours,
+// the HSV flag and the residual scale as OrthoProducer::init takes them.  out: what the
+// fragment shader writes (W*W*4 floats, result / 255), before the RGBA8 framebuffer
+// rounds it.  Returns 0.
+extern "C" int ref_gl_ortho_tile(int variant, int W, int level, int tx, int ty, int face, const unsigned char *parent,
+                                 const unsigned char *residual, const unsigned char *noise, const float *noise_amp,
+                                 int n_amp, const float *root_color, const float *noise_color, int hsv, float scale,
+                                 float *out)
+{
+    using namespace refgl;
+    if (variant < 0 || variant >= (int)(sizeof(g_ortho) / sizeof(g_ortho[0]))) return 1;
+    GPUTileStorage storage;
+    storage.tileSize = W;
+    TileCache cache;
+    cache.storage = &storage;
+    Texture2DArray parentTex, outTex, noiseTex;
+    parentTex.alloc(W, W, 2, 4, false);
+    parentTex.format = RGBA8;
+    outTex.alloc(W, W, 3, 4, false);   // float: the shader's output is returned unrounded
+    noiseTex.alloc(W, W, 6, 4, true);
+    noiseTex.format = RGBA8;
+    for (size_t k = 0; k < (size_t)6 * W * W * 4; ++k) noiseTex.store[k] = (float)noise[k] / 255.0f;
+    Texture2D residualTex, orthoTex;
+    residualTex.alloc(W, W, 1, 4, false);
+    residualTex.format = RGBA8;
+    FrameBuffer fb;
+    fb.init(W);
+    Program prog;
+    prog.table = g_ortho[variant].table;
+    prog.run = g_ortho[variant].run;
+    reset_samplers(prog.table);
+
+    OrthoProducer o;
+    o.cache = &cache;
+    o.frameBuffer = &fb;
+    o.upsample = &prog;
+    o.noiseTexture = &noiseTex;
+    o.residualTexture = &residualTex;
+    o.orthoTexture = &orthoTex;
+    o.rootNoiseColor = vec4f(root_color[0], root_color[1], root_color[2], root_color[3]);
+    o.noiseColor = vec4f(noise_color[0], noise_color[1], noise_color[2], noise_color[3]);
+    o.noiseAmp.assign(noise_amp, noise_amp + n_amp);
+    o.noiseHsv = hsv != 0;
+    o.scale = scale;
+    o.face = face;
+    GPUTileStorage::GPUSlot parentSlot, outSlot;
+    parentSlot.owner = outSlot.owner = &storage;
+    parentSlot.t = &parentTex;
+    parentSlot.l = 1;
+    outSlot.t = &outTex;
+    outSlot.l = 2;
+    if (level > 0) {
+        for (size_t k = 0; k < (size_t)W * W * 4; ++k) parentTex.store[(size_t)W * W * 4 + k] = (float)parent[k] / 255.0f;
+        o.tiles[std::make_tuple(level - 1, tx / 2, ty / 2)].data = &parentSlot;
+    }
+    CPUTileStorage<unsigned char> rstorage;
+    rstorage.tileSize = W;
+    TileCache rcache;
+    rcache.storage = &rstorage;
+    TileProducer rproducer;
+    rproducer.cache = &rcache;
+    CPUTileStorage<unsigned char>::CPUSlot rslot;
+    rslot.owner = &rstorage;
+    rslot.data = (unsigned char *)residual;
+    if (residual) rproducer.tiles[std::make_tuple(level, tx, ty)].data = &rslot;
+    o.residualTiles = &rproducer;
+    o.bind_uniforms();
+    if (!o.doCreateTile(level, tx, ty, &outSlot)) return 2;
+    std::memcpy(out, &outTex.store[(size_t)2 * W * W * 4], sizeof(float) * W * W * 4);
+    return 0;
+}
+
 // One fragment of the layer program `shader` (LAYER_SHADERS order) at the interpolated
 // varying st: uniforms river (water programs), depth and color (fill program); data
 // (4 floats) and the fragment depth it writes.  Returns 0.
@@ -640,11 +763,11 @@ def generate_gpu(root):
     norm = _read(root, NORMAL_CPP)
     src = ["// generated by oracle/ref_build.py from the reference's sources\n#include <cstring>\n#include <vector>\n"
            "#include \"ork_gl.h\"\n#include \"proland/math/noise.h\"\n"]
-    shader_parts, tables = [], {"g_upsample": [], "g_normal": [], "g_blend": []}
+    shader_parts, tables = [], {"g_upsample": [], "g_normal": [], "g_blend": [], "g_ortho": []}
     # full-screen quads: st in pixels (upsample, normals) or in [0, 1] (blend), as
     # each program's vertex shader makes it
     for kind, shaders, unit in (("g_upsample", UPSAMPLE_SHADERS, False), ("g_normal", NORMAL_SHADERS, False),
-                                ("g_blend", BLEND_SHADERS, True)):
+                                ("g_blend", BLEND_SHADERS, True), ("g_ortho", ORTHO_SHADERS, False)):
         for name, rel, defines in shaders:
             ns = "%s_%s" % (kind[2:], name)
             body, uniforms, _ = ref_glsl.shader_to_cpp(_read(root, rel), ns, "_FRAGMENT_", defines)
@@ -677,12 +800,19 @@ def generate_gpu(root):
                                     'this->deformU = normals->getUniform4f("deform");',
                                     after="void NormalProducer::init(")
     ndct, ndct_line = extract_function(norm, r"bool\s+NormalProducer::doCreateTile\s*\(")
+    ortho = _read(root, ORTHO_CPP)
+    oups, oups_line = extract_block(ortho, 'tileWidthU = upsample->getUniform1f("tileWidth");',
+                                    'rootNoiseColorU = upsample->getUniform4f("rootNoiseColor");',
+                                    after="void OrthoProducer::init(")
+    odct, odct_line = extract_function(ortho, r"bool\s+OrthoProducer::doCreateTile\s*\(")
     src.append("namespace refgl {\n")
     src.append("void ElevationProducer::bind_uniforms()\n{\n// %s:%d\n%s// %s:%d\n%s}\n"
                % (ELEV_CPP, ups_line, ups, ELEV_CPP, bls_line, bls))
     src.append("// %s:%d\n%s" % (ELEV_CPP, dct_line, dct))
     src.append("// %s:%d\nvoid NormalProducer::bind_uniforms()\n{\n%s}\n" % (NORMAL_CPP, nups_line, nups))
     src.append("// %s:%d\n%s" % (NORMAL_CPP, ndct_line, ndct))
+    src.append("// %s:%d\nvoid OrthoProducer::bind_uniforms()\n{\n%s}\n" % (ORTHO_CPP, oups_line, oups))
+    src.append("// %s:%d\n%s" % (ORTHO_CPP, odct_line, odct))
     src.append("}  // namespace refgl\n")
     src.append(_GPU_DRIVERS)
     os.makedirs(GEN_DIR, exist_ok=True)
@@ -697,9 +827,9 @@ def build(root=DEFAULT_ROOT, force=False):
     None without the reference (the GPU machine has none; the pin runs where it is)."""
     if not os.path.isdir(os.path.join(root, "src")):
         return LIB if os.path.exists(LIB) else None
-    srcs = [os.path.join(root, p) for p in (NOISE_CPP, ELEV_CPP, CPU_ELEV_CPP, MIPMAP_CPP, NORMAL_CPP)]
+    srcs = [os.path.join(root, p) for p in (NOISE_CPP, ELEV_CPP, CPU_ELEV_CPP, MIPMAP_CPP, NORMAL_CPP, ORTHO_CPP)]
     srcs += [os.path.join(root, rel) for _, rel, _ in UPSAMPLE_SHADERS + NORMAL_SHADERS + BLEND_SHADERS +
-             LAYER_SHADERS]
+             LAYER_SHADERS + ORTHO_SHADERS]
     srcs += [os.path.abspath(__file__), os.path.join(HERE, "ref_glsl.py")]
     srcs += [os.path.join(HERE, "ref_stubs", h) for h in ("pmath.h", "glsl.h", "ork_gl.h")]
     if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= max(os.path.getmtime(p) for p in srcs):

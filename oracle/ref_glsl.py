@@ -27,7 +27,8 @@ for _set in ("xyzw", "rgba", "stpq"):
         _SWZ[_c] = _i
 
 _TYPES = {"float": "U_FLOAT", "int": "U_INT", "vec2": "U_VEC2", "vec3": "U_VEC3", "vec4": "U_VEC4",
-          "mat3": "U_MAT3", "mat4": "U_MAT4", "sampler2D": "U_SAMPLER2D", "sampler2DArray": "U_SAMPLER2DARRAY"}
+          "ivec4": "U_IVEC4", "mat3": "U_MAT3", "mat4": "U_MAT4", "sampler2D": "U_SAMPLER2D",
+          "sampler2DArray": "U_SAMPLER2DARRAY"}
 
 
 def strip_comments(src):

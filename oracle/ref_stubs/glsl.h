@@ -153,6 +153,11 @@ typedef vec<2> vec2;
 typedef vec<3> vec3;
 typedef vec<4> vec4;
 
+// integer vectors: only as uniforms whose components are read (v.x is v.c[0])
+struct ivec4 {
+    int c[4] = {0, 0, 0, 0};
+};
+
 #define GLSL_BINOP(OP)                                                                       \
     template <int N> inline vec<N> operator OP(const vec<N> &a, const vec<N> &b)            \
     {                                                                                        \

@@ -1,7 +1,7 @@
 // Stand-ins for the parts of Ork (the engine the reference builds on, not part of
 // the reference tree) that the extracted GPU producer code calls:
-// ElevationProducer::doCreateTile and NormalProducer::doCreateTile, and the
-// uniform look-ups of their init functions.  TEST INFRASTRUCTURE ONLY
+// ElevationProducer::doCreateTile, NormalProducer::doCreateTile and
+// OrthoProducer::doCreateTile, and the uniform look-ups of their init functions.  TEST INFRASTRUCTURE ONLY
 // (oracle/ref_build.py compiles them with the extracted code and the reference's
 // shaders, rewritten as C++ against glsl.h).
 //
@@ -16,7 +16,7 @@
 //   attachment; clear() fills it with the clear colour.
 // * GPUSlot::copyPixels copies the read colour attachment into the slot's layer.
 // * TileProducer::doCreateTile (drawing the layers) runs a hook the harness gives.
-// * Texture2D::setSubImage copies float pixels in.
+// * Texture2D::setSubImage copies float or byte pixels in.
 // * vec3<T>, vec4<T>, mat3<T>, mat4<T>: component-wise arithmetic in T;
 //   length = sqrt(x*x + y*y + z*z), normalize divides each component by it
 //   (and reports it), crossProduct the determinant form, matrices row-major
@@ -86,6 +86,9 @@ template <class T> struct vec4 {
     T x, y, z, w;
     vec4() : x(0), y(0), z(0), w(0) {}
     vec4(T a, T b, T c, T d) : x(a), y(b), z(c), w(d) {}
+    vec4 operator*(const vec4 &o) const { return vec4(x * o.x, y * o.y, z * o.z, w * o.w); }
+    vec4 operator*(T s) const { return vec4(x * s, y * s, z * s, w * s); }
+    vec4 operator/(T s) const { return vec4(x / s, y / s, z / s, w / s); }
     template <class U> vec4<U> cast() const { return vec4<U>((U)x, (U)y, (U)z, (U)w); }
 };
 
@@ -138,6 +141,7 @@ typedef vec3<float> vec3f;
 typedef vec3<double> vec3d;
 typedef vec4<float> vec4f;
 typedef vec4<double> vec4d;
+typedef vec4<int> vec4i;
 typedef mat3<float> mat3f;
 typedef mat3<double> mat3d;
 typedef mat4<float> mat4f;
@@ -152,7 +156,7 @@ struct Logger {
 // ---- textures, buffers -----------------------------------------------------------------
 enum TextureInternalFormat { R16F, R32F, RG8, RGBA8, RG32F, RGBA32F, RGB32F };
 enum TextureFormat { RED, RG, RGB, RGBA };
-enum PixelType { FLOAT };
+enum PixelType { FLOAT, UNSIGNED_BYTE };
 enum BufferId { COLOR0, COLOR1, DEPTH };
 enum Function { LESS, ALWAYS, NOTEQUAL };
 
@@ -186,19 +190,26 @@ struct Texture {
     int getHeight() { return view.h; }
 };
 struct Texture2D : Texture {
-    // RED FLOAT pixels into a single-component texture
-    void setSubImage(int, int x, int y, int w, int h, TextureFormat, PixelType, const Buffer::Parameters &,
+    // FLOAT or UNSIGNED_BYTE pixels of 1-4 components (RED, RG, RGB, RGBA) into the
+    // texture's first components; a byte k reads back as k / 255 (GL's unorm8)
+    void setSubImage(int, int x, int y, int w, int h, TextureFormat f, PixelType t, const Buffer::Parameters &,
                      const Buffer &pixels)
     {
-        const float *src = (const float *)dynamic_cast<const CPUBuffer &>(pixels).data;
+        const void *src = dynamic_cast<const CPUBuffer &>(pixels).data;
+        const int n = f == RED ? 1 : f == RG ? 2 : f == RGB ? 3 : 4;
         for (int j = 0; j < h; ++j)
-            for (int i = 0; i < w; ++i) store[((size_t)(y + j) * view.w + x + i) * view.comps] = src[i + (size_t)j * w];
+            for (int i = 0; i < w; ++i)
+                for (int k = 0; k < n; ++k) {
+                    const size_t s = ((size_t)j * w + i) * n + k;
+                    store[((size_t)(y + j) * view.w + x + i) * view.comps + k] =
+                        t == FLOAT ? ((const float *)src)[s] : (float)((const unsigned char *)src)[s] / 255.0f;
+                }
     }
 };
 struct Texture2DArray : Texture {};
 
 // ---- programs and uniforms ---------------------------------------------------------------
-enum UniformKind { U_FLOAT, U_INT, U_VEC2, U_VEC3, U_VEC4, U_MAT3, U_MAT4, U_SAMPLER2D, U_SAMPLER2DARRAY };
+enum UniformKind { U_FLOAT, U_INT, U_VEC2, U_VEC3, U_VEC4, U_IVEC4, U_MAT3, U_MAT4, U_SAMPLER2D, U_SAMPLER2DARRAY };
 struct UniformEntry {
     const char *name;
     UniformKind kind;
@@ -225,6 +236,11 @@ struct Uniform {
         float *d = (float *)dst;
         d[0] = v.x; d[1] = v.y; d[2] = v.z; d[3] = v.w;
     }
+    void set(const vec4i &v)
+    {
+        int *d = (int *)dst;
+        d[0] = v.x; d[1] = v.y; d[2] = v.z; d[3] = v.w;
+    }
     void set(ptr<Texture> t)
     {
         if (kind == U_SAMPLER2D)
@@ -248,6 +264,7 @@ struct Uniform {
 typedef Uniform Uniform1f;
 typedef Uniform Uniform3f;
 typedef Uniform Uniform4f;
+typedef Uniform Uniform4i;
 typedef Uniform UniformMatrix3f;
 typedef Uniform UniformMatrix4f;
 typedef Uniform UniformSampler;
@@ -272,6 +289,7 @@ struct Program {
     ptr<Uniform1f> getUniform1f(const char *n) { return lookup(n, U_FLOAT, U_INT); }
     ptr<Uniform3f> getUniform3f(const char *n) { return lookup(n, U_VEC3, U_VEC3); }
     ptr<Uniform4f> getUniform4f(const char *n) { return lookup(n, U_VEC4, U_VEC4); }
+    ptr<Uniform4i> getUniform4i(const char *n) { return lookup(n, U_IVEC4, U_IVEC4); }
     ptr<UniformMatrix3f> getUniformMatrix3f(const char *n) { return lookup(n, U_MAT3, U_MAT3); }
     ptr<UniformMatrix4f> getUniformMatrix4f(const char *n) { return lookup(n, U_MAT4, U_MAT4); }
     ptr<UniformSampler> getUniformSampler(const char *n) { return lookup(n, U_SAMPLER2D, U_SAMPLER2DARRAY); }

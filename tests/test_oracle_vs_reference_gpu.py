@@ -1,6 +1,6 @@
 """The oracle's restatement of the shader path against the reference's own GPU path,
-compiled here by oracle/ref_build.py: ElevationProducer::doCreateTile and
-NormalProducer::doCreateTile as written (their uniform set-up, the noise-layer
+compiled here by oracle/ref_build.py: ElevationProducer::doCreateTile,
+NormalProducer::doCreateTile and OrthoProducer::doCreateTile as written (their uniform set-up, the noise-layer
 choice, the residual window, the FP64 sphere patch frames) drawing the reference's
 upsample and normal shaders, rewritten mechanically as C++ (oracle/ref_glsl.py)
 against the GLSL stand-in oracle/ref_stubs/glsl.h.
@@ -26,7 +26,9 @@ What is compared, and how tightly:
   bit;
 * the layers' fragment programs (road, water with river = 0, 1, 2, fill) bit for
   bit, and a producer with layers: the blend programs of graph1 and the demo
-  drawn by ElevationProducer::doCreateTile after given layer planes, bit for bit.
+  drawn by ElevationProducer::doCreateTile after given layer planes, bit for bit;
+* the ortho producer: createOrthoNoise byte for byte, and OrthoProducer::doCreateTile
+  with the terrain3 and demo ortho shaders byte for byte after the 8-bit store.
 
 Texture sampling is the oracle's documented choice (the nearest texel) on both
 sides.  Runs where the reference tree is present; skipped elsewhere."""
@@ -320,3 +322,57 @@ def test_layered_tiles_blend(ref, oracle_lib, noise_tables, variant, blend):
         assert np.array_equal(out[..., 0], wf) and np.array_equal(out[..., 1], wc), (variant, level)
         assert np.array_equal(out[..., 2], oracle_lib.layer_blend(W, wf, z, w, BLEND[blend])), (variant, blend, level)
         assert np.array_equal(out[..., 3], w)
+
+
+ORTHO = {"terrain3": 0, "demo": 1}
+
+
+@pytest.mark.parametrize("W", [20, 196, 260])
+def test_ortho_noise_table(ref, oracle_lib, product, W):
+    """createOrthoNoise (OrthoProducer.cpp:26-122), compiled as written: its RGBA8
+    table is the oracle's and the product's byte for byte."""
+    want = np.empty((6, W, W, 4), np.uint8)
+    ref.ref_ortho_noise(W, want.ctypes.data)
+    assert np.array_equal(oracle_lib.ortho_noise(W), want)
+    assert np.array_equal(np.asarray(product.ortho_noise(W)).reshape(want.shape), want)
+
+
+def _unorm8_even(data):
+    """The RGBA8 framebuffer's store of the shader's output, rounding ties to even
+    (the oracle's choice; GL leaves the rounding of ties to the implementation)."""
+    return np.rint(np.clip(data, 0.0, 1.0).astype(np.float32) * np.float32(255.0)).astype(np.uint8)
+
+
+@pytest.mark.parametrize("variant", sorted(ORTHO))
+@pytest.mark.parametrize("hsv", [False, True])
+def test_ortho_tiles(ref, oracle_lib, variant, hsv):
+    """OrthoProducer::doCreateTile (its uniforms: the parent window, the residual
+    scale, the noise layer and rotation, the noise colour in RGB or HSV form) drawing
+    the upsample ortho shader of terrain3 or the demo: after the framebuffer's 8-bit
+    store, every tile byte for byte the oracle's -- levels 0-9, faces 0-6, with and
+    without a residual tile, parents and residuals random bytes."""
+    import ctypes as C
+    W = 196
+    noise = np.empty((6, W, W, 4), np.uint8)
+    ref.ref_ortho_noise(W, noise.ctypes.data)
+    amps = np.float32([-1.0, 30.0, 20.0, 12.0, 8.0, 5.0, 3.0, 2.0, 1.0, 0.5])
+    rng = np.random.default_rng(17 + 2 * ORTHO[variant] + int(hsv))
+    for k, (level, tx, ty) in enumerate([(0, 0, 0), (1, 1, 0), (2, 3, 1), (4, 9, 14), (7, 100, 33), (9, 511, 2)]):
+        for has_res in (True, False):
+            face = k % 7
+            parent = rng.integers(0, 256, (W, W, 4)).astype(np.uint8) if level > 0 else None
+            res = rng.integers(0, 256, (W, W, 4)).astype(np.uint8) if has_res else None
+            root_color = rng.uniform(0, 1, 4).astype(np.float32)
+            noise_color = rng.uniform(0.2, 1.5, 4).astype(np.float32)
+            scale = float(rng.choice([1.0, 2.0, 3.5]))
+            out = np.empty((W, W, 4), np.float32)
+            rc = ref.ref_gl_ortho_tile(ORTHO[variant], W, level, tx, ty, face,
+                                       None if parent is None else parent.ctypes.data,
+                                       None if res is None else res.ctypes.data, noise.ctypes.data, _p(amps),
+                                       len(amps), _p(root_color), _p(noise_color), int(hsv), C.c_float(scale), _p(out))
+            assert rc == 0
+            rot, layer = oracle_lib.noise_select(face, level, tx, ty)
+            amp = float(amps[level]) if level < len(amps) else 0.0
+            want = oracle_lib.ortho_tile(W, level, tx, ty, parent, res, noise[layer], rot, amp, root_color=root_color,
+                                         noise_color=noise_color, scale=scale, hsv=hsv)
+            assert np.array_equal(_unorm8_even(out), want), (variant, hsv, level, tx, ty, face, has_res)
