@@ -37,6 +37,10 @@ The GPU path, in a second unit (``ref_gpu.cpp``):
   matrix arithmetic);
 * ``OrthoProducer::doCreateTile`` (``ortho/OrthoProducer.cpp:273-385``) the same way,
   and ``createOrthoNoise`` (``:26-122``) in the first unit;
+* ``ElevationGraphLayer::drawCurveAltitude`` and ``GraphLayer::drawCurve`` of a part, and
+  the lines of ``RoadElevationLayer::doCreateTile`` that place one road (its scale, tile
+  offset, ``BASEWIDTH`` / ``TOTALWIDTH`` and the drawCurveAltitude call), on stand-in
+  curves whose meshes the framebuffer stand-in records;
 * the shaders those functions draw -- the upsample shaders of terrain1, terrain2,
   terrain4 (flipped diagonals) and the demo (modulated noise, with and without
   ``NO_CLAMP``), the normal shaders of terrain1, terrain2 (sphere) and the demo
@@ -76,6 +80,9 @@ ELEV_CPP = "src/terrain/sources/proland/dem/ElevationProducer.cpp"
 CPU_ELEV_CPP = "src/terrain/sources/proland/dem/CPUElevationProducer.cpp"
 MIPMAP_CPP = "src/terrain/sources/proland/preprocess/terrain/HeightMipmap.cpp"
 ORTHO_CPP = "src/terrain/sources/proland/ortho/OrthoProducer.cpp"
+GRAPH_LAYER_CPP = "src/graph/sources/proland/dem/ElevationGraphLayer.cpp"
+ROAD_LAYER_CPP = "src/graph/sources/proland/dem/RoadElevationLayer.cpp"
+GRAPH_PRODUCER_CPP = "src/graph/sources/proland/graph/producer/GraphLayer.cpp"
 
 
 def _read(root, rel):
@@ -358,6 +365,60 @@ _GPU_PRELUDE = r"""
 namespace refgl {
 Logger *Logger::DEBUG_LOGGER = nullptr;
 using proland::cnoise;
+using std::abs;
+using std::atan2;
+using std::floor;
+using std::max;
+
+// The graph types drawCurveAltitude reads (graph/Curve.h, dem/ElevationCurveData.h):
+// a polyline with its curvilinear coordinates and width; the altitude profile is
+// the identity, getAltitude(s) = s, so that a vertex's altitude shows where on the
+// curve it was sampled.
+struct Node {};
+typedef ptr<Node> NodePtr;
+struct Curve {
+    vector<vec2d> points;
+    vector<float> s;
+    float width = 0.0f;
+    Node start, end;
+    int getSize() const { return (int)points.size(); }
+    vec2d getXY(int i) const { return points[i]; }
+    float getS(int i) const { return s[i]; }
+    float getWidth() const { return width; }
+    ptr<Curve> getAncestor() const { return ptr<Curve>(const_cast<Curve *>(this)); }
+    NodePtr getStart() const { return NodePtr(const_cast<Node *>(&start)); }
+    NodePtr getEnd() const { return NodePtr(const_cast<Node *>(&end)); }
+};
+typedef ptr<Curve> CurvePtr;
+struct ElevationCurveData {
+    float getAltitude(float s) { return s; }
+};
+
+// GraphLayer's members the drawing functions call: isDeformed, and extremity, here
+// whether the caller asks for a cap at that end; and GraphLayer::drawCurve of a part.
+struct GraphLayer {
+    bool deformed = false, cap_start = false, cap_end = false;
+    bool isDeformed() const { return deformed; }
+    bool extremity(CurvePtr c, NodePtr p) { return p.p == &c->start ? cap_start : cap_end; }
+    void drawCurve(const vec3d &tileCoords, CurvePtr p, const vec4f &part, ptr<FrameBuffer> fb, ptr<Program> prog,
+                   Mesh<vec4f, unsigned int> &mesh, vec2d *nx, vec2d *ny, vec2d *lx, vec2d *ly);
+};
+
+struct ElevationGraphLayer : GraphLayer {
+    void drawCurveAltitude(const vec3d &tileCoords, CurvePtr p, ElevationCurveData *data, float width, float nwidth,
+                           float stepLength, bool caps, ptr<FrameBuffer> fb, ptr<Program> prog,
+                           Mesh<vec4f, unsigned int> &mesh, vec2d *nx, vec2d *ny, vec2d *lx, vec2d *ly);
+};
+
+// The lines of RoadElevationLayer::doCreateTile that place one road on a tile.
+struct RoadElevationLayer : ElevationGraphLayer {
+    int tileSize = 101, tileBorder = 2;
+    ptr<Program> layerProgram;
+    Mesh<vec4f, unsigned int> *meshuv = nullptr;
+    int getTileSize() { return tileSize; }
+    int getTileBorder() { return tileBorder; }
+    void draw_road(const vec3d &q, CurvePtr c, ElevationCurveData *cData, ptr<FrameBuffer> fb, float *scale_out);
+};
 
 // The members ElevationProducer::doCreateTile and its init's uniform look-ups use
 // (ElevationProducer.h), on the stand-in producer.
@@ -463,7 +524,7 @@ struct LayerPlanes {
 void draw_layer_planes(void *arg)
 {
     const LayerPlanes &L = *(const LayerPlanes *)arg;
-    std::vector<float> &c = L.fb->color[L.fb->draw];
+    std::vector<float> &c = L.fb->color[L.fb->draw_buffer];
     for (int p = 0; p < L.fb->w * L.fb->h; ++p) {
         c[(size_t)p * 4 + 2] = L.z[p];
         c[(size_t)p * 4 + 3] = L.w[p];
@@ -661,6 +722,105 @@ extern "C" int ref_gl_ortho_tile(int variant, int W, int level, int tx, int ty, 
     return 0;
 }
 
+namespace {
+std::vector<refgl::FrameBuffer::Drawn> g_drawn;
+
+// a curve of n points (xy: 2n doubles), their curvilinear coordinates (or 0) and width
+refgl::Curve make_curve(const double *xy, const float *s, int n, float width)
+{
+    refgl::Curve c;
+    for (int k = 0; k < n; ++k) {
+        c.points.push_back(refgl::vec2d(xy[2 * k], xy[2 * k + 1]));
+        c.s.push_back(s ? s[k] : 0.0f);
+    }
+    c.width = width;
+    return c;
+}
+}  // namespace
+
+// One road through the lines of RoadElevationLayer::doCreateTile that place it on tile
+// q = (x, y, size) of a tileSize-wide storage with the given border (scale, tile
+// offset, BASEWIDTH / TOTALWIDTH, the drawCurveAltitude call) and
+// ElevationGraphLayer::drawCurveAltitude: the road's n points (xy, 2n doubles), their
+// curvilinear coordinates s (the altitude profile is s itself), its width, caps at the
+// start / end.  Returns the number of meshes drawn (ref_drawn_mesh reads them), or -1;
+// scale_out: the layer's scale.
+extern "C" int ref_road_meshes(double qx, double qy, double qz, int tile_size, int border, const double *xy,
+                               const float *s, int n, float width, int cap_start, int cap_end, float *scale_out)
+{
+    using namespace refgl;
+    if (n < 2) return -1;
+    Curve c = make_curve(xy, s, n, width);
+    ElevationCurveData data;
+    FrameBuffer fb;
+    Program prog;
+    Mesh<vec4f, unsigned int> mesh;
+    RoadElevationLayer layer;
+    layer.tileSize = tile_size;
+    layer.tileBorder = border;
+    layer.layerProgram = &prog;
+    layer.meshuv = &mesh;
+    layer.cap_start = cap_start != 0;
+    layer.cap_end = cap_end != 0;
+    layer.draw_road(vec3d(qx, qy, qz), &c, &data, &fb, scale_out);
+    g_drawn = fb.drawn;
+    return (int)g_drawn.size();
+}
+
+// ElevationGraphLayer::drawCurveAltitude called directly (flat tile): tile coordinates
+// (centre x, centre y, factor), the curve, and the function's width, nwidth,
+// stepLength and caps arguments.  Returns the number of meshes drawn, or -1.
+extern "C" int ref_curve_altitude(double cx, double cy, double factor, const double *xy, const float *s, int n,
+                                  float width, float nwidth, float step, int cap_start, int cap_end)
+{
+    using namespace refgl;
+    if (n < 2) return -1;
+    Curve c = make_curve(xy, s, n, width);
+    ElevationCurveData data;
+    FrameBuffer fb;
+    Program prog;
+    Mesh<vec4f, unsigned int> mesh;
+    ElevationGraphLayer layer;
+    layer.cap_start = cap_start != 0;
+    layer.cap_end = cap_end != 0;
+    layer.drawCurveAltitude(vec3d(cx, cy, factor), &c, &data, width, nwidth, step, true, &fb, &prog, mesh, nullptr,
+                            nullptr, nullptr, nullptr);
+    g_drawn = fb.drawn;
+    return (int)g_drawn.size();
+}
+
+// GraphLayer::drawCurve(tileCoords, p, part, ...) on a flat tile: the curve's points and
+// width, part = (offset a, offset b, w at a, w at b).  Returns the number of meshes drawn.
+extern "C" int ref_curve_part(double cx, double cy, double factor, const double *xy, int n, float width,
+                              const float *part)
+{
+    using namespace refgl;
+    if (n < 2) return -1;
+    Curve c = make_curve(xy, nullptr, n, width);
+    FrameBuffer fb;
+    Program prog;
+    Mesh<vec4f, unsigned int> mesh;
+    GraphLayer layer;
+    layer.drawCurve(vec3d(cx, cy, factor), &c, vec4f(part[0], part[1], part[2], part[3]), &fb, &prog, mesh, nullptr,
+                    nullptr, nullptr, nullptr);
+    g_drawn = fb.drawn;
+    return (int)g_drawn.size();
+}
+
+// Mesh k of the last ref_road_meshes / ref_curve_altitude / ref_curve_part: its mode (0 triangles, 1 strip), vertex and index
+// counts, and (when the buffers are given) its (x, y, z, w) vertices and indices.
+extern "C" int ref_drawn_mesh(int k, int *mode, int *n_vertices, int *n_indices, float *vertices, unsigned *indices)
+{
+    if (k < 0 || k >= (int)g_drawn.size()) return 1;
+    const refgl::FrameBuffer::Drawn &d = g_drawn[k];
+    *mode = d.mode;
+    *n_vertices = (int)d.vertices.size() / 4;
+    *n_indices = (int)d.indices.size();
+    if (vertices) std::memcpy(vertices, d.vertices.data(), d.vertices.size() * sizeof(float));
+    if (indices) std::memcpy(indices, d.indices.data(), d.indices.size() * sizeof(unsigned));
+    return 0;
+}
+
 // One fragment of the layer program `shader` (LAYER_SHADERS order) at the interpolated
 // varying st: uniforms river (water programs), depth and color (fill program); data
 // (4 floats) and the fragment depth it writes.  Returns 0.
@@ -811,6 +971,29 @@ def generate_gpu(root):
     src.append("// %s:%d\n%s" % (ELEV_CPP, dct_line, dct))
     src.append("// %s:%d\nvoid NormalProducer::bind_uniforms()\n{\n%s}\n" % (NORMAL_CPP, nups_line, nups))
     src.append("// %s:%d\n%s" % (NORMAL_CPP, ndct_line, ndct))
+    graph = _read(root, GRAPH_LAYER_CPP)
+    road = _read(root, ROAD_LAYER_CPP)
+    dca, dca_line = extract_function(graph, r"void\s+ElevationGraphLayer::drawCurveAltitude\s*\(")
+    dcp, dcp_line = extract_function(_read(root, GRAPH_PRODUCER_CPP),
+                                     r"void\s+GraphLayer::drawCurve\s*\(\s*const vec3d &tileCoords,\s*CurvePtr p,"
+                                     r"\s*const vec4f &part")
+    macros, macros_line = extract_block(road, "#define BASEWIDTH(", "#define TOTALWIDTH(")
+    placing, placing_line = extract_block(road, "float scale = 2.0f * (getTileSize()", "vec3d tileOffset = vec3d(",
+                                          after="bool RoadElevationLayer::doCreateTile(")
+    cw, cw_line = extract_block(road, "float cwidth = c->getWidth();", "float cwidth = c->getWidth();",
+                                after="bool RoadElevationLayer::doCreateTile(")
+    widths, widths_line = extract_block(road, "float w = BASEWIDTH(cwidth, scale);", "float tw = TOTALWIDTH(w);",
+                                        after="bool RoadElevationLayer::doCreateTile(")
+    call, call_line = extract_block(road, "ElevationGraphLayer::drawCurveAltitude(tileOffset, c, cData,",
+                                    "ElevationGraphLayer::drawCurveAltitude(tileOffset, c, cData,",
+                                    after="bool RoadElevationLayer::doCreateTile(")
+    src.append("// %s:%d\n%s" % (GRAPH_LAYER_CPP, dca_line, dca))
+    src.append("// %s:%d\n%s" % (GRAPH_PRODUCER_CPP, dcp_line, dcp))
+    src.append("}  // namespace refgl\n// %s:%d\n%snamespace refgl {\n" % (ROAD_LAYER_CPP, macros_line, macros))
+    src.append("void RoadElevationLayer::draw_road(const vec3d &q, CurvePtr c, ElevationCurveData *cData, "
+               "ptr<FrameBuffer> fb, float *scale_out)\n{\n    vec2d nx, ny, lx, ly;\n"
+               "    // %s:%d\n%s    // :%d\n%s    // :%d\n%s    // :%d\n%s    *scale_out = scale;\n}\n"
+               % (ROAD_LAYER_CPP, placing_line, placing, cw_line, cw, widths_line, widths, call_line, call))
     src.append("// %s:%d\nvoid OrthoProducer::bind_uniforms()\n{\n%s}\n" % (ORTHO_CPP, oups_line, oups))
     src.append("// %s:%d\n%s" % (ORTHO_CPP, odct_line, odct))
     src.append("}  // namespace refgl\n")
@@ -827,7 +1010,8 @@ def build(root=DEFAULT_ROOT, force=False):
     None without the reference (the GPU machine has none; the pin runs where it is)."""
     if not os.path.isdir(os.path.join(root, "src")):
         return LIB if os.path.exists(LIB) else None
-    srcs = [os.path.join(root, p) for p in (NOISE_CPP, ELEV_CPP, CPU_ELEV_CPP, MIPMAP_CPP, NORMAL_CPP, ORTHO_CPP)]
+    srcs = [os.path.join(root, p) for p in (NOISE_CPP, ELEV_CPP, CPU_ELEV_CPP, MIPMAP_CPP, NORMAL_CPP, ORTHO_CPP,
+                                            GRAPH_LAYER_CPP, ROAD_LAYER_CPP, GRAPH_PRODUCER_CPP)]
     srcs += [os.path.join(root, rel) for _, rel, _ in UPSAMPLE_SHADERS + NORMAL_SHADERS + BLEND_SHADERS +
              LAYER_SHADERS + ORTHO_SHADERS]
     srcs += [os.path.abspath(__file__), os.path.join(HERE, "ref_glsl.py")]

@@ -16,6 +16,7 @@
 //   attachment; clear() fills it with the clear colour.
 // * GPUSlot::copyPixels copies the read colour attachment into the slot's layer.
 // * TileProducer::doCreateTile (drawing the layers) runs a hook the harness gives.
+// * FrameBuffer::draw(program, mesh) records the mesh (mode, vertices, indices).
 // * Texture2D::setSubImage copies float or byte pixels in.
 // * vec3<T>, vec4<T>, mat3<T>, mat4<T>: component-wise arithmetic in T;
 //   length = sqrt(x*x + y*y + z*z), normalize divides each component by it
@@ -26,6 +27,11 @@
 #include <cassert>
 #include <cmath>
 #include <cstring>
+// The C++ <math.h> declares the float overloads of the math functions in the global
+// namespace (sqrt(2.0f) is a float square root), as the reference's translation units
+// see them through the engine headers: RoadElevationLayer.cpp's BASEWIDTH calls
+// sqrt(2.0f) with no `using namespace std`.
+#include <math.h>
 #include <map>
 #include <sstream>
 #include <string>
@@ -58,6 +64,16 @@ template <class T> struct ptr {  // non-owning: the harness owns every object
 inline bool isFinite(float x) { return std::isfinite(x); }
 
 // ---- Ork math ----------------------------------------------------------------------
+template <class T> struct vec2 {
+    T x, y;
+    vec2() : x(0), y(0) {}
+    vec2(T a, T b) : x(a), y(b) {}
+    vec2 operator+(const vec2 &o) const { return vec2(x + o.x, y + o.y); }
+    vec2 operator-(const vec2 &o) const { return vec2(x - o.x, y - o.y); }
+    vec2 operator*(T s) const { return vec2(x * s, y * s); }
+    T length() const { return std::sqrt(x * x + y * y); }
+};
+
 template <class T> struct vec3 {
     T x, y, z;
     vec3() : x(0), y(0), z(0) {}
@@ -77,6 +93,7 @@ template <class T> struct vec3 {
         return vec3(x / *previousLength, y / *previousLength, z / *previousLength);
     }
     vec3 crossProduct(const vec3 &v) const { return vec3(y * v.z - z * v.y, z * v.x - x * v.z, x * v.y - y * v.x); }
+    vec2<T> xy() const { return vec2<T>(x, y); }
     template <class U> vec3<U> cast() const { return vec3<U>((U)x, (U)y, (U)z); }
     static const vec3 UNIT_Y;
 };
@@ -137,6 +154,7 @@ template <class T> struct mat4 {
     }
 };
 
+typedef vec2<double> vec2d;
 typedef vec3<float> vec3f;
 typedef vec3<double> vec3d;
 typedef vec4<float> vec4f;
@@ -298,7 +316,7 @@ struct Program {
 struct FrameBuffer {
     int w = 0, h = 0;
     vector<float> color[2];  // RGBA float attachments COLOR0, COLOR1
-    int draw = 0, read = 0;
+    int draw_buffer = 0, read_buffer = 0;
     float clear_color[4] = {0, 0, 0, 0};
     void init(int W)
     {
@@ -313,16 +331,52 @@ struct FrameBuffer {
     void clear(bool color_, bool, bool)
     {
         if (!color_) return;
-        for (size_t k = 0; k < color[draw].size(); ++k) color[draw][k] = clear_color[k % 4];
+        for (size_t k = 0; k < color[draw_buffer].size(); ++k) color[draw_buffer][k] = clear_color[k % 4];
     }
     void drawQuad(ptr<Program> p) { p->run(*this); }
     void write(int i, int j, const float *rgba)
     {
-        std::memcpy(&color[draw][((size_t)j * w + i) * 4], rgba, 4 * sizeof(float));
+        std::memcpy(&color[draw_buffer][((size_t)j * w + i) * 4], rgba, 4 * sizeof(float));
     }
     void setDepthTest(bool, Function = LESS) {}
-    void setDrawBuffer(BufferId b) { draw = b == COLOR1 ? 1 : 0; }
-    void setReadBuffer(BufferId b) { read = b == COLOR1 ? 1 : 0; }
+    // meshes drawn by draw(program, mesh): mode, (x, y, z, w) vertices and indices
+    struct Drawn {
+        int mode;
+        vector<float> vertices;
+        vector<unsigned int> indices;
+    };
+    vector<Drawn> drawn;
+    template <class M> void draw(ptr<Program>, const M &mesh)
+    {
+        Drawn d;
+        d.mode = mesh.mode;
+        for (const auto &v : mesh.vertices) {
+            d.vertices.push_back(v.x);
+            d.vertices.push_back(v.y);
+            d.vertices.push_back(v.z);
+            d.vertices.push_back(v.w);
+        }
+        d.indices = mesh.indices;
+        drawn.push_back(d);
+    }
+    void setDrawBuffer(BufferId b) { draw_buffer = b == COLOR1 ? 1 : 0; }
+    void setReadBuffer(BufferId b) { read_buffer = b == COLOR1 ? 1 : 0; }
+};
+
+// ---- meshes ---------------------------------------------------------------------------------
+enum MeshMode { TRIANGLES, TRIANGLE_STRIP };
+template <class V, class I> struct Mesh {
+    int mode = TRIANGLES;
+    vector<V> vertices;
+    vector<I> indices;
+    void setMode(MeshMode m) { mode = m; }
+    void clear()
+    {
+        vertices.clear();
+        indices.clear();
+    }
+    void addVertex(const V &v) { vertices.push_back(v); }
+    void addIndice(I i) { indices.push_back(i); }
 };
 
 // ---- tile storage, cache and producers ------------------------------------------------------
@@ -356,7 +410,7 @@ struct GPUTileStorage : TileStorage {
             for (int j = 0; j < h; ++j)
                 for (int i = 0; i < w; ++i)
                     for (int k = 0; k < comps; ++k) {
-                        float v = fb->color[fb->read][((size_t)(y + j) * fb->w + x + i) * 4 + k];
+                        float v = fb->color[fb->read_buffer][((size_t)(y + j) * fb->w + x + i) * 4 + k];
                         if (unorm8) v = std::floor((v < 0.0f ? 0.0f : (v > 1.0f ? 1.0f : v)) * 255.0f + 0.5f) / 255.0f;
                         tx.store[(((size_t)l * tx.view.h + y + j) * tx.view.w + x + i) * comps + k] = v;
                     }

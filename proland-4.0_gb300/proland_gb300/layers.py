@@ -47,6 +47,12 @@ def base_width(width, scale):
     return f32(f32(width) + f32(f32(2.0) * f32(math.sqrt(2.0))) / f32(scale))
 
 
+def _length(v):
+    """Length of a 2D vector as the reference's vec2d::length forms it: sqrt(x*x + y*y)
+    in double (hypot can differ in the last bit)."""
+    return math.sqrt(v[0] * v[0] + v[1] * v[1])
+
+
 def _clip(transform, x, y):
     cx, cy, factor = transform[:3]
     return (x - cx) * factor, (y - cy) * factor
@@ -87,11 +93,11 @@ def curve_altitude_meshes(points, altitudes, width, nwidth, step, transform, sta
     for i in range(n):
         cur = pts[i]
         if i == 0:
-            d = (pts[1] - cur) / np.hypot(*(pts[1] - cur))
+            d = (pts[1] - cur) / _length(pts[1] - cur)
         elif i == n - 1:
-            d = (cur - pts[i - 1]) / np.hypot(*(cur - pts[i - 1]))
+            d = (cur - pts[i - 1]) / _length(cur - pts[i - 1])
         else:
-            d = (cur - pts[i - 1]) / np.hypot(*(cur - pts[i - 1])) + (pts[i + 1] - cur) / np.hypot(*(pts[i + 1] - cur))
+            d = (cur - pts[i - 1]) / _length(cur - pts[i - 1]) + (pts[i + 1] - cur) / _length(pts[i + 1] - cur)
             l = (d[0] * d[0] + d[1] * d[1]) * 0.5
             d = d / l
         dx, dy = d[0] * w, d[1] * w
@@ -101,10 +107,10 @@ def curve_altitude_meshes(points, altitudes, width, nwidth, step, transform, sta
         vert(strip, cur[0] + dy, cur[1] - dx, alt[i], nwidth)
         if i < n - 1:
             nxt = pts[i + 1]
-            seg = np.hypot(*(nxt - cur))
+            seg = _length(nxt - cur)
             nx, ny = w * (nxt[0] - cur[0]) / seg, w * (nxt[1] - cur[1]) / seg
             for j in range(1, int(math.floor(seg / step))):
-                c = j * step / seg
+                c = float(f32(f32(j) * f32(step))) / seg     # int * float is a float product
                 x, y = cur[0] + c * (nxt[0] - cur[0]), cur[1] + c * (nxt[1] - cur[1])
                 z = alt[i] + c * (alt[i + 1] - alt[i])
                 vert(strip, x - ny, y + nx, z, -nwidth)
@@ -132,12 +138,14 @@ def road_strip(points, altitudes, width, tile_origin, tile_size, W, border=2):
 def curve_part_strip(points, part, transform):
     """GraphLayer::drawCurve(tileCoords, p, part, ...)'s strip: vertices (x, y, 0, part.z)
     at the curve points offset by part.x along the float direction (dy, dx), and (x, y,
-    0, part.w) offset by part.y along (dy, -dx)."""
+    0, part.w) offset by part.y along (dy, -dx); part is a vec4f, so the offsets
+    dy * part.x ... are float products."""
     pts = np.asarray(points, np.float64)
+    part = np.asarray(part, np.float32)
     n = len(pts)
     out = []
     prevl = f32(0.0)
-    nextl = f32(np.hypot(*(pts[1] - pts[0])))
+    nextl = f32(_length(pts[1] - pts[0]))
     for i in range(n):
         cur = pts[i]
         if i == 0:
@@ -149,17 +157,18 @@ def curve_part_strip(points, part, transform):
         else:
             dx = f32((cur[0] - pts[i - 1][0]) / prevl)
             dy = f32((cur[1] - pts[i - 1][1]) / prevl)
-            dx = f32(dx + f32((pts[i + 1][0] - cur[0]) / nextl))
-            dy = f32(dy + f32((pts[i + 1][1] - cur[1]) / nextl))
+            # float += double: the sum is formed in double and rounded once
+            dx = f32(float(dx) + (pts[i + 1][0] - cur[0]) / float(nextl))
+            dy = f32(float(dy) + (pts[i + 1][1] - cur[1]) / float(nextl))
             l = f32(f32(f32(dx * dx) + f32(dy * dy)) * f32(0.5))
             dx, dy = f32(dx / l), f32(dy / l)
-        a = _clip(transform, cur[0] + float(dy) * part[0], cur[1] + float(dx) * part[0])
-        b = _clip(transform, cur[0] + float(dy) * part[1], cur[1] - float(dx) * part[1])
-        out.append((a[0], a[1], 0.0, part[2]))
-        out.append((b[0], b[1], 0.0, part[3]))
+        a = _clip(transform, cur[0] + float(f32(dy * part[0])), cur[1] + float(f32(dx * part[0])))
+        b = _clip(transform, cur[0] + float(f32(dy * part[1])), cur[1] - float(f32(dx * part[1])))
+        out.append((a[0], a[1], 0.0, float(part[2])))
+        out.append((b[0], b[1], 0.0, float(part[3])))
         prevl = nextl
         if i < n - 2:
-            nextl = f32(np.hypot(*(pts[i + 2] - pts[i + 1])))
+            nextl = f32(_length(pts[i + 2] - pts[i + 1]))
     return np.asarray(out, np.float32)
 
 

@@ -28,7 +28,10 @@ What is compared, and how tightly:
   bit, and a producer with layers: the blend programs of graph1 and the demo
   drawn by ElevationProducer::doCreateTile after given layer planes, bit for bit;
 * the ortho producer: createOrthoNoise byte for byte, and OrthoProducer::doCreateTile
-  with the terrain3 and demo ortho shaders byte for byte after the 8-bit store.
+  with the terrain3 and demo ortho shaders byte for byte after the 8-bit store;
+* the layers' meshes: ElevationGraphLayer::drawCurveAltitude, GraphLayer::drawCurve
+  of a part and RoadElevationLayer's placement of a road, against the product's mesh
+  builder (proland_gb300.layers), vertex and index for index.
 
 Texture sampling is the oracle's documented choice (the nearest texel) on both
 sides.  Runs where the reference tree is present; skipped elsewhere."""
@@ -376,3 +379,106 @@ def test_ortho_tiles(ref, oracle_lib, variant, hsv):
             want = oracle_lib.ortho_tile(W, level, tx, ty, parent, res, noise[layer], rot, amp, root_color=root_color,
                                          noise_color=noise_color, scale=scale, hsv=hsv)
             assert np.array_equal(_unorm8_even(out), want), (variant, hsv, level, tx, ty, face, has_res)
+
+
+def _drawn(ref, n):
+    import ctypes as C
+    out = []
+    for k in range(n):
+        m, nv, ni = C.c_int(), C.c_int(), C.c_int()
+        assert ref.ref_drawn_mesh(k, C.byref(m), C.byref(nv), C.byref(ni), None, None) == 0
+        v = np.empty((nv.value, 4), np.float32)
+        ix = np.empty(ni.value, np.uint32)
+        ref.ref_drawn_mesh(k, C.byref(m), C.byref(nv), C.byref(ni), v.ctypes.data, ix.ctypes.data)
+        out.append((v, ix if ni.value else None, m.value))
+    return out
+
+
+def _same_meshes(got, want):
+    assert len(got) == len(want)
+    for (gv, gi, gm), (wv, wi, wm) in zip(got, want):
+        assert gm == wm
+        assert np.array_equal(gv, np.asarray(wv, np.float32)), np.abs(gv - wv).max()
+        assert (gi is None and wi is None) or np.array_equal(gi, wi)
+
+
+def _polyline(rng, origin, size, n):
+    pts = np.column_stack([origin[0] + rng.uniform(-100, size + 100, n), origin[1] + rng.uniform(-100, size + 100, n)])
+    s = np.float32(np.concatenate([[0.0], np.cumsum(np.sqrt((np.diff(pts, axis=0) ** 2).sum(1)))]))
+    return pts, s
+
+
+def test_road_layer_meshes(ref, product):
+    """RoadElevationLayer::doCreateTile's placement of a road (scale, tile offset,
+    BASEWIDTH / TOTALWIDTH, the drawCurveAltitude call) and
+    ElevationGraphLayer::drawCurveAltitude itself, against the product's mesh builder
+    (proland_gb300.layers: tile_transform, base_width, curve_altitude_meshes,
+    road_strip): every mesh -- start cap, strip, end cap -- vertex and index for index.
+    The altitude profile is the identity (getAltitude(s) = s) and the builder gets the
+    points' s as their altitudes, so that z shows where each vertex sampled the curve."""
+    import ctypes as C
+    from proland_gb300 import layers
+    rng = np.random.default_rng(8)
+    for trial in range(24):
+        W = (101, 197)[trial % 2]
+        size = 4000.0 / (1 << (trial % 5))
+        origin = (float(rng.uniform(-8000, 8000)), float(rng.uniform(-8000, 8000)))
+        pts, s = _polyline(rng, origin, size, 2 + trial % 5)
+        width = float(rng.uniform(3.0, 40.0))
+        cs, ce = trial % 2, (trial // 2) % 2
+        sc = C.c_float()
+        n = ref.ref_road_meshes(origin[0], origin[1], size, W, 2, np.ascontiguousarray(pts).ctypes.data,
+                                s.ctypes.data, len(pts), width, cs, ce, C.byref(sc))
+        tr = layers.tile_transform(origin, size, W)
+        assert np.float32(sc.value) == np.float32(tr[3])
+        base = layers.base_width(width, tr[3])
+        total = np.float32(base * np.float32(3.0))
+        step = max(np.float32(1.0), np.float32(np.float32(1.0) / tr[3]))
+        want = layers.curve_altitude_meshes(pts, s, total, np.float32(total / base), step, tr, start_cap=bool(cs),
+                                            end_cap=bool(ce))
+        _same_meshes(_drawn(ref, n), want)
+        if not cs:
+            assert np.array_equal(_drawn(ref, n)[0][0], layers.road_strip(pts, s, width, origin, size, W))
+
+
+def test_water_curve_meshes(ref, product):
+    """drawCurveAltitude with the water layer's arguments (WaterElevationLayer.cpp:
+    the other curves at width w, nwidth 1, no caps; rivers at TOTALWIDTH with caps)."""
+    from proland_gb300 import layers
+    rng = np.random.default_rng(9)
+    for trial in range(16):
+        W, size = 101, 2000.0 / (1 << (trial % 4))
+        origin = (float(rng.uniform(-5000, 5000)), float(rng.uniform(-5000, 5000)))
+        tr = layers.tile_transform(origin, size, W)
+        pts, s = _polyline(rng, origin, size, 2 + trial % 4)
+        w = np.float32(rng.uniform(2.0, 60.0))
+        step = max(np.float32(1.0), np.float32(np.float32(1.0) / tr[3]))
+        if trial % 2:
+            base = layers.base_width(w, tr[3])
+            width, nwidth, cs, ce = np.float32(base * np.float32(3.0)), None, trial % 3 == 0, trial % 4 == 1
+            nwidth = np.float32(width / base)
+        else:
+            width, nwidth, cs, ce = w, np.float32(w / w), False, False
+        n = ref.ref_curve_altitude(tr[0], tr[1], tr[2], np.ascontiguousarray(pts).ctypes.data, s.ctypes.data,
+                                   len(pts), float(width), float(nwidth), float(step), int(cs), int(ce))
+        want = layers.curve_altitude_meshes(pts, s, width, nwidth, step, tr, start_cap=cs, end_cap=ce)
+        _same_meshes(_drawn(ref, n), want)
+
+
+def test_curve_part_strips(ref, product):
+    """GraphLayer::drawCurve(tileCoords, p, part, ...) against layers.curve_part_strip:
+    the water layer's boundary parts (0, +-12, 1, 2) and random ones."""
+    from proland_gb300 import layers
+    rng = np.random.default_rng(10)
+    for trial in range(16):
+        W, size = 101, 3000.0 / (1 << (trial % 4))
+        origin = (float(rng.uniform(-5000, 5000)), float(rng.uniform(-5000, 5000)))
+        tr = layers.tile_transform(origin, size, W)
+        pts, _ = _polyline(rng, origin, size, 2 + trial % 6)
+        part = [(0.0, 12.0, 1.0, 2.0), (0.0, -12.0, 1.0, 2.0)][trial % 2] if trial < 8 else \
+            tuple(float(v) for v in rng.uniform(-20, 20, 4))
+        n = ref.ref_curve_part(tr[0], tr[1], tr[2], np.ascontiguousarray(pts).ctypes.data, len(pts), 10.0,
+                               _p(np.float32(part)))
+        got = _drawn(ref, n)
+        assert len(got) == 1 and got[0][2] == 1 and got[0][1] is None
+        assert np.array_equal(got[0][0], layers.curve_part_strip(pts, part, tr)), trial   # part as plain floats
