@@ -647,6 +647,7 @@ def ref_lib():
         L.ref_gl_layer_fragment.argtypes = [C.c_int, C.c_int, C.c_float, _f32p, C.c_float, C.c_float, _f32p,
                                             C.POINTER(C.c_float)]
         L.ref_ortho_noise.argtypes = [C.c_int, C.c_void_p]
+        L.ref_sphere_uniforms.argtypes = [C.c_int] * 4 + [C.c_float, _f32p]
         L.ref_road_meshes.argtypes = [C.c_double] * 3 + [C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_int,
                                                          C.c_float, C.c_int, C.c_int, C.POINTER(C.c_float)]
         L.ref_curve_altitude.argtypes = [C.c_double] * 3 + [C.c_void_p, C.c_void_p, C.c_int, C.c_float, C.c_float,

@@ -722,6 +722,38 @@ extern "C" int ref_gl_ortho_tile(int variant, int W, int level, int tx, int ty, 
     return 0;
 }
 
+// The uniforms NormalProducer::doCreateTile sets for a spherical tile (demo normal
+// shader, RGBA32F storage), as the producer builds them (row-major): patchCorners[16],
+// patchVerticals[16], patchCornerNorms[4], worldToTangentFrame[9],
+// parentToTangentFrame[9] (level > 0), deform[4].  Returns 0.
+extern "C" int ref_gl_normal_tile(int variant, int W, int level, int tx, int ty, const float *elev_rgba, int format,
+                                  const float *parent, float root_quad_size, int grid_mesh_size, int deform,
+                                  float *out);
+extern "C" int ref_sphere_uniforms(int W, int level, int tx, int ty, float root_quad_size, float *out58)
+{
+    std::vector<float> elev((size_t)W * W * 4, 0.0f), parent((size_t)(W - 4) * (W - 4) * 4, 0.0f),
+        out((size_t)(W - 4) * (W - 4) * 4);
+    const int rc = ref_gl_normal_tile(2, W, level, tx, ty, elev.data(), 0, parent.data(), root_quad_size, 24, 1,
+                                      out.data());
+    if (rc) return rc;
+    struct Want {
+        const char *name;
+        int rows, cols;
+    };
+    static const Want want[] = {{"patchCorners", 4, 4}, {"patchVerticals", 4, 4}, {"patchCornerNorms", 1, 4},
+                                {"worldToTangentFrame", 3, 3}, {"parentToTangentFrame", 3, 3}, {"deform", 1, 4}};
+    float *o = out58;
+    for (const Want &w : want) {
+        const refgl::UniformEntry *e = g_normal[2].table;
+        while (e->name && std::string(e->name) != w.name) ++e;
+        if (!e->name) return 3;
+        const float *d = (const float *)e->dst;   // a matrix is column-major in the shader
+        for (int r = 0; r < w.rows; ++r)
+            for (int c = 0; c < w.cols; ++c) *o++ = w.rows == 1 ? d[c] : d[c * w.rows + r];
+    }
+    return 0;
+}
+
 namespace {
 std::vector<refgl::FrameBuffer::Drawn> g_drawn;
 

@@ -482,3 +482,23 @@ def test_curve_part_strips(ref, product):
         got = _drawn(ref, n)
         assert len(got) == 1 and got[0][2] == 1 and got[0][1] is None
         assert np.array_equal(got[0][0], layers.curve_part_strip(pts, part, tr)), trial   # part as plain floats
+
+
+@pytest.mark.parametrize("D,level,tx,ty", [(12.72e6, 0, 0, 0), (12.72e6, 1, 1, 0), (12.72e6, 3, 5, 2),
+                                           (12.72e6, 12, 1000, 3000), (6.4e6, 16, 40000, 12345), (100000.0, 2, 1, 3)])
+def test_sphere_patch_frames(ref, oracle_lib, product, D, level, tx, ty):
+    """NormalProducer::doCreateTile's FP64 patch frame, read back from the uniforms it
+    sets (NormalProducer.cpp:215-273), is the oracle's frame and the product's
+    (tp_sphere_frame) bit for bit, parentToTangentFrame the oracle's."""
+    u = np.empty(58, np.float32)
+    assert ref.ref_sphere_uniforms(101, level, tx, ty, D, _p(u)) == 0
+    C_, N_, L_, W2T, P2T, deform = u[:16], u[16:32], u[32:36], u[36:45], u[45:54], u[54:58]
+    D = float(np.float32(D))     # getRootQuadSize() is a float
+    f = oracle_lib.sphere_frame(D, level, tx, ty)
+    assert np.array_equal(C_, np.float32(f.C)) and np.array_equal(N_, np.float32(f.N))
+    assert np.array_equal(L_, np.float32(f.L)) and np.array_equal(W2T, np.float32(f.W2T))
+    assert deform[2] == np.float32(f.size) and deform[3] == np.float32(f.R)
+    mine = product.sphere_frame(D, level, tx, ty)
+    assert np.array_equal(mine[:45], u[:45])
+    if level > 0:
+        assert np.array_equal(P2T, oracle_lib.parent_to_tangent(D, level, tx, ty))
