@@ -612,6 +612,14 @@ def quadtree_requests(cam, root, max_level, split, dist_factor=1.0, ground=0.0):
 _REF = None
 
 
+def ref_file(rel):
+    """A file of the reference tree (path relative to its root) where the tree is on
+    this machine, else None: the reference's own data for the pin tests."""
+    from . import ref_build
+    path = os.path.join(ref_build.DEFAULT_ROOT, rel)
+    return path if os.path.exists(path) else None
+
+
 def ref_lib():
     """oracle/_ref/libref.so: pieces of the reference's C++ compiled from its sources by
     oracle/ref_build.py (noise.cpp, createDemNoise, the noise-layer choice, the CPU
@@ -648,6 +656,8 @@ def ref_lib():
                                             C.POINTER(C.c_float)]
         L.ref_ortho_noise.argtypes = [C.c_int, C.c_void_p]
         L.ref_sphere_uniforms.argtypes = [C.c_int] * 4 + [C.c_float, _f32p]
+        L.ref_residual_tile.argtypes = [C.c_char_p, C.c_int, C.c_float, C.c_int, C.c_int, C.c_int, C.c_int,
+                                        C.c_void_p, C.POINTER(C.c_int)]
         L.ref_road_meshes.argtypes = [C.c_double] * 3 + [C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_int,
                                                          C.c_float, C.c_int, C.c_int, C.POINTER(C.c_float)]
         L.ref_curve_altitude.argtypes = [C.c_double] * 3 + [C.c_void_p, C.c_void_p, C.c_int, C.c_float, C.c_float,

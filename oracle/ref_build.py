@@ -41,6 +41,10 @@ The GPU path, in a second unit (``ref_gpu.cpp``):
   the lines of ``RoadElevationLayer::doCreateTile`` that place one road (its scale, tile
   offset, ``BASEWIDTH`` / ``TOTALWIDTH`` and the drawCurveAltitude call), on stand-in
   curves whose meshes the framebuffer stand-in records;
+* in a third unit, ``ResidualProducer``'s ``init``, ``hasTile``, ``doCreateTile``,
+  ``getTileSize``, ``getTileId``, ``readTile`` and ``upsample`` as written, with the
+  reference's ``core/sources/proland/util/mfs.cpp`` and a libtiff stand-in
+  (``oracle/ref_stubs/tiffio.h``, zlib), so that it reads the reference's own pyramids;
 * the shaders those functions draw -- the upsample shaders of terrain1, terrain2,
   terrain4 (flipped diagonals) and the demo (modulated noise, with and without
   ``NO_CLAMP``), the normal shaders of terrain1, terrain2 (sphere) and the demo
@@ -364,6 +368,7 @@ LAYER_SHADERS = [
 _GPU_PRELUDE = r"""
 namespace refgl {
 Logger *Logger::DEBUG_LOGGER = nullptr;
+Logger *Logger::ERROR_LOGGER = nullptr;
 using proland::cnoise;
 using std::abs;
 using std::atan2;
@@ -938,6 +943,100 @@ extern "C" int ref_gl_normal_tile(int variant, int W, int level, int tx, int ty,
 """
 
 
+RESIDUAL_CPP = "src/terrain/sources/proland/dem/ResidualProducer.cpp"
+MFS_CPP = "src/core/sources/proland/util/mfs.cpp"
+
+_RESIDUAL_PRELUDE = r"""
+#include <pthread.h>
+#include <sys/types.h>
+#include <cstdio>
+#include <string>
+#include "ork_gl.h"
+#include "tiffio.h"
+#include "proland/util/mfs.h"
+
+namespace refgl {
+using namespace std;   // as ResidualProducer.cpp
+
+// Ork's file helpers the functions call: fopen into a FILE **, a 64-bit fseek
+inline void fopen(FILE **f, const char *name, const char *mode) { *f = std::fopen(name, mode); }
+inline int fseek64(FILE *f, long long off, int whence) { return fseeko(f, (off_t)off, whence); }
+
+// The members the extracted functions use (ResidualProducer.h).
+struct ResidualProducer : TileProducer {
+    std::string name;
+    int tileSize = 0, rootLevel = 0, deltaLevel = 0, rootTx = 0, rootTy = 0, minLevel = 0, maxLevel = 0;
+    float scale = 1.0f;
+    unsigned int header = 0;
+    unsigned int *offsets = nullptr;
+    void *mutex = nullptr;
+    FILE *tileFile = nullptr;
+    std::vector<ptr<ResidualProducer> > producers;
+    static void *key;
+    ~ResidualProducer() { delete[] offsets; }
+    void init(ptr<TileCache> cache, const char *name, int deltaLevel = 0, float zscale = 1.0);
+    bool hasTile(int level, int tx, int ty);
+    bool doCreateTile(int level, int tx, int ty, TileStorage::Slot *data);
+    void upsample(int level, int tx, int ty, float *parentTile, float *result);
+    int getTileSize(int level);
+    int getTileId(int level, int tx, int ty);
+    void readTile(int level, int tx, int ty, unsigned char *compressedData, unsigned char *uncompressedData,
+                  float *tile, float *result);
+};
+"""
+
+_RESIDUAL_DRIVER = r"""
+}  // namespace refgl
+
+// One residual tile through ResidualProducer::init (the .dat at `path`, deltaLevel,
+// zscale), hasTile and doCreateTile, into a one-channel CPU slot of tile_width^2 floats
+// (the tile written from its lower left corner at pitch tile_width).  has: hasTile.
+// Returns 0, or 1 when the file does not open as a pyramid.
+extern "C" int ref_residual_tile(const char *path, int delta, float zscale, int tile_width, int level, int tx, int ty,
+                                 float *out, int *has)
+{
+    using namespace refgl;
+    CPUTileStorage<float> storage;
+    storage.tileSize = tile_width;
+    TileCache cache;
+    cache.storage = &storage;
+    ResidualProducer r;
+    r.init(&cache, path, delta, zscale);
+    if (r.maxLevel < 0 || r.tileSize + 5 != tile_width) return 1;
+    *has = r.hasTile(level, tx, ty) ? 1 : 0;
+    CPUTileStorage<float>::CPUSlot slot;
+    slot.owner = &storage;
+    slot.data = out;
+    r.doCreateTile(level, tx, ty, &slot);
+    return 0;
+}
+"""
+
+
+def generate_residual(root):
+    """oracle/_ref/gen/ref_residual.cpp: ResidualProducer's file reading, tile ids,
+    delta chain and upsample as written (with mfs.cpp compiled beside it and the
+    libtiff stand-in)."""
+    res = _read(root, RESIDUAL_CPP)
+    src = ["// generated by oracle/ref_build.py from the reference's sources\n", _RESIDUAL_PRELUDE]
+    block, line = extract_block(res, "#define MAX_TILE_SIZE", "#define MAX_TILE_SIZE")
+    src.append("// %s:%d\n%s" % (RESIDUAL_CPP, line, block))
+    block, line = extract_block(res, "void *ResidualProducer::key = NULL;", "void *ResidualProducer::key = NULL;")
+    src.append("// :%d\n%s" % (line, block))
+    for sig in (r"void\s+residualDelete\s*\(", r"void\s+ResidualProducer::init\s*\(\s*ptr<TileCache>",
+                r"bool\s+ResidualProducer::hasTile\s*\(", r"bool\s+ResidualProducer::doCreateTile\s*\(",
+                r"int\s+ResidualProducer::getTileSize\s*\(", r"int\s+ResidualProducer::getTileId\s*\(",
+                r"void\s+ResidualProducer::readTile\s*\(", r"void\s+ResidualProducer::upsample\s*\("):
+        body, line = extract_function(res, sig)
+        src.append("// :%d\n%s" % (line, body))
+    src.append(_RESIDUAL_DRIVER)
+    os.makedirs(GEN_DIR, exist_ok=True)
+    path = os.path.join(GEN_DIR, "ref_residual.cpp")
+    with open(path, "w") as f:
+        f.write("".join(src))
+    return path
+
+
 def _load_sibling(name):
     """oracle/<name>.py by path (this file also runs as a script and is loaded by path)."""
     import importlib.util
@@ -1043,25 +1142,28 @@ def build(root=DEFAULT_ROOT, force=False):
     if not os.path.isdir(os.path.join(root, "src")):
         return LIB if os.path.exists(LIB) else None
     srcs = [os.path.join(root, p) for p in (NOISE_CPP, ELEV_CPP, CPU_ELEV_CPP, MIPMAP_CPP, NORMAL_CPP, ORTHO_CPP,
-                                            GRAPH_LAYER_CPP, ROAD_LAYER_CPP, GRAPH_PRODUCER_CPP)]
+                                            GRAPH_LAYER_CPP, ROAD_LAYER_CPP, GRAPH_PRODUCER_CPP, RESIDUAL_CPP,
+                                            MFS_CPP)]
     srcs += [os.path.join(root, rel) for _, rel, _ in UPSAMPLE_SHADERS + NORMAL_SHADERS + BLEND_SHADERS +
              LAYER_SHADERS + ORTHO_SHADERS]
     srcs += [os.path.abspath(__file__), os.path.join(HERE, "ref_glsl.py")]
-    srcs += [os.path.join(HERE, "ref_stubs", h) for h in ("pmath.h", "glsl.h", "ork_gl.h")]
+    srcs += [os.path.join(HERE, "ref_stubs", h) for h in ("pmath.h", "glsl.h", "ork_gl.h", "tiffio.h")]
     if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= max(os.path.getmtime(p) for p in srcs):
         return LIB
     gen = generate(root)
     gen_gpu = generate_gpu(root)
+    gen_res = generate_residual(root)
     tmp = LIB + ".tmp%d" % os.getpid()
     inc = ["-I", os.path.join(HERE, "ref_stubs"), "-I", os.path.join(root, NOISE_DIR),
            "-I", os.path.join(root, "src/core/sources/proland/math")]
-    flags = ["-O2", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-w"]
+    flags = ["-O2", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-w", "-DPROLAND_API="]
     objs = []
-    for unit, std in ((gen, "c++14"), (gen_gpu, "c++17"), (os.path.join(root, NOISE_CPP), "c++14")):
+    for unit, std in ((gen, "c++14"), (gen_gpu, "c++17"), (gen_res, "c++17"), (os.path.join(root, NOISE_CPP), "c++14"),
+                      (os.path.join(root, MFS_CPP), "c++14")):
         obj = os.path.join(GEN_DIR, os.path.basename(unit) + ".o")
         subprocess.check_call(["g++", "-c", "-std=" + std] + flags + inc + ["-o", obj, unit])
         objs.append(obj)
-    subprocess.check_call(["g++", "-shared", "-o", tmp] + objs)
+    subprocess.check_call(["g++", "-shared", "-o", tmp] + objs + ["-lz", "-lpthread"])
     os.replace(tmp, LIB)
     return LIB
 

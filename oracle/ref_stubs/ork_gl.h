@@ -168,6 +168,7 @@ typedef mat4<double> mat4d;
 // ---- logging ------------------------------------------------------------------------
 struct Logger {
     static Logger *DEBUG_LOGGER;
+    static Logger *ERROR_LOGGER;
     void log(const string &, const string &) {}
 };
 
@@ -420,6 +421,8 @@ struct GPUTileStorage : TileStorage {
 };
 
 template <class T> struct CPUTileStorage : TileStorage {
+    int channels = 1;
+    int getChannels() { return channels; }
     struct CPUSlot : TileStorage::Slot {
         T *data = nullptr;
     };
@@ -440,6 +443,7 @@ struct TileProducer {
     float rootQuadSize = 0.0f;
     int border = 2;
     virtual ~TileProducer() {}
+    void init(ptr<TileCache> c, bool) { cache = c; }
     ptr<TileCache> getCache() { return cache; }
     TileCache::Tile *findTile(int level, int tx, int ty)
     {

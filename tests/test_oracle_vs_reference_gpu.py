@@ -502,3 +502,58 @@ def test_sphere_patch_frames(ref, oracle_lib, product, D, level, tx, ty):
     assert np.array_equal(mine[:45], u[:45])
     if level > 0:
         assert np.array_equal(P2T, oracle_lib.parent_to_tangent(D, level, tx, ty))
+
+
+DEM_FILES = ["terrain/examples/terrain4", "edit/examples/edit3", "edit/examples/edit4", "graph/examples/graph1",
+             "river/examples/river1"]
+
+
+@pytest.mark.parametrize("name", DEM_FILES)
+@pytest.mark.parametrize("delta,zscale", [(0, 1.0), (2, 0.5), (3, 2.0)])
+def test_residual_producer_on_reference_pyramids(ref, oracle_lib, product, name, delta, zscale):
+    """ResidualProducer as written (ResidualProducer.cpp: init reading the .dat header
+    and offsets, hasTile, doCreateTile with the deltaLevel chain of readTile and
+    upsample, getTileSize / getTileId below minLevel, int16 * scale * zscale), on the
+    reference's own DEM.dat pyramids, its TIFF strips inflated by zlib: every tile of
+    levels 0-3 and a spread of deeper ones is the product's host residual tile
+    (tp_residual_tile) bit for bit, and both answer hasTile alike.
+
+    Only tiles the pyramid holds are read: at pyramid level p = level + delta >= minLevel,
+    tx, ty < 2^(p - minLevel) (below minLevel every (tx, ty) names the level's single
+    tile).  hasTile checks the root only, and the elevation producer asks for
+    (level, tx / mod, ty / mod), which stays inside; the reference reads past its
+    offsets table for a tile outside, where the product returns TP_E_BAD_ARG."""
+    import ctypes as C
+    import struct
+    path = oracle_lib.ref_file("src/%s/DEM.dat" % name)
+    if path is None:
+        pytest.skip("the reference's pyramids are not on this machine")
+    min_level, max_level, tile_size = struct.unpack("<3i", open(path, "rb").read(12))
+    W = tile_size + 5
+    storage = product.TileStorage(W, 1, 8, on_device=product.TileStorage.BOOKKEEPING)
+    prod = product.ResidualProducer(product.TileCache(storage, "residuals"), path, delta=delta, zscale=zscale)
+    rng = np.random.default_rng(len(name) + delta)
+    checked = 0
+    for level in range(0, max_level - delta + 1):
+        p = level + delta
+        n = 1 << (p - min_level) if p >= min_level else 1 << level
+        tiles = {(x, y) for x in range(min(n, 4)) for y in range(min(n, 4))}
+        tiles |= {(int(rng.integers(0, n)), int(rng.integers(0, n))) for _ in range(6)}
+        for tx, ty in sorted(tiles):
+            out = np.full((W, W), np.nan, np.float32)
+            has = C.c_int()
+            assert ref.ref_residual_tile(path.encode(), delta, zscale, W, level, tx, ty, out.ctypes.data,
+                                         C.byref(has)) == 0
+            assert prod.has_tile(level, tx, ty) == bool(has.value), (level, tx, ty)
+            if has.value:
+                written = ~np.isnan(out)    # a tile below minLevel fills the slot's corner
+                assert np.array_equal(prod.tile(level, tx, ty)[written], out[written]), (level, tx, ty)
+                checked += 1
+    # past the pyramid's last level: no tile on either side
+    for tx, ty in ((0, 0), (1, 0)):
+        has = C.c_int()
+        out = np.zeros((W, W), np.float32)
+        ref.ref_residual_tile(path.encode(), delta, zscale, W, max_level - delta + 1, tx, ty, out.ctypes.data,
+                              C.byref(has))
+        assert not has.value and not prod.has_tile(max_level - delta + 1, tx, ty)
+    assert checked >= 20
