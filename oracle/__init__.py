@@ -658,6 +658,8 @@ def ref_lib():
         L.ref_sphere_uniforms.argtypes = [C.c_int] * 4 + [C.c_float, _f32p]
         L.ref_residual_tile.argtypes = [C.c_char_p, C.c_int, C.c_float, C.c_int, C.c_int, C.c_int, C.c_int,
                                         C.c_void_p, C.POINTER(C.c_int)]
+        L.ref_ortho_dat_tile.argtypes = [C.c_char_p, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_int,
+                                         C.POINTER(C.c_int), C.POINTER(C.c_int)]
         L.ref_road_meshes.argtypes = [C.c_double] * 3 + [C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_int,
                                                          C.c_float, C.c_int, C.c_int, C.POINTER(C.c_float)]
         L.ref_curve_altitude.argtypes = [C.c_double] * 3 + [C.c_void_p, C.c_void_p, C.c_int, C.c_float, C.c_float,

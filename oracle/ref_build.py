@@ -42,7 +42,8 @@ The GPU path, in a second unit (``ref_gpu.cpp``):
   offset, ``BASEWIDTH`` / ``TOTALWIDTH`` and the drawCurveAltitude call), on stand-in
   curves whose meshes the framebuffer stand-in records;
 * in a third unit, ``ResidualProducer``'s ``init``, ``hasTile``, ``doCreateTile``,
-  ``getTileSize``, ``getTileId``, ``readTile`` and ``upsample`` as written, with the
+  ``getTileSize``, ``getTileId``, ``readTile`` and ``upsample``, and
+  ``OrthoCPUProducer``'s ``init``, ``hasTile``, ``doCreateTile`` and ``getTileId``, as written, with the
   reference's ``core/sources/proland/util/mfs.cpp`` and a libtiff stand-in
   (``oracle/ref_stubs/tiffio.h``, zlib), so that it reads the reference's own pyramids;
 * the shaders those functions draw -- the upsample shaders of terrain1, terrain2,
@@ -944,6 +945,7 @@ extern "C" int ref_gl_normal_tile(int variant, int W, int level, int tx, int ty,
 
 
 RESIDUAL_CPP = "src/terrain/sources/proland/dem/ResidualProducer.cpp"
+ORTHO_CPU_CPP = "src/terrain/sources/proland/ortho/OrthoCPUProducer.cpp"
 MFS_CPP = "src/core/sources/proland/util/mfs.cpp"
 
 _RESIDUAL_PRELUDE = r"""
@@ -983,6 +985,23 @@ struct ResidualProducer : TileProducer {
     void readTile(int level, int tx, int ty, unsigned char *compressedData, unsigned char *uncompressedData,
                   float *tile, float *result);
 };
+
+// The members OrthoCPUProducer's extracted functions use (OrthoCPUProducer.h).
+struct OrthoCPUProducer : TileProducer {
+    std::string name;
+    int maxLevel = 0, tileSize = 0, channels = 0, border = 2;
+    bool dxt = false;
+    long long header = 0;
+    long long *offsets = nullptr;
+    void *mutex = nullptr;
+    FILE *tileFile = nullptr;
+    static void *key;
+    ~OrthoCPUProducer() { delete[] offsets; }
+    void init(ptr<TileCache> cache, const char *name);
+    bool hasTile(int level, int tx, int ty);
+    bool doCreateTile(int level, int tx, int ty, TileStorage::Slot *data);
+    int getTileId(int level, int tx, int ty);
+};
 """
 
 _RESIDUAL_DRIVER = r"""
@@ -1010,6 +1029,38 @@ extern "C" int ref_residual_tile(const char *path, int delta, float zscale, int 
     r.doCreateTile(level, tx, ty, &slot);
     return 0;
 }
+
+// One tile of an ortho pyramid through OrthoCPUProducer::init, hasTile and doCreateTile
+// into a CPU slot of width^2 * channels bytes (`capacity` at least that).  info: the
+// pyramid's (maxLevel, tileSize, channels, border, width).  has: hasTile.  Returns 0,
+// 1 when the file does not open, 2 when `out` is too small.
+extern "C" int ref_ortho_dat_tile(const char *path, int level, int tx, int ty, unsigned char *out, int capacity,
+                                  int *info, int *has)
+{
+    using namespace refgl;
+    CPUTileStorage<unsigned char> storage;
+    TileCache cache;
+    cache.storage = &storage;
+    OrthoCPUProducer o;
+    o.init(&cache, path);
+    if (o.maxLevel < 0) return 1;
+    const int width = o.tileSize + 2 * o.border;
+    info[0] = o.maxLevel;
+    info[1] = o.tileSize;
+    info[2] = o.channels;
+    info[3] = o.border;
+    info[4] = width;
+    if (capacity < width * width * o.channels) return 2;
+    storage.tileSize = width;
+    storage.channels = o.channels;
+    *has = o.hasTile(level, tx, ty) ? 1 : 0;
+    CPUTileStorage<unsigned char>::CPUSlot slot;
+    slot.owner = &storage;
+    slot.data = out;
+    slot.size = width * width * o.channels;
+    if (*has) o.doCreateTile(level, tx, ty, &slot);
+    return 0;
+}
 """
 
 
@@ -1028,6 +1079,16 @@ def generate_residual(root):
                 r"int\s+ResidualProducer::getTileSize\s*\(", r"int\s+ResidualProducer::getTileId\s*\(",
                 r"void\s+ResidualProducer::readTile\s*\(", r"void\s+ResidualProducer::upsample\s*\("):
         body, line = extract_function(res, sig)
+        src.append("// :%d\n%s" % (line, body))
+    ortho = _read(root, ORTHO_CPU_CPP)
+    block, line = extract_block(ortho, "#define MAX_TILE_SIZE", "#define MAX_TILE_SIZE")
+    src.append("#undef MAX_TILE_SIZE\n// %s:%d\n%s" % (ORTHO_CPU_CPP, line, block))
+    block, line = extract_block(ortho, "void *OrthoCPUProducer::key = NULL;", "void *OrthoCPUProducer::key = NULL;")
+    src.append("// :%d\n%s" % (line, block))
+    for sig in (r"void\s+orthoCPUDelete\s*\(", r"void\s+OrthoCPUProducer::init\s*\(\s*ptr<TileCache>",
+                r"bool\s+OrthoCPUProducer::hasTile\s*\(", r"bool\s+OrthoCPUProducer::doCreateTile\s*\(",
+                r"int\s+OrthoCPUProducer::getTileId\s*\("):
+        body, line = extract_function(ortho, sig)
         src.append("// :%d\n%s" % (line, body))
     src.append(_RESIDUAL_DRIVER)
     os.makedirs(GEN_DIR, exist_ok=True)
@@ -1143,7 +1204,7 @@ def build(root=DEFAULT_ROOT, force=False):
         return LIB if os.path.exists(LIB) else None
     srcs = [os.path.join(root, p) for p in (NOISE_CPP, ELEV_CPP, CPU_ELEV_CPP, MIPMAP_CPP, NORMAL_CPP, ORTHO_CPP,
                                             GRAPH_LAYER_CPP, ROAD_LAYER_CPP, GRAPH_PRODUCER_CPP, RESIDUAL_CPP,
-                                            MFS_CPP)]
+                                            ORTHO_CPU_CPP, MFS_CPP)]
     srcs += [os.path.join(root, rel) for _, rel, _ in UPSAMPLE_SHADERS + NORMAL_SHADERS + BLEND_SHADERS +
              LAYER_SHADERS + ORTHO_SHADERS]
     srcs += [os.path.abspath(__file__), os.path.join(HERE, "ref_glsl.py")]

@@ -425,6 +425,7 @@ template <class T> struct CPUTileStorage : TileStorage {
     int getChannels() { return channels; }
     struct CPUSlot : TileStorage::Slot {
         T *data = nullptr;
+        int size = 0;
     };
 };
 

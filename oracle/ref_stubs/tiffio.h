@@ -6,9 +6,11 @@
  * The types are libtiff 3's (tsize_t a 32-bit int, toff_t a 32-bit unsigned), which
  * the function-pointer casts in readTile (mfs_read, mfs_lseek, ...) were written for.
  * TIFFReadEncodedStrip reads the first image directory of a little- or big-endian
- * TIFF -- StripOffsets (273), StripByteCounts (279), Compression (259) -- and returns
- * strip 0 inflated by zlib (Compression 8 or 32946, Deflate) or copied (1, none), the
- * forms of the reference's pyramids (one strip per tile, no predictor). */
+ * TIFF -- StripOffsets (273), StripByteCounts (279), Compression (259), and the strip's
+ * decoded size from ImageWidth (256), ImageLength (257), BitsPerSample (258),
+ * SamplesPerPixel (277), RowsPerStrip (278) -- and returns strip 0 inflated by zlib
+ * (Compression 8 or 32946, Deflate) or copied (1, none), at most that size, the forms
+ * of the reference's pyramids (one strip per tile, no predictor). */
 #ifndef TIFFIO_STUB_H
 #define TIFFIO_STUB_H
 
@@ -67,7 +69,7 @@ inline tsize_t TIFFReadEncodedStrip(TIFF *t, tstrip_t strip, tdata_t buf, tsize_
     const uint32_t ifd = tiff_stub_rd(&b[4], 4, le);
     if ((size_t)ifd + 2 > b.size()) return -1;
     const uint32_t count = tiff_stub_rd(&b[ifd], 2, le);
-    uint32_t comp = 1, off = 0, cnt = 0;
+    uint32_t comp = 1, off = 0, cnt = 0, width = 0, length = 0, bits = 1, spp = 1, rows = 0xFFFFFFFFu;
     for (uint32_t k = 0; k < count && (size_t)ifd + 2 + 12 * (k + 1) <= b.size(); ++k) {
         const unsigned char *e = &b[ifd + 2 + 12 * k];
         const uint32_t tag = tiff_stub_rd(e, 2, le), type = tiff_stub_rd(e + 2, 2, le), num = tiff_stub_rd(e + 4, 4, le);
@@ -82,10 +84,17 @@ inline tsize_t TIFFReadEncodedStrip(TIFF *t, tstrip_t strip, tdata_t buf, tsize_
         if (tag == 259) comp = value;
         if (tag == 273) off = value;
         if (tag == 279) cnt = value;
+        if (tag == 256) width = value;
+        if (tag == 257) length = value;
+        if (tag == 258) bits = value;
+        if (tag == 277) spp = value;
+        if (tag == 278) rows = value;
     }
     if ((size_t)off + cnt > b.size()) return -1;
+    const uint64_t strip_bytes = (uint64_t)width * (rows < length ? rows : length) * spp * bits / 8;
+    if (strip_bytes == 0 || strip_bytes > (1u << 24)) return -1;
     if (comp == 1) {
-        if (cnt > 256 * 256 * 2) return -1;
+        if (cnt > strip_bytes) return -1;
         memcpy(buf, &b[off], cnt);
         return (tsize_t)cnt;
     }
@@ -96,7 +105,7 @@ inline tsize_t TIFFReadEncodedStrip(TIFF *t, tstrip_t strip, tdata_t buf, tsize_
     z.next_in = (Bytef *)&b[off];
     z.avail_in = cnt;
     z.next_out = (Bytef *)buf;
-    z.avail_out = 256 * 256 * 2;   /* readTile's buffer: MAX_TILE_SIZE^2 int16 samples */
+    z.avail_out = (uInt)strip_bytes;
     const int rc = inflate(&z, Z_FINISH);
     const tsize_t n = (tsize_t)z.total_out;
     inflateEnd(&z);

@@ -557,3 +557,30 @@ def test_residual_producer_on_reference_pyramids(ref, oracle_lib, product, name,
                               C.byref(has))
         assert not has.value and not prod.has_tile(max_level - delta + 1, tx, ty)
     assert checked >= 20
+
+
+def test_ortho_cpu_producer_on_reference_pyramid(ref, oracle_lib, product):
+    """OrthoCPUProducer as written (OrthoCPUProducer.cpp: init reading the header and
+    64-bit offsets, hasTile, doCreateTile inflating the tile's TIFF strip, getTileId) on
+    the reference's graph1/RGB.dat: every tile byte for byte the product's reader
+    (tp_ortho_dat_read_tile), the header fields alike."""
+    import ctypes as C
+    path = oracle_lib.ref_file("src/graph/examples/graph1/RGB.dat")
+    if path is None:
+        pytest.skip("the reference's pyramids are not on this machine")
+    d = product.OrthoDat(path)
+    info = (C.c_int * 5)()
+    checked = 0
+    for level in range(0, d.max_level + 2):
+        for tx in range(1 << level):
+            for ty in range(1 << level):
+                out = np.zeros((d.width, d.width, d.channels), np.uint8)
+                has = C.c_int()
+                assert ref.ref_ortho_dat_tile(path.encode(), level, tx, ty, out.ctypes.data, out.size, info,
+                                              C.byref(has)) == 0
+                assert list(info) == [d.max_level, d.tile_size, d.channels, 0 if d.flags & 2 else 2, d.width]
+                assert bool(has.value) == (level <= d.max_level)
+                if has.value:
+                    assert np.array_equal(d.tile(level, tx, ty), out), (level, tx, ty)
+                    checked += 1
+    assert checked == sum(4 ** l for l in range(d.max_level + 1))
