@@ -660,6 +660,12 @@ def ref_lib():
                                         C.c_void_p, C.POINTER(C.c_int)]
         L.ref_ortho_dat_tile.argtypes = [C.c_char_p, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_int,
                                          C.POINTER(C.c_int), C.POINTER(C.c_int)]
+        L.ref_cache_create.argtypes = [C.c_int, C.c_int]
+        L.ref_cache_get.argtypes = [C.c_int] * 4 + [C.POINTER(C.c_int)]
+        L.ref_cache_put.argtypes = [C.c_int] * 4
+        L.ref_cache_find.argtypes = [C.c_int] * 5
+        L.ref_cache_prefetch.argtypes = [C.c_int] * 4
+        L.ref_cache_counts.argtypes = [C.POINTER(C.c_int)] * 3
         L.ref_road_meshes.argtypes = [C.c_double] * 3 + [C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_int,
                                                          C.c_float, C.c_int, C.c_int, C.POINTER(C.c_float)]
         L.ref_curve_altitude.argtypes = [C.c_double] * 3 + [C.c_void_p, C.c_void_p, C.c_int, C.c_float, C.c_float,

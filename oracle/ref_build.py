@@ -46,6 +46,9 @@ The GPU path, in a second unit (``ref_gpu.cpp``):
   ``OrthoCPUProducer``'s ``init``, ``hasTile``, ``doCreateTile`` and ``getTileId``, as written, with the
   reference's ``core/sources/proland/util/mfs.cpp`` and a libtiff stand-in
   (``oracle/ref_stubs/tiffio.h``, zlib), so that it reads the reference's own pyramids;
+* in a fourth unit, ``TileCache``'s and ``TileStorage``'s functions
+  (``core/sources/proland/producer/TileCache.cpp``, ``TileStorage.cpp``) as written, for a
+  step-by-step comparison with the product's cache;
 * the shaders those functions draw -- the upsample shaders of terrain1, terrain2,
   terrain4 (flipped diagonals) and the demo (modulated noise, with and without
   ``NO_CLAMP``), the normal shaders of terrain1, terrain2 (sphere) and the demo
@@ -1098,6 +1101,269 @@ def generate_residual(root):
     return path
 
 
+CACHE_CPP = "src/core/sources/proland/producer/TileCache.cpp"
+STORAGE_CPP = "src/core/sources/proland/producer/TileStorage.cpp"
+
+_CACHE_PRELUDE = r"""
+#include <pthread.h>
+#include <cassert>
+#include <cstdarg>
+#include <list>
+#include <map>
+#include <string>
+#include <utility>
+#include <vector>
+#include "ork_gl.h"
+
+namespace refcache {
+using namespace std;   // as TileCache.cpp and TileStorage.cpp
+using refgl::ptr;
+
+// Ork stand-ins: Object, the debug logger, tasks with a done flag, a scheduler.
+struct Object {
+    explicit Object(const char *) {}
+    virtual ~Object() {}
+};
+struct Logger {
+    static Logger *DEBUG_LOGGER;
+    void logf(const char *, const char *, ...) {}
+};
+Logger *Logger::DEBUG_LOGGER = nullptr;
+struct Task {
+    enum reason { DATA_NEEDED, DATA_CHANGED };
+    bool done = false;
+    bool isDone() { return done; }
+    void setIsDone(bool d, unsigned int, reason) { done = d; }
+};
+struct Scheduler {
+    void reschedule(ptr<Task> t, Task::reason r, unsigned int) { t->setIsDone(false, 0, r); }
+};
+
+// The declarations of TileStorage.h and TileCache.h the extracted functions define.
+struct TileStorage : Object {
+    struct Slot {
+        std::pair<int, std::pair<int, std::pair<int, int> > > id;
+        void *producerTask;
+        int index = -1;   // the harness's name for the slot
+        Slot(TileStorage *owner);
+        virtual ~Slot();
+        TileStorage *getOwner();
+        void lock(bool lock);
+    private:
+        TileStorage *owner;
+        void *mutex;
+    };
+    TileStorage(int tileSize, int capacity);
+    TileStorage();
+    virtual ~TileStorage();
+    Slot *newSlot();
+    void deleteSlot(Slot *t);
+    int getTileSize();
+    int getCapacity();
+    int getFreeSlots();
+    void init(int tileSize, int capacity);
+    int tileSize, capacity;
+    std::list<Slot *> freeSlots;
+};
+
+// a producer whose createTile returns the task to reuse, or a new one not done
+struct TileProducer {
+    std::vector<Task *> tasks;
+    ~TileProducer()
+    {
+        for (Task *t : tasks) delete t;
+    }
+    ptr<Task> createTile(int, int, int, TileStorage::Slot *, unsigned int, ptr<Task> task)
+    {
+        if (task.p) return task;
+        tasks.push_back(new Task());
+        return ptr<Task>(tasks.back());
+    }
+};
+
+struct TileCache : Object {
+    class Tile {
+    public:
+        typedef std::pair<int, std::pair<int, int> > Id;
+        typedef std::pair<int, Id> TId;
+        const int producerId;
+        const int level;
+        const int tx;
+        const int ty;
+        const ptr<Task> task;
+        Tile(int producerId, int level, int tx, int ty, ptr<Task> task, TileStorage::Slot *data);
+        ~Tile();
+        TileStorage::Slot *getData(bool check = true);
+        Id getId() const;
+        TId getTId() const;
+        static Id getId(int level, int tx, int ty);
+        static TId getTId(int producerId, int level, int tx, int ty);
+        TileStorage::Slot *data;
+        int users;
+    };
+    TileCache(ptr<TileStorage> storage, std::string name, ptr<Scheduler> scheduler = ptr<Scheduler>());
+    TileCache();
+    virtual ~TileCache();
+    ptr<TileStorage> getStorage();
+    ptr<Scheduler> getScheduler();
+    int getUsedTiles();
+    int getUnusedTiles();
+    Tile *findTile(int producerId, int level, int tx, int ty, bool includeCache = false);
+    Tile *getTile(int producerId, int level, int tx, int ty, unsigned int deadline, int *users = NULL);
+    ptr<Task> prefetchTile(int producerId, int level, int tx, int ty);
+    int putTile(Tile *t);
+    void invalidateTiles(int producerId);
+    void invalidateTile(int producerId, int level, int tx, int ty);
+    void init(ptr<TileStorage> storage, std::string name, ptr<Scheduler> scheduler = ptr<Scheduler>());
+    void createTileTaskDeleted(int producerId, int level, int tx, int ty);
+    typedef std::map<Tile::TId, std::list<Tile *>::iterator> Cache;
+    std::string name;
+    int nextProducerId;
+    std::map<int, TileProducer *> producers;
+    ptr<TileStorage> storage;
+    ptr<Scheduler> scheduler;
+    std::map<Tile::TId, Tile *> usedTiles;
+    Cache unusedTiles;
+    std::list<Tile *> unusedTilesOrder;
+    std::map<Tile::TId, Task *> deletedTiles;
+    int queries;
+    int misses;
+    void *mutex;
+};
+"""
+
+_CACHE_DRIVER = r"""
+}  // namespace refcache
+
+namespace {
+struct CacheHarness {
+    refcache::TileStorage storage;
+    refcache::TileCache cache;
+    std::vector<refcache::TileProducer *> producers;
+    ~CacheHarness()
+    {
+        // release every tile (the cache's destructor expects no used tile)
+        for (auto &u : cache.usedTiles) u.second->users = 0;
+        std::vector<refcache::TileCache::Tile *> used;
+        for (auto &u : cache.usedTiles) used.push_back(u.second);
+        for (refcache::TileCache::Tile *t : used) {
+            t->users = 1;
+            cache.putTile(t);
+        }
+        for (refcache::TileProducer *p : producers) delete p;
+    }
+};
+CacheHarness *g_cache = nullptr;
+
+int slot_of(refcache::TileCache::Tile *t) { return t ? t->data->index : -1; }
+}  // namespace
+
+// A TileCache over a storage of `capacity` slots (created in index order, as the
+// storages' init functions do) shared by `nproducers` producers (ids 0, 1, ...).
+extern "C" void ref_cache_create(int capacity, int nproducers)
+{
+    delete g_cache;
+    g_cache = new CacheHarness();
+    g_cache->storage.init(1, capacity);
+    for (int k = 0; k < capacity; ++k) {
+        refcache::TileStorage::Slot *s = new refcache::TileStorage::Slot(&g_cache->storage);
+        s->index = k;
+        g_cache->storage.freeSlots.push_back(s);
+    }
+    g_cache->cache.init(&g_cache->storage, "cache");
+    for (int k = 0; k < nproducers; ++k) {
+        g_cache->producers.push_back(new refcache::TileProducer());
+        g_cache->cache.producers[k] = g_cache->producers.back();
+    }
+}
+
+// getTile: the tile's slot or -1 (cache full); users_before: its users before the call
+extern "C" int ref_cache_get(int producer, int level, int tx, int ty, int *users_before)
+{
+    int users = -1;
+    refcache::TileCache::Tile *t = g_cache->cache.getTile(producer, level, tx, ty, 0, &users);
+    *users_before = t ? users : -1;
+    return slot_of(t);
+}
+
+// putTile of the used tile (producer, level, tx, ty): its users after, or -1 if not used
+extern "C" int ref_cache_put(int producer, int level, int tx, int ty)
+{
+    refcache::TileCache::Tile *t = g_cache->cache.findTile(producer, level, tx, ty, false);
+    return t ? g_cache->cache.putTile(t) : -1;
+}
+
+// findTile: the tile's slot or -1
+extern "C" int ref_cache_find(int producer, int level, int tx, int ty, int include_cache)
+{
+    return slot_of(g_cache->cache.findTile(producer, level, tx, ty, include_cache != 0));
+}
+
+// prefetchTile: 1 when it created the tile (a task returned), else 0
+extern "C" int ref_cache_prefetch(int producer, int level, int tx, int ty)
+{
+    return g_cache->cache.prefetchTile(producer, level, tx, ty).p != nullptr ? 1 : 0;
+}
+
+extern "C" void ref_cache_counts(int *used, int *unused, int *free_slots)
+{
+    *used = g_cache->cache.getUsedTiles();
+    *unused = g_cache->cache.getUnusedTiles();
+    *free_slots = g_cache->storage.getFreeSlots();
+}
+
+// whether the task of the tile (used or cached) is done; -1 without such a tile
+extern "C" int ref_cache_done(int producer, int level, int tx, int ty)
+{
+    refcache::TileCache::Tile *t = g_cache->cache.findTile(producer, level, tx, ty, true);
+    return t ? (t->task->isDone() ? 1 : 0) : -1;
+}
+
+// the tile's task runs: marks it done (what the scheduler does)
+extern "C" void ref_cache_produce(int producer, int level, int tx, int ty)
+{
+    refcache::TileCache::Tile *t = g_cache->cache.findTile(producer, level, tx, ty, true);
+    if (t) t->task->setIsDone(true, 0, refcache::Task::DATA_NEEDED);
+}
+
+extern "C" void ref_cache_invalidate(int producer) { g_cache->cache.invalidateTiles(producer); }
+"""
+
+
+def generate_cache(root):
+    """oracle/_ref/gen/ref_cache.cpp: TileCache's and TileStorage's functions as written."""
+    cache = _read(root, CACHE_CPP)
+    storage = _read(root, STORAGE_CPP)
+    src = ["// generated by oracle/ref_build.py from the reference's sources\n", _CACHE_PRELUDE]
+    storage_sigs = [r"^TileStorage::Slot::Slot\(", r"^TileStorage::Slot::~Slot\(",
+                    r"TileStorage \*TileStorage::Slot::getOwner\(", r"void TileStorage::Slot::lock\(",
+                    r"^TileStorage::TileStorage\(\)", r"void TileStorage::init\(", r"^TileStorage::~TileStorage\(",
+                    r"TileStorage::Slot \*TileStorage::newSlot\(", r"void TileStorage::deleteSlot\(",
+                    r"int TileStorage::getTileSize\(", r"int TileStorage::getCapacity\(",
+                    r"int TileStorage::getFreeSlots\("]
+    cache_sigs = [r"^TileCache::Tile::Tile\(", r"^TileCache::Tile::~Tile\(",
+                  r"TileStorage::Slot \*TileCache::Tile::getData\(",
+                  r"TileCache::Tile::Id TileCache::Tile::getId\(\) const",
+                  r"TileCache::Tile::TId TileCache::Tile::getTId\(\) const",
+                  r"TileCache::Tile::Id TileCache::Tile::getId\(int", r"TileCache::Tile::TId TileCache::Tile::getTId\(int",
+                  r"^TileCache::TileCache\(\)", r"void TileCache::init\(", r"^TileCache::~TileCache\(",
+                  r"ptr<TileStorage> TileCache::getStorage\(", r"int TileCache::getUsedTiles\(",
+                  r"int TileCache::getUnusedTiles\(", r"TileCache::Tile\* TileCache::findTile\(",
+                  r"TileCache::Tile\* TileCache::getTile\(", r"ptr<Task> TileCache::prefetchTile\(",
+                  r"int TileCache::putTile\(", r"void TileCache::invalidateTiles\(",
+                  r"void TileCache::invalidateTile\(", r"void TileCache::createTileTaskDeleted\("]
+    for text, rel, sigs in ((storage, STORAGE_CPP, storage_sigs), (cache, CACHE_CPP, cache_sigs)):
+        for sig in sigs:
+            body, line = extract_function(text, sig)
+            src.append("// %s:%d\n%s" % (rel, line, body))
+    src.append(_CACHE_DRIVER)
+    os.makedirs(GEN_DIR, exist_ok=True)
+    path = os.path.join(GEN_DIR, "ref_cache.cpp")
+    with open(path, "w") as f:
+        f.write("".join(src))
+    return path
+
+
 def _load_sibling(name):
     """oracle/<name>.py by path (this file also runs as a script and is loaded by path)."""
     import importlib.util
@@ -1204,7 +1470,7 @@ def build(root=DEFAULT_ROOT, force=False):
         return LIB if os.path.exists(LIB) else None
     srcs = [os.path.join(root, p) for p in (NOISE_CPP, ELEV_CPP, CPU_ELEV_CPP, MIPMAP_CPP, NORMAL_CPP, ORTHO_CPP,
                                             GRAPH_LAYER_CPP, ROAD_LAYER_CPP, GRAPH_PRODUCER_CPP, RESIDUAL_CPP,
-                                            ORTHO_CPU_CPP, MFS_CPP)]
+                                            ORTHO_CPU_CPP, MFS_CPP, CACHE_CPP, STORAGE_CPP)]
     srcs += [os.path.join(root, rel) for _, rel, _ in UPSAMPLE_SHADERS + NORMAL_SHADERS + BLEND_SHADERS +
              LAYER_SHADERS + ORTHO_SHADERS]
     srcs += [os.path.abspath(__file__), os.path.join(HERE, "ref_glsl.py")]
@@ -1214,12 +1480,14 @@ def build(root=DEFAULT_ROOT, force=False):
     gen = generate(root)
     gen_gpu = generate_gpu(root)
     gen_res = generate_residual(root)
+    gen_cache = generate_cache(root)
     tmp = LIB + ".tmp%d" % os.getpid()
     inc = ["-I", os.path.join(HERE, "ref_stubs"), "-I", os.path.join(root, NOISE_DIR),
            "-I", os.path.join(root, "src/core/sources/proland/math")]
     flags = ["-O2", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-w", "-DPROLAND_API="]
     objs = []
-    for unit, std in ((gen, "c++14"), (gen_gpu, "c++17"), (gen_res, "c++17"), (os.path.join(root, NOISE_CPP), "c++14"),
+    for unit, std in ((gen, "c++14"), (gen_gpu, "c++17"), (gen_res, "c++17"), (gen_cache, "c++17"),
+                      (os.path.join(root, NOISE_CPP), "c++14"),
                       (os.path.join(root, MFS_CPP), "c++14")):
         obj = os.path.join(GEN_DIR, os.path.basename(unit) + ".o")
         subprocess.check_call(["g++", "-c", "-std=" + std] + flags + inc + ["-o", obj, unit])
