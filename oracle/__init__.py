@@ -666,6 +666,8 @@ def ref_lib():
         L.ref_cache_find.argtypes = [C.c_int] * 5
         L.ref_cache_prefetch.argtypes = [C.c_int] * 4
         L.ref_cache_counts.argtypes = [C.POINTER(C.c_int)] * 3
+        L.ref_quadtree.argtypes = [C.c_double, C.c_int, C.c_float, C.c_float, C.c_double, C.c_double, C.c_double,
+                                   C.c_float, C.c_void_p, C.c_int]
         L.ref_road_meshes.argtypes = [C.c_double] * 3 + [C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_int,
                                                          C.c_float, C.c_int, C.c_int, C.POINTER(C.c_float)]
         L.ref_curve_altitude.argtypes = [C.c_double] * 3 + [C.c_void_p, C.c_void_p, C.c_int, C.c_float, C.c_float,

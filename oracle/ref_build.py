@@ -49,6 +49,9 @@ The GPU path, in a second unit (``ref_gpu.cpp``):
 * in a fourth unit, ``TileCache``'s and ``TileStorage``'s functions
   (``core/sources/proland/producer/TileCache.cpp``, ``TileStorage.cpp``) as written, for a
   step-by-step comparison with the product's cache;
+* in a fifth unit, ``TerrainQuad``'s ``update`` / ``subdivide`` and ``TerrainNode``'s
+  ``getCameraDist`` (``core/sources/proland/terrain/``) as written, for the view-driven
+  requests;
 * the shaders those functions draw -- the upsample shaders of terrain1, terrain2,
   terrain4 (flipped diagonals) and the demo (modulated noise, with and without
   ``NO_CLAMP``), the normal shaders of terrain1, terrain2 (sphere) and the demo
@@ -1364,6 +1367,158 @@ def generate_cache(root):
     return path
 
 
+QUAD_CPP = "src/core/sources/proland/terrain/TerrainQuad.cpp"
+NODE_CPP = "src/core/sources/proland/terrain/TerrainNode.cpp"
+
+_QUAD_PRELUDE = r"""
+#include <algorithm>
+#include <cassert>
+#include <cmath>
+#include <map>
+#include <memory>
+#include <tuple>
+#include <vector>
+
+namespace refquad {
+using namespace std;   // as TerrainQuad.cpp and TerrainNode.cpp
+
+// an owning pointer in the place of Ork's reference-counted ptr
+template <class T> struct ptr {
+    std::shared_ptr<T> s;
+    ptr() {}
+    ptr(T *q) : s(q) {}
+    T *operator->() const { return s.get(); }
+    bool operator==(const T *q) const { return s.get() == q; }
+};
+struct Object {
+    explicit Object(const char *) {}
+    virtual ~Object() {}
+};
+inline bool isFinite(float x) { return std::isfinite(x); }
+struct vec3d {
+    double x, y, z;
+};
+struct box3d {
+    double xmin, xmax, ymin, ymax, zmin, zmax;
+    box3d(double a, double b, double c, double d, double e, double f)
+        : xmin(a), xmax(b), ymin(c), ymax(d), zmin(e), zmax(f) {}
+};
+struct SceneManager {
+    enum visibility { FULLY_VISIBLE, PARTIALLY_VISIBLE, INVISIBLE };
+};
+
+// The TerrainNode members TerrainQuad::update calls: every quad partially visible
+// (the test has no view frustum), nothing occluded; getVisibility records the boxes
+// in the order update meets them.
+struct TerrainNode {
+    bool splitInvisibleQuads = false;
+    int maxLevel = 0;
+    float splitDist = 2.0f, distFactor = 1.0f;
+    vec3d localCameraPos{0, 0, 0};
+    static float groundHeightAtCamera;
+    std::vector<std::tuple<double, double, double> > visits;
+    SceneManager::visibility getVisibility(const box3d &b)
+    {
+        visits.push_back(std::make_tuple(b.xmin, b.ymin, b.xmax - b.xmin));
+        return SceneManager::PARTIALLY_VISIBLE;
+    }
+    bool isOccluded(const box3d &) { return false; }
+    bool addOccluder(const box3d &) { return false; }
+    float getCameraDist(const box3d &localBox) const;
+    float getSplitDistance() const;
+    vec3d getLocalCamera() const;
+};
+float TerrainNode::groundHeightAtCamera = 0.0f;
+
+// The declaration of TerrainQuad.h the extracted functions define.
+struct TerrainQuad : Object {
+    const TerrainQuad *parent;
+    const int level;
+    const int tx;
+    const int ty;
+    const double ox;
+    const double oy;
+    const double l;
+    float zmin;
+    float zmax;
+    ptr<TerrainQuad> children[4];
+    SceneManager::visibility visible;
+    bool occluded;
+    bool drawable;
+    TerrainQuad(TerrainNode *owner, const TerrainQuad *parent, int tx, int ty, double ox, double oy, double l,
+                float zmin, float zmax);
+    bool isLeaf() const;
+    void update();
+    TerrainNode *owner;
+    void subdivide();
+};
+"""
+
+_QUAD_DRIVER = r"""
+void collect(const TerrainQuad *q, std::map<std::tuple<double, double, double>, const TerrainQuad *> &m)
+{
+    m[std::make_tuple(q->ox, q->oy, q->l)] = q;
+    if (!q->isLeaf())
+        for (int k = 0; k < 4; ++k) collect(q->children[k].s.get(), m);
+}
+}  // namespace refquad
+
+// The quads of a terrain's quadtree after TerrainQuad::update of its root (the root
+// quad of TerrainNode::init, [-size, size]^2 with size = root_size / 2) for a camera at
+// (cx, cy, cz) and the ground height at the camera: (level, tx, ty) in the order
+// update visits them (3 ints each, at most `capacity` quads).  Returns the count.
+extern "C" int ref_quadtree(double root_size, int max_level, float split_dist, float dist_factor, double cx, double cy,
+                            double cz, float ground, int *out, int capacity)
+{
+    using namespace refquad;
+    TerrainNode node;
+    node.maxLevel = max_level;
+    node.splitDist = split_dist;
+    node.distFactor = dist_factor;
+    node.localCameraPos = vec3d{cx, cy, cz};
+    TerrainNode::groundHeightAtCamera = ground;
+    const float size = (float)(root_size / 2.0);
+    TerrainQuad root(&node, NULL, 0, 0, -size, -size, 2.0 * size, 0.0f, 0.0f);
+    root.update();
+    std::map<std::tuple<double, double, double>, const TerrainQuad *> quads;
+    collect(&root, quads);
+    int n = 0;
+    for (const auto &v : node.visits) {
+        const TerrainQuad *q = quads.at(v);
+        if (n < capacity) {
+            out[3 * n] = q->level;
+            out[3 * n + 1] = q->tx;
+            out[3 * n + 2] = q->ty;
+        }
+        ++n;
+    }
+    return n;
+}
+"""
+
+
+def generate_quadtree(root):
+    """oracle/_ref/gen/ref_quadtree.cpp: TerrainQuad's update / subdivide and
+    TerrainNode's distance functions as written."""
+    quad = _read(root, QUAD_CPP)
+    node = _read(root, NODE_CPP)
+    src = ["// generated by oracle/ref_build.py from the reference's sources\n", _QUAD_PRELUDE]
+    for text, rel, sigs in ((quad, QUAD_CPP, [r"^TerrainQuad::TerrainQuad\(", r"bool TerrainQuad::isLeaf\(",
+                                              r"void TerrainQuad::update\(", r"void TerrainQuad::subdivide\("]),
+                            (node, NODE_CPP, [r"float TerrainNode::getCameraDist\(",
+                                              r"float TerrainNode::getSplitDistance\(",
+                                              r"vec3d TerrainNode::getLocalCamera\("])):
+        for sig in sigs:
+            body, line = extract_function(text, sig)
+            src.append("// %s:%d\n%s" % (rel, line, body))
+    src.append(_QUAD_DRIVER)
+    os.makedirs(GEN_DIR, exist_ok=True)
+    path = os.path.join(GEN_DIR, "ref_quadtree.cpp")
+    with open(path, "w") as f:
+        f.write("".join(src))
+    return path
+
+
 def _load_sibling(name):
     """oracle/<name>.py by path (this file also runs as a script and is loaded by path)."""
     import importlib.util
@@ -1470,7 +1625,7 @@ def build(root=DEFAULT_ROOT, force=False):
         return LIB if os.path.exists(LIB) else None
     srcs = [os.path.join(root, p) for p in (NOISE_CPP, ELEV_CPP, CPU_ELEV_CPP, MIPMAP_CPP, NORMAL_CPP, ORTHO_CPP,
                                             GRAPH_LAYER_CPP, ROAD_LAYER_CPP, GRAPH_PRODUCER_CPP, RESIDUAL_CPP,
-                                            ORTHO_CPU_CPP, MFS_CPP, CACHE_CPP, STORAGE_CPP)]
+                                            ORTHO_CPU_CPP, MFS_CPP, CACHE_CPP, STORAGE_CPP, QUAD_CPP, NODE_CPP)]
     srcs += [os.path.join(root, rel) for _, rel, _ in UPSAMPLE_SHADERS + NORMAL_SHADERS + BLEND_SHADERS +
              LAYER_SHADERS + ORTHO_SHADERS]
     srcs += [os.path.abspath(__file__), os.path.join(HERE, "ref_glsl.py")]
@@ -1481,12 +1636,13 @@ def build(root=DEFAULT_ROOT, force=False):
     gen_gpu = generate_gpu(root)
     gen_res = generate_residual(root)
     gen_cache = generate_cache(root)
+    gen_quad = generate_quadtree(root)
     tmp = LIB + ".tmp%d" % os.getpid()
     inc = ["-I", os.path.join(HERE, "ref_stubs"), "-I", os.path.join(root, NOISE_DIR),
            "-I", os.path.join(root, "src/core/sources/proland/math")]
     flags = ["-O2", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-w", "-DPROLAND_API="]
     objs = []
-    for unit, std in ((gen, "c++14"), (gen_gpu, "c++17"), (gen_res, "c++17"), (gen_cache, "c++17"),
+    for unit, std in ((gen, "c++14"), (gen_gpu, "c++17"), (gen_res, "c++17"), (gen_cache, "c++17"), (gen_quad, "c++17"),
                       (os.path.join(root, NOISE_CPP), "c++14"),
                       (os.path.join(root, MFS_CPP), "c++14")):
         obj = os.path.join(GEN_DIR, os.path.basename(unit) + ".o")
