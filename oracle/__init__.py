@@ -668,6 +668,9 @@ def ref_lib():
         L.ref_cache_counts.argtypes = [C.POINTER(C.c_int)] * 3
         L.ref_quadtree.argtypes = [C.c_double, C.c_int, C.c_float, C.c_float, C.c_double, C.c_double, C.c_double,
                                    C.c_float, C.c_void_p, C.c_int]
+        L.ref_sampler_create.argtypes = [C.c_double, C.c_int, C.c_float, C.c_int]
+        L.ref_sampler_frame.argtypes = [C.c_double] * 3 + [C.c_void_p]
+        L.ref_sampler_users.argtypes = [C.c_int] * 3
         L.ref_road_meshes.argtypes = [C.c_double] * 3 + [C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_int,
                                                          C.c_float, C.c_int, C.c_int, C.POINTER(C.c_float)]
         L.ref_curve_altitude.argtypes = [C.c_double] * 3 + [C.c_void_p, C.c_void_p, C.c_int, C.c_float, C.c_float,

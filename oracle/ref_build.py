@@ -52,6 +52,9 @@ The GPU path, in a second unit (``ref_gpu.cpp``):
 * in a fifth unit, ``TerrainQuad``'s ``update`` / ``subdivide`` and ``TerrainNode``'s
   ``getCameraDist`` (``core/sources/proland/terrain/``) as written, for the view-driven
   requests;
+* in a sixth unit, ``TileSampler``'s ``update``, ``prefetch``, ``putTiles``, ``getTiles`` and
+  ``needTile`` with ``TileProducer``'s cache calls, over the quadtree and cache functions
+  above, for a frame-by-frame comparison with the product's sampler;
 * the shaders those functions draw -- the upsample shaders of terrain1, terrain2,
   terrain4 (flipped diagonals) and the demo (modulated noise, with and without
   ``NO_CLAMP``), the normal shaders of terrain1, terrain2 (sphere) and the demo
@@ -1107,42 +1110,27 @@ def generate_residual(root):
 CACHE_CPP = "src/core/sources/proland/producer/TileCache.cpp"
 STORAGE_CPP = "src/core/sources/proland/producer/TileStorage.cpp"
 
-_CACHE_PRELUDE = r"""
-#include <pthread.h>
-#include <cassert>
-#include <cstdarg>
-#include <list>
-#include <map>
-#include <string>
-#include <utility>
-#include <vector>
-#include "ork_gl.h"
+STORAGE_SIGS = [r"^TileStorage::Slot::Slot\(", r"^TileStorage::Slot::~Slot\(",
+                r"TileStorage \*TileStorage::Slot::getOwner\(", r"void TileStorage::Slot::lock\(",
+                r"^TileStorage::TileStorage\(\)", r"void TileStorage::init\(", r"^TileStorage::~TileStorage\(",
+                r"TileStorage::Slot \*TileStorage::newSlot\(", r"void TileStorage::deleteSlot\(",
+                r"int TileStorage::getTileSize\(", r"int TileStorage::getCapacity\(",
+                r"int TileStorage::getFreeSlots\("]
+CACHE_SIGS = [r"^TileCache::Tile::Tile\(", r"^TileCache::Tile::~Tile\(",
+              r"TileStorage::Slot \*TileCache::Tile::getData\(",
+              r"TileCache::Tile::Id TileCache::Tile::getId\(\) const",
+              r"TileCache::Tile::TId TileCache::Tile::getTId\(\) const",
+              r"TileCache::Tile::Id TileCache::Tile::getId\(int", r"TileCache::Tile::TId TileCache::Tile::getTId\(int",
+              r"^TileCache::TileCache\(\)", r"void TileCache::init\(", r"^TileCache::~TileCache\(",
+              r"ptr<TileStorage> TileCache::getStorage\(", r"ptr<Scheduler> TileCache::getScheduler\(",
+              r"int TileCache::getUsedTiles\(",
+              r"int TileCache::getUnusedTiles\(", r"TileCache::Tile\* TileCache::findTile\(",
+              r"TileCache::Tile\* TileCache::getTile\(", r"ptr<Task> TileCache::prefetchTile\(",
+              r"int TileCache::putTile\(", r"void TileCache::invalidateTiles\(",
+              r"void TileCache::invalidateTile\(", r"void TileCache::createTileTaskDeleted\("]
 
-namespace refcache {
-using namespace std;   // as TileCache.cpp and TileStorage.cpp
-using refgl::ptr;
-
-// Ork stand-ins: Object, the debug logger, tasks with a done flag, a scheduler.
-struct Object {
-    explicit Object(const char *) {}
-    virtual ~Object() {}
-};
-struct Logger {
-    static Logger *DEBUG_LOGGER;
-    void logf(const char *, const char *, ...) {}
-};
-Logger *Logger::DEBUG_LOGGER = nullptr;
-struct Task {
-    enum reason { DATA_NEEDED, DATA_CHANGED };
-    bool done = false;
-    bool isDone() { return done; }
-    void setIsDone(bool d, unsigned int, reason) { done = d; }
-};
-struct Scheduler {
-    void reschedule(ptr<Task> t, Task::reason r, unsigned int) { t->setIsDone(false, 0, r); }
-};
-
-// The declarations of TileStorage.h and TileCache.h the extracted functions define.
+_DECL_STORAGE = r"""
+// The declaration of TileStorage.h the extracted functions define.
 struct TileStorage : Object {
     struct Slot {
         std::pair<int, std::pair<int, std::pair<int, int> > > id;
@@ -1169,21 +1157,10 @@ struct TileStorage : Object {
     std::list<Slot *> freeSlots;
 };
 
-// a producer whose createTile returns the task to reuse, or a new one not done
-struct TileProducer {
-    std::vector<Task *> tasks;
-    ~TileProducer()
-    {
-        for (Task *t : tasks) delete t;
-    }
-    ptr<Task> createTile(int, int, int, TileStorage::Slot *, unsigned int, ptr<Task> task)
-    {
-        if (task.p) return task;
-        tasks.push_back(new Task());
-        return ptr<Task>(tasks.back());
-    }
-};
+"""
 
+_DECL_CACHE = r"""
+// The declaration of TileCache.h the extracted functions define.
 struct TileCache : Object {
     class Tile {
     public:
@@ -1234,6 +1211,59 @@ struct TileCache : Object {
     void *mutex;
 };
 """
+
+_CACHE_PRELUDE = r"""
+#include <pthread.h>
+#include <cassert>
+#include <cstdarg>
+#include <list>
+#include <map>
+#include <string>
+#include <utility>
+#include <vector>
+#include "ork_gl.h"
+
+namespace refcache {
+using namespace std;   // as TileCache.cpp and TileStorage.cpp
+using refgl::ptr;
+
+// Ork stand-ins: Object, the debug logger, tasks with a done flag, a scheduler.
+struct Object {
+    explicit Object(const char *) {}
+    virtual ~Object() {}
+};
+struct Logger {
+    static Logger *DEBUG_LOGGER;
+    void logf(const char *, const char *, ...) {}
+};
+Logger *Logger::DEBUG_LOGGER = nullptr;
+struct Task {
+    enum reason { DATA_NEEDED, DATA_CHANGED };
+    bool done = false;
+    bool isDone() { return done; }
+    void setIsDone(bool d, unsigned int, reason) { done = d; }
+};
+struct Scheduler {
+    void reschedule(ptr<Task> t, Task::reason r, unsigned int) { t->setIsDone(false, 0, r); }
+};
+
+""" + _DECL_STORAGE + r"""
+// a producer whose createTile returns the task to reuse, or a new one not done
+struct TileProducer {
+    std::vector<Task *> tasks;
+    ~TileProducer()
+    {
+        for (Task *t : tasks) delete t;
+    }
+    ptr<Task> createTile(int, int, int, TileStorage::Slot *, unsigned int, ptr<Task> task)
+    {
+        if (task.p) return task;
+        tasks.push_back(new Task());
+        return ptr<Task>(tasks.back());
+    }
+};
+
+""" + _DECL_CACHE
 
 _CACHE_DRIVER = r"""
 }  // namespace refcache
@@ -1338,24 +1368,7 @@ def generate_cache(root):
     cache = _read(root, CACHE_CPP)
     storage = _read(root, STORAGE_CPP)
     src = ["// generated by oracle/ref_build.py from the reference's sources\n", _CACHE_PRELUDE]
-    storage_sigs = [r"^TileStorage::Slot::Slot\(", r"^TileStorage::Slot::~Slot\(",
-                    r"TileStorage \*TileStorage::Slot::getOwner\(", r"void TileStorage::Slot::lock\(",
-                    r"^TileStorage::TileStorage\(\)", r"void TileStorage::init\(", r"^TileStorage::~TileStorage\(",
-                    r"TileStorage::Slot \*TileStorage::newSlot\(", r"void TileStorage::deleteSlot\(",
-                    r"int TileStorage::getTileSize\(", r"int TileStorage::getCapacity\(",
-                    r"int TileStorage::getFreeSlots\("]
-    cache_sigs = [r"^TileCache::Tile::Tile\(", r"^TileCache::Tile::~Tile\(",
-                  r"TileStorage::Slot \*TileCache::Tile::getData\(",
-                  r"TileCache::Tile::Id TileCache::Tile::getId\(\) const",
-                  r"TileCache::Tile::TId TileCache::Tile::getTId\(\) const",
-                  r"TileCache::Tile::Id TileCache::Tile::getId\(int", r"TileCache::Tile::TId TileCache::Tile::getTId\(int",
-                  r"^TileCache::TileCache\(\)", r"void TileCache::init\(", r"^TileCache::~TileCache\(",
-                  r"ptr<TileStorage> TileCache::getStorage\(", r"int TileCache::getUsedTiles\(",
-                  r"int TileCache::getUnusedTiles\(", r"TileCache::Tile\* TileCache::findTile\(",
-                  r"TileCache::Tile\* TileCache::getTile\(", r"ptr<Task> TileCache::prefetchTile\(",
-                  r"int TileCache::putTile\(", r"void TileCache::invalidateTiles\(",
-                  r"void TileCache::invalidateTile\(", r"void TileCache::createTileTaskDeleted\("]
-    for text, rel, sigs in ((storage, STORAGE_CPP, storage_sigs), (cache, CACHE_CPP, cache_sigs)):
+    for text, rel, sigs in ((storage, STORAGE_CPP, STORAGE_SIGS), (cache, CACHE_CPP, CACHE_SIGS)):
         for sig in sigs:
             body, line = extract_function(text, sig)
             src.append("// %s:%d\n%s" % (rel, line, body))
@@ -1370,43 +1383,12 @@ def generate_cache(root):
 QUAD_CPP = "src/core/sources/proland/terrain/TerrainQuad.cpp"
 NODE_CPP = "src/core/sources/proland/terrain/TerrainNode.cpp"
 
-_QUAD_PRELUDE = r"""
-#include <algorithm>
-#include <cassert>
-#include <cmath>
-#include <map>
-#include <memory>
-#include <tuple>
-#include <vector>
+QUAD_SIGS = [r"^TerrainQuad::TerrainQuad\(", r"bool TerrainQuad::isLeaf\(", r"void TerrainQuad::update\(",
+             r"void TerrainQuad::subdivide\("]
+NODE_SIGS = [r"float TerrainNode::getCameraDist\(", r"float TerrainNode::getSplitDistance\(",
+             r"vec3d TerrainNode::getLocalCamera\("]
 
-namespace refquad {
-using namespace std;   // as TerrainQuad.cpp and TerrainNode.cpp
-
-// an owning pointer in the place of Ork's reference-counted ptr
-template <class T> struct ptr {
-    std::shared_ptr<T> s;
-    ptr() {}
-    ptr(T *q) : s(q) {}
-    T *operator->() const { return s.get(); }
-    bool operator==(const T *q) const { return s.get() == q; }
-};
-struct Object {
-    explicit Object(const char *) {}
-    virtual ~Object() {}
-};
-inline bool isFinite(float x) { return std::isfinite(x); }
-struct vec3d {
-    double x, y, z;
-};
-struct box3d {
-    double xmin, xmax, ymin, ymax, zmin, zmax;
-    box3d(double a, double b, double c, double d, double e, double f)
-        : xmin(a), xmax(b), ymin(c), ymax(d), zmin(e), zmax(f) {}
-};
-struct SceneManager {
-    enum visibility { FULLY_VISIBLE, PARTIALLY_VISIBLE, INVISIBLE };
-};
-
+_DECL_QUAD = r"""
 // The TerrainNode members TerrainQuad::update calls: every quad partially visible
 // (the test has no view frustum), nothing occluded; getVisibility records the boxes
 // in the order update meets them.
@@ -1451,8 +1433,50 @@ struct TerrainQuad : Object {
     void update();
     TerrainNode *owner;
     void subdivide();
+    TerrainNode *getOwner();
+    int getDepth() const;
 };
 """
+
+_QUAD_PRELUDE = r"""
+#include <algorithm>
+#include <cassert>
+#include <cmath>
+#include <map>
+#include <memory>
+#include <tuple>
+#include <vector>
+
+namespace refquad {
+using namespace std;   // as TerrainQuad.cpp and TerrainNode.cpp
+
+// an owning pointer in the place of Ork's reference-counted ptr
+template <class T> struct ptr {
+    std::shared_ptr<T> s;
+    ptr() {}
+    ptr(T *q) : s(q) {}
+    T *operator->() const { return s.get(); }
+    bool operator==(const T *q) const { return s.get() == q; }
+    bool operator!=(const T *q) const { return s.get() != q; }
+};
+struct Object {
+    explicit Object(const char *) {}
+    virtual ~Object() {}
+};
+inline bool isFinite(float x) { return std::isfinite(x); }
+struct vec3d {
+    double x, y, z;
+};
+struct box3d {
+    double xmin, xmax, ymin, ymax, zmin, zmax;
+    box3d(double a, double b, double c, double d, double e, double f)
+        : xmin(a), xmax(b), ymin(c), ymax(d), zmin(e), zmax(f) {}
+};
+struct SceneManager {
+    enum visibility { FULLY_VISIBLE, PARTIALLY_VISIBLE, INVISIBLE };
+};
+
+""" + _DECL_QUAD
 
 _QUAD_DRIVER = r"""
 void collect(const TerrainQuad *q, std::map<std::tuple<double, double, double>, const TerrainQuad *> &m)
@@ -1503,17 +1527,296 @@ def generate_quadtree(root):
     quad = _read(root, QUAD_CPP)
     node = _read(root, NODE_CPP)
     src = ["// generated by oracle/ref_build.py from the reference's sources\n", _QUAD_PRELUDE]
-    for text, rel, sigs in ((quad, QUAD_CPP, [r"^TerrainQuad::TerrainQuad\(", r"bool TerrainQuad::isLeaf\(",
-                                              r"void TerrainQuad::update\(", r"void TerrainQuad::subdivide\("]),
-                            (node, NODE_CPP, [r"float TerrainNode::getCameraDist\(",
-                                              r"float TerrainNode::getSplitDistance\(",
-                                              r"vec3d TerrainNode::getLocalCamera\("])):
+    for text, rel, sigs in ((quad, QUAD_CPP, QUAD_SIGS), (node, NODE_CPP, NODE_SIGS)):
         for sig in sigs:
             body, line = extract_function(text, sig)
             src.append("// %s:%d\n%s" % (rel, line, body))
     src.append(_QUAD_DRIVER)
     os.makedirs(GEN_DIR, exist_ok=True)
     path = os.path.join(GEN_DIR, "ref_quadtree.cpp")
+    with open(path, "w") as f:
+        f.write("".join(src))
+    return path
+
+
+PRODUCER_CPP = "src/core/sources/proland/producer/TileProducer.cpp"
+SAMPLER_CPP = "src/core/sources/proland/terrain/TileSampler.cpp"
+PRODUCER_SIGS = [r"float TileProducer::getRootQuadSize\(", r"void TileProducer::setRootQuadSize\(",
+                 r"int TileProducer::getId\(", r"ptr<TileCache> TileProducer::getCache\(",
+                 r"bool TileProducer::isGpuProducer\(", r"int TileProducer::getBorder\(",
+                 r"bool TileProducer::hasTile\(", r"bool TileProducer::hasChildren\(",
+                 r"TileCache::Tile\* TileProducer::findTile\(", r"TileCache::Tile\* TileProducer::getTile\(",
+                 r"bool TileProducer::prefetchTile\(", r"void TileProducer::putTile\(",
+                 r"void TileProducer::update\(ptr<SceneManager>"]
+SAMPLER_SIGS = [r"void TileSampler::init\(", r"ptr<Task> TileSampler::update\(", r"^TileSampler::Tree::Tree\(",
+                r"^TileSampler::Tree::~Tree\(", r"void TileSampler::Tree::recursiveDelete\(",
+                r"bool TileSampler::needTile\(", r"void TileSampler::putTiles\(", r"void TileSampler::getTiles\(",
+                r"void TileSampler::prefetch\("]
+
+_SAMPLER_PRELUDE = r"""
+#include <pthread.h>
+#include <algorithm>
+#include <cassert>
+#include <cmath>
+#include <list>
+#include <map>
+#include <memory>
+#include <string>
+#include <tuple>
+#include <type_traits>
+#include <utility>
+#include <vector>
+
+namespace refsampler {
+using namespace std;   // as the extracted files
+
+struct TerrainQuad;
+// Ork's ptr: owning for terrain quads (their children are dropped by assignment),
+// a plain reference to objects the harness owns otherwise.
+template <class T> struct ptr {
+    std::shared_ptr<T> s;
+    ptr() {}
+    ptr(T *q) : s(q, [](T *x) { if (std::is_same<T, TerrainQuad>::value) delete x; }) {}
+    template <class U> ptr(const ptr<U> &o) : s(o.s, o.s.get()) {}
+    T *operator->() const { return s.get(); }
+    T *get() const { return s.get(); }
+    template <class U> ptr<U> cast() const
+    {
+        ptr<U> r;
+        r.s = std::shared_ptr<U>(s, dynamic_cast<U *>(s.get()));
+        return r;
+    }
+    bool operator==(const T *q) const { return s.get() == q; }
+    bool operator!=(const T *q) const { return s.get() != q; }
+};
+
+struct Object {
+    explicit Object(const char *) {}
+    virtual ~Object() {}
+};
+struct Logger {
+    static Logger *DEBUG_LOGGER, *ERROR_LOGGER;
+    void log(const string &, const string &) {}
+    void logf(const char *, const char *, ...) {}
+};
+Logger *Logger::DEBUG_LOGGER = nullptr;
+Logger *Logger::ERROR_LOGGER = nullptr;
+inline bool isFinite(float x) { return std::isfinite(x); }
+struct vec2f {
+    float x, y;
+    vec2f(float a, float b) : x(a), y(b) {}
+};
+struct vec3d {
+    double x, y, z;
+};
+struct box3d {
+    double xmin, xmax, ymin, ymax, zmin, zmax;
+    box3d(double a, double b, double c, double d, double e, double f)
+        : xmin(a), xmax(b), ymin(c), ymax(d), zmin(e), zmax(f) {}
+};
+struct SceneManager {
+    enum visibility { FULLY_VISIBLE, PARTIALLY_VISIBLE, INVISIBLE };
+};
+struct Task {
+    enum reason { DATA_NEEDED, DATA_CHANGED };
+    bool done = false;
+    Task() {}
+    Task(const char *, bool, int) {}
+    virtual ~Task() {}
+    bool isDone() { return done; }
+    void setIsDone(bool d, unsigned int, reason) { done = d; }
+    virtual bool run() { return true; }
+};
+struct TaskGraph : Task {
+    std::vector<Task *> tasks;
+    void addTask(ptr<Task> t) { tasks.push_back(t.get()); }
+    void addDependency(ptr<Task>, ptr<Task>) {}
+    bool isEmpty() { return tasks.empty(); }
+};
+// the cache has no scheduler: prefetchTile creates nothing (a scheduler that does not
+// prefetch for the producer)
+struct Scheduler {
+    bool supportsPrefetch(bool) { return false; }
+    void schedule(ptr<Task>) {}
+    void reschedule(ptr<Task> t, Task::reason r, unsigned int) { t->setIsDone(false, 0, r); }
+};
+"""
+
+_SAMPLER_CLASSES = r"""
+struct GPUTileStorage : TileStorage {
+    void *getTileMap() { return nullptr; }   // no tile map: update's tile-map task never runs
+};
+
+struct TileLayer {
+    void useTile(int, int, int, unsigned int) {}
+    void unuseTile(int, int, int) {}
+    void prefetchTile(int, int, int) {}
+    void setCache(ptr<TileCache>, int) {}
+    void setTileSize(int, int, float) {}
+};
+
+// The TileProducer members the extracted functions use (TileProducer.h); createTile
+// hands out a task, not done, or the one to reuse.
+struct TileProducer {
+    ptr<TileCache> cache;
+    int id = 0;
+    float rootQuadSize = 0.0f;
+    bool gpuProducer = true;
+    std::vector<ptr<TileLayer> > layers;
+    std::vector<Task *> tasks;
+    virtual ~TileProducer()
+    {
+        for (Task *t : tasks) delete t;
+    }
+    float getRootQuadSize();
+    void setRootQuadSize(float size);
+    int getId();
+    ptr<TileCache> getCache();
+    bool isGpuProducer();
+    virtual int getBorder();
+    virtual bool hasTile(int level, int tx, int ty);
+    virtual bool hasChildren(int level, int tx, int ty);
+    TileCache::Tile *findTile(int level, int tx, int ty, bool includeCache = false, bool done = false);
+    TileCache::Tile *getTile(int level, int tx, int ty, unsigned int deadline);
+    bool prefetchTile(int level, int tx, int ty);
+    void putTile(TileCache::Tile *t);
+    virtual void update(ptr<SceneManager> scene);
+    bool updateTileMap(float, vec2f, int) { return false; }
+    ptr<Task> createTile(int, int, int, TileStorage::Slot *, unsigned int, ptr<Task> task)
+    {
+        if (task.get()) return task;
+        tasks.push_back(new Task());
+        return ptr<Task>(tasks.back());
+    }
+};
+
+struct TileFilter {
+    virtual ~TileFilter() {}
+    virtual bool storeTile(ptr<TerrainQuad> q) = 0;
+};
+
+// The declaration of TileSampler.h the extracted functions define.
+struct TileSampler : Object {
+    class Tree {
+    public:
+        bool newTree;
+        bool needTile;
+        Tree *parent;
+        TileCache::Tile *t;
+        Tree *children[4];
+        Tree(Tree *parent);
+        virtual ~Tree();
+        virtual void recursiveDelete(TileSampler *owner);
+    };
+    TileSampler() : Object("TileSampler") {}
+    void init(const string &name, ptr<TileProducer> producer);
+    ptr<Task> update(ptr<SceneManager> scene, ptr<TerrainQuad> root);
+    bool needTile(ptr<TerrainQuad> q);
+    void putTiles(Tree **t, ptr<TerrainQuad> q);
+    void getTiles(Tree *parent, Tree **t, ptr<TerrainQuad> q, ptr<TaskGraph> result);
+    void prefetch(Tree *t, ptr<TerrainQuad> q, int &prefetchCount);
+    string name;
+    ptr<TileProducer> producer;
+    std::vector<ptr<TerrainNode> > terrains;
+    bool storeLeaf, storeParent, storeInvisible, async, mipmap;
+    std::vector<TileFilter *> storeFilters;
+    Tree *root;
+    void *lastProgram;
+};
+"""
+
+_SAMPLER_DRIVER = r"""
+namespace {
+struct SamplerHarness {
+    GPUTileStorage storage;
+    TileCache cache;
+    TileProducer producer;
+    TerrainNode node;
+    TerrainQuad *root = nullptr;
+    TileSampler sampler;
+    ~SamplerHarness()
+    {
+        if (sampler.root) sampler.root->recursiveDelete(&sampler);
+        sampler.root = nullptr;
+        delete root;
+    }
+};
+SamplerHarness *g_sampler = nullptr;
+}  // namespace
+}  // namespace refsampler
+
+// A terrain (root quad of size root_size, as TerrainNode::init makes it), one producer on
+// a cache of `capacity` slots and a TileSampler with the reference's defaults.
+extern "C" void ref_sampler_create(double root_size, int max_level, float split_dist, int capacity)
+{
+    using namespace refsampler;
+    delete g_sampler;
+    g_sampler = new SamplerHarness();
+    SamplerHarness &h = *g_sampler;
+    h.storage.init(1, capacity);
+    for (int k = 0; k < capacity; ++k) {
+        TileStorage::Slot *s = new TileStorage::Slot(&h.storage);
+        s->index = k;
+        h.storage.freeSlots.push_back(s);
+    }
+    h.cache.init(&h.storage, "tiles");
+    h.producer.cache = &h.cache;
+    h.producer.id = h.cache.nextProducerId++;
+    h.cache.producers[h.producer.id] = &h.producer;
+    h.node.maxLevel = max_level;
+    h.node.splitDist = split_dist;
+    const float size = (float)(root_size / 2.0);
+    h.root = new TerrainQuad(&h.node, NULL, 0, 0, -size, -size, 2.0 * size, 0.0f, 0.0f);
+    h.sampler.init("elevation", &h.producer);
+}
+
+// One frame: the camera moves, the quadtree updates, TileSampler::update acquires and
+// releases.  out: used tiles, unused tiles, free slots, the cache's queries and misses.
+extern "C" void ref_sampler_frame(double cx, double cy, double cz, int *out5)
+{
+    using namespace refsampler;
+    SamplerHarness &h = *g_sampler;
+    h.node.localCameraPos = vec3d{cx, cy, cz};
+    h.node.visits.clear();
+    h.root->update();
+    ptr<TerrainQuad> root;
+    root.s = std::shared_ptr<TerrainQuad>(h.root, [](TerrainQuad *) {});   // the harness owns the root
+    h.sampler.update(ptr<SceneManager>(), root);
+    out5[0] = h.cache.getUsedTiles();
+    out5[1] = h.cache.getUnusedTiles();
+    out5[2] = h.storage.getFreeSlots();
+    out5[3] = h.cache.queries;
+    out5[4] = h.cache.misses;
+}
+
+// users of tile (level, tx, ty) in the cache (0: cached unused, -1: absent)
+extern "C" int ref_sampler_users(int level, int tx, int ty)
+{
+    using namespace refsampler;
+    TileCache::Tile *t = g_sampler->cache.findTile(0, level, tx, ty, true);
+    return t ? t->users : -1;
+}
+"""
+
+
+def generate_sampler(root):
+    """oracle/_ref/gen/ref_sampler.cpp: the terrain quadtree, the tile cache, the
+    producer's cache calls and TileSampler's update as written, in one namespace."""
+    texts = {rel: _read(root, rel) for rel in (STORAGE_CPP, CACHE_CPP, QUAD_CPP, NODE_CPP, PRODUCER_CPP,
+                                               SAMPLER_CPP)}
+    src = ["// generated by oracle/ref_build.py from the reference's sources\n", _SAMPLER_PRELUDE, _DECL_STORAGE,
+           "struct TileProducer;\n", _DECL_CACHE, _DECL_QUAD, _SAMPLER_CLASSES]
+    cls, line = extract_block(texts[SAMPLER_CPP], "class UpdateTileMapTask : public Task", "};")
+    src.append("// %s:%d\n%s" % (SAMPLER_CPP, line, cls))
+    extra = [(QUAD_CPP, [r"TerrainNode \*TerrainQuad::getOwner\(", r"int TerrainQuad::getDepth\("])]
+    for rel, sigs in [(STORAGE_CPP, STORAGE_SIGS), (CACHE_CPP, CACHE_SIGS), (QUAD_CPP, QUAD_SIGS),
+                      (NODE_CPP, NODE_SIGS), (PRODUCER_CPP, PRODUCER_SIGS), (SAMPLER_CPP, SAMPLER_SIGS)] + extra:
+        for sig in sigs:
+            body, line = extract_function(texts[rel], sig)
+            src.append("// %s:%d\n%s" % (rel, line, body))
+    src.append(_SAMPLER_DRIVER)
+    os.makedirs(GEN_DIR, exist_ok=True)
+    path = os.path.join(GEN_DIR, "ref_sampler.cpp")
     with open(path, "w") as f:
         f.write("".join(src))
     return path
@@ -1625,7 +1928,8 @@ def build(root=DEFAULT_ROOT, force=False):
         return LIB if os.path.exists(LIB) else None
     srcs = [os.path.join(root, p) for p in (NOISE_CPP, ELEV_CPP, CPU_ELEV_CPP, MIPMAP_CPP, NORMAL_CPP, ORTHO_CPP,
                                             GRAPH_LAYER_CPP, ROAD_LAYER_CPP, GRAPH_PRODUCER_CPP, RESIDUAL_CPP,
-                                            ORTHO_CPU_CPP, MFS_CPP, CACHE_CPP, STORAGE_CPP, QUAD_CPP, NODE_CPP)]
+                                            ORTHO_CPU_CPP, MFS_CPP, CACHE_CPP, STORAGE_CPP, QUAD_CPP, NODE_CPP,
+                                            PRODUCER_CPP, SAMPLER_CPP)]
     srcs += [os.path.join(root, rel) for _, rel, _ in UPSAMPLE_SHADERS + NORMAL_SHADERS + BLEND_SHADERS +
              LAYER_SHADERS + ORTHO_SHADERS]
     srcs += [os.path.abspath(__file__), os.path.join(HERE, "ref_glsl.py")]
@@ -1637,12 +1941,14 @@ def build(root=DEFAULT_ROOT, force=False):
     gen_res = generate_residual(root)
     gen_cache = generate_cache(root)
     gen_quad = generate_quadtree(root)
+    gen_sampler = generate_sampler(root)
     tmp = LIB + ".tmp%d" % os.getpid()
     inc = ["-I", os.path.join(HERE, "ref_stubs"), "-I", os.path.join(root, NOISE_DIR),
            "-I", os.path.join(root, "src/core/sources/proland/math")]
     flags = ["-O2", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-w", "-DPROLAND_API="]
     objs = []
     for unit, std in ((gen, "c++14"), (gen_gpu, "c++17"), (gen_res, "c++17"), (gen_cache, "c++17"), (gen_quad, "c++17"),
+                      (gen_sampler, "c++17"),
                       (os.path.join(root, NOISE_CPP), "c++14"),
                       (os.path.join(root, MFS_CPP), "c++14")):
         obj = os.path.join(GEN_DIR, os.path.basename(unit) + ".o")

@@ -1573,6 +1573,32 @@ uint64_t req_key(int level, int tx, int ty)
     return ((uint64_t)level << 58) | ((uint64_t)(uint32_t)tx << 29) | (uint64_t)(uint32_t)ty;
 }
 
+// The place of a quad in the walk TileSampler::putTiles / getTiles make over a quadtree
+// (TileSampler.cpp:385-461): the root, then each child's subtree in index order
+// (tx & 1) + 2 (ty & 1), a parent before its children.  Sorting by this key orders
+// releases and acquisitions as the reference does, so that its caches' LRU lists
+// receive the tiles in the same order and evict the same tiles.
+// The key: the child indices from the root, 2 bits per level left-aligned (the bits of
+// tx and ty interleaved, tx in the low bit of each pair), then the level.
+uint64_t spread_bits(uint32_t v)   // bit i of v -> bit 2i
+{
+    uint64_t x = v;
+    x = (x | (x << 16)) & 0x0000FFFF0000FFFFull;
+    x = (x | (x << 8)) & 0x00FF00FF00FF00FFull;
+    x = (x | (x << 4)) & 0x0F0F0F0F0F0F0F0Full;
+    x = (x | (x << 2)) & 0x3333333333333333ull;
+    x = (x | (x << 1)) & 0x5555555555555555ull;
+    return x;
+}
+
+uint64_t walk_order(uint64_t key)
+{
+    const int level = (int)(key >> 58);
+    const uint32_t tx = (uint32_t)(key >> 29) & 0x1FFFFFFFu, ty = (uint32_t)key & 0x1FFFFFFFu;
+    const uint64_t path = (spread_bits(tx) | (spread_bits(ty) << 1)) << (2 * (29 - level));
+    return (path << 5) | (uint64_t)level;
+}
+
 void sampler_drop(tp_sampler *s, size_t pos, bool cancel)
 {
     tp_sampler::Quad &q = s->held[pos];
@@ -1623,23 +1649,33 @@ extern "C" int tp_sampler_update(tp_sampler *s, const tp_tile_req *reqs, int n, 
     std::vector<int> fresh_idx;
     {
         // quads kept: stamped; quads that disappeared: their tiles go back to the caches
-        // first, so that their slots can take the new tiles
+        // first, so that their slots can take the new tiles, in the walk order of
+        // TileSampler::putTiles
         tp::TraceScope ts("sampler release", tp::kPhSamplerRelease);
         for (int i = 0; i < n; ++i) {
             const uint32_t *at = s->index.find(req_key(reqs[i].level, reqs[i].tx, reqs[i].ty));
             if (at) s->held[*at].stamp = frame;
             else fresh_idx.push_back(i);
         }
-        for (size_t pos = s->held.size(); pos-- > 0;)
-            if (s->held[pos].stamp != frame) sampler_drop(s, pos, false);
+        std::vector<std::pair<uint64_t, uint64_t> > gone;   // (walk order, quad key)
+        for (const tp_sampler::Quad &q : s->held)
+            if (q.stamp != frame) gone.emplace_back(walk_order(q.key), q.key);
+        std::sort(gone.begin(), gone.end());
+        for (const auto &g : gone) sampler_drop(s, *s->index.find(g.second), false);
     }
+    // the new quads acquired in the same walk order (a request list lists children near
+    // to far); reported in request order
+    std::vector<std::pair<uint64_t, int> > walk;   // (walk order, request index)
+    walk.reserve(fresh_idx.size());
+    for (int i : fresh_idx) walk.emplace_back(walk_order(req_key(reqs[i].level, reqs[i].tx, reqs[i].ty)), i);
+    std::sort(walk.begin(), walk.end());
     s->fresh.clear();
     const size_t kept = s->held.size();
     int rc = TP_OK;
     {
         tp::TraceScope ts("sampler acquire", tp::kPhSamplerAcquire);
-        for (int i : fresh_idx) {
-            const tp_tile_req &r = reqs[i];
+        for (const auto &w : walk) {
+            const tp_tile_req &r = reqs[w.second];
             const uint64_t k = req_key(r.level, r.tx, r.ty);
             if (s->index.find(k)) continue;  // requested twice
             tp_sampler::Quad q;
@@ -1660,7 +1696,16 @@ extern "C" int tp_sampler_update(tp_sampler *s, const tp_tile_req *reqs, int n, 
             }
             s->index.insert(k, (uint32_t)s->held.size());
             s->held.push_back(q);
-            s->fresh.push_back(r);
+        }
+    }
+    if (rc == TP_OK) {
+        std::vector<char> reported(s->held.size() - kept, 0);   // each new quad once, in request order
+        for (int i : fresh_idx) {
+            const uint32_t *at = s->index.find(req_key(reqs[i].level, reqs[i].tx, reqs[i].ty));
+            if (at && *at >= kept && !reported[*at - kept]) {
+                reported[*at - kept] = 1;
+                s->fresh.push_back(reqs[i]);
+            }
         }
     }
     if (rc == TP_OK) rc = tp_scheduler_run(s->producers.data(), (int)np, stream);

@@ -55,3 +55,31 @@ def test_random_views(ref, product, seed):
         got = S.quadtree_requests(cam, root=root, max_level=max_level, split=split, dist_factor=dist_factor,
                                   ground=ground, capacity=1 << 18)
         assert got == want
+
+
+@pytest.mark.parametrize("capacity", [4500, 6000])
+def test_sampler_over_a_camera_path(ref, product, capacity):
+    """TileSampler::update as written (TileSampler.cpp: prefetch, putTiles, getTiles,
+    needTile, the Tree; with the reference's defaults, a producer whose scheduler does
+    not prefetch) over the reference's quadtree and TileCache, frame by frame along a
+    camera path, beside the product's sampler (tp_sampler_update) fed the product's
+    requests: after every frame the used and unused tile counts, the free slots and the
+    cache's query and miss counters are the same -- the sampler releases and acquires
+    tiles in the same walk order, so its cache evicts the same tiles once it is full of
+    used and cached tiles."""
+    from proland_gb300 import streaming as S
+    max_level = 10
+    ref.ref_sampler_create(S.ROOT_SIZE, max_level, S.SPLIT_DIST, capacity)
+    storage = product.TileStorage(101, 1, capacity, on_device=product.TileStorage.BOOKKEEPING)
+    cache = product.TileCache(storage, "residuals")
+    sampler = product.TileSampler(product.ResidualProducer(cache))
+    full = 0
+    for k, cam in enumerate(S.camera_path(frames=240)):
+        out = np.zeros(5, np.int32)
+        ref.ref_sampler_frame(cam[0], cam[1], cam[2], out.ctypes.data)
+        sampler.update(S.quadtree_requests(cam, max_level=max_level))
+        mine = (cache.get_used_tiles(), cache.get_unused_tiles(), storage.get_free_slots()) + cache.stats()
+        assert mine == tuple(int(v) for v in out), (k, mine, list(out))
+        full += int(out[2] == 0)
+    sampler.close()
+    assert full > 20      # the cache evicted for many frames
