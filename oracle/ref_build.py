@@ -1541,7 +1541,8 @@ def generate_quadtree(root):
 
 PRODUCER_CPP = "src/core/sources/proland/producer/TileProducer.cpp"
 SAMPLER_CPP = "src/core/sources/proland/terrain/TileSampler.cpp"
-PRODUCER_SIGS = [r"float TileProducer::getRootQuadSize\(", r"void TileProducer::setRootQuadSize\(",
+PRODUCER_SIGS = [r"ptr<Task> TileProducer::startCreateTile\(", r"void TileProducer::stopCreateTile\(",
+                 r"float TileProducer::getRootQuadSize\(", r"void TileProducer::setRootQuadSize\(",
                  r"int TileProducer::getId\(", r"ptr<TileCache> TileProducer::getCache\(",
                  r"bool TileProducer::isGpuProducer\(", r"int TileProducer::getBorder\(",
                  r"bool TileProducer::hasTile\(", r"bool TileProducer::hasChildren\(",
@@ -1651,6 +1652,8 @@ struct TileLayer {
     void useTile(int, int, int, unsigned int) {}
     void unuseTile(int, int, int) {}
     void prefetchTile(int, int, int) {}
+    void startCreateTile(int, int, int, unsigned int, ptr<Task>, ptr<TaskGraph>) {}
+    void stopCreateTile(int, int, int) {}
     void setCache(ptr<TileCache>, int) {}
     void setTileSize(int, int, float) {}
 };
@@ -1682,12 +1685,40 @@ struct TileProducer {
     void putTile(TileCache::Tile *t);
     virtual void update(ptr<SceneManager> scene);
     bool updateTileMap(float, vec2f, int) { return false; }
-    ptr<Task> createTile(int, int, int, TileStorage::Slot *, unsigned int, ptr<Task> task)
+    virtual ptr<Task> startCreateTile(int level, int tx, int ty, unsigned int deadline, ptr<Task> task,
+                                      ptr<TaskGraph> owner);
+    virtual void stopCreateTile(int level, int tx, int ty);
+    // a task graph holding the tile's task (TileProducer::createTaskGraph makes a
+    // CreateTileTaskGraph)
+    ptr<TaskGraph> createTaskGraph(ptr<Task> task)
+    {
+        TaskGraph *g = new TaskGraph();
+        tasks.push_back(g);
+        g->addTask(task);
+        return ptr<TaskGraph>(g);
+    }
+    // as TileProducer::createTile: a new task (or the one to reuse), made ready by
+    // startCreateTile, which acquires the tiles the tile is made from
+    ptr<Task> createTile(int level, int tx, int ty, TileStorage::Slot *, unsigned int deadline, ptr<Task> task)
     {
         if (task.get()) return task;
         tasks.push_back(new Task());
-        return ptr<Task>(tasks.back());
+        return startCreateTile(level, tx, ty, deadline, ptr<Task>(tasks.back()), ptr<TaskGraph>());
     }
+};
+
+// The members ElevationProducer's and NormalProducer's start / stopCreateTile use.
+struct ElevationProducer : TileProducer {
+    ptr<TileProducer> residualTiles;
+    ptr<Task> startCreateTile(int level, int tx, int ty, unsigned int deadline, ptr<Task> task,
+                              ptr<TaskGraph> owner) override;
+    void stopCreateTile(int level, int tx, int ty) override;
+};
+struct NormalProducer : TileProducer {
+    ptr<TileProducer> elevationTiles;
+    ptr<Task> startCreateTile(int level, int tx, int ty, unsigned int deadline, ptr<Task> task,
+                              ptr<TaskGraph> owner) override;
+    void stopCreateTile(int level, int tx, int ty) override;
 };
 
 struct TileFilter {
@@ -1789,6 +1820,78 @@ extern "C" void ref_sampler_frame(double cx, double cy, double cz, int *out5)
     out5[4] = h.cache.misses;
 }
 
+namespace refsampler {
+namespace {
+// residual, elevation and normal producers on caches of their own (ElevationProducer /
+// NormalProducer start and stop their tiles as written)
+struct DepsHarness {
+    GPUTileStorage storage[3];
+    TileCache cache[3];
+    TileProducer residuals;
+    ElevationProducer elevations;
+    NormalProducer normals;
+    TileProducer *producer(int k) { return k == 0 ? &residuals : k == 1 ? (TileProducer *)&elevations : &normals; }
+    ~DepsHarness()
+    {
+        // the caches' destructors expect every tile released
+        for (int k = 2; k >= 0; --k) {
+            std::vector<TileCache::Tile *> used;
+            for (auto &u : cache[k].usedTiles) used.push_back(u.second);
+            for (TileCache::Tile *t : used) {
+                t->users = 1;
+                cache[k].putTile(t);
+            }
+        }
+    }
+};
+DepsHarness *g_deps = nullptr;
+}  // namespace
+}  // namespace refsampler
+
+// tile widths: residuals rw, elevations w, normals w - 4; `capacity` slots each
+extern "C" void ref_deps_create(int w, int rw, int capacity)
+{
+    using namespace refsampler;
+    delete g_deps;
+    g_deps = new DepsHarness();
+    DepsHarness &h = *g_deps;
+    const int widths[3] = {rw, w, w - 4};
+    for (int k = 0; k < 3; ++k) {
+        h.storage[k].init(widths[k], capacity);
+        for (int s = 0; s < capacity; ++s) {
+            TileStorage::Slot *slot = new TileStorage::Slot(&h.storage[k]);
+            slot->index = s;
+            h.storage[k].freeSlots.push_back(slot);
+        }
+        h.cache[k].init(&h.storage[k], "cache");
+        TileProducer *p = h.producer(k);
+        p->cache = &h.cache[k];
+        p->id = h.cache[k].nextProducerId++;
+        h.cache[k].producers[p->id] = p;
+    }
+    h.elevations.residualTiles = &h.residuals;
+    h.normals.elevationTiles = &h.elevations;
+}
+
+// getTile on producer k (0 residuals, 1 elevations, 2 normals): 0, or -1 when the cache is full
+extern "C" int ref_deps_get(int k, int level, int tx, int ty)
+{
+    return refsampler::g_deps->producer(k)->getTile(level, tx, ty, 0) ? 0 : -1;
+}
+
+// users of tile (level, tx, ty) of producer k (0: cached unused, -1: absent)
+extern "C" int ref_deps_users(int k, int level, int tx, int ty)
+{
+    refsampler::TileCache::Tile *t = refsampler::g_deps->cache[k].findTile(0, level, tx, ty, true);
+    return t ? t->users : -1;
+}
+
+extern "C" void ref_deps_counts(int k, int *used, int *unused)
+{
+    *used = refsampler::g_deps->cache[k].getUsedTiles();
+    *unused = refsampler::g_deps->cache[k].getUnusedTiles();
+}
+
 // users of tile (level, tx, ty) in the cache (0: cached unused, -1: absent)
 extern "C" int ref_sampler_users(int level, int tx, int ty)
 {
@@ -1803,12 +1906,14 @@ def generate_sampler(root):
     """oracle/_ref/gen/ref_sampler.cpp: the terrain quadtree, the tile cache, the
     producer's cache calls and TileSampler's update as written, in one namespace."""
     texts = {rel: _read(root, rel) for rel in (STORAGE_CPP, CACHE_CPP, QUAD_CPP, NODE_CPP, PRODUCER_CPP,
-                                               SAMPLER_CPP)}
+                                               SAMPLER_CPP, ELEV_CPP, NORMAL_CPP)}
     src = ["// generated by oracle/ref_build.py from the reference's sources\n", _SAMPLER_PRELUDE, _DECL_STORAGE,
            "struct TileProducer;\n", _DECL_CACHE, _DECL_QUAD, _SAMPLER_CLASSES]
     cls, line = extract_block(texts[SAMPLER_CPP], "class UpdateTileMapTask : public Task", "};")
     src.append("// %s:%d\n%s" % (SAMPLER_CPP, line, cls))
-    extra = [(QUAD_CPP, [r"TerrainNode \*TerrainQuad::getOwner\(", r"int TerrainQuad::getDepth\("])]
+    extra = [(QUAD_CPP, [r"TerrainNode \*TerrainQuad::getOwner\(", r"int TerrainQuad::getDepth\("]),
+             (ELEV_CPP, [r"ptr<Task> ElevationProducer::startCreateTile\(", r"void ElevationProducer::stopCreateTile\("]),
+             (NORMAL_CPP, [r"ptr<Task> NormalProducer::startCreateTile\(", r"void NormalProducer::stopCreateTile\("])]
     for rel, sigs in [(STORAGE_CPP, STORAGE_SIGS), (CACHE_CPP, CACHE_SIGS), (QUAD_CPP, QUAD_SIGS),
                       (NODE_CPP, NODE_SIGS), (PRODUCER_CPP, PRODUCER_SIGS), (SAMPLER_CPP, SAMPLER_SIGS)] + extra:
         for sig in sigs:

@@ -81,3 +81,47 @@ def test_cache_steps_match_reference(ref, product, seed):
         prods[pid].put_tile(t)
     assert len(pairing) == capacity      # every slot was handed out
     assert fulls > 0 or capacity > 6     # small caches filled up
+
+
+@pytest.mark.parametrize("seed", range(6))
+def test_tile_dependencies_match_reference(ref, product, seed):
+    """The tiles a tile's task holds while it waits: ElevationProducer::startCreateTile
+    (the parent elevation tile and the residual tile (level, tx / mod, ty / mod), mod the
+    residual / elevation size ratio) and NormalProducer::startCreateTile (the parent
+    normal tile and the elevation tile), as written, run by the reference's TileCache
+    when it creates a tile (TileProducer::createTile calls startCreateTile) -- against
+    the product's producers on bookkeeping-only storages: after every getTile of an
+    elevation or normal tile, the used and unused counts of the residual, elevation and
+    normal caches agree, and at the end the users of every requested tile, its parent
+    and the residual and elevation tiles of its place."""
+    tp = product
+    rng = np.random.default_rng(seed)
+    W, RW, cap = 101, (101, 197)[seed % 2], 400
+    ref.ref_deps_create(W, RW, cap)
+    rc = tp.TileCache(tp.TileStorage(RW, 1, cap, on_device=tp.TileStorage.BOOKKEEPING), "residuals")
+    ec = tp.TileCache(tp.TileStorage(W, 3, cap, on_device=tp.TileStorage.BOOKKEEPING), "elevations")
+    nc = tp.TileCache(tp.TileStorage(W - 4, 2, cap, on_device=tp.TileStorage.BOOKKEEPING), "normals")
+    r = tp.ResidualProducer(rc)
+    e = tp.ElevationProducer(ec, r, params=tp.make_params())
+    n = tp.NormalProducer(nc, e)
+    prods, caches, asked = [r, e, n], [rc, ec, nc], set()
+    for step in range(150):
+        k = int(rng.choice([1, 2, 2]))
+        lv = int(rng.integers(0, 6))
+        x, y = int(rng.integers(0, 1 << lv)), int(rng.integers(0, 1 << lv))
+        assert ref.ref_deps_get(k, lv, x, y) == 0 and prods[k].get_tile(lv, x, y) is not None
+        asked.add((k, lv, x, y))
+        for c in range(3):
+            used, unused = C.c_int(), C.c_int()
+            ref.ref_deps_counts(c, C.byref(used), C.byref(unused))
+            assert (used.value, unused.value) == (caches[c].get_used_tiles(), caches[c].get_unused_tiles()), \
+                (seed, step, c)
+    mod = (RW - 5) // (W - 5)
+    for k, lv, x, y in sorted(asked):
+        for c, (l2, x2, y2) in ((k, (lv, x, y)), (k, (lv - 1, x // 2, y // 2)), (0, (lv, x // mod, y // mod)),
+                                (1, (lv, x, y))):
+            if l2 < 0:
+                continue
+            f = prods[c].find_tile(l2, x2, y2, include_cache=True)
+            assert ref.ref_deps_users(c, l2, x2, y2) == (f.info()["users"] if f is not None else -1), \
+                (k, lv, x, y, c, l2, x2, y2)
