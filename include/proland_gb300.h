@@ -350,7 +350,11 @@ int tp_create_tile(tp_producer *p, int level, int tx, int ty, tp_tile **tile_out
  * LRUs), acquires the new quads' tiles (getTile, producers in the order given) and
  * produces them in one scheduler run on `stream` (normal tiles of new elevation
  * tiles fused into the elevation launch); *new_count receives the number of new
- * quads.  On failure (TP_E_CACHE_FULL) no tile of the update stays acquired.
+ * quads.  Releases and acquisitions follow TileSampler::putTiles / getTiles's walk of
+ * the quadtree (parents first, children in index order (tx & 1) + 2 (ty & 1)), so
+ * that a full cache evicts the tiles the reference's would; the new quads are
+ * reported in request order.  On failure (TP_E_CACHE_FULL) no tile of the update
+ * stays acquired.
  * tp_sampler_new_tiles copies the last update's new quads (returns their count);
  * tp_sampler_find returns a held tile of producer number `producer`.  Destroying
  * the sampler releases every tile it holds. */
