@@ -37,6 +37,8 @@ The GPU path, in a second unit (``ref_gpu.cpp``):
   matrix arithmetic);
 * ``OrthoProducer::doCreateTile`` (``ortho/OrthoProducer.cpp:273-385``) the same way,
   and ``createOrthoNoise`` (``:26-122``) in the first unit;
+* ``WaterElevationLayer::doCreateTile`` with ``GraphLayer::drawArea``, over a stand-in
+  graph, its draws recorded with the framebuffer state and uniforms at each;
 * ``ElevationGraphLayer::drawCurveAltitude`` and ``GraphLayer::drawCurve`` of a part, and
   the lines of ``RoadElevationLayer::doCreateTile`` that place one road (its scale, tile
   offset, ``BASEWIDTH`` / ``TOTALWIDTH`` and the drawCurveAltitude call), on stand-in
@@ -97,6 +99,7 @@ ORTHO_CPP = "src/terrain/sources/proland/ortho/OrthoProducer.cpp"
 GRAPH_LAYER_CPP = "src/graph/sources/proland/dem/ElevationGraphLayer.cpp"
 ROAD_LAYER_CPP = "src/graph/sources/proland/dem/RoadElevationLayer.cpp"
 GRAPH_PRODUCER_CPP = "src/graph/sources/proland/graph/producer/GraphLayer.cpp"
+WATER_LAYER_CPP = "src/graph/sources/proland/dem/WaterElevationLayer.cpp"
 
 
 def _read(root, rel):
@@ -389,40 +392,153 @@ using std::max;
 // a polyline with its curvilinear coordinates and width; the altitude profile is
 // the identity, getAltitude(s) = s, so that a vertex's altitude shows where on the
 // curve it was sampled.
+// A curve's type, parent and first area (WaterElevationLayer reads them; no parent:
+// the curve is its own), and whether a cap is wanted at each end (GraphLayer::extremity).
 struct Node {};
 typedef ptr<Node> NodePtr;
+struct Area;
 struct Curve {
     vector<vec2d> points;
     vector<float> s;
     float width = 0.0f;
+    int type = 0;
+    Curve *parent = nullptr;
+    Area *area1 = nullptr;
+    bool cap_start = false, cap_end = false;
     Node start, end;
     int getSize() const { return (int)points.size(); }
     vec2d getXY(int i) const { return points[i]; }
     float getS(int i) const { return s[i]; }
     float getWidth() const { return width; }
+    int getType() const { return type; }
+    ptr<Curve> getParent() const { return ptr<Curve>(parent); }
+    ptr<Area> getArea1() const { return ptr<Area>(area1); }
     ptr<Curve> getAncestor() const { return ptr<Curve>(const_cast<Curve *>(this)); }
     NodePtr getStart() const { return NodePtr(const_cast<Node *>(&start)); }
     NodePtr getEnd() const { return NodePtr(const_cast<Node *>(&end)); }
 };
 typedef ptr<Curve> CurvePtr;
-struct ElevationCurveData {
+struct CurveData {
+    virtual ~CurveData() {}
+};
+struct ElevationCurveData : CurveData {
     float getAltitude(float s) { return s; }
 };
+// an area: its boundary curves with their orientations (graph/Area.h)
+struct Area {
+    vector<std::pair<Curve *, int> > curves;
+    int getCurveCount() const { return (int)curves.size(); }
+    CurvePtr getCurve(int j, int &orientation) const
+    {
+        orientation = curves[j].second;
+        return CurvePtr(curves[j].first);
+    }
+};
+typedef ptr<Area> AreaPtr;
+// the tessellator records the contours it is given (GLU, which triangulates them, is
+// not here)
+struct Tesselator {
+    vector<vector<vec2d> > contours;
+    void beginPolygon(ptr<Mesh<vec2f, unsigned int> >) { contours.clear(); }
+    void beginContour() { contours.emplace_back(); }
+    void newVertex(double x, double y) { contours.back().push_back(vec2d(x, y)); }
+    void endContour() {}
+    void endPolygon() {}
+};
 
-// GraphLayer's members the drawing functions call: isDeformed, and extremity, here
-// whether the caller asks for a cap at that end; and GraphLayer::drawCurve of a part.
+// GraphLayer's members the drawing functions call: isDeformed, extremity (here
+// whether the curve asks for a cap at that end), GraphLayer::drawCurve of a part and
+// drawArea.
 struct GraphLayer {
-    bool deformed = false, cap_start = false, cap_end = false;
+    bool deformed = false;
     bool isDeformed() const { return deformed; }
-    bool extremity(CurvePtr c, NodePtr p) { return p.p == &c->start ? cap_start : cap_end; }
+    bool extremity(CurvePtr c, NodePtr p) { return p.p == &c->start ? c->cap_start : c->cap_end; }
     void drawCurve(const vec3d &tileCoords, CurvePtr p, const vec4f &part, ptr<FrameBuffer> fb, ptr<Program> prog,
                    Mesh<vec4f, unsigned int> &mesh, vec2d *nx, vec2d *ny, vec2d *lx, vec2d *ly);
+    void drawArea(const vec3d &tileCoords, AreaPtr a, Tesselator &tess);
 };
 
 struct ElevationGraphLayer : GraphLayer {
     void drawCurveAltitude(const vec3d &tileCoords, CurvePtr p, ElevationCurveData *data, float width, float nwidth,
                            float stepLength, bool caps, ptr<FrameBuffer> fb, ptr<Program> prog,
                            Mesh<vec4f, unsigned int> &mesh, vec2d *nx, vec2d *ny, vec2d *lx, vec2d *ly);
+};
+
+// WaterElevationLayer::doCreateTile's graph: curves and areas, in the order its
+// iterators give them (graph/Graph.h), on an object slot of the graph producer's tile.
+struct GraphObject {
+    virtual ~GraphObject() {}
+};
+struct Graph : GraphObject {
+    vector<Curve *> curves;
+    vector<Area *> areas;
+    struct AreaIterator {
+        const Graph *g = nullptr;
+        size_t k = 0;
+        bool hasNext() { return k < g->areas.size(); }
+        AreaPtr next() { return AreaPtr(g->areas[k++]); }
+    };
+    struct CurveIterator {
+        const Graph *g = nullptr;
+        size_t k = 0;
+        bool hasNext() { return k < g->curves.size(); }
+        CurvePtr next() { return CurvePtr(g->curves[k++]); }
+    };
+    AreaIterator area_it;
+    CurveIterator curve_it;
+    int getCurveCount() { return (int)curves.size(); }
+    int getAreaCount() { return (int)areas.size(); }
+    ptr<AreaIterator> getAreas()
+    {
+        area_it.g = this;
+        area_it.k = 0;
+        return ptr<AreaIterator>(&area_it);
+    }
+    ptr<CurveIterator> getCurves()
+    {
+        curve_it.g = this;
+        curve_it.k = 0;
+        return ptr<CurveIterator>(&curve_it);
+    }
+};
+typedef ptr<Graph> GraphPtr;
+struct ObjectTileStorage {
+    struct ObjectSlot : TileStorage::Slot {
+        ptr<GraphObject> data;
+    };
+};
+struct SceneManager {
+    static FrameBuffer *current;
+    static ptr<FrameBuffer> getCurrentFrameBuffer() { return ptr<FrameBuffer>(current); }
+};
+struct WaterElevationCurveData {
+    enum riverType { RIVER = 0, ISLAND = 1, LAKE = 2 };
+};
+
+// The members WaterElevationLayer::doCreateTile uses (WaterElevationLayer.h,
+// GraphLayer / TileLayer): the tile's coordinates q, flat (no deformation).
+struct WaterElevationLayer : ElevationGraphLayer {
+    int displayLevel = 0;
+    ptr<TileProducer> graphProducer;
+    ptr<Program> layerProgram, fillProg;
+    ptr<Mesh<vec2f, unsigned int> > mesh;
+    ptr<Mesh<vec4f, unsigned int> > meshuv;
+    ptr<Tesselator> tess;
+    ptr<Uniform3f> tileOffsetU;
+    ptr<Uniform1i> riverU;
+    ptr<Uniform3f> fillOffsetU;
+    ptr<Uniform1f> depthU;
+    ptr<Uniform4f> colorU;
+    vec3d q;
+    int tileSize = 101, tileBorder = 2;
+    std::map<Curve *, ElevationCurveData> curveData;
+    vec3d getTileCoords(int, int, int) { return q; }
+    void getDeformParameters(const vec3d &, vec2d &, vec2d &, vec2d &, vec2d &) {}
+    int getTileSize() { return tileSize; }
+    int getTileBorder() { return tileBorder; }
+    CurveData *findCurveData(CurvePtr c) { return &curveData[c.p]; }
+    int getProducerId() { return 0; }
+    bool doCreateTile(int level, int tx, int ty, TileStorage::Slot *data);
 };
 
 // The lines of RoadElevationLayer::doCreateTile that place one road on a tile.
@@ -807,8 +923,8 @@ extern "C" int ref_road_meshes(double qx, double qy, double qz, int tile_size, i
     layer.tileBorder = border;
     layer.layerProgram = &prog;
     layer.meshuv = &mesh;
-    layer.cap_start = cap_start != 0;
-    layer.cap_end = cap_end != 0;
+    c.cap_start = cap_start != 0;
+    c.cap_end = cap_end != 0;
     layer.draw_road(vec3d(qx, qy, qz), &c, &data, &fb, scale_out);
     g_drawn = fb.drawn;
     return (int)g_drawn.size();
@@ -828,8 +944,8 @@ extern "C" int ref_curve_altitude(double cx, double cy, double factor, const dou
     Program prog;
     Mesh<vec4f, unsigned int> mesh;
     ElevationGraphLayer layer;
-    layer.cap_start = cap_start != 0;
-    layer.cap_end = cap_end != 0;
+    c.cap_start = cap_start != 0;
+    c.cap_end = cap_end != 0;
     layer.drawCurveAltitude(vec3d(cx, cy, factor), &c, &data, width, nwidth, step, true, &fb, &prog, mesh, nullptr,
                             nullptr, nullptr, nullptr);
     g_drawn = fb.drawn;
@@ -852,6 +968,126 @@ extern "C" int ref_curve_part(double cx, double cy, double factor, const double 
                     nullptr, nullptr, nullptr);
     g_drawn = fb.drawn;
     return (int)g_drawn.size();
+}
+
+namespace {
+struct WaterDraws {
+    int river = 0;
+    float depth = 0.0f, color[4] = {0, 0, 0, 0}, offset[3] = {0, 0, 0}, fill_offset[3] = {0, 0, 0};
+};
+void water_snapshot(void *arg, refgl::FrameBuffer::Drawn &d)
+{
+    const WaterDraws &w = *(const WaterDraws *)arg;
+    d.extra = {(float)w.river, w.depth, w.color[0], w.color[1], w.color[2], w.color[3]};
+}
+std::vector<std::vector<refgl::vec2d> > g_contours;
+}  // namespace
+
+// WaterElevationLayer::doCreateTile on tile q = (x, y, size) at `level` of a
+// tile_size-wide storage, over a graph of n_curves curves -- curve k has info[6k..6k+5]
+// = (points, type, parent: 1 itself / 0 none, area1: 1 set / 0 none, cap at start, cap
+// at end), its points in xy (2 doubles each, curve after curve), their curvilinear
+// coordinates in s, its width -- and n_areas areas, area a listing area_info (its curve
+// count, then (curve index, orientation) pairs).  The draws are read by
+// ref_drawn_mesh and ref_water_draw, the area contours by ref_water_contour.  Returns
+// the number of draws, or -1.
+extern "C" int ref_water_layer(double qx, double qy, double qz, int tile_size, int level, int n_curves,
+                               const int *info, const double *xy, const float *s, const float *widths, int n_areas,
+                               const int *area_info)
+{
+    using namespace refgl;
+    std::vector<Curve> curves(n_curves);
+    std::vector<Area> areas(n_areas);
+    Graph g;
+    for (int k = 0, at = 0; k < n_curves; ++k) {
+        const int *c = info + 6 * k;
+        for (int i = 0; i < c[0]; ++i, ++at) {
+            curves[k].points.push_back(vec2d(xy[2 * at], xy[2 * at + 1]));
+            curves[k].s.push_back(s[at]);
+        }
+        curves[k].type = c[1];
+        curves[k].parent = c[2] ? &curves[k] : nullptr;
+        curves[k].area1 = c[3] && n_areas ? &areas[0] : nullptr;
+        curves[k].cap_start = c[4] != 0;
+        curves[k].cap_end = c[5] != 0;
+        curves[k].width = widths[k];
+        g.curves.push_back(&curves[k]);
+    }
+    for (int a = 0, at = 0; a < n_areas; ++a) {
+        const int n = area_info[at++];
+        for (int j = 0; j < n; ++j, at += 2) {
+            if (area_info[at] < 0 || area_info[at] >= n_curves) return -1;
+            areas[a].curves.push_back(std::make_pair(&curves[area_info[at]], area_info[at + 1]));
+        }
+        g.areas.push_back(&areas[a]);
+    }
+    ObjectTileStorage::ObjectSlot graphSlot;
+    graphSlot.data = ptr<GraphObject>(&g);
+    TileProducer graphProducer;
+    graphProducer.tiles[std::make_tuple(level, 0, 0)].data = &graphSlot;
+    FrameBuffer fb;
+    SceneManager::current = &fb;
+    WaterDraws w;
+    fb.on_draw = water_snapshot;
+    fb.on_draw_arg = &w;
+    Program layerProgram, fillProg;
+    Mesh<vec2f, unsigned int> mesh;
+    Mesh<vec4f, unsigned int> meshuv;
+    Tesselator tess;
+    Uniform tileOffsetU{U_VEC3, w.offset}, riverU{U_INT, &w.river}, fillOffsetU{U_VEC3, w.fill_offset},
+        depthU{U_FLOAT, &w.depth}, colorU{U_VEC4, w.color};
+    WaterElevationLayer layer;
+    layer.graphProducer = &graphProducer;
+    layer.layerProgram = &layerProgram;
+    layer.fillProg = &fillProg;
+    layer.mesh = &mesh;
+    layer.meshuv = &meshuv;
+    layer.tess = &tess;
+    layer.tileOffsetU = &tileOffsetU;
+    layer.riverU = &riverU;
+    layer.fillOffsetU = &fillOffsetU;
+    layer.depthU = &depthU;
+    layer.colorU = &colorU;
+    layer.q = vec3d(qx, qy, qz);
+    layer.tileSize = tile_size;
+    layer.doCreateTile(level, 0, 0, nullptr);
+    SceneManager::current = nullptr;
+    for (FrameBuffer::Drawn &d : fb.drawn) d.extra.push_back(d.program == &fillProg ? 0.0f : 1.0f);
+    g_drawn = fb.drawn;
+    g_contours = tess.contours;
+    return (int)g_drawn.size();
+}
+
+// Draw k of the last ref_water_layer: state[0..7] = program (0 fill, 1 layer), river,
+// depth test on, depth function (0 LESS, 1 ALWAYS, 2 NOTEQUAL), depth mask, colour mask
+// of z, colour mask of w, mode; uniforms[0..4] = fill depth and colour.
+extern "C" int ref_water_draw(int k, int *state, float *uniforms)
+{
+    if (k < 0 || k >= (int)g_drawn.size()) return 1;
+    const refgl::FrameBuffer::Drawn &d = g_drawn[k];
+    state[0] = (int)d.extra[6];
+    state[1] = (int)d.extra[0];
+    state[2] = d.depth_test;
+    state[3] = d.depth_func;
+    state[4] = d.depth_mask;
+    state[5] = d.color_mask[2];
+    state[6] = d.color_mask[3];
+    state[7] = d.mode;
+    for (int i = 0; i < 5; ++i) uniforms[i] = d.extra[1 + i];
+    return 0;
+}
+
+// contour k of the areas the last ref_water_layer filled, in clip coordinates: its
+// vertex count, and its vertices (2 doubles each) when `out` is given
+extern "C" int ref_water_contour(int k, double *out)
+{
+    if (k < 0 || k >= (int)g_contours.size()) return -1;
+    if (out)
+        for (size_t i = 0; i < g_contours[k].size(); ++i) {
+            out[2 * i] = g_contours[k][i].x;
+            out[2 * i + 1] = g_contours[k][i].y;
+        }
+    return (int)g_contours[k].size();
 }
 
 // Mesh k of the last ref_road_meshes / ref_curve_altitude / ref_curve_part: its mode (0 triangles, 1 strip), vertex and index
@@ -2010,6 +2246,14 @@ def generate_gpu(root):
                                     after="bool RoadElevationLayer::doCreateTile(")
     src.append("// %s:%d\n%s" % (GRAPH_LAYER_CPP, dca_line, dca))
     src.append("// %s:%d\n%s" % (GRAPH_PRODUCER_CPP, dcp_line, dcp))
+    dra, dra_line = extract_function(_read(root, GRAPH_PRODUCER_CPP), r"void\s+GraphLayer::drawArea\s*\(")
+    src.append("// %s:%d\n%s" % (GRAPH_PRODUCER_CPP, dra_line, dra))
+    water = _read(root, WATER_LAYER_CPP)
+    wdct, wdct_line = extract_function(water, r"bool\s+WaterElevationLayer::doCreateTile\s*\(")
+    wmac, wmac_line = extract_block(water, "#define BASEWIDTH(", "#define TOTALWIDTH(")
+    src.append("}  // namespace refgl\n#undef BASEWIDTH\n#undef TOTALWIDTH\n// %s:%d\n%snamespace refgl {\n"
+               "FrameBuffer *SceneManager::current = nullptr;\n// %s:%d\n%s"
+               % (WATER_LAYER_CPP, wmac_line, wmac, WATER_LAYER_CPP, wdct_line, wdct))
     src.append("}  // namespace refgl\n// %s:%d\n%snamespace refgl {\n" % (ROAD_LAYER_CPP, macros_line, macros))
     src.append("void RoadElevationLayer::draw_road(const vec3d &q, CurvePtr c, ElevationCurveData *cData, "
                "ptr<FrameBuffer> fb, float *scale_out)\n{\n    vec2d nx, ny, lx, ly;\n"
@@ -2032,7 +2276,8 @@ def build(root=DEFAULT_ROOT, force=False):
     if not os.path.isdir(os.path.join(root, "src")):
         return LIB if os.path.exists(LIB) else None
     srcs = [os.path.join(root, p) for p in (NOISE_CPP, ELEV_CPP, CPU_ELEV_CPP, MIPMAP_CPP, NORMAL_CPP, ORTHO_CPP,
-                                            GRAPH_LAYER_CPP, ROAD_LAYER_CPP, GRAPH_PRODUCER_CPP, RESIDUAL_CPP,
+                                            GRAPH_LAYER_CPP, ROAD_LAYER_CPP, GRAPH_PRODUCER_CPP, WATER_LAYER_CPP,
+                                            RESIDUAL_CPP,
                                             ORTHO_CPU_CPP, MFS_CPP, CACHE_CPP, STORAGE_CPP, QUAD_CPP, NODE_CPP,
                                             PRODUCER_CPP, SAMPLER_CPP)]
     srcs += [os.path.join(root, rel) for _, rel, _ in UPSAMPLE_SHADERS + NORMAL_SHADERS + BLEND_SHADERS +

@@ -155,6 +155,7 @@ template <class T> struct mat4 {
 };
 
 typedef vec2<double> vec2d;
+typedef vec2<float> vec2f;
 typedef vec3<float> vec3f;
 typedef vec3<double> vec3d;
 typedef vec4<float> vec4f;
@@ -281,6 +282,7 @@ struct Uniform {
     }
 };
 typedef Uniform Uniform1f;
+typedef Uniform Uniform1i;
 typedef Uniform Uniform3f;
 typedef Uniform Uniform4f;
 typedef Uniform Uniform4i;
@@ -339,25 +341,55 @@ struct FrameBuffer {
     {
         std::memcpy(&color[draw_buffer][((size_t)j * w + i) * 4], rgba, 4 * sizeof(float));
     }
-    void setDepthTest(bool, Function = LESS) {}
-    // meshes drawn by draw(program, mesh): mode, (x, y, z, w) vertices and indices
+    // the depth test, depth and colour write masks of the next draws
+    bool depth_test = false;
+    int depth_func = LESS;
+    bool color_mask[4] = {true, true, true, true};
+    bool depth_mask = true;
+    void setDepthTest(bool on, Function f = LESS)
+    {
+        depth_test = on;
+        depth_func = f;
+    }
+    void setColorMask(bool r, bool g, bool b, bool a)
+    {
+        color_mask[0] = r; color_mask[1] = g; color_mask[2] = b; color_mask[3] = a;
+    }
+    void setDepthMask(bool d) { depth_mask = d; }
+    // meshes drawn by draw(program, mesh): mode, (x, y, z, w) vertices (z, w 0 for 2D
+    // vertices), indices, the program, the state above and what `on_draw` adds
     struct Drawn {
         int mode;
         vector<float> vertices;
         vector<unsigned int> indices;
+        const Program *program = nullptr;
+        bool depth_test = false, depth_mask = true, color_mask[4];
+        int depth_func = LESS;
+        vector<float> extra;
     };
     vector<Drawn> drawn;
-    template <class M> void draw(ptr<Program>, const M &mesh)
+    void (*on_draw)(void *, Drawn &) = nullptr;
+    void *on_draw_arg = nullptr;
+    template <class T> static void push4(vector<float> &o, const vec4<T> &v)
+    {
+        o.push_back(v.x); o.push_back(v.y); o.push_back(v.z); o.push_back(v.w);
+    }
+    template <class T> static void push4(vector<float> &o, const vec2<T> &v)
+    {
+        o.push_back(v.x); o.push_back(v.y); o.push_back(0.0f); o.push_back(0.0f);
+    }
+    template <class M> void draw(ptr<Program> prog, const M &mesh)
     {
         Drawn d;
         d.mode = mesh.mode;
-        for (const auto &v : mesh.vertices) {
-            d.vertices.push_back(v.x);
-            d.vertices.push_back(v.y);
-            d.vertices.push_back(v.z);
-            d.vertices.push_back(v.w);
-        }
+        for (const auto &v : mesh.vertices) push4(d.vertices, v);
         d.indices = mesh.indices;
+        d.program = prog.get();
+        d.depth_test = depth_test;
+        d.depth_func = depth_func;
+        d.depth_mask = depth_mask;
+        for (int k = 0; k < 4; ++k) d.color_mask[k] = color_mask[k];
+        if (on_draw) on_draw(on_draw_arg, d);
         drawn.push_back(d);
     }
     void setDrawBuffer(BufferId b) { draw_buffer = b == COLOR1 ? 1 : 0; }

@@ -584,3 +584,101 @@ def test_ortho_cpu_producer_on_reference_pyramid(ref, oracle_lib, product):
                     assert np.array_equal(d.tile(level, tx, ty), out), (level, tx, ty)
                     checked += 1
     assert checked == sum(4 ** l for l in range(d.max_level + 1))
+
+
+RIVER, ISLAND, LAKE = 0, 1, 2   # WaterElevationCurveData::riverType
+
+
+def _loop(rng, cx, cy, r, n):
+    a = np.sort(rng.uniform(0, 2 * np.pi, n))
+    pts = np.column_stack([cx + r * np.cos(a), cy + r * np.sin(a)])
+    return np.vstack([pts, pts[:1]])
+
+
+def _curve_s(pts):
+    return np.float32(np.concatenate([[0.0], np.cumsum(np.sqrt((np.diff(pts, axis=0) ** 2).sum(1)))]))
+
+
+@pytest.mark.parametrize("seed", range(4))
+def test_water_layer_pass_sequence(ref, product, seed):
+    """WaterElevationLayer::doCreateTile as written (WaterElevationLayer.cpp:240-365),
+    with GraphLayer::drawArea, drawCurve and drawCurveAltitude, over a stand-in graph
+    (a lake with an island, a mixed area, curves of other types, rivers with caps, a
+    river too narrow to draw), against proland_gb300.layers.water_layer given the
+    inputs its docstring asks of the caller (areas, boundaries with the island
+    orientation flipped, the other curves, the rivers -- chosen by the reference's
+    filters): draw for draw, the program, the river uniform, the depth test and depth
+    mask, the z / w colour masks and the fill depth match the product's mesh, program,
+    state and fill depth, and every curve mesh is the product's vertex and index for
+    index.  (The fill triangles are GLU's in the reference; the stand-in tessellator
+    records the area contours, which are the clip-space contours of the areas.)"""
+    import ctypes as C
+    from proland_gb300 import layers
+    tp = product
+    rng = np.random.default_rng(seed)
+    W, size, level = 101, 2000.0, 3
+    origin = (float(rng.uniform(-3000, 3000)), float(rng.uniform(-3000, 3000)))
+    ox, oy = origin
+    cx, cy = ox + size / 2, oy + size / 2
+    lake = _loop(rng, cx, cy, 700.0, 9)
+    island = _loop(rng, cx + 60, cy - 40, 150.0, 6)
+    other = np.column_stack([np.linspace(ox - 50, ox + size + 50, 5), oy + rng.uniform(0, size, 5)])
+    river = np.column_stack([ox + rng.uniform(0, size, 4), np.linspace(oy - 80, oy + size + 80, 4)])
+    narrow = np.column_stack([np.linspace(ox, ox + size, 3), oy + rng.uniform(0, size, 3)])
+    # (points, type, has parent, in an area, cap start, cap end, width)
+    curves = [(lake, LAKE, 1, 1, 0, 0, 30.0), (island, ISLAND, 1, 1, 0, 0, 20.0), (other, 3, 1, 0, 0, 0, 25.0),
+              (other[::-1].copy(), ISLAND, 1, 0, 0, 0, 40.0), (river, RIVER, 1, 0, seed % 2, 1, 35.0),
+              (narrow, RIVER, 1, 0, 0, 0, 1.0)]
+    areas = [[(0, 0), (1, 0)], [(1, 1)], [(0, 1)]]   # mixed (island skipped), island, lake reversed
+    info = np.array([[len(c[0]), c[1], c[2], c[3], c[4], c[5]] for c in curves], np.int32)
+    xy = np.ascontiguousarray(np.vstack([c[0] for c in curves]), np.float64)
+    s = np.concatenate([_curve_s(c[0]) for c in curves]).astype(np.float32)
+    widths = np.float32([c[6] for c in curves])
+    area_info = np.array(sum([[len(a)] + [v for pair in a for v in pair] for a in areas], []), np.int32)
+    n = ref.ref_water_layer(ox, oy, size, W, level, len(curves), info.ctypes.data, xy.ctypes.data, s.ctypes.data,
+                            _p(widths), len(areas), area_info.ctypes.data)
+    assert n > 0
+    # the product's inputs, chosen by the reference's rules
+    tr = layers.tile_transform(origin, size, W)
+    scale = tr[3]
+    contour = [np.vstack([curves[k][0] if o == 0 else curves[k][0][::-1] for k, o in a]) for a in areas]
+    boundaries = []
+    for a in areas:
+        island_area = all(curves[k][1] == ISLAND for k, _ in a)
+        for k, o in a:
+            if island_area:
+                o = 1 - o
+            elif curves[k][1] == ISLAND:
+                continue
+            boundaries.append((curves[k][0], o))
+    others = [(c[0], _curve_s(c[0]), c[6]) for c in curves
+              if not (np.float32(c[6]) * scale <= 1 or c[1] in (LAKE, RIVER) or c[3])]
+    rivers = [(c[0], _curve_s(c[0]), c[6], bool(c[4]), bool(c[5])) for c in curves if c[1] == RIVER]
+    want = layers.water_layer(origin, size, W, areas=[[cnt] for cnt in contour], boundaries=boundaries,
+                              curves=others, rivers=rivers)
+    assert len(want) == n
+    drawn = _drawn(ref, n)
+    for k, (v, ix, mode, prog, state, fill_depth) in enumerate(want):
+        st = (C.c_int * 8)()
+        un = np.empty(5, np.float32)
+        assert ref.ref_water_draw(k, st, _p(un)) == 0
+        fill, river, test_on, func, depth_mask, z_mask, w_mask, rmode = list(st)
+        assert test_on == 1
+        assert prog == (tp.LAYER_FILL if fill == 0 else 1 + river), k
+        assert state == func | (0 if depth_mask else tp.NO_DEPTH_WRITE) | (0 if z_mask else tp.NO_Z_WRITE) | \
+            (0 if w_mask else tp.NO_W_WRITE), k
+        if fill == 0:
+            assert np.float32(fill_depth) == un[0] and not np.any(un[1:]), k
+            continue
+        assert rmode == mode, k
+        got = drawn[k]
+        assert np.array_equal(got[0], np.asarray(v, np.float32)), k
+        assert (got[1] is None and ix is None) or np.array_equal(got[1], ix), k
+    # the areas' contours, as the tessellator received them
+    for a, cnt in enumerate(contour):
+        m = ref.ref_water_contour(a, None)
+        pts = np.empty((m, 2), np.float64)
+        ref.ref_water_contour(a, pts.ctypes.data)
+        X = (cnt[:, 0] - tr[0]) * tr[2]
+        Y = (cnt[:, 1] - tr[1]) * tr[2]
+        assert np.array_equal(pts, np.column_stack([X, Y])), a
