@@ -674,6 +674,7 @@ def ref_lib():
         L.ref_water_layer.argtypes = [C.c_double] * 3 + [C.c_int] * 3 + [C.c_void_p, C.c_void_p, C.c_void_p,
                                                                          _f32p, C.c_int, C.c_void_p]
         L.ref_water_draw.argtypes = [C.c_int, C.POINTER(C.c_int), _f32p]
+        L.ref_road_layer.argtypes = [C.c_double] * 3 + [C.c_int] * 3 + [C.c_void_p, C.c_void_p, C.c_void_p, _f32p]
         L.ref_water_contour.argtypes = [C.c_int, C.c_void_p]
         L.ref_deps_create.argtypes = [C.c_int] * 3
         L.ref_deps_get.argtypes = [C.c_int] * 4

@@ -541,13 +541,28 @@ struct WaterElevationLayer : ElevationGraphLayer {
     bool doCreateTile(int level, int tx, int ty, TileStorage::Slot *data);
 };
 
-// The lines of RoadElevationLayer::doCreateTile that place one road on a tile.
+struct RoadElevationCurveData {
+    enum roadType { ROAD = 0, UNKNOWN = 1, BRIDGE = 2 };
+};
+
+// The members RoadElevationLayer::doCreateTile uses (RoadElevationLayer.h, GraphLayer /
+// TileLayer), and draw_road: its lines that place one road on a tile.
 struct RoadElevationLayer : ElevationGraphLayer {
     int tileSize = 101, tileBorder = 2;
+    int displayLevel = 0;
+    ptr<TileProducer> graphProducer;
     ptr<Program> layerProgram;
     Mesh<vec4f, unsigned int> *meshuv = nullptr;
+    ptr<Uniform3f> tileOffsetU;
+    vec3d q;
+    std::map<Curve *, ElevationCurveData> curveData;
     int getTileSize() { return tileSize; }
     int getTileBorder() { return tileBorder; }
+    vec3d getTileCoords(int, int, int) { return q; }
+    void getDeformParameters(const vec3d &, vec2d &, vec2d &, vec2d &, vec2d &) {}
+    CurveData *findCurveData(CurvePtr c) { return &curveData[c.p]; }
+    int getProducerId() { return 0; }
+    bool doCreateTile(int level, int tx, int ty, TileStorage::Slot *data);
     void draw_road(const vec3d &q, CurvePtr c, ElevationCurveData *cData, ptr<FrameBuffer> fb, float *scale_out);
 };
 
@@ -1055,6 +1070,66 @@ extern "C" int ref_water_layer(double qx, double qy, double qz, int tile_size, i
     for (FrameBuffer::Drawn &d : fb.drawn) d.extra.push_back(d.program == &fillProg ? 0.0f : 1.0f);
     g_drawn = fb.drawn;
     g_contours = tess.contours;
+    return (int)g_drawn.size();
+}
+
+namespace {
+// a graph of curves (ref_water_layer's encoding) for the layers' harnesses
+void build_graph(int n_curves, const int *info, const double *xy, const float *s, const float *widths,
+                 std::vector<refgl::Curve> &curves, refgl::Graph &g)
+{
+    curves.assign(n_curves, refgl::Curve());
+    for (int k = 0, at = 0; k < n_curves; ++k) {
+        const int *c = info + 6 * k;
+        for (int i = 0; i < c[0]; ++i, ++at) {
+            curves[k].points.push_back(refgl::vec2d(xy[2 * at], xy[2 * at + 1]));
+            curves[k].s.push_back(s[at]);
+        }
+        curves[k].type = c[1];
+        curves[k].parent = c[2] ? &curves[k] : nullptr;
+        curves[k].cap_start = c[4] != 0;
+        curves[k].cap_end = c[5] != 0;
+        curves[k].width = widths[k];
+        g.curves.push_back(&curves[k]);
+    }
+}
+}  // namespace
+
+// RoadElevationLayer::doCreateTile on tile q = (x, y, size) at `level`, over a graph of
+// curves encoded as for ref_water_layer (type 0 ROAD), after ElevationProducer's
+// setDepthTest(true, LESS).  The draws are read by ref_drawn_mesh and ref_water_draw.
+// Returns their number.
+extern "C" int ref_road_layer(double qx, double qy, double qz, int tile_size, int level, int n_curves,
+                              const int *info, const double *xy, const float *s, const float *widths)
+{
+    using namespace refgl;
+    std::vector<Curve> curves;
+    Graph g;
+    build_graph(n_curves, info, xy, s, widths, curves, g);
+    ObjectTileStorage::ObjectSlot graphSlot;
+    graphSlot.data = ptr<GraphObject>(&g);
+    TileProducer graphProducer;
+    graphProducer.tiles[std::make_tuple(level, 0, 0)].data = &graphSlot;
+    FrameBuffer fb;
+    fb.setDepthTest(true, LESS);
+    SceneManager::current = &fb;
+    WaterDraws w;
+    fb.on_draw = water_snapshot;
+    fb.on_draw_arg = &w;
+    Program layerProgram;
+    Mesh<vec4f, unsigned int> meshuv;
+    Uniform tileOffsetU{U_VEC3, w.offset};
+    RoadElevationLayer layer;
+    layer.graphProducer = &graphProducer;
+    layer.layerProgram = &layerProgram;
+    layer.meshuv = &meshuv;
+    layer.tileOffsetU = &tileOffsetU;
+    layer.q = vec3d(qx, qy, qz);
+    layer.tileSize = tile_size;
+    layer.doCreateTile(level, 0, 0, nullptr);
+    SceneManager::current = nullptr;
+    for (FrameBuffer::Drawn &d : fb.drawn) d.extra.push_back(1.0f);
+    g_drawn = fb.drawn;
     return (int)g_drawn.size();
 }
 
@@ -2259,6 +2334,8 @@ def generate_gpu(root):
                "ptr<FrameBuffer> fb, float *scale_out)\n{\n    vec2d nx, ny, lx, ly;\n"
                "    // %s:%d\n%s    // :%d\n%s    // :%d\n%s    // :%d\n%s    *scale_out = scale;\n}\n"
                % (ROAD_LAYER_CPP, placing_line, placing, cw_line, cw, widths_line, widths, call_line, call))
+    rdct, rdct_line = extract_function(road, r"bool\s+RoadElevationLayer::doCreateTile\s*\(")
+    src.append("// %s:%d\n%s" % (ROAD_LAYER_CPP, rdct_line, rdct))
     src.append("// %s:%d\nvoid OrthoProducer::bind_uniforms()\n{\n%s}\n" % (ORTHO_CPP, oups_line, oups))
     src.append("// %s:%d\n%s" % (ORTHO_CPP, odct_line, odct))
     src.append("}  // namespace refgl\n")

@@ -27,8 +27,8 @@ import math
 
 import numpy as np
 
-from . import (DEPTH_ALWAYS, DEPTH_LESS, DEPTH_NOTEQUAL, LAYER_FILL, LAYER_WATER_LARGE, LAYER_WATER_RIVER,
-               NO_DEPTH_WRITE, NO_W_WRITE, NO_Z_WRITE, TRIANGLE_STRIP, TRIANGLES)
+from . import (DEPTH_ALWAYS, DEPTH_LESS, DEPTH_NOTEQUAL, LAYER_FILL, LAYER_ROAD, LAYER_WATER_LARGE,
+               LAYER_WATER_RIVER, NO_DEPTH_WRITE, NO_W_WRITE, NO_Z_WRITE, TRIANGLE_STRIP, TRIANGLES)
 
 f32 = np.float32
 
@@ -133,6 +133,30 @@ def road_strip(points, altitudes, width, tile_origin, tile_size, W, border=2):
     total = f32(base * f32(3.0))
     step = max(f32(1.0), f32(f32(1.0) / scale))
     return curve_altitude_meshes(points, altitudes, total, f32(total / base), step, tr)[0][0]
+
+
+def road_layer(tile_origin, tile_size, W, roads=(), border=2):
+    """The meshes RoadElevationLayer::doCreateTile (RoadElevationLayer.cpp:388-437) draws
+    on one tile, in its order, as (vertices, indices or None, mode, program, state,
+    fill_depth) for a producer's layer callback: for each road = (points, altitudes,
+    width[, start_cap, end_cap]) whose width * scale > 1, its TOTALWIDTH(BASEWIDTH(width))
+    altitude strip (nwidth TOTALWIDTH / BASEWIDTH, step max(1, 1 / scale)) with a cap at
+    each end the graph marks as an extremity, road program, LESS with depth writes, z and
+    w.  The graph filters (curve type ROAD, parents) are the caller's."""
+    tr = tile_transform(tile_origin, tile_size, W, border)
+    scale = tr[3]
+    step = max(f32(1.0), f32(f32(1.0) / scale))
+    out = []
+    for r in roads:
+        pts, alt, width = r[:3]
+        caps = tuple(r[3:5]) if len(r) > 3 else (False, False)
+        if f32(width) * scale <= 1.0:
+            continue
+        base = base_width(width, scale)
+        total = f32(base * f32(3.0))
+        for v, ix, mode in curve_altitude_meshes(pts, alt, total, f32(total / base), step, tr, *caps):
+            out.append((v, ix, mode, LAYER_ROAD, DEPTH_LESS, 0.0))
+    return out
 
 
 def curve_part_strip(points, part, transform):

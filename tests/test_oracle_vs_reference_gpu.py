@@ -682,3 +682,44 @@ def test_water_layer_pass_sequence(ref, product, seed):
         X = (cnt[:, 0] - tr[0]) * tr[2]
         Y = (cnt[:, 1] - tr[1]) * tr[2]
         assert np.array_equal(pts, np.column_stack([X, Y])), a
+
+
+@pytest.mark.parametrize("seed", range(4))
+def test_road_layer_draws(ref, product, seed):
+    """RoadElevationLayer::doCreateTile as written (RoadElevationLayer.cpp:388-437) over a
+    stand-in graph -- roads with and without caps at their ends, a road too narrow to draw,
+    a curve of another type, a curve without a parent at a level above 0 -- after the
+    elevation producer's LESS depth test, against proland_gb300.layers.road_layer given
+    the roads the reference's filters keep: draw for draw, the road program under LESS with
+    depth writes, z and w written, and every mesh vertex and index for index."""
+    import ctypes as C
+    from proland_gb300 import layers
+    tp = product
+    rng = np.random.default_rng(20 + seed)
+    W, size, level = (101, 197)[seed % 2], 1500.0, 4
+    ox, oy = float(rng.uniform(-4000, 4000)), float(rng.uniform(-4000, 4000))
+
+    def road(n):
+        return np.column_stack([ox + rng.uniform(-100, size + 100, n), oy + rng.uniform(-100, size + 100, n)])
+    # (points, type, has parent, -, cap start, cap end, width)
+    curves = [(road(4), 0, 1, 0, 1, 0, 12.0), (road(3), 0, 1, 0, 0, 1, 30.0), (road(5), 0, 1, 0, 1, 1, 8.0),
+              (road(3), 0, 1, 0, 0, 0, 0.5), (road(3), 1, 1, 0, 0, 0, 20.0), (road(3), 0, 0, 0, 0, 0, 20.0)]
+    info = np.array([[len(c[0]), c[1], c[2], c[3], c[4], c[5]] for c in curves], np.int32)
+    xy = np.ascontiguousarray(np.vstack([c[0] for c in curves]), np.float64)
+    s = np.concatenate([_curve_s(c[0]) for c in curves]).astype(np.float32)
+    widths = np.float32([c[6] for c in curves])
+    n = ref.ref_road_layer(ox, oy, size, W, level, len(curves), info.ctypes.data, xy.ctypes.data, s.ctypes.data,
+                           _p(widths))
+    kept = [(c[0], _curve_s(c[0]), c[6], bool(c[4]), bool(c[5])) for c in curves if c[1] == 0 and c[2]]
+    want = layers.road_layer((ox, oy), size, W, roads=kept)
+    assert len(want) == n and n >= 3
+    drawn = _drawn(ref, n)
+    for k, (v, ix, mode, prog, state, _) in enumerate(want):
+        st = (C.c_int * 8)()
+        un = np.empty(5, np.float32)
+        ref.ref_water_draw(k, st, _p(un))
+        _, _, test_on, func, depth_mask, z_mask, w_mask, rmode = list(st)
+        assert (prog, state) == (tp.LAYER_ROAD, tp.DEPTH_LESS)
+        assert (test_on, func, depth_mask, z_mask, w_mask, rmode) == (1, 0, 1, 1, 1, mode), k
+        assert np.array_equal(drawn[k][0], np.asarray(v, np.float32)), k
+        assert (drawn[k][1] is None and ix is None) or np.array_equal(drawn[k][1], ix), k
