@@ -212,3 +212,22 @@ def test_each_kernel_variant(gpu, oracle_lib):
     }
     for name, meshes in batches.items():
         assert run_tiles(gpu, oracle_lib, W, meshes, 0, 9) >= 3, name
+
+
+@pytest.mark.parametrize("W", [101, 197])
+def test_road_layer_tiles_match_oracle(gpu, oracle_lib, W):
+    """layers.road_layer's meshes (strips with start and end caps, narrow roads left out)
+    drawn by the layer kernel, bit for bit against the oracle, both blend programs."""
+    from proland_gb300 import layers
+    rng = np.random.default_rng(5 + W)
+    meshes = []
+    for k in range(6):
+        roads = []
+        for r in range(3):
+            pts = np.column_stack([rng.uniform(-150, 1150, 4), rng.uniform(-150, 1150, 4)])
+            roads.append((pts, rng.uniform(-30, 250, 4), float(rng.uniform(4, 45)), bool((k + r) & 1),
+                          bool((k + r) & 2)))
+        roads.append((np.array([[0.0, 500.0], [1000.0, 520.0]]), [10.0, 20.0], 0.5))   # too narrow to draw
+        meshes.append(as_batch(layers.road_layer((0.0, 0.0), 1000.0, W, roads=roads)))
+    for blend_mode in (0, 1):
+        assert run_tiles(gpu, oracle_lib, W, meshes, blend_mode, W + blend_mode) >= 5
