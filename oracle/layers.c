@@ -27,8 +27,10 @@
  * a0 + (a1 - a0) l1 + (a2 - a0) l2 with l_k = e_k / (2 area) in float (a constant
  * attribute stays exact), fp32 depth clamped to [0, 1], triangles and their fragments
  * in draw order (GL's strip order (k+1, k, k+2) for odd k), each fragment tested
- * against the depth stored at its texel and written through the masks.  Parity with the GL path
- * is unpinned: the reference has no fixture for it.
+ * against the depth stored at its texel and written through the masks.  The fragment
+ * programs and both blends equal the reference's shaders compiled as C++
+ * (tests/test_oracle_vs_reference_gpu.py); the rasterisation rule is this oracle's, as the
+ * GL driver's is not source.
  */
 #include "oracle.h"
 
