@@ -655,6 +655,8 @@ def ref_lib():
         L.ref_gl_layer_fragment.argtypes = [C.c_int, C.c_int, C.c_float, _f32p, C.c_float, C.c_float, _f32p,
                                             C.POINTER(C.c_float)]
         L.ref_ortho_noise.argtypes = [C.c_int, C.c_void_p]
+        L.ref_gl_ortho_tile_channels.argtypes = [C.c_int] * 6 + [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, _f32p,
+                                                                 C.c_int, _f32p, _f32p, C.c_int, C.c_float, _f32p]
         L.ref_sphere_uniforms.argtypes = [C.c_int] * 4 + [C.c_float, _f32p]
         L.ref_residual_tile.argtypes = [C.c_char_p, C.c_int, C.c_float, C.c_int, C.c_int, C.c_int, C.c_int,
                                         C.c_void_p, C.POINTER(C.c_int)]

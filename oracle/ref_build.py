@@ -800,10 +800,27 @@ extern "C" int ref_gl_elevation_tile_layers(int variant, int blend_variant, int 
 // the HSV flag and the residual scale as OrthoProducer::init takes them.  out: what the
 // fragment shader writes (W*W*4 floats, result / 255), before the RGBA8 framebuffer
 // rounds it.  Returns 0.
+extern "C" int ref_gl_ortho_tile_channels(int variant, int W, int level, int tx, int ty, int face,
+                                          const unsigned char *parent, const unsigned char *residual, int channels,
+                                          const unsigned char *noise, const float *noise_amp, int n_amp,
+                                          const float *root_color, const float *noise_color, int hsv, float scale,
+                                          float *out);
 extern "C" int ref_gl_ortho_tile(int variant, int W, int level, int tx, int ty, int face, const unsigned char *parent,
                                  const unsigned char *residual, const unsigned char *noise, const float *noise_amp,
                                  int n_amp, const float *root_color, const float *noise_color, int hsv, float scale,
                                  float *out)
+{
+    return ref_gl_ortho_tile_channels(variant, W, level, tx, ty, face, parent, residual, 4, noise, noise_amp, n_amp,
+                                      root_color, noise_color, hsv, scale, out);
+}
+
+// The same with a residual producer of `channels` channels (residual: W*W*channels bytes),
+// which doCreateTile uploads as RED, RG, RGB or RGBA.
+extern "C" int ref_gl_ortho_tile_channels(int variant, int W, int level, int tx, int ty, int face,
+                                          const unsigned char *parent, const unsigned char *residual, int channels,
+                                          const unsigned char *noise, const float *noise_amp, int n_amp,
+                                          const float *root_color, const float *noise_color, int hsv, float scale,
+                                          float *out)
 {
     using namespace refgl;
     if (variant < 0 || variant >= (int)(sizeof(g_ortho) / sizeof(g_ortho[0]))) return 1;
@@ -841,6 +858,7 @@ extern "C" int ref_gl_ortho_tile(int variant, int W, int level, int tx, int ty, 
     o.noiseHsv = hsv != 0;
     o.scale = scale;
     o.face = face;
+    o.channels = channels;
     GPUTileStorage::GPUSlot parentSlot, outSlot;
     parentSlot.owner = outSlot.owner = &storage;
     parentSlot.t = &parentTex;

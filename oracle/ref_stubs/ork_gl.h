@@ -211,7 +211,8 @@ struct Texture {
 };
 struct Texture2D : Texture {
     // FLOAT or UNSIGNED_BYTE pixels of 1-4 components (RED, RG, RGB, RGBA) into the
-    // texture's first components; a byte k reads back as k / 255 (GL's unorm8)
+    // texture; a byte k reads back as k / 255 (GL's unorm8); as GL's pixel transfer does,
+    // components the pixels lack are 0, alpha 1
     void setSubImage(int, int x, int y, int w, int h, TextureFormat f, PixelType t, const Buffer::Parameters &,
                      const Buffer &pixels)
     {
@@ -219,10 +220,11 @@ struct Texture2D : Texture {
         const int n = f == RED ? 1 : f == RG ? 2 : f == RGB ? 3 : 4;
         for (int j = 0; j < h; ++j)
             for (int i = 0; i < w; ++i)
-                for (int k = 0; k < n; ++k) {
+                for (int k = 0; k < view.comps; ++k) {
                     const size_t s = ((size_t)j * w + i) * n + k;
-                    store[((size_t)(y + j) * view.w + x + i) * view.comps + k] =
-                        t == FLOAT ? ((const float *)src)[s] : (float)((const unsigned char *)src)[s] / 255.0f;
+                    float v = k == 3 ? 1.0f : 0.0f;
+                    if (k < n) v = t == FLOAT ? ((const float *)src)[s] : (float)((const unsigned char *)src)[s] / 255.0f;
+                    store[((size_t)(y + j) * view.w + x + i) * view.comps + k] = v;
                 }
     }
 };

@@ -723,3 +723,33 @@ def test_road_layer_draws(ref, product, seed):
         assert (test_on, func, depth_mask, z_mask, w_mask, rmode) == (1, 0, 1, 1, 1, mode), k
         assert np.array_equal(drawn[k][0], np.asarray(v, np.float32)), k
         assert (drawn[k][1] is None and ix is None) or np.array_equal(drawn[k][1], ix), k
+
+
+@pytest.mark.parametrize("channels", [1, 2, 3])
+def test_ortho_tiles_with_fewer_residual_channels(ref, oracle_lib, channels):
+    """A residual pyramid of 1-3 channels: OrthoProducer::doCreateTile uploads its tiles as
+    RED / RG / RGB into the RGBA residual texture (the missing components 0, alpha 1, as
+    GL's pixel transfer fills them); the oracle reads such a tile as rgba_words expands it.
+    Tiles byte for byte alike, RGB and HSV noise."""
+    import ctypes as C
+    W = 196
+    noise = np.empty((6, W, W, 4), np.uint8)
+    ref.ref_ortho_noise(W, noise.ctypes.data)
+    amps = np.float32([-1.0, 30.0, 20.0, 12.0, 8.0])
+    rng = np.random.default_rng(60 + channels)
+    for hsv in (False, True):
+        for level, tx, ty in [(0, 0, 0), (2, 3, 1), (4, 9, 14)]:
+            parent = rng.integers(0, 256, (W, W, 4)).astype(np.uint8) if level > 0 else None
+            res = np.ascontiguousarray(rng.integers(0, 256, (W, W, channels)).astype(np.uint8))
+            root_color = rng.uniform(0, 1, 4).astype(np.float32)
+            noise_color = rng.uniform(0.2, 1.5, 4).astype(np.float32)
+            out = np.empty((W, W, 4), np.float32)
+            assert ref.ref_gl_ortho_tile_channels(1, W, level, tx, ty, 0, None if parent is None else parent.ctypes.data,
+                                                  res.ctypes.data, channels, noise.ctypes.data, _p(amps), len(amps),
+                                                  _p(root_color), _p(noise_color), int(hsv), C.c_float(2.0),
+                                                  _p(out)) == 0
+            rot, layer = oracle_lib.noise_select(0, level, tx, ty)
+            want = oracle_lib.ortho_tile(W, level, tx, ty, parent, oracle_lib.rgba_words(res), noise[layer], rot,
+                                         float(amps[level]), root_color=root_color, noise_color=noise_color,
+                                         scale=2.0, hsv=hsv)
+            assert np.array_equal(_unorm8_even(out), want), (channels, hsv, level)
