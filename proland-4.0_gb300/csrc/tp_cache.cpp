@@ -1557,6 +1557,7 @@ struct tp_sampler {
     static constexpr int kMaxProducers = 8;
     struct Quad {
         uint64_t key;
+        uint64_t walk;   // its place in TileSampler's walk of the quadtree (walk_order)
         uint32_t stamp;  // the last update whose quadtree held it
         tp_tile *tiles[kMaxProducers];
     };
@@ -1659,7 +1660,7 @@ extern "C" int tp_sampler_update(tp_sampler *s, const tp_tile_req *reqs, int n, 
         }
         std::vector<std::pair<uint64_t, uint64_t> > gone;   // (walk order, quad key)
         for (const tp_sampler::Quad &q : s->held)
-            if (q.stamp != frame) gone.emplace_back(walk_order(q.key), q.key);
+            if (q.stamp != frame) gone.emplace_back(q.walk, q.key);
         std::sort(gone.begin(), gone.end());
         for (const auto &g : gone) sampler_drop(s, *s->index.find(g.second), false);
     }
@@ -1680,6 +1681,7 @@ extern "C" int tp_sampler_update(tp_sampler *s, const tp_tile_req *reqs, int n, 
             if (s->index.find(k)) continue;  // requested twice
             tp_sampler::Quad q;
             q.key = k;
+            q.walk = w.first;
             q.stamp = frame;
             size_t got = 0;
             for (; got < np; ++got) {
