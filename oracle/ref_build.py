@@ -2391,14 +2391,15 @@ def build(root=DEFAULT_ROOT, force=False):
     inc = ["-I", os.path.join(HERE, "ref_stubs"), "-I", os.path.join(root, NOISE_DIR),
            "-I", os.path.join(root, "src/core/sources/proland/math")]
     flags = ["-O2", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-w", "-DPROLAND_API="]
-    objs = []
-    for unit, std in ((gen, "c++14"), (gen_gpu, "c++17"), (gen_res, "c++17"), (gen_cache, "c++17"), (gen_quad, "c++17"),
-                      (gen_sampler, "c++17"),
-                      (os.path.join(root, NOISE_CPP), "c++14"),
-                      (os.path.join(root, MFS_CPP), "c++14")):
-        obj = os.path.join(GEN_DIR, os.path.basename(unit) + ".o")
-        subprocess.check_call(["g++", "-c", "-std=" + std] + flags + inc + ["-o", obj, unit])
-        objs.append(obj)
+    units = [(gen, "c++14"), (gen_gpu, "c++17"), (gen_res, "c++17"), (gen_cache, "c++17"), (gen_quad, "c++17"),
+             (gen_sampler, "c++17"), (os.path.join(root, NOISE_CPP), "c++14"), (os.path.join(root, MFS_CPP), "c++14")]
+    objs = [os.path.join(GEN_DIR, os.path.basename(unit) + ".o") for unit, _ in units]
+    import concurrent.futures as cf
+    with cf.ThreadPoolExecutor(max_workers=len(units)) as ex:
+        jobs = [ex.submit(subprocess.check_call, ["g++", "-c", "-std=" + std] + flags + inc + ["-o", obj, unit])
+                for (unit, std), obj in zip(units, objs)]
+        for j in jobs:
+            j.result()
     subprocess.check_call(["g++", "-shared", "-o", tmp] + objs + ["-lz", "-lpthread"])
     os.replace(tmp, LIB)
     return LIB
