@@ -25,6 +25,14 @@ as they are written, read from the reference tree at build time:
   the member functions as written, on a stand-in class holding ``tileSize`` and
   ``topLevelSize``.
 
+The preprocess pyramid, in its own unit (``ref_mipmap.cpp``): ``HeightMipmap``'s
+constructor, ``compute1``/``compute2``, ``readTile``, ``buildBaseLevelTiles``,
+``buildMipmapLevel``, ``buildResiduals``, ``getTileHeight``, ``reset``, ``getTile``,
+``getApproxTile``/``saveApproxTile`` and the residual functions (``HeightMipmap.cpp``),
+``AbstractTileCache``'s LRU ``getTile``, clamped ``getTileHeight`` and ``reset``
+(``AbstractTileCache.cpp``) and ``rotation`` (``ColorMipmap.cpp``), on stand-in class
+declarations and libtiff's writer over in-memory files.
+
 The GPU path, in a second unit (``ref_gpu.cpp``):
 
 * ``ElevationProducer::doCreateTile`` (``ElevationProducer.cpp:280-405``, its layered
@@ -338,6 +346,269 @@ extern "C" void ref_compute_approx_tile(int tile_size, int top_level_size, float
 """)
     os.makedirs(GEN_DIR, exist_ok=True)
     path = os.path.join(GEN_DIR, "ref_pieces.cpp")
+    with open(path, "w") as f:
+        f.write("".join(src))
+    return path
+
+
+# ---- the preprocess pyramid: HeightMipmap's levels and residuals -----------------------
+TILE_CACHE_CPP = "src/terrain/sources/proland/preprocess/terrain/AbstractTileCache.cpp"
+COLOR_MIPMAP_CPP = "src/terrain/sources/proland/preprocess/terrain/ColorMipmap.cpp"
+_MIPMAP_PRELUDE = r"""
+#include <assert.h>
+#include <math.h>
+#include <stdint.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <algorithm>
+#include <list>
+#include <map>
+#include <string>
+#include <vector>
+
+#define printf(...) ((void)0)
+
+namespace refmip {
+using std::list;
+using std::map;
+using std::max;
+using std::min;
+using std::string;
+
+// libtiff's writer and directory reader over files held in memory.  A file is its list of
+// directories, a directory the one strip written into it: the pyramid's tiles are one
+// Deflate strip each, and reading a lossless strip back gives the bytes written.
+typedef int32_t tsize_t;
+enum {
+    TIFFTAG_IMAGEWIDTH = 256, TIFFTAG_IMAGELENGTH = 257, TIFFTAG_BITSPERSAMPLE = 258, TIFFTAG_COMPRESSION = 259,
+    TIFFTAG_PHOTOMETRIC = 262, TIFFTAG_ORIENTATION = 274, TIFFTAG_SAMPLESPERPIXEL = 277, TIFFTAG_PLANARCONFIG = 284,
+    COMPRESSION_DEFLATE = 32946, ORIENTATION_BOTLEFT = 4, PLANARCONFIG_CONTIG = 1, PHOTOMETRIC_MINISBLACK = 1
+};
+typedef std::vector<std::vector<unsigned char>> MemTiff;
+static map<string, MemTiff> g_tiff;
+struct TIFF {
+    string name;
+    bool writing;
+    MemTiff dirs;
+    std::vector<unsigned char> strip;
+    int dir;
+};
+TIFF *TIFFOpen(const char *name, const char *mode)
+{
+    TIFF *f = new TIFF{name, mode[0] == 'w', MemTiff(), {}, 0};
+    if (!f->writing) {
+        auto i = g_tiff.find(name);
+        if (i == g_tiff.end()) {
+            delete f;
+            return nullptr;
+        }
+        f->dirs = i->second;
+    }
+    return f;
+}
+int TIFFSetField(TIFF *, int, ...) { return 1; }
+tsize_t TIFFWriteEncodedStrip(TIFF *f, int, void *data, tsize_t size)
+{
+    const unsigned char *p = (const unsigned char *)data;
+    f->strip.assign(p, p + size);
+    return size;
+}
+int TIFFWriteDirectory(TIFF *f)
+{
+    f->dirs.push_back(f->strip);
+    f->strip.clear();
+    return 1;
+}
+int TIFFSetDirectory(TIFF *f, int d)
+{
+    f->dir = d;
+    return d < (int)f->dirs.size();
+}
+tsize_t TIFFReadEncodedStrip(TIFF *f, int, void *buf, tsize_t)
+{
+    if (f->dir >= (int)f->dirs.size()) return -1;
+    const std::vector<unsigned char> &s = f->dirs[f->dir];
+    memcpy(buf, s.data(), s.size());
+    return (tsize_t)s.size();
+}
+void TIFFClose(TIFF *f)
+{
+    if (f->writing) g_tiff[f->name] = f->dirs;
+    delete f;
+}
+// Util.cpp's flog: whether a file is still to be made (its log-file restart is left out)
+bool flog(const string &name) { return g_tiff.find(name) == g_tiff.end(); }
+// Ork's fopen(FILE **, name, mode)
+inline void fopen(FILE **f, const char *name, const char *mode) { *f = ::fopen(name, mode); }
+
+// AbstractTileCache.h and HeightMipmap.h: the classes' members and virtual functions,
+// all public so that the test driver can set the current level
+struct vec4f {
+    float x, y, z, w;
+};
+struct AbstractTileCache {
+    struct Tile {
+        int tx, ty;
+        unsigned char *data;
+        Tile(int tx, int ty, unsigned char *data = NULL) : tx(tx), ty(ty), data(data) {}
+        ~Tile() { delete[] data; }
+        int key(int width) { return tx + ty * width; }
+    };
+    AbstractTileCache(int width, int height, int tileSize, int channels, int capacity = 20)
+        : width(width), height(height), tileSize(tileSize), channels(channels), capacity(capacity) {}
+    virtual ~AbstractTileCache() { reset(0, 0, 0); }
+    int getWidth() { return width; }
+    int getHeight() { return height; }
+    int getTileSize() { return tileSize; }
+    unsigned char *getTile(int tx, int ty);
+    virtual float getTileHeight(int x, int y);
+    virtual void reset(int width, int height, int tileSize);
+    virtual unsigned char *readTile(int tx, int ty) = 0;
+    int width, height, tileSize, channels, capacity;
+    typedef map<int, list<Tile *>::iterator> Cache;
+    Cache tileCache;
+    list<Tile *> tileCacheOrder;
+};
+struct HeightMipmap : AbstractTileCache {
+    struct HeightFunction {
+        virtual float getHeight(int x, int y) = 0;
+    };
+    HeightMipmap *left, *right, *bottom, *top;
+    int leftr, rightr, bottomr, topr;
+    HeightMipmap(HeightFunction *height, int topLevelSize, int baseLevelSize, int tileSize, float scale,
+                 const string &cache);
+    ~HeightMipmap();
+    void compute1();
+    bool compute2();
+    virtual float getTileHeight(int x, int y);
+    virtual void reset(int width, int height, int tileSize);
+    virtual unsigned char *readTile(int tx, int ty);
+    virtual void getTile(int level, int tx, int ty, float *tile);
+    HeightFunction *height;
+    int topLevelSize, baseLevelSize, tileSize;
+    float scale;
+    string cache;
+    int minLevel, maxLevel, currentMipLevel;
+    unsigned char *tile;
+    int currentLevel, constantTile;
+    void buildBaseLevelTiles();
+    void buildBaseLevelTile(int tx, int ty, TIFF *f);
+    void buildMipmapLevel(int level);
+    void buildResiduals(int level);
+    void getApproxTile(int level, int tx, int ty, float *tile);
+    void saveApproxTile(int level, int tx, int ty, float *tile);
+    void computeResidual(float *parentTile, float *tile, int level, int tx, int ty, float *residual, float &maxR,
+                         float &meanR);
+    void encodeResidual(int level, float *residual, unsigned char *encoded);
+    void computeApproxTile(float *parentTile, float *residual, int level, int tx, int ty, float *tile, float &maxErr);
+};
+"""
+
+_MIPMAP_DRIVER = r"""
+// the input map: int16 samples on a (baseLevelSize + 1)^2 grid, read with clamped coordinates
+struct GridHeights : HeightMipmap::HeightFunction {
+    const int16_t *h = nullptr;
+    int n = 0;
+    float getHeight(int x, int y)
+    {
+        x = x < 0 ? 0 : (x > n - 1 ? n - 1 : x);
+        y = y < 0 ? 0 : (y > n - 1 ? n - 1 : y);
+        return h[(size_t)y * n + x];
+    }
+};
+static HeightMipmap *g_mip = nullptr;
+static GridHeights g_heights;
+}  // namespace refmip
+
+using namespace refmip;
+
+// HeightMipmap's pyramid of `base` ((ts << max_level) + 1 square): compute1 (base-level
+// tiles), compute2 until it is done (the levels below), then buildResiduals for levels
+// 1..max_level, as HeightMipmap::generate runs them.  The approximation tiles go to files
+// in `dir`.  Returns maxLevel.
+extern "C" int ref_mipmap_build(const int16_t *base, int ts, int max_level, float scale, const char *dir)
+{
+    delete g_mip;
+    g_tiff.clear();
+    g_heights.h = base;
+    g_heights.n = (ts << max_level) + 1;
+    g_mip = new HeightMipmap(&g_heights, ts, ts << max_level, ts, scale, dir);
+    g_mip->compute1();
+    while (g_mip->compute2()) {
+    }
+    for (int level = 1; level <= g_mip->maxLevel; ++level) g_mip->buildResiduals(level);
+    g_heights.h = nullptr;
+    return g_mip->maxLevel;
+}
+
+// HeightMipmap::getTile of (level, tx, ty), the cache set to that level as buildResiduals
+// sets it: (ts + 5)^2 floats
+extern "C" void ref_mipmap_level_tile(int level, int tx, int ty, float *out)
+{
+    HeightMipmap *m = g_mip;
+    m->currentLevel = level;
+    const int n = m->baseLevelSize >> (m->maxLevel - level);
+    m->reset(n, n, min(m->topLevelSize << level, m->tileSize));
+    m->getTile(level, tx, ty, out);
+}
+
+// the approximation tile of (level, tx, ty) (level < maxLevel): getApproxTile, (ts + 5)^2 floats
+extern "C" void ref_mipmap_approx_tile(int level, int tx, int ty, float *out)
+{
+    g_mip->getApproxTile(level, tx, ty, out);
+}
+
+// the encoded residual of (level, tx, ty) from buildResiduals' files: its byte count, or -1
+extern "C" int ref_mipmap_residual(int level, int tx, int ty, unsigned char *out, int cap)
+{
+    HeightMipmap *m = g_mip;
+    const int nTiles = max(1, (m->baseLevelSize / m->tileSize) >> (m->maxLevel - level));
+    const int per = min(nTiles, 16);
+    char name[512];
+    snprintf(name, sizeof(name), "%s/residual-%.2d-%.4d-%.4d.tiff", m->cache.c_str(), level, tx / per, ty / per);
+    auto i = g_tiff.find(name);
+    const int d = tx % per + (ty % per) * per;
+    if (i == g_tiff.end() || d >= (int)i->second.size() || (int)i->second[d].size() > cap) return -1;
+    memcpy(out, i->second[d].data(), i->second[d].size());
+    return (int)i->second[d].size();
+}
+
+extern "C" void ref_mipmap_free()
+{
+    delete g_mip;
+    g_mip = nullptr;
+    g_tiff.clear();
+}
+"""
+
+
+def generate_mipmap(root):
+    """oracle/_ref/gen/ref_mipmap.cpp: HeightMipmap's pyramid build as written -- base-level
+    tiles, decimated levels, the residual chain -- with AbstractTileCache's tile cache and
+    clamped reads, against in-memory TIFF files."""
+    mip = _read(root, MIPMAP_CPP)
+    src = ["// generated by oracle/ref_build.py from the reference's sources\n", _MIPMAP_PRELUDE]
+    tc = _read(root, TILE_CACHE_CPP)
+    for sig in (r"unsigned char\s*\*\s*AbstractTileCache::getTile\s*\(", r"float\s+AbstractTileCache::getTileHeight\s*\(",
+                r"void\s+AbstractTileCache::reset\s*\("):
+        body, line = extract_function(tc, sig)
+        src.append("// %s:%d\n%s" % (TILE_CACHE_CPP, line, body))
+    body, line = extract_function(_read(root, COLOR_MIPMAP_CPP), r"void\s+rotation\s*\(\s*int\s+r\s*,.*\)\s*$")
+    src.append("// %s:%d\n%s" % (COLOR_MIPMAP_CPP, line, body))
+    for sig in (r"HeightMipmap::HeightMipmap\s*\(", r"HeightMipmap::~HeightMipmap\s*\(", r"void\s+HeightMipmap::compute1\s*\(",
+                r"bool\s+HeightMipmap::compute2\s*\(", r"unsigned char\s*\*\s*HeightMipmap::readTile\s*\(",
+                r"void\s+HeightMipmap::buildBaseLevelTiles\s*\(", r"void\s+HeightMipmap::buildBaseLevelTile\s*\(",
+                r"void\s+HeightMipmap::buildMipmapLevel\s*\(", r"void\s+HeightMipmap::buildResiduals\s*\(",
+                r"float\s+HeightMipmap::getTileHeight\s*\(", r"void\s+HeightMipmap::reset\s*\(",
+                r"void\s+HeightMipmap::getTile\s*\(", r"void\s+HeightMipmap::getApproxTile\s*\(",
+                r"void\s+HeightMipmap::saveApproxTile\s*\(", r"void\s+HeightMipmap::computeResidual\s*\(",
+                r"void\s+HeightMipmap::encodeResidual\s*\(", r"void\s+HeightMipmap::computeApproxTile\s*\("):
+        body, line = extract_function(mip, sig)
+        src.append("// %s:%d\n%s" % (MIPMAP_CPP, line, body))
+    src.append(_MIPMAP_DRIVER)
+    os.makedirs(GEN_DIR, exist_ok=True)
+    path = os.path.join(GEN_DIR, "ref_mipmap.cpp")
     with open(path, "w") as f:
         f.write("".join(src))
     return path
@@ -2374,7 +2645,7 @@ def build(root=DEFAULT_ROOT, force=False):
                                             GRAPH_LAYER_CPP, ROAD_LAYER_CPP, GRAPH_PRODUCER_CPP, WATER_LAYER_CPP,
                                             RESIDUAL_CPP,
                                             ORTHO_CPU_CPP, MFS_CPP, CACHE_CPP, STORAGE_CPP, QUAD_CPP, NODE_CPP,
-                                            PRODUCER_CPP, SAMPLER_CPP)]
+                                            PRODUCER_CPP, SAMPLER_CPP, TILE_CACHE_CPP, COLOR_MIPMAP_CPP)]
     srcs += [os.path.join(root, rel) for _, rel, _ in UPSAMPLE_SHADERS + NORMAL_SHADERS + BLEND_SHADERS +
              LAYER_SHADERS + ORTHO_SHADERS]
     srcs += [os.path.abspath(__file__), os.path.join(HERE, "ref_glsl.py")]
@@ -2387,12 +2658,13 @@ def build(root=DEFAULT_ROOT, force=False):
     gen_cache = generate_cache(root)
     gen_quad = generate_quadtree(root)
     gen_sampler = generate_sampler(root)
+    gen_mip = generate_mipmap(root)
     tmp = LIB + ".tmp%d" % os.getpid()
     inc = ["-I", os.path.join(HERE, "ref_stubs"), "-I", os.path.join(root, NOISE_DIR),
            "-I", os.path.join(root, "src/core/sources/proland/math")]
     flags = ["-O2", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-w", "-DPROLAND_API="]
     units = [(gen, "c++14"), (gen_gpu, "c++17"), (gen_res, "c++17"), (gen_cache, "c++17"), (gen_quad, "c++17"),
-             (gen_sampler, "c++17"), (os.path.join(root, NOISE_CPP), "c++14"), (os.path.join(root, MFS_CPP), "c++14")]
+             (gen_sampler, "c++17"), (gen_mip, "c++17"), (os.path.join(root, NOISE_CPP), "c++14"), (os.path.join(root, MFS_CPP), "c++14")]
     objs = [os.path.join(GEN_DIR, os.path.basename(unit) + ".o") for unit, _ in units]
     import concurrent.futures as cf
     with cf.ThreadPoolExecutor(max_workers=len(units)) as ex:

@@ -2,8 +2,9 @@
 sources by oracle/ref_build.py (oracle/_ref/libref.so): the LCG and cnoise of
 math/noise.h / noise.cpp, createDemNoise's table (ElevationProducer.cpp:50-133),
 the noise-layer choice (ElevationProducer.cpp:345-376), CPUElevationProducer's
-residual addressing and stencil loop (CPUElevationProducer.cpp:178-245) and
-HeightMipmap's residual / encode / approximation functions (HeightMipmap.cpp:449-559).
+residual addressing and stencil loop (CPUElevationProducer.cpp:178-245),
+HeightMipmap's residual / encode / approximation functions (HeightMipmap.cpp:449-559)
+and its whole pyramid build (base-level tiles, decimated levels, residual chain).
 Every comparison is bit for bit.  The product's host-side noise code is checked
 against the same compiled reference; its CUDA kernels are checked against the
 oracle by the GPU tests, which this pin anchors.
@@ -132,3 +133,42 @@ def test_heightmipmap_residual_encode_approx(ref, oracle_lib, W):
         err = C.c_float()
         ref.ref_compute_approx_tile(n, n, _f(parent), _f(res), 3, tx, ty, _f(tile), C.byref(err))
         assert np.array_equal(tile, approx)
+
+
+@pytest.mark.parametrize("ts,max_level,scale,seed", [(8, 5, 1.0, 3), (12, 3, 4.0, 7), (24, 2, 2.5, 11)])
+def test_heightmipmap_pyramid(ref, oracle_lib, tmp_path, ts, max_level, scale, seed):
+    """HeightMipmap's whole pyramid build (HeightMipmap.cpp:83-97, 131-323, 327-559, with
+    AbstractTileCache.cpp's tile cache and clamped reads): the base-level tiles, each
+    coarser level decimated from the one above, and the residual chain of buildResiduals
+    (encoded residuals and the approximation tiles saved for the next level), against the
+    oracle's level tiles (or_level_tile) and residual chain (or_compute_residual), bit for
+    bit.  The (8, 5) case has 32 x 32 tiles at the finest level, two files of 16 x 16
+    tiles a side."""
+    base = oracle_lib.fbm_heights((ts << max_level) + 1, octaves=8, base_cells=2, seed=seed)
+    assert ref.ref_mipmap_build(base.ctypes.data_as(C.POINTER(C.c_int16)), ts, max_level, scale,
+                                str(tmp_path).encode()) == max_level
+    W = ts + 5
+    try:
+        got = np.empty((W, W), np.float32)
+        prev = {}
+        for level in range(max_level + 1):
+            cur = {}
+            for ty in range(1 << level):
+                for tx in range(1 << level):
+                    want = oracle_lib.level_tile(base, ts, max_level, level, tx, ty, scale)
+                    ref.ref_mipmap_level_tile(level, tx, ty, _f(got))
+                    assert np.array_equal(got, want), (level, tx, ty)
+                    if level == 0:
+                        cur[tx, ty] = want
+                        continue
+                    _, enc, approx = oracle_lib.compute_residual(W, tx, ty, prev[tx // 2, ty // 2], want)
+                    raw = np.zeros(2 * W * W, np.uint8)
+                    assert ref.ref_mipmap_residual(level, tx, ty, raw.ctypes.data, raw.size) == raw.size
+                    assert np.array_equal(raw.view("<i2").reshape(W, W), enc), (level, tx, ty)
+                    if level < max_level:
+                        ref.ref_mipmap_approx_tile(level, tx, ty, _f(got))
+                        assert np.array_equal(got, approx), (level, tx, ty)
+                    cur[tx, ty] = approx
+            prev = cur
+    finally:
+        ref.ref_mipmap_free()
