@@ -651,6 +651,8 @@ def ref_lib():
         L.ref_mipmap_level_tile.argtypes = [C.c_int] * 3 + [_f32p]
         L.ref_mipmap_approx_tile.argtypes = [C.c_int] * 3 + [_f32p]
         L.ref_mipmap_residual.argtypes = [C.c_int] * 3 + [C.c_void_p, C.c_int]
+        L.ref_mipmap_build_sized.argtypes = [C.POINTER(C.c_int16), C.c_int, C.c_int, C.c_int, C.c_float, C.c_char_p]
+        L.ref_mipmap_generate.argtypes = [C.c_int] * 3 + [C.c_float, C.c_char_p]
         L.ref_gl_elevation_tile.argtypes = [C.c_int] * 6 + [_f32p, _f32p, C.c_int, _f32p, _f32p, C.c_int,
                                                             C.c_float, C.c_int, C.c_int, _f32p]
         L.ref_gl_normal_tile.argtypes = [C.c_int] * 5 + [_f32p, C.c_int, _f32p, C.c_float, C.c_int, C.c_int, _f32p]

@@ -28,10 +28,12 @@ as they are written, read from the reference tree at build time:
 The preprocess pyramid, in its own unit (``ref_mipmap.cpp``): ``HeightMipmap``'s
 constructor, ``compute1``/``compute2``, ``readTile``, ``buildBaseLevelTiles``,
 ``buildMipmapLevel``, ``buildResiduals``, ``getTileHeight``, ``reset``, ``getTile``,
-``getApproxTile``/``saveApproxTile`` and the residual functions (``HeightMipmap.cpp``),
+``getApproxTile``/``saveApproxTile``, the residual functions and the ``.dat`` writer
+``generate``/``produceTile``/``produceTilesLebeguesOrder`` (``HeightMipmap.cpp``),
 ``AbstractTileCache``'s LRU ``getTile``, clamped ``getTileHeight`` and ``reset``
 (``AbstractTileCache.cpp``) and ``rotation`` (``ColorMipmap.cpp``), on stand-in class
-declarations and libtiff's writer over in-memory files.
+declarations and libtiff's writer over in-memory files (client-procedure files written
+out as TIFF 6.0 with a zlib strip, for the ``.dat`` tiles through ``mfs.cpp``).
 
 The GPU path, in a second unit (``ref_gpu.cpp``):
 
@@ -357,15 +359,20 @@ COLOR_MIPMAP_CPP = "src/terrain/sources/proland/preprocess/terrain/ColorMipmap.c
 _MIPMAP_PRELUDE = r"""
 #include <assert.h>
 #include <math.h>
+#include <stdarg.h>
 #include <stdint.h>
 #include <stdio.h>
+#include <stdlib.h>
 #include <string.h>
+#include <zlib.h>
 
 #include <algorithm>
 #include <list>
 #include <map>
 #include <string>
 #include <vector>
+
+#include "proland/util/mfs.h"
 
 #define printf(...) ((void)0)
 
@@ -378,8 +385,20 @@ using std::string;
 
 // libtiff's writer and directory reader over files held in memory.  A file is its list of
 // directories, a directory the one strip written into it: the pyramid's tiles are one
-// Deflate strip each, and reading a lossless strip back gives the bytes written.
+// Deflate strip each, and reading a lossless strip back gives the bytes written.  A file
+// opened on client procedures (TIFFClientOpen, how HeightMipmap::produceTile writes the
+// .dat tiles) is written out at TIFFClose as a little-endian TIFF 6.0 file: the header,
+// the strip compressed by zlib at the default level (libtiff's Deflate), then one image
+// directory with the fields set on it and the strip's offset, byte count and row count.
 typedef int32_t tsize_t;
+typedef uint32_t toff_t;
+typedef void *thandle_t;
+typedef tsize_t (*TIFFReadWriteProc)(thandle_t, void *, tsize_t);
+typedef toff_t (*TIFFSeekProc)(thandle_t, toff_t, int);
+typedef int (*TIFFCloseProc)(thandle_t);
+typedef toff_t (*TIFFSizeProc)(thandle_t);
+typedef int (*TIFFMapFileProc)(thandle_t, void **, toff_t *);
+typedef void (*TIFFUnmapFileProc)(thandle_t, void *, toff_t);
 enum {
     TIFFTAG_IMAGEWIDTH = 256, TIFFTAG_IMAGELENGTH = 257, TIFFTAG_BITSPERSAMPLE = 258, TIFFTAG_COMPRESSION = 259,
     TIFFTAG_PHOTOMETRIC = 262, TIFFTAG_ORIENTATION = 274, TIFFTAG_SAMPLESPERPIXEL = 277, TIFFTAG_PLANARCONFIG = 284,
@@ -393,6 +412,11 @@ struct TIFF {
     MemTiff dirs;
     std::vector<unsigned char> strip;
     int dir;
+    thandle_t handle = nullptr;  // client procedures, when opened on them
+    TIFFReadWriteProc write = nullptr;
+    TIFFSeekProc seek = nullptr;
+    TIFFCloseProc close = nullptr;
+    map<int, uint32_t> fields;
 };
 TIFF *TIFFOpen(const char *name, const char *mode)
 {
@@ -407,7 +431,67 @@ TIFF *TIFFOpen(const char *name, const char *mode)
     }
     return f;
 }
-int TIFFSetField(TIFF *, int, ...) { return 1; }
+TIFF *TIFFClientOpen(const char *name, const char *, thandle_t h, TIFFReadWriteProc, TIFFReadWriteProc wr,
+                     TIFFSeekProc sk, TIFFCloseProc cl, TIFFSizeProc, TIFFMapFileProc, TIFFUnmapFileProc)
+{
+    TIFF *f = new TIFF{name, true, MemTiff(), {}, 0};
+    f->handle = h;
+    f->write = wr;
+    f->seek = sk;
+    f->close = cl;
+    return f;
+}
+int TIFFSetField(TIFF *f, int tag, ...)
+{
+    va_list ap;
+    va_start(ap, tag);
+    f->fields[tag] = va_arg(ap, uint32_t);
+    va_end(ap);
+    return 1;
+}
+static void tiff_put(std::vector<unsigned char> &b, uint32_t v, int n)
+{
+    for (int k = 0; k < n; ++k) b.push_back((unsigned char)(v >> (8 * k)));
+}
+// the client file of TIFFClose: header, compressed strip, image directory
+static void tiff_write_client(TIFF *f)
+{
+    const std::vector<unsigned char> &raw = f->dirs.empty() ? f->strip : f->dirs[0];
+    uLongf zn = compressBound(raw.size());
+    std::vector<unsigned char> z(zn);
+    compress2(z.data(), &zn, raw.data(), raw.size(), Z_DEFAULT_COMPRESSION);
+    z.resize(zn);
+    std::vector<unsigned char> b = {'I', 'I'};
+    tiff_put(b, 42, 2);
+    tiff_put(b, 8 + (uint32_t)((z.size() + 1) & ~(size_t)1), 4);
+    b.insert(b.end(), z.begin(), z.end());
+    if (b.size() & 1) b.push_back(0);
+    map<int, uint32_t> fl = f->fields;
+    if (!fl.count(TIFFTAG_COMPRESSION)) fl[TIFFTAG_COMPRESSION] = 1;
+    fl[273] = 8;                        // StripOffsets
+    fl[278] = fl[TIFFTAG_IMAGELENGTH];  // RowsPerStrip
+    fl[279] = (uint32_t)z.size();       // StripByteCounts
+    const uint32_t spp = fl.count(TIFFTAG_SAMPLESPERPIXEL) ? fl[TIFFTAG_SAMPLESPERPIXEL] : 1;
+    tiff_put(b, (uint32_t)fl.size(), 2);
+    for (auto &e : fl) {
+        const bool wide = e.first == 256 || e.first == 257 || e.first == 273 || e.first == 278 || e.first == 279;
+        const uint32_t count = e.first == TIFFTAG_BITSPERSAMPLE ? spp : 1;
+        tiff_put(b, e.first, 2);
+        tiff_put(b, wide ? 4 : 3, 2);
+        tiff_put(b, count, 4);
+        if (wide) {
+            tiff_put(b, e.second, 4);
+        } else {
+            // up to two SHORTs fit in the entry; the pyramid's tiles have at most two samples
+            tiff_put(b, e.second, 2);
+            tiff_put(b, count > 1 ? e.second : 0, 2);
+        }
+    }
+    tiff_put(b, 0, 4);
+    f->seek(f->handle, 0, SEEK_SET);
+    f->write(f->handle, b.data(), (tsize_t)b.size());
+    f->close(f->handle);
+}
 tsize_t TIFFWriteEncodedStrip(TIFF *f, int, void *data, tsize_t size)
 {
     const unsigned char *p = (const unsigned char *)data;
@@ -434,7 +518,11 @@ tsize_t TIFFReadEncodedStrip(TIFF *f, int, void *buf, tsize_t)
 }
 void TIFFClose(TIFF *f)
 {
-    if (f->writing) g_tiff[f->name] = f->dirs;
+    if (f->write) {
+        tiff_write_client(f);
+    } else if (f->writing) {
+        g_tiff[f->name] = f->dirs;
+    }
     delete f;
 }
 // Util.cpp's flog: whether a file is still to be made (its log-file restart is left out)
@@ -492,6 +580,7 @@ struct HeightMipmap : AbstractTileCache {
     int minLevel, maxLevel, currentMipLevel;
     unsigned char *tile;
     int currentLevel, constantTile;
+    void generate(int rootLevel, int rootTx, int rootTy, float scale, const string &file);
     void buildBaseLevelTiles();
     void buildBaseLevelTile(int tx, int ty, TIFF *f);
     void buildMipmapLevel(int level);
@@ -502,6 +591,9 @@ struct HeightMipmap : AbstractTileCache {
                          float &meanR);
     void encodeResidual(int level, float *residual, unsigned char *encoded);
     void computeApproxTile(float *parentTile, float *residual, int level, int tx, int ty, float *tile, float &maxErr);
+    void produceTile(int level, int tx, int ty, unsigned int *offset, unsigned int *offsets, FILE *f);
+    void produceTilesLebeguesOrder(int l, int level, int tx, int ty, unsigned int *offset, unsigned int *offsets,
+                                   FILE *f);
 };
 """
 
@@ -523,23 +615,36 @@ static GridHeights g_heights;
 
 using namespace refmip;
 
-// HeightMipmap's pyramid of `base` ((ts << max_level) + 1 square): compute1 (base-level
-// tiles), compute2 until it is done (the levels below), then buildResiduals for levels
-// 1..max_level, as HeightMipmap::generate runs them.  The approximation tiles go to files
-// in `dir`.  Returns maxLevel.
-extern "C" int ref_mipmap_build(const int16_t *base, int ts, int max_level, float scale, const char *dir)
+// HeightMipmap's pyramid of `base` ((top << max_level) + 1 square, tiles of ts >= top
+// intervals): compute1 (base-level tiles), compute2 until it is done (the levels below),
+// then buildResiduals for levels 1..max_level, as HeightMipmap::generate runs them.  The
+// approximation tiles go to files in `dir`.  Returns maxLevel.
+extern "C" int ref_mipmap_build_sized(const int16_t *base, int top, int ts, int max_level, float scale,
+                                      const char *dir)
 {
     delete g_mip;
     g_tiff.clear();
     g_heights.h = base;
-    g_heights.n = (ts << max_level) + 1;
-    g_mip = new HeightMipmap(&g_heights, ts, ts << max_level, ts, scale, dir);
+    g_heights.n = (top << max_level) + 1;
+    g_mip = new HeightMipmap(&g_heights, top, top << max_level, ts, scale, dir);
     g_mip->compute1();
     while (g_mip->compute2()) {
     }
     for (int level = 1; level <= g_mip->maxLevel; ++level) g_mip->buildResiduals(level);
     g_heights.h = nullptr;
     return g_mip->maxLevel;
+}
+extern "C" int ref_mipmap_build(const int16_t *base, int ts, int max_level, float scale, const char *dir)
+{
+    return ref_mipmap_build_sized(base, ts, ts, max_level, scale, dir);
+}
+
+// HeightMipmap::generate after ref_mipmap_build_sized: the .dat pyramid file at `path`
+// (its residual levels are built already, so generate only writes the file); minLevel
+extern "C" int ref_mipmap_generate(int root_level, int root_tx, int root_ty, float scale, const char *path)
+{
+    g_mip->generate(root_level, root_tx, root_ty, scale, path);
+    return g_mip->minLevel;
 }
 
 // HeightMipmap::getTile of (level, tx, ty), the cache set to that level as buildResiduals
@@ -603,7 +708,9 @@ def generate_mipmap(root):
                 r"float\s+HeightMipmap::getTileHeight\s*\(", r"void\s+HeightMipmap::reset\s*\(",
                 r"void\s+HeightMipmap::getTile\s*\(", r"void\s+HeightMipmap::getApproxTile\s*\(",
                 r"void\s+HeightMipmap::saveApproxTile\s*\(", r"void\s+HeightMipmap::computeResidual\s*\(",
-                r"void\s+HeightMipmap::encodeResidual\s*\(", r"void\s+HeightMipmap::computeApproxTile\s*\("):
+                r"void\s+HeightMipmap::encodeResidual\s*\(", r"void\s+HeightMipmap::computeApproxTile\s*\(",
+                r"void\s+HeightMipmap::generate\s*\(", r"void\s+HeightMipmap::produceTile\s*\(",
+                r"void\s+HeightMipmap::produceTilesLebeguesOrder\s*\("):
         body, line = extract_function(mip, sig)
         src.append("// %s:%d\n%s" % (MIPMAP_CPP, line, body))
     src.append(_MIPMAP_DRIVER)

@@ -3,8 +3,9 @@ sources by oracle/ref_build.py (oracle/_ref/libref.so): the LCG and cnoise of
 math/noise.h / noise.cpp, createDemNoise's table (ElevationProducer.cpp:50-133),
 the noise-layer choice (ElevationProducer.cpp:345-376), CPUElevationProducer's
 residual addressing and stencil loop (CPUElevationProducer.cpp:178-245),
-HeightMipmap's residual / encode / approximation functions (HeightMipmap.cpp:449-559)
-and its whole pyramid build (base-level tiles, decimated levels, residual chain).
+HeightMipmap's residual / encode / approximation functions (HeightMipmap.cpp:449-559),
+its whole pyramid build (base-level tiles, decimated levels, residual chain) and the
+.dat files its generate writes, read back by the library's and the oracle's readers.
 Every comparison is bit for bit.  The product's host-side noise code is checked
 against the same compiled reference; its CUDA kernels are checked against the
 oracle by the GPU tests, which this pin anchors.
@@ -170,5 +171,60 @@ def test_heightmipmap_pyramid(ref, oracle_lib, tmp_path, ts, max_level, scale, s
                         assert np.array_equal(got, approx), (level, tx, ty)
                     cur[tx, ty] = approx
             prev = cur
+    finally:
+        ref.ref_mipmap_free()
+
+
+def _roundf(x32):
+    """C's roundf (half away from zero) of float32 values, exactly."""
+    x = np.asarray(x32, np.float64)
+    return np.sign(x) * np.floor(np.abs(x) + 0.5)
+
+
+@pytest.mark.parametrize("top,ts,max_level,scale,root", [(8, 8, 4, 1.0, (0, 0, 0)), (6, 24, 4, 2.0, (2, 1, 3)),
+                                                         (12, 12, 3, 0.5, (5, 17, 9))])
+def test_heightmipmap_dat_file_reads_back(ref, oracle_lib, product, tmp_path, top, ts, max_level, scale, root):
+    """HeightMipmap::generate's .dat file (HeightMipmap.cpp:99-129, 561-654: the header, the
+    tile offsets in Lebesgue order, all-zero tiles sharing the first one's bytes, each tile
+    a Deflate TIFF), written by the reference's code through a TIFF writer stand-in, read
+    back by the library's own .dat reader and the oracle's: the header, and every tile equal to the residual
+    buildResiduals encoded; the root tile is the level-0 heights over the scale, rounded.
+    (6, 24) has minLevel 2: levels 0 and 1 are single tiles of 6 and 12 intervals.  The
+    lower-left quadrant of the terrain is flat, so its residual tiles are all zero."""
+    n = (top << max_level) + 1
+    base = oracle_lib.fbm_heights(n, octaves=8, base_cells=2, seed=ts + max_level)
+    base[: n // 2, : n // 2] = 1234
+    assert ref.ref_mipmap_build_sized(base.ctypes.data_as(C.POINTER(C.c_int16)), top, ts, max_level, scale,
+                                      str(tmp_path).encode()) == max_level
+    path = str(tmp_path / "pyramid.dat")
+    try:
+        min_level = ref.ref_mipmap_generate(*root, scale, path.encode())
+        d = product.DatPyramid(path)
+        od = oracle_lib.DatFile.open(path)
+        ntiles = min_level + ((1 << (2 * (max_level - min_level) + 2)) - 1) // 3
+        assert [d.min_level, d.max_level, d.tile_size, d.root_level, d.root_tx, d.root_ty, d.ntiles] == \
+            [min_level, max_level, ts, *root, ntiles]
+        assert (1 << min_level) * top == ts and np.float32(d.scale) == np.float32(scale)
+        W = ts + 5
+        got = np.empty((W, W), np.float32)
+        ref.ref_mipmap_level_tile(0, 0, 0, _f(got))
+        root_tile = _roundf(got[: top + 5, : top + 5])
+        assert np.array_equal(d.tile_int16(0, 0, 0), root_tile)
+        if top == ts:
+            assert np.array_equal(got, oracle_lib.level_tile(base, ts, max_level, 0, 0, 0, scale))
+        zeros = 0
+        raw = np.zeros(2 * W * W, np.uint8)
+        for level in range(1, max_level + 1):
+            w = min(top << level, ts) + 5
+            for ty in range(1 << max(level - min_level, 0)):
+                for tx in range(1 << max(level - min_level, 0)):
+                    nb = ref.ref_mipmap_residual(level, tx, ty, raw.ctypes.data, raw.size)
+                    assert nb == 2 * w * w
+                    want = raw[:nb].view("<i2").reshape(w, w)
+                    assert np.array_equal(d.tile_int16(level, tx, ty), want), (level, tx, ty)
+                    assert np.array_equal(od.tile_int16(level, tx, ty), want), (level, tx, ty)
+                    zeros += not want.any()
+        assert zeros > 0 and np.abs(root_tile).max() > 0
+        d.close()
     finally:
         ref.ref_mipmap_free()
