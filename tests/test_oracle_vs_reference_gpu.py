@@ -523,23 +523,35 @@ def test_residual_producer_on_reference_pyramids(ref, oracle_lib, product, name,
     tile).  hasTile checks the root only, and the elevation producer asks for
     (level, tx / mod, ty / mod), which stays inside; the reference reads past its
     offsets table for a tile outside, where the product returns TP_E_BAD_ARG."""
-    import ctypes as C
-    import struct
     path = oracle_lib.ref_file("src/%s/DEM.dat" % name)
     if path is None:
         pytest.skip("the reference's pyramids are not on this machine")
-    min_level, max_level, tile_size = struct.unpack("<3i", open(path, "rb").read(12))
+    assert _residual_producers_agree(ref, product, path, delta, zscale, len(name) + delta) >= 20
+
+
+def _residual_producers_agree(ref, product, path, delta, zscale, seed):
+    """The reference's ResidualProducer and the product's on the .dat file at `path`: every
+    tile of the first four pyramid levels and six random ones per deeper level alike, hasTile
+    alike, and no tile past the last level.  With a root tile at level r > 0 (deltaLevel is
+    then 0), pyramid level l is asked for at level r + l, at (rootTx << l, rootTy << l)
+    plus the tile's place in the pyramid.  Returns the number of tiles compared."""
+    import ctypes as C
+    import struct
+    min_level, max_level, tile_size, root_level, root_tx, root_ty = struct.unpack(
+        "<6i", open(path, "rb").read(24))
+    eff = delta if root_level == 0 else 0
     W = tile_size + 5
     storage = product.TileStorage(W, 1, 8, on_device=product.TileStorage.BOOKKEEPING)
     prod = product.ResidualProducer(product.TileCache(storage, "residuals"), path, delta=delta, zscale=zscale)
-    rng = np.random.default_rng(len(name) + delta)
+    rng = np.random.default_rng(seed)
     checked = 0
-    for level in range(0, max_level - delta + 1):
-        p = level + delta
-        n = 1 << (p - min_level) if p >= min_level else 1 << level
+    for p in range(eff, max_level + 1):
+        level = p - eff + root_level
+        n = 1 << (p - min_level) if p >= min_level else 1 << (p - eff)
         tiles = {(x, y) for x in range(min(n, 4)) for y in range(min(n, 4))}
         tiles |= {(int(rng.integers(0, n)), int(rng.integers(0, n))) for _ in range(6)}
-        for tx, ty in sorted(tiles):
+        for x, y in sorted(tiles):
+            tx, ty = (root_tx << (p - eff)) + x, (root_ty << (p - eff)) + y
             out = np.full((W, W), np.nan, np.float32)
             has = C.c_int()
             assert ref.ref_residual_tile(path.encode(), delta, zscale, W, level, tx, ty, out.ctypes.data,
@@ -549,14 +561,45 @@ def test_residual_producer_on_reference_pyramids(ref, oracle_lib, product, name,
                 written = ~np.isnan(out)    # a tile below minLevel fills the slot's corner
                 assert np.array_equal(prod.tile(level, tx, ty)[written], out[written]), (level, tx, ty)
                 checked += 1
-    # past the pyramid's last level: no tile on either side
-    for tx, ty in ((0, 0), (1, 0)):
+    # past the pyramid's last level, and beside a root tile above level 0: no tile on either side
+    last = max_level - eff + root_level + 1
+    outside = [(last, root_tx << (last - root_level), root_ty << (last - root_level)),
+               (last, (root_tx << (last - root_level)) + 1, root_ty << (last - root_level))]
+    if root_level > 0:
+        outside.append((root_level, root_tx + 1, root_ty))
+    for level, tx, ty in outside:
         has = C.c_int()
         out = np.zeros((W, W), np.float32)
-        ref.ref_residual_tile(path.encode(), delta, zscale, W, max_level - delta + 1, tx, ty, out.ctypes.data,
-                              C.byref(has))
-        assert not has.value and not prod.has_tile(max_level - delta + 1, tx, ty)
-    assert checked >= 20
+        ref.ref_residual_tile(path.encode(), delta, zscale, W, level, tx, ty, out.ctypes.data, C.byref(has))
+        assert not has.value and not prod.has_tile(level, tx, ty), (level, tx, ty)
+    return checked
+
+
+@pytest.mark.parametrize("top,ts,max_level,root,delta,zscale", [
+    (6, 24, 5, (0, 0, 0), 0, 1.0), (6, 24, 5, (0, 0, 0), 2, 0.5), (6, 24, 5, (3, 5, 2), 2, 2.0),
+    (24, 24, 3, (2, 1, 3), 0, 1.0), (12, 24, 4, (0, 0, 0), 1, 1.0)])
+def test_residual_producer_on_generated_pyramids(ref, oracle_lib, product, tmp_path, top, ts, max_level, root,
+                                                 delta, zscale):
+    """The same comparison on pyramids that the reference's own preprocess writes
+    (HeightMipmap::generate over a synthetic terrain): minLevel 2 and 1 with
+    root tiles of 6 and 12 intervals, which ResidualProducer upsamples below minLevel;
+    root tiles at levels 3 and 2 (where the deltaLevel asked for is set to 0); deltaLevel
+    0-2.  (A deltaLevel above minLevel is an assertion in ResidualProducer::init and an
+    error from tp_residual_producer_create.  ResidualProducer::readTile also asserts that a
+    stored tile, TIFF header and directory included, is smaller than the raw tile,
+    ResidualProducer.cpp:291; for tiles of 12 intervals (578 raw bytes) a noisy residual
+    strip plus that overhead is not, so the stored levels here have 24 intervals.)"""
+    import ctypes as C
+    n = (top << max_level) + 1
+    base = oracle_lib.fbm_heights(n, octaves=8, base_cells=2, seed=top + ts)
+    assert ref.ref_mipmap_build_sized(base.ctypes.data_as(C.POINTER(C.c_int16)), top, ts, max_level, 1.0,
+                                      str(tmp_path).encode()) == max_level
+    path = str(tmp_path / "DEM.dat")
+    try:
+        ref.ref_mipmap_generate(*root, 1.0, path.encode())
+    finally:
+        ref.ref_mipmap_free()
+    assert _residual_producers_agree(ref, product, path, delta, zscale, top + delta) >= 10
 
 
 def test_ortho_cpu_producer_on_reference_pyramid(ref, oracle_lib, product):
