@@ -97,3 +97,17 @@ def test_residual_root_chain_matches_oracle(product, oracle_lib, name, delta, zs
         raw = d.tile_int16(lvl + delta, 0, 0).astype(np.float32) * scale
         w = raw.shape[0]
         assert np.array_equal(t[:w, :w], raw.astype(np.float32))
+
+
+def test_delta_level_past_min_level_is_an_error(product):
+    # ResidualProducer::init asserts deltaLevel <= minLevel (ResidualProducer.cpp:122);
+    # the library refuses it with TP_E_BAD_ARG and accepts deltaLevel = minLevel
+    path = os.path.join(GOLDEN, "dem_edit3_mini.dat")
+    d = product.DatPyramid(path)
+    W = d.tile_size + 5
+    storage = product.TileStorage(W, 1, 4, on_device=product.TileStorage.BOOKKEEPING)
+    product.ResidualProducer(product.TileCache(storage, "ok"), path, delta=d.min_level)
+    with pytest.raises(product.TPError) as e:
+        product.ResidualProducer(product.TileCache(storage, "past"), path, delta=d.min_level + 1)
+    assert e.value.code == product.TP_E_BAD_ARG and "minLevel" in str(e.value)
+    d.close()
